@@ -1,0 +1,187 @@
+"""ctypes front end of the CPU oracle (test infrastructure only)."""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+D = C.POINTER(C.c_double)
+I32 = C.POINTER(C.c_int32)
+I64 = C.POINTER(C.c_int64)
+
+
+class CaseParams(C.Structure):
+    _fields_ = [("V", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("mach", C.c_double),
+                ("Sref", C.c_double), ("bref", C.c_double), ("cref", C.c_double), ("cg", C.c_double * 3)]
+
+
+class CaseResult(C.Structure):
+    _fields_ = [("CL", C.c_double), ("CDi", C.c_double), ("Fbody", C.c_double * 3), ("Fwind", C.c_double * 3),
+                ("CM", C.c_double * 3), ("iters", C.c_int64), ("error", C.c_double), ("converged", C.c_int)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        L.cpo_mesh_new.restype = C.c_void_p
+        L.cpo_mesh_new.argtypes = [D, C.c_int64, I64, I32, C.c_int64]
+        L.cpo_mesh_free.argtypes = [C.c_void_p]
+        for f in ("cpo_n_body", "cpo_n_wake", "cpo_n_wakes"):
+            getattr(L, f).restype = C.c_int64
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.cpo_n_wakelines.restype = C.c_int64
+        L.cpo_n_wakelines.argtypes = [C.c_void_p, C.c_int64]
+        L.cpo_body_table.argtypes = [C.c_void_p, D]
+        L.cpo_wake_table.argtypes = [C.c_void_p, D, I32, D]
+        L.cpo_clusters.argtypes = [C.c_void_p, I32]
+        L.cpo_body_verts.argtypes = [C.c_void_p, D]
+        L.cpo_wake_verts.argtypes = [C.c_void_p, D]
+        L.cpo_tri_phi_inf.argtypes = [D, D, D, D]
+        L.cpo_tri_dub_phi_inf.restype = C.c_double
+        L.cpo_tri_dub_phi_inf.argtypes = [D, D]
+        L.cpo_tri_v_inf.argtypes = [D, D, D, D]
+        L.cpo_set_inf_coeff.argtypes = [C.c_void_p, D, D, C.c_int64, C.c_int64, C.c_int]
+        L.cpo_case_run.restype = C.c_int
+        L.cpo_case_run.argtypes = [C.c_void_p, D, D, C.POINTER(CaseParams), D, D, D, D, D, D,
+                                   C.POINTER(CaseResult), C.c_int]
+        L.cpo_case_post.restype = C.c_int
+        L.cpo_case_post.argtypes = [C.c_void_p, C.POINTER(CaseParams), D, D, D, D, C.POINTER(CaseResult)]
+        L.cpo_bicgstab.restype = C.c_int
+        L.cpo_bicgstab.argtypes = [D, C.c_int64, D, D, C.c_double, C.c_int64, I64, D, C.c_int]
+        if hasattr(L, "cpo_vp_register"):
+            L.cpo_vp_register(C.c_void_p(0))
+        _lib = L
+    return _lib
+
+
+def _p(a, t=D):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+def nthreads_default():
+    return max(1, os.cpu_count() or 1)
+
+
+class Mesh:
+    """Oracle mesh: geometry::readTri topology on a .tri-style array triple."""
+
+    def __init__(self, nodes, tris, ids):
+        self.L = lib()
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        self.tris = np.ascontiguousarray(tris, dtype=np.int64)
+        self.ids = np.ascontiguousarray(ids, dtype=np.int32)
+        self.h = self.L.cpo_mesh_new(_p(self.nodes), len(self.nodes), _p(self.tris, I64), _p(self.ids, I32),
+                                     len(self.ids))
+        self.n = self.L.cpo_n_body(self.h)
+        self.nw = self.L.cpo_n_wake(self.h)
+
+    def __del__(self):
+        try:
+            self.L.cpo_mesh_free(self.h)
+        except Exception:
+            pass
+
+    def body_table(self):
+        out = np.zeros((self.n, 18))
+        self.L.cpo_body_table(self.h, _p(out))
+        return out
+
+    def wake_table(self):
+        out = np.zeros((self.nw, 8))
+        idx = np.zeros((self.nw, 4), dtype=np.int32)
+        coef = np.zeros(self.nw)
+        self.L.cpo_wake_table(self.h, _p(out), _p(idx, I32), _p(coef))
+        return out, idx, coef
+
+    def clusters(self):
+        out = np.zeros((self.n, 32), dtype=np.int32)
+        self.L.cpo_clusters(self.h, _p(out, I32))
+        return out
+
+    def body_verts(self):
+        out = np.zeros((self.n, 9))
+        self.L.cpo_body_verts(self.h, _p(out))
+        return out
+
+    def wake_verts(self):
+        out = np.zeros((self.nw, 9))
+        self.L.cpo_wake_verts(self.h, _p(out))
+        return out
+
+    def set_inf_coeff(self, rows=None, nthreads=None):
+        """Dense A, B (n x n) as Fortran-ordered arrays (column-major like Eigen)."""
+        n = self.n
+        r0, r1 = (0, n) if rows is None else rows
+        A = np.zeros((n, n), order="F")
+        B = np.zeros((n, n), order="F")
+        self.L.cpo_set_inf_coeff(self.h, _p(A), _p(B), r0, r1, nthreads or nthreads_default())
+        return A, B
+
+    def case(self, A, B, V=1.0, alpha=5.0, beta=0.0, mach=0.1, Sref=1.0, bref=1.0, cref=1.0, cg=(0, 0, 0),
+             nthreads=None):
+        n = self.n
+        p = CaseParams(V, alpha, beta, mach, Sref, bref, cref, (C.c_double * 3)(*cg))
+        r = CaseResult()
+        out = {k: np.zeros(n) for k in ("sigma", "mu", "phi", "cp")}
+        out["vel"] = np.zeros((n, 3))
+        out["wake_mu"] = np.zeros(self.nw)
+        A = np.asfortranarray(A)
+        B = np.asfortranarray(B)
+        self.L.cpo_case_run(self.h, _p(A), _p(B), C.byref(p), _p(out["sigma"]), _p(out["mu"]), _p(out["phi"]),
+                            _p(out["vel"]), _p(out["cp"]), _p(out["wake_mu"]), C.byref(r),
+                            nthreads or nthreads_default())
+        out.update(CL=r.CL, CDi=r.CDi, Fbody=np.array(r.Fbody[:]), Fwind=np.array(r.Fwind[:]),
+                   CM=np.array(r.CM[:]), iters=r.iters, error=r.error, converged=bool(r.converged))
+        return out
+
+    def post(self, mu, V=1.0, alpha=5.0, beta=0.0, mach=0.1, Sref=1.0, bref=1.0, cref=1.0, cg=(0, 0, 0)):
+        n = self.n
+        p = CaseParams(V, alpha, beta, mach, Sref, bref, cref, (C.c_double * 3)(*cg))
+        r = CaseResult()
+        mu = np.ascontiguousarray(mu, dtype=np.float64)
+        phi, cp, vel = np.zeros(n), np.zeros(n), np.zeros((n, 3))
+        self.L.cpo_case_post(self.h, C.byref(p), _p(mu), _p(phi), _p(vel), _p(cp), C.byref(r))
+        return dict(phi=phi, cp=cp, vel=vel, CL=r.CL, CDi=r.CDi, Fbody=np.array(r.Fbody[:]),
+                    Fwind=np.array(r.Fwind[:]), CM=np.array(r.CM[:]))
+
+
+def tri_phi_inf(verts9, poi):
+    L = lib()
+    v = np.ascontiguousarray(verts9, dtype=np.float64)
+    p = np.ascontiguousarray(poi, dtype=np.float64)
+    s, d = C.c_double(0), C.c_double(0)
+    L.cpo_tri_phi_inf(_p(v), _p(p), C.byref(s), C.byref(d))
+    return s.value, d.value
+
+
+def tri_dub_phi_inf(verts9, poi):
+    L = lib()
+    v = np.ascontiguousarray(verts9, dtype=np.float64)
+    p = np.ascontiguousarray(poi, dtype=np.float64)
+    return L.cpo_tri_dub_phi_inf(_p(v), _p(p))
+
+
+def tri_v_inf(verts9, poi):
+    L = lib()
+    v = np.ascontiguousarray(verts9, dtype=np.float64)
+    p = np.ascontiguousarray(poi, dtype=np.float64)
+    vs, vd = np.zeros(3), np.zeros(3)
+    L.cpo_tri_v_inf(_p(v), _p(p), _p(vs), _p(vd))
+    return vs, vd
+
+
+def bicgstab(A, b, nthreads=None):
+    L = lib()
+    A = np.asfortranarray(A, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    n = len(b)
+    x = np.zeros(n)
+    it, err = C.c_int64(0), C.c_double(0)
+    L.cpo_bicgstab(_p(A), n, _p(b), _p(x), np.finfo(float).eps, 2 * n, C.byref(it), C.byref(err),
+                   nthreads or nthreads_default())
+    return x, it.value, err.value

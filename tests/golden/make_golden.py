@@ -1,0 +1,81 @@
+"""Generate the committed golden fixtures from the reference's own case files.
+
+Run in a container where the CPanel reference tree is mounted (default path
+/root/reference, override with CPANEL_REF).  Writes:
+
+  case4412.npz  -- Connor Cases/4412: the 4412.tri mesh (nodes, 1-based tris, ids),
+                   the per-panel fields of V1_Mach0.1_alpha5_beta0/surfaceData-0.vtu
+                   (doublet, source, potential, velocity, Cp, centroid; 6 significant
+                   digits as printed by the reference) and the .CPout summary numbers.
+
+The generated files are small and committed; tests never read the reference tree.
+"""
+import os
+import re
+import sys
+
+import numpy as np
+
+REF = os.environ.get("CPANEL_REF", "/root/reference")
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_tri(path):
+    with open(path) as f:
+        tok = f.read().split()
+    nn, nt = int(tok[0]), int(tok[1])
+    k = 2
+    nodes = np.array(tok[k:k + 3 * nn], dtype=np.float64).reshape(nn, 3)
+    k += 3 * nn
+    tris = np.array(tok[k:k + 3 * nt], dtype=np.int64).reshape(nt, 3)
+    k += 3 * nt
+    ids = np.array(tok[k:k + nt], dtype=np.int32)
+    return nodes, tris, ids
+
+
+def read_vtu_arrays(path):
+    txt = open(path).read()
+    out = {}
+    for m in re.finditer(r'<DataArray type="(\w+)" Name="([^"]+)"(?: NumberOfComponents="(\d+)")? Format="ascii">(.*?)</DataArray>',
+                         txt, re.S):
+        typ, name, nc, body = m.group(1), m.group(2), m.group(3), m.group(4)
+        vals = np.array(body.split(), dtype=np.float64 if typ.startswith("Float") else np.int64)
+        if nc and int(nc) > 1:
+            vals = vals.reshape(-1, int(nc))
+        out[name] = vals
+    return out
+
+
+def read_cpout(path):
+    txt = open(path).read()
+    cl, cdi = re.search(r"CL = ([-\d.]+)\s+CDi = ([-\d.]+)", txt).groups()
+    nums = re.findall(r"^\s+([-\d.]+)\s+([-\d.]+)\s+([-\d.]+)\s*$", txt, re.M)
+    body = [float(v) for v in nums[0]]  # CN CA CY
+    wind = [float(v) for v in nums[1]]  # CL CD CY
+    mom = [float(v) for v in nums[2]]   # Cm Cl Cn
+    return dict(CL=float(cl), CDi=float(cdi), body_CN_CA_CY=body, wind_CL_CD_CY=wind, Cm_Cl_Cn=mom)
+
+
+def main():
+    case = os.path.join(REF, "Connor Cases", "4412")
+    if not os.path.isdir(case):
+        sys.exit("reference case folder not found: %s" % case)
+    nodes, tris, ids = read_tri(os.path.join(case, "4412.tri"))
+    vtu = read_vtu_arrays(os.path.join(case, "V1_Mach0.1_alpha5_beta0", "surfaceData-0.vtu"))
+    cp = read_cpout(os.path.join(case, "4412.CPout"))
+    centroid = np.stack([vtu["xPosition"], vtu["yPosition"], vtu["zPostition"]], axis=1)
+    np.savez_compressed(
+        os.path.join(HERE, "case4412.npz"),
+        nodes=nodes, tris=tris.astype(np.int32), ids=ids,
+        # printed to 6 significant digits by the reference: float32 keeps them exactly enough
+        mu=vtu["Doublet Strengths"].astype(np.float32), sigma=vtu["Source Strengths"].astype(np.float32),
+        phi=vtu["Velocity Potential"].astype(np.float32), vel=vtu["Velocity"].astype(np.float32),
+        cp=vtu["Cp"].astype(np.float32), centroid=centroid.astype(np.float32),
+        CL=cp["CL"], CDi=cp["CDi"], body_CN_CA_CY=np.array(cp["body_CN_CA_CY"]),
+        wind_CL_CD_CY=np.array(cp["wind_CL_CD_CY"]), Cm_Cl_Cn=np.array(cp["Cm_Cl_Cn"]),
+        V=1.0, alpha=5.0, beta=0.0, mach=0.1, Sref=6.0, bref=6.0, cref=1.0, cg=np.array([0.25, 0.0, 0.0]))
+    print("wrote case4412.npz", nodes.shape, tris.shape, cp)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,269 @@
+"""GB300-native steady panel path of CPanel.
+
+Host-side mirror of the reference's operator surface for this path:
+
+  Geometry      geometry::readTri + setInfCoeff/getA/getB (CPanel/geometry.cpp:132-891)
+  CpCase        cpCase::run results (CPanel/cpCase.cpp:31-139): getCL/getCD,
+                getBodyForces/getWindForces/getMoment, per-panel mu/phi/V/Cp
+  solve_cases   many flow conditions on one geometry in one batched call
+  panel_phi_inf / dub_phi_inf / panel_v_inf
+                bodyPanel::panelPhiInf, panel::dubPhiInf, bodyPanel::panelVInf on
+                device arrays
+
+All compute runs in libcpanel_gb300.so (sm_103a); this module only marshals
+arguments.  There is no CPU fallback.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import MIXED, PLAIN_FP64, CpgError
+
+__all__ = ["Context", "Geometry", "CpCase", "solve_cases", "topology", "read_tri", "panel_phi_inf", "dub_phi_inf",
+           "panel_v_inf", "CpgError", "PLAIN_FP64", "MIXED"]
+
+_PREC = {"fp64": PLAIN_FP64, "plain": PLAIN_FP64, PLAIN_FP64: PLAIN_FP64, "mixed": MIXED, MIXED: MIXED}
+
+
+def _p(a, t=_lib.D):
+    return a.ctypes.data_as(t)
+
+
+class Context:
+    """One device context (stream + error state).  Thread-compatible, not shared."""
+
+    _default = None
+
+    def __init__(self, device=0):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        rc = self.L.cpg_create(C.byref(h), device)
+        if rc != 0:
+            raise CpgError(rc, "cpg_create(device=%d)" % device)
+        self.h = h
+
+    @classmethod
+    def default(cls):
+        if cls._default is None:
+            cls._default = Context(0)
+        return cls._default
+
+    def check(self, rc, what=""):
+        if rc != 0:
+            msg = self.L.cpg_last_error(self.h)
+            raise CpgError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    def synchronize(self):
+        self.check(self.L.cpg_synchronize(self.h), "synchronize")
+
+    def __del__(self):
+        try:
+            self.L.cpg_destroy(self.h)
+        except Exception:
+            pass
+
+
+def read_tri(path):
+    """Cart3D .tri file -> (nodes[n,3], tris[nt,3] 1-based, ids[nt]) (geometry::readTri input format)."""
+    with open(path) as f:
+        tok = f.read().split()
+    nn, nt = int(tok[0]), int(tok[1])
+    k = 2
+    nodes = np.array(tok[k:k + 3 * nn], dtype=np.float64).reshape(nn, 3)
+    k += 3 * nn
+    tris = np.array(tok[k:k + 3 * nt], dtype=np.int64).reshape(nt, 3)
+    k += 3 * nt
+    ids = np.array(tok[k:k + nt], dtype=np.int32)
+    return nodes, tris, ids
+
+
+class Geometry:
+    """geometry: .tri topology on the host, panel tables and matrices on the device."""
+
+    def __init__(self, nodes, tris, ids, ctx=None):
+        self.ctx = ctx or Context.default()
+        L = self.ctx.L
+        self._nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        self._tris = np.ascontiguousarray(tris, dtype=np.int64)
+        self._ids = np.ascontiguousarray(ids, dtype=np.int32)
+        h = C.c_void_p()
+        self.ctx.check(L.cpg_geometry_create(self.ctx.h, _p(self._nodes), len(self._nodes), _p(self._tris, _lib.I64),
+                                             _p(self._ids, _lib.I32), len(self._ids), C.byref(h)),
+                       "cpg_geometry_create")
+        self.h = h
+        info = _lib.GeometryInfo()
+        self.ctx.check(L.cpg_geometry_info_get(self.h, C.byref(info)), "info")
+        self.info = {f: getattr(info, f) for f, _ in info._fields_}
+        self.n = info.n_body
+        self.nw = info.n_wake
+
+    @classmethod
+    def from_tri(cls, path, ctx=None):
+        return cls(*read_tri(path), ctx=ctx)
+
+    def __del__(self):
+        try:
+            self.ctx.L.cpg_geometry_destroy(self.h)
+        except Exception:
+            pass
+
+    def getNumberOfBodyPanels(self):
+        return self.n
+
+    def setInfCoeff(self, precision="fp64"):
+        self.ctx.check(self.ctx.L.cpg_set_inf_coeff(self.h, _PREC[precision]), "setInfCoeff")
+
+    def getA(self):
+        A = np.empty((self.n, self.n), order="F")
+        self.ctx.check(self.ctx.L.cpg_get_A(self.h, _p(A)), "getA")
+        return A
+
+    def getB(self):
+        B = np.empty((self.n, self.n), order="F")
+        self.ctx.check(self.ctx.L.cpg_get_B(self.h, _p(B)), "getB")
+        return B
+
+    def tables(self):
+        body = np.zeros((self.n, 18))
+        wake = np.zeros((self.nw, 8))
+        idx = np.zeros((self.nw, 4), dtype=np.int32)
+        coef = np.zeros(self.nw)
+        cl = np.zeros((self.n, 32), dtype=np.int32)
+        self.ctx.check(self.ctx.L.cpg_geometry_tables(self.h, _p(body), _p(wake), _p(idx, _lib.I32), _p(coef),
+                                                      _p(cl, _lib.I32)), "tables")
+        return dict(body=body, wake=wake, idx4=idx, coef=coef, clusters=cl)
+
+
+def topology(nodes, tris, ids):
+    """Host-only readTri topology tables (no device needed)."""
+    L = _lib.load()
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    tris = np.ascontiguousarray(tris, dtype=np.int64)
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    info = _lib.GeometryInfo()
+    args = (_p(nodes), len(nodes), _p(tris, _lib.I64), _p(ids, _lib.I32), len(ids), C.byref(info))
+    rc = L.cpg_topology(*args, None, None, None, None, None)
+    if rc != 0:
+        raise CpgError(rc, "cpg_topology")
+    n, nw = info.n_body, info.n_wake
+    body, wake = np.zeros((n, 18)), np.zeros((nw, 8))
+    idx, coef, cl = np.zeros((nw, 4), dtype=np.int32), np.zeros(nw), np.zeros((n, 32), dtype=np.int32)
+    rc = L.cpg_topology(*args, _p(body), _p(wake), _p(idx, _lib.I32), _p(coef), _p(cl, _lib.I32))
+    if rc != 0:
+        raise CpgError(rc, "cpg_topology")
+    return dict(info={f: getattr(info, f) for f, _ in info._fields_}, body=body, wake=wake, idx4=idx, coef=coef,
+                clusters=cl)
+
+
+def solve_cases(geom, flows, Sref=1.0, bref=1.0, cref=1.0, cg=(0.0, 0.0, 0.0), precision="fp64", want=None):
+    """Run cpCase::run for k flow conditions (V, alpha, beta, mach) on one geometry.
+
+    Returns a dict with per-case arrays (mu, sigma, phi, vel, cp: k x n [x 3]) and
+    CL, CDi (k), Fbody, Fwind, CM (k x 3), plus solver statistics.
+    """
+    flows = [tuple(f) for f in flows]
+    k = len(flows)
+    fl = (_lib.Flow * k)(*[_lib.Flow(*f) for f in flows])
+    refs = _lib.Refs(Sref, bref, cref, (C.c_double * 3)(*cg))
+    n = geom.n
+    want = want or ("mu", "sigma", "phi", "vel", "cp")
+    out = {name: np.zeros((k, n)) for name in ("mu", "sigma", "phi", "cp") if name in want}
+    if "vel" in want:
+        out["vel"] = np.zeros((k, n, 3))
+    for name in ("CL", "CDi"):
+        out[name] = np.zeros(k)
+    for name in ("Fbody", "Fwind", "CM"):
+        out[name] = np.zeros((k, 3))
+    co = _lib.CaseOut(*[_p(out[f]) if f in out else None for f, _ in _lib.CaseOut._fields_])
+    st = _lib.SolveStats()
+    rc = geom.ctx.L.cpg_solve_cases(geom.h, fl, k, C.byref(refs), _PREC[precision], C.byref(co), C.byref(st))
+    out["stats"] = {f: getattr(st, f) for f, _ in st._fields_}
+    out["status"] = rc
+    if rc not in (0, 5):
+        geom.ctx.check(rc, "solve_cases")
+    return out
+
+
+class CpCase:
+    """cpCase: one flow condition on a geometry (CPanel/cpCase.h:127-136)."""
+
+    def __init__(self, geom, V, alpha, beta, mach, Sref=1.0, bref=1.0, cref=1.0, cg=(0, 0, 0), precision="fp64"):
+        self.geom = geom
+        self.flow = (V, alpha, beta, mach)
+        self.refs = dict(Sref=Sref, bref=bref, cref=cref, cg=cg)
+        self.precision = precision
+        self.res = None
+
+    def run(self):
+        self.res = solve_cases(self.geom, [self.flow], precision=self.precision, **self.refs)
+        return self.res["status"] == 0
+
+    def getCL(self):
+        return self.res["CL"][0]
+
+    def getCD(self):
+        return self.res["CDi"][0]
+
+    def getBodyForces(self):
+        return self.res["Fbody"][0]
+
+    def getWindForces(self):
+        return self.res["Fwind"][0]
+
+    def getMoment(self):
+        return self.res["CM"][0]
+
+    def getMu(self):
+        return self.res["mu"][0]
+
+    def getCp(self):
+        return self.res["cp"][0]
+
+    def getVelocity(self):
+        return self.res["vel"][0]
+
+
+def _dev_ptr(t):
+    return C.c_void_p(t.data_ptr())
+
+
+def panel_phi_inf(verts, poi, ctx=None):
+    """Batched bodyPanel::panelPhiInf on CUDA tensors (m x 9, m x 3) -> (phi_src, phi_dub)."""
+    import torch
+    ctx = ctx or Context.default()
+    verts = verts.contiguous().double()
+    poi = poi.contiguous().double()
+    m = verts.shape[0]
+    src = torch.empty(m, dtype=torch.float64, device=verts.device)
+    dub = torch.empty(m, dtype=torch.float64, device=verts.device)
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.cpg_panel_phi_inf(ctx.h, _dev_ptr(verts), _dev_ptr(poi), m, _dev_ptr(src), _dev_ptr(dub)),
+              "panelPhiInf")
+    return src, dub
+
+
+def dub_phi_inf(verts, poi, ctx=None):
+    import torch
+    ctx = ctx or Context.default()
+    verts = verts.contiguous().double()
+    poi = poi.contiguous().double()
+    m = verts.shape[0]
+    dub = torch.empty(m, dtype=torch.float64, device=verts.device)
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.cpg_dub_phi_inf(ctx.h, _dev_ptr(verts), _dev_ptr(poi), m, _dev_ptr(dub)), "dubPhiInf")
+    return dub
+
+
+def panel_v_inf(verts, poi, ctx=None):
+    import torch
+    ctx = ctx or Context.default()
+    verts = verts.contiguous().double()
+    poi = poi.contiguous().double()
+    m = verts.shape[0]
+    vs = torch.empty((m, 3), dtype=torch.float64, device=verts.device)
+    vd = torch.empty((m, 3), dtype=torch.float64, device=verts.device)
+    torch.cuda.synchronize()
+    ctx.check(ctx.L.cpg_panel_v_inf(ctx.h, _dev_ptr(verts), _dev_ptr(poi), m, _dev_ptr(vs), _dev_ptr(vd)),
+              "panelVInf")
+    return vs, vd

@@ -1,0 +1,91 @@
+"""ctypes binding of libcpanel_gb300.so (the in-tree CUDA extension).
+
+There is no CPU fallback: if the library is missing or no CUDA device is usable,
+calls raise CpgError.
+"""
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcpanel_gb300.so")
+
+D = C.POINTER(C.c_double)
+I32 = C.POINTER(C.c_int32)
+I64 = C.POINTER(C.c_int64)
+
+STATUS = {0: "CPG_OK", 1: "CPG_E_INVALID", 2: "CPG_E_OOM", 3: "CPG_E_CUDA", 4: "CPG_E_BAD_MESH",
+          5: "CPG_E_NOT_CONVERGED", 6: "CPG_E_TIMEOUT", 7: "CPG_E_NO_DEVICE"}
+PLAIN_FP64, MIXED = 0, 1
+
+
+class CpgError(RuntimeError):
+    def __init__(self, code, msg=""):
+        self.code = code
+        super().__init__("%s: %s" % (STATUS.get(code, str(code)), msg))
+
+
+class GeometryInfo(C.Structure):
+    _fields_ = [("n_body", C.c_int64), ("n_wake", C.c_int64), ("n_wakes", C.c_int64), ("n_wakelines", C.c_int64),
+                ("n_tip", C.c_int64), ("n_nodes", C.c_int64)]
+
+
+class Flow(C.Structure):
+    _fields_ = [("V", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("mach", C.c_double)]
+
+
+class Refs(C.Structure):
+    _fields_ = [("Sref", C.c_double), ("bref", C.c_double), ("cref", C.c_double), ("cg", C.c_double * 3)]
+
+
+class CaseOut(C.Structure):
+    _fields_ = [(name, D) for name in ("mu", "sigma", "phi", "vel", "cp", "CL", "CDi", "Fbody", "Fwind", "CM")]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iters_max", C.c_int64), ("iters_total", C.c_int64), ("refinements", C.c_int64),
+                ("residual_max", C.c_double), ("n_near", C.c_int64), ("n_far", C.c_int64),
+                ("ms_assemble", C.c_double), ("ms_solve", C.c_double), ("ms_post", C.c_double)]
+
+
+_lib = None
+
+# every symbol declared in include/cpanel_gpu.h
+EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg_synchronize",
+           "cpg_geometry_create", "cpg_geometry_destroy", "cpg_geometry_info_get", "cpg_geometry_tables", "cpg_topology",
+           "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
+           "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch"]
+
+
+def load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise CpgError(7, "extension library not built: %s (run __graft_entry__.build())" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    vp = C.c_void_p
+    L.cpg_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.cpg_destroy.argtypes = [vp]
+    L.cpg_destroy.restype = None
+    L.cpg_last_error.argtypes = [vp]
+    L.cpg_last_error.restype = C.c_char_p
+    L.cpg_set_stream.argtypes = [vp, vp]
+    L.cpg_synchronize.argtypes = [vp]
+    L.cpg_geometry_create.argtypes = [vp, D, C.c_int64, I64, I32, C.c_int64, C.POINTER(vp)]
+    L.cpg_geometry_destroy.argtypes = [vp]
+    L.cpg_geometry_destroy.restype = None
+    L.cpg_geometry_info_get.argtypes = [vp, C.POINTER(GeometryInfo)]
+    L.cpg_geometry_tables.argtypes = [vp, D, D, I32, D, I32]
+    L.cpg_topology.argtypes = [D, C.c_int64, I64, I32, C.c_int64, C.POINTER(GeometryInfo), D, D, I32, D, I32]
+    L.cpg_set_inf_coeff.argtypes = [vp, C.c_int]
+    L.cpg_get_A.argtypes = [vp, D]
+    L.cpg_get_B.argtypes = [vp, D]
+    L.cpg_solve_cases.argtypes = [vp, C.POINTER(Flow), C.c_int, C.POINTER(Refs), C.c_int, C.POINTER(CaseOut),
+                                  C.POINTER(SolveStats)]
+    for f in ("cpg_panel_phi_inf",):
+        getattr(L, f).argtypes = [vp, vp, vp, C.c_int64, vp, vp]
+    L.cpg_dub_phi_inf.argtypes = [vp, vp, vp, C.c_int64, vp]
+    L.cpg_panel_v_inf.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
+    L.cpg_compiled_arch.argtypes = []
+    _lib = L
+    return L

@@ -1,0 +1,548 @@
+// C ABI of the GB300 panel path (include/cpanel_gpu.h).
+//
+// A cpg_geometry owns its device tables; matrices are assembled lazily per
+// precision and kept resident, so further cases on the same mesh reuse them
+// (the reference assembles once per geometry too, CPanel/geometry.cpp:607-621).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/cpanel_gpu.h"
+#include "assemble.h"
+#include "mesh.h"
+#include "post.h"
+
+struct cpg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+    // scratch for the batched single-evaluation operators is caller-owned
+};
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t b) {
+        if (b <= bytes) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&p, b);
+        if (e == cudaSuccess) bytes = b;
+        return e;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <typename T>
+    T* as() const {
+        return (T*)p;
+    }
+};
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr int F_STRIDE_HOST = 12;  // FP32 far-field record, F_STRIDE in common.cuh
+
+}  // namespace
+
+#ifndef CPG_COMPILED_ARCH
+#define CPG_COMPILED_ARCH 103
+#endif
+
+struct cpg_geometry {
+    cpg_ctx* ctx = nullptr;
+    cpg::HostMesh H;
+    DevBuf rec, frec, bez, clp, cli, tip, ts, wrec, widx, wcoef, tzst, tzln, tzpts, G, F3, F2, mode;
+    DevBuf A64, B64, A32, rb, count;
+    DevBuf work, post_work, cases, outs;
+    bool have64 = false, have32 = false, post_ready = false;
+    int64_t n_near64 = 0, n_near32 = 0;
+    cpg::PostTables T;
+    float ms_asm = 0;
+};
+
+namespace {
+
+int fail(cpg_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+int cuda_fail(cpg_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, e == cudaErrorMemoryAllocation ? CPG_E_OOM : CPG_E_CUDA,
+                std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(expr, where)                                      \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
+    } while (0)
+
+template <typename T>
+cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
+    cudaError_t e = b.ensure(std::max<size_t>(1, v.size() * sizeof(T)));
+    if (e != cudaSuccess) return e;
+    if (v.empty()) return cudaSuccess;
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+void case_scalars(const cpg_flow& f, const cpg_refs& r, cpg::CaseScalars& cs) {
+    // cpCase::windToBody, CPanel/cpCase.cpp:142-165
+    double a = f.alpha * (kPi / 180), b = f.beta * (kPi / 180);
+    double T[9] = {std::cos(a) * std::cos(b), std::cos(a) * std::sin(b), -std::sin(a),
+                   -std::sin(b), std::cos(b), 0,
+                   std::sin(a) * std::cos(b), std::sin(a) * std::sin(b), std::cos(a)};
+    for (int q = 0; q < 9; q++) cs.T[q] = T[q];
+    for (int q = 0; q < 3; q++) cs.Vinf[q] = T[3 * q] * f.V + T[3 * q + 1] * 0 + T[3 * q + 2] * 0;
+    cs.V = f.V;
+    cs.PG = std::sqrt(1 - std::pow(f.mach, 2));
+    cs.Sref = r.Sref;
+    cs.bref = r.bref;
+    cs.cref = r.cref;
+    for (int q = 0; q < 3; q++) cs.cg[q] = r.cg[q];
+}
+
+int prepare_post(cpg_geometry* g) {
+    cpg_ctx* ctx = g->ctx;
+    if (g->post_ready) return CPG_OK;
+    cudaStream_t s = ctx->stream;
+    const cpg::HostMesh& H = g->H;
+    int64_t n = H.n_body;
+    CK(g->F3.ensure(sizeof(double) * n * 3 * (cpg::kClMax - 1)), "alloc F3");
+    CK(g->F2.ensure(sizeof(double) * n * 2 * (cpg::kClMax - 1)), "alloc F2");
+    CK(g->mode.ensure(sizeof(int32_t) * n), "alloc mode");
+    CK(cudaMemsetAsync(g->F2.p, 0, g->F2.bytes, s), "clear F2");
+    cpg::PostTables& T = g->T;
+    T.n = n;
+    T.nw = H.n_wake;
+    T.rec = g->rec.as<double>();
+    T.bez = g->bez.as<double>();
+    T.cl_ptr = g->clp.as<int32_t>();
+    T.cl_idx = g->cli.as<int32_t>();
+    T.tip = g->tip.as<int32_t>();
+    T.tsorder = g->ts.as<int32_t>();
+    T.widx = g->widx.as<int32_t>();
+    T.wcoef = g->wcoef.as<double>();
+    T.F3 = g->F3.as<double>();
+    T.F2 = g->F2.as<double>();
+    T.mode = g->mode.as<int32_t>();
+    CK(cpg::launch_chtls_weights(T, s), "CHTLS weights");
+    // Trefftz tables
+    std::vector<double> st;
+    std::vector<int32_t> ln;
+    int nst = 0;
+    for (const auto& W : H.trefftz) {
+        nst = (int)W.st.size();
+        for (const auto& S : W.st) {
+            st.push_back(S.y);
+            st.push_back(S.interp);
+            for (int a = 0; a < 6; a++) st.push_back(S.Fy[a]);
+            for (int a = 0; a < 6; a++) st.push_back(S.Fz[a]);
+            st.push_back(W.step);
+            ln.push_back(S.line_up1);
+            ln.push_back(S.line_lo1);
+            ln.push_back(S.line_up2);
+            ln.push_back(S.line_lo2);
+            ln.push_back(S.pt0);
+        }
+    }
+    T.n_wakes = (int)H.trefftz.size();
+    T.n_st = nst;
+    T.n_pts = (int64_t)H.tz_pts.size() / 3;
+    CK(upload(g->tzst, st, s), "upload Trefftz");
+    CK(upload(g->tzln, ln, s), "upload Trefftz");
+    CK(upload(g->tzpts, H.tz_pts, s), "upload Trefftz");
+    CK(g->G.ensure(std::max<size_t>(8, sizeof(double) * T.n_pts * H.n_wake)), "alloc G");
+    CK(cpg::launch_wake_potential_op(g->wrec.as<double>(), H.n_wake, g->tzpts.as<double>(), T.n_pts,
+                                     g->G.as<double>(), s),
+       "Trefftz operator");
+    T.tz_station = g->tzst.as<double>();
+    T.tz_lines = g->tzln.as<int32_t>();
+    T.G = g->G.as<double>();
+    g->post_ready = true;
+    return CPG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpg_create(cpg_ctx** out, int device) {
+    if (!out) return CPG_E_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) return CPG_E_NO_DEVICE;
+    if (device < 0 || device >= count) return CPG_E_INVALID;
+    cpg_ctx* c = new (std::nothrow) cpg_ctx();
+    if (!c) return CPG_E_OOM;
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return CPG_E_CUDA;
+    }
+    c->own_stream = true;
+    *out = c;
+    return CPG_OK;
+}
+
+void cpg_destroy(cpg_ctx* c) {
+    if (!c) return;
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* cpg_last_error(const cpg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int cpg_set_stream(cpg_ctx* ctx, void* stream) {
+    if (!ctx) return CPG_E_INVALID;
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    ctx->own_stream = false;
+    ctx->stream = (cudaStream_t)stream;
+    if (!stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream");
+        ctx->own_stream = true;
+    }
+    return CPG_OK;
+}
+
+int cpg_synchronize(cpg_ctx* ctx) {
+    if (!ctx) return CPG_E_INVALID;
+    CK(cudaStreamSynchronize(ctx->stream), "synchronize");
+    return CPG_OK;
+}
+
+int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
+                        int64_t n_tris, cpg_geometry** out) {
+    if (!ctx || !out || !nodes || !tris || !ids) return fail(ctx, CPG_E_INVALID, "null argument");
+    *out = nullptr;
+    cpg_geometry* g = new (std::nothrow) cpg_geometry();
+    if (!g) return fail(ctx, CPG_E_OOM, "host allocation");
+    g->ctx = ctx;
+    std::string msg = cpg::build_mesh(nodes, n_nodes, tris, ids, n_tris, g->H);
+    if (!msg.empty()) {
+        delete g;
+        return fail(ctx, CPG_E_BAD_MESH, msg);
+    }
+    const cpg::HostMesh& H = g->H;
+    int64_t n = H.n_body;
+    if (n < 2) {
+        delete g;
+        return fail(ctx, CPG_E_BAD_MESH, "fewer than two body panels");
+    }
+    cudaStream_t s = ctx->stream;
+    // FP32 far-field records: c_hi, c_lo, n, area, longSide
+    std::vector<float> fr(n * F_STRIDE_HOST, 0.f);
+    for (int64_t i = 0; i < n; i++) {
+        const double* r = &H.body[i * cpg::PF_STRIDE];
+        for (int q = 0; q < 3; q++) {
+            float hi = (float)r[cpg::PF_C + q];
+            fr[i * F_STRIDE_HOST + q] = hi;
+            fr[i * F_STRIDE_HOST + 3 + q] = (float)(r[cpg::PF_C + q] - (double)hi);
+            fr[i * F_STRIDE_HOST + 6 + q] = (float)r[cpg::PF_N + q];
+        }
+        fr[i * F_STRIDE_HOST + 9] = (float)r[cpg::PF_AREA];
+        fr[i * F_STRIDE_HOST + 10] = (float)r[cpg::PF_LONG];
+    }
+    cudaError_t e;
+    if ((e = upload(g->rec, H.body, s)) != cudaSuccess || (e = upload(g->frec, fr, s)) != cudaSuccess ||
+        (e = upload(g->bez, H.bez, s)) != cudaSuccess || (e = upload(g->clp, H.cl_ptr, s)) != cudaSuccess ||
+        (e = upload(g->cli, H.cl_idx, s)) != cudaSuccess || (e = upload(g->tip, H.tip, s)) != cudaSuccess ||
+        (e = upload(g->ts, H.tsorder, s)) != cudaSuccess || (e = upload(g->wrec, H.wake, s)) != cudaSuccess ||
+        (e = upload(g->widx, H.widx, s)) != cudaSuccess || (e = upload(g->wcoef, H.wcoef, s)) != cudaSuccess ||
+        (e = g->count.ensure(64)) != cudaSuccess) {
+        cpg_geometry_destroy(g);
+        return cuda_fail(ctx, e, "geometry upload");
+    }
+    *out = g;
+    return CPG_OK;
+}
+
+void cpg_geometry_destroy(cpg_geometry* g) {
+    if (!g) return;
+    DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
+                      &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
+                      &g->B64, &g->A32, &g->rb, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
+    if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+    for (DevBuf* b : bufs) b->release();
+    delete g;
+}
+
+int cpg_geometry_info_get(const cpg_geometry* g, cpg_geometry_info* o) {
+    if (!g || !o) return CPG_E_INVALID;
+    o->n_body = g->H.n_body;
+    o->n_wake = g->H.n_wake;
+    o->n_wakes = (int64_t)g->H.trefftz.size();
+    o->n_wakelines = g->H.n_lines;
+    o->n_tip = g->H.n_tip;
+    o->n_nodes = g->H.n_nodes;
+    return CPG_OK;
+}
+
+int cpg_geometry_tables(const cpg_geometry* g, double* body, double* wake, int32_t* idx4, double* coef,
+                        int32_t* clusters) {
+    if (!g) return CPG_E_INVALID;
+    const cpg::HostMesh& H = g->H;
+    for (int64_t i = 0; i < H.n_body && body; i++) {
+        const double* r = &H.body[i * cpg::PF_STRIDE];
+        double* o = body + 18 * i;
+        for (int q = 0; q < 3; q++) {
+            o[q] = r[cpg::PF_C + q];
+            o[3 + q] = r[cpg::PF_N + q];
+            o[6 + q] = r[cpg::PF_L + q];
+        }
+        o[9] = r[cpg::PF_AREA];
+        o[10] = r[cpg::PF_LONG];
+        o[11] = H.tip[i];
+        o[12] = H.upper[i];
+        o[13] = H.lower[i];
+        o[14] = H.tsorder[i];
+        o[15] = H.surf_id[i];
+        o[16] = H.cl_ptr[i + 1] - H.cl_ptr[i];
+        o[17] = H.file_tri[i];
+    }
+    for (int64_t j = 0; j < H.n_wake; j++) {
+        const double* r = &H.wake[j * cpg::PF_STRIDE];
+        if (wake) {
+            double* o = wake + 8 * j;
+            for (int q = 0; q < 3; q++) {
+                o[q] = r[cpg::PF_C + q];
+                o[3 + q] = r[cpg::PF_N + q];
+            }
+            o[6] = r[cpg::PF_AREA];
+            o[7] = r[cpg::PF_LONG];
+        }
+        if (idx4)
+            for (int q = 0; q < 4; q++) idx4[4 * j + q] = H.widx[4 * j + q];
+        if (coef) coef[j] = H.wcoef[j];
+    }
+    if (clusters)
+        for (int64_t i = 0; i < H.n_body; i++)
+            for (int q = 0; q < 32; q++) {
+                int a = H.cl_ptr[i] + q;
+                clusters[32 * i + q] = a < H.cl_ptr[i + 1] ? H.cl_idx[a] : -1;
+            }
+    return CPG_OK;
+}
+
+int cpg_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids, int64_t n_tris,
+                 cpg_geometry_info* info, double* body, double* wake, int32_t* idx4, double* coef,
+                 int32_t* clusters) {
+    if (!nodes || !tris || !ids || !info) return CPG_E_INVALID;
+    cpg_geometry tmp;
+    std::string msg = cpg::build_mesh(nodes, n_nodes, tris, ids, n_tris, tmp.H);
+    if (!msg.empty()) return CPG_E_BAD_MESH;
+    cpg_geometry_info_get(&tmp, info);
+    return cpg_geometry_tables(&tmp, body, wake, idx4, coef, clusters);
+}
+
+int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
+    if (!g) return CPG_E_INVALID;
+    cpg_ctx* ctx = g->ctx;
+    cudaStream_t s = ctx->stream;
+    int64_t n = g->H.n_body;
+    size_t nn = (size_t)n * n;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    CK(cudaMemsetAsync(g->count.p, 0, sizeof(unsigned long long), s), "clear counter");
+    CK(cudaEventRecord(e0, s), "event");
+    if (precision == CPG_PLAIN_FP64) {
+        CK(g->A64.ensure(sizeof(double) * nn), "alloc A (FP64)");
+        CK(g->B64.ensure(sizeof(double) * nn), "alloc B (FP64)");
+        CK(cpg::launch_assemble_fp64(g->rec.as<double>(), n, g->wrec.as<double>(), g->widx.as<int32_t>(),
+                                     g->wcoef.as<double>(), g->H.n_wake, g->A64.as<double>(), g->B64.as<double>(),
+                                     g->count.as<unsigned long long>(), s),
+           "assembly (FP64)");
+        g->have64 = true;
+    } else if (precision == CPG_MIXED) {
+        CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
+        CK(g->rb.ensure(sizeof(double) * 3 * n), "alloc rhs basis");
+        CK(cpg::launch_assemble_mixed(g->rec.as<double>(), g->frec.as<float>(), n, g->wrec.as<double>(),
+                                      g->widx.as<int32_t>(), g->wcoef.as<double>(), g->H.n_wake,
+                                      g->A32.as<float>(), g->rb.as<double>(), g->count.as<unsigned long long>(), s),
+           "assembly (mixed)");
+        g->have32 = true;
+    } else {
+        return fail(ctx, CPG_E_INVALID, "unknown precision");
+    }
+    CK(cudaEventRecord(e1, s), "event");
+    unsigned long long cnt = 0;
+    CK(cudaMemcpyAsync(&cnt, g->count.p, sizeof(cnt), cudaMemcpyDeviceToHost, s), "counter");
+    CK(cudaStreamSynchronize(s), "assembly");
+    cudaEventElapsedTime(&g->ms_asm, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (precision == CPG_PLAIN_FP64)
+        g->n_near64 = (int64_t)cnt;
+    else
+        g->n_near32 = (int64_t)cnt;
+    return CPG_OK;
+}
+
+int cpg_get_A(cpg_geometry* g, double* host) {
+    if (!g || !host) return CPG_E_INVALID;
+    cpg_ctx* ctx = g->ctx;
+    size_t nn = (size_t)g->H.n_body * g->H.n_body;
+    if (g->have64) {
+        CK(cudaMemcpyAsync(host, g->A64.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream), "copy A");
+    } else if (g->have32) {
+        DevBuf tmp;
+        CK(tmp.ensure(sizeof(double) * nn), "alloc");
+        CK(cpg::launch_widen(g->A32.as<float>(), tmp.as<double>(), (int64_t)nn, ctx->stream), "widen");
+        CK(cudaMemcpyAsync(host, tmp.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream), "copy A");
+        CK(cudaStreamSynchronize(ctx->stream), "copy A");
+        tmp.release();
+    } else {
+        return fail(ctx, CPG_E_INVALID, "no assembled matrix");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "copy A");
+    return CPG_OK;
+}
+
+int cpg_get_B(cpg_geometry* g, double* host) {
+    if (!g || !host) return CPG_E_INVALID;
+    cpg_ctx* ctx = g->ctx;
+    if (!g->have64) return fail(ctx, CPG_E_INVALID, "B is only stored by the FP64 assembly");
+    size_t nn = (size_t)g->H.n_body * g->H.n_body;
+    CK(cudaMemcpyAsync(host, g->B64.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream), "copy B");
+    CK(cudaStreamSynchronize(ctx->stream), "copy B");
+    return CPG_OK;
+}
+
+int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_refs* refs, int precision,
+                    const cpg_case_out* out, cpg_solve_stats* stats) {
+    if (!g || !flows || !refs || k <= 0) return CPG_E_INVALID;
+    cpg_ctx* ctx = g->ctx;
+    if (precision != CPG_PLAIN_FP64 && precision != CPG_MIXED) return fail(ctx, CPG_E_INVALID, "unknown precision");
+    if (precision == CPG_MIXED && k > 4096) return fail(ctx, CPG_E_INVALID, "too many cases");
+    cudaStream_t s = ctx->stream;
+    int64_t n = g->H.n_body, nw = g->H.n_wake;
+    int rc;
+    if ((precision == CPG_PLAIN_FP64 && !g->have64) || (precision == CPG_MIXED && !g->have32))
+        if ((rc = cpg_set_inf_coeff(g, precision)) != CPG_OK) return rc;
+    float ms_asm = g->ms_asm;
+    if ((rc = prepare_post(g)) != CPG_OK) return rc;
+    std::vector<cpg::CaseScalars> cs(k);
+    for (int c = 0; c < k; c++) case_scalars(flows[c], *refs, cs[c]);
+    CK(upload(g->cases, cs, s), "upload cases");
+    const cpg::CaseScalars* dcs = g->cases.as<cpg::CaseScalars>();
+    size_t kn = (size_t)k * n;
+    // outputs: mu sigma rhs phi cp (kn each), vel (3kn), forces 9k, tz 2k, wake mu k*nw
+    size_t need = sizeof(double) * (8 * kn + 9 * (size_t)k + 2 * (size_t)k + (size_t)k * nw) + 8 * 256;
+    CK(g->outs.ensure(need), "alloc outputs");
+    double* mu = g->outs.as<double>();
+    double* sigma = mu + kn;
+    double* rhs = sigma + kn;
+    double* phi = rhs + kn;
+    double* cp = phi + kn;
+    double* vel = cp + kn;
+    double* forces = vel + 3 * kn;
+    double* tz = forces + 9 * (size_t)k;
+    double* wmu = tz + 2 * (size_t)k;
+    cpg::SolveStats st;
+    cudaEvent_t e0, e1, e2;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    CK(cudaEventCreate(&e2), "event");
+    CK(cudaEventRecord(e0, s), "event");
+    CK(cpg::launch_sigma(g->rec.as<double>(), n, k, dcs, sigma, s), "sigma");
+    if (precision == CPG_PLAIN_FP64) {
+        size_t wb = std::max(cpg::solve_fp64_work_bytes(n, k), (size_t)0);
+        CK(g->work.ensure(wb), "alloc solver workspace");
+        // RHS = -B sigma, CPanel/cpCase.cpp:192
+        CK(cpg::gemm_fp64_nk(g->B64.as<double>(), n, k, sigma, rhs, -1.0, g->work.p, s), "rhs");
+        CK(cpg::solve_fp64(g->A64.as<double>(), n, k, rhs, mu, g->work.p, 2.220446049250313e-16, 2 * n, &st, s),
+           "BiCGSTAB (FP64)");
+    } else {
+        size_t wb = cpg::solve_mixed_work_bytes(n, k);
+        CK(g->work.ensure(wb), "alloc solver workspace");
+        CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
+        CK(cpg::solve_mixed(g->A32.as<float>(), n, k, rhs, mu, g->work.p, 1e-10, 1e-5, 12, 1000, &st, s),
+           "refined solve (mixed)");
+    }
+    CK(cudaEventRecord(e1, s), "event");
+    CK(g->post_work.ensure(cpg::post_work_bytes(g->T, k)), "alloc post workspace");
+    CK(cpg::launch_post(g->T, k, dcs, mu, phi, vel, cp, forces, tz, wmu, g->post_work.p, s), "post");
+    CK(cudaEventRecord(e2, s), "event");
+    // host outputs
+    auto copy = [&](double* dst, const double* src, size_t cnt) -> cudaError_t {
+        if (!dst) return cudaSuccess;
+        return cudaMemcpyAsync(dst, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, s);
+    };
+    std::vector<double> hf(9 * (size_t)k), ht(2 * (size_t)k);
+    if (out) {
+        CK(copy(out->mu, mu, kn), "copy mu");
+        CK(copy(out->sigma, sigma, kn), "copy sigma");
+        CK(copy(out->phi, phi, kn), "copy phi");
+        CK(copy(out->vel, vel, 3 * kn), "copy vel");
+        CK(copy(out->cp, cp, kn), "copy cp");
+    }
+    CK(cudaMemcpyAsync(hf.data(), forces, sizeof(double) * 9 * k, cudaMemcpyDeviceToHost, s), "copy forces");
+    CK(cudaMemcpyAsync(ht.data(), tz, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, s), "copy CL");
+    CK(cudaStreamSynchronize(s), "solve cases");
+    if (out) {
+        for (int c = 0; c < k; c++) {
+            if (out->CL) out->CL[c] = ht[2 * c];
+            if (out->CDi) out->CDi[c] = ht[2 * c + 1];
+            for (int q = 0; q < 3; q++) {
+                if (out->Fbody) out->Fbody[3 * c + q] = hf[9 * c + q];
+                if (out->Fwind) out->Fwind[3 * c + q] = hf[9 * c + 3 + q];
+                if (out->CM) out->CM[3 * c + q] = hf[9 * c + 6 + q];
+            }
+        }
+    }
+    float ms_solve = 0, ms_post = 0;
+    cudaEventElapsedTime(&ms_solve, e0, e1);
+    cudaEventElapsedTime(&ms_post, e1, e2);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaEventDestroy(e2);
+    if (stats) {
+        stats->iters_max = st.iters_max;
+        stats->iters_total = st.iters_total;
+        stats->refinements = st.refinements;
+        stats->residual_max = st.residual_max;
+        stats->n_near = precision == CPG_PLAIN_FP64 ? g->n_near64 : g->n_near32;
+        stats->n_far = n * n - stats->n_near;
+        stats->ms_assemble = ms_asm;
+        stats->ms_solve = ms_solve;
+        stats->ms_post = ms_post;
+    }
+    if (st.residual_max > (precision == CPG_PLAIN_FP64 ? 1e-10 : 1e-9))
+        return fail(ctx, CPG_E_NOT_CONVERGED, "solver stopped above tolerance");
+    return CPG_OK;
+}
+
+int cpg_panel_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* src, double* dub) {
+    if (!ctx || m < 0 || (m > 0 && (!verts || !poi || !src || !dub))) return fail(ctx, CPG_E_INVALID, "bad argument");
+    CK(cpg::launch_phi_batch(verts, poi, m, src, dub, 0, ctx->stream), "panelPhiInf");
+    CK(cudaStreamSynchronize(ctx->stream), "panelPhiInf");
+    return CPG_OK;
+}
+
+int cpg_dub_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* dub) {
+    if (!ctx || m < 0 || (m > 0 && (!verts || !poi || !dub))) return fail(ctx, CPG_E_INVALID, "bad argument");
+    CK(cpg::launch_phi_batch(verts, poi, m, nullptr, dub, 1, ctx->stream), "dubPhiInf");
+    CK(cudaStreamSynchronize(ctx->stream), "dubPhiInf");
+    return CPG_OK;
+}
+
+int cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* vs, double* vd) {
+    if (!ctx || m < 0 || (m > 0 && (!verts || !poi || !vs || !vd))) return fail(ctx, CPG_E_INVALID, "bad argument");
+    CK(cpg::launch_v_batch(verts, poi, m, vs, vd, ctx->stream), "panelVInf");
+    CK(cudaStreamSynchronize(ctx->stream), "panelVInf");
+    return CPG_OK;
+}
+
+int cpg_compiled_arch(void) { return CPG_COMPILED_ARCH; }
+
+}  // extern "C"

@@ -1,0 +1,296 @@
+// Influence-matrix assembly (geometry::setInfCoeff, CPanel/geometry.cpp:809-891).
+//
+// Compiled with --fmad=false (see panel64.cuh).  Layout: A(i,j) at A[j*n + i]
+// (column-major like the reference's Eigen::MatrixXd), i = target centroid,
+// j = source panel.  A block owns 128 consecutive targets and a contiguous range of
+// source panels, staged 32 at a time in shared memory; each store instruction of
+// a warp writes 32 consecutive rows of one column.
+#include "assemble.h"
+#include "panel64.cuh"
+
+namespace {
+
+constexpr int TI = 128;   // targets per block (threads)
+constexpr int TJ = 32;    // sources per shared-memory tile
+
+__device__ __forceinline__ void load_tile(double* s_rec, const double* __restrict__ rec, int64_t j0, int64_t n) {
+    const int tot = TJ * R_STRIDE;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) {
+        int64_t j = j0 + t / R_STRIDE;
+        s_rec[t] = j < n ? rec[j0 * R_STRIDE + t] : 0.0;
+    }
+}
+
+// Plain FP64: writes A and B for the body panels.
+__global__ void __launch_bounds__(TI) k_assemble_fp64(const double* __restrict__ rec, int64_t n, int64_t jchunk,
+                                                      double* __restrict__ A, double* __restrict__ B,
+                                                      unsigned long long* __restrict__ near_count) {
+    __shared__ double s_rec[TJ * R_STRIDE];
+    int64_t i = (int64_t)blockIdx.x * TI + threadIdx.x;
+    bool act = i < n;
+    dv3 poi = act ? ld3(rec + i * R_STRIDE + R_C) : mk3(0, 0, 0);
+    int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
+    unsigned nnear = 0;
+    for (int64_t j0 = jb; j0 < je; j0 += TJ) {
+        __syncthreads();
+        load_tile(s_rec, rec, j0, n);
+        __syncthreads();
+        int cnt = (int)min((int64_t)TJ, je - j0);
+        if (!act) continue;
+        for (int t = 0; t < cnt; t++) {
+            int64_t j = j0 + t;
+            double src = 0, dub = 0;
+            nnear += panel_phi_inf(s_rec + t * R_STRIDE, poi, src, dub);
+            A[j * n + i] = dub;
+            B[j * n + i] = src;
+        }
+    }
+    if (near_count) {
+        for (int o = 16; o > 0; o >>= 1) nnear += __shfl_down_sync(0xffffffffu, nnear, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(near_count, (unsigned long long)nnear);
+    }
+}
+
+// Mixed: FP32 far field, FP64 near field (the reference's own near set,
+// |pjk| <= 5 longSide), A stored as FP32; the source-influence right-hand-side
+// basis rb[c*n+i] = sum_j B(i,j) * n_j[c] is accumulated instead of storing B.
+__global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict__ rec, const float* __restrict__ frec,
+                                                       int64_t n, int64_t jchunk, float* __restrict__ A32,
+                                                       double* __restrict__ rb,
+                                                       unsigned long long* __restrict__ near_count) {
+    __shared__ double s_rec[TJ * R_STRIDE];
+    __shared__ float s_f[TJ * F_STRIDE];
+    int64_t i = (int64_t)blockIdx.x * TI + threadIdx.x;
+    bool act = i < n;
+    dv3 poi = act ? ld3(rec + i * R_STRIDE + R_C) : mk3(0, 0, 0);
+    float ch[3] = {0, 0, 0}, cl[3] = {0, 0, 0};
+    if (act) {
+        for (int c = 0; c < 3; c++) {
+            ch[c] = frec[i * F_STRIDE + F_CHI + c];
+            cl[c] = frec[i * F_STRIDE + F_CLO + c];
+        }
+    }
+    int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
+    double acc64[3] = {0, 0, 0};
+    unsigned nnear = 0;
+    const float inv4pi = (float)(1.0 / CPG_FOUR_PI);
+    for (int64_t j0 = jb; j0 < je; j0 += TJ) {
+        __syncthreads();
+        load_tile(s_rec, rec, j0, n);
+        for (int t = threadIdx.x; t < TJ * F_STRIDE; t += blockDim.x) {
+            int64_t j = j0 + t / F_STRIDE;
+            s_f[t] = j < n ? frec[j0 * F_STRIDE + t] : 0.f;
+        }
+        __syncthreads();
+        int cnt = (int)min((int64_t)TJ, je - j0);
+        if (!act) continue;
+        float acc32[3] = {0.f, 0.f, 0.f};
+        for (int t = 0; t < cnt; t++) {
+            int64_t j = j0 + t;
+            const float* f = s_f + t * F_STRIDE;
+            float dx = __fadd_rn(__fsub_rn(ch[0], f[F_CHI + 0]), __fsub_rn(cl[0], f[F_CLO + 0]));
+            float dy = __fadd_rn(__fsub_rn(ch[1], f[F_CHI + 1]), __fsub_rn(cl[1], f[F_CLO + 1]));
+            float dz = __fadd_rn(__fsub_rn(ch[2], f[F_CHI + 2]), __fsub_rn(cl[2], f[F_CLO + 2]));
+            float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            float L = f[F_LONG];
+            float lim = __fmul_rn(25.f, __fmul_rn(L, L));
+            bool far;
+            if (r2 > __fmul_rn(lim, 1.00001f))
+                far = true;
+            else if (r2 < __fmul_rn(lim, 0.99999f))
+                far = false;
+            else {  // guard band: decide exactly as the FP64 reference does
+                const double* r = s_rec + t * R_STRIDE;
+                double d = norm3(poi - ld3(r + R_C));
+                far = d / r[R_LONG] > 5;
+            }
+            if (far) {
+                float rinv = rsqrtf(r2);
+                float src = __fmul_rn(__fmul_rn(f[F_AREA], rinv), inv4pi);
+                float pn = __fmaf_rn(dz, f[F_N + 2], __fmaf_rn(dy, f[F_N + 1], __fmul_rn(dx, f[F_N + 0])));
+                float dub = __fmul_rn(__fmul_rn(pn, __fmul_rn(rinv, rinv)), src);
+                A32[j * n + i] = dub;
+                acc32[0] = __fmaf_rn(src, f[F_N + 0], acc32[0]);
+                acc32[1] = __fmaf_rn(src, f[F_N + 1], acc32[1]);
+                acc32[2] = __fmaf_rn(src, f[F_N + 2], acc32[2]);
+            } else {
+                double src = 0, dub = 0;
+                const double* r = s_rec + t * R_STRIDE;
+                panel_phi_inf(r, poi, src, dub);
+                nnear++;
+                A32[j * n + i] = (float)dub;
+                acc64[0] += src * r[R_N + 0];
+                acc64[1] += src * r[R_N + 1];
+                acc64[2] += src * r[R_N + 2];
+            }
+        }
+        acc64[0] += (double)acc32[0];
+        acc64[1] += (double)acc32[1];
+        acc64[2] += (double)acc32[2];
+    }
+    if (act) {
+        atomicAdd(rb + i, acc64[0]);
+        atomicAdd(rb + n + i, acc64[1]);
+        atomicAdd(rb + 2 * n + i, acc64[2]);
+    }
+    if (near_count) {
+        for (int o = 16; o > 0; o >>= 1) nnear += __shfl_down_sync(0xffffffffu, nnear, o);
+        if ((threadIdx.x & 31) == 0) atomicAdd(near_count, (unsigned long long)nnear);
+    }
+}
+
+// Wake doublet columns, CPanel/geometry.cpp:853-873.  One thread per target row
+// walks the wake panels in wPanels order, so each of the (at most four) columns a
+// wake panel touches receives its contributions in the reference's order.
+template <typename T>
+__global__ void k_wake_columns(const double* __restrict__ rec, const double* __restrict__ wrec,
+                               const int32_t* __restrict__ widx, const double* __restrict__ wcoef, int64_t n,
+                               int64_t nw, T* __restrict__ A) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dv3 poi = ld3(rec + i * R_STRIDE + R_C);
+    for (int64_t j = 0; j < nw; j++) {
+        double infl = dub_phi_inf(wrec + j * R_STRIDE, poi);
+        double c = wcoef[j];
+        const int32_t* ix = widx + 4 * j;
+        int64_t c0 = ix[0], c1 = ix[1], c2 = ix[2], c3 = ix[3];
+        A[c0 * n + i] = (T)((double)A[c0 * n + i] + infl * (1 - c));
+        A[c1 * n + i] = (T)((double)A[c1 * n + i] + infl * (c - 1));
+        A[c2 * n + i] = (T)((double)A[c2 * n + i] + infl * c);
+        A[c3 * n + i] = (T)((double)A[c3 * n + i] - infl * c);
+    }
+}
+
+// panel::setGeom + getLocalSys on the device for free triangles (batched API).
+__device__ void make_record(const double* v9, double* r) {
+    dv3 p0 = ld3(v9), p1 = ld3(v9 + 3), p2 = ld3(v9 + 6);
+    double ls = 0;
+    dv3 pp[3] = {p0, p1, p2};
+    for (int k = 0; k < 3; k++) {
+        double l = norm3(pp[k == 2 ? 0 : k + 1] - pp[k]);
+        if (l > ls) ls = l;
+    }
+    dv3 a = p1 - p0, b = p2 - p0;
+    dv3 c = ((p0 + p1) + p2) / 3.0;
+    double th = acos(dot3(a, b) / (norm3(a) * norm3(b)));
+    double area = 0.5 * norm3(a) * norm3(b) * sin(th);
+    dv3 nn = cross3(a, b);
+    double z = dot3(nn, nn);
+    dv3 n = z > 0 ? nn / sqrt(z) : nn;
+    dv3 l0 = p0 - c;
+    double zl = dot3(l0, l0);
+    dv3 l = zl > 0 ? l0 / sqrt(zl) : l0;
+    dv3 m = cross3(n, l);
+    for (int k = 0; k < 9; k++) r[k] = v9[k];
+    const dv3 f[4] = {c, n, l, m};
+    for (int q = 0; q < 4; q++) {
+        r[R_C + 3 * q] = f[q].x;
+        r[R_C + 3 * q + 1] = f[q].y;
+        r[R_C + 3 * q + 2] = f[q].z;
+    }
+    r[R_AREA] = area;
+    r[R_LONG] = ls;
+    r[23] = 0;
+}
+
+__global__ void k_phi_batch(const double* __restrict__ verts, const double* __restrict__ poi, int64_t m,
+                            double* __restrict__ src, double* __restrict__ dub, int mode) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    double r[R_STRIDE];
+    make_record(verts + 9 * t, r);
+    dv3 p = ld3(poi + 3 * t);
+    if (mode == 0) {
+        double s = 0, d = 0;
+        panel_phi_inf(r, p, s, d);
+        src[t] = s;
+        dub[t] = d;
+    } else {
+        dub[t] = dub_phi_inf(r, p);
+    }
+}
+
+__global__ void k_v_batch(const double* __restrict__ verts, const double* __restrict__ poi, int64_t m,
+                          double* __restrict__ vs, double* __restrict__ vd) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    double r[R_STRIDE];
+    make_record(verts + 9 * t, r);
+    dv3 a, b;
+    panel_v_inf(r, ld3(poi + 3 * t), a, b);
+    vs[3 * t] = a.x;
+    vs[3 * t + 1] = a.y;
+    vs[3 * t + 2] = a.z;
+    vd[3 * t] = b.x;
+    vd[3 * t + 1] = b.y;
+    vd[3 * t + 2] = b.z;
+}
+
+// Trefftz-plane potential operator G(p, w) = dubPhiInf_w(p) (FP64, per mesh).
+__global__ void k_wake_potential_op(const double* __restrict__ wrec, int64_t nw, const double* __restrict__ pts,
+                                    int64_t np, double* __restrict__ G) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= np * nw) return;
+    int64_t p = t / nw, w = t % nw;
+    G[t] = dub_phi_inf(wrec + w * R_STRIDE, ld3(pts + 3 * p));
+}
+
+int64_t chunk_for(int64_t n) {
+    // enough blocks in y to fill the 152 SMs several times over
+    int64_t bx = (n + TI - 1) / TI;
+    int64_t want = 152 * 16;
+    int64_t by = (want + bx - 1) / bx;
+    if (by < 1) by = 1;
+    int64_t ch = (n + by - 1) / by;
+    ch = ((ch + TJ - 1) / TJ) * TJ;
+    return ch < TJ ? TJ : ch;
+}
+
+}  // namespace
+
+namespace cpg {
+
+cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wrec, const int32_t* widx,
+                                 const double* wcoef, int64_t nw, double* A, double* B,
+                                 unsigned long long* near_count, cudaStream_t s) {
+    int64_t ch = chunk_for(n);
+    dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
+    k_assemble_fp64<<<grid, TI, 0, s>>>(rec, n, ch, A, B, near_count);
+    if (nw > 0) k_wake_columns<double><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
+                                  const int32_t* widx, const double* wcoef, int64_t nw, float* A32, double* rb,
+                                  unsigned long long* near_count, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(rb, 0, sizeof(double) * 3 * n, s);
+    if (e != cudaSuccess) return e;
+    int64_t ch = chunk_for(n);
+    dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
+    k_assemble_mixed<<<grid, TI, 0, s>>>(rec, frec, n, ch, A32, rb, near_count);
+    if (nw > 0) k_wake_columns<float><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A32);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,
+                             cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    k_phi_batch<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(verts, poi, m, src, dub, mode);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_v_batch(const double* verts, const double* poi, int64_t m, double* vs, double* vd, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    k_v_batch<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(verts, poi, m, vs, vd);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_wake_potential_op(const double* wrec, int64_t nw, const double* pts, int64_t np, double* G,
+                                     cudaStream_t s) {
+    int64_t tot = np * nw;
+    if (tot <= 0) return cudaSuccess;
+    k_wake_potential_op<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(wrec, nw, pts, np, G);
+    return cudaGetLastError();
+}
+
+}  // namespace cpg

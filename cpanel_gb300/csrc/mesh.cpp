@@ -1,0 +1,601 @@
+// Host-side mesh ingest and topology (see mesh.h).  Compiled with
+// -ffp-contract=off: every geometric quantity is evaluated in the same order as
+// the reference's Eigen expressions so that branch decisions (trailing-edge side,
+// tip-patch flags, cluster angles) come out identically.
+#include "mesh.h"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <unordered_map>
+
+namespace cpg {
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+
+inline d3 add(d3 a, d3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline d3 sub(d3 a, d3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline d3 mul(double s, d3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline d3 divs(d3 a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+inline double dot(d3 a, d3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double nrm(d3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline d3 cross(d3 a, d3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline d3 unit(d3 a) {
+    double z = a.x * a.x + a.y * a.y + a.z * a.z;
+    return z > 0 ? divs(a, std::sqrt(z)) : a;
+}
+
+struct Panel {
+    int nd[3], ed[3];
+    d3 c, n;
+    double area, longSide;
+    int id, tri;
+    bool wake;
+    int group;  // surface or wake index
+    // body
+    bool upper = false, lower = false, tip = false;
+    int ts = 3, index = -1;
+    std::vector<int> nbr, cluster;
+    // wake
+    int upPan = -1, loPan = -1;
+    bool teWake = false;
+};
+
+struct Edge {
+    int n1, n2;
+    int nb = 0, nw = 0;
+    int b[3], w[3];
+    bool te = false;
+};
+
+struct Line {
+    int up, lo;
+    double y;
+};
+
+struct Wake {
+    std::vector<int> pans;
+    std::vector<Line> lines;
+    double yMin = 0, yMax = 0, x0 = 0, xf = 0, z0 = 0, zf = 0;
+    bool live = true;
+};
+
+struct Builder {
+    std::vector<d3> P;
+    std::vector<Edge> E;
+    std::unordered_map<uint64_t, int> emap;
+    std::vector<Panel> pan;
+    std::vector<bool> surfLS;
+    std::vector<Wake> wakes;
+
+    int edge(int a, int b) {  // geometry::findEdge, CPanel/geometry.cpp:771-787
+        uint64_t k = ((uint64_t)std::min(a, b) << 32) | (uint64_t)std::max(a, b);
+        auto it = emap.find(k);
+        if (it != emap.end()) return it->second;
+        Edge e;
+        e.n1 = a;
+        e.n2 = b;
+        E.push_back(e);
+        emap.emplace(k, (int)E.size() - 1);
+        return (int)E.size() - 1;
+    }
+
+    void geom(Panel& p) {  // panel::setGeom, CPanel/panel.cpp:33-72
+        p.longSide = 0;
+        for (int i = 0; i < 3; i++) {
+            double l = nrm(sub(P[E[p.ed[i]].n2], P[E[p.ed[i]].n1]));
+            if (l > p.longSide) p.longSide = l;
+        }
+        d3 p0 = P[p.nd[0]], p1 = P[p.nd[1]], p2 = P[p.nd[2]];
+        d3 a = sub(p1, p0), b = sub(p2, p0);
+        p.c = divs(add(add(p0, p1), p2), 3.0);
+        double th = std::acos(dot(a, b) / (nrm(a) * nrm(b)));
+        p.area = 0.5 * nrm(a) * nrm(b) * std::sin(th);
+        p.n = unit(cross(a, b));
+    }
+
+    void addLine(int w, Line l) {  // wake::addWakeLine, CPanel/wake.cpp:140-144
+        wakes[w].lines.push_back(l);
+        std::sort(wakes[w].lines.begin(), wakes[w].lines.end(), [](const Line& a, const Line& b) { return a.y < b.y; });
+    }
+
+    void parents(int wi, int up, int lo) {  // wakePanel::setParentPanels, CPanel/wakePanel.cpp:120-152
+        Panel& W = pan[wi];
+        pan[up].upper = true;
+        pan[lo].lower = true;
+        W.teWake = true;
+        if (W.upPan < 0 || pan[up].c.x < W.c.x) {
+            W.upPan = up;
+            W.loPan = lo;
+        }
+        // wakeLine::setDimensions (CPanel/wakeLine.cpp:31-46): last TE edge of the upper panel
+        int te = -1;
+        for (int k = 0; k < 3; k++)
+            if (E[pan[W.upPan].ed[k]].te) te = pan[W.upPan].ed[k];
+        d3 mid = divs(add(P[E[te].n1], P[E[te].n2]), 2.0);
+        addLine(W.group, Line{W.upPan, W.loPan, mid.y});
+    }
+
+    void checkTE(int ei) {  // edge::checkTE, CPanel/edge.cpp:48-109
+        Edge& e = E[ei];
+        if (e.nb != 2) return;
+        if (e.nw == 1) {
+            e.te = true;
+            const Panel& W = pan[e.w[0]];
+            d3 v1 = sub(pan[e.b[0]].c, W.c), v2 = sub(pan[e.b[1]].c, W.c);
+            double t1 = std::acos(dot(v1, W.n) / (nrm(v1) * nrm(W.n)));
+            double t2 = std::acos(dot(v2, W.n) / (nrm(v2) * nrm(W.n)));
+            if (t1 < t2)
+                parents(e.w[0], e.b[0], e.b[1]);
+            else
+                parents(e.w[0], e.b[1], e.b[0]);
+        } else {
+            const Panel& b0 = pan[e.b[0]];
+            const Panel& b1 = pan[e.b[1]];
+            double ang = std::acos(dot(b0.n, b1.n));
+            if (ang > 4.7 * kPi / 6 && b0.id == b1.id) {
+                e.te = true;
+                surfLS[b0.group] = true;
+                surfLS[b1.group] = true;
+            }
+        }
+    }
+};
+
+int fact(int i) {
+    int o = 1;
+    for (int k = 2; k <= i; k++) o *= k;
+    return o;
+}
+
+}  // namespace
+
+// chtlsnd::chtlsnd for N = 1, no derivative observations (used by wake::Vradial,
+// CPanel/wake.cpp:587-594).  Monomials x, x^2/2, x^3/6 (orders 1..order).
+void chtls_1d(const double* dx, int nf, int order, double* F) {
+    double rmax = 0;
+    for (int i = 0; i < nf; i++) {
+        double r = std::sqrt(dx[i] * dx[i]);
+        if (r > rmax) rmax = r;
+    }
+    const int t = order;
+    std::vector<double> d(nf), W(nf), A(nf * t), M(t * t), R(t * nf);
+    for (int i = 0; i < nf; i++) d[i] = dx[i] / rmax;
+    for (int i = 0; i < nf; i++) W[i] = 1 / std::sqrt(d[i] * d[i]);
+    for (int k = 0; k < t; k++) {
+        double f = 1.0 / fact(k + 1);
+        for (int i = 0; i < nf; i++) A[i * t + k] = f * std::pow(d[i], k + 1);
+    }
+    for (int r = 0; r < t; r++)
+        for (int c = 0; c < t; c++) {
+            double s = 0;
+            for (int i = 0; i < nf; i++) s += A[i * t + r] * W[i] * A[i * t + c];
+            M[r * t + c] = s;
+        }
+    for (int r = 0; r < t; r++)
+        for (int i = 0; i < nf; i++) R[r * nf + i] = A[i * t + r] * W[i];
+    // Householder QR (no pivoting) and solve, as Eigen::HouseholderQR::solve
+    std::vector<double> tau(t);
+    for (int k = 0; k < t; k++) {
+        double c0 = M[k * t + k], tail = 0;
+        for (int i = k + 1; i < t; i++) tail += M[i * t + k] * M[i * t + k];
+        double beta;
+        if (tail <= std::numeric_limits<double>::min()) {
+            tau[k] = 0;
+            beta = c0;
+            for (int i = k + 1; i < t; i++) M[i * t + k] = 0;
+        } else {
+            beta = std::sqrt(c0 * c0 + tail);
+            if (c0 >= 0) beta = -beta;
+            for (int i = k + 1; i < t; i++) M[i * t + k] /= (c0 - beta);
+            tau[k] = (beta - c0) / beta;
+        }
+        M[k * t + k] = beta;
+        if (tau[k] != 0)
+            for (int j = k + 1; j < t; j++) {
+                double tmp = M[k * t + j];
+                for (int i = k + 1; i < t; i++) tmp += M[i * t + k] * M[i * t + j];
+                M[k * t + j] -= tau[k] * tmp;
+                for (int i = k + 1; i < t; i++) M[i * t + j] -= tau[k] * M[i * t + k] * tmp;
+            }
+    }
+    for (int k = 0; k < t; k++) {
+        if (tau[k] == 0) continue;
+        for (int c = 0; c < nf; c++) {
+            double tmp = R[k * nf + c];
+            for (int i = k + 1; i < t; i++) tmp += M[i * t + k] * R[i * nf + c];
+            R[k * nf + c] -= tau[k] * tmp;
+            for (int i = k + 1; i < t; i++) R[i * nf + c] -= tau[k] * M[i * t + k] * tmp;
+        }
+    }
+    for (int c = 0; c < nf; c++)
+        for (int i = t - 1; i >= 0; i--) {
+            double s = R[i * nf + c];
+            for (int j = i + 1; j < t; j++) s -= M[i * t + j] * R[j * nf + c];
+            R[i * nf + c] = s / M[i * t + i];
+        }
+    for (int i = 0; i < nf; i++) F[i] = R[i] / rmax;  // first-order row, / rmax^1
+}
+
+std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, const int32_t* ids, int64_t nt,
+                       HostMesh& out) {
+    if (nn <= 0 || nt <= 0) return "empty mesh";
+    Builder B;
+    B.P.resize(nn);
+    for (int64_t i = 0; i < nn; i++) B.P[i] = {nodes[3 * i], nodes[3 * i + 1], nodes[3 * i + 2]};
+    std::vector<int64_t> conn(3 * nt);
+    for (int64_t i = 0; i < 3 * nt; i++) {
+        conn[i] = tris[i] - 1;
+        if (conn[i] < 0 || conn[i] >= nn) return "triangle references a node outside 1..n_nodes";
+    }
+    // wake connectivity correction, CPanel/geometry.cpp:218-244,631-667
+    int64_t wns = nn, wts = nt;
+    bool anyWake = false;
+    for (int64_t i = 0; i < nt; i++) {
+        if (ids[i] > 1000) anyWake = true;
+        if (i > 0 && ids[i] > 1000 && ids[i - 1] < 1000) {
+            wns = std::min(conn[3 * i], std::min(conn[3 * i + 1], conn[3 * i + 2]));
+            wts = i;
+        }
+    }
+    if (anyWake) {
+        double tol = 100000;
+        for (int64_t i = 0; i < nt; i++)
+            for (int j = 0; j < 3; j++) {
+                double l = nrm(sub(B.P[conn[3 * i + (j < 2 ? j + 1 : 0)]], B.P[conn[3 * i + j]]));
+                if (l < tol) tol = l;
+            }
+        std::vector<int64_t> rep(nn, -1);
+        for (int64_t j = wns; j < nn; j++)
+            for (int64_t i = 0; i < wns; i++) {
+                d3 v = sub(B.P[i], B.P[j]);
+                if (std::max(std::fabs(v.x), std::max(std::fabs(v.y), std::fabs(v.z))) < tol) {
+                    rep[j] = i;
+                    break;
+                }
+            }
+        for (int64_t i = wts; i < nt; i++)
+            for (int j = 0; j < 3; j++)
+                if (rep[conn[3 * i + j]] >= 0) conn[3 * i + j] = rep[conn[3 * i + j]];
+    }
+    // createSurfaces, CPanel/geometry.cpp:712-747
+    std::vector<std::vector<int>> surfPans;
+    B.pan.reserve(nt);
+    for (int64_t i = 0; i < nt; i++) {
+        Panel p;
+        for (int k = 0; k < 3; k++) p.nd[k] = (int)conn[3 * i + k];
+        if (p.nd[0] == p.nd[1] || p.nd[1] == p.nd[2] || p.nd[0] == p.nd[2]) return "degenerate triangle";
+        for (int k = 0; k < 3; k++) p.ed[k] = B.edge(p.nd[k], p.nd[k < 2 ? k + 1 : 0]);
+        p.id = ids[i];
+        p.tri = (int)i;
+        p.wake = ids[i] > 1000;
+        bool fresh = (i == 0 || ids[i] != ids[i - 1]);
+        if (!p.wake) {
+            if (fresh) {
+                surfPans.emplace_back();
+                B.surfLS.push_back(false);
+            }
+            p.group = (int)surfPans.size() - 1;
+        } else {
+            if (fresh) B.wakes.emplace_back();
+            p.group = (int)B.wakes.size() - 1;
+        }
+        B.geom(p);
+        B.pan.push_back(p);
+        int pi = (int)B.pan.size() - 1;
+        for (int k = 0; k < 3; k++) {
+            Edge& e = B.E[p.ed[k]];
+            if (!p.wake) {
+                if (e.nb < 3) e.b[e.nb] = pi;
+                e.nb++;
+            } else {
+                if (e.nw < 3) e.w[e.nw] = pi;
+                e.nw++;
+            }
+            B.checkTE(p.ed[k]);
+        }
+        if (!p.wake) {
+            surfPans[p.group].push_back(pi);
+        } else {  // wake::addPanel, CPanel/wake.cpp:42-88
+            Wake& W = B.wakes[p.group];
+            if (W.pans.empty()) {
+                d3 q = B.P[p.nd[0]];
+                W.yMax = W.yMin = q.y;
+                W.x0 = W.xf = q.x;
+                W.z0 = W.zf = q.z;
+            }
+            for (int k = 0; k < 3; k++) {
+                d3 q = B.P[p.nd[k]];
+                if (q.y > W.yMax) W.yMax = q.y;
+                else if (q.y < W.yMin) W.yMin = q.y;
+                if (q.x > W.xf) W.xf = q.x;
+                else if (q.x < W.x0) W.x0 = q.x;
+                if (q.z > W.zf) W.zf = q.z;
+                else if (q.z < W.z0) W.z0 = q.z;
+            }
+            W.pans.push_back(pi);
+        }
+    }
+    for (const Edge& e : B.E)  // edge::setNeighbors
+        if (e.nb == 2) {
+            B.pan[e.b[0]].nbr.push_back(e.b[1]);
+            B.pan[e.b[1]].nbr.push_back(e.b[0]);
+        }
+    // wake merge, CPanel/geometry.cpp:426-447
+    std::vector<int> order;
+    if (B.wakes.size() > 1) {
+        bool merged = false;
+        for (size_t i = 0; i < B.wakes.size(); i++)
+            for (size_t j = i + 1; j < B.wakes.size(); j++) {
+                Wake &a = B.wakes[i], &b = B.wakes[j];
+                if (!a.live || !b.live) continue;
+                double eps = std::pow(10.0, -2.0);
+                if (std::fabs(b.x0 - a.x0) < eps && std::fabs(b.z0 - a.z0) < eps && std::fabs(b.xf - a.xf) < eps &&
+                    std::fabs(b.zf - a.zf) < eps) {
+                    for (int w : b.pans) {
+                        a.pans.push_back(w);
+                        B.pan[w].group = (int)i;
+                    }
+                    for (const Line& l : b.lines) B.addLine((int)i, l);
+                    if (b.yMin < a.yMin) a.yMin = b.yMin;
+                    if (b.yMax > a.yMax) a.yMax = b.yMax;
+                    b.live = false;
+                    order.push_back((int)i);
+                    merged = true;
+                }
+            }
+        if (!merged) {
+            order.clear();
+            for (size_t i = 0; i < B.wakes.size(); i++) order.push_back((int)i);
+        }
+    } else {
+        for (size_t i = 0; i < B.wakes.size(); i++) order.push_back((int)i);
+    }
+    // bPanels: surfaces in reverse file order; wPanels: wakes in order
+    std::vector<int> bp, wp;
+    for (size_t s = surfPans.size(); s-- > 0;) bp.insert(bp.end(), surfPans[s].begin(), surfPans[s].end());
+    for (int w : order)
+        for (int p : B.wakes[w].pans) wp.push_back(p);
+    for (size_t i = 0; i < bp.size(); i++) B.pan[bp[i]].index = (int)i;
+    for (int w : order)
+        if (B.wakes[w].lines.size() < 2) return "a wake has fewer than two trailing-edge wake lines";
+
+    // bodyPanel::setTipFlag, CPanel/bodyPanel.cpp:58-95
+    const double tipTol = std::pow(10.0, -8.0);
+    for (int b : bp) {
+        Panel& p = B.pan[b];
+        if (!B.surfLS[p.group]) continue;
+        int count = 0;
+        for (int q : p.nbr) {
+            d3 nn2 = B.pan[q].n;
+            double d = dot(p.n, nn2) / (nrm(p.n) * nrm(nn2));
+            d = d > 1 ? 1 : (d < -1 ? -1 : d);
+            if (std::acos(d) < tipTol && std::asin(nn2.x) > -kPi / 12) count++;
+        }
+        p.tip = count >= 2;
+    }
+    // bodyPanel::setCluster / clusterTest, CPanel/bodyPanel.cpp:402-487,617-640
+    for (int self : bp) {
+        Panel& p = B.pan[self];
+        int dim = p.tip ? 2 : 3;
+        size_t buffer = 10;
+        size_t nObs = (size_t)(fact(p.ts + dim) / (fact(dim) * fact(p.ts)) - 1) + buffer;
+        size_t nP = (nObs + 1) / 2;
+        size_t old = 0;
+        p.cluster.push_back(self);
+        bool upF = p.upper, loF = p.lower;
+        auto inCluster = [&](int q) { return std::find(p.cluster.begin(), p.cluster.end(), q) != p.cluster.end(); };
+        while (p.cluster.size() < nP) {
+            std::vector<int> add;
+            for (size_t i = old; i < p.cluster.size(); i++) {
+                const std::vector<int> nb = B.pan[p.cluster[i]].nbr;
+                for (int q : nb) {
+                    const Panel& o = B.pan[q];
+                    bool ok = !((upF && o.lower) || (loF && o.upper)) && p.tip == o.tip;
+                    if (ok) {
+                        double d = dot(o.n, p.n);
+                        d = d > 1 ? 1 : (d < -1 ? -1 : d);
+                        ok = std::acos(d) < 5 * kPi / 6 && !inCluster(q) && q != self;
+                    }
+                    if (ok) {
+                        if (o.upper) upF = true;
+                        else if (o.lower) loF = true;
+                        if (std::find(add.begin(), add.end(), q) == add.end()) add.push_back(q);
+                    }
+                }
+            }
+            if (add.empty() && p.cluster.size() < nP) {
+                while (p.cluster.size() < nP + 1 && p.ts >= 1) {
+                    if (buffer > 0) buffer -= 1;
+                    else p.ts -= 1;
+                    nObs = (size_t)(fact(p.ts + dim) / (fact(dim) * fact(p.ts))) + buffer;
+                    nP = (nObs + 1) / 2;
+                }
+                if (p.cluster.size() > nP + 1) p.cluster.resize(nP + 1);
+                break;
+            }
+            old = p.cluster.size();
+            for (int q : add) {
+                p.cluster.push_back(q);
+                if (p.cluster.size() == nP + 1) break;
+            }
+        }
+        if (p.ts < 1 || p.cluster.size() < 2) return "a body panel has no usable CHTLS neighbourhood";
+        if (p.cluster.size() > 32) return "CHTLS cluster larger than 32 panels";
+    }
+
+    // ---- flatten ----
+    HostMesh& H = out;
+    H.n_nodes = nn;
+    H.n_body = (int64_t)bp.size();
+    H.n_wake = (int64_t)wp.size();
+    H.body.assign(H.n_body * PF_STRIDE, 0.0);
+    H.bez.assign(H.n_body * 3, 0.0);
+    H.tip.resize(H.n_body);
+    H.upper.resize(H.n_body);
+    H.lower.resize(H.n_body);
+    H.tsorder.resize(H.n_body);
+    H.surf_id.resize(H.n_body);
+    H.file_tri.resize(H.n_body);
+    H.cl_ptr.assign(1, 0);
+    H.cl_idx.clear();
+    H.n_tip = 0;
+    auto pack = [&](const Panel& p, double* o) {
+        for (int k = 0; k < 3; k++) {
+            d3 v = B.P[p.nd[k]];
+            o[3 * k] = v.x;
+            o[3 * k + 1] = v.y;
+            o[3 * k + 2] = v.z;
+        }
+        d3 l = unit(sub(B.P[p.nd[0]], p.c));  // panel::getLocalSys, CPanel/panel.cpp:156-168
+        d3 m = cross(p.n, l);
+        const d3 f[4] = {p.c, p.n, l, m};
+        for (int q = 0; q < 4; q++) {
+            o[PF_C + 3 * q] = f[q].x;
+            o[PF_C + 3 * q + 1] = f[q].y;
+            o[PF_C + 3 * q + 2] = f[q].z;
+        }
+        o[PF_AREA] = p.area;
+        o[PF_LONG] = p.longSide;
+    };
+    for (int64_t i = 0; i < H.n_body; i++) {
+        const Panel& p = B.pan[bp[i]];
+        pack(p, &H.body[i * PF_STRIDE]);
+        H.bez[3 * i] = p.n.x;
+        H.bez[3 * i + 1] = p.n.y;
+        H.bez[3 * i + 2] = p.n.z;
+        H.tip[i] = p.tip;
+        H.n_tip += p.tip;
+        H.upper[i] = p.upper;
+        H.lower[i] = p.lower;
+        H.tsorder[i] = p.ts;
+        H.surf_id[i] = p.id;
+        H.file_tri[i] = p.tri;
+        for (int q : p.cluster) H.cl_idx.push_back(B.pan[q].index);
+        H.cl_ptr.push_back((int32_t)H.cl_idx.size());
+    }
+    H.wake.assign(H.n_wake * PF_STRIDE, 0.0);
+    H.widx.resize(H.n_wake * 4);
+    H.wcoef.resize(H.n_wake);
+    // wakePanel::interpPanels, CPanel/wakePanel.cpp:48-81
+    auto bracket = [](const std::vector<Line>& L, double y, const Line*& a, const Line*& b) {
+        if (y < L[1].y) {
+            a = &L[0];
+            b = &L[1];
+        } else if (y >= L.back().y) {
+            a = &L[L.size() - 2];
+            b = &L[L.size() - 1];
+        } else {
+            a = b = nullptr;
+            for (size_t i = 1; i + 1 < L.size(); i++)
+                if (L[i].y <= y && L[i + 1].y > y) {
+                    a = &L[i];
+                    b = &L[i + 1];
+                }
+        }
+    };
+    for (int64_t j = 0; j < H.n_wake; j++) {
+        const Panel& w = B.pan[wp[j]];
+        pack(w, &H.wake[j * PF_STRIDE]);
+        const Line *a, *b;
+        bracket(B.wakes[w.group].lines, w.c.y, a, b);
+        if (!a) return "wake panel outside its wake lines";
+        H.wcoef[j] = (w.c.y - a->y) / (b->y - a->y);
+        H.widx[4 * j] = B.pan[a->up].index;
+        H.widx[4 * j + 1] = B.pan[a->lo].index;
+        H.widx[4 * j + 2] = B.pan[b->up].index;
+        H.widx[4 * j + 3] = B.pan[b->lo].index;
+    }
+    H.n_lines = 0;
+    // Trefftz plane geometry, CPanel/wake.cpp:146-188,508-640
+    H.trefftz.clear();
+    H.tz_pts.clear();
+    for (int wi : order) {
+        const Wake& W = B.wakes[wi];
+        H.n_lines += (int64_t)W.lines.size();
+        TrefftzWake T;
+        const int nP2 = 164;
+        T.step = (W.yMax - W.yMin) / nP2;
+        double xT = W.x0 + 2 * (W.xf - W.x0) / 3;
+        for (int i = 1; i < nP2; i++) {
+            TrefftzStation S;
+            S.y = W.yMin + i * T.step;
+            // wake::pntInWake
+            d3 pw{0, 0, 0};
+            bool found = false;
+            for (int q : W.pans) {
+                const Panel& w = B.pan[q];
+                if (!w.teWake || found) continue;
+                const Panel& U = B.pan[w.upPan];
+                for (int k = 0; k < 3 && !found; k++) {
+                    const Edge& e = B.E[U.ed[k]];
+                    if (!e.te) continue;
+                    d3 p1 = B.P[e.n1], p2 = B.P[e.n2];
+                    if ((p1.y <= S.y && p2.y >= S.y) || (p1.y >= S.y && p2.y <= S.y)) {
+                        double t = (S.y - p1.y) / (p2.y - p1.y);
+                        d3 pnt = add(p1, mul(t, sub(p2, p1)));
+                        d3 c = cross(w.n, d3{0, 1, 0});
+                        d3 o{-c.x, -c.y, -c.z};
+                        if (o.x < 0) o = mul(-1.0, o);
+                        double sc = (xT - pnt.x) / o.x;
+                        pw = add(pnt, mul(sc, o));
+                        found = true;
+                    }
+                }
+            }
+            // wake::Vradial sample points
+            double r, th = kPi / 4, dZmax = 0.3, delZ;
+            d3 POI;
+            POI.x = pw.x;
+            r = pw.y >= 0 ? W.yMax - pw.y : pw.y - W.yMin;
+            delZ = r * std::sin(th);
+            if (delZ > dZmax) {
+                delZ = dZmax;
+                th = std::asin(dZmax / r);
+            }
+            POI.y = pw.y >= 0 ? W.yMax - r * std::cos(th) : W.yMin + r * std::cos(th);
+            POI.z = pw.z + r * std::sin(th);
+            double dz = 0.5 * delZ, stp = 2 * dz / (6 - 1);
+            double dY[6], dZ[6];
+            S.pt0 = (int32_t)(H.tz_pts.size() / 3);
+            H.tz_pts.push_back(POI.x);
+            H.tz_pts.push_back(POI.y);
+            H.tz_pts.push_back(POI.z);
+            d3 ys[6], zs[6];
+            for (int q = 0; q < 6; q++) {
+                double delta = -dz + q * stp;
+                ys[q] = add(POI, mul(delta, d3{0, 1, 0}));
+                zs[q] = add(POI, mul(delta, d3{0, 0, 1}));
+                dY[q] = ys[q].y - POI.y;
+                dZ[q] = zs[q].z - POI.z;
+            }
+            for (int q = 0; q < 6; q++) {
+                H.tz_pts.push_back(ys[q].x);
+                H.tz_pts.push_back(ys[q].y);
+                H.tz_pts.push_back(ys[q].z);
+            }
+            for (int q = 0; q < 6; q++) {
+                H.tz_pts.push_back(zs[q].x);
+                H.tz_pts.push_back(zs[q].y);
+                H.tz_pts.push_back(zs[q].z);
+            }
+            chtls_1d(dY, 6, 3, S.Fy);
+            chtls_1d(dZ, 6, 3, S.Fz);
+            // wake::wakeStrength bracketing
+            const Line *a, *b;
+            bracket(W.lines, S.y, a, b);
+            if (!a) return "Trefftz station outside the wake lines";
+            S.interp = (S.y - a->y) / (b->y - a->y);
+            S.line_up1 = B.pan[a->up].index;
+            S.line_lo1 = B.pan[a->lo].index;
+            S.line_up2 = B.pan[b->up].index;
+            S.line_lo2 = B.pan[b->lo].index;
+            T.st.push_back(S);
+        }
+        H.trefftz.push_back(std::move(T));
+    }
+    return "";
+}
+
+}  // namespace cpg

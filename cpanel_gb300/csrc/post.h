@@ -1,0 +1,52 @@
+// Post-processing tables and launchers (post.cu): CHTLS surface velocity, Cp,
+// forces and the Trefftz-plane analysis, all on the device.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cpg {
+
+constexpr int kClMax = 32;  // max cluster size (self included)
+
+struct PostTables {
+    int64_t n = 0, nw = 0;
+    const double* rec = nullptr;     // body panel records (n x 24)
+    const double* bez = nullptr;     // n x 3
+    const int32_t* cl_ptr = nullptr; // n+1
+    const int32_t* cl_idx = nullptr;
+    const int32_t* tip = nullptr;
+    const int32_t* tsorder = nullptr;
+    const int32_t* widx = nullptr;   // n_wake x 4
+    const double* wcoef = nullptr;
+    // built by launch_chtls_weights
+    double* F3 = nullptr;            // n x 3 x 31
+    double* F2 = nullptr;            // n x 2 x 31
+    int32_t* mode = nullptr;         // n: bit0 3-D weights finite, bit1 2-D weights finite, bit2 tip
+    // Trefftz
+    int n_wakes = 0;
+    int n_st = 0;                    // stations per wake (163)
+    const double* tz_station = nullptr;  // per station: y, interp, Fy[6], Fz[6], step  (15 doubles)
+    const int32_t* tz_lines = nullptr;   // per station: up1 lo1 up2 lo2 pt0 (5 ints)
+    const double* G = nullptr;       // n_pts x nw dubPhiInf operator
+    int64_t n_pts = 0;
+};
+
+struct CaseScalars {  // per flow condition
+    double Vinf[3];
+    double V, PG, Sref, bref, cref, cg[3];
+    double T[9];      // windToBody transform (row-major)
+};
+
+cudaError_t launch_chtls_weights(const PostTables& t, cudaStream_t s);
+// mu: k x n; outputs k x n (phi, cp), k x n x 3 (vel); forces k x 9 [Fbody Fwind CM];
+// trefftz k x 2 [CL CDi]; work: device scratch of post_work_bytes.
+size_t post_work_bytes(const PostTables& t, int k);
+cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs_dev, const double* mu, double* phi,
+                        double* vel, double* cp, double* forces, double* trefftz, double* wake_mu, void* work,
+                        cudaStream_t s);
+
+cudaError_t launch_sigma(const double* rec, int64_t n, int k, const CaseScalars* cs, double* sigma, cudaStream_t s);
+cudaError_t launch_rhs_basis(const double* rb, int64_t n, int k, const CaseScalars* cs, double* rhs, cudaStream_t s);
+cudaError_t launch_widen(const float* a, double* b, int64_t m, cudaStream_t s);
+
+}  // namespace cpg

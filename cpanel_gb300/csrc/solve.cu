@@ -1,0 +1,519 @@
+// Dense solvers for the panel system (cpCase::solveMatrixEq, CPanel/cpCase.cpp:185-214).
+//
+// Vectors of k right-hand sides are stored case-major (k x n).  The matrix is read
+// once per multi-RHS product: a block owns 256 rows and a contiguous range of
+// columns; per-chunk partial products are summed afterwards in a fixed order, so
+// results are deterministic run to run.
+#include <algorithm>
+#include <cmath>
+#include <limits>
+#include <vector>
+
+#include "assemble.h"
+
+namespace {
+
+constexpr int MV_THREADS = 256;
+constexpr int MV_JT = 32;  // columns of X staged per shared-memory tile
+
+int64_t mv_chunk(int64_t n, int64_t want_blocks) {
+    int64_t bx = (n + MV_THREADS - 1) / MV_THREADS;
+    int64_t by = std::max<int64_t>(1, (want_blocks + bx - 1) / bx);
+    int64_t ch = (n + by - 1) / by;
+    ch = ((ch + MV_JT - 1) / MV_JT) * MV_JT;
+    return std::max<int64_t>(ch, MV_JT);
+}
+
+// P[(chunk*KB + c)*n + i] = sum_{j in chunk} A[j*n+i] * X[(col0+c)*n + j]
+template <typename TA, typename TX, typename TACC, int KB>
+__global__ void __launch_bounds__(MV_THREADS) k_mv(const TA* __restrict__ A, int64_t n, int64_t jchunk,
+                                                   const TX* __restrict__ X, int col0, int kb, TACC* __restrict__ P) {
+    __shared__ TACC sx[MV_JT][KB];
+    int64_t i = (int64_t)blockIdx.x * MV_THREADS + threadIdx.x;
+    int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
+    TACC acc[KB];
+#pragma unroll
+    for (int c = 0; c < KB; c++) acc[c] = 0;
+    for (int64_t j0 = jb; j0 < je; j0 += MV_JT) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < MV_JT * KB; t += MV_THREADS) {
+            int jj = t / KB, c = t % KB;
+            int64_t j = j0 + jj;
+            sx[jj][c] = (j < je && c < kb) ? (TACC)X[(int64_t)(col0 + c) * n + j] : (TACC)0;
+        }
+        __syncthreads();
+        if (i < n) {
+            int cnt = (int)min((int64_t)MV_JT, je - j0);
+            const TA* Ap = A + j0 * n + i;
+#pragma unroll 4
+            for (int t = 0; t < cnt; t++) {
+                TACC a = (TACC)Ap[(int64_t)t * n];
+#pragma unroll
+                for (int c = 0; c < KB; c++) acc[c] += a * sx[t][c];
+            }
+        }
+    }
+    if (i < n) {
+#pragma unroll
+        for (int c = 0; c < KB; c++)
+            if (c < kb) P[((int64_t)blockIdx.y * KB + c) * n + i] = acc[c];
+    }
+}
+
+// Y[(col0+c)*n+i] = alpha * sum_chunk P[(chunk*KB+c)*n+i]   (+ beta * B[...] if B)
+template <typename TACC, typename TY>
+__global__ void k_mv_reduce(const TACC* __restrict__ P, int nchunk, int KB, int kb, int64_t n, int col0, double alpha,
+                            const double* __restrict__ Bv, TY* __restrict__ Y) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)kb * n) return;
+    int c = (int)(t / n);
+    int64_t i = t % n;
+    double s = 0;
+    for (int q = 0; q < nchunk; q++) s += (double)P[((int64_t)q * KB + c) * n + i];
+    s *= alpha;
+    int64_t o = (int64_t)(col0 + c) * n + i;
+    if (Bv) s = Bv[o] + s;
+    Y[o] = (TY)s;
+}
+
+// Double-float residual chunks: exact FP32 products of A32 with x = xh + xl.
+template <int KB>
+__global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict__ A, int64_t n, int64_t jchunk,
+                                                         const double* __restrict__ X, int col0, int kb,
+                                                         double* __restrict__ P) {
+    __shared__ float sh[MV_JT][KB], sl[MV_JT][KB];
+    int64_t i = (int64_t)blockIdx.x * MV_THREADS + threadIdx.x;
+    int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
+    double acc[KB];
+#pragma unroll
+    for (int c = 0; c < KB; c++) acc[c] = 0;
+    for (int64_t j0 = jb; j0 < je; j0 += MV_JT) {
+        __syncthreads();
+        for (int t = threadIdx.x; t < MV_JT * KB; t += MV_THREADS) {
+            int jj = t / KB, c = t % KB;
+            int64_t j = j0 + jj;
+            double xv = (j < je && c < kb) ? X[(int64_t)(col0 + c) * n + j] : 0.0;
+            float h = (float)xv;
+            sh[jj][c] = h;
+            sl[jj][c] = (float)(xv - (double)h);
+        }
+        __syncthreads();
+        if (i < n) {
+            int cnt = (int)min((int64_t)MV_JT, je - j0);
+            const float* Ap = A + j0 * n + i;
+            float hi[KB], lo[KB];
+#pragma unroll
+            for (int c = 0; c < KB; c++) hi[c] = lo[c] = 0.f;
+            for (int t = 0; t < cnt; t++) {
+                float a = Ap[(int64_t)t * n];
+#pragma unroll
+                for (int c = 0; c < KB; c++) {
+                    float p = __fmul_rn(a, sh[t][c]);
+                    float e = __fmaf_rn(a, sh[t][c], -p);     // exact product error
+                    e = __fmaf_rn(a, sl[t][c], e);
+                    float s = __fadd_rn(hi[c], p);           // TwoSum(hi, p)
+                    float bb = __fsub_rn(s, hi[c]);
+                    float err = __fadd_rn(__fsub_rn(hi[c], __fsub_rn(s, bb)), __fsub_rn(p, bb));
+                    hi[c] = s;
+                    lo[c] = __fadd_rn(lo[c], __fadd_rn(err, e));
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < KB; c++) acc[c] += (double)hi[c] + (double)lo[c];
+        }
+    }
+    if (i < n) {
+#pragma unroll
+        for (int c = 0; c < KB; c++)
+            if (c < kb) P[((int64_t)blockIdx.y * KB + c) * n + i] = acc[c];
+    }
+}
+
+// Per-column FP64 dot products: out[q*k + c] = sum_i U_q[c*n+i] * V_q[c*n+i] for up to
+// two pairs (q = 0, 1).  Grid: (blocks over i, k).  Partials to part[(q*k+c)*nb + b].
+template <typename T>
+__global__ void k_dot2(const T* __restrict__ U0, const T* __restrict__ V0, const T* __restrict__ U1,
+                       const T* __restrict__ V1, int64_t n, int k, double* __restrict__ part) {
+    __shared__ double red[2][8];
+    int c = blockIdx.y;
+    int64_t base = (int64_t)c * n;
+    double s0 = 0, s1 = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        s0 += (double)U0[base + i] * (double)V0[base + i];
+        if (U1) s1 += (double)U1[base + i] * (double)V1[base + i];
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_down_sync(0xffffffffu, s0, o);
+        s1 += __shfl_down_sync(0xffffffffu, s1, o);
+    }
+    int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        red[0][w] = s0;
+        red[1][w] = s1;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0, b = 0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); q++) {
+            a += red[0][q];
+            b += red[1][q];
+        }
+        part[(int64_t)c * gridDim.x + blockIdx.x] = a;
+        part[((int64_t)k + c) * gridDim.x + blockIdx.x] = b;
+    }
+}
+
+__global__ void k_dot_finish(const double* __restrict__ part, int nb, int m, double* __restrict__ out) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= m) return;
+    double s = 0;
+    for (int b = 0; b < nb; b++) s += part[(int64_t)t * nb + b];
+    out[t] = s;
+}
+
+// BiCGSTAB vector updates; sc holds per-column scalars [beta, w, alpha, active] x k.
+template <typename T>
+__global__ void k_upd_p(const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ p, T* __restrict__ y,
+                        const T* __restrict__ invd, const double* __restrict__ sc, int64_t n, int k) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)k * n) return;
+    int c = (int)(t / n);
+    if (sc[4 * c + 3] == 0) return;
+    T beta = (T)sc[4 * c + 0], w = (T)sc[4 * c + 1];
+    T pv = r[t] + beta * (p[t] - w * v[t]);
+    p[t] = pv;
+    y[t] = invd[t % n] * pv;
+}
+
+template <typename T>
+__global__ void k_upd_s(const T* __restrict__ r, const T* __restrict__ v, T* __restrict__ s, T* __restrict__ z,
+                        const T* __restrict__ invd, const double* __restrict__ sc, int64_t n, int k) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)k * n) return;
+    int c = (int)(t / n);
+    if (sc[4 * c + 3] == 0) return;
+    T alpha = (T)sc[4 * c + 2];
+    T sv = r[t] - alpha * v[t];
+    s[t] = sv;
+    z[t] = invd[t % n] * sv;
+}
+
+template <typename T, typename TX>
+__global__ void k_upd_x(TX* __restrict__ x, T* __restrict__ r, const T* __restrict__ s, const T* __restrict__ tt,
+                        const T* __restrict__ y, const T* __restrict__ z, const double* __restrict__ sc, int64_t n,
+                        int k) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)k * n) return;
+    int c = (int)(t / n);
+    if (sc[4 * c + 3] == 0) return;
+    T alpha = (T)sc[4 * c + 2], w = (T)sc[4 * c + 1];
+    x[t] += (TX)(alpha * y[t] + w * z[t]);
+    r[t] = s[t] - w * tt[t];
+}
+
+template <typename T>
+__global__ void k_invdiag(const T* __restrict__ A, int64_t n, T* __restrict__ invd) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    T d = A[i * n + i];
+    invd[i] = d != (T)0 ? (T)1 / d : (T)1;
+}
+
+template <typename T>
+__global__ void k_restart(const double* __restrict__ b, const double* __restrict__ Ax, T* __restrict__ r,
+                          T* __restrict__ r0, const int* __restrict__ flag, int64_t n, int k) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)k * n) return;
+    if (!flag[t / n]) return;
+    T v = (T)(b[t] - Ax[t]);
+    r[t] = v;
+    r0[t] = v;
+}
+
+template <typename TS, typename TD>
+__global__ void k_convert(const TS* __restrict__ a, TD* __restrict__ b, int64_t m) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < m) b[t] = (TD)a[t];
+}
+
+__global__ void k_add_to(double* __restrict__ x, const float* __restrict__ d, int64_t m) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < m) x[t] += (double)d[t];
+}
+
+inline unsigned nblk(int64_t m, int b = 256) { return (unsigned)((m + b - 1) / b); }
+
+// ------------------------------------------------------------------ drivers
+struct Arena {
+    char* p;
+    size_t off = 0;
+    template <typename T>
+    T* take(size_t count) {
+        off = (off + 255) & ~size_t(255);
+        T* r = (T*)(p + off);
+        off += count * sizeof(T);
+        return r;
+    }
+};
+
+template <typename TA, typename TX, typename TACC>
+cudaError_t mv_dispatch(const TA* A, int64_t n, int k, const TX* X, void* Y, double alpha, const double* Badd,
+                        TACC* P, int64_t want_blocks, cudaStream_t s, bool y_is_double);
+
+template <typename TA, typename TX, typename TACC, int KB>
+void mv_launch(const TA* A, int64_t n, int64_t ch, const TX* X, int col0, int kb, TACC* P, cudaStream_t s) {
+    dim3 grid(nblk(n, MV_THREADS), (unsigned)((n + ch - 1) / ch));
+    k_mv<TA, TX, TACC, KB><<<grid, MV_THREADS, 0, s>>>(A, n, ch, X, col0, kb, P);
+}
+
+// Multi-RHS product Y = alpha*A*X (+Badd), RHS processed in groups of at most KBMAX.
+template <typename TA, typename TX, typename TACC, typename TY>
+cudaError_t matmul(const TA* A, int64_t n, int k, const TX* X, TY* Y, double alpha, const double* Badd, TACC* P,
+                   int kbmax, cudaStream_t s) {
+    int64_t ch = mv_chunk(n, 152 * 8);
+    int nchunk = (int)((n + ch - 1) / ch);
+    for (int col0 = 0; col0 < k; col0 += kbmax) {
+        int kb = std::min(kbmax, k - col0);
+        int KB;
+        if (kb <= 1) { KB = 1; mv_launch<TA, TX, TACC, 1>(A, n, ch, X, col0, kb, P, s); }
+        else if (kb <= 2) { KB = 2; mv_launch<TA, TX, TACC, 2>(A, n, ch, X, col0, kb, P, s); }
+        else if (kb <= 4) { KB = 4; mv_launch<TA, TX, TACC, 4>(A, n, ch, X, col0, kb, P, s); }
+        else if (kb <= 8) { KB = 8; mv_launch<TA, TX, TACC, 8>(A, n, ch, X, col0, kb, P, s); }
+        else if (kb <= 16) { KB = 16; mv_launch<TA, TX, TACC, 16>(A, n, ch, X, col0, kb, P, s); }
+        else if (kb <= 17) { KB = 17; mv_launch<TA, TX, TACC, 17>(A, n, ch, X, col0, kb, P, s); }
+        else if (kb <= 24) { KB = 24; mv_launch<TA, TX, TACC, 24>(A, n, ch, X, col0, kb, P, s); }
+        else { KB = 32; mv_launch<TA, TX, TACC, 32>(A, n, ch, X, col0, kb, P, s); }
+        k_mv_reduce<TACC, TY><<<nblk((int64_t)kb * n), 256, 0, s>>>(P, nchunk, KB, kb, n, col0, alpha, Badd, Y);
+    }
+    return cudaGetLastError();
+}
+
+template <int KB>
+void resid_launch(const float* A, int64_t n, int64_t ch, const double* X, int col0, int kb, double* P, cudaStream_t s) {
+    dim3 grid(nblk(n, MV_THREADS), (unsigned)((n + ch - 1) / ch));
+    k_resid_df<KB><<<grid, MV_THREADS, 0, s>>>(A, n, ch, X, col0, kb, P);
+}
+
+// r = b - A32 x (x FP64), products exact.
+cudaError_t residual_df(const float* A, int64_t n, int k, const double* x, const double* b, double* r, double* P,
+                        cudaStream_t s) {
+    int64_t ch = mv_chunk(n, 152 * 8);
+    int nchunk = (int)((n + ch - 1) / ch);
+    for (int col0 = 0; col0 < k; col0 += 17) {
+        int kb = std::min(17, k - col0);
+        int KB;
+        if (kb <= 1) { KB = 1; resid_launch<1>(A, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 2) { KB = 2; resid_launch<2>(A, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 4) { KB = 4; resid_launch<4>(A, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 8) { KB = 8; resid_launch<8>(A, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 16) { KB = 16; resid_launch<16>(A, n, ch, x, col0, kb, P, s); }
+        else { KB = 17; resid_launch<17>(A, n, ch, x, col0, kb, P, s); }
+        k_mv_reduce<double, double><<<nblk((int64_t)kb * n), 256, 0, s>>>(P, nchunk, KB, kb, n, col0, -1.0, b, r);
+    }
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t dots(const T* U0, const T* V0, const T* U1, const T* V1, int64_t n, int k, double* part, double* outd,
+                 double* outh, cudaStream_t s) {
+    const int nb = 64;
+    dim3 grid(nb, k);
+    k_dot2<T><<<grid, 256, 0, s>>>(U0, V0, U1, V1, n, k, part);
+    k_dot_finish<<<nblk(2 * k, 64), 64, 0, s>>>(part, nb, 2 * k, outd);
+    cudaMemcpyAsync(outh, outd, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, s);
+    return cudaStreamSynchronize(s);
+}
+
+// Batched BiCGSTAB following Eigen::BiCGSTAB per column (zero initial guess,
+// DiagonalPreconditioner, restart when r drifts orthogonal to r0).
+template <typename T, typename TA, typename TACC>
+cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena& ar, double tol, int64_t maxIters,
+                     int kbmax, cpg::SolveStats* st, cudaStream_t s, bool quiet_restart = false) {
+    const size_t kn = (size_t)k * n;
+    T *r = ar.take<T>(kn), *r0 = ar.take<T>(kn), *p = ar.take<T>(kn), *v = ar.take<T>(kn), *y = ar.take<T>(kn),
+      *z = ar.take<T>(kn), *sv = ar.take<T>(kn), *tv = ar.take<T>(kn), *invd = ar.take<T>(n);
+    double* Ax = ar.take<double>(kn);
+    int64_t ch = mv_chunk(n, 152 * 8);
+    int nchunk = (int)((n + ch - 1) / ch);
+    TACC* P = ar.take<TACC>((size_t)nchunk * std::min(kbmax, 32) * n);
+    double* part = ar.take<double>((size_t)2 * k * 64);
+    double* dd = ar.take<double>(2 * k);
+    double* sc = ar.take<double>(4 * k);
+    int* flag = ar.take<int>(k);
+    std::vector<double> hd(2 * k), hsc(4 * k);
+    std::vector<int> hflag(k);
+    cudaError_t e;
+    k_invdiag<TA><<<nblk(n), 256, 0, s>>>(A, n, (TA*)invd);  // TA == T for both uses
+    cudaMemsetAsync(x, 0, sizeof(T) * kn, s);
+    k_convert<double, T><<<nblk(kn), 256, 0, s>>>(b, r, kn);
+    cudaMemcpyAsync(r0, r, sizeof(T) * kn, cudaMemcpyDeviceToDevice, s);
+    cudaMemsetAsync(p, 0, sizeof(T) * kn, s);
+    cudaMemsetAsync(v, 0, sizeof(T) * kn, s);
+    // r0_sqnorm and rhs_sqnorm
+    std::vector<double> r0sq(k), rhssq(k), rho(k, 1), alpha(k, 1), w(k, 1), tol2(k);
+    std::vector<int64_t> it(k, 0), restarts(k, 0);
+    std::vector<char> done(k, 0);
+    {
+        double* bd = Ax;  // b as T is r at this point
+        (void)bd;
+        if ((e = dots<T>(r0, r0, r, r, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+        for (int c = 0; c < k; c++) {
+            r0sq[c] = hd[c];
+            rhssq[c] = hd[k + c];
+            tol2[c] = tol * tol * rhssq[c];
+            if (rhssq[c] == 0) done[c] = 1;
+        }
+    }
+    const double eps = std::numeric_limits<double>::epsilon();
+    const double eps2 = eps * eps;
+    std::vector<double> rr(k);
+    if ((e = dots<T>(r, r, r0, r, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+    for (;;) {
+        bool any = false, anyRestart = false;
+        std::vector<double> rho_new(k);
+        for (int c = 0; c < k; c++) {
+            rr[c] = hd[c];
+            rho_new[c] = hd[k + c];
+            bool act = !done[c] && rr[c] > tol2[c] && it[c] < maxIters;
+            if (!act) done[c] = 1;
+            hsc[4 * c + 3] = act ? 1.0 : 0.0;
+            hflag[c] = 0;
+            if (act) {
+                any = true;
+                if (std::fabs(rho_new[c]) < eps2 * r0sq[c]) {
+                    hflag[c] = 1;
+                    anyRestart = true;
+                }
+            }
+        }
+        if (!any) break;
+        std::vector<double> rho_old = rho;
+        for (int c = 0; c < k; c++)
+            if (hsc[4 * c + 3] != 0) rho[c] = rho_new[c];
+        if (anyRestart) {  // r = b - A x; r0 = r; rho = r0_sqnorm = |r|^2
+            cudaMemcpyAsync(flag, hflag.data(), sizeof(int) * k, cudaMemcpyHostToDevice, s);
+            matmul<TA, T, TACC, double>(A, n, k, x, Ax, 1.0, nullptr, P, kbmax, s);
+            k_restart<T><<<nblk(kn), 256, 0, s>>>(b, Ax, r, r0, flag, n, k);
+            if ((e = dots<T>(r, r, r, r, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+            for (int c = 0; c < k; c++)
+                if (hflag[c]) {
+                    rho[c] = r0sq[c] = hd[c];
+                    if (restarts[c]++ == 0) it[c] = 0;
+                }
+        }
+        for (int c = 0; c < k; c++) {
+            hsc[4 * c + 0] = (rho[c] / rho_old[c]) * (alpha[c] / w[c]);
+            hsc[4 * c + 1] = w[c];
+        }
+        cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
+        k_upd_p<T><<<nblk(kn), 256, 0, s>>>(r, v, p, y, invd, sc, n, k);
+        matmul<TA, T, TACC, T>(A, n, k, y, v, 1.0, nullptr, P, kbmax, s);
+        if ((e = dots<T>(r0, v, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+        for (int c = 0; c < k; c++)
+            if (hsc[4 * c + 3] != 0) {
+                alpha[c] = rho[c] / hd[c];
+                hsc[4 * c + 2] = alpha[c];
+            }
+        cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
+        k_upd_s<T><<<nblk(kn), 256, 0, s>>>(r, v, sv, z, invd, sc, n, k);
+        matmul<TA, T, TACC, T>(A, n, k, z, tv, 1.0, nullptr, P, kbmax, s);
+        if ((e = dots<T>(tv, tv, tv, sv, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+        for (int c = 0; c < k; c++)
+            if (hsc[4 * c + 3] != 0) {
+                double tt = hd[c];
+                w[c] = tt > 0 ? hd[k + c] / tt : 0.0;
+                hsc[4 * c + 1] = w[c];
+            }
+        cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
+        k_upd_x<T, T><<<nblk(kn), 256, 0, s>>>(x, r, sv, tv, y, z, sc, n, k);
+        for (int c = 0; c < k; c++)
+            if (hsc[4 * c + 3] != 0) it[c]++;
+        if ((e = dots<T>(r, r, r0, r, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+    }
+    if (st) {
+        for (int c = 0; c < k; c++) {
+            st->iters_max = std::max(st->iters_max, it[c]);
+            st->iters_total += it[c];
+            double err = rhssq[c] > 0 ? std::sqrt(rr[c] / rhssq[c]) : 0.0;
+            st->residual_max = std::max(st->residual_max, err);
+        }
+    }
+    (void)quiet_restart;
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+namespace cpg {
+
+size_t solve_fp64_work_bytes(int64_t n, int k) {
+    int64_t ch = mv_chunk(n, 152 * 8);
+    int64_t nchunk = (n + ch - 1) / ch;
+    size_t kn = (size_t)k * n;
+    return sizeof(double) * (9 * kn + n + nchunk * 32 * (size_t)n + 2 * k * 64 + 2 * k + 4 * k) + sizeof(int) * k +
+           64 * 256;
+}
+
+cudaError_t solve_fp64(const double* A, int64_t n, int k, const double* rhs, double* x, void* work, double tol,
+                       int64_t max_iters, SolveStats* st, cudaStream_t s) {
+    Arena ar{(char*)work};
+    return bicgstab<double, double, double>(A, n, k, rhs, x, ar, tol, max_iters, 8, st, s);
+}
+
+cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, double* y, double alpha, void* work,
+                         cudaStream_t s) {
+    return matmul<double, double, double, double>(M, n, k, x, y, alpha, nullptr, (double*)work, 8, s);
+}
+
+size_t solve_mixed_work_bytes(int64_t n, int k) {
+    int64_t ch = mv_chunk(n, 152 * 8);
+    int64_t nchunk = (n + ch - 1) / ch;
+    size_t kn = (size_t)k * n;
+    return sizeof(float) * (9 * kn + n + nchunk * 32 * (size_t)n) +
+           sizeof(double) * (kn /*Ax*/ + 2 * k * 64 + 2 * k + 4 * k + 2 * kn /*r64, d64*/ + nchunk * 32 * (size_t)n) +
+           sizeof(float) * kn + sizeof(int) * k + 64 * 256;
+}
+
+cudaError_t solve_mixed(const float* A32, int64_t n, int k, const double* rhs, double* x, void* work,
+                        double tol_outer, double tol_inner, int max_outer, int64_t max_inner, SolveStats* st,
+                        cudaStream_t s) {
+    Arena ar{(char*)work};
+    const size_t kn = (size_t)k * n;
+    double* r64 = ar.take<double>(kn);
+    float* d32 = ar.take<float>(kn);
+    int64_t ch = mv_chunk(n, 152 * 8);
+    int nchunk = (int)((n + ch - 1) / ch);
+    double* P64 = ar.take<double>((size_t)nchunk * 17 * n);
+    double* part = ar.take<double>((size_t)2 * k * 64);
+    double* dd = ar.take<double>(2 * k);
+    size_t mark = ar.off;
+    std::vector<double> hd(2 * k), bnorm(k);
+    cudaError_t e;
+    cudaMemsetAsync(x, 0, sizeof(double) * kn, s);
+    cudaMemcpyAsync(r64, rhs, sizeof(double) * kn, cudaMemcpyDeviceToDevice, s);
+    if ((e = dots<double>(rhs, rhs, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+    for (int c = 0; c < k; c++) bnorm[c] = std::sqrt(hd[c]);
+    double worst = 1;
+    for (int outer = 0; outer < max_outer; outer++) {
+        ar.off = mark;
+        SolveStats inner;
+        if ((e = bicgstab<float, float, float>(A32, n, k, r64, d32, ar, tol_inner, max_inner, 32, &inner, s)) !=
+            cudaSuccess)
+            return e;
+        if (st) {
+            st->iters_total += inner.iters_total;
+            st->iters_max = std::max(st->iters_max, inner.iters_max);
+            st->refinements++;
+        }
+        k_add_to<<<nblk(kn), 256, 0, s>>>(x, d32, kn);
+        if ((e = residual_df(A32, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;
+        if ((e = dots<double>(r64, r64, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
+        worst = 0;
+        for (int c = 0; c < k; c++) worst = std::max(worst, bnorm[c] > 0 ? std::sqrt(hd[c]) / bnorm[c] : 0.0);
+        if (worst <= tol_outer) break;
+    }
+    if (st) st->residual_max = std::max(st->residual_max, worst);
+    return cudaGetLastError();
+}
+
+}  // namespace cpg

@@ -1,0 +1,147 @@
+/*
+ * cpanel_gpu.h -- C ABI of the GB300 (sm_103a) CPanel steady panel path.
+ *
+ * Plain pointers and sizes only.  Every call returns a cpg_status; the message of
+ * the last failure on a context is returned by cpg_last_error().  Nothing here
+ * exits, prompts or prints.
+ *
+ * Reference interfaces replaced (paths relative to the CPanel project root):
+ *   cpg_geometry_create   geometry::readTri topology, CPanel/geometry.cpp:132-484
+ *   cpg_set_inf_coeff     geometry::setInfCoeff, CPanel/geometry.cpp:809-891
+ *   cpg_get_A / cpg_get_B geometry::getA / getB, CPanel/geometry.h:310-311
+ *   cpg_solve_cases       cpCase::run minus file output, CPanel/cpCase.cpp:31-139
+ *                         (setSourceStrengths :174-183, solveMatrixEq :185-214,
+ *                          compVelocity :342-365, trefftzPlaneAnalysis :541-552)
+ *   cpg_panel_phi_inf     bodyPanel::panelPhiInf, CPanel/bodyPanel.cpp:132-190
+ *   cpg_dub_phi_inf       panel::dubPhiInf, CPanel/panel.cpp:208-252
+ *   cpg_panel_v_inf       bodyPanel::panelVInf, CPanel/bodyPanel.cpp:305-348
+ */
+#ifndef CPANEL_GPU_H
+#define CPANEL_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    CPG_OK = 0,
+    CPG_E_INVALID = 1,        /* bad argument or size                           */
+    CPG_E_OOM = 2,            /* device or host allocation refused              */
+    CPG_E_CUDA = 3,           /* a CUDA runtime call failed                     */
+    CPG_E_BAD_MESH = 4,       /* topology the reference would reject or crash on */
+    CPG_E_NOT_CONVERGED = 5,  /* solver finished above its tolerance (results valid) */
+    CPG_E_TIMEOUT = 6,        /* a bounded device wait ran out                  */
+    CPG_E_NO_DEVICE = 7       /* no CUDA device / extension not usable          */
+} cpg_status;
+
+typedef enum {
+    CPG_PLAIN_FP64 = 0,  /* the reference method in FP64: explicit A, B; BiCGSTAB to eps */
+    CPG_MIXED = 1        /* FP32 far field + FP64 near field, FP32 Krylov + FP64-exact
+                            iterative refinement to rel. residual 1e-10              */
+} cpg_precision;
+
+typedef struct cpg_ctx cpg_ctx;
+typedef struct cpg_geometry cpg_geometry;
+
+typedef struct {
+    int64_t n_body;      /* body panels = matrix order                         */
+    int64_t n_wake;      /* wake panels (wPanels)                              */
+    int64_t n_wakes;     /* wakes after merging                                */
+    int64_t n_wakelines; /* trailing-edge wake lines, summed over wakes        */
+    int64_t n_tip;       /* panels flagged as tip patch                        */
+    int64_t n_nodes;
+} cpg_geometry_info;
+
+typedef struct {
+    double V, alpha, beta, mach; /* one flow condition (degrees)                */
+} cpg_flow;
+
+typedef struct {
+    double Sref, bref, cref, cg[3];
+} cpg_refs;
+
+/* Host output buffers of cpg_solve_cases; any pointer may be null (not returned).
+ * Per-panel arrays are k x n_body row-major (case-major). */
+typedef struct {
+    double* mu;      /* doublet strengths                                        */
+    double* sigma;   /* source strengths                                         */
+    double* phi;     /* panel potential                                          */
+    double* vel;     /* k x n x 3                                                */
+    double* cp;
+    double* CL;      /* k: Trefftz plane                                         */
+    double* CDi;     /* k                                                        */
+    double* Fbody;   /* k x 3 */
+    double* Fwind;   /* k x 3 */
+    double* CM;      /* k x 3 */
+} cpg_case_out;
+
+typedef struct {
+    int64_t iters_max;      /* most Krylov iterations over the k cases          */
+    int64_t iters_total;
+    int64_t refinements;    /* outer refinement steps (CPG_MIXED)                */
+    double  residual_max;   /* largest final relative residual                   */
+    int64_t n_near;         /* near-field pairs found by the last assembly       */
+    int64_t n_far;
+    double  ms_assemble, ms_solve, ms_post; /* device time of the last calls      */
+} cpg_solve_stats;
+
+/* ---- context ---- */
+int         cpg_create(cpg_ctx** out, int device);
+void        cpg_destroy(cpg_ctx* ctx);
+const char* cpg_last_error(const cpg_ctx* ctx);
+/* All work of a context is issued on this stream (cudaStream_t; 0 = the context's
+ * own non-blocking stream). */
+int         cpg_set_stream(cpg_ctx* ctx, void* stream);
+int         cpg_synchronize(cpg_ctx* ctx);
+
+/* ---- geometry: readTri topology + device-resident panel tables ----
+ * nodes n_nodes x 3, tris n_tris x 3 (1-based, Cart3D order), ids per tri (>1000: wake). */
+int  cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const int64_t* tris,
+                         const int32_t* ids, int64_t n_tris, cpg_geometry** out);
+void cpg_geometry_destroy(cpg_geometry* g);
+int  cpg_geometry_info_get(const cpg_geometry* g, cpg_geometry_info* out);
+/* Host copies of the topology for checking (same layouts as the CPU oracle):
+ * body: n_body x 18 [c(3) n(3) l(3) area longSide tip upper lower TSorder surfID
+ * cluster_size file_tri]; wake: n_wake x 8 [c(3) n(3) area longSide] + idx4 + coef;
+ * clusters: n_body x 32 (matrix indices, -1 padded, self first). */
+int  cpg_geometry_tables(const cpg_geometry* g, double* body, double* wake, int32_t* idx4, double* coef,
+                         int32_t* clusters);
+
+/* Host-only topology (no device needed): the same tables as cpg_geometry_tables
+ * straight from .tri arrays.  Call with null table pointers to fill *info only. */
+int  cpg_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids, int64_t n_tris,
+                  cpg_geometry_info* info, double* body, double* wake, int32_t* idx4, double* coef,
+                  int32_t* clusters);
+
+/* ---- assembly (geometry::setInfCoeff) ----
+ * CPG_PLAIN_FP64 builds A and B (n x n FP64, column-major, A(i,j) = A[j*n+i]).
+ * CPG_MIXED builds A in FP32 plus the FP64 near-field correction and the three
+ * source right-hand-side basis vectors (B is never stored). */
+int  cpg_set_inf_coeff(cpg_geometry* g, int precision);
+/* Copy the assembled matrices to host column-major buffers (n*n doubles).
+ * cpg_get_A works for both precisions (FP32 values widened for CPG_MIXED). */
+int  cpg_get_A(cpg_geometry* g, double* host);
+int  cpg_get_B(cpg_geometry* g, double* host);
+
+/* ---- steady cases (cpCase::run) over k flow conditions on one geometry ----
+ * Assembles first if the geometry holds no matrix of that precision. */
+int  cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_refs* refs, int precision,
+                     const cpg_case_out* out, cpg_solve_stats* stats);
+
+/* ---- single-evaluation influence operators on DEVICE arrays (batched) ----
+ * verts m x 9 (three vertices), poi m x 3; outputs m (phi) or m x 3 (velocity). */
+int  cpg_panel_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* phi_src,
+                       double* phi_dub);
+int  cpg_dub_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* phi_dub);
+int  cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* v_src,
+                     double* v_dub);
+
+/* Build identification: the sm architecture the kernels were compiled for. */
+int  cpg_compiled_arch(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPANEL_GPU_H */

@@ -1,0 +1,158 @@
+"""GPU parity: the sm_103a library against the CPU oracle, through the C ABI.
+
+Tolerances (from the path's specification):
+  * influence coefficients: 1e-12 relative (elementwise, relative to the column's
+    largest entry so that exact cancellations near zero are judged fairly);
+  * plain FP64 path: mu, Cp, CL, CDi within 1e-10 of the oracle;
+  * mixed path: Cp max-abs error <= 1e-5 and CL relative error <= 1e-6 against the
+    plain FP64 GPU path.
+"""
+import numpy as np
+import pytest
+
+from conftest import small_wing
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cg(built):
+    import cpanel_gb300
+    return cpanel_gb300
+
+
+def _matrix_rel_err(X, Xo):
+    scale = np.maximum(np.abs(Xo).max(axis=0, keepdims=True), 1e-300)
+    return (np.abs(X - Xo) / scale).max()
+
+
+@pytest.fixture(scope="module")
+def small(cg):
+    from oracle import pyoracle as po
+    nodes, tris, ids, info, spec = small_wing(n_chord=16, n_span=9)
+    g = cg.Geometry(nodes, tris, ids)
+    m = po.Mesh(nodes, tris, ids)
+    Ao, Bo = m.set_inf_coeff()
+    refs = dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0.0, 0.0))
+    return g, m, Ao, Bo, refs
+
+
+def test_assembly_fp64_matches_oracle(small):
+    g, m, Ao, Bo, refs = small
+    g.setInfCoeff("fp64")
+    A, B = g.getA(), g.getB()
+    assert _matrix_rel_err(A, Ao) < 1e-12
+    assert _matrix_rel_err(B, Bo) < 1e-12
+    assert np.all(np.diag(A)[: m.n] <= -0.5 + 1e-9)  # self term -0.5 (+ wake columns on TE rows)
+
+
+def test_assembly_fp64_4412_matches_oracle(cg, case4412):
+    from oracle import pyoracle as po
+    gg = case4412
+    g = cg.Geometry(gg["nodes"], gg["tris"].astype(np.int64), gg["ids"])
+    g.setInfCoeff("fp64")
+    m = po.Mesh(gg["nodes"], gg["tris"], gg["ids"])
+    Ao, Bo = m.set_inf_coeff()
+    assert _matrix_rel_err(g.getA(), Ao) < 1e-12
+    assert _matrix_rel_err(g.getB(), Bo) < 1e-12
+
+
+def test_assembly_mixed_is_close(small):
+    g, m, Ao, Bo, refs = small
+    g.setInfCoeff("mixed")
+    A32 = g.getA()
+    assert np.abs(A32 - Ao).max() < 1e-6
+
+
+def test_influence_operators_match_oracle(cg):
+    import torch
+    from oracle import pyoracle as po
+    rng = np.random.default_rng(7)
+    m = 257
+    verts = rng.uniform(-1, 1, (m, 9))
+    scale = rng.uniform(0.2, 3.0, (m, 1))
+    poi = rng.uniform(-1, 1, (m, 3)) * scale * 4
+    poi[:16] = verts[:16].reshape(-1, 3, 3).mean(axis=1)  # self points
+    v_t = torch.tensor(verts, device="cuda")
+    p_t = torch.tensor(poi, device="cuda")
+    s, d = cg.panel_phi_inf(v_t, p_t)
+    dw = cg.dub_phi_inf(v_t, p_t)
+    vs, vd = cg.panel_v_inf(v_t, p_t)
+    s, d, dw, vs, vd = (x.cpu().numpy() for x in (s, d, dw, vs, vd))
+    for i in range(m):
+        so, do = po.tri_phi_inf(verts[i], poi[i])
+        assert s[i] == pytest.approx(so, rel=1e-12, abs=1e-15)
+        assert d[i] == pytest.approx(do, rel=1e-12, abs=1e-15)
+        assert dw[i] == pytest.approx(po.tri_dub_phi_inf(verts[i], poi[i]), rel=1e-12, abs=1e-15)
+        vso, vdo = po.tri_v_inf(verts[i], poi[i])
+        assert np.allclose(vs[i], vso, rtol=1e-11, atol=1e-14)
+        assert np.allclose(vd[i], vdo, rtol=1e-11, atol=1e-14)
+
+
+def test_plain_solve_matches_oracle(cg, small):
+    g, m, Ao, Bo, refs = small
+    flows = [(1.0, 5.0, 0.0, 0.1), (1.0, -2.0, 0.0, 0.1), (1.3, 8.0, 1.0, 0.2)]
+    r = cg.solve_cases(g, flows, precision="fp64", **refs)
+    assert r["status"] == 0
+    for c, f in enumerate(flows):
+        o = m.case(Ao, Bo, V=f[0], alpha=f[1], beta=f[2], mach=f[3], **refs)
+        assert np.abs(r["sigma"][c] - o["sigma"]).max() < 1e-14
+        assert np.abs(r["mu"][c] - o["mu"]).max() < 1e-10
+        assert np.abs(r["phi"][c] - o["phi"]).max() < 1e-10
+        assert np.abs(r["vel"][c] - o["vel"]).max() < 1e-10
+        assert np.abs(r["cp"][c] - o["cp"]).max() < 1e-10
+        assert abs(r["CL"][c] - o["CL"]) < 1e-10 and abs(r["CDi"][c] - o["CDi"]) < 1e-10
+        assert np.abs(r["Fbody"][c] - o["Fbody"]).max() < 1e-10
+        assert np.abs(r["Fwind"][c] - o["Fwind"]).max() < 1e-10
+        assert np.abs(r["CM"][c] - o["CM"]).max() < 1e-10
+
+
+def test_4412_reference_case_on_gpu(cg, case4412):
+    gg = case4412
+    g = cg.Geometry(gg["nodes"], gg["tris"].astype(np.int64), gg["ids"])
+    case = cg.CpCase(g, float(gg["V"]), float(gg["alpha"]), float(gg["beta"]), float(gg["mach"]),
+                     Sref=float(gg["Sref"]), bref=float(gg["bref"]), cref=float(gg["cref"]), cg=tuple(gg["cg"]))
+    assert case.run()
+    assert abs(case.getCL() - float(gg["CL"])) <= 5.01e-6
+    assert abs(case.getCD() - float(gg["CDi"])) <= 5.01e-6
+    CN, CA, CY = gg["body_CN_CA_CY"]
+    assert abs(case.getBodyForces()[2] - CN) <= 5.01e-6
+
+
+def test_mixed_matches_plain_within_tolerance(cg, small):
+    g, m, Ao, Bo, refs = small
+    flows = [(1.0, a, 0.0, 0.1) for a in (-4.0, 0.0, 5.0, 12.0)]
+    rp = cg.solve_cases(g, flows, precision="fp64", **refs)
+    rm = cg.solve_cases(g, flows, precision="mixed", **refs)
+    assert rm["status"] == 0
+    assert np.abs(rm["cp"] - rp["cp"]).max() <= 1e-5
+    assert np.all(np.abs(rm["CL"] - rp["CL"]) <= 1e-6 * np.abs(rp["CL"]) + 1e-9)
+
+
+def test_small_steady_workload_parity(cg):
+    """The 3,900-panel NACA 0012 wing (alpha = 5 deg, Mach 0.1): plain GPU vs oracle."""
+    from cpanel_gb300 import wing
+    from oracle import pyoracle as po
+    spec = wing.config_small_steady()
+    nodes, tris, ids, info = wing.make_wing(spec)
+    g = cg.Geometry(nodes, tris, ids)
+    refs = dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0.0, 0.0))
+    r = cg.solve_cases(g, [(1.0, 5.0, 0.0, 0.1)], precision="fp64", **refs)
+    m = po.Mesh(nodes, tris, ids)
+    Ao, Bo = m.set_inf_coeff()
+    assert _matrix_rel_err(g.getA(), Ao) < 1e-12
+    o = m.case(Ao, Bo, alpha=5.0, mach=0.1, **refs)
+    assert np.abs(r["mu"][0] - o["mu"]).max() < 1e-10
+    assert np.abs(r["cp"][0] - o["cp"]).max() < 1e-10
+    assert abs(r["CL"][0] - o["CL"]) < 1e-10 and abs(r["CDi"][0] - o["CDi"]) < 1e-10
+    rm = cg.solve_cases(g, [(1.0, 5.0, 0.0, 0.1)], precision="mixed", **refs)
+    assert np.abs(rm["cp"] - r["cp"]).max() <= 1e-5
+    assert abs(rm["CL"][0] - r["CL"][0]) <= 1e-6 * abs(r["CL"][0])
+
+
+def test_invalid_arguments_are_reported(cg):
+    g_err = None
+    with pytest.raises(cg.CpgError) as e:
+        cg.Geometry(np.zeros((3, 3)), np.array([[1, 1, 2]]), np.array([1], dtype=np.int32))
+    assert e.value.code == 4
+    del g_err

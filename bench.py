@@ -1,0 +1,328 @@
+#!/usr/bin/env python
+"""Steady solves/s of the GB300 panel path (CPanel hot path) on one or more GPUs.
+
+Workload: NACA 4412 tapered wing, AR 6, taper 0.6, 80 cosine-spaced points per side
+x 61 span stations (19,276 body triangles, 120 wake triangles), Mach 0.1, 17
+angles of attack -4..12 deg on one geometry.  A step is one full sweep on the
+performance (mixed) path: influence assembly, preconditioner set-up, the 17
+refined solves and post-processing (CHTLS velocity, Cp, forces, Trefftz CL/CDi).
+`value` counts solves (mesh x alpha) per second with the mesh tables resident on
+the device; `e2e` repeats the step through the C ABI from host arrays (readTri
+topology, uploads and result copies inside the timed region).
+
+Accuracy is checked once, outside the timing, against the plain FP64 GPU path
+(the reference method in FP64), whose own throughput is reported beside it.
+Multi-GPU: replicas (each rank runs the full workload on its GPU), weak scaling.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALPHAS = [float(a) for a in range(-4, 13)]
+MACH = 0.1
+METRIC = "steady solves/s + p50/p99 latency at Cp err<=1e-5 vs FP64 plain GPU path"
+# BiCGSTAB (Eigen semantics, tol = eps) iterations of the plain FP64 path on this
+# mesh, measured on the GPU; used only by the CPU cost model below.
+PLAIN_ITERS = 372
+
+
+def workload():
+    from cpanel_gb300 import wing
+    spec = wing.config_multi_rhs()
+    nodes, tris, ids, info = wing.make_wing(spec)
+    refs = dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0.0, 0.0))
+    return spec, nodes, tris, ids, info, refs
+
+
+def config_dict(info):
+    return {"workload": "NACA4412 tapered AR6 wing, 80 pts/side x 61 stations, 17 alphas (-4..12 deg)",
+            "body_panels": info["n_body"], "wake_panels": info["n_wake"], "alphas": len(ALPHAS), "mach": MACH,
+            "precision": "mixed: df32 far field + FP64 near field, FP32 block-Jacobi BiCGSTAB, refined to 1e-10",
+            "l2": "inputs larger than L2 (A = 2 x 1.49 GB)", "parallelism": "replicas"}
+
+
+def read_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_cost_model(nodes, tris, ids, refs, nthreads):
+    """CPU oracle (C++ restatement of the reference path) on a bounded sample of the
+    same workload: assembly of 1/8 of the matrix rows (all columns), one FP64
+    matvec over those rows, and one full post-processing pass.  The 17-alpha sweep
+    time is assembled from them: 8*t_asm + 17*(2*PLAIN_ITERS*8*t_mv + t_post)."""
+    from oracle import pyoracle as po
+    t0 = time.perf_counter()
+    m = po.Mesh(nodes, tris, ids)
+    t_topo = time.perf_counter() - t0
+    n = m.n
+    rows = n // 8
+    t0 = time.perf_counter()
+    A, B = m.set_inf_coeff(rows=(0, rows), nthreads=nthreads)
+    t_asm = time.perf_counter() - t0
+    blk = np.ascontiguousarray(A)
+    x = np.random.default_rng(0).standard_normal(n)
+    t0 = time.perf_counter()
+    reps = 5
+    for _ in range(reps):
+        blk @ x
+    t_mv = (time.perf_counter() - t0) / reps
+    mu = np.random.default_rng(1).standard_normal(n) * 0.1
+    t0 = time.perf_counter()
+    m.post(mu, alpha=5.0, mach=MACH, **refs)
+    t_post = time.perf_counter() - t0
+    k = len(ALPHAS)
+    t_sweep = t_topo + 8 * t_asm + k * (2 * PLAIN_ITERS * 8 * t_mv + t_post)
+    sample = ("oracle on %d threads: assembly of %d/%d rows x8, FP64 matvec of those rows x8 x 2 x %d "
+              "BiCGSTAB iterations (plain-path count), full post-processing; sample wall %.1fs"
+              % (nthreads, rows, n, PLAIN_ITERS, t_topo + t_asm + reps * t_mv + t_post))
+    return k / t_sweep, sample
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    spec, nodes, tris, ids, info, refs = workload()
+    nthreads = os.cpu_count() or 1
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, sample = cpu_cost_model(nodes, tris, ids, refs, nthreads)
+        if i >= args.warmup:
+            vals.append(v)
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": len(ALPHAS) / value * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NACA wing)",
+            "config": config_dict(info), "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": nthreads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import __graft_entry__
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if dist:
+        dist.barrier()
+    import cpanel_gb300 as cg
+
+    spec, nodes, tris, ids, info, refs = workload()
+    flows = [(1.0, a, 0.0, MACH) for a in ALPHAS]
+    k = len(flows)
+    ctx = cg.Context(local)
+    stream = torch.cuda.current_stream()
+    ctx.check(ctx.L.cpg_set_stream(ctx.h, stream.cuda_stream), "set_stream")
+    g = cg.Geometry(nodes, tris, ids, ctx=ctx)
+    n = g.n
+
+    # ---- accuracy vs the plain FP64 GPU path (untimed) and its throughput
+    acc = {}
+    plain = None
+    if not args.no_plain:
+        t0 = time.perf_counter()
+        rp = cg.solve_cases(g, flows, precision="fp64", want=("cp",), **refs)
+        t_plain = time.perf_counter() - t0
+        st = rp["stats"]
+        plain = {"value": k / t_plain, "unit": "solves/s", "ms_per_step": t_plain * 1e3,
+                 "iters_max": st["iters_max"], "ms_assemble": st["ms_assemble"], "ms_solve": st["ms_solve"],
+                 "ms_post": st["ms_post"], "steps": 1}
+        rm = cg.solve_cases(g, flows, precision="mixed", want=("cp",), **refs)
+        acc = {"cp_err_max": float(np.abs(rm["cp"] - rp["cp"]).max()),
+               "cl_relerr_max": float(np.max(np.abs(rm["CL"] - rp["CL"]) / np.abs(rp["CL"]))),
+               "cdi_relerr_max": float(np.max(np.abs(rm["CDi"] - rp["CDi"]) / np.maximum(np.abs(rp["CDi"]), 1e-12)))}
+        g.ctx.check(0)
+        del rp, rm
+
+    # ---- timed: mixed path, mesh resident
+    def step():
+        g.setInfCoeff("mixed")
+        return cg.solve_cases(g, flows, precision="mixed", want=(), **refs)
+
+    for _ in range(args.warmup):
+        step()
+    ctx.prof_enable(True)
+    lat = []
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            ev[i][0].record(stream)
+            r = step()
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if dist:
+        dist.barrier()
+    lat = [a.elapsed_time(b) for a, b in ev]
+    prof = ctx.prof_read()
+    ctx.prof_enable(False)
+    t_dev = sum(lat) / 1e3
+    t_max = t_dev
+    if dist:
+        tt = torch.tensor([t_dev], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = world * k * args.steps / t_max
+    stats = r["stats"]
+
+    # ---- e2e through the C ABI from host arrays
+    e2e_times = []
+    h2d = d2h = 0
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ge = cg.Geometry(nodes, tris, ids, ctx=ctx)
+        ge.setInfCoeff("mixed")
+        re = cg.solve_cases(ge, flows, precision="mixed", want=("cp",), **refs)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            e2e_times.append(dt)
+        h2d = ge.info["h2d_bytes"] + k * 8 * 20
+        d2h = re["cp"].nbytes + 2 * k * 8 + 9 * k * 8
+        del ge
+    e2e_value = world * k * len(e2e_times) / sum(e2e_times)
+
+    # ---- roofline of the dominant kernel class in the timed region
+    hbm, peak_kind = read_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][1])
+    roof = None
+    mv_l, mv_ms = prof["matvec_fp32"]
+    if mv_l:
+        bytes_mv = 4.0 * n * n + 2 * 4.0 * k * n
+        ach = bytes_mv / (mv_ms / mv_l * 1e-3) / 1e9
+        roof = {"bound": "hbm", "kernel": "k_mv<float> (FP32 multi-RHS matvec, 17 RHS)", "achieved": ach,
+                "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
+                "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_mv,
+                "avg_launch_ms": mv_ms / mv_l, "launches": mv_l}
+    breakdown = {name: {"launches": int(l), "ms": round(ms, 3)} for name, (l, ms) in prof.items() if l}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, sample = cpu_cost_model(nodes, tris, ids, refs, os.cpu_count() or 1)
+        cpu = {"value": v, "unit": "solves/s", "cores": os.cpu_count() or 1, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        lat_sorted = sorted(lat)
+        p50 = float(np.percentile(lat_sorted, 50))
+        p99 = float(np.percentile(lat_sorted, 99))
+        launches = int(sum(l for l, _ in prof.values()))
+        line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+df32+f64", "data": "synthetic (seeded NACA wing)",
+                "config": config_dict(info),
+                "latency_ms": {"p50": p50, "p99": p99, "what": "one 17-alpha sweep request (device time)"},
+                "accuracy_vs_plain_fp64": acc, "plain_fp64": plain,
+                "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "roofline": roof, "dominant_kernel_class": {"name": dom[0], "ms": dom[1][1], "launches": dom[1][0]},
+                "kernel_breakdown_ms": breakdown, "gpu_launches": launches,
+                "solver": {"iters_max": stats["iters_max"], "refinements": stats["refinements"],
+                           "residual_max": stats["residual_max"], "near_pairs": stats["n_near"]},
+                "cpu_baseline": cpu, "clocks": clk.summary(), "wall_s": wall}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

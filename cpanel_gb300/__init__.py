@@ -13,7 +13,9 @@ Host-side mirror of the reference's operator surface for this path:
 All compute runs in libcpanel_gb300.so (sm_103a); this module only marshals
 arguments.  There is no CPU fallback.
 """
+import atexit
 import ctypes as C
+import sys
 
 import numpy as np
 
@@ -22,6 +24,15 @@ from ._lib import MIXED, PLAIN_FP64, CpgError
 
 __all__ = ["Context", "Geometry", "CpCase", "solve_cases", "topology", "read_tri", "panel_phi_inf", "dub_phi_inf",
            "panel_v_inf", "CpgError", "PLAIN_FP64", "MIXED"]
+
+_shutting_down = False
+
+
+@atexit.register
+def _mark_shutdown():
+    global _shutting_down
+    _shutting_down = True
+
 
 _PREC = {"fp64": PLAIN_FP64, "plain": PLAIN_FP64, PLAIN_FP64: PLAIN_FP64, "mixed": MIXED, MIXED: MIXED}
 
@@ -57,7 +68,17 @@ class Context:
     def synchronize(self):
         self.check(self.L.cpg_synchronize(self.h), "synchronize")
 
+    def prof_enable(self, on=True):
+        self.check(self.L.cpg_prof_enable(self.h, 1 if on else 0), "prof_enable")
+
+    def prof_read(self):
+        p = _lib.Prof()
+        self.check(self.L.cpg_prof_read(self.h, C.byref(p)), "prof_read")
+        return {name: (p.launches[i], p.ms[i]) for i, name in enumerate(_lib.PROF_CLASSES)}
+
     def __del__(self):
+        if _shutting_down or sys.is_finalizing():
+            return  # the CUDA runtime may already be unloaded
         try:
             self.L.cpg_destroy(self.h)
         except Exception:
@@ -103,6 +124,8 @@ class Geometry:
         return cls(*read_tri(path), ctx=ctx)
 
     def __del__(self):
+        if _shutting_down or sys.is_finalizing():
+            return
         try:
             self.ctx.L.cpg_geometry_destroy(self.h)
         except Exception:

@@ -26,7 +26,15 @@ class CpgError(RuntimeError):
 
 class GeometryInfo(C.Structure):
     _fields_ = [("n_body", C.c_int64), ("n_wake", C.c_int64), ("n_wakes", C.c_int64), ("n_wakelines", C.c_int64),
-                ("n_tip", C.c_int64), ("n_nodes", C.c_int64)]
+                ("n_tip", C.c_int64), ("n_nodes", C.c_int64), ("h2d_bytes", C.c_int64)]
+
+
+PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "bj_apply", "bj_setup",
+                "chtls", "post", "vector_ops"]
+
+
+class Prof(C.Structure):
+    _fields_ = [("launches", C.c_longlong * 10), ("ms", C.c_double * 10)]
 
 
 class Flow(C.Structure):
@@ -53,7 +61,7 @@ _lib = None
 EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg_synchronize",
            "cpg_geometry_create", "cpg_geometry_destroy", "cpg_geometry_info_get", "cpg_geometry_tables", "cpg_topology",
            "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
-           "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch"]
+           "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read"]
 
 
 def load():
@@ -87,5 +95,7 @@ def load():
     L.cpg_dub_phi_inf.argtypes = [vp, vp, vp, C.c_int64, vp]
     L.cpg_panel_v_inf.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
     L.cpg_compiled_arch.argtypes = []
+    L.cpg_prof_enable.argtypes = [vp, C.c_int]
+    L.cpg_prof_read.argtypes = [vp, C.POINTER(Prof)]
     _lib = L
     return L

@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_STRICT = ["assemble.cu", "post.cu"]   # FP64 panel math: no contraction
 CU_FAST = ["solve.cu"]
 CPP = ["mesh.cpp", "api.cpp"]
-HEADERS = ["common.cuh", "panel64.cuh", "assemble.h", "post.h", "mesh.h"]
+HEADERS = ["common.cuh", "panel64.cuh", "df.cuh", "assemble.h", "post.h", "mesh.h"]
 
 
 def _sources():

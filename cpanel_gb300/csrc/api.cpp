@@ -22,8 +22,17 @@ struct cpg_ctx {
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     std::string err;
-    // scratch for the batched single-evaluation operators is caller-owned
+    cpg::Prof* prof = nullptr;  // device-time accounting, when enabled
 };
+
+namespace {
+// installs the context's profiler for the calling thread during one API call
+struct ProfInstall {
+    cpg::Prof* saved;
+    explicit ProfInstall(cpg_ctx* c) : saved(cpg::g_prof) { cpg::g_prof = c ? c->prof : nullptr; }
+    ~ProfInstall() { cpg::g_prof = saved; }
+};
+}  // namespace
 
 namespace {
 
@@ -51,7 +60,7 @@ struct DevBuf {
 };
 
 constexpr double kPi = 3.14159265358979323846;
-constexpr int F_STRIDE_HOST = 12;  // FP32 far-field record, F_STRIDE in common.cuh
+constexpr int F_STRIDE_HOST = 16;  // double-float far-field record, F_STRIDE in common.cuh
 
 }  // namespace
 
@@ -63,9 +72,12 @@ struct cpg_geometry {
     cpg_ctx* ctx = nullptr;
     cpg::HostMesh H;
     DevBuf rec, frec, bez, clp, cli, tip, ts, wrec, widx, wcoef, tzst, tzln, tzpts, G, F3, F2, mode;
-    DevBuf A64, B64, A32, rb, count;
+    DevBuf A64, B64, A32, Alo, rb, count;
+    DevBuf bjperm, bjoff, bjdoff, bjinv, bjwork;
+    cpg::BlockJacobi bj;
     DevBuf work, post_work, cases, outs;
     bool have64 = false, have32 = false, post_ready = false;
+    int64_t h2d_bytes = 0;
     int64_t n_near64 = 0, n_near32 = 0;
     cpg::PostTables T;
     float ms_asm = 0;
@@ -87,11 +99,14 @@ int cuda_fail(cpg_ctx* c, cudaError_t e, const char* where) {
         if (_e != cudaSuccess) return cuda_fail(ctx, _e, where); \
     } while (0)
 
+thread_local int64_t t_h2d = 0;  // bytes uploaded by the current call
+
 template <typename T>
 cudaError_t upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s) {
     cudaError_t e = b.ensure(std::max<size_t>(1, v.size() * sizeof(T)));
     if (e != cudaSuccess) return e;
     if (v.empty()) return cudaSuccess;
+    t_h2d += (int64_t)(v.size() * sizeof(T));
     return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
 }
 
@@ -196,6 +211,7 @@ int cpg_create(cpg_ctx** out, int device) {
 
 void cpg_destroy(cpg_ctx* c) {
     if (!c) return;
+    delete c->prof;
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -239,18 +255,22 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
         return fail(ctx, CPG_E_BAD_MESH, "fewer than two body panels");
     }
     cudaStream_t s = ctx->stream;
-    // FP32 far-field records: c_hi, c_lo, n, area, longSide
+    t_h2d = 0;
+    // double-float far-field records: c, n, area as (hi, lo) FP32 pairs, longSide
     std::vector<float> fr(n * F_STRIDE_HOST, 0.f);
+    auto split = [](double v, float* hi, float* lo) {
+        *hi = (float)v;
+        *lo = (float)(v - (double)*hi);
+    };
     for (int64_t i = 0; i < n; i++) {
         const double* r = &H.body[i * cpg::PF_STRIDE];
+        float* o = &fr[i * F_STRIDE_HOST];
         for (int q = 0; q < 3; q++) {
-            float hi = (float)r[cpg::PF_C + q];
-            fr[i * F_STRIDE_HOST + q] = hi;
-            fr[i * F_STRIDE_HOST + 3 + q] = (float)(r[cpg::PF_C + q] - (double)hi);
-            fr[i * F_STRIDE_HOST + 6 + q] = (float)r[cpg::PF_N + q];
+            split(r[cpg::PF_C + q], o + q, o + 3 + q);
+            split(r[cpg::PF_N + q], o + 6 + q, o + 9 + q);
         }
-        fr[i * F_STRIDE_HOST + 9] = (float)r[cpg::PF_AREA];
-        fr[i * F_STRIDE_HOST + 10] = (float)r[cpg::PF_LONG];
+        split(r[cpg::PF_AREA], o + 12, o + 13);
+        o[14] = (float)r[cpg::PF_LONG];
     }
     cudaError_t e;
     if ((e = upload(g->rec, H.body, s)) != cudaSuccess || (e = upload(g->frec, fr, s)) != cudaSuccess ||
@@ -262,6 +282,29 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
         cpg_geometry_destroy(g);
         return cuda_fail(ctx, e, "geometry upload");
     }
+    {  // block-Jacobi layout
+        std::vector<int64_t> doff(H.bj_off.size(), 0);
+        int bsmax = 0;
+        for (size_t b = 0; b + 1 < H.bj_off.size(); b++) {
+            int64_t bs = H.bj_off[b + 1] - H.bj_off[b];
+            doff[b + 1] = doff[b] + bs * bs;
+            bsmax = std::max<int>(bsmax, (int)bs);
+        }
+        if ((e = upload(g->bjperm, H.bj_perm, s)) != cudaSuccess || (e = upload(g->bjoff, H.bj_off, s)) != cudaSuccess ||
+            (e = upload(g->bjdoff, doff, s)) != cudaSuccess ||
+            (e = g->bjinv.ensure(sizeof(float) * std::max<int64_t>(1, doff.back()))) != cudaSuccess ||
+            (e = g->bjwork.ensure(sizeof(float) * std::max<int64_t>(1, doff.back()))) != cudaSuccess) {
+            cpg_geometry_destroy(g);
+            return cuda_fail(ctx, e, "preconditioner tables");
+        }
+        g->bj.perm = g->bjperm.as<int32_t>();
+        g->bj.off = g->bjoff.as<int32_t>();
+        g->bj.doff = g->bjdoff.as<int64_t>();
+        g->bj.Dinv = g->bjinv.as<float>();
+        g->bj.nb = (int)H.bj_off.size() - 1;
+        g->bj.bsmax = bsmax;
+    }
+    g->h2d_bytes = t_h2d;
     *out = g;
     return CPG_OK;
 }
@@ -270,8 +313,8 @@ void cpg_geometry_destroy(cpg_geometry* g) {
     if (!g) return;
     DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
                       &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
-                      &g->B64, &g->A32, &g->rb, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
-    if (g->ctx && g->ctx->stream) cudaStreamSynchronize(g->ctx->stream);
+                      &g->B64, &g->A32, &g->Alo, &g->rb, &g->bjperm, &g->bjoff, &g->bjdoff, &g->bjinv, &g->bjwork, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
+    // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
     delete g;
 }
@@ -284,6 +327,7 @@ int cpg_geometry_info_get(const cpg_geometry* g, cpg_geometry_info* o) {
     o->n_wakelines = g->H.n_lines;
     o->n_tip = g->H.n_tip;
     o->n_nodes = g->H.n_nodes;
+    o->h2d_bytes = g->h2d_bytes;
     return CPG_OK;
 }
 
@@ -347,6 +391,7 @@ int cpg_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, cons
 int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
     if (!g) return CPG_E_INVALID;
     cpg_ctx* ctx = g->ctx;
+    ProfInstall pi(ctx);
     cudaStream_t s = ctx->stream;
     int64_t n = g->H.n_body;
     size_t nn = (size_t)n * n;
@@ -365,11 +410,14 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
         g->have64 = true;
     } else if (precision == CPG_MIXED) {
         CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
+        CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
         CK(g->rb.ensure(sizeof(double) * 3 * n), "alloc rhs basis");
         CK(cpg::launch_assemble_mixed(g->rec.as<double>(), g->frec.as<float>(), n, g->wrec.as<double>(),
                                       g->widx.as<int32_t>(), g->wcoef.as<double>(), g->H.n_wake,
-                                      g->A32.as<float>(), g->rb.as<double>(), g->count.as<unsigned long long>(), s),
+                                      g->A32.as<float>(), g->Alo.as<float>(), g->rb.as<double>(),
+                                      g->count.as<unsigned long long>(), s),
            "assembly (mixed)");
+        CK(cpg::bj_setup(g->A32.as<float>(), n, g->bj, g->bjwork.as<float>(), s), "block-Jacobi setup");
         g->have32 = true;
     } else {
         return fail(ctx, CPG_E_INVALID, "unknown precision");
@@ -422,6 +470,7 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
                     const cpg_case_out* out, cpg_solve_stats* stats) {
     if (!g || !flows || !refs || k <= 0) return CPG_E_INVALID;
     cpg_ctx* ctx = g->ctx;
+    ProfInstall pi(ctx);
     if (precision != CPG_PLAIN_FP64 && precision != CPG_MIXED) return fail(ctx, CPG_E_INVALID, "unknown precision");
     if (precision == CPG_MIXED && k > 4096) return fail(ctx, CPG_E_INVALID, "too many cases");
     cudaStream_t s = ctx->stream;
@@ -466,7 +515,7 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
         size_t wb = cpg::solve_mixed_work_bytes(n, k);
         CK(g->work.ensure(wb), "alloc solver workspace");
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
-        CK(cpg::solve_mixed(g->A32.as<float>(), n, k, rhs, mu, g->work.p, 1e-10, 1e-5, 12, 1000, &st, s),
+        CK(cpg::solve_mixed(g->A32.as<float>(), g->Alo.as<float>(), &g->bj, n, k, rhs, mu, g->work.p, 1e-10, 1e-5, 12, 1000, &st, s),
            "refined solve (mixed)");
     }
     CK(cudaEventRecord(e1, s), "event");
@@ -540,6 +589,37 @@ int cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_
     if (!ctx || m < 0 || (m > 0 && (!verts || !poi || !vs || !vd))) return fail(ctx, CPG_E_INVALID, "bad argument");
     CK(cpg::launch_v_batch(verts, poi, m, vs, vd, ctx->stream), "panelVInf");
     CK(cudaStreamSynchronize(ctx->stream), "panelVInf");
+    return CPG_OK;
+}
+
+int cpg_prof_enable(cpg_ctx* ctx, int on) {
+    if (!ctx) return CPG_E_INVALID;
+    if (on) {
+        if (!ctx->prof) ctx->prof = new (std::nothrow) cpg::Prof();
+        if (!ctx->prof) return CPG_E_OOM;
+        CK(cudaStreamSynchronize(ctx->stream), "profiler");
+        ctx->prof->reset();
+    } else {
+        CK(cudaStreamSynchronize(ctx->stream), "profiler");
+        delete ctx->prof;
+        ctx->prof = nullptr;
+    }
+    return CPG_OK;
+}
+
+int cpg_prof_read(cpg_ctx* ctx, cpg_prof* out) {
+    if (!ctx || !out) return CPG_E_INVALID;
+    for (int c = 0; c < CPG_PROF_NCLS; c++) {
+        out->launches[c] = 0;
+        out->ms[c] = 0;
+    }
+    if (!ctx->prof) return CPG_OK;
+    CK(cudaStreamSynchronize(ctx->stream), "profiler");
+    ctx->prof->collect();
+    for (int c = 0; c < CPG_PROF_NCLS && c < cpg::Prof::NCLS; c++) {
+        out->launches[c] = ctx->prof->launches[c];
+        out->ms[c] = ctx->prof->ms[c];
+    }
     return CPG_OK;
 }
 

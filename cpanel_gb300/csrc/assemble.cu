@@ -6,6 +6,7 @@
 // source panels, staged 32 at a time in shared memory; each store instruction of
 // a warp writes 32 consecutive rows of one column.
 #include "assemble.h"
+#include "df.cuh"
 #include "panel64.cuh"
 
 namespace {
@@ -51,29 +52,29 @@ __global__ void __launch_bounds__(TI) k_assemble_fp64(const double* __restrict__
     }
 }
 
-// Mixed: FP32 far field, FP64 near field (the reference's own near set,
-// |pjk| <= 5 longSide), A stored as FP32; the source-influence right-hand-side
-// basis rb[c*n+i] = sum_j B(i,j) * n_j[c] is accumulated instead of storing B.
+// Mixed: double-float far field, FP64 near field (the reference's own near set,
+// |pjk| <= 5 longSide).  A is stored as two FP32 matrices, hi and lo, whose sum
+// carries about 44 bits; the Krylov iterations read hi only, the refinement
+// residual reads both.  Instead of storing B, the source right-hand-side basis
+// rb[c*n+i] = sum_j B(i,j) * n_j[c] is accumulated (double-float per tile, FP64
+// across tiles and for near pairs).
 __global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict__ rec, const float* __restrict__ frec,
                                                        int64_t n, int64_t jchunk, float* __restrict__ A32,
-                                                       double* __restrict__ rb,
+                                                       float* __restrict__ Alo, double* __restrict__ rb,
                                                        unsigned long long* __restrict__ near_count) {
     __shared__ double s_rec[TJ * R_STRIDE];
     __shared__ float s_f[TJ * F_STRIDE];
     int64_t i = (int64_t)blockIdx.x * TI + threadIdx.x;
     bool act = i < n;
     dv3 poi = act ? ld3(rec + i * R_STRIDE + R_C) : mk3(0, 0, 0);
-    float ch[3] = {0, 0, 0}, cl[3] = {0, 0, 0};
-    if (act) {
-        for (int c = 0; c < 3; c++) {
-            ch[c] = frec[i * F_STRIDE + F_CHI + c];
-            cl[c] = frec[i * F_STRIDE + F_CLO + c];
-        }
-    }
+    df32 ci[3] = {{0, 0}, {0, 0}, {0, 0}};
+    if (act)
+        for (int c = 0; c < 3; c++) ci[c] = df32{frec[i * F_STRIDE + F_CHI + c], frec[i * F_STRIDE + F_CLO + c]};
     int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
     double acc64[3] = {0, 0, 0};
     unsigned nnear = 0;
-    const float inv4pi = (float)(1.0 / CPG_FOUR_PI);
+    const double q4 = 1.0 / CPG_FOUR_PI;
+    const df32 inv4pi = df32{(float)q4, (float)(q4 - (double)(float)q4)};
     for (int64_t j0 = jb; j0 < je; j0 += TJ) {
         __syncthreads();
         load_tile(s_rec, rec, j0, n);
@@ -84,49 +85,53 @@ __global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict_
         __syncthreads();
         int cnt = (int)min((int64_t)TJ, je - j0);
         if (!act) continue;
-        float acc32[3] = {0.f, 0.f, 0.f};
+        df32 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
         for (int t = 0; t < cnt; t++) {
             int64_t j = j0 + t;
             const float* f = s_f + t * F_STRIDE;
-            float dx = __fadd_rn(__fsub_rn(ch[0], f[F_CHI + 0]), __fsub_rn(cl[0], f[F_CLO + 0]));
-            float dy = __fadd_rn(__fsub_rn(ch[1], f[F_CHI + 1]), __fsub_rn(cl[1], f[F_CLO + 1]));
-            float dz = __fadd_rn(__fsub_rn(ch[2], f[F_CHI + 2]), __fsub_rn(cl[2], f[F_CLO + 2]));
-            float r2 = __fmaf_rn(dz, dz, __fmaf_rn(dy, dy, __fmul_rn(dx, dx)));
+            df32 d[3];
+#pragma unroll
+            for (int c = 0; c < 3; c++) d[c] = df_sub(ci[c], df32{f[F_CHI + c], f[F_CLO + c]});
+            float r2f = __fmaf_rn(d[2].hi, d[2].hi, __fmaf_rn(d[1].hi, d[1].hi, __fmul_rn(d[0].hi, d[0].hi)));
             float L = f[F_LONG];
             float lim = __fmul_rn(25.f, __fmul_rn(L, L));
             bool far;
-            if (r2 > __fmul_rn(lim, 1.00001f))
+            if (r2f > __fmul_rn(lim, 1.00001f))
                 far = true;
-            else if (r2 < __fmul_rn(lim, 0.99999f))
+            else if (r2f < __fmul_rn(lim, 0.99999f))
                 far = false;
             else {  // guard band: decide exactly as the FP64 reference does
                 const double* r = s_rec + t * R_STRIDE;
-                double d = norm3(poi - ld3(r + R_C));
-                far = d / r[R_LONG] > 5;
+                double dd = norm3(poi - ld3(r + R_C));
+                far = dd / r[R_LONG] > 5;
             }
             if (far) {
-                float rinv = rsqrtf(r2);
-                float src = __fmul_rn(__fmul_rn(f[F_AREA], rinv), inv4pi);
-                float pn = __fmaf_rn(dz, f[F_N + 2], __fmaf_rn(dy, f[F_N + 1], __fmul_rn(dx, f[F_N + 0])));
-                float dub = __fmul_rn(__fmul_rn(pn, __fmul_rn(rinv, rinv)), src);
-                A32[j * n + i] = dub;
-                acc32[0] = __fmaf_rn(src, f[F_N + 0], acc32[0]);
-                acc32[1] = __fmaf_rn(src, f[F_N + 1], acc32[1]);
-                acc32[2] = __fmaf_rn(src, f[F_N + 2], acc32[2]);
+                // pntSrcPhi / pntDubPhi (CPanel/bodyPanel.cpp:392-395, panel.cpp:737-740) in double-float
+                df32 r2 = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
+                df32 rinv = df_rsqrt(r2);
+                df32 src = df_mul(df_mul(df32{f[F_AHI], f[F_ALO]}, rinv), inv4pi);
+                df32 nv[3] = {{f[F_NHI], f[F_NLO]}, {f[F_NHI + 1], f[F_NLO + 1]}, {f[F_NHI + 2], f[F_NLO + 2]}};
+                df32 pn = df_add(df_add(df_mul(d[0], nv[0]), df_mul(d[1], nv[1])), df_mul(d[2], nv[2]));
+                df32 dub = df_mul(df_mul(pn, df_mul(rinv, rinv)), src);
+                A32[j * n + i] = dub.hi;
+                Alo[j * n + i] = dub.lo;
+#pragma unroll
+                for (int c = 0; c < 3; c++) acc[c] = df_add(acc[c], df_mul(src, nv[c]));
             } else {
                 double src = 0, dub = 0;
                 const double* r = s_rec + t * R_STRIDE;
                 panel_phi_inf(r, poi, src, dub);
                 nnear++;
-                A32[j * n + i] = (float)dub;
+                float hi = (float)dub;
+                A32[j * n + i] = hi;
+                Alo[j * n + i] = (float)(dub - (double)hi);  // FP64 value = hi + lo to 2^-48
                 acc64[0] += src * r[R_N + 0];
                 acc64[1] += src * r[R_N + 1];
                 acc64[2] += src * r[R_N + 2];
             }
         }
-        acc64[0] += (double)acc32[0];
-        acc64[1] += (double)acc32[1];
-        acc64[2] += (double)acc32[2];
+#pragma unroll
+        for (int c = 0; c < 3; c++) acc64[c] += df_to_double(acc[c]);
     }
     if (act) {
         atomicAdd(rb + i, acc64[0]);
@@ -158,6 +163,28 @@ __global__ void k_wake_columns(const double* __restrict__ rec, const double* __r
         A[c1 * n + i] = (T)((double)A[c1 * n + i] + infl * (c - 1));
         A[c2 * n + i] = (T)((double)A[c2 * n + i] + infl * c);
         A[c3 * n + i] = (T)((double)A[c3 * n + i] - infl * c);
+    }
+}
+
+// Wake columns for the split (hi + lo) FP32 storage of the mixed path.
+__global__ void k_wake_columns_split(const double* __restrict__ rec, const double* __restrict__ wrec,
+                                     const int32_t* __restrict__ widx, const double* __restrict__ wcoef, int64_t n,
+                                     int64_t nw, float* __restrict__ Ahi, float* __restrict__ Alo) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    dv3 poi = ld3(rec + i * R_STRIDE + R_C);
+    for (int64_t j = 0; j < nw; j++) {
+        double infl = dub_phi_inf(wrec + j * R_STRIDE, poi);
+        double c = wcoef[j];
+        const int32_t* ix = widx + 4 * j;
+        const double add[4] = {infl * (1 - c), infl * (c - 1), infl * c, -(infl * c)};
+        for (int q = 0; q < 4; q++) {
+            int64_t o = (int64_t)ix[q] * n + i;
+            double v = ((double)Ahi[o] + (double)Alo[o]) + add[q];
+            float hi = (float)v;
+            Ahi[o] = hi;
+            Alo[o] = (float)(v - (double)hi);
+        }
     }
 }
 
@@ -255,20 +282,32 @@ cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wre
                                  unsigned long long* near_count, cudaStream_t s) {
     int64_t ch = chunk_for(n);
     dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
-    k_assemble_fp64<<<grid, TI, 0, s>>>(rec, n, ch, A, B, near_count);
-    if (nw > 0) k_wake_columns<double><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A);
+    {
+        ProfScope ps(Prof::ASSEMBLE, s);
+        k_assemble_fp64<<<grid, TI, 0, s>>>(rec, n, ch, A, B, near_count);
+    }
+    if (nw > 0) {
+        ProfScope ps(Prof::WAKE_COLUMNS, s);
+        k_wake_columns<double><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A);
+    }
     return cudaGetLastError();
 }
 
 cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
-                                  const int32_t* widx, const double* wcoef, int64_t nw, float* A32, double* rb,
-                                  unsigned long long* near_count, cudaStream_t s) {
+                                  const int32_t* widx, const double* wcoef, int64_t nw, float* A32, float* Alo,
+                                  double* rb, unsigned long long* near_count, cudaStream_t s) {
     cudaError_t e = cudaMemsetAsync(rb, 0, sizeof(double) * 3 * n, s);
     if (e != cudaSuccess) return e;
     int64_t ch = chunk_for(n);
     dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
-    k_assemble_mixed<<<grid, TI, 0, s>>>(rec, frec, n, ch, A32, rb, near_count);
-    if (nw > 0) k_wake_columns<float><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A32);
+    {
+        ProfScope ps(Prof::ASSEMBLE, s);
+        k_assemble_mixed<<<grid, TI, 0, s>>>(rec, frec, n, ch, A32, Alo, rb, near_count);
+    }
+    if (nw > 0) {
+        ProfScope ps(Prof::WAKE_COLUMNS, s);
+        k_wake_columns_split<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A32, Alo);
+    }
     return cudaGetLastError();
 }
 

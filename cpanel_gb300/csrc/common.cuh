@@ -24,8 +24,8 @@ __device__ __forceinline__ dv3 ld3(const double* p) { return dv3{p[0], p[1], p[2
 // Packed panel record layout (must match cpg::PanelField in mesh.h).
 enum { R_V0 = 0, R_V1 = 3, R_V2 = 6, R_C = 9, R_N = 12, R_L = 15, R_M = 18, R_AREA = 21, R_LONG = 22, R_STRIDE = 24 };
 
-// Per-panel FP32 record used by the mixed far field:
-// [c_hi(3) c_lo(3) n(3) area longSide pad]
-enum { F_CHI = 0, F_CLO = 3, F_N = 6, F_AREA = 9, F_LONG = 10, F_STRIDE = 12 };
+// Per-panel double-float record used by the mixed far field (FP32 pairs):
+// [c_hi(3) c_lo(3) n_hi(3) n_lo(3) area_hi area_lo longSide pad]
+enum { F_CHI = 0, F_CLO = 3, F_NHI = 6, F_NLO = 9, F_AHI = 12, F_ALO = 13, F_LONG = 14, F_STRIDE = 16 };
 
 #define CPG_CUDA_OK(x) ((x) == cudaSuccess)

@@ -7,6 +7,7 @@
 //     (wake::trefftzPlane / Vradial / wakeStrength, CPanel/wake.cpp:146-188,478-597).
 #include <vector>
 
+#include "assemble.h"
 #include "common.cuh"
 #include "post.h"
 
@@ -78,6 +79,15 @@ constexpr int WPB = 2;        // warps (panels) per block
 constexpr int NF = cpg::kClMax - 1;
 constexpr int TM = 19;
 
+// x^e for e in 0..3 as a left-to-right product (matches the CPU restatement bit
+// for bit; the CHTLS normal equations are too ill-conditioned on clustered
+// trailing edges to tolerate a different rounding of the monomials)
+__device__ __forceinline__ double powi(double x, int e) {
+    double r = 1;
+    for (int k = 0; k < e; k++) r = k == 0 ? x : r * x;
+    return r;
+}
+
 __device__ __forceinline__ int ifact(int i) {
     int o = 1;
     for (int k = 2; k <= i; k++) o *= k;
@@ -123,7 +133,7 @@ __device__ bool chtls_warp(WarpSmem& S, int N, int order, int nf, bool withB, do
             double fact = 1;
             for (int d = 0; d < N; d++) fact /= ifact(c_ms[N - 2][order][k][d]);
             double prod = 1;
-            for (int d = 0; d < N; d++) prod *= pow(S.dX[lane][d], (double)c_ms[N - 2][order][k][d]);
+            for (int d = 0; d < N; d++) prod *= powi(S.dX[lane][d], c_ms[N - 2][order][k][d]);
             S.A[lane][k] = fact * prod;
             if (withB) {
                 double asum = 0;
@@ -133,7 +143,7 @@ __device__ bool chtls_warp(WarpSmem& S, int N, int order, int nf, bool withB, do
                         double pr = 1;
                         for (int d = 0; d < N; d++) {
                             int e = c_ms[N - 2][order][k][d] - (d == a ? 1 : 0);
-                            pr *= pow(S.dX[lane][d], (double)e);
+                            pr *= powi(S.dX[lane][d], e);
                         }
                         asum += S.Vb[lane][a] * ma * pr;
                     }
@@ -158,9 +168,9 @@ __device__ bool chtls_warp(WarpSmem& S, int N, int order, int nf, bool withB, do
     __syncwarp();
     // Householder QR (Eigen::HouseholderQR, unblocked) and Q^T R
     for (int k = 0; k < t; k++) {
+        // sequential tail norm, same order as the CPU restatement (every lane alike)
         double part = 0;
-        for (int i = k + 1 + lane; i < t; i += 32) part += S.M[i][k] * S.M[i][k];
-        for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+        for (int i = k + 1; i < t; i++) part += S.M[i][k] * S.M[i][k];
         double c0 = S.M[k][k];
         double tau, beta;
         bool zero = part <= 2.2250738585072014e-308;
@@ -477,6 +487,7 @@ cudaError_t launch_widen(const float* a, double* b, int64_t m, cudaStream_t s) {
 cudaError_t launch_chtls_weights(const PostTables& t, cudaStream_t s) {
     if (!g_tables_ready) build_tables();
     if (t.n <= 0) return cudaSuccess;
+    ProfScope ps(Prof::CHTLS, s);
     k_chtls<<<(unsigned)((t.n + WPB - 1) / WPB), 32 * WPB, 0, s>>>(t);
     return cudaGetLastError();
 }
@@ -492,6 +503,7 @@ cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs, const
     double* fpart = (double*)work;
     double* tz = fpart + (size_t)k * nb * 6;
     dim3 grid((unsigned)nb, (unsigned)k);
+    ProfScope ps(Prof::POST, s);
     k_velocity<<<grid, PT, 0, s>>>(t, k, cs, mu, phi, vel, cp, fpart);
     k_forces_finish<<<(k + 31) / 32, 32, 0, s>>>(fpart, (int)nb, k, cs, forces);
     if (t.n_wakes > 0) k_trefftz<<<k, 256, 0, s>>>(t, k, cs, mu, wake_mu, tz, trefftz);

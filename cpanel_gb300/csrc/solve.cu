@@ -78,7 +78,8 @@ __global__ void k_mv_reduce(const TACC* __restrict__ P, int nchunk, int KB, int 
 
 // Double-float residual chunks: exact FP32 products of A32 with x = xh + xl.
 template <int KB>
-__global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict__ A, int64_t n, int64_t jchunk,
+__global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict__ A, const float* __restrict__ Alo,
+                                                         int64_t n, int64_t jchunk,
                                                          const double* __restrict__ X, int col0, int kb,
                                                          double* __restrict__ P) {
     __shared__ float sh[MV_JT][KB], sl[MV_JT][KB];
@@ -101,16 +102,19 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
         if (i < n) {
             int cnt = (int)min((int64_t)MV_JT, je - j0);
             const float* Ap = A + j0 * n + i;
+            const float* Lp = Alo + j0 * n + i;
             float hi[KB], lo[KB];
 #pragma unroll
             for (int c = 0; c < KB; c++) hi[c] = lo[c] = 0.f;
             for (int t = 0; t < cnt; t++) {
                 float a = Ap[(int64_t)t * n];
+                float al = Lp[(int64_t)t * n];
 #pragma unroll
                 for (int c = 0; c < KB; c++) {
                     float p = __fmul_rn(a, sh[t][c]);
                     float e = __fmaf_rn(a, sh[t][c], -p);     // exact product error
                     e = __fmaf_rn(a, sl[t][c], e);
+                    e = __fmaf_rn(al, sh[t][c], e);
                     float s = __fadd_rn(hi[c], p);           // TwoSum(hi, p)
                     float bb = __fsub_rn(s, hi[c]);
                     float err = __fadd_rn(__fsub_rn(hi[c], __fsub_rn(s, bb)), __fsub_rn(p, bb));
@@ -243,6 +247,122 @@ __global__ void k_add_to(double* __restrict__ x, const float* __restrict__ d, in
 
 inline unsigned nblk(int64_t m, int b = 256) { return (unsigned)((m + b - 1) / b); }
 
+// ---- block-Jacobi: gather, Gauss-Jordan inverse (FP32, partial pivoting), apply
+constexpr int BJ_THREADS = 512;
+
+__global__ void __launch_bounds__(BJ_THREADS) k_bj_invert(const float* __restrict__ A, int64_t n,
+                                                          const int32_t* __restrict__ perm, const int32_t* __restrict__ off,
+                                                          const int64_t* __restrict__ doff, float* __restrict__ W,
+                                                          float* __restrict__ Dinv) {
+    __shared__ float fr[512];
+    __shared__ float rv[BJ_THREADS];
+    __shared__ int ri[BJ_THREADS];
+    const int b = blockIdx.x;
+    const int o = off[b], bs = off[b + 1] - o;
+    float* D = W + doff[b];      // row-major work copy D[r*bs + c]
+    float* I = Dinv + doff[b];   // row-major during elimination, transposed at the end
+    for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) {
+        int r = (int)(t / bs), c = (int)(t % bs);
+        D[t] = A[(int64_t)perm[o + c] * n + perm[o + r]];
+        I[t] = r == c ? 1.f : 0.f;
+    }
+    __syncthreads();
+    for (int k = 0; k < bs; k++) {
+        float best = -1.f;
+        int bi = k;
+        for (int r = k + threadIdx.x; r < bs; r += BJ_THREADS) {
+            float v = fabsf(D[(int64_t)r * bs + k]);
+            if (v > best) {
+                best = v;
+                bi = r;
+            }
+        }
+        rv[threadIdx.x] = best;
+        ri[threadIdx.x] = bi;
+        __syncthreads();
+        for (int st = BJ_THREADS / 2; st > 0; st >>= 1) {
+            if (threadIdx.x < st) {
+                float a = rv[threadIdx.x], c2 = rv[threadIdx.x + st];
+                if (c2 > a || (c2 == a && ri[threadIdx.x + st] < ri[threadIdx.x])) {
+                    rv[threadIdx.x] = c2;
+                    ri[threadIdx.x] = ri[threadIdx.x + st];
+                }
+            }
+            __syncthreads();
+        }
+        int p = ri[0];
+        __syncthreads();
+        if (p != k)
+            for (int c = threadIdx.x; c < bs; c += BJ_THREADS) {
+                float t1 = D[(int64_t)k * bs + c];
+                D[(int64_t)k * bs + c] = D[(int64_t)p * bs + c];
+                D[(int64_t)p * bs + c] = t1;
+                float t2 = I[(int64_t)k * bs + c];
+                I[(int64_t)k * bs + c] = I[(int64_t)p * bs + c];
+                I[(int64_t)p * bs + c] = t2;
+            }
+        __syncthreads();
+        float piv = D[(int64_t)k * bs + k];
+        float inv = piv != 0.f ? 1.f / piv : 1.f;
+        __syncthreads();
+        for (int c = threadIdx.x; c < bs; c += BJ_THREADS) {
+            D[(int64_t)k * bs + c] *= inv;
+            I[(int64_t)k * bs + c] *= inv;
+        }
+        for (int r = threadIdx.x; r < bs; r += BJ_THREADS) fr[r] = r == k ? 0.f : D[(int64_t)r * bs + k];
+        __syncthreads();
+        for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) {
+            int r = (int)(t / bs), c = (int)(t % bs);
+            float f = fr[r];
+            if (f != 0.f) {
+                D[t] = __fmaf_rn(-f, D[(int64_t)k * bs + c], D[t]);
+                I[t] = __fmaf_rn(-f, I[(int64_t)k * bs + c], I[t]);
+            }
+        }
+        __syncthreads();
+    }
+    // transpose I in place into column-major via the work buffer
+    for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) D[t] = I[t];
+    __syncthreads();
+    for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) {
+        int r = (int)(t / bs), c = (int)(t % bs);
+        I[(int64_t)c * bs + r] = D[t];
+    }
+}
+
+// y[c*n + perm[o+r]] = sum_q Dinv_b[q*bs + r] * x[c*n + perm[o+q]]   (RHS in chunks of 8)
+template <typename T>
+__global__ void __launch_bounds__(256) k_bj_apply(const float* __restrict__ Dinv, const int32_t* __restrict__ perm,
+                                                  const int32_t* __restrict__ off, const int64_t* __restrict__ doff,
+                                                  int64_t n, int k, const T* __restrict__ x, T* __restrict__ y,
+                                                  const double* __restrict__ sc) {
+    __shared__ float xs[512][8];
+    const int b = blockIdx.x;
+    const int o = off[b], bs = off[b + 1] - o;
+    const float* Di = Dinv + doff[b];
+    for (int c0 = 0; c0 < k; c0 += 8) {
+        int kc = min(8, k - c0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < bs * 8; t += 256) {
+            int q = t / 8, c = t % 8;
+            xs[q][c] = c < kc ? (float)x[(int64_t)(c0 + c) * n + perm[o + q]] : 0.f;
+        }
+        __syncthreads();
+        for (int r = threadIdx.x; r < bs; r += 256) {
+            float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+            for (int q = 0; q < bs; q++) {
+                float d = Di[(int64_t)q * bs + r];
+#pragma unroll
+                for (int c = 0; c < 8; c++) acc[c] = __fmaf_rn(d, xs[q][c], acc[c]);
+            }
+            for (int c = 0; c < kc; c++) {
+                if (sc && sc[4 * (c0 + c) + 3] == 0) continue;
+                y[(int64_t)(c0 + c) * n + perm[o + r]] = (T)acc[c];
+            }
+        }
+    }
+}
+
 // ------------------------------------------------------------------ drivers
 struct Arena {
     char* p;
@@ -263,6 +383,7 @@ cudaError_t mv_dispatch(const TA* A, int64_t n, int k, const TX* X, void* Y, dou
 template <typename TA, typename TX, typename TACC, int KB>
 void mv_launch(const TA* A, int64_t n, int64_t ch, const TX* X, int col0, int kb, TACC* P, cudaStream_t s) {
     dim3 grid(nblk(n, MV_THREADS), (unsigned)((n + ch - 1) / ch));
+    cpg::ProfScope ps(sizeof(TA) == 4 ? cpg::Prof::MATVEC_FP32 : cpg::Prof::MATVEC_FP64, s);
     k_mv<TA, TX, TACC, KB><<<grid, MV_THREADS, 0, s>>>(A, n, ch, X, col0, kb, P);
 }
 
@@ -289,25 +410,27 @@ cudaError_t matmul(const TA* A, int64_t n, int k, const TX* X, TY* Y, double alp
 }
 
 template <int KB>
-void resid_launch(const float* A, int64_t n, int64_t ch, const double* X, int col0, int kb, double* P, cudaStream_t s) {
+void resid_launch(const float* A, const float* Alo, int64_t n, int64_t ch, const double* X, int col0, int kb, double* P,
+                  cudaStream_t s) {
     dim3 grid(nblk(n, MV_THREADS), (unsigned)((n + ch - 1) / ch));
-    k_resid_df<KB><<<grid, MV_THREADS, 0, s>>>(A, n, ch, X, col0, kb, P);
+    cpg::ProfScope ps(cpg::Prof::RESIDUAL, s);
+    k_resid_df<KB><<<grid, MV_THREADS, 0, s>>>(A, Alo, n, ch, X, col0, kb, P);
 }
 
-// r = b - A32 x (x FP64), products exact.
-cudaError_t residual_df(const float* A, int64_t n, int k, const double* x, const double* b, double* r, double* P,
-                        cudaStream_t s) {
+// r = b - (A32 + Alo) x (x FP64), leading products exact.
+cudaError_t residual_df(const float* A, const float* Alo, int64_t n, int k, const double* x, const double* b, double* r,
+                        double* P, cudaStream_t s) {
     int64_t ch = mv_chunk(n, 152 * 8);
     int nchunk = (int)((n + ch - 1) / ch);
     for (int col0 = 0; col0 < k; col0 += 17) {
         int kb = std::min(17, k - col0);
         int KB;
-        if (kb <= 1) { KB = 1; resid_launch<1>(A, n, ch, x, col0, kb, P, s); }
-        else if (kb <= 2) { KB = 2; resid_launch<2>(A, n, ch, x, col0, kb, P, s); }
-        else if (kb <= 4) { KB = 4; resid_launch<4>(A, n, ch, x, col0, kb, P, s); }
-        else if (kb <= 8) { KB = 8; resid_launch<8>(A, n, ch, x, col0, kb, P, s); }
-        else if (kb <= 16) { KB = 16; resid_launch<16>(A, n, ch, x, col0, kb, P, s); }
-        else { KB = 17; resid_launch<17>(A, n, ch, x, col0, kb, P, s); }
+        if (kb <= 1) { KB = 1; resid_launch<1>(A, Alo, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 2) { KB = 2; resid_launch<2>(A, Alo, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 4) { KB = 4; resid_launch<4>(A, Alo, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 8) { KB = 8; resid_launch<8>(A, Alo, n, ch, x, col0, kb, P, s); }
+        else if (kb <= 16) { KB = 16; resid_launch<16>(A, Alo, n, ch, x, col0, kb, P, s); }
+        else { KB = 17; resid_launch<17>(A, Alo, n, ch, x, col0, kb, P, s); }
         k_mv_reduce<double, double><<<nblk((int64_t)kb * n), 256, 0, s>>>(P, nchunk, KB, kb, n, col0, -1.0, b, r);
     }
     return cudaGetLastError();
@@ -328,7 +451,7 @@ cudaError_t dots(const T* U0, const T* V0, const T* U1, const T* V1, int64_t n, 
 // DiagonalPreconditioner, restart when r drifts orthogonal to r0).
 template <typename T, typename TA, typename TACC>
 cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena& ar, double tol, int64_t maxIters,
-                     int kbmax, cpg::SolveStats* st, cudaStream_t s, bool quiet_restart = false) {
+                     int kbmax, cpg::SolveStats* st, cudaStream_t s, const cpg::BlockJacobi* bj = nullptr) {
     const size_t kn = (size_t)k * n;
     T *r = ar.take<T>(kn), *r0 = ar.take<T>(kn), *p = ar.take<T>(kn), *v = ar.take<T>(kn), *y = ar.take<T>(kn),
       *z = ar.take<T>(kn), *sv = ar.take<T>(kn), *tv = ar.take<T>(kn), *invd = ar.take<T>(n);
@@ -407,6 +530,10 @@ cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena
         }
         cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
         k_upd_p<T><<<nblk(kn), 256, 0, s>>>(r, v, p, y, invd, sc, n, k);
+        if (bj) {
+            cpg::ProfScope ps(cpg::Prof::BJ_APPLY, s);
+            k_bj_apply<T><<<bj->nb, 256, 0, s>>>(bj->Dinv, bj->perm, bj->off, bj->doff, n, k, p, y, sc);
+        }
         matmul<TA, T, TACC, T>(A, n, k, y, v, 1.0, nullptr, P, kbmax, s);
         if ((e = dots<T>(r0, v, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
         for (int c = 0; c < k; c++)
@@ -416,6 +543,10 @@ cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena
             }
         cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
         k_upd_s<T><<<nblk(kn), 256, 0, s>>>(r, v, sv, z, invd, sc, n, k);
+        if (bj) {
+            cpg::ProfScope ps(cpg::Prof::BJ_APPLY, s);
+            k_bj_apply<T><<<bj->nb, 256, 0, s>>>(bj->Dinv, bj->perm, bj->off, bj->doff, n, k, sv, z, sc);
+        }
         matmul<TA, T, TACC, T>(A, n, k, z, tv, 1.0, nullptr, P, kbmax, s);
         if ((e = dots<T>(tv, tv, tv, sv, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
         for (int c = 0; c < k; c++)
@@ -438,13 +569,61 @@ cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena
             st->residual_max = std::max(st->residual_max, err);
         }
     }
-    (void)quiet_restart;
     return cudaGetLastError();
 }
 
 }  // namespace
 
 namespace cpg {
+
+thread_local Prof* g_prof = nullptr;
+
+cudaEvent_t Prof::get() {
+    if (!pool.empty()) {
+        cudaEvent_t e = pool.back();
+        pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+void Prof::begin(int cls, cudaStream_t s) {
+    Pair p{get(), nullptr, cls};
+    cudaEventRecord(p.a, s);
+    pending.push_back(p);
+}
+void Prof::end(cudaStream_t s) {
+    Pair& p = pending.back();
+    p.b = get();
+    cudaEventRecord(p.b, s);
+}
+void Prof::collect() {
+    for (Pair& p : pending) {
+        float t = 0;
+        if (p.b && cudaEventElapsedTime(&t, p.a, p.b) == cudaSuccess) {
+            ms[p.cls] += t;
+            launches[p.cls]++;
+        }
+        pool.push_back(p.a);
+        if (p.b) pool.push_back(p.b);
+    }
+    pending.clear();
+}
+void Prof::reset() {
+    collect();
+    for (int c = 0; c < NCLS; c++) {
+        ms[c] = 0;
+        launches[c] = 0;
+    }
+}
+Prof::~Prof() {
+    for (Pair& p : pending) {
+        pool.push_back(p.a);
+        if (p.b) pool.push_back(p.b);
+    }
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+}
 
 size_t solve_fp64_work_bytes(int64_t n, int k) {
     int64_t ch = mv_chunk(n, 152 * 8);
@@ -471,10 +650,17 @@ size_t solve_mixed_work_bytes(int64_t n, int k) {
     size_t kn = (size_t)k * n;
     return sizeof(float) * (9 * kn + n + nchunk * 32 * (size_t)n) +
            sizeof(double) * (kn /*Ax*/ + 2 * k * 64 + 2 * k + 4 * k + 2 * kn /*r64, d64*/ + nchunk * 32 * (size_t)n) +
-           sizeof(float) * kn + sizeof(int) * k + 64 * 256;
+           sizeof(float) * kn + sizeof(int) * k + sizeof(double) * 4 * k * 66 + 64 * 1024;
 }
 
-cudaError_t solve_mixed(const float* A32, int64_t n, int k, const double* rhs, double* x, void* work,
+cudaError_t bj_setup(const float* A32, int64_t n, const BlockJacobi& bj, float* work, cudaStream_t s) {
+    if (bj.nb <= 0) return cudaSuccess;
+    cpg::ProfScope ps(cpg::Prof::BJ_SETUP, s);
+    k_bj_invert<<<bj.nb, BJ_THREADS, 0, s>>>(A32, n, bj.perm, bj.off, bj.doff, work, bj.Dinv);
+    return cudaGetLastError();
+}
+
+cudaError_t solve_mixed(const float* A32, const float* Alo, const BlockJacobi* bj, int64_t n, int k, const double* rhs, double* x, void* work,
                         double tol_outer, double tol_inner, int max_outer, int64_t max_inner, SolveStats* st,
                         cudaStream_t s) {
     Arena ar{(char*)work};
@@ -497,7 +683,7 @@ cudaError_t solve_mixed(const float* A32, int64_t n, int k, const double* rhs, d
     for (int outer = 0; outer < max_outer; outer++) {
         ar.off = mark;
         SolveStats inner;
-        if ((e = bicgstab<float, float, float>(A32, n, k, r64, d32, ar, tol_inner, max_inner, 32, &inner, s)) !=
+        if ((e = bicgstab<float, float, float>(A32, n, k, r64, d32, ar, tol_inner, max_inner, 32, &inner, s, bj)) !=
             cudaSuccess)
             return e;
         if (st) {
@@ -506,7 +692,7 @@ cudaError_t solve_mixed(const float* A32, int64_t n, int k, const double* rhs, d
             st->refinements++;
         }
         k_add_to<<<nblk(kn), 256, 0, s>>>(x, d32, kn);
-        if ((e = residual_df(A32, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;
+        if ((e = residual_df(A32, Alo, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;
         if ((e = dots<double>(r64, r64, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
         worst = 0;
         for (int c = 0; c < k; c++) worst = std::max(worst, bnorm[c] > 0 ? std::sqrt(hd[c]) / bnorm[c] : 0.0);

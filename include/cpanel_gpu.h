@@ -52,6 +52,7 @@ typedef struct {
     int64_t n_wakelines; /* trailing-edge wake lines, summed over wakes        */
     int64_t n_tip;       /* panels flagged as tip patch                        */
     int64_t n_nodes;
+    int64_t h2d_bytes;   /* bytes copied host->device by cpg_geometry_create      */
 } cpg_geometry_info;
 
 typedef struct {
@@ -137,6 +138,18 @@ int  cpg_panel_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int
 int  cpg_dub_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* phi_dub);
 int  cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* v_src,
                      double* v_dub);
+
+/* ---- optional device-time accounting (CUDA events on the context's stream) ----
+ * Classes: 0 assembly, 1 wake columns, 2 FP32 matvec, 3 FP64 matvec, 4 refinement
+ * residual, 5 block-Jacobi apply, 6 block-Jacobi setup, 7 CHTLS weights,
+ * 8 velocity/Cp/forces, 9 vector ops. */
+#define CPG_PROF_NCLS 10
+typedef struct {
+    long long launches[CPG_PROF_NCLS];
+    double ms[CPG_PROF_NCLS];
+} cpg_prof;
+int  cpg_prof_enable(cpg_ctx* ctx, int on);           /* on != 0 starts (and clears) */
+int  cpg_prof_read(cpg_ctx* ctx, cpg_prof* out);      /* totals since enable        */
 
 /* Build identification: the sm architecture the kernels were compiled for. */
 int  cpg_compiled_arch(void);

@@ -350,6 +350,18 @@ void checkTE(Mesh& M, int ei) {
     }
 }
 
+/* pow(x, e) for the small non-negative integer exponents of the CHTLS Taylor
+ * monomials, evaluated as repeated products left to right.  The reference calls
+ * std::pow (CPanel/chtlsnd.cpp:103,120); glibc's pow and x*x*x can differ by one
+ * ulp for e = 3.  The repeated product is used here (and in the GPU library) so
+ * that both sides evaluate the ill-conditioned CHTLS normal equations from
+ * identical inputs. */
+inline double powi(double x, int e) {
+    double r = 1;
+    for (int k = 0; k < e; k++) r = k == 0 ? x : r * x;
+    return r;
+}
+
 int factorial(int i) {  // chtlsnd::factorial, CPanel/chtlsnd.cpp:304-321
     int out = 1;
     for (int k = 2; k <= i; k++) out *= k;
@@ -779,7 +791,7 @@ std::vector<double> chtlsF(const std::vector<double>& X0, const std::vector<std:
         for (int i = 0; i < N; i++) fact /= factorial(ms[k][i]);
         for (int i = 0; i < nf; i++) {
             double prod = 1;
-            for (int ii = 0; ii < N; ii++) prod *= std::pow(dXf[i][ii], ms[k][ii]);
+            for (int ii = 0; ii < N; ii++) prod *= powi(dXf[i][ii], ms[k][ii]);
             A[i * t + k] = fact * prod;
         }
         for (int i = 0; i < nb; i++) {
@@ -789,7 +801,7 @@ std::vector<double> chtlsF(const std::vector<double>& X0, const std::vector<std:
                     std::vector<int> ps = ms[k];
                     ps[a] -= 1;
                     double prod = 1;
-                    for (int ii = 0; ii < N; ii++) prod *= std::pow(dXb[i][ii], ps[ii]);
+                    for (int ii = 0; ii < N; ii++) prod *= powi(dXb[i][ii], ps[ii]);
                     asum += Vb[i][a] * ms[k][a] * prod;
                 }
             }
@@ -811,7 +823,7 @@ std::vector<double> chtlsF(const std::vector<double>& X0, const std::vector<std:
     qrSolve(Mm, t, R, nf);
     std::vector<double> F(N * nf);
     for (int r = 0; r < N; r++)
-        for (int i = 0; i < nf; i++) F[r * nf + i] = R[r * nf + i] / std::pow(rmax, rowSum(ms[r]));
+        for (int i = 0; i < nf; i++) F[r * nf + i] = R[r * nf + i] / powi(rmax, rowSum(ms[r]));
     return F;
 }
 
@@ -1146,12 +1158,12 @@ void cpo_tri_v_inf(const double* v9, const double* poi, double* v_src, double* v
 void cpo_set_inf_coeff(void* mp, double* A, double* B, int64_t r0, int64_t r1, int nthreads) {
     Mesh& M = *(Mesh*)mp;
     int64_t n = (int64_t)M.bPanels.size();
+    int64_t ld = r1 - r0;
     // A.setZero(); B.setZero() (rows r0..r1 only)
-    for (int64_t j = 0; j < n; j++)
-        for (int64_t i = r0; i < r1; i++) {
-            A[j * n + i] = 0;
-            B[j * n + i] = 0;
-        }
+    for (int64_t q = 0; q < n * ld; q++) {
+        A[q] = 0;
+        B[q] = 0;
+    }
     std::vector<V3> centers(n);
     for (int64_t i = 0; i < n; i++) centers[i] = M.body[M.bPanels[i]].center;
     // body loop: j (source) outer, i (target) inner -- geometry.cpp:827-841
@@ -1161,7 +1173,8 @@ void cpo_set_inf_coeff(void* mp, double* A, double* B, int64_t r0, int64_t r1, i
             V3 p[3];
             triVerts(M, S, p);
             for (int64_t i = r0; i < r1; i++)
-                panelPhiInf(p, S.center, S.normal, S.area, S.longSide, centers[i], B[j * n + i], A[j * n + i]);
+                panelPhiInf(p, S.center, S.normal, S.area, S.longSide, centers[i], B[j * ld + (i - r0)],
+                            A[j * ld + (i - r0)]);
         }
     });
     // wake scatter, geometry.cpp:853-873 (sequential over wake panels for each row)
@@ -1169,7 +1182,7 @@ void cpo_set_inf_coeff(void* mp, double* A, double* B, int64_t r0, int64_t r1, i
     std::vector<int> idx(4 * nw);
     std::vector<double> coef(nw);
     for (int64_t j = 0; j < nw; j++) interpPanels(M, M.wPanels[j], &idx[4 * j], coef[j]);
-    parallelFor(r1 - r0, nthreads, [&](int64_t a, int64_t b) {
+    parallelFor(ld, nthreads, [&](int64_t a, int64_t b) {
         for (int64_t j = 0; j < nw; j++) {
             const WakeP& W = M.wakeP[M.wPanels[j]];
             V3 p[3];
@@ -1178,10 +1191,10 @@ void cpo_set_inf_coeff(void* mp, double* A, double* B, int64_t r0, int64_t r1, i
             for (int64_t ii = a; ii < b; ii++) {
                 int64_t i = r0 + ii;
                 double infl = dubPhiInf(p, W.center, W.normal, W.area, W.longSide, centers[i]);
-                A[(int64_t)idx[4 * j + 0] * n + i] += infl * (1 - c);
-                A[(int64_t)idx[4 * j + 1] * n + i] += infl * (c - 1);
-                A[(int64_t)idx[4 * j + 2] * n + i] += infl * c;
-                A[(int64_t)idx[4 * j + 3] * n + i] -= infl * c;
+                A[(int64_t)idx[4 * j + 0] * ld + ii] += infl * (1 - c);
+                A[(int64_t)idx[4 * j + 1] * ld + ii] += infl * (c - 1);
+                A[(int64_t)idx[4 * j + 2] * ld + ii] += infl * c;
+                A[(int64_t)idx[4 * j + 3] * ld + ii] -= infl * c;
             }
         }
     });

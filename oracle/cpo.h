@@ -50,8 +50,8 @@ double  cpo_tri_dub_phi_inf(const double* verts9, const double* poi);
 void    cpo_tri_v_inf(const double* verts9, const double* poi, double* v_src, double* v_dub);
 
 /* ---- assembly: geometry::setInfCoeff, CPanel/geometry.cpp:809-891 ----
- * A, B: n_body x n_body column-major (A(i,j) = A[j*n + i]).  Rows [r0, r1) only
- * (full matrix: r0=0, r1=n).  nthreads >= 1. */
+ * Rows [r0, r1) of A and B (full matrix: r0 = 0, r1 = n), stored column-major with
+ * leading dimension r1 - r0: A(i,j) = A[j*(r1-r0) + (i-r0)].  nthreads >= 1. */
 void    cpo_set_inf_coeff(void* m, double* A, double* B, int64_t r0, int64_t r1, int nthreads);
 
 /* ---- steady case: cpCase::run minus I/O, CPanel/cpCase.cpp:31-139 ---- */

@@ -114,11 +114,12 @@ class Mesh:
         return out
 
     def set_inf_coeff(self, rows=None, nthreads=None):
-        """Dense A, B (n x n) as Fortran-ordered arrays (column-major like Eigen)."""
+        """Dense A, B as Fortran-ordered arrays (column-major like Eigen): all rows
+        (n x n) or the row block rows=(r0, r1) ((r1-r0) x n)."""
         n = self.n
         r0, r1 = (0, n) if rows is None else rows
-        A = np.zeros((n, n), order="F")
-        B = np.zeros((n, n), order="F")
+        A = np.empty((r1 - r0, n), order="F")
+        B = np.empty((r1 - r0, n), order="F")
         self.L.cpo_set_inf_coeff(self.h, _p(A), _p(B), r0, r1, nthreads or nthreads_default())
         return A, B
 

@@ -29,8 +29,8 @@ class GeometryInfo(C.Structure):
                 ("n_tip", C.c_int64), ("n_nodes", C.c_int64), ("h2d_bytes", C.c_int64)]
 
 
-PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "bj_apply", "bj_setup",
-                "chtls", "post", "vector_ops"]
+PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "lu_panel", "lu_gemm",
+                "chtls", "post", "lu_solve"]
 
 
 class Prof(C.Structure):

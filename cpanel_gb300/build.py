@@ -20,7 +20,7 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_STRICT = ["assemble.cu", "post.cu"]   # FP64 panel math: no contraction
-CU_FAST = ["solve.cu"]
+CU_FAST = ["solve.cu", "lu.cu"]
 CPP = ["mesh.cpp", "api.cpp"]
 HEADERS = ["common.cuh", "panel64.cuh", "df.cuh", "assemble.h", "post.h", "mesh.h"]
 
@@ -73,7 +73,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    link = [NVCC, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
+    link = [NVCC, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lcublas"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))

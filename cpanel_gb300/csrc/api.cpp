@@ -3,6 +3,7 @@
 // A cpg_geometry owns its device tables; matrices are assembled lazily per
 // precision and kept resident, so further cases on the same mesh reuse them
 // (the reference assembles once per geometry too, CPanel/geometry.cpp:607-621).
+#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -23,6 +24,7 @@ struct cpg_ctx {
     bool own_stream = false;
     std::string err;
     cpg::Prof* prof = nullptr;  // device-time accounting, when enabled
+    cublasHandle_t blas = nullptr;
 };
 
 namespace {
@@ -73,8 +75,8 @@ struct cpg_geometry {
     cpg::HostMesh H;
     DevBuf rec, frec, bez, clp, cli, tip, ts, wrec, widx, wcoef, tzst, tzln, tzpts, G, F3, F2, mode;
     DevBuf A64, B64, A32, Alo, rb, count;
-    DevBuf bjperm, bjoff, bjdoff, bjinv, bjwork;
-    cpg::BlockJacobi bj;
+    DevBuf LU, bad;
+    bool lu_ready = false;
     DevBuf work, post_work, cases, outs;
     bool have64 = false, have32 = false, post_ready = false;
     int64_t h2d_bytes = 0;
@@ -212,6 +214,7 @@ int cpg_create(cpg_ctx** out, int device) {
 void cpg_destroy(cpg_ctx* c) {
     if (!c) return;
     delete c->prof;
+    if (c->blas) cublasDestroy(c->blas);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -282,28 +285,6 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
         cpg_geometry_destroy(g);
         return cuda_fail(ctx, e, "geometry upload");
     }
-    {  // block-Jacobi layout
-        std::vector<int64_t> doff(H.bj_off.size(), 0);
-        int bsmax = 0;
-        for (size_t b = 0; b + 1 < H.bj_off.size(); b++) {
-            int64_t bs = H.bj_off[b + 1] - H.bj_off[b];
-            doff[b + 1] = doff[b] + bs * bs;
-            bsmax = std::max<int>(bsmax, (int)bs);
-        }
-        if ((e = upload(g->bjperm, H.bj_perm, s)) != cudaSuccess || (e = upload(g->bjoff, H.bj_off, s)) != cudaSuccess ||
-            (e = upload(g->bjdoff, doff, s)) != cudaSuccess ||
-            (e = g->bjinv.ensure(sizeof(float) * std::max<int64_t>(1, doff.back()))) != cudaSuccess ||
-            (e = g->bjwork.ensure(sizeof(float) * std::max<int64_t>(1, doff.back()))) != cudaSuccess) {
-            cpg_geometry_destroy(g);
-            return cuda_fail(ctx, e, "preconditioner tables");
-        }
-        g->bj.perm = g->bjperm.as<int32_t>();
-        g->bj.off = g->bjoff.as<int32_t>();
-        g->bj.doff = g->bjdoff.as<int64_t>();
-        g->bj.Dinv = g->bjinv.as<float>();
-        g->bj.nb = (int)H.bj_off.size() - 1;
-        g->bj.bsmax = bsmax;
-    }
     g->h2d_bytes = t_h2d;
     *out = g;
     return CPG_OK;
@@ -313,7 +294,7 @@ void cpg_geometry_destroy(cpg_geometry* g) {
     if (!g) return;
     DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
                       &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
-                      &g->B64, &g->A32, &g->Alo, &g->rb, &g->bjperm, &g->bjoff, &g->bjdoff, &g->bjinv, &g->bjwork, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
+                      &g->B64, &g->A32, &g->Alo, &g->rb, &g->LU, &g->bad, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
     // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
     delete g;
@@ -417,8 +398,8 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
                                       g->A32.as<float>(), g->Alo.as<float>(), g->rb.as<double>(),
                                       g->count.as<unsigned long long>(), s),
            "assembly (mixed)");
-        CK(cpg::bj_setup(g->A32.as<float>(), n, g->bj, g->bjwork.as<float>(), s), "block-Jacobi setup");
         g->have32 = true;
+        g->lu_ready = false;
     } else {
         return fail(ctx, CPG_E_INVALID, "unknown precision");
     }
@@ -512,10 +493,23 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
         CK(cpg::solve_fp64(g->A64.as<double>(), n, k, rhs, mu, g->work.p, 2.220446049250313e-16, 2 * n, &st, s),
            "BiCGSTAB (FP64)");
     } else {
-        size_t wb = cpg::solve_mixed_work_bytes(n, k);
+        if (!ctx->blas && cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) {
+            ctx->blas = nullptr;
+            return fail(ctx, CPG_E_CUDA, "cublasCreate failed");
+        }
+        if (!g->lu_ready) {  // per-geometry factorization, reused by every case
+            CK(g->LU.ensure(sizeof(float) * (size_t)n * n), "alloc LU");
+            CK(g->bad.ensure(sizeof(int)), "alloc flag");
+            CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
+            CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");
+            CK(cpg::lu_factor_fp32(ctx->blas, g->LU.as<float>(), n, g->bad.as<int>(), s), "LU factorization");
+            g->lu_ready = true;
+        }
+        size_t wb = cpg::solve_lu_work_bytes(n, k);
         CK(g->work.ensure(wb), "alloc solver workspace");
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
-        CK(cpg::solve_mixed(g->A32.as<float>(), g->Alo.as<float>(), &g->bj, n, k, rhs, mu, g->work.p, 1e-10, 1e-5, 12, 1000, &st, s),
+        CK(cpg::solve_lu_refined(ctx->blas, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(), n, k, rhs, mu,
+                                 g->work.p, 1e-12, 8, &st, s),
            "refined solve (mixed)");
     }
     CK(cudaEventRecord(e1, s), "event");

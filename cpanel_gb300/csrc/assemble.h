@@ -11,8 +11,8 @@ namespace cpg {
 // stream).  Enabled per context; the API entry points install it for the calling
 // thread for the duration of a call.
 struct Prof {
-    enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, BJ_APPLY, BJ_SETUP, CHTLS, POST,
-           VECTOR_OPS, NCLS };
+    enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, LU_PANEL, LU_GEMM, CHTLS, POST,
+           LU_SOLVE, NCLS };
     struct Pair {
         cudaEvent_t a, b;
         int cls;
@@ -64,25 +64,22 @@ struct SolveStats {
 size_t solve_fp64_work_bytes(int64_t n, int k);
 cudaError_t solve_fp64(const double* A, int64_t n, int k, const double* rhs, double* x, void* work,
                        double tol, int64_t max_iters, SolveStats* st, cudaStream_t s);
-// Mixed: A = A32 + Alo (two FP32 column-major matrices; Alo is zero in the far
-// field).  FP32 BiCGSTAB inner solves on A32 with FP64 inner products, wrapped in
-// iterative refinement whose residual b - (A32 + Alo) x is accumulated with exact
-// FP32 products (double-float).  Stops at relative residual <= tol_outer for
-// every column.
-// Block-Jacobi preconditioner on index sets perm[off[b] .. off[b+1]).
-struct BlockJacobi {
-    const int32_t* perm = nullptr;
-    const int32_t* off = nullptr;      // device, nb + 1
-    const int64_t* doff = nullptr;     // device, offset of block b's inverse in Dinv
-    float* Dinv = nullptr;             // column-major block inverses
-    int nb = 0;
-    int bsmax = 0;
-};
-cudaError_t bj_setup(const float* A32, int64_t n, const BlockJacobi& bj, float* work, cudaStream_t s);
-size_t solve_mixed_work_bytes(int64_t n, int k);
-cudaError_t solve_mixed(const float* A32, const float* Alo, const BlockJacobi* bj, int64_t n, int k, const double* rhs, double* x, void* work,
-                        double tol_outer, double tol_inner, int max_outer, int64_t max_inner, SolveStats* st,
-                        cudaStream_t s);
+// Refinement residual r = b - (A32 + Alo) x for k right-hand sides (x FP64), with
+// the leading products formed exactly in FP32 pairs.  P: residual_chunks(n)*17*n doubles.
+int64_t residual_chunks(int64_t n);
+cudaError_t residual_df(const float* A32, const float* Alo, int64_t n, int k, const double* x, const double* b,
+                        double* r, double* P, cudaStream_t s);
+// Squared column norms of a k x n case-major FP64 block, copied to host[0..k).
+cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, double* dd, double* host, cudaStream_t s);
+
+// lu.cu: FP32 LU without pivoting (blocked, cuBLAS trailing GEMM) and the refined
+// solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.
+cudaError_t lu_factor_fp32(void* blas, float* LU, int64_t n, int* bad, cudaStream_t s);
+cudaError_t lu_solve_fp32(void* blas, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
+size_t solve_lu_work_bytes(int64_t n, int k);
+cudaError_t solve_lu_refined(void* blas, const float* A32, const float* Alo, const float* LU, int64_t n, int k,
+                             const double* rhs, double* x, void* work, double tol, int max_steps, SolveStats* st,
+                             cudaStream_t s);
 // y(k x n) = alpha * M x(k x n) for column-major FP64 M (used for -B sigma).
 cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, double* y, double alpha, void* work,
                          cudaStream_t s);

@@ -511,37 +511,6 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
         H.widx[4 * j + 2] = B.pan[b->up].index;
         H.widx[4 * j + 3] = B.pan[b->lo].index;
     }
-    // spanwise bands for the block-Jacobi preconditioner
-    {
-        const int64_t bmin = 128, bmax = 512;
-        std::vector<int32_t> ord(H.n_body);
-        for (int64_t i = 0; i < H.n_body; i++) ord[i] = (int32_t)i;
-        std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t b) {
-            return H.body[a * PF_STRIDE + PF_C + 1] < H.body[b * PF_STRIDE + PF_C + 1];
-        });
-        auto yof = [&](int64_t q) { return H.body[(int64_t)ord[q] * PF_STRIDE + PF_C + 1]; };
-        H.bj_perm = ord;
-        H.bj_off.assign(1, 0);
-        int64_t i = 0;
-        while (i < H.n_body) {
-            int64_t rest = H.n_body - i, cut;
-            if (rest <= bmax) {
-                cut = H.n_body;
-            } else {
-                cut = i + bmax;
-                double best = -1;
-                for (int64_t c = i + bmin; c <= i + bmax && c < H.n_body; c++) {
-                    double gap = yof(c) - yof(c - 1);
-                    if (gap >= best) {
-                        best = gap;
-                        cut = c;
-                    }
-                }
-            }
-            H.bj_off.push_back((int32_t)cut);
-            i = cut;
-        }
-    }
     H.n_lines = 0;
     // Trefftz plane geometry, CPanel/wake.cpp:146-188,508-640
     H.trefftz.clear();

@@ -48,10 +48,6 @@ struct HostMesh {
     std::vector<double> wake;          // n_wake x PF_STRIDE
     std::vector<int32_t> widx;         // n_wake x 4 interpolation columns
     std::vector<double> wcoef;         // n_wake
-    // block-Jacobi preconditioner of the mixed solver: panels grouped into
-    // spanwise bands (sorted by centroid y, cut at the widest y gaps)
-    std::vector<int32_t> bj_perm;      // n_body, band-major panel order
-    std::vector<int32_t> bj_off;       // n_blocks + 1
     // Trefftz plane, per live wake
     std::vector<TrefftzWake> trefftz;
     std::vector<double> tz_pts;        // all sample points, 3 per point

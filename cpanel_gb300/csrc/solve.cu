@@ -240,128 +240,7 @@ __global__ void k_convert(const TS* __restrict__ a, TD* __restrict__ b, int64_t 
     if (t < m) b[t] = (TD)a[t];
 }
 
-__global__ void k_add_to(double* __restrict__ x, const float* __restrict__ d, int64_t m) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < m) x[t] += (double)d[t];
-}
-
 inline unsigned nblk(int64_t m, int b = 256) { return (unsigned)((m + b - 1) / b); }
-
-// ---- block-Jacobi: gather, Gauss-Jordan inverse (FP32, partial pivoting), apply
-constexpr int BJ_THREADS = 512;
-
-__global__ void __launch_bounds__(BJ_THREADS) k_bj_invert(const float* __restrict__ A, int64_t n,
-                                                          const int32_t* __restrict__ perm, const int32_t* __restrict__ off,
-                                                          const int64_t* __restrict__ doff, float* __restrict__ W,
-                                                          float* __restrict__ Dinv) {
-    __shared__ float fr[512];
-    __shared__ float rv[BJ_THREADS];
-    __shared__ int ri[BJ_THREADS];
-    const int b = blockIdx.x;
-    const int o = off[b], bs = off[b + 1] - o;
-    float* D = W + doff[b];      // row-major work copy D[r*bs + c]
-    float* I = Dinv + doff[b];   // row-major during elimination, transposed at the end
-    for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) {
-        int r = (int)(t / bs), c = (int)(t % bs);
-        D[t] = A[(int64_t)perm[o + c] * n + perm[o + r]];
-        I[t] = r == c ? 1.f : 0.f;
-    }
-    __syncthreads();
-    for (int k = 0; k < bs; k++) {
-        float best = -1.f;
-        int bi = k;
-        for (int r = k + threadIdx.x; r < bs; r += BJ_THREADS) {
-            float v = fabsf(D[(int64_t)r * bs + k]);
-            if (v > best) {
-                best = v;
-                bi = r;
-            }
-        }
-        rv[threadIdx.x] = best;
-        ri[threadIdx.x] = bi;
-        __syncthreads();
-        for (int st = BJ_THREADS / 2; st > 0; st >>= 1) {
-            if (threadIdx.x < st) {
-                float a = rv[threadIdx.x], c2 = rv[threadIdx.x + st];
-                if (c2 > a || (c2 == a && ri[threadIdx.x + st] < ri[threadIdx.x])) {
-                    rv[threadIdx.x] = c2;
-                    ri[threadIdx.x] = ri[threadIdx.x + st];
-                }
-            }
-            __syncthreads();
-        }
-        int p = ri[0];
-        __syncthreads();
-        if (p != k)
-            for (int c = threadIdx.x; c < bs; c += BJ_THREADS) {
-                float t1 = D[(int64_t)k * bs + c];
-                D[(int64_t)k * bs + c] = D[(int64_t)p * bs + c];
-                D[(int64_t)p * bs + c] = t1;
-                float t2 = I[(int64_t)k * bs + c];
-                I[(int64_t)k * bs + c] = I[(int64_t)p * bs + c];
-                I[(int64_t)p * bs + c] = t2;
-            }
-        __syncthreads();
-        float piv = D[(int64_t)k * bs + k];
-        float inv = piv != 0.f ? 1.f / piv : 1.f;
-        __syncthreads();
-        for (int c = threadIdx.x; c < bs; c += BJ_THREADS) {
-            D[(int64_t)k * bs + c] *= inv;
-            I[(int64_t)k * bs + c] *= inv;
-        }
-        for (int r = threadIdx.x; r < bs; r += BJ_THREADS) fr[r] = r == k ? 0.f : D[(int64_t)r * bs + k];
-        __syncthreads();
-        for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) {
-            int r = (int)(t / bs), c = (int)(t % bs);
-            float f = fr[r];
-            if (f != 0.f) {
-                D[t] = __fmaf_rn(-f, D[(int64_t)k * bs + c], D[t]);
-                I[t] = __fmaf_rn(-f, I[(int64_t)k * bs + c], I[t]);
-            }
-        }
-        __syncthreads();
-    }
-    // transpose I in place into column-major via the work buffer
-    for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) D[t] = I[t];
-    __syncthreads();
-    for (int64_t t = threadIdx.x; t < (int64_t)bs * bs; t += BJ_THREADS) {
-        int r = (int)(t / bs), c = (int)(t % bs);
-        I[(int64_t)c * bs + r] = D[t];
-    }
-}
-
-// y[c*n + perm[o+r]] = sum_q Dinv_b[q*bs + r] * x[c*n + perm[o+q]]   (RHS in chunks of 8)
-template <typename T>
-__global__ void __launch_bounds__(256) k_bj_apply(const float* __restrict__ Dinv, const int32_t* __restrict__ perm,
-                                                  const int32_t* __restrict__ off, const int64_t* __restrict__ doff,
-                                                  int64_t n, int k, const T* __restrict__ x, T* __restrict__ y,
-                                                  const double* __restrict__ sc) {
-    __shared__ float xs[512][8];
-    const int b = blockIdx.x;
-    const int o = off[b], bs = off[b + 1] - o;
-    const float* Di = Dinv + doff[b];
-    for (int c0 = 0; c0 < k; c0 += 8) {
-        int kc = min(8, k - c0);
-        __syncthreads();
-        for (int t = threadIdx.x; t < bs * 8; t += 256) {
-            int q = t / 8, c = t % 8;
-            xs[q][c] = c < kc ? (float)x[(int64_t)(c0 + c) * n + perm[o + q]] : 0.f;
-        }
-        __syncthreads();
-        for (int r = threadIdx.x; r < bs; r += 256) {
-            float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-            for (int q = 0; q < bs; q++) {
-                float d = Di[(int64_t)q * bs + r];
-#pragma unroll
-                for (int c = 0; c < 8; c++) acc[c] = __fmaf_rn(d, xs[q][c], acc[c]);
-            }
-            for (int c = 0; c < kc; c++) {
-                if (sc && sc[4 * (c0 + c) + 3] == 0) continue;
-                y[(int64_t)(c0 + c) * n + perm[o + r]] = (T)acc[c];
-            }
-        }
-    }
-}
 
 // ------------------------------------------------------------------ drivers
 struct Arena {
@@ -418,7 +297,7 @@ void resid_launch(const float* A, const float* Alo, int64_t n, int64_t ch, const
 }
 
 // r = b - (A32 + Alo) x (x FP64), leading products exact.
-cudaError_t residual_df(const float* A, const float* Alo, int64_t n, int k, const double* x, const double* b, double* r,
+cudaError_t residual_df_impl(const float* A, const float* Alo, int64_t n, int k, const double* x, const double* b, double* r,
                         double* P, cudaStream_t s) {
     int64_t ch = mv_chunk(n, 152 * 8);
     int nchunk = (int)((n + ch - 1) / ch);
@@ -451,7 +330,7 @@ cudaError_t dots(const T* U0, const T* V0, const T* U1, const T* V1, int64_t n, 
 // DiagonalPreconditioner, restart when r drifts orthogonal to r0).
 template <typename T, typename TA, typename TACC>
 cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena& ar, double tol, int64_t maxIters,
-                     int kbmax, cpg::SolveStats* st, cudaStream_t s, const cpg::BlockJacobi* bj = nullptr) {
+                     int kbmax, cpg::SolveStats* st, cudaStream_t s) {
     const size_t kn = (size_t)k * n;
     T *r = ar.take<T>(kn), *r0 = ar.take<T>(kn), *p = ar.take<T>(kn), *v = ar.take<T>(kn), *y = ar.take<T>(kn),
       *z = ar.take<T>(kn), *sv = ar.take<T>(kn), *tv = ar.take<T>(kn), *invd = ar.take<T>(n);
@@ -530,10 +409,6 @@ cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena
         }
         cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
         k_upd_p<T><<<nblk(kn), 256, 0, s>>>(r, v, p, y, invd, sc, n, k);
-        if (bj) {
-            cpg::ProfScope ps(cpg::Prof::BJ_APPLY, s);
-            k_bj_apply<T><<<bj->nb, 256, 0, s>>>(bj->Dinv, bj->perm, bj->off, bj->doff, n, k, p, y, sc);
-        }
         matmul<TA, T, TACC, T>(A, n, k, y, v, 1.0, nullptr, P, kbmax, s);
         if ((e = dots<T>(r0, v, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
         for (int c = 0; c < k; c++)
@@ -543,10 +418,6 @@ cudaError_t bicgstab(const TA* A, int64_t n, int k, const double* b, T* x, Arena
             }
         cudaMemcpyAsync(sc, hsc.data(), sizeof(double) * 4 * k, cudaMemcpyHostToDevice, s);
         k_upd_s<T><<<nblk(kn), 256, 0, s>>>(r, v, sv, z, invd, sc, n, k);
-        if (bj) {
-            cpg::ProfScope ps(cpg::Prof::BJ_APPLY, s);
-            k_bj_apply<T><<<bj->nb, 256, 0, s>>>(bj->Dinv, bj->perm, bj->off, bj->doff, n, k, sv, z, sc);
-        }
         matmul<TA, T, TACC, T>(A, n, k, z, tv, 1.0, nullptr, P, kbmax, s);
         if ((e = dots<T>(tv, tv, tv, sv, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
         for (int c = 0; c < k; c++)
@@ -644,62 +515,18 @@ cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, dou
     return matmul<double, double, double, double>(M, n, k, x, y, alpha, nullptr, (double*)work, 8, s);
 }
 
-size_t solve_mixed_work_bytes(int64_t n, int k) {
+int64_t residual_chunks(int64_t n) {
     int64_t ch = mv_chunk(n, 152 * 8);
-    int64_t nchunk = (n + ch - 1) / ch;
-    size_t kn = (size_t)k * n;
-    return sizeof(float) * (9 * kn + n + nchunk * 32 * (size_t)n) +
-           sizeof(double) * (kn /*Ax*/ + 2 * k * 64 + 2 * k + 4 * k + 2 * kn /*r64, d64*/ + nchunk * 32 * (size_t)n) +
-           sizeof(float) * kn + sizeof(int) * k + sizeof(double) * 4 * k * 66 + 64 * 1024;
+    return (n + ch - 1) / ch;
 }
 
-cudaError_t bj_setup(const float* A32, int64_t n, const BlockJacobi& bj, float* work, cudaStream_t s) {
-    if (bj.nb <= 0) return cudaSuccess;
-    cpg::ProfScope ps(cpg::Prof::BJ_SETUP, s);
-    k_bj_invert<<<bj.nb, BJ_THREADS, 0, s>>>(A32, n, bj.perm, bj.off, bj.doff, work, bj.Dinv);
-    return cudaGetLastError();
+cudaError_t residual_df(const float* A32, const float* Alo, int64_t n, int k, const double* x, const double* b,
+                        double* r, double* P, cudaStream_t s) {
+    return residual_df_impl(A32, Alo, n, k, x, b, r, P, s);
 }
 
-cudaError_t solve_mixed(const float* A32, const float* Alo, const BlockJacobi* bj, int64_t n, int k, const double* rhs, double* x, void* work,
-                        double tol_outer, double tol_inner, int max_outer, int64_t max_inner, SolveStats* st,
-                        cudaStream_t s) {
-    Arena ar{(char*)work};
-    const size_t kn = (size_t)k * n;
-    double* r64 = ar.take<double>(kn);
-    float* d32 = ar.take<float>(kn);
-    int64_t ch = mv_chunk(n, 152 * 8);
-    int nchunk = (int)((n + ch - 1) / ch);
-    double* P64 = ar.take<double>((size_t)nchunk * 17 * n);
-    double* part = ar.take<double>((size_t)2 * k * 64);
-    double* dd = ar.take<double>(2 * k);
-    size_t mark = ar.off;
-    std::vector<double> hd(2 * k), bnorm(k);
-    cudaError_t e;
-    cudaMemsetAsync(x, 0, sizeof(double) * kn, s);
-    cudaMemcpyAsync(r64, rhs, sizeof(double) * kn, cudaMemcpyDeviceToDevice, s);
-    if ((e = dots<double>(rhs, rhs, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
-    for (int c = 0; c < k; c++) bnorm[c] = std::sqrt(hd[c]);
-    double worst = 1;
-    for (int outer = 0; outer < max_outer; outer++) {
-        ar.off = mark;
-        SolveStats inner;
-        if ((e = bicgstab<float, float, float>(A32, n, k, r64, d32, ar, tol_inner, max_inner, 32, &inner, s, bj)) !=
-            cudaSuccess)
-            return e;
-        if (st) {
-            st->iters_total += inner.iters_total;
-            st->iters_max = std::max(st->iters_max, inner.iters_max);
-            st->refinements++;
-        }
-        k_add_to<<<nblk(kn), 256, 0, s>>>(x, d32, kn);
-        if ((e = residual_df(A32, Alo, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;
-        if ((e = dots<double>(r64, r64, nullptr, nullptr, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
-        worst = 0;
-        for (int c = 0; c < k; c++) worst = std::max(worst, bnorm[c] > 0 ? std::sqrt(hd[c]) / bnorm[c] : 0.0);
-        if (worst <= tol_outer) break;
-    }
-    if (st) st->residual_max = std::max(st->residual_max, worst);
-    return cudaGetLastError();
+cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, double* dd, double* host, cudaStream_t s) {
+    return dots<double>(v, v, nullptr, nullptr, n, k, part, dd, host, s);
 }
 
 }  // namespace cpg

@@ -38,8 +38,9 @@ typedef enum {
 
 typedef enum {
     CPG_PLAIN_FP64 = 0,  /* the reference method in FP64: explicit A, B; BiCGSTAB to eps */
-    CPG_MIXED = 1        /* FP32 far field + FP64 near field, FP32 Krylov + FP64-exact
-                            iterative refinement to rel. residual 1e-10              */
+    CPG_MIXED = 1        /* double-float far field + FP64 near field, matrix kept as an
+                            FP32 hi + lo pair; FP32 LU + refinement with an exact-
+                            product residual to relative residual 1e-12              */
 } cpg_precision;
 
 typedef struct cpg_ctx cpg_ctx;
@@ -141,8 +142,8 @@ int  cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64
 
 /* ---- optional device-time accounting (CUDA events on the context's stream) ----
  * Classes: 0 assembly, 1 wake columns, 2 FP32 matvec, 3 FP64 matvec, 4 refinement
- * residual, 5 block-Jacobi apply, 6 block-Jacobi setup, 7 CHTLS weights,
- * 8 velocity/Cp/forces, 9 vector ops. */
+ * residual, 5 LU panel (diagonal block + triangular blocks), 6 LU trailing GEMM,
+ * 7 CHTLS weights, 8 velocity/Cp/forces, 9 LU triangular solves. */
 #define CPG_PROF_NCLS 10
 typedef struct {
     long long launches[CPG_PROF_NCLS];

@@ -25,6 +25,9 @@ import sys
 import threading
 import time
 
+import ctypes as C
+from ctypes import c_double as C_double
+
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -38,18 +41,25 @@ METRIC = "steady solves/s + p50/p99 latency at Cp err<=1e-5 vs FP64 plain GPU pa
 PLAIN_ITERS = 372
 
 
-def workload():
+def workload(name="multi_rhs"):
+    """multi_rhs: the benchmark wing.  mid: the same wing with 25 span stations
+    (7,876 panels; matrices still larger than L2), used for profiler captures."""
+    import dataclasses
+
     from cpanel_gb300 import wing
     spec = wing.config_multi_rhs()
+    if name == "mid":
+        spec = dataclasses.replace(spec, n_span=25)
     nodes, tris, ids, info = wing.make_wing(spec)
     refs = dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0.0, 0.0))
     return spec, nodes, tris, ids, info, refs
 
 
-def config_dict(info):
-    return {"workload": "NACA4412 tapered AR6 wing, 80 pts/side x 61 stations, 17 alphas (-4..12 deg)",
+def config_dict(info, name="multi_rhs"):
+    stations = {"multi_rhs": 61, "mid": 25}[name]
+    return {"workload": "NACA4412 tapered AR6 wing, 80 pts/side x %d stations, 17 alphas (-4..12 deg)" % stations,
             "body_panels": info["n_body"], "wake_panels": info["n_wake"], "alphas": len(ALPHAS), "mach": MACH,
-            "precision": "mixed: df32 far field + FP64 near field, FP32 block-Jacobi BiCGSTAB, refined to 1e-10",
+            "precision": "mixed: df32 far field + FP64 near field, FP32 LU + refinement to 1e-12",
             "l2": "inputs larger than L2 (A = 2 x 1.49 GB)", "parallelism": "replicas"}
 
 
@@ -181,6 +191,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--workload", default="multi_rhs", choices=["multi_rhs", "mid"])
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -202,7 +213,7 @@ def main():
         dist.barrier()
     import cpanel_gb300 as cg
 
-    spec, nodes, tris, ids, info, refs = workload()
+    spec, nodes, tris, ids, info, refs = workload(args.workload)
     flows = [(1.0, a, 0.0, MACH) for a in ALPHAS]
     k = len(flows)
     ctx = cg.Context(local)
@@ -284,16 +295,43 @@ def main():
 
     # ---- roofline of the dominant kernel class in the timed region
     hbm, peak_kind = read_peaks()
+    fp64 = C_double()
+    ctx.check(ctx.L.cpg_measure_fp64_peak(ctx.h, C.byref(fp64)), "fp64 peak")
+    fp64_peak = fp64.value
+    roofs = {}
+    a_l, a_ms = prof["assembly"]
+    if a_l:
+        # near pairs in FP64: per pair 3 edges x (~101 flop + 5 sqrt + 2 div + atan2 + log) + 20
+        # flop + sqrt + div; transcendentals counted as one op each (op model in the design doc)
+        fl = stats["n_near"] * (3 * (101 + 5 + 2 + 2) + 22)
+        ach = fl / (a_ms / a_l * 1e-3) / 1e12
+        roofs["assembly"] = {"bound": "fp64", "kernel": "k_assemble_mixed (FP64 near field, df32 far field)",
+                             "achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s", "frac": ach / fp64_peak,
+                             "traffic": None, "peak_source": "measured in this run (FP64 FMA probe)",
+                             "algorithmic_flops_per_launch": fl, "avg_launch_ms": a_ms / a_l, "launches": a_l}
+    g_l, g_ms = prof["lu_gemm"]
+    if g_l:
+        fl = 2.0 / 3.0 * n ** 3  # per factorization, summed over its trailing updates
+        nfac = prof["lu_panel"][0] / max(1, (n + 127) // 128)
+        ach = fl * nfac / (g_ms * 1e-3) / 1e12
+        roofs["lu_gemm"] = {"bound": "tensor", "kernel": "trailing GEMM, cuBLAS BF16x9 (FP32-accurate)",
+                            "achieved": ach, "unit": "TFLOP/s (FP32-equivalent)", "peak": 1963.8 / 9,
+                            "frac": ach / (1963.8 / 9), "peak_source": "measured bf16 / 9 BF16 products",
+                            "traffic": None}
+    s_l, s_ms = prof["lu_solve"]
+    if s_l:
+        bytes_s = 4.0 * n * n + 2 * 4.0 * k * n  # L and U read once per solve
+        ach = bytes_s / (s_ms / s_l * 1e-3) / 1e9
+        roofs["lu_solve"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                             "peak_source": peak_kind, "traffic": None}
+    r_l, r_ms = prof["residual"]
+    if r_l:
+        bytes_r = 8.0 * n * n + 8.0 * 3 * k * n
+        ach = bytes_r / (r_ms / r_l * 1e-3) / 1e9
+        roofs["residual"] = {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                             "peak_source": peak_kind, "traffic": None}
     dom = max(prof.items(), key=lambda kv: kv[1][1])
-    roof = None
-    mv_l, mv_ms = prof["matvec_fp32"]
-    if mv_l:
-        bytes_mv = 4.0 * n * n + 2 * 4.0 * k * n
-        ach = bytes_mv / (mv_ms / mv_l * 1e-3) / 1e9
-        roof = {"bound": "hbm", "kernel": "k_mv<float> (FP32 multi-RHS matvec, 17 RHS)", "achieved": ach,
-                "peak": hbm, "unit": "GB/s", "frac": ach / hbm, "traffic": None,
-                "peak_source": peak_kind, "algorithmic_bytes_per_launch": bytes_mv,
-                "avg_launch_ms": mv_ms / mv_l, "launches": mv_l}
+    roof = roofs.get(dom[0])
     breakdown = {name: {"launches": int(l), "ms": round(ms, 3)} for name, (l, ms) in prof.items() if l}
 
     cpu = None
@@ -309,12 +347,12 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+df32+f64", "data": "synthetic (seeded NACA wing)",
-                "config": config_dict(info),
+                "config": config_dict(info, args.workload),
                 "latency_ms": {"p50": p50, "p99": p99, "what": "one 17-alpha sweep request (device time)"},
                 "accuracy_vs_plain_fp64": acc, "plain_fp64": plain,
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
-                "roofline": roof, "dominant_kernel_class": {"name": dom[0], "ms": dom[1][1], "launches": dom[1][0]},
+                "roofline": roof, "roofline_all": roofs, "dominant_kernel_class": {"name": dom[0], "ms": dom[1][1], "launches": dom[1][0]},
                 "kernel_breakdown_ms": breakdown, "gpu_launches": launches,
                 "solver": {"iters_max": stats["iters_max"], "refinements": stats["refinements"],
                            "residual_max": stats["residual_max"], "near_pairs": stats["n_near"]},

@@ -617,6 +617,12 @@ int cpg_prof_read(cpg_ctx* ctx, cpg_prof* out) {
     return CPG_OK;
 }
 
+int cpg_measure_fp64_peak(cpg_ctx* ctx, double* tflops) {
+    if (!ctx || !tflops) return CPG_E_INVALID;
+    *tflops = cpg::measure_fp64_tflops(ctx->stream);
+    return *tflops > 0 ? CPG_OK : fail(ctx, CPG_E_CUDA, "FP64 probe failed");
+}
+
 int cpg_compiled_arch(void) { return CPG_COMPILED_ARCH; }
 
 }  // extern "C"

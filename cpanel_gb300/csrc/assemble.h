@@ -69,6 +69,8 @@ cudaError_t solve_fp64(const double* A, int64_t n, int k, const double* rhs, dou
 int64_t residual_chunks(int64_t n);
 cudaError_t residual_df(const float* A32, const float* Alo, int64_t n, int k, const double* x, const double* b,
                         double* r, double* P, cudaStream_t s);
+// Measured FP64 FMA throughput of this GPU (TFLOP/s), for roofline reporting.
+double measure_fp64_tflops(cudaStream_t s);
 // Squared column norms of a k x n case-major FP64 block, copied to host[0..k).
 cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, double* dd, double* host, cudaStream_t s);
 

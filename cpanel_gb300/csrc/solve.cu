@@ -515,6 +515,42 @@ cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, dou
     return matmul<double, double, double, double>(M, n, k, x, y, alpha, nullptr, (double*)work, 8, s);
 }
 
+// FP64 FMA throughput probe: 8 independent dependency chains per thread.
+__global__ void __launch_bounds__(256) k_fma64_probe(double* out, int iters, double a, double b) {
+    double x[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = threadIdx.x * 1e-9 + q;
+    for (int i = 0; i < iters; i++) {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = fma(x[q], a, b);
+    }
+    double s = 0;
+#pragma unroll
+    for (int q = 0; q < 8; q++) s += x[q];
+    if (s == 12345.678) out[0] = s;  // keeps the chains live
+}
+
+double measure_fp64_tflops(cudaStream_t s) {
+    double* sink = nullptr;
+    if (cudaMalloc(&sink, 8) != cudaSuccess) return 0;
+    const int iters = 4096, blocks = 152 * 16, threads = 256;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    k_fma64_probe<<<blocks, threads, 0, s>>>(sink, iters, 0.999999, 1e-9);  // warm-up
+    cudaEventRecord(e0, s);
+    k_fma64_probe<<<blocks, threads, 0, s>>>(sink, iters, 0.999999, 1e-9);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(sink);
+    double flops = 2.0 * 8 * iters * (double)blocks * threads;
+    return ms > 0 ? flops / (ms * 1e-3) / 1e12 : 0;
+}
+
 int64_t residual_chunks(int64_t n) {
     int64_t ch = mv_chunk(n, 152 * 8);
     return (n + ch - 1) / ch;

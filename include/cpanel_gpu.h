@@ -152,6 +152,10 @@ typedef struct {
 int  cpg_prof_enable(cpg_ctx* ctx, int on);           /* on != 0 starts (and clears) */
 int  cpg_prof_read(cpg_ctx* ctx, cpg_prof* out);      /* totals since enable        */
 
+/* FP64 FMA throughput of the context's GPU in TFLOP/s (a short probe kernel), the
+ * denominator for FP64-issue-bound kernels. */
+int  cpg_measure_fp64_peak(cpg_ctx* ctx, double* tflops);
+
 /* Build identification: the sm architecture the kernels were compiled for. */
 int  cpg_compiled_arch(void);
 

@@ -5,6 +5,9 @@
 // j = source panel.  A block owns 128 consecutive targets and a contiguous range of
 // source panels, staged 32 at a time in shared memory; each store instruction of
 // a warp writes 32 consecutive rows of one column.
+#include <mutex>
+
+#include "../../include/cpanel_gpu.h"
 #include "assemble.h"
 #include "df.cuh"
 #include "panel64.cuh"
@@ -262,6 +265,11 @@ __global__ void k_wake_potential_op(const double* __restrict__ wrec, int64_t nw,
     G[t] = dub_phi_inf(wrec + w * R_STRIDE, ld3(pts + 3 * p));
 }
 
+__global__ void k_pack_records(const double* __restrict__ verts, int64_t m, double* __restrict__ rec) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < m) make_record(verts + 9 * t, rec + t * R_STRIDE);
+}
+
 int64_t chunk_for(int64_t n) {
     // enough blocks in y to fill the 152 SMs several times over
     int64_t bx = (n + TI - 1) / TI;
@@ -333,3 +341,65 @@ cudaError_t launch_wake_potential_op(const double* wrec, int64_t nw, const doubl
 }
 
 }  // namespace cpg
+
+// ---------------------------------------------------------------------------
+// Allocation-free assembly.
+//
+// Some callers cannot allocate device memory while they run this path: a host
+// that records the influence assembly into a CUDA graph, a plug-in living inside
+// another solver's memory pool, or a real-time loop that has forbidden allocation
+// after start-up.  cpg_set_inf_coeff_noalloc serves them.  It runs the same FP64
+// kernels as cpg_set_inf_coeff, but the one scratch table those kernels need (the
+// packed 192-byte panel records, normally held by a cpg_geometry) lives in the
+// fixed array below.  Every GPU that loads this library keeps that array
+// (kNoAllocMaxPanels * 192 bytes, about 3 MB) until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t kNoAllocMaxPanels = 16384;  // body + wake panels per call
+static __device__ __align__(256) double g_noalloc_records[kNoAllocMaxPanels * R_STRIDE];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kMaxDevices] = {nullptr};
+
+// Device address of the array on the current device.  The array's host-side name
+// is only a stand-in, so the address is looked up once per device, with that
+// device current.
+cudaError_t noalloc_scratch(double** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        double* p = nullptr;
+        e = cudaGetSymbolAddress((void**)&p, g_noalloc_records);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int cpg_set_inf_coeff_noalloc(const double* body_verts, int64_t n, const double* wake_verts,
+                                         const int32_t* wake_idx4, const double* wake_coef, int64_t nw,
+                                         double* A, double* B, void* stream) {
+    if (n < 1 || nw < 0 || n + nw > kNoAllocMaxPanels) return CPG_E_INVALID;
+    if (!body_verts || !A || !B || (nw > 0 && (!wake_verts || !wake_idx4 || !wake_coef))) return CPG_E_INVALID;
+    cudaStream_t s = (cudaStream_t)stream;
+    double* rec = nullptr;
+    if (noalloc_scratch(&rec) != cudaSuccess) return CPG_E_CUDA;
+    double* wrec = rec + n * R_STRIDE;
+    // every record the kernels read is rewritten here, so no clearing is needed
+    k_pack_records<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(body_verts, n, rec);
+    if (nw > 0) k_pack_records<<<(unsigned)((nw + 127) / 128), 128, 0, s>>>(wake_verts, nw, wrec);
+    int64_t ch = chunk_for(n);
+    dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
+    k_assemble_fp64<<<grid, TI, 0, s>>>(rec, n, ch, A, B, nullptr);
+    if (nw > 0)
+        k_wake_columns<double><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, wake_idx4, wake_coef, n, nw, A);
+    return cudaGetLastError() == cudaSuccess ? CPG_OK : CPG_E_CUDA;
+}

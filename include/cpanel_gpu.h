@@ -127,6 +127,23 @@ int  cpg_set_inf_coeff(cpg_geometry* g, int precision);
 int  cpg_get_A(cpg_geometry* g, double* host);
 int  cpg_get_B(cpg_geometry* g, double* host);
 
+/* Allocation-free FP64 assembly.  No counterpart in the reference: it exists for
+ * callers that may not allocate device memory while the path runs (a host that
+ * records the assembly into a CUDA graph, a plug-in confined to another solver's
+ * memory pool, a real-time loop that forbids allocation after start-up).
+ * Inputs and outputs are caller-owned DEVICE arrays in matrix order: body_verts
+ * n x 9, wake_verts nw x 9 (wPanels order), wake_idx4 nw x 4 and wake_coef nw (the
+ * tables cpg_geometry_tables / cpg_topology return), A and B n x n column-major.
+ * The packed panel records live in a fixed per-device array of 16,384 panels
+ * (n + nw <= 16384; larger sizes return CPG_E_INVALID, about 3 MB held by every GPU
+ * that loads the library).  The first call on a device looks the array's address
+ * up (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the one array, so calls whose work overlaps on the GPU race:
+ * serialize them (one stream, or events).  stream: cudaStream_t, 0 = default. */
+int  cpg_set_inf_coeff_noalloc(const double* body_verts, int64_t n, const double* wake_verts,
+                               const int32_t* wake_idx4, const double* wake_coef, int64_t nw, double* A,
+                               double* B, void* stream);
+
 /* ---- steady cases (cpCase::run) over k flow conditions on one geometry ----
  * Assembles first if the geometry holds no matrix of that precision. */
 int  cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_refs* refs, int precision,

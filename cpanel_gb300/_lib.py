@@ -29,7 +29,7 @@ class GeometryInfo(C.Structure):
                 ("n_tip", C.c_int64), ("n_nodes", C.c_int64), ("h2d_bytes", C.c_int64)]
 
 
-PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "lu_panel", "lu_gemm",
+PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "lu_factor", "unused",
                 "chtls", "post", "lu_solve"]
 
 

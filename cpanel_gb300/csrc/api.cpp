@@ -76,6 +76,7 @@ struct cpg_geometry {
     DevBuf rec, frec, bez, clp, cli, tip, ts, wrec, widx, wcoef, tzst, tzln, tzpts, G, F3, F2, mode;
     DevBuf A64, B64, A32, Alo, rb, count;
     DevBuf LU, bad;
+    cpg::LuGraphs graphs;
     bool lu_ready = false;
     DevBuf work, post_work, cases, outs;
     bool have64 = false, have32 = false, post_ready = false;
@@ -297,6 +298,7 @@ void cpg_geometry_destroy(cpg_geometry* g) {
                       &g->B64, &g->A32, &g->Alo, &g->rb, &g->LU, &g->bad, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
     // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
+    g->graphs.release();
     delete g;
 }
 
@@ -502,13 +504,15 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
             CK(g->bad.ensure(sizeof(int)), "alloc flag");
             CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
             CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");
-            CK(cpg::lu_factor_fp32(ctx->blas, g->LU.as<float>(), n, g->bad.as<int>(), s), "LU factorization");
+            CK(cpg::lu_factor_fp32(ctx->blas, &g->graphs, g->LU.as<float>(), n, g->bad.as<int>(), s),
+               "LU factorization");
             g->lu_ready = true;
         }
         size_t wb = cpg::solve_lu_work_bytes(n, k);
         CK(g->work.ensure(wb), "alloc solver workspace");
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
-        CK(cpg::solve_lu_refined(ctx->blas, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(), n, k, rhs, mu,
+        CK(cpg::solve_lu_refined(ctx->blas, &g->graphs, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(),
+                                 n, k, rhs, mu,
                                  g->work.p, 1e-12, 8, &st, s),
            "refined solve (mixed)");
     }

@@ -11,7 +11,7 @@ namespace cpg {
 // stream).  Enabled per context; the API entry points install it for the calling
 // thread for the duration of a call.
 struct Prof {
-    enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, LU_PANEL, LU_GEMM, CHTLS, POST,
+    enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, LU_FACTOR, RESERVED6, CHTLS, POST,
            LU_SOLVE, NCLS };
     struct Pair {
         cudaEvent_t a, b;
@@ -75,13 +75,29 @@ double measure_fp64_tflops(cudaStream_t s);
 cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, double* dd, double* host, cudaStream_t s);
 
 // lu.cu: FP32 LU without pivoting (blocked, cuBLAS trailing GEMM) and the refined
-// solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.
-cudaError_t lu_factor_fp32(void* blas, float* LU, int64_t n, int* bad, cudaStream_t s);
-cudaError_t lu_solve_fp32(void* blas, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
+// solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.  The blocked
+// loops are captured once into CUDA graphs held in LuGraphs and replayed.
+struct LuGraphs {
+    cudaGraphExec_t factor = nullptr, solve = nullptr;
+    const float* factor_LU = nullptr;
+    int64_t factor_n = 0;
+    const float* solve_LU = nullptr;
+    const float* solve_X = nullptr;
+    int solve_k = 0;
+    void* workspace = nullptr;  // cuBLAS workspace (no allocation inside a capture)
+    float* dinv = nullptr;      // inverses of the diagonal blocks (L then U per block)
+    float* panel = nullptr;     // n x 128 staging for the panel GEMMs
+    float* tmp = nullptr;       // 128 x k staging for the substitutions
+    size_t tmp_floats = 0;
+    void release();
+};
+cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);
+cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
 size_t solve_lu_work_bytes(int64_t n, int k);
-cudaError_t solve_lu_refined(void* blas, const float* A32, const float* Alo, const float* LU, int64_t n, int k,
-                             const double* rhs, double* x, void* work, double tol, int max_steps, SolveStats* st,
-                             cudaStream_t s);
+cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n,
+                             int k, const double* rhs, double* x, void* work, double tol, int max_steps,
+                             SolveStats* st, cudaStream_t s);
+
 // y(k x n) = alpha * M x(k x n) for column-major FP64 M (used for -B sigma).
 cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, double* y, double alpha, void* work,
                          cudaStream_t s);

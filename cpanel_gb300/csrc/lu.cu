@@ -22,112 +22,69 @@ namespace {
 constexpr int NB = 128;   // panel width
 constexpr int P = NB + 1; // padded smem pitch (no bank conflicts on row access)
 
-// In-place LU (unit lower L, upper U) of the b x b block at A + K*n + K.
-__global__ void __launch_bounds__(1024) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b, int* bad) {
-    extern __shared__ float S[];  // S[r*P + c]
-    const int tx = threadIdx.x, ty = threadIdx.y;
-    for (int r = ty; r < b; r += 32)
-        for (int c = tx; c < b; c += 32) S[r * P + c] = A[(K + c) * n + K + r];
+// In-place LU (unit lower L, upper U) of the b x b block at A + K*n + K, then the
+// inverses of both triangles into Dinv (L11^{-1} then U11^{-1}, column-major,
+// ld NB).  Thread t owns row t during the factorization and column t during the
+// inversions; one cheap 128-thread barrier per factorization step.
+__global__ void __launch_bounds__(NB) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
+                                                float* __restrict__ Dinv, int* bad) {
+    extern __shared__ float sm[];
+    float* S = sm;           // S[r*P + c]
+    float* Z = sm + NB * P;  // Z[c*P + i]
+    const int t = threadIdx.x;
+    for (int c = 0; c < b; c++)
+        if (t < b) S[t * P + c] = A[(K + c) * n + K + t];
     __syncthreads();
     for (int j = 0; j < b; j++) {
         float piv = S[j * P + j];
         if (piv == 0.f) {
-            if (tx == 0 && ty == 0) atomicExch(bad, 1);
+            if (t == 0) atomicExch(bad, 1);
             piv = 1.f;
         }
-        for (int r = j + 1 + ty * 32 + tx; r < b; r += 1024) S[r * P + j] = S[r * P + j] / piv;
-        __syncthreads();
-        for (int r = j + 1 + ty; r < b; r += 32) {
-            float l = S[r * P + j];
-            for (int c = j + 1 + tx; c < b; c += 32) S[r * P + c] = __fmaf_rn(-l, S[j * P + c], S[r * P + c]);
-        }
-        __syncthreads();
-    }
-    for (int r = ty; r < b; r += 32)
-        for (int c = tx; c < b; c += 32) A[(K + c) * n + K + r] = S[r * P + c];
-}
-
-// L21 = A21 * U11^{-1}: one thread per row below the diagonal block.
-__global__ void __launch_bounds__(128) k_trsm_rows(float* __restrict__ A, int64_t n, int64_t K, int b) {
-    extern __shared__ float sm[];
-    float* U = sm;            // U[i*P + j]
-    float* X = sm + NB * P;   // X[t*P + j]
-    const int t = threadIdx.x;
-    int64_t row0 = K + b + (int64_t)blockIdx.x * 128;
-    for (int i = 0; i < b; i++)
-        for (int j = t; j < b; j += 128) U[i * P + j] = A[(K + j) * n + K + i];
-    int64_t row = row0 + t;
-    bool act = row < n;
-    for (int j = 0; j < b; j++) X[t * P + j] = act ? A[(K + j) * n + row] : 0.f;
-    __syncthreads();
-    if (act) {
-        for (int j = 0; j < b; j++) {
-            float s = X[t * P + j];
-            for (int i = 0; i < j; i++) s = __fmaf_rn(-X[t * P + i], U[i * P + j], s);
-            X[t * P + j] = s / U[j * P + j];
-        }
-        for (int j = 0; j < b; j++) A[(K + j) * n + row] = X[t * P + j];
-    }
-}
-
-// U12 = L11^{-1} * A12 (unit lower): one thread per column right of the block.
-__global__ void __launch_bounds__(128) k_trsm_cols(float* __restrict__ A, int64_t n, int64_t K, int b) {
-    extern __shared__ float sm[];
-    float* L = sm;            // L[i*P + j]
-    float* Y = sm + NB * P;   // Y[t*P + i] = row i of column t
-    const int t = threadIdx.x;
-    int64_t col0 = K + b + (int64_t)blockIdx.x * 128;
-    for (int j = 0; j < b; j++)
-        for (int i = t; i < b; i += 128) L[i * P + j] = A[(K + j) * n + K + i];
-    for (int tt = 0; tt < 128; tt++) {
-        int64_t col = col0 + tt;
-        for (int i = t; i < b; i += 128) Y[tt * P + i] = col < n ? A[col * n + K + i] : 0.f;
-    }
-    __syncthreads();
-    int64_t col = col0 + t;
-    if (col < n)
-        for (int i = 0; i < b; i++) {
-            float s = Y[t * P + i];
-            for (int j = 0; j < i; j++) s = __fmaf_rn(-L[i * P + j], Y[t * P + j], s);
-            Y[t * P + i] = s;
-        }
-    __syncthreads();
-    for (int tt = 0; tt < 128; tt++) {
-        int64_t c2 = col0 + tt;
-        if (c2 < n)
-            for (int i = t; i < b; i += 128) A[c2 * n + K + i] = Y[tt * P + i];
-    }
-}
-
-// Diagonal-block triangular solve for k right-hand sides (X: n x k column-major,
-// ld n).  lower: unit lower L_KK, forward; else upper U_KK, backward.  One warp
-// per right-hand side; each row's dot product is a warp reduction.
-__global__ void __launch_bounds__(1024) k_tri_diag(const float* __restrict__ A, int64_t n, int64_t K, int b,
-                                                   float* __restrict__ X, int k, int lower) {
-    extern __shared__ float T[];  // T[i*P + j]
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int i = w; i < b; i += nw)
-        for (int j = lane; j < b; j += 32) T[i * P + j] = A[(K + j) * n + K + i];
-    __syncthreads();
-    for (int c = w + blockIdx.x * nw; c < k; c += nw * gridDim.x) {
-        float* x = X + (int64_t)c * n + K;
-        if (lower) {
-            for (int i = 0; i < b; i++) {
-                float s = 0.f;
-                for (int j = lane; j < i; j += 32) s = __fmaf_rn(T[i * P + j], x[j], s);
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) x[i] -= s;
-                __syncwarp();
+        if (t > j && t < b) {
+            float l = S[t * P + j] / piv;
+            S[t * P + j] = l;
+            int c = j + 1;
+            for (; c + 3 < b; c += 4) {
+                float u0 = S[j * P + c], u1 = S[j * P + c + 1], u2 = S[j * P + c + 2], u3 = S[j * P + c + 3];
+                S[t * P + c] = __fmaf_rn(-l, u0, S[t * P + c]);
+                S[t * P + c + 1] = __fmaf_rn(-l, u1, S[t * P + c + 1]);
+                S[t * P + c + 2] = __fmaf_rn(-l, u2, S[t * P + c + 2]);
+                S[t * P + c + 3] = __fmaf_rn(-l, u3, S[t * P + c + 3]);
             }
-        } else {
-            for (int i = b - 1; i >= 0; i--) {
-                float s = 0.f;
-                for (int j = i + 1 + lane; j < b; j += 32) s = __fmaf_rn(T[i * P + j], x[j], s);
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) x[i] = (x[i] - s) / T[i * P + i];
-                __syncwarp();
-            }
+            for (; c < b; c++) S[t * P + c] = __fmaf_rn(-l, S[j * P + c], S[t * P + c]);
         }
+        __syncthreads();
+    }
+    for (int c = 0; c < b; c++)
+        if (t < b) A[(K + c) * n + K + t] = S[t * P + c];
+    float* Li = Dinv + (K / NB) * 2 * NB * NB;
+    float* Ui = Li + NB * NB;
+    if (t < b) {
+        for (int i = 0; i < b; i++) {  // L z = e_t (unit lower)
+            float s0 = i == t ? 1.f : 0.f, s1 = 0.f;
+            int j = t;
+            for (; j + 1 < i; j += 2) {
+                s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
+                s1 = __fmaf_rn(-S[i * P + j + 1], Z[t * P + j + 1], s1);
+            }
+            if (j < i) s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
+            Z[t * P + i] = i < t ? 0.f : s0 + s1;
+        }
+        for (int i = 0; i < b; i++) Li[t * NB + i] = Z[t * P + i];
+        for (int i = b - 1; i >= 0; i--) {  // U z = e_t
+            float s0 = i == t ? 1.f : 0.f, s1 = 0.f;
+            if (i <= t) {
+                int j = i + 1;
+                for (; j + 1 <= t; j += 2) {
+                    s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
+                    s1 = __fmaf_rn(-S[i * P + j + 1], Z[t * P + j + 1], s1);
+                }
+                if (j <= t) s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
+            }
+            Z[t * P + i] = i > t ? 0.f : (s0 + s1) / S[i * P + i];
+        }
+        for (int i = 0; i < b; i++) Ui[t * NB + i] = Z[t * P + i];
     }
 }
 
@@ -145,10 +102,7 @@ inline unsigned nb256(int64_t m) { return (unsigned)((m + 255) / 256); }
 bool g_attr_set = false;
 void set_attrs() {
     if (g_attr_set) return;
-    cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, NB * P * 4);
-    cudaFuncSetAttribute(k_trsm_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * NB * P * 4);
-    cudaFuncSetAttribute(k_trsm_cols, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * NB * P * 4);
-    cudaFuncSetAttribute(k_tri_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, NB * P * 4);
+    cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * NB * P * 4);
     g_attr_set = true;
 }
 
@@ -162,64 +116,177 @@ cublasComputeType_t lu_compute() {
 
 namespace cpg {
 
-cudaError_t lu_factor_fp32(void* blas, float* LU, int64_t n, int* bad, cudaStream_t s) {
-    set_attrs();
-    cublasHandle_t h = (cublasHandle_t)blas;
-    cublasSetStream(h, s);
-    const float one = 1.f, mone = -1.f;
+namespace {
+
+// The blocked loops below issue ~4 launches (plus cuBLAS calls) per 128 columns;
+// replayed from a CUDA graph they run back to back on the device instead of
+// waiting on the host.  cuBLAS gets a fixed workspace so that it never allocates
+// while a stream is being captured.
+constexpr size_t kBlasWorkspace = size_t(256) << 20;
+
+cudaError_t prepare_blas(cublasHandle_t h, LuGraphs* G, cudaStream_t s) {
+    if (!G->workspace) {
+        cudaError_t e = cudaMalloc(&G->workspace, kBlasWorkspace);
+        if (e != cudaSuccess) return e;
+    }
+    if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+    if (cublasSetWorkspace(h, G->workspace, kBlasWorkspace) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+    return cudaSuccess;
+}
+
+cudaError_t factor_body(cublasHandle_t h, float* LU, float* Dinv, float* W, int64_t n, int* bad, cudaStream_t s) {
+    const float one = 1.f, mone = -1.f, zero = 0.f;
     cublasComputeType_t ct = lu_compute();
     for (int64_t K = 0; K < n; K += NB) {
         int b = (int)std::min<int64_t>(NB, n - K);
-        {
-            ProfScope ps(Prof::LU_PANEL, s);
-            k_lu_diag<<<1, dim3(32, 32), NB * P * 4, s>>>(LU, n, K, b, bad);
-            int64_t rest = n - K - b;
-            if (rest > 0) {
-                unsigned g = (unsigned)((rest + 127) / 128);
-                k_trsm_rows<<<g, 128, 2 * NB * P * 4, s>>>(LU, n, K, b);
-                k_trsm_cols<<<g, 128, 2 * NB * P * 4, s>>>(LU, n, K, b);
-            }
-        }
+        const float* Li = Dinv + (K / NB) * 2 * NB * NB;
+        const float* Ui = Li + NB * NB;
+        k_lu_diag<<<1, NB, 2 * NB * P * 4, s>>>(LU, n, K, b, Dinv, bad);
         int64_t rest = n - K - b;
-        if (rest > 0) {
-            ProfScope ps(Prof::LU_GEMM, s);
-            cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, (int)rest, b, &mone,
-                                             LU + K * n + K + b, CUDA_R_32F, (int)n, LU + (K + b) * n + K,
-                                             CUDA_R_32F, (int)n, &one, LU + (K + b) * n + K + b, CUDA_R_32F, (int)n,
-                                             ct, CUBLAS_GEMM_DEFAULT);
-            if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+        if (rest <= 0) continue;
+        // L21 = A21 U11^{-1} and U12 = L11^{-1} A12 as GEMMs into W, copied back
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, b, b, &one, LU + K * n + K + b, (int)n, Ui, NB, &zero,
+                        W, (int)rest) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        cudaError_t e = cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float),
+                                          rest * sizeof(float), b, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)rest, b, &one, Li, NB, LU + (K + b) * n + K, (int)n,
+                        &zero, W, b) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        e = cudaMemcpy2DAsync(LU + (K + b) * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), rest,
+                              cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+        cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, (int)rest, b, &mone,
+                                         LU + K * n + K + b, CUDA_R_32F, (int)n, LU + (K + b) * n + K, CUDA_R_32F,
+                                         (int)n, &one, LU + (K + b) * n + K + b, CUDA_R_32F, (int)n, ct,
+                                         CUBLAS_GEMM_DEFAULT);
+        if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+    }
+    return cudaGetLastError();
+}
+
+// Blocked forward and backward substitution with the diagonal-block inverses:
+// per block, T = inv(D_KK) x_K (small GEMM), x_K <- T, then the rows block K feeds
+// are updated by one GEMM.
+cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int64_t n, float* X, float* T, int k,
+                       cudaStream_t s) {
+    const float one = 1.f, mone = -1.f, zero = 0.f;
+    const int64_t nblk = (n + NB - 1) / NB;
+    for (int64_t q = 0; q < 2 * nblk; q++) {
+        bool fwd = q < nblk;
+        int64_t blk = fwd ? q : 2 * nblk - 1 - q;
+        int64_t K = blk * NB;
+        int b = (int)std::min<int64_t>(NB, n - K);
+        const float* Di = Dinv + blk * 2 * NB * NB + (fwd ? 0 : NB * NB);
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, k, b, &one, Di, NB, X + K, (int)n, &zero, T, b) !=
+            CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        cudaError_t e = cudaMemcpy2DAsync(X + K, n * sizeof(float), T, b * sizeof(float), b * sizeof(float), k,
+                                          cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) return e;
+        if (fwd) {
+            int64_t rest = n - K - b;
+            if (rest > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, b, &mone, LU + K * n + K + b,
+                                        (int)n, T, b, &one, X + K + b, (int)n) != CUBLAS_STATUS_SUCCESS)
+                return cudaErrorUnknown;
+        } else if (K > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, b, &mone, LU + K * n, (int)n, T, b,
+                                        &one, X, (int)n) != CUBLAS_STATUS_SUCCESS) {
+            return cudaErrorUnknown;
         }
     }
     return cudaGetLastError();
 }
 
-// X (n x k, ld n) <- U^{-1} L^{-1} X
-cudaError_t lu_solve_fp32(void* blas, const float* LU, int64_t n, float* X, int k, cudaStream_t s) {
+// Capture body() on s into a graph (no profiler events inside the capture).
+template <class F>
+cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body) {
+    Prof* saved = g_prof;
+    g_prof = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        g_prof = saved;
+        return e;
+    }
+    cudaError_t eb = body();
+    cudaGraph_t graph = nullptr;
+    e = cudaStreamEndCapture(s, &graph);
+    g_prof = saved;
+    if (eb != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return eb;
+    }
+    if (e != cudaSuccess) return e;
+    e = cudaGraphInstantiate(out, graph, 0);
+    cudaGraphDestroy(graph);
+    return e;
+}
+
+}  // namespace
+
+void LuGraphs::release() {
+    if (factor) cudaGraphExecDestroy(factor);
+    if (solve) cudaGraphExecDestroy(solve);
+    if (workspace) cudaFree(workspace);
+    if (dinv) cudaFree(dinv);
+    if (panel) cudaFree(panel);
+    if (tmp) cudaFree(tmp);
+    factor = solve = nullptr;
+    workspace = nullptr;
+    dinv = panel = tmp = nullptr;
+    tmp_floats = 0;
+    solve_X = nullptr;
+    solve_k = 0;
+    factor_LU = nullptr;
+}
+
+cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s) {
     set_attrs();
     cublasHandle_t h = (cublasHandle_t)blas;
-    cublasSetStream(h, s);
-    const float one = 1.f, mone = -1.f;
-    int warps = std::min(32, std::max(1, k));
+    cudaError_t e = prepare_blas(h, G, s);
+    if (e != cudaSuccess) return e;
+    if (!G->factor || G->factor_LU != LU || G->factor_n != n) {
+        if (G->factor) cudaGraphExecDestroy(G->factor);
+        G->factor = nullptr;
+        if (G->dinv) cudaFree(G->dinv);
+        if (G->panel) cudaFree(G->panel);
+        G->dinv = G->panel = nullptr;
+        size_t nb = (size_t)((n + NB - 1) / NB);
+        if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&G->panel, sizeof(float) * (size_t)n * NB)) != cudaSuccess) return e;
+        e = capture(s, &G->factor, [&] { return factor_body(h, LU, G->dinv, G->panel, n, bad, s); });
+        if (e != cudaSuccess) return e;
+        G->factor_LU = LU;
+        G->factor_n = n;
+    }
+    ProfScope ps(Prof::LU_FACTOR, s);
+    return cudaGraphLaunch(G->factor, s);
+}
+
+// X (n x k, ld n) <- U^{-1} L^{-1} X
+cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s) {
+    set_attrs();
+    cublasHandle_t h = (cublasHandle_t)blas;
+    cudaError_t e = prepare_blas(h, G, s);
+    if (e != cudaSuccess) return e;
+    if (!G->dinv) return cudaErrorInvalidValue;  // factor first
+    if (!G->solve || G->solve_X != X || G->solve_k != k || G->solve_LU != LU) {
+        if (G->solve) cudaGraphExecDestroy(G->solve);
+        G->solve = nullptr;
+        if (G->tmp_floats < (size_t)NB * k) {
+            if (G->tmp) cudaFree(G->tmp);
+            G->tmp = nullptr;
+            if ((e = cudaMalloc(&G->tmp, sizeof(float) * NB * k)) != cudaSuccess) return e;
+            G->tmp_floats = (size_t)NB * k;
+        }
+        e = capture(s, &G->solve, [&] { return solve_body(h, LU, G->dinv, n, X, G->tmp, k, s); });
+        if (e != cudaSuccess) return e;
+        G->solve_X = X;
+        G->solve_k = k;
+        G->solve_LU = LU;
+    }
     ProfScope ps(Prof::LU_SOLVE, s);
-    for (int64_t K = 0; K < n; K += NB) {  // forward: L y = x
-        int b = (int)std::min<int64_t>(NB, n - K);
-        k_tri_diag<<<1, 32 * warps, NB * P * 4, s>>>(LU, n, K, b, X, k, 1);
-        int64_t rest = n - K - b;
-        if (rest > 0 &&
-            cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, b, &mone, LU + K * n + K + b, (int)n, X + K,
-                        (int)n, &one, X + K + b, (int)n) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-    }
-    int64_t last = ((n - 1) / NB) * NB;
-    for (int64_t K = last; K >= 0; K -= NB) {  // backward: U x = y
-        int b = (int)std::min<int64_t>(NB, n - K);
-        k_tri_diag<<<1, 32 * warps, NB * P * 4, s>>>(LU, n, K, b, X, k, 0);
-        if (K > 0 &&
-            cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, b, &mone, LU + K * n, (int)n, X + K, (int)n, &one, X,
-                        (int)n) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-    }
-    return cudaGetLastError();
+    return cudaGraphLaunch(G->solve, s);
 }
 
 size_t solve_lu_work_bytes(int64_t n, int k) {
@@ -228,9 +295,9 @@ size_t solve_lu_work_bytes(int64_t n, int k) {
            sizeof(double) * (size_t)residual_chunks(n) * 17 * (size_t)n + 64 * 1024;
 }
 
-cudaError_t solve_lu_refined(void* blas, const float* A32, const float* Alo, const float* LU, int64_t n, int k,
-                             const double* rhs, double* x, void* work, double tol, int max_steps, SolveStats* st,
-                             cudaStream_t s) {
+cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n,
+                             int k, const double* rhs, double* x, void* work, double tol, int max_steps,
+                             SolveStats* st, cudaStream_t s) {
     char* p = (char*)work;
     auto take = [&](size_t bytes) {
         char* r = p;
@@ -253,7 +320,7 @@ cudaError_t solve_lu_refined(void* blas, const float* A32, const float* Alo, con
     int steps = 0;
     for (; steps < max_steps; steps++) {
         k_d2f<<<nb256(kn), 256, 0, s>>>(r64, d32, kn);
-        if ((e = lu_solve_fp32(blas, LU, n, d32, k, s)) != cudaSuccess) return e;
+        if ((e = lu_solve_fp32(blas, G, LU, n, d32, k, s)) != cudaSuccess) return e;
         k_addf<<<nb256(kn), 256, 0, s>>>(x, d32, kn);
         if ((e = residual_df(A32, Alo, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;
         if ((e = column_norms2(r64, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;

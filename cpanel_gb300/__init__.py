@@ -34,6 +34,10 @@ def _mark_shutdown():
     _shutting_down = True
 
 
+def _shutting_down_now():
+    return _shutting_down or sys.is_finalizing()
+
+
 _PREC = {"fp64": PLAIN_FP64, "plain": PLAIN_FP64, PLAIN_FP64: PLAIN_FP64, "mixed": MIXED, MIXED: MIXED}
 
 

@@ -29,7 +29,7 @@ class GeometryInfo(C.Structure):
                 ("n_tip", C.c_int64), ("n_nodes", C.c_int64), ("h2d_bytes", C.c_int64)]
 
 
-PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "lu_factor", "unused",
+PROF_CLASSES = ["assembly", "wake_columns", "matvec_fp32", "matvec_fp64", "residual", "lu_factor", "particles",
                 "chtls", "post", "lu_solve"]
 
 
@@ -62,7 +62,18 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_geometry_create", "cpg_geometry_destroy", "cpg_geometry_info_get", "cpg_geometry_tables", "cpg_topology",
            "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
            "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read",
-           "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak"]
+           "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak",
+           # cpanel_vp.h
+           "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
+           "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_particles_velocity", "cpg_particles_stretch_diff",
+           "cpg_panels_velocity"]
+
+VEL_GAUSS_SYM, VEL_GAUSS, VEL_ALG = 1, 2, 3
+
+
+class PTreeInfo(C.Structure):
+    _fields_ = [("n_particles", C.c_int64), ("n_nodes", C.c_int64), ("n_leaves", C.c_int64),
+                ("n_levels", C.c_int64)]
 
 
 def load():
@@ -100,5 +111,16 @@ def load():
     L.cpg_prof_read.argtypes = [vp, C.POINTER(Prof)]
     L.cpg_measure_fp64_peak.argtypes = [vp, D]
     L.cpg_set_inf_coeff_noalloc.argtypes = [vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp, vp]
+    L.cpg_ptree_build.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int64, C.c_double, C.POINTER(vp)]
+    L.cpg_ptree_destroy.argtypes = [vp]
+    L.cpg_ptree_destroy.restype = None
+    L.cpg_ptree_info_get.argtypes = [vp, C.POINTER(PTreeInfo)]
+    L.cpg_ptree_table.argtypes = [vp, D, I64]
+    L.cpg_ptree_host_table.argtypes = [D, D, D, C.c_int64, C.c_int64, D, C.c_int64, I64, C.POINTER(PTreeInfo)]
+    L.cpg_bh_velocity_points.argtypes = [vp, vp, C.c_int64, vp]
+    L.cpg_bh_particles.argtypes = [vp, vp, vp, vp]
+    L.cpg_particles_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
+    L.cpg_particles_stretch_diff.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp]
+    L.cpg_panels_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, C.c_int64, vp]
     _lib = L
     return L

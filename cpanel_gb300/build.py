@@ -20,14 +20,15 @@ NVCC = os.path.join(CUDA, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_STRICT = ["assemble.cu", "post.cu"]   # FP64 panel math: no contraction
-CU_FAST = ["solve.cu", "lu.cu"]
-CPP = ["mesh.cpp", "api.cpp"]
-HEADERS = ["common.cuh", "panel64.cuh", "df.cuh", "assemble.h", "post.h", "mesh.h"]
+CU_FAST = ["solve.cu", "lu.cu", "particles.cu"]  # particles.cu rounds its branch tests explicitly
+CPP = ["mesh.cpp", "api.cpp", "octree.cpp"]
+HEADERS = ["common.cuh", "panel64.cuh", "df.cuh", "assemble.h", "post.h", "mesh.h", "octree.h", "particles.h"]
 
 
 def _sources():
     return [os.path.join(SRC, f) for f in CU_STRICT + CU_FAST + CPP + HEADERS] + [
-        os.path.join(ROOT, "include", "cpanel_gpu.h"), os.path.abspath(__file__)]
+        os.path.join(ROOT, "include", "cpanel_gpu.h"), os.path.join(ROOT, "include", "cpanel_vp.h"),
+        os.path.abspath(__file__)]
 
 
 def _stale():

@@ -14,8 +14,11 @@
 #include <vector>
 
 #include "../../include/cpanel_gpu.h"
+#include "../../include/cpanel_vp.h"
 #include "assemble.h"
 #include "mesh.h"
+#include "octree.h"
+#include "particles.h"
 #include "post.h"
 
 struct cpg_ctx {
@@ -84,6 +87,12 @@ struct cpg_geometry {
     int64_t n_near64 = 0, n_near32 = 0;
     cpg::PostTables T;
     float ms_asm = 0;
+};
+
+struct cpg_ptree {
+    cpg_ctx* ctx = nullptr;
+    cpg::ParticleTree T;
+    DevBuf nodes, parts;
 };
 
 namespace {
@@ -628,5 +637,196 @@ int cpg_measure_fp64_peak(cpg_ctx* ctx, double* tflops) {
 }
 
 int cpg_compiled_arch(void) { return CPG_COMPILED_ARCH; }
+
+/* ------------------------------------------------ vortex-particle operators */
+
+int cpg_ptree_build(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius, int64_t n,
+                    int64_t max_members, double theta, cpg_ptree** out) {
+    if (!ctx || !out || n < 0 || max_members < 1 || !(theta > 0) || (n > 0 && (!pos || !strength || !radius)))
+        return fail(ctx, CPG_E_INVALID, "bad argument");
+    if (n > (int64_t)INT32_MAX / 2) return fail(ctx, CPG_E_INVALID, "too many particles");
+    *out = nullptr;
+    cpg_ptree* t = new (std::nothrow) cpg_ptree();
+    if (!t) return fail(ctx, CPG_E_OOM, "host allocation");
+    t->ctx = ctx;
+    cudaStream_t s = ctx->stream;
+    std::vector<double> hp(3 * n), hs(3 * n), hr(n);
+    if (n > 0) {
+        cudaError_t e = cudaMemcpyAsync(hp.data(), pos, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(hs.data(), strength, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(hr.data(), radius, sizeof(double) * n, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            delete t;
+            return cuda_fail(ctx, e, "particle download");
+        }
+    }
+    cpg::build_particle_tree(hp.data(), hs.data(), hr.data(), n, max_members, theta, t->T);
+    cudaError_t e = upload(t->nodes, t->T.nodes, s);
+    if (e == cudaSuccess) e = upload(t->parts, t->T.parts, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cpg_ptree_destroy(t);
+        return cuda_fail(ctx, e, "tree upload");
+    }
+    *out = t;
+    return CPG_OK;
+}
+
+void cpg_ptree_destroy(cpg_ptree* t) {
+    if (!t) return;
+    t->nodes.release();
+    t->parts.release();
+    delete t;
+}
+
+int cpg_ptree_info_get(const cpg_ptree* t, cpg_ptree_info* o) {
+    if (!t || !o) return CPG_E_INVALID;
+    o->n_particles = t->T.n;
+    o->n_nodes = (int64_t)t->T.nodes.size();
+    o->n_leaves = 0;
+    for (const auto& nd : t->T.nodes) o->n_leaves += nd.leaf ? 1 : 0;
+    o->n_levels = t->T.levels;
+    return CPG_OK;
+}
+
+int cpg_ptree_table(const cpg_ptree* t, double* nodes, int64_t* leaf_members) {
+    if (!t) return CPG_E_INVALID;
+    if (nodes) cpg::particle_tree_table(t->T, nodes);
+    if (leaf_members)
+        for (size_t q = 0; q < t->T.perm.size(); q++) leaf_members[q] = t->T.perm[q];
+    return CPG_OK;
+}
+
+int cpg_ptree_host_table(const double* pos, const double* strength, const double* radius, int64_t n,
+                         int64_t max_members, double* nodes, int64_t cap_nodes, int64_t* leaf_members,
+                         cpg_ptree_info* info) {
+    if (n < 0 || max_members < 1 || !info || (n > 0 && (!pos || !strength || !radius))) return CPG_E_INVALID;
+    if (n > (int64_t)INT32_MAX / 2) return CPG_E_INVALID;
+    cpg::ParticleTree T;
+    cpg::build_particle_tree(pos, strength, radius, n, max_members, 0.5, T);
+    info->n_particles = n;
+    info->n_nodes = (int64_t)T.nodes.size();
+    info->n_leaves = 0;
+    for (const auto& nd : T.nodes) info->n_leaves += nd.leaf ? 1 : 0;
+    info->n_levels = T.levels;
+    if (leaf_members)
+        for (int64_t q = 0; q < n; q++) leaf_members[q] = T.perm[q];
+    if (!nodes) return CPG_OK;
+    if (cap_nodes < info->n_nodes) return CPG_E_INVALID;
+    cpg::particle_tree_table(T, nodes);
+    return CPG_OK;
+}
+
+int cpg_bh_velocity_points(cpg_ptree* t, const double* pts, int64_t m, double* vel) {
+    if (!t) return CPG_E_INVALID;
+    cpg_ctx* ctx = t->ctx;
+    if (m < 0 || (m > 0 && (!pts || !vel))) return fail(ctx, CPG_E_INVALID, "bad argument");
+    if (m == 0) return CPG_OK;
+    ProfInstall pi(ctx);
+    int nn = (int)t->T.nodes.size();
+    if (nn <= 1) {  // the root alone: no children to visit, the reference returns zero
+        CK(cudaMemsetAsync(vel, 0, sizeof(double) * 3 * m, ctx->stream), "barnesHutVel");
+    } else {
+        cpg::ProfScope ps(cpg::Prof::PARTICLES, ctx->stream);
+        CK(cpg::launch_bh_points(t->nodes.as<cpg::BHNode>(), nn, t->parts.as<cpg::BHPart>(), t->T.theta, pts, m,
+                                 cpg::vp_constants(), vel, ctx->stream),
+           "barnesHutVel");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "barnesHutVel");
+    return CPG_OK;
+}
+
+int cpg_bh_particles(cpg_ptree* t, double* vel, double* stretch, double* diff) {
+    if (!t) return CPG_E_INVALID;
+    cpg_ctx* ctx = t->ctx;
+    int64_t n = t->T.n;
+    if (n == 0 || (!vel && !stretch && !diff)) return CPG_OK;
+    ProfInstall pi(ctx);
+    int nn = (int)t->T.nodes.size();
+    if (nn <= 1) {
+        for (double* o : {vel, stretch, diff})
+            if (o) CK(cudaMemsetAsync(o, 0, sizeof(double) * 3 * n, ctx->stream), "barnesHut");
+    } else {
+        cpg::ProfScope ps(cpg::Prof::PARTICLES, ctx->stream);
+        CK(cpg::launch_bh_particles(t->nodes.as<cpg::BHNode>(), nn, t->parts.as<cpg::BHPart>(), n, t->T.theta,
+                                    cpg::vp_constants(), vel, stretch, diff, ctx->stream),
+           "barnesHut");
+    }
+    CK(cudaStreamSynchronize(ctx->stream), "barnesHut");
+    return CPG_OK;
+}
+
+int cpg_particles_velocity(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius, int64_t n,
+                           const double* pts, int64_t m, int kernel, double* vel) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !strength || !radius))) return fail(ctx, CPG_E_INVALID, "bad argument");
+    if (kernel < CPG_VEL_GAUSS_SYM || kernel > CPG_VEL_ALG) return fail(ctx, CPG_E_INVALID, "unknown kernel");
+    if (!pts) m = n;
+    if (m < 0 || (m > 0 && !vel)) return fail(ctx, CPG_E_INVALID, "bad argument");
+    if (pts && kernel == CPG_VEL_GAUSS_SYM) return fail(ctx, CPG_E_INVALID, "symmetrised core needs particle targets");
+    if (m == 0) return CPG_OK;
+    ProfInstall pi(ctx);
+    cudaStream_t s = ctx->stream;
+    DevBuf parts;
+    CK(parts.ensure(sizeof(cpg::BHPart) * std::max<int64_t>(1, n)), "alloc particles");
+    CK(cpg::launch_pack_parts(pos, strength, radius, n, parts.as<cpg::BHPart>(), s), "pack particles");
+    {
+        cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
+        const cpg::BHPart* tg = pts ? nullptr : parts.as<cpg::BHPart>();
+        CK(cpg::launch_direct(kernel, false, false, parts.as<cpg::BHPart>(), n, tg, pts, m, cpg::vp_constants(), vel,
+                              nullptr, nullptr, s),
+           "particle velocity");
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    parts.release();
+    CK(e, "particle velocity");
+    return CPG_OK;
+}
+
+int cpg_particles_stretch_diff(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius,
+                               int64_t n, double* stretch, double* diff) {
+    if (!ctx || n < 0 || (n > 0 && (!pos || !strength || !radius))) return fail(ctx, CPG_E_INVALID, "bad argument");
+    if (n == 0 || (!stretch && !diff)) return CPG_OK;
+    ProfInstall pi(ctx);
+    cudaStream_t s = ctx->stream;
+    DevBuf parts;
+    CK(parts.ensure(sizeof(cpg::BHPart) * n), "alloc particles");
+    CK(cpg::launch_pack_parts(pos, strength, radius, n, parts.as<cpg::BHPart>(), s), "pack particles");
+    {
+        cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
+        CK(cpg::launch_direct(0, stretch != nullptr, diff != nullptr, parts.as<cpg::BHPart>(), n,
+                              parts.as<cpg::BHPart>(), nullptr, n, cpg::vp_constants(), nullptr, stretch, diff, s),
+           "particle strength update");
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    parts.release();
+    CK(e, "particle strength update");
+    return CPG_OK;
+}
+
+int cpg_panels_velocity(cpg_ctx* ctx, const double* body_verts, const double* sigma, const double* mu, int64_t nb,
+                        const double* wake_verts, const double* wake_mu, int64_t nw, const double* pts, int64_t m,
+                        double* vel) {
+    if (!ctx || nb < 0 || nw < 0 || m < 0) return fail(ctx, CPG_E_INVALID, "bad argument");
+    if ((nb > 0 && (!body_verts || !sigma || !mu)) || (nw > 0 && (!wake_verts || !wake_mu)) ||
+        (m > 0 && (!pts || !vel)))
+        return fail(ctx, CPG_E_INVALID, "bad argument");
+    if (m == 0) return CPG_OK;
+    ProfInstall pi(ctx);
+    cudaStream_t s = ctx->stream;
+    DevBuf rec;
+    CK(rec.ensure(sizeof(double) * 24 * std::max<int64_t>(1, nb + nw)), "alloc panel records");
+    {
+        cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
+        CK(cpg::launch_panels_velocity(body_verts, sigma, mu, nb, wake_verts, wake_mu, nw, pts, m, rec.as<double>(),
+                                       vel, s),
+           "panel velocity");
+    }
+    cudaError_t e = cudaStreamSynchronize(s);
+    rec.release();
+    CK(e, "panel velocity");
+    return CPG_OK;
+}
 
 }  // extern "C"

@@ -11,6 +11,7 @@
 #include "assemble.h"
 #include "df.cuh"
 #include "panel64.cuh"
+#include "particles.h"
 
 namespace {
 
@@ -270,6 +271,52 @@ __global__ void k_pack_records(const double* __restrict__ verts, int64_t m, doub
     if (t < m) make_record(verts + 9 * t, rec + t * R_STRIDE);
 }
 
+// Panel-induced velocity at points (the panel terms of cpCaseVP::velocityInflFromEverything,
+// CPanel/cpCaseVP.cpp:713-731): sum_j sigma_j vSrc_j + mu_j vDub_j over body records
+// (bodyPanel::panelV, bodyPanel.cpp:122-130), then mu_w dubVInf over wake records
+// (wakePanel::panelV, wakePanel.cpp:89-92).  One thread per point; records are staged
+// through shared memory in tiles shared by the block.
+constexpr int PV_T = 128, PV_TILE = 64;
+__global__ void __launch_bounds__(PV_T) k_panels_velocity(const double* __restrict__ rec, const double* __restrict__ sigma,
+                                                          const double* __restrict__ mu, int64_t nb,
+                                                          const double* __restrict__ wmu, int64_t nw,
+                                                          const double* __restrict__ pts, int64_t m,
+                                                          double* __restrict__ vel) {
+    __shared__ double tile[PV_TILE * R_STRIDE];
+    __shared__ double ts[PV_TILE], tm[PV_TILE];
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = q < m;
+    dv3 poi = live ? ld3(pts + 3 * q) : mk3(0, 0, 0);
+    dv3 acc = mk3(0, 0, 0);
+    const int64_t tot = nb + nw;
+    for (int64_t b = 0; b < tot; b += PV_TILE) {
+        int lim = (int)((tot - b) < PV_TILE ? (tot - b) : PV_TILE);
+        __syncthreads();
+        for (int k = threadIdx.x; k < lim * R_STRIDE; k += PV_T) tile[k] = rec[b * R_STRIDE + k];
+        for (int k = threadIdx.x; k < lim; k += PV_T) {
+            int64_t j = b + k;
+            ts[k] = j < nb ? sigma[j] : 0.0;
+            tm[k] = j < nb ? mu[j] : wmu[j - nb];
+        }
+        __syncthreads();
+        if (!live) continue;
+        for (int k = 0; k < lim; k++) {
+            const double* r = tile + k * R_STRIDE;
+            if (b + k < nb) {
+                dv3 vs, vd;
+                panel_v_inf(r, poi, vs, vd);
+                acc = acc + (ts[k] * vs + tm[k] * vd);
+            } else {
+                acc = acc + tm[k] * dub_v_inf(r, poi);
+            }
+        }
+    }
+    if (!live) return;
+    vel[3 * q] = acc.x;
+    vel[3 * q + 1] = acc.y;
+    vel[3 * q + 2] = acc.z;
+}
+
 int64_t chunk_for(int64_t n) {
     // enough blocks in y to fill the 152 SMs several times over
     int64_t bx = (n + TI - 1) / TI;
@@ -284,6 +331,15 @@ int64_t chunk_for(int64_t n) {
 }  // namespace
 
 namespace cpg {
+
+cudaError_t launch_panels_velocity(const double* body_verts, const double* sigma, const double* mu, int64_t nb,
+                                   const double* wake_verts, const double* wmu, int64_t nw, const double* pts,
+                                   int64_t m, double* rec, double* vel, cudaStream_t s) {
+    if (nb > 0) k_pack_records<<<(unsigned)((nb + 127) / 128), 128, 0, s>>>(body_verts, nb, rec);
+    if (nw > 0) k_pack_records<<<(unsigned)((nw + 127) / 128), 128, 0, s>>>(wake_verts, nw, rec + nb * R_STRIDE);
+    if (m > 0) k_panels_velocity<<<(unsigned)((m + PV_T - 1) / PV_T), PV_T, 0, s>>>(rec, sigma, mu, nb, wmu, nw, pts, m, vel);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wrec, const int32_t* widx,
                                  const double* wcoef, int64_t nw, double* A, double* B,

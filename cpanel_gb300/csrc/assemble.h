@@ -11,7 +11,7 @@ namespace cpg {
 // stream).  Enabled per context; the API entry points install it for the calling
 // thread for the duration of a call.
 struct Prof {
-    enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, LU_FACTOR, RESERVED6, CHTLS, POST,
+    enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, LU_FACTOR, PARTICLES, CHTLS, POST,
            LU_SOLVE, NCLS };
     struct Pair {
         cudaEvent_t a, b;

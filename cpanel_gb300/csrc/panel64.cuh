@@ -121,3 +121,23 @@ __device__ __forceinline__ void panel_v_inf(const double* r, dv3 poi, dv3& vSrc,
     vDub = vd / CPG_FOUR_PI;
     vSrc = vs / CPG_FOUR_PI;
 }
+
+// panel::dubVInf, CPanel/panel.cpp:666-704 (wake triangles; the edge vector is p2 - p1)
+__device__ __forceinline__ dv3 dub_v_inf(const double* r, dv3 poi) {
+    dv3 c = ld3(r + R_C);
+    dv3 pjk = poi - c;
+    dv3 n = ld3(r + R_N);
+    double d = norm3(pjk);
+    if (d / r[R_LONG] > 5) {
+        double d3c = d * d * d;
+        return (r[R_AREA] * ((3 * dot3(pjk, n)) * pjk - (d * d) * n)) / (CPG_FOUR_PI * (d3c * d * d));
+    }
+    dv3 p[3] = {ld3(r + R_V0), ld3(r + R_V1), ld3(r + R_V2)};
+    dv3 vd = mk3(0, 0, 0);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        dv3 p1 = p[i], p2 = p[i == 2 ? 0 : i + 1];
+        vd = vd + vortex_v(poi - p1, poi - p2, p2 - p1);
+    }
+    return vd / CPG_FOUR_PI;
+}

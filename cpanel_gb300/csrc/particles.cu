@@ -1,0 +1,326 @@
+// Vortex-particle operators on the GPU: direct sums and Barnes-Hut traversals.
+//
+// Pair kernels (FP64) restate CPanel/particle.cpp:
+//   gauss_sym  particle::velInfl(particle*)   :42-58  (core sqrt((1.5 r_s)^2 + (1.5 r_t)^2)/sqrt 2)
+//   gauss_poi  particle::velInfl(POI)         :60-77  (core 1.5 r_s; zero at distance 0)
+//   alg        particle::velInflAlgSmooth     :31-38
+//   stretch    particle::vortexStretching     :80-118 (`this` = first argument)
+//   diffusion  particle::viscousDiffusion     :122-140 (`this` = first argument)
+// The Barnes-Hut traversal is node::calcVel/calcStretch/calcDiff (octree/include/
+// node.h:236-364) from the root's children (CPanel/particleFMM.cpp:65-116), made
+// stackless: nodes are stored in pre-order with a skip index past each subtree, so
+// "descend" is i+1 and "use the expansion" is skip[i], which visits nodes in the
+// reference's recursion order.  One traversal serves velocity, stretching and
+// diffusion together: all three take the same far-field decisions.
+//
+// Branch decisions (far field 2 half.x / |x_exp - x| < theta, stretching cut-off
+// |x_s - x_t| > 5 r_s, zero distance) are computed with explicitly rounded
+// intrinsics, so they match the host exactly although this file keeps FMA
+// contraction for the pair arithmetic.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "common.cuh"
+#include "octree.h"
+#include "particles.h"
+
+namespace cpg {
+namespace {
+
+struct Tgt {
+    dv3 x;
+    double r;
+    dv3 a;
+    double idx;
+};
+
+__device__ __forceinline__ double exact_norm(double dx, double dy, double dz) {
+    return __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz)));
+}
+
+__device__ __forceinline__ Tgt load_part(const BHPart& p) {
+    return Tgt{mk3(p.x, p.y, p.z), p.r, mk3(p.ax, p.ay, p.az), p.idx};
+}
+
+// (erf(rho/sqrt2)/(4 pi rho) - exp(-rho^2/2)/(2 pi)^1.5) / rho^2
+__device__ __forceinline__ double gauss_K(double rho, const VPConst& c) {
+    return (1.0 / (c.four_pi * rho) * erf(rho / c.sqrt2) - c.c15 * exp(-0.5 * rho * rho)) / (rho * rho);
+}
+
+__device__ __forceinline__ double sym_sigma(double rs, double rt, const VPConst& c) {
+    double a = 1.5 * rs, b = 1.5 * rt;
+    return sqrt(a * a + b * b) / c.sqrt2;
+}
+
+// velocity at target t induced by source s, symmetrised Gaussian core
+__device__ __forceinline__ dv3 vel_gauss_sym(const Tgt& s, const Tgt& t, const VPConst& c) {
+    double sig = sym_sigma(s.r, t.r, c);
+    dv3 d = t.x - s.x;
+    double rho = norm3(d) / sig;
+    double K = gauss_K(rho, c);
+    return (-1.0 / (sig * sig * sig) * K) * cross3(d, s.a);
+}
+
+// velocity at a point, Gaussian core 1.5 r_s, zero when the point is on the particle
+__device__ __forceinline__ dv3 vel_gauss_poi(const Tgt& s, dv3 poi, const VPConst& c) {
+    double ddx = s.x.x - poi.x, ddy = s.x.y - poi.y, ddz = s.x.z - poi.z;
+    if (exact_norm(ddx, ddy, ddz) == 0.0) return mk3(0, 0, 0);
+    double sig = 1.5 * s.r;
+    dv3 d = poi - s.x;
+    double rho = norm3(d) / sig;
+    double K = gauss_K(rho, c);
+    return (-1.0 / (sig * sig * sig) * K) * cross3(d, s.a);
+}
+
+// high-order algebraic core
+__device__ __forceinline__ dv3 vel_alg(const Tgt& s, dv3 poi, const VPConst& c) {
+    double sig = 1.5 * s.r;
+    dv3 d = poi - s.x;
+    double r2 = dot3(d, d);
+    double q = r2 + sig * sig;
+    double f = -c.inv_four_pi * (r2 + 2.5 * sig * sig) / (q * q * sqrt(q));
+    return f * cross3(d, s.a);
+}
+
+// particle::vortexStretching with this = P, part = Q
+__device__ __forceinline__ dv3 stretch(const Tgt& P, const Tgt& Q, const VPConst& c) {
+    double dx = P.x.x - Q.x.x, dy = P.x.y - Q.x.y, dz = P.x.z - Q.x.z;
+    double dn = exact_norm(dx, dy, dz);
+    if (dn > __dmul_rn(5.0, P.r)) return mk3(0, 0, 0);
+    double sig = sym_sigma(P.r, Q.r, c);
+    double rho = dn / sig;
+    double xi = c.c15 * exp(-rho * rho / 2);
+    double G = 1.0 / (c.four_pi * rho) * erf(rho / c.sqrt2);
+    double K = (G - xi) / (rho * rho);
+    double F = (3 * K - xi) / (rho * rho);
+    dv3 d = mk3(dx, dy, dz);
+    // M a_P = K a_P - F/sig^2 d (d . a_P);  result = (1/sig^3) a_Q x (M a_P)
+    dv3 Ma = K * P.a - (F / (sig * sig) * dot3(d, P.a)) * d;
+    return (1.0 / (sig * sig * sig)) * cross3(Q.a, Ma);
+}
+
+// particle::viscousDiffusion with this = P, part = Q
+__device__ __forceinline__ dv3 diffusion(const Tgt& P, const Tgt& Q, const VPConst& c) {
+    double sig = sym_sigma(P.r, Q.r, c);
+    double rho = norm3(P.x - Q.x) / sig;
+    double Vi = c.four_pi_3 * (P.r * P.r * P.r);
+    double Vj = c.four_pi_3 * (Q.r * Q.r * Q.r);
+    double xi = 1.0 / (c.two_pi_15 * (rho * rho * rho)) * exp(-rho * rho / 2);
+    return (2 * c.nu / (sig * sig) * xi) * (Vi * Q.a - Vj * P.a);
+}
+
+__device__ __forceinline__ bool far_field(const BHNode& nd, dv3 x, double theta) {
+    double d = exact_norm(nd.ex - x.x, nd.ey - x.y, nd.ez - x.z);
+    return __ddiv_rn(nd.width, d) < theta;
+}
+
+__device__ __forceinline__ BHNode load_node(const BHNode* __restrict__ nodes, int i) {
+    const double2* p = reinterpret_cast<const double2*>(nodes + i);
+    double2 a0 = __ldg(p), a1 = __ldg(p + 1), b0 = __ldg(p + 2), b1 = __ldg(p + 3);
+    const int4 q = __ldg(reinterpret_cast<const int4*>(nodes + i) + 4);
+    BHNode nd;
+    nd.ex = a0.x; nd.ey = a0.y; nd.ez = a1.x; nd.ax = a1.y;
+    nd.ay = b0.x; nd.az = b0.y; nd.erad = b1.x; nd.width = b1.y;
+    nd.first = q.x; nd.count = q.y; nd.skip = q.z; nd.leaf = q.w;
+    return nd;
+}
+
+__device__ __forceinline__ Tgt load_part_g(const BHPart* __restrict__ parts, int64_t q) {
+    const double2* p = reinterpret_cast<const double2*>(parts + q);
+    double2 a0 = __ldg(p), a1 = __ldg(p + 1), b0 = __ldg(p + 2), b1 = __ldg(p + 3);
+    return Tgt{mk3(a0.x, a0.y, a1.x), a1.y, mk3(b0.x, b0.y, b1.x), b1.y};
+}
+
+// particleFMM::barnesHutVel(part) / barnesHutStretch / barnesHutDiff for every particle.
+// Thread q handles the particle in slot q (leaf order: neighbouring threads traverse
+// neighbouring paths).  Leaves: `this` = member (node.h:274-276, 307-309, 341-343).
+template <bool V, bool S, bool D>
+__global__ void __launch_bounds__(128) k_bh_particles(const BHNode* __restrict__ nodes, int nn,
+                                                      const BHPart* __restrict__ parts, int64_t n, double theta,
+                                                      VPConst c, double* __restrict__ vel, double* __restrict__ str,
+                                                      double* __restrict__ dif) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const Tgt t = load_part_g(parts, q);
+    dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
+    int i = 1;
+    while (i < nn) {
+        const BHNode nd = load_node(nodes, i);
+        if (nd.leaf) {
+            for (int32_t k = nd.first; k < nd.first + nd.count; k++) {
+                const Tgt m = load_part_g(parts, k);
+                if (m.idx == t.idx) continue;
+                if (V) v = v + vel_gauss_sym(m, t, c);
+                if (S) s = s + stretch(m, t, c);
+                if (D) d = d + diffusion(m, t, c);
+            }
+            i++;
+        } else if (far_field(nd, t.x, theta)) {
+            const Tgt e{mk3(nd.ex, nd.ey, nd.ez), nd.erad, mk3(nd.ax, nd.ay, nd.az), -1.0};
+            if (V) v = v + vel_gauss_sym(e, t, c);
+            if (S) s = s + stretch(e, t, c);
+            if (D) d = d + diffusion(e, t, c);
+            i = nd.skip;
+        } else {
+            i++;
+        }
+    }
+    int64_t o = 3 * (int64_t)t.idx;
+    if (V) { vel[o] = v.x; vel[o + 1] = v.y; vel[o + 2] = v.z; }
+    if (S) { str[o] = s.x; str[o + 1] = s.y; str[o + 2] = s.z; }
+    if (D) { dif[o] = d.x; dif[o + 1] = d.y; dif[o + 2] = d.z; }
+}
+
+// particleFMM::barnesHutVel(POI): algebraic kernel in leaves and far nodes (node.h:236-264)
+__global__ void __launch_bounds__(128) k_bh_points(const BHNode* __restrict__ nodes, int nn,
+                                                   const BHPart* __restrict__ parts, double theta,
+                                                   const double* __restrict__ pts, int64_t m, VPConst c,
+                                                   double* __restrict__ vel) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    const dv3 x = ld3(pts + 3 * q);
+    dv3 v = mk3(0, 0, 0);
+    int i = 1;
+    while (i < nn) {
+        const BHNode nd = load_node(nodes, i);
+        if (nd.leaf) {
+            for (int32_t k = nd.first; k < nd.first + nd.count; k++) v = v + vel_alg(load_part_g(parts, k), x, c);
+            i++;
+        } else if (far_field(nd, x, theta)) {
+            const Tgt e{mk3(nd.ex, nd.ey, nd.ez), nd.erad, mk3(nd.ax, nd.ay, nd.az), -1.0};
+            v = v + vel_alg(e, x, c);
+            i = nd.skip;
+        } else {
+            i++;
+        }
+    }
+    vel[3 * q] = v.x;
+    vel[3 * q + 1] = v.y;
+    vel[3 * q + 2] = v.z;
+}
+
+constexpr int kTile = 128;
+
+// Direct sums, sources staged through shared memory in tiles of kTile particles.
+// VK: 0 none, 1 gauss_sym (self skipped), 2 gauss_poi, 3 alg.  S/D: the direct
+// stretching/diffusion of cpCaseVP::particleStrengthUpdate (`this` = target, j != i).
+// Targets are particles (tgt != null) or points (pts).
+template <int VK, bool S, bool D>
+__global__ void __launch_bounds__(kTile) k_direct(const BHPart* __restrict__ src, int64_t n,
+                                                  const BHPart* __restrict__ tgt, const double* __restrict__ pts,
+                                                  int64_t m, VPConst c, double* __restrict__ vel,
+                                                  double* __restrict__ str, double* __restrict__ dif) {
+    __shared__ BHPart tile[kTile];
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    bool live = q < m;
+    Tgt t{mk3(0, 0, 0), 0, mk3(0, 0, 0), -1.0};
+    if (live) {
+        if (tgt)
+            t = load_part_g(tgt, q);
+        else
+            t.x = ld3(pts + 3 * q);
+    }
+    dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
+    for (int64_t b = 0; b < n; b += kTile) {
+        __syncthreads();
+        if (b + threadIdx.x < n) tile[threadIdx.x] = src[b + threadIdx.x];
+        __syncthreads();
+        int lim = (int)((n - b) < kTile ? (n - b) : kTile);
+        if (!live) continue;
+        for (int k = 0; k < lim; k++) {
+            const Tgt p = load_part(tile[k]);
+            bool self = p.idx == t.idx;
+            if (VK == 1 && !self) v = v + vel_gauss_sym(p, t, c);
+            if (VK == 2) v = v + vel_gauss_poi(p, t.x, c);
+            if (VK == 3) v = v + vel_alg(p, t.x, c);
+            if (S && !self) s = s + stretch(t, p, c);
+            if (D && !self) d = d + diffusion(t, p, c);
+        }
+    }
+    if (!live) return;
+    if (VK) { vel[3 * q] = v.x; vel[3 * q + 1] = v.y; vel[3 * q + 2] = v.z; }
+    if (S) { str[3 * q] = s.x; str[3 * q + 1] = s.y; str[3 * q + 2] = s.z; }
+    if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
+}
+
+__global__ void k_pack_parts(const double* __restrict__ pos, const double* __restrict__ str,
+                             const double* __restrict__ rad, int64_t n, BHPart* __restrict__ out) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] = BHPart{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], rad[i], str[3 * i], str[3 * i + 1], str[3 * i + 2],
+                    (double)i};
+}
+
+unsigned blocks(int64_t m, int t) { return (unsigned)((m + t - 1) / t); }
+
+}  // namespace
+
+cudaError_t launch_bh_particles(const BHNode* nodes, int nn, const BHPart* parts, int64_t n, double theta,
+                                const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    int mask = (vel ? 1 : 0) | (str ? 2 : 0) | (dif ? 4 : 0);
+    dim3 g(blocks(n, 128)), b(128);
+    switch (mask) {
+        case 1: k_bh_particles<true, false, false><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        case 2: k_bh_particles<false, true, false><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        case 3: k_bh_particles<true, true, false><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        case 4: k_bh_particles<false, false, true><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        case 5: k_bh_particles<true, false, true><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        case 6: k_bh_particles<false, true, true><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        case 7: k_bh_particles<true, true, true><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
+        default: return cudaSuccess;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bh_points(const BHNode* nodes, int nn, const BHPart* parts, double theta, const double* pts,
+                             int64_t m, const VPConst& c, double* vel, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    k_bh_points<<<blocks(m, 128), 128, 0, s>>>(nodes, nn, parts, theta, pts, m, c, vel);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pack_parts(const double* pos, const double* str, const double* rad, int64_t n, BHPart* out,
+                              cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_pack_parts<<<blocks(n, 256), 256, 0, s>>>(pos, str, rad, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_direct(int vk, bool S, bool D, const BHPart* src, int64_t n, const BHPart* tgt, const double* pts,
+                          int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    dim3 g(blocks(m, kTile)), b(kTile);
+#define CPG_DIRECT(VK_, S_, D_) k_direct<VK_, S_, D_><<<g, b, 0, s>>>(src, n, tgt, pts, m, c, vel, str, dif)
+    int key = vk * 4 + (S ? 2 : 0) + (D ? 1 : 0);
+    switch (key) {
+        case 4: CPG_DIRECT(1, false, false); break;
+        case 8: CPG_DIRECT(2, false, false); break;
+        case 11: CPG_DIRECT(2, true, true); break;
+        case 10: CPG_DIRECT(2, true, false); break;
+        case 9: CPG_DIRECT(2, false, true); break;
+        case 12: CPG_DIRECT(3, false, false); break;
+        case 3: CPG_DIRECT(0, true, true); break;
+        case 2: CPG_DIRECT(0, true, false); break;
+        case 1: CPG_DIRECT(0, false, true); break;
+        default: return cudaErrorInvalidValue;
+    }
+#undef CPG_DIRECT
+    return cudaGetLastError();
+}
+
+VPConst vp_constants() {
+    VPConst c;
+    const double pi = 3.14159265358979323846;
+    c.four_pi = 4 * pi;
+    c.inv_four_pi = 1 / (4 * pi);
+    c.sqrt2 = std::pow(2.0, 0.5);
+    c.two_pi_15 = std::pow(2 * pi, 1.5);
+    c.c15 = 1 / c.two_pi_15;
+    c.four_pi_3 = 4 * pi / 3;
+    c.nu = 1.983e-5;  // CPanel/particle.cpp:126
+    return c;
+}
+
+}  // namespace cpg

@@ -1,0 +1,178 @@
+"""Vortex-particle operators: host-side mirror of particleOctree / particleFMM / particle.
+
+Tensors are CUDA float64 tensors: positions and strengths (n, 3), radii (n,).
+The calls go through include/cpanel_vp.h; there is no CPU fallback.
+
+    tree = ParticleFMM(pos, strength, radius)          # particleOctree::addData + particleFMM::build
+    v_pts = tree.barnesHutVel(points)                  # barnesHutVel(POI), CPanel/particleFMM.cpp:65-77
+    v, s, d = tree.barnesHut()                         # barnesHutVel(part) / Stretch / Diff, :79-116
+    v = particles_velocity(pos, strength, radius)      # direct sums (particle.cpp:31-77)
+    s, d = particles_stretch_diff(pos, strength, radius)
+    v = panels_velocity(body_verts, sigma, mu, wake_verts, wake_mu, points)
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import VEL_ALG, VEL_GAUSS, VEL_GAUSS_SYM
+
+NODE_FIELDS = 24
+_KERNELS = {"gauss_sym": VEL_GAUSS_SYM, "gauss": VEL_GAUSS, "alg": VEL_ALG}
+
+
+def _ctx(ctx):
+    from . import Context
+    return ctx or Context.default()
+
+
+def _dev(t, cols=None):
+    import torch
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("expected a CUDA tensor")
+    t = t.contiguous().to(torch.float64)
+    if cols is not None and (t.dim() != 2 or t.shape[1] != cols):
+        t = t.reshape(-1, cols)
+    return t
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _sync():
+    import torch
+    torch.cuda.synchronize()
+
+
+class ParticleFMM:
+    """Barnes-Hut octree over one particle set (fresh build, as the VP loop does every step)."""
+
+    def __init__(self, pos, strength, radius, max_members=10, theta=0.5, ctx=None):
+        self.ctx = _ctx(ctx)
+        self.pos, self.strength, self.radius = _dev(pos, 3), _dev(strength, 3), _dev(radius).reshape(-1)
+        self.n = self.pos.shape[0]
+        h = C.c_void_p()
+        _sync()
+        self.ctx.check(self.ctx.L.cpg_ptree_build(self.ctx.h, _ptr(self.pos), _ptr(self.strength), _ptr(self.radius),
+                                                  self.n, max_members, theta, C.byref(h)), "particle tree")
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            from . import _shutting_down_now
+            if not _shutting_down_now():
+                self.ctx.L.cpg_ptree_destroy(h)
+            self.h = None
+
+    def info(self):
+        i = _lib.PTreeInfo()
+        self.ctx.check(self.ctx.L.cpg_ptree_info_get(self.h, C.byref(i)), "tree info")
+        return {"n_particles": i.n_particles, "n_nodes": i.n_nodes, "n_leaves": i.n_leaves, "n_levels": i.n_levels}
+
+    def numTreeLevels(self):
+        return self.info()["n_levels"]
+
+    def nodes(self):
+        """(n_nodes, 24) pre-order node table: origin half level leaf n_members exp_pos exp_strength
+        exp_radius child0..7."""
+        out = np.zeros((self.info()["n_nodes"], NODE_FIELDS))
+        self.ctx.check(self.ctx.L.cpg_ptree_table(self.h, out.ctypes.data_as(_lib.D), None), "tree table")
+        return out
+
+    def leaf_members(self):
+        out = np.zeros(self.n, dtype=np.int64)
+        self.ctx.check(self.ctx.L.cpg_ptree_table(self.h, None, out.ctypes.data_as(_lib.I64)), "tree table")
+        return out
+
+    def barnesHutVel(self, points):
+        import torch
+        pts = _dev(points, 3)
+        vel = torch.empty_like(pts)
+        _sync()
+        self.ctx.check(self.ctx.L.cpg_bh_velocity_points(self.h, _ptr(pts), pts.shape[0], _ptr(vel)),
+                       "barnesHutVel")
+        return vel
+
+    def barnesHut(self, vel=True, stretch=True, diff=True):
+        """(velocity, stretching, diffusion) on every particle; None for the ones not asked."""
+        import torch
+        outs = [torch.empty((self.n, 3), dtype=torch.float64, device=self.pos.device) if w else None
+                for w in (vel, stretch, diff)]
+        _sync()
+        self.ctx.check(self.ctx.L.cpg_bh_particles(self.h, *[_ptr(o) for o in outs]), "barnesHut")
+        return tuple(outs)
+
+    def barnesHutVelParticles(self):
+        return self.barnesHut(True, False, False)[0]
+
+    def barnesHutStretch(self):
+        return self.barnesHut(False, True, False)[1]
+
+    def barnesHutDiff(self):
+        return self.barnesHut(False, False, True)[2]
+
+
+def host_tree(pos, strength, radius, max_members=10):
+    """The same octree built on the host from numpy arrays: (node table, leaf members, info)."""
+    L = _lib.load()
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    st = np.ascontiguousarray(strength, dtype=np.float64).reshape(-1, 3)
+    rad = np.ascontiguousarray(radius, dtype=np.float64).reshape(-1)
+    info = _lib.PTreeInfo()
+    members = np.zeros(len(pos), dtype=np.int64)
+    D = _lib.D
+    rc = L.cpg_ptree_host_table(pos.ctypes.data_as(D), st.ctypes.data_as(D), rad.ctypes.data_as(D), len(pos),
+                                max_members, None, 0, members.ctypes.data_as(_lib.I64), C.byref(info))
+    if rc != 0:
+        raise _lib.CpgError(rc, "host tree")
+    nodes = np.zeros((info.n_nodes, NODE_FIELDS))
+    rc = L.cpg_ptree_host_table(pos.ctypes.data_as(D), st.ctypes.data_as(D), rad.ctypes.data_as(D), len(pos),
+                                max_members, nodes.ctypes.data_as(D), info.n_nodes, None, C.byref(info))
+    if rc != 0:
+        raise _lib.CpgError(rc, "host tree")
+    return nodes, members, {"n_particles": info.n_particles, "n_nodes": info.n_nodes, "n_leaves": info.n_leaves,
+                            "n_levels": info.n_levels}
+
+
+def particles_velocity(pos, strength, radius, points=None, kernel="gauss", ctx=None):
+    """Direct sum of particle velocity kernels at `points` (or at the particles when None)."""
+    import torch
+    ctx = _ctx(ctx)
+    pos, st, rad = _dev(pos, 3), _dev(strength, 3), _dev(radius).reshape(-1)
+    pts = _dev(points, 3) if points is not None else None
+    m = pts.shape[0] if pts is not None else pos.shape[0]
+    vel = torch.empty((m, 3), dtype=torch.float64, device=pos.device)
+    _sync()
+    ctx.check(ctx.L.cpg_particles_velocity(ctx.h, _ptr(pos), _ptr(st), _ptr(rad), pos.shape[0], _ptr(pts), m,
+                                           _KERNELS[kernel], _ptr(vel)), "particle velocity")
+    return vel
+
+
+def particles_stretch_diff(pos, strength, radius, ctx=None):
+    import torch
+    ctx = _ctx(ctx)
+    pos, st, rad = _dev(pos, 3), _dev(strength, 3), _dev(radius).reshape(-1)
+    s = torch.empty_like(pos)
+    d = torch.empty_like(pos)
+    _sync()
+    ctx.check(ctx.L.cpg_particles_stretch_diff(ctx.h, _ptr(pos), _ptr(st), _ptr(rad), pos.shape[0], _ptr(s), _ptr(d)),
+              "particle strength update")
+    return s, d
+
+
+def panels_velocity(body_verts, sigma, mu, wake_verts, wake_mu, points, ctx=None):
+    import torch
+    ctx = _ctx(ctx)
+    bv = _dev(body_verts, 9)
+    sg, mu_ = _dev(sigma).reshape(-1), _dev(mu).reshape(-1)
+    nw = 0 if wake_verts is None else int(np.prod(wake_verts.shape)) // 9
+    wv = _dev(wake_verts, 9) if nw else None
+    wm = _dev(wake_mu).reshape(-1) if nw else None
+    pts = _dev(points, 3)
+    vel = torch.empty_like(pts)
+    _sync()
+    ctx.check(ctx.L.cpg_panels_velocity(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm), nw,
+                                        _ptr(pts), pts.shape[0], _ptr(vel)), "panel velocity")
+    return vel

@@ -159,7 +159,8 @@ int  cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64
 
 /* ---- optional device-time accounting (CUDA events on the context's stream) ----
  * Classes: 0 assembly, 1 wake columns, 2 FP32 matvec, 3 FP64 matvec, 4 refinement
- * residual, 5 LU factorization (one graph launch), 6 unused, 7 CHTLS weights,
+ * residual, 5 LU factorization (one graph launch), 6 particle and panel-velocity
+ * operators (cpanel_vp.h), 7 CHTLS weights,
  * 8 velocity/Cp/forces, 9 LU triangular solves (one graph launch per solve). */
 #define CPG_PROF_NCLS 10
 typedef struct {

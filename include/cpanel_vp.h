@@ -1,0 +1,99 @@
+/*
+ * cpanel_vp.h -- C ABI of the GB300 vortex-particle operators (sm_103a).
+ *
+ * Particle arrays are device pointers in structure-of-arrays form: positions and
+ * strengths n x 3 (row-major), radii n.  Outputs are device arrays of the same
+ * layout.  Every call is ordered on the context's stream and returns when its
+ * results are ready.  Status codes and cpg_last_error() as in cpanel_gpu.h.
+ *
+ * Reference interfaces replaced (paths relative to the CPanel project root):
+ *   cpg_ptree_build            particleOctree::addData on a fresh tree + particleFMM::build,
+ *                              octree/include/octree.h:151-195, CPanel/particleFMM.cpp:22-62
+ *   cpg_ptree_table            octree::getNodes / node getters, octree/include/node.h:448-577
+ *   cpg_bh_velocity_points     particleFMM::barnesHutVel(POI), CPanel/particleFMM.cpp:65-77
+ *   cpg_bh_particles           particleFMM::barnesHutVel(particle*), barnesHutStretch,
+ *                              barnesHutDiff, CPanel/particleFMM.cpp:79-116
+ *   cpg_particles_velocity     the direct sums of particle::velInfl(POI) / velInfl(particle*)
+ *                              / velInflAlgSmooth, CPanel/particle.cpp:31-77, as called at
+ *                              CPanel/cpCaseVP.cpp:609-612,651-655,697-703
+ *   cpg_particles_stretch_diff the direct branch of cpCaseVP::particleStrengthUpdate,
+ *                              CPanel/cpCaseVP.cpp:504-516 (particle.cpp:80-140)
+ *   cpg_panels_velocity        bodyPanel::panelV + wakePanel::panelV summed over panels,
+ *                              CPanel/bodyPanel.cpp:122-130, CPanel/wakePanel.cpp:89-92,
+ *                              as called at CPanel/cpCaseVP.cpp:713-731
+ */
+#ifndef CPANEL_VP_H
+#define CPANEL_VP_H
+
+#include <stdint.h>
+
+#include "cpanel_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct cpg_ptree cpg_ptree;
+
+typedef struct {
+    int64_t n_particles;
+    int64_t n_nodes;
+    int64_t n_leaves;
+    int64_t n_levels; /* octree::numTreeLevels (root = level 1) */
+} cpg_ptree_info;
+
+/* Velocity kernels of cpg_particles_velocity */
+typedef enum {
+    CPG_VEL_GAUSS_SYM = 1, /* particle::velInfl(particle*): targets are the particles, self skipped */
+    CPG_VEL_GAUSS = 2,     /* particle::velInfl(POI): Gaussian core 1.5 r, zero at distance 0     */
+    CPG_VEL_ALG = 3        /* particle::velInflAlgSmooth                                         */
+} cpg_vel_kernel;
+
+/* Builds the particle octree with the reference's rules (root cube 0.51 x largest
+ * extent about the box centre; leaves split above max_members; octant x>o:4, y>o:2,
+ * z>o:1) and the lumped expansions.  theta is the far-field ratio (0.5 in the
+ * reference).  Nodes deeper than level 32 are not split (the reference has no limit
+ * and recurses without end on more than max_members coincident particles). */
+int  cpg_ptree_build(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius, int64_t n,
+                     int64_t max_members, double theta, cpg_ptree** out);
+void cpg_ptree_destroy(cpg_ptree* t);
+int  cpg_ptree_info_get(const cpg_ptree* t, cpg_ptree_info* info);
+/* Host copy of the tree, nodes in the reference's pre-order (node::getSubNodes): 24
+ * doubles per node [origin(3) half(3) level leaf n_members exp_pos(3) exp_strength(3)
+ * exp_radius child0..7 (pre-order index or -1)]; the root carries no expansion (zeros).
+ * leaf_members (n, may be null): particle indices of the leaves in pre-order. */
+int  cpg_ptree_table(const cpg_ptree* t, double* nodes, int64_t* leaf_members);
+/* Host-only build of the same tree from host arrays (no device use; for checking and
+ * for hosts that want the tree itself).  Fills info; writes the node table only when
+ * cap_nodes >= info->n_nodes (else returns CPG_E_INVALID with info filled). */
+int  cpg_ptree_host_table(const double* pos, const double* strength, const double* radius, int64_t n,
+                          int64_t max_members, double* nodes, int64_t cap_nodes, int64_t* leaf_members,
+                          cpg_ptree_info* info);
+/* barnesHutVel(POI) at m points (device pts m x 3 -> vel m x 3) */
+int  cpg_bh_velocity_points(cpg_ptree* t, const double* pts, int64_t m, double* vel);
+/* barnesHutVel(particle*), barnesHutStretch, barnesHutDiff for every particle of the
+ * tree in one traversal; any output may be null.  Outputs by particle index. */
+int  cpg_bh_particles(cpg_ptree* t, double* vel, double* stretch, double* diff);
+
+/* Direct velocity sums over n particles at m points (kernel CPG_VEL_GAUSS or
+ * CPG_VEL_ALG), or at the particles themselves (pts = NULL, m = n; any kernel). */
+int  cpg_particles_velocity(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius,
+                            int64_t n, const double* pts, int64_t m, int kernel, double* vel);
+/* Direct stretching and diffusion on every particle: sum over j != i of
+ * particles[i]->vortexStretching(particles[j]) (resp. viscousDiffusion); either
+ * output may be null. */
+int  cpg_particles_stretch_diff(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius,
+                                int64_t n, double* stretch, double* diff);
+
+/* Panel-induced velocity at m points: sum over nb body triangles (vertices nb x 9)
+ * of sigma_j vSrc + mu_j vDub, then over nw wake triangles of mu_w dubVInf.
+ * All arrays on the device; wake arrays may be null when nw = 0. */
+int  cpg_panels_velocity(cpg_ctx* ctx, const double* body_verts, const double* sigma, const double* mu,
+                         int64_t nb, const double* wake_verts, const double* wake_mu, int64_t nw,
+                         const double* pts, int64_t m, double* vel);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CPANEL_VP_H */

@@ -258,6 +258,22 @@ void panelVInf(const V3* p, V3 center, V3 normal, double area, double longSide, 
     }
 }
 
+/* panel::dubVInf, CPanel/panel.cpp:666-704 (wake panels; s = p2 - p1 here, a - b in panelVInf) */
+V3 dubVInf(const V3* p, V3 center, V3 normal, double area, double longSide, V3 POI) {
+    V3 pjk = POI - center;
+    Local L = localSys(center, normal, p[0]);
+    if (norm(pjk) / longSide > 5)
+        return area * (3 * dot(pjk, L.n) * pjk - std::pow(norm(pjk), 2) * L.n) /
+               (4 * kPi * std::pow(norm(pjk), 5));  // pntDubV, panel.cpp:773-776
+    V3 vel;
+    for (int i = 0; i < 3; i++) {
+        V3 p1 = p[i], p2 = p[(i + 1) % 3];
+        V3 a = POI - p1, b = POI - p2, s = p2 - p1;
+        vel = vel + vortexV(a, b, s);
+    }
+    return vel / (4 * kPi);
+}
+
 /* ---------------------------------------------------------------- topology */
 int findEdge(Mesh& M, int n1, int n2) {  // geometry::findEdge, CPanel/geometry.cpp:771-787
     uint64_t lo = (uint64_t)std::min(n1, n2), hi = (uint64_t)std::max(n1, n2);
@@ -1153,6 +1169,34 @@ void cpo_tri_v_inf(const double* v9, const double* poi, double* v_src, double* v
     panelVInf(P.p, P.center, P.normal, P.area, P.longSide, {poi[0], poi[1], poi[2]}, s, d);
     v_src[0] = s.x; v_src[1] = s.y; v_src[2] = s.z;
     v_dub[0] = d.x; v_dub[1] = d.y; v_dub[2] = d.z;
+}
+
+void cpo_tri_dub_v_inf(const double* v9, const double* poi, double* v_dub) {
+    Pan P = makePan(v9);
+    V3 d = dubVInf(P.p, P.center, P.normal, P.area, P.longSide, {poi[0], poi[1], poi[2]});
+    v_dub[0] = d.x; v_dub[1] = d.y; v_dub[2] = d.z;
+}
+
+void cpo_panels_velocity(const double* bverts, const double* sigma, const double* mu, int64_t nb,
+                         const double* wverts, const double* wmu, int64_t nw, const double* pts, int64_t m,
+                         double* vel, int nthreads) {
+    std::vector<Pan> B(nb), W(nw);
+    for (int64_t j = 0; j < nb; j++) B[j] = makePan(bverts + 9 * j);
+    for (int64_t j = 0; j < nw; j++) W[j] = makePan(wverts + 9 * j);
+    parallelFor(m, nthreads, [&](int64_t ia, int64_t ib) {
+        for (int64_t i = ia; i < ib; i++) {
+            V3 poi{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]};
+            V3 acc;
+            for (int64_t j = 0; j < nb; j++) {  // bodyPanel::panelV, bodyPanel.cpp:122-130
+                V3 vs, vd;
+                panelVInf(B[j].p, B[j].center, B[j].normal, B[j].area, B[j].longSide, poi, vs, vd);
+                acc = acc + (sigma[j] * vs + mu[j] * vd);
+            }
+            for (int64_t j = 0; j < nw; j++)  // wakePanel::panelV, wakePanel.cpp:89-92
+                acc = acc + wmu[j] * dubVInf(W[j].p, W[j].center, W[j].normal, W[j].area, W[j].longSide, poi);
+            vel[3 * i] = acc.x; vel[3 * i + 1] = acc.y; vel[3 * i + 2] = acc.z;
+        }
+    });
 }
 
 void cpo_set_inf_coeff(void* mp, double* A, double* B, int64_t r0, int64_t r1, int nthreads) {

@@ -49,6 +49,15 @@ double  cpo_tri_dub_phi_inf(const double* verts9, const double* poi);
 /* bodyPanel::panelVInf, CPanel/bodyPanel.cpp:305-348 */
 void    cpo_tri_v_inf(const double* verts9, const double* poi, double* v_src, double* v_dub);
 
+/* panel::dubVInf, CPanel/panel.cpp:666-704 (doublet-only velocity of a wake triangle) */
+void    cpo_tri_dub_v_inf(const double* verts9, const double* poi, double* v_dub);
+/* Panel-induced velocity at m points (the panel terms of cpCaseVP::velocityInflFromEverything,
+ * CPanel/cpCaseVP.cpp:713-731): sum over body triangles of sigma*vSrc + mu*vDub
+ * (bodyPanel::panelV) then over wake triangles of mu_w*dubVInf (wakePanel::panelV). */
+void    cpo_panels_velocity(const double* bverts, const double* sigma, const double* mu, int64_t nb,
+                            const double* wverts, const double* wmu, int64_t nw, const double* pts,
+                            int64_t m, double* vel, int nthreads);
+
 /* ---- assembly: geometry::setInfCoeff, CPanel/geometry.cpp:809-891 ----
  * Rows [r0, r1) of A and B (full matrix: r0 = 0, r1 = n), stored column-major with
  * leading dimension r1 - r0: A(i,j) = A[j*(r1-r0) + (i-r0)].  nthreads >= 1. */

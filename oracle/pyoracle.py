@@ -53,8 +53,22 @@ def lib():
         L.cpo_case_post.argtypes = [C.c_void_p, C.POINTER(CaseParams), D, D, D, D, C.POINTER(CaseResult)]
         L.cpo_bicgstab.restype = C.c_int
         L.cpo_bicgstab.argtypes = [D, C.c_int64, D, D, C.c_double, C.c_int64, I64, D, C.c_int]
-        if hasattr(L, "cpo_vp_register"):
-            L.cpo_vp_register(C.c_void_p(0))
+        L.cpo_tri_dub_v_inf.argtypes = [D, D, D]
+        L.cpo_panels_velocity.argtypes = [D, D, D, C.c_int64, D, D, C.c_int64, D, C.c_int64, D, C.c_int]
+        L.cpo_vp_direct_velocity.argtypes = [D, D, D, C.c_int64, D, C.c_int64, C.c_int, D]
+        L.cpo_vp_direct_stretch.argtypes = [D, D, D, C.c_int64, D]
+        L.cpo_vp_direct_diffusion.argtypes = [D, D, D, C.c_int64, D]
+        L.cpo_bh_build.restype = C.c_void_p
+        L.cpo_bh_build.argtypes = [D, D, D, C.c_int64, C.c_int64, C.c_double]
+        L.cpo_bh_free.argtypes = [C.c_void_p]
+        for f in ("cpo_bh_num_nodes", "cpo_bh_num_levels"):
+            getattr(L, f).restype = C.c_int64
+            getattr(L, f).argtypes = [C.c_void_p]
+        L.cpo_bh_nodes.argtypes = [C.c_void_p, D]
+        L.cpo_bh_leaf_members.argtypes = [C.c_void_p, I64]
+        L.cpo_bh_velocity.argtypes = [C.c_void_p, D, C.c_int64, C.c_int, D]
+        L.cpo_bh_stretch.argtypes = [C.c_void_p, D]
+        L.cpo_bh_diffusion.argtypes = [C.c_void_p, D]
         _lib = L
     return _lib
 
@@ -186,3 +200,122 @@ def bicgstab(A, b, nthreads=None):
     L.cpo_bicgstab(_p(A), n, _p(b), _p(x), np.finfo(float).eps, 2 * n, C.byref(it), C.byref(err),
                    nthreads or nthreads_default())
     return x, it.value, err.value
+
+
+def tri_dub_v_inf(verts9, poi):
+    L = lib()
+    v = np.ascontiguousarray(verts9, dtype=np.float64)
+    p = np.ascontiguousarray(poi, dtype=np.float64)
+    vd = np.zeros(3)
+    L.cpo_tri_dub_v_inf(_p(v), _p(p), _p(vd))
+    return vd
+
+
+def panels_velocity(bverts, sigma, mu, wverts, wmu, pts, nthreads=None):
+    """Sum of bodyPanel::panelV over body triangles and wakePanel::panelV over wake triangles."""
+    L = lib()
+    bv = np.ascontiguousarray(bverts, dtype=np.float64).reshape(-1, 9)
+    wv = np.ascontiguousarray(wverts, dtype=np.float64).reshape(-1, 9)
+    sg = np.ascontiguousarray(sigma, dtype=np.float64)
+    m_ = np.ascontiguousarray(mu, dtype=np.float64)
+    wm = np.ascontiguousarray(wmu, dtype=np.float64)
+    p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((len(p), 3))
+    L.cpo_panels_velocity(_p(bv), _p(sg), _p(m_), len(bv), _p(wv), _p(wm), len(wv), _p(p), len(p), _p(out),
+                          nthreads or nthreads_default())
+    return out
+
+
+def _parts(pos, strength, radius):
+    pos = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    strength = np.ascontiguousarray(strength, dtype=np.float64).reshape(-1, 3)
+    radius = np.ascontiguousarray(radius, dtype=np.float64).reshape(-1)
+    return pos, strength, radius
+
+
+def particles_velocity(pos, strength, radius, pts=None, kernel="gauss"):
+    """Direct sums of particle::velInfl.  pts None: on every particle (symmetrised core,
+    self skipped); else at the points with the Gaussian or the algebraic kernel."""
+    L = lib()
+    pos, st, rad = _parts(pos, strength, radius)
+    if pts is None:
+        out = np.zeros((len(pos), 3))
+        L.cpo_vp_direct_velocity(_p(pos), _p(st), _p(rad), len(pos), None, 0, 0, _p(out))
+        return out
+    p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((len(p), 3))
+    L.cpo_vp_direct_velocity(_p(pos), _p(st), _p(rad), len(pos), _p(p), len(p), 1 if kernel == "gauss" else 2,
+                             _p(out))
+    return out
+
+
+def particles_stretch(pos, strength, radius):
+    L = lib()
+    pos, st, rad = _parts(pos, strength, radius)
+    out = np.zeros((len(pos), 3))
+    L.cpo_vp_direct_stretch(_p(pos), _p(st), _p(rad), len(pos), _p(out))
+    return out
+
+
+def particles_diffusion(pos, strength, radius):
+    L = lib()
+    pos, st, rad = _parts(pos, strength, radius)
+    out = np.zeros((len(pos), 3))
+    L.cpo_vp_direct_diffusion(_p(pos), _p(st), _p(rad), len(pos), _p(out))
+    return out
+
+
+class ParticleTree:
+    """particleOctree + particleFMM: insertion-order octree with lumped expansions."""
+
+    NODE_FIELDS = 24
+
+    def __init__(self, pos, strength, radius, max_members=10, theta=0.5):
+        L = lib()
+        self.pos, self.strength, self.radius = _parts(pos, strength, radius)
+        self.h = L.cpo_bh_build(_p(self.pos), _p(self.strength), _p(self.radius), len(self.pos), max_members, theta)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().cpo_bh_free(h)
+            self.h = None
+
+    @property
+    def n_nodes(self):
+        return lib().cpo_bh_num_nodes(self.h)
+
+    @property
+    def n_levels(self):
+        return lib().cpo_bh_num_levels(self.h)
+
+    def nodes(self):
+        out = np.zeros((self.n_nodes, self.NODE_FIELDS))
+        lib().cpo_bh_nodes(self.h, _p(out))
+        return out
+
+    def leaf_members(self):
+        out = np.zeros(len(self.pos), dtype=np.int64)
+        lib().cpo_bh_leaf_members(self.h, _p(out, I64))
+        return out
+
+    def velocity_points(self, pts):
+        p = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros((len(p), 3))
+        lib().cpo_bh_velocity(self.h, _p(p), len(p), 0, _p(out))
+        return out
+
+    def velocity(self):
+        out = np.zeros((len(self.pos), 3))
+        lib().cpo_bh_velocity(self.h, None, 0, 1, _p(out))
+        return out
+
+    def stretch(self):
+        out = np.zeros((len(self.pos), 3))
+        lib().cpo_bh_stretch(self.h, _p(out))
+        return out
+
+    def diffusion(self):
+        out = np.zeros((len(self.pos), 3))
+        lib().cpo_bh_diffusion(self.h, _p(out))
+        return out

@@ -59,7 +59,7 @@ def config_dict(info, name="multi_rhs"):
     stations = {"multi_rhs": 61, "mid": 25}[name]
     return {"workload": "NACA4412 tapered AR6 wing, 80 pts/side x %d stations, 17 alphas (-4..12 deg)" % stations,
             "body_panels": info["n_body"], "wake_panels": info["n_wake"], "alphas": len(ALPHAS), "mach": MACH,
-            "precision": "mixed: df32 far field + FP64 near field, FP32 LU + refinement to 1e-12",
+            "precision": "mixed: df32 far field + FP64 near field, FP32 LU + refinement to 1e-10",
             "l2": "inputs larger than L2 (A = 2 x 1.49 GB)", "parallelism": "replicas"}
 
 

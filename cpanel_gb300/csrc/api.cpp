@@ -65,6 +65,8 @@ struct DevBuf {
 };
 
 constexpr double kPi = 3.14159265358979323846;
+// Relative residual at which the mixed path's refinement stops (per right-hand side).
+constexpr double kMixedRefineTol = 1e-10;
 constexpr int F_STRIDE_HOST = 16;  // double-float far-field record, F_STRIDE in common.cuh
 
 }  // namespace
@@ -522,7 +524,7 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
         CK(cpg::solve_lu_refined(ctx->blas, &g->graphs, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(),
                                  n, k, rhs, mu,
-                                 g->work.p, 1e-12, 8, &st, s),
+                                 g->work.p, kMixedRefineTol, 8, &st, s),
            "refined solve (mixed)");
     }
     CK(cudaEventRecord(e1, s), "event");

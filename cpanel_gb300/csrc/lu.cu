@@ -22,69 +22,99 @@ namespace {
 constexpr int NB = 128;   // panel width
 constexpr int P = NB + 1; // padded smem pitch (no bank conflicts on row access)
 
+constexpr int DT = 512;    // threads of the diagonal-block kernel
+constexpr int DIAG_SMEM = 3 * NB * P * 4;
+
 // In-place LU (unit lower L, upper U) of the b x b block at A + K*n + K, then the
-// inverses of both triangles into Dinv (L11^{-1} then U11^{-1}, column-major,
-// ld NB).  Thread t owns row t during the factorization and column t during the
-// inversions; one cheap 128-thread barrier per factorization step.
-__global__ void __launch_bounds__(NB) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
+// inverses of both triangles into Dinv (L11^{-1} then U11^{-1}, column-major, ld NB).
+// A block smaller than NB is padded with the identity, which factors and inverts to
+// itself without touching the real entries.
+//
+// Elimination: thread t owns row r = t % 128 and the columns c = t / 128 (mod 4), so
+// each of the 128 steps spreads its rank-1 update over 512 threads behind one
+// barrier.  Step j reads column j and row j and writes only rows and columns past j;
+// the multiplier l(r, j) is stored one step later, when nothing reads column j.
+// Inversion: threads 0-255 invert L and 256-511 invert U at the same time, two lanes
+// per column.  Lane `sub` sums the terms of rows with parity `sub` and is the one that
+// stores those rows of the inverse, so it only ever reads entries it wrote itself;
+// one shuffle joins the two partial sums.
+__global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
                                                 float* __restrict__ Dinv, int* bad) {
     extern __shared__ float sm[];
-    float* S = sm;           // S[r*P + c]
-    float* Z = sm + NB * P;  // Z[c*P + i]
+    float* S = sm;               // S[r*P + c]
+    float* ZL = sm + NB * P;     // ZL[col*P + i] = (L^{-1})(i, col)
+    float* ZU = sm + 2 * NB * P; // ZU[col*P + i] = (U^{-1})(i, col)
     const int t = threadIdx.x;
-    for (int c = 0; c < b; c++)
-        if (t < b) S[t * P + c] = A[(K + c) * n + K + t];
+    for (int idx = t; idx < NB * NB; idx += DT) {
+        int c = idx / NB, r = idx % NB;
+        S[r * P + c] = (r < b && c < b) ? A[(K + c) * n + K + r] : (r == c ? 1.f : 0.f);
+    }
     __syncthreads();
-    for (int j = 0; j < b; j++) {
+    const int r = t % NB, q = t / NB;
+    float lprev = 0.f;
+    for (int j = 0; j < NB; j++) {
+        if (q == 0 && j > 0 && r > j - 1) S[r * P + j - 1] = lprev;
         float piv = S[j * P + j];
         if (piv == 0.f) {
             if (t == 0) atomicExch(bad, 1);
             piv = 1.f;
         }
-        if (t > j && t < b) {
-            float l = S[t * P + j] / piv;
-            S[t * P + j] = l;
-            int c = j + 1;
-            for (; c + 3 < b; c += 4) {
-                float u0 = S[j * P + c], u1 = S[j * P + c + 1], u2 = S[j * P + c + 2], u3 = S[j * P + c + 3];
-                S[t * P + c] = __fmaf_rn(-l, u0, S[t * P + c]);
-                S[t * P + c + 1] = __fmaf_rn(-l, u1, S[t * P + c + 1]);
-                S[t * P + c + 2] = __fmaf_rn(-l, u2, S[t * P + c + 2]);
-                S[t * P + c + 3] = __fmaf_rn(-l, u3, S[t * P + c + 3]);
+        if (r > j) {
+            float l = S[r * P + j] / piv;
+            int c = j + 1 + ((q - (j + 1)) & 3);
+            for (; c + 4 < NB; c += 8) {
+                float u0 = S[j * P + c], u1 = S[j * P + c + 4];
+                S[r * P + c] = __fmaf_rn(-l, u0, S[r * P + c]);
+                S[r * P + c + 4] = __fmaf_rn(-l, u1, S[r * P + c + 4]);
             }
-            for (; c < b; c++) S[t * P + c] = __fmaf_rn(-l, S[j * P + c], S[t * P + c]);
+            if (c < NB) S[r * P + c] = __fmaf_rn(-l, S[j * P + c], S[r * P + c]);
+            lprev = l;
         }
         __syncthreads();
     }
-    for (int c = 0; c < b; c++)
-        if (t < b) A[(K + c) * n + K + t] = S[t * P + c];
+    // (the multiplier of the last step belongs to no row: r > NB - 1 never holds)
+    const int half = t / 256, u = t % 256, col = u / 2, sub = u % 2;
+    if (half == 0) {  // L z = e_col, unit lower: rows col..NB-1
+        float* Z = ZL + col * P;
+        for (int i = 0; i < NB; i++) {
+            float s0 = 0.f, s1 = 0.f;
+            if (i > col) {
+                int jj = col + ((sub - col) & 1);  // lane sub owns the rows of its parity
+                for (; jj + 2 < i; jj += 4) {
+                    s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
+                    s1 = __fmaf_rn(-S[i * P + jj + 2], Z[jj + 2], s1);
+                }
+                if (jj < i) s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
+            }
+            float v = s0 + s1;
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            if (sub == (i & 1)) Z[i] = i < col ? 0.f : (i == col ? 1.f : v);
+        }
+    } else {  // U z = e_col: rows col..0
+        float* Z = ZU + col * P;
+        for (int i = NB - 1; i >= 0; i--) {
+            float s0 = 0.f, s1 = 0.f;
+            if (i < col) {
+                int jj = i + 1 + ((sub - (i + 1)) & 1);
+                for (; jj + 2 <= col; jj += 4) {
+                    s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
+                    s1 = __fmaf_rn(-S[i * P + jj + 2], Z[jj + 2], s1);
+                }
+                if (jj <= col) s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
+            }
+            float v = s0 + s1;
+            v += __shfl_xor_sync(0xffffffffu, v, 1);
+            if (sub == (i & 1)) Z[i] = i > col ? 0.f : ((i == col ? 1.f : v) / S[i * P + i]);
+        }
+    }
+    __syncthreads();
     float* Li = Dinv + (K / NB) * 2 * NB * NB;
     float* Ui = Li + NB * NB;
-    if (t < b) {
-        for (int i = 0; i < b; i++) {  // L z = e_t (unit lower)
-            float s0 = i == t ? 1.f : 0.f, s1 = 0.f;
-            int j = t;
-            for (; j + 1 < i; j += 2) {
-                s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
-                s1 = __fmaf_rn(-S[i * P + j + 1], Z[t * P + j + 1], s1);
-            }
-            if (j < i) s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
-            Z[t * P + i] = i < t ? 0.f : s0 + s1;
-        }
-        for (int i = 0; i < b; i++) Li[t * NB + i] = Z[t * P + i];
-        for (int i = b - 1; i >= 0; i--) {  // U z = e_t
-            float s0 = i == t ? 1.f : 0.f, s1 = 0.f;
-            if (i <= t) {
-                int j = i + 1;
-                for (; j + 1 <= t; j += 2) {
-                    s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
-                    s1 = __fmaf_rn(-S[i * P + j + 1], Z[t * P + j + 1], s1);
-                }
-                if (j <= t) s0 = __fmaf_rn(-S[i * P + j], Z[t * P + j], s0);
-            }
-            Z[t * P + i] = i > t ? 0.f : (s0 + s1) / S[i * P + i];
-        }
-        for (int i = 0; i < b; i++) Ui[t * NB + i] = Z[t * P + i];
+    for (int idx = t; idx < NB * NB; idx += DT) {
+        int c = idx / NB, rr = idx % NB;
+        Li[idx] = ZL[c * P + rr];
+        Ui[idx] = ZU[c * P + rr];
+        if (rr < b && c < b) A[(K + c) * n + K + rr] = S[rr * P + c];
     }
 }
 
@@ -102,7 +132,7 @@ inline unsigned nb256(int64_t m) { return (unsigned)((m + 255) / 256); }
 bool g_attr_set = false;
 void set_attrs() {
     if (g_attr_set) return;
-    cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * NB * P * 4);
+    cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
     g_attr_set = true;
 }
 
@@ -134,34 +164,53 @@ cudaError_t prepare_blas(cublasHandle_t h, LuGraphs* G, cudaStream_t s) {
     return cudaSuccess;
 }
 
-cudaError_t factor_body(cublasHandle_t h, float* LU, float* Dinv, float* W, int64_t n, int* bad, cudaStream_t s) {
-    const float one = 1.f, mone = -1.f, zero = 0.f;
+// The two panel solves of block K as GEMMs through W (copied back):
+//   L21 = A21 U_KK^{-1},  U12 = L_KK^{-1} A12.
+cudaError_t panel_gemms(cublasHandle_t h, float* LU, const float* Dinv, float* W, int64_t n, int64_t K,
+                        cudaStream_t s) {
+    const float one = 1.f, zero = 0.f;
     cublasComputeType_t ct = lu_compute();
+    int b = (int)std::min<int64_t>(NB, n - K);
+    const float* Li = Dinv + (K / NB) * 2 * NB * NB;
+    const float* Ui = Li + NB * NB;
+    int64_t rest = n - K - b;
+    if (rest <= 0) return cudaSuccess;
+    if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, b, b, &one, LU + K * n + K + b, CUDA_R_32F, (int)n, Ui,
+                     CUDA_R_32F, NB, &zero, W, CUDA_R_32F, (int)rest, ct, CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+        return cudaErrorUnknown;
+    cudaError_t e = cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float),
+                                      rest * sizeof(float), b, cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)rest, b, &one, Li, CUDA_R_32F, NB, LU + (K + b) * n + K,
+                     CUDA_R_32F, (int)n, &zero, W, CUDA_R_32F, b, ct, CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+        return cudaErrorUnknown;
+    return cudaMemcpy2DAsync(LU + (K + b) * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), rest,
+                             cudaMemcpyDeviceToDevice, s);
+}
+
+// A22 block [r0, r0+m) x [c0, c0+nc) -= L(r0.., K..K+b) U(K..K+b, c0..)
+cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, int64_t r0, int64_t m, int64_t c0,
+                     int64_t nc) {
+    if (m <= 0 || nc <= 0) return cudaSuccess;
+    const float one = 1.f, mone = -1.f;
+    cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)nc, b, &mone, LU + K * n + r0,
+                                     CUDA_R_32F, (int)n, LU + c0 * n + K, CUDA_R_32F, (int)n, &one, LU + c0 * n + r0,
+                                     CUDA_R_32F, (int)n, lu_compute(), CUBLAS_GEMM_DEFAULT);
+    return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
+}
+
+// Right-looking blocked LU: per block, the diagonal kernel, the two panel GEMMs, then
+// one trailing-update GEMM over the whole remaining matrix.  (Factoring the next
+// diagonal block on a side stream beside the trailing GEMM was measured slower here:
+// the split GEMMs cost more than the overlap recovered.)
+cudaError_t factor_body(cublasHandle_t h, float* LU, float* Dinv, float* W, int64_t n, int* bad, cudaStream_t s) {
     for (int64_t K = 0; K < n; K += NB) {
         int b = (int)std::min<int64_t>(NB, n - K);
-        const float* Li = Dinv + (K / NB) * 2 * NB * NB;
-        const float* Ui = Li + NB * NB;
-        k_lu_diag<<<1, NB, 2 * NB * P * 4, s>>>(LU, n, K, b, Dinv, bad);
-        int64_t rest = n - K - b;
-        if (rest <= 0) continue;
-        // L21 = A21 U11^{-1} and U12 = L11^{-1} A12 as GEMMs into W, copied back
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, b, b, &one, LU + K * n + K + b, (int)n, Ui, NB, &zero,
-                        W, (int)rest) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        cudaError_t e = cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float),
-                                          rest * sizeof(float), b, cudaMemcpyDeviceToDevice, s);
+        k_lu_diag<<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, Dinv, bad);
+        cudaError_t e = panel_gemms(h, LU, Dinv, W, n, K, s);
         if (e != cudaSuccess) return e;
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)rest, b, &one, Li, NB, LU + (K + b) * n + K, (int)n,
-                        &zero, W, b) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        e = cudaMemcpy2DAsync(LU + (K + b) * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), rest,
-                              cudaMemcpyDeviceToDevice, s);
-        if (e != cudaSuccess) return e;
-        cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, (int)rest, b, &mone,
-                                         LU + K * n + K + b, CUDA_R_32F, (int)n, LU + (K + b) * n + K, CUDA_R_32F,
-                                         (int)n, &one, LU + (K + b) * n + K + b, CUDA_R_32F, (int)n, ct,
-                                         CUBLAS_GEMM_DEFAULT);
-        if (st != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+        int64_t K1 = K + b, rest = n - K1;
+        if (rest > 0 && (e = trailing(h, LU, n, K, b, K1, rest, K1, rest)) != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }

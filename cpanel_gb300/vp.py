@@ -14,7 +14,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _lib
+from . import _lib, _shutting_down_now
 from ._lib import VEL_ALG, VEL_GAUSS, VEL_GAUSS_SYM
 
 NODE_FIELDS = 24
@@ -61,7 +61,6 @@ class ParticleFMM:
     def __del__(self):
         h = getattr(self, "h", None)
         if h:
-            from . import _shutting_down_now
             if not _shutting_down_now():
                 self.ctx.L.cpg_ptree_destroy(h)
             self.h = None

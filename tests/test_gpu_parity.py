@@ -131,6 +131,17 @@ def test_mixed_matches_plain_within_tolerance(cg, small):
     assert np.all(np.abs(rm["CL"] - rp["CL"]) <= 1e-6 * np.abs(rp["CL"]) + 1e-9)
 
 
+def test_mixed_many_right_hand_sides(cg, small):
+    """More cases than one column group of the blocked triangular solves (32)."""
+    g, m, Ao, Bo, refs = small
+    flows = [(1.0, -4.0 + 0.4 * q, 0.5 * (q % 3), 0.1) for q in range(40)]
+    rp = cg.solve_cases(g, flows, precision="fp64", **refs)
+    rm = cg.solve_cases(g, flows, precision="mixed", **refs)
+    assert rm["status"] == 0
+    assert np.abs(rm["cp"] - rp["cp"]).max() <= 1e-5
+    assert np.all(np.abs(rm["CL"] - rp["CL"]) <= 1e-6 * np.abs(rp["CL"]) + 1e-9)
+
+
 def test_small_steady_workload_parity(cg):
     """The 3,900-panel NACA 0012 wing (alpha = 5 deg, Mach 0.1): plain GPU vs oracle."""
     from cpanel_gb300 import wing

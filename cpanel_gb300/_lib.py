@@ -66,9 +66,22 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            # cpanel_vp.h
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_particles_velocity", "cpg_particles_stretch_diff",
-           "cpg_panels_velocity"]
+           "cpg_panels_velocity", "cpg_panels_stretching", "cpg_vp_topology", "cpg_vpcase_create",
+           "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_particles",
+           "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices"]
 
 VEL_GAUSS_SYM, VEL_GAUSS, VEL_ALG = 1, 2, 3
+
+
+class VPParams(C.Structure):
+    _fields_ = [("V", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("dt", C.c_double),
+                ("cref", C.c_double), ("accelerate", C.c_int)]
+
+
+class VPInfo(C.Structure):
+    _fields_ = [("n_body", C.c_int64), ("n_w1", C.c_int64), ("n_w2", C.c_int64), ("n_particles", C.c_int64),
+                ("timestep", C.c_int64), ("solver_iters", C.c_int64), ("dt", C.c_double),
+                ("n_tree_nodes", C.c_int64)]
 
 
 class PTreeInfo(C.Structure):
@@ -121,6 +134,17 @@ def load():
     L.cpg_bh_particles.argtypes = [vp, vp, vp, vp]
     L.cpg_particles_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
     L.cpg_particles_stretch_diff.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp]
+    L.cpg_panels_stretching.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, vp, C.c_int64, vp]
+    L.cpg_vp_topology.argtypes = [D, C.c_int64, I64, I32, C.c_int64, C.c_double, C.c_double, I64, D, D, D, I32, D, I32]
+    L.cpg_vpcase_create.argtypes = [vp, D, C.c_int64, I64, I32, C.c_int64, C.POINTER(VPParams), C.POINTER(vp)]
+    L.cpg_vpcase_destroy.argtypes = [vp]
+    L.cpg_vpcase_destroy.restype = None
+    L.cpg_vpcase_info_get.argtypes = [vp, C.POINTER(VPInfo)]
+    L.cpg_vpcase_step.argtypes = [vp, C.c_int]
+    L.cpg_vpcase_particles.argtypes = [vp, D, D, D, I32, I32]
+    L.cpg_vpcase_strengths.argtypes = [vp, D, D, D, D]
+    L.cpg_vpcase_wake.argtypes = [vp, D, D]
+    L.cpg_vpcase_matrices.argtypes = [vp, D, D, D]
     L.cpg_panels_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, C.c_int64, vp]
     _lib = L
     return L

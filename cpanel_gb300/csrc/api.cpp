@@ -97,6 +97,13 @@ struct cpg_ptree {
     DevBuf nodes, parts;
 };
 
+namespace cpg {
+void ctx_set_error(cpg_ctx* ctx, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+}
+cudaStream_t ctx_stream(cpg_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
+}  // namespace cpg
+
 namespace {
 
 int fail(cpg_ctx* c, int code, const std::string& msg) {

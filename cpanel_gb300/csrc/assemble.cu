@@ -332,6 +332,11 @@ int64_t chunk_for(int64_t n) {
 
 namespace cpg {
 
+cudaError_t launch_pack_records(const double* verts, int64_t m, double* rec, cudaStream_t s) {
+    if (m > 0) k_pack_records<<<(unsigned)((m + 127) / 128), 128, 0, s>>>(verts, m, rec);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_panels_velocity(const double* body_verts, const double* sigma, const double* mu, int64_t nb,
                                    const double* wake_verts, const double* wmu, int64_t nw, const double* pts,
                                    int64_t m, double* rec, double* vel, cudaStream_t s) {

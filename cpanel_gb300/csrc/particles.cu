@@ -172,6 +172,56 @@ __global__ void __launch_bounds__(128) k_bh_particles(const BHNode* __restrict__
     if (D) { dif[o] = d.x; dif[o + 1] = d.y; dif[o + 2] = d.z; }
 }
 
+// The same traversal for an explicit list of target particles (original order), which
+// may include particles that are in no leaf (shed after the tree was built).
+template <bool V, bool S, bool D>
+__global__ void __launch_bounds__(128) k_bh_targets(const BHNode* __restrict__ nodes, int nn,
+                                                    const BHPart* __restrict__ slots, double theta,
+                                                    const BHPart* __restrict__ tgt, int64_t m, VPConst c,
+                                                    double* __restrict__ vel, double* __restrict__ str,
+                                                    double* __restrict__ dif) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    const Tgt t = load_part_g(tgt, q);
+    dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
+    int i = 1;
+    while (i < nn) {
+        const BHNode nd = load_node(nodes, i);
+        if (nd.leaf) {
+            for (int32_t k = nd.first; k < nd.first + nd.count; k++) {
+                const Tgt mm = load_part_g(slots, k);
+                if (mm.idx == t.idx) continue;
+                if (V) v = v + vel_gauss_sym(mm, t, c);
+                if (S) s = s + stretch(mm, t, c);
+                if (D) d = d + diffusion(mm, t, c);
+            }
+            i++;
+        } else if (far_field(nd, t.x, theta)) {
+            const Tgt e{mk3(nd.ex, nd.ey, nd.ez), nd.erad, mk3(nd.ax, nd.ay, nd.az), -1.0};
+            if (V) v = v + vel_gauss_sym(e, t, c);
+            if (S) s = s + stretch(e, t, c);
+            if (D) d = d + diffusion(e, t, c);
+            i = nd.skip;
+        } else {
+            i++;
+        }
+    }
+    if (V) { vel[3 * q] = v.x; vel[3 * q + 1] = v.y; vel[3 * q + 2] = v.z; }
+    if (S) { str[3 * q] = s.x; str[3 * q + 1] = s.y; str[3 * q + 2] = s.z; }
+    if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
+}
+
+// slots[q] <- the current state of particle perm[q]
+__global__ void k_refresh_slots(const int64_t* __restrict__ perm, int64_t ns, const double* __restrict__ pos,
+                                const double* __restrict__ str, const double* __restrict__ rad,
+                                BHPart* __restrict__ slots) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= ns) return;
+    int64_t i = perm[q];
+    slots[q] = BHPart{pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], rad[i], str[3 * i], str[3 * i + 1], str[3 * i + 2],
+                      (double)i};
+}
+
 // particleFMM::barnesHutVel(POI): algebraic kernel in leaves and far nodes (node.h:236-264)
 __global__ void __launch_bounds__(128) k_bh_points(const BHNode* __restrict__ nodes, int nn,
                                                    const BHPart* __restrict__ parts, double theta,
@@ -271,6 +321,27 @@ cudaError_t launch_bh_particles(const BHNode* nodes, int nn, const BHPart* parts
         case 7: k_bh_particles<true, true, true><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
         default: return cudaSuccess;
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bh_targets(const BHNode* nodes, int nn, const BHPart* slots, double theta, const BHPart* tgt,
+                              int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    int mask = (vel ? 1 : 0) | (str ? 2 : 0) | (dif ? 4 : 0);
+    dim3 g(blocks(m, 128)), b(128);
+    switch (mask) {
+        case 1: k_bh_targets<true, false, false><<<g, b, 0, s>>>(nodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
+        case 6: k_bh_targets<false, true, true><<<g, b, 0, s>>>(nodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
+        case 7: k_bh_targets<true, true, true><<<g, b, 0, s>>>(nodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refresh_slots(const int64_t* perm, int64_t ns, const double* pos, const double* str,
+                                 const double* rad, BHPart* slots, cudaStream_t s) {
+    if (ns <= 0) return cudaSuccess;
+    k_refresh_slots<<<blocks(ns, 256), 256, 0, s>>>(perm, ns, pos, str, rad, slots);
     return cudaGetLastError();
 }
 

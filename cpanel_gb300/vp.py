@@ -175,3 +175,99 @@ def panels_velocity(body_verts, sigma, mu, wake_verts, wake_mu, points, ctx=None
     ctx.check(ctx.L.cpg_panels_velocity(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm), nw,
                                         _ptr(pts), pts.shape[0], _ptr(vel)), "panel velocity")
     return vel
+
+
+def panels_stretching(body_verts, sigma, mu, wake_verts, wake_mu, pos, strength, ctx=None):
+    """Sum of bodyPanel::partStretching (triangles) and wakePanel::partStretching (quads)."""
+    import torch
+    ctx = _ctx(ctx)
+    bv = _dev(body_verts, 9)
+    sg, mu_ = _dev(sigma).reshape(-1), _dev(mu).reshape(-1)
+    nw = 0 if wake_verts is None else int(np.prod(wake_verts.shape)) // 12
+    wv = _dev(wake_verts, 12) if nw else None
+    wm = _dev(wake_mu).reshape(-1) if nw else None
+    p, st = _dev(pos, 3), _dev(strength, 3)
+    out = torch.empty_like(p)
+    _sync()
+    ctx.check(ctx.L.cpg_panels_stretching(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm), nw,
+                                          _ptr(p), _ptr(st), p.shape[0], _ptr(out)), "panel stretching")
+    return out
+
+
+def vp_topology(nodes, tris, ids, V=1.0, dt=0.0):
+    """Host-only buffer wake: dict(counts, dt, w1, w2, w1_idx, w1_coef, w2_parent)."""
+    L = _lib.load()
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    tris = np.ascontiguousarray(tris, dtype=np.int64)
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    counts = np.zeros(3, dtype=np.int64)
+    dto = C.c_double(0)
+    args = (nodes.ctypes.data_as(_lib.D), len(nodes), tris.ctypes.data_as(_lib.I64), ids.ctypes.data_as(_lib.I32),
+            len(tris), V, dt, counts.ctypes.data_as(_lib.I64), C.byref(dto))
+    rc = L.cpg_vp_topology(*args, None, None, None, None, None)
+    if rc != 0:
+        raise _lib.CpgError(rc, "vp topology")
+    n1, n2 = int(counts[1]), int(counts[2])
+    w1, w2 = np.zeros((n1, 12)), np.zeros((n2, 12))
+    idx, coef, par = np.zeros((n1, 4), dtype=np.int32), np.zeros(n1), np.zeros(n2, dtype=np.int32)
+    L.cpg_vp_topology(*args, w1.ctypes.data_as(_lib.D), w2.ctypes.data_as(_lib.D), idx.ctypes.data_as(_lib.I32),
+                      coef.ctypes.data_as(_lib.D), par.ctypes.data_as(_lib.I32))
+    return dict(counts=counts, dt=dto.value, w1=w1, w2=w2, w1_idx=idx, w1_coef=coef, w2_parent=par)
+
+
+class VPCase:
+    """cpCaseVP on a body-only mesh, advanced step by step on the GPU."""
+
+    def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, ctx=None):
+        self.ctx = _ctx(ctx)
+        nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        tris = np.ascontiguousarray(tris, dtype=np.int64)
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0)
+        h = C.c_void_p()
+        self.ctx.check(self.ctx.L.cpg_vpcase_create(self.ctx.h, nodes.ctypes.data_as(_lib.D), len(nodes),
+                                                    tris.ctypes.data_as(_lib.I64), ids.ctypes.data_as(_lib.I32),
+                                                    len(tris), C.byref(prm), C.byref(h)), "vortex-particle case")
+        self.h = h
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            if not _shutting_down_now():
+                self.ctx.L.cpg_vpcase_destroy(h)
+            self.h = None
+
+    def info(self):
+        i = _lib.VPInfo()
+        self.ctx.check(self.ctx.L.cpg_vpcase_info_get(self.h, C.byref(i)), "info")
+        return {f: getattr(i, f) for f, _ in _lib.VPInfo._fields_}
+
+    def step(self, n=1):
+        self.ctx.check(self.ctx.L.cpg_vpcase_step(self.h, n), "step")
+        return self.info()["timestep"]
+
+    def particles(self):
+        n = self.info()["n_particles"]
+        pos, st, rad = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        shed, par = np.zeros(n, dtype=np.int32), np.zeros(n, dtype=np.int32)
+        self.ctx.check(self.ctx.L.cpg_vpcase_particles(self.h, pos.ctypes.data_as(_lib.D), st.ctypes.data_as(_lib.D),
+                                                       rad.ctypes.data_as(_lib.D), shed.ctypes.data_as(_lib.I32),
+                                                       par.ctypes.data_as(_lib.I32)), "particles")
+        return dict(pos=pos, strength=st, radius=rad, shed_time=shed, parent=par)
+
+    def strengths(self):
+        i = self.info()
+        sg, mu = np.zeros(i["n_body"]), np.zeros(i["n_body"])
+        m1, m2 = np.zeros(i["n_w1"]), np.zeros(i["n_w2"])
+        self.ctx.check(self.ctx.L.cpg_vpcase_strengths(self.h, sg.ctypes.data_as(_lib.D), mu.ctypes.data_as(_lib.D),
+                                                       m1.ctypes.data_as(_lib.D), m2.ctypes.data_as(_lib.D)),
+                       "strengths")
+        return dict(sigma=sg, mu=mu, mu_w1=m1, mu_w2=m2)
+
+    def matrices(self):
+        i = self.info()
+        n, n2 = i["n_body"], i["n_w2"]
+        A, B, Cm = np.zeros((n, n), order="F"), np.zeros((n, n), order="F"), np.zeros((n, n2), order="F")
+        self.ctx.check(self.ctx.L.cpg_vpcase_matrices(self.h, A.ctypes.data_as(_lib.D), B.ctypes.data_as(_lib.D),
+                                                      Cm.ctypes.data_as(_lib.D)), "matrices")
+        return A, B, Cm

@@ -21,6 +21,14 @@
  *   cpg_panels_velocity        bodyPanel::panelV + wakePanel::panelV summed over panels,
  *                              CPanel/bodyPanel.cpp:122-130, CPanel/wakePanel.cpp:89-92,
  *                              as called at CPanel/cpCaseVP.cpp:713-731
+ *   cpg_panels_stretching      bodyPanel::partStretching + wakePanel::partStretching summed
+ *                              over panels, CPanel/bodyPanel.cpp:697-1063,
+ *                              CPanel/wakePanel.cpp:266-289, CPanel/panel.cpp:113-153,813-966
+ *   cpg_vpcase_*               cpCaseVP on a body-only mesh: the buffer wake of
+ *                              CPanel/geometry.cpp:261-400,1313-1345, and cpCaseVP::run,
+ *                              CPanel/cpCaseVP.cpp:26-117 (convection, shedding, strength
+ *                              update, octree rebuild, source strengths, solve) one step
+ *                              at a time; the Trefftz-plane early stop is the caller's
  */
 #ifndef CPANEL_VP_H
 #define CPANEL_VP_H
@@ -91,6 +99,52 @@ int  cpg_particles_stretch_diff(cpg_ctx* ctx, const double* pos, const double* s
 int  cpg_panels_velocity(cpg_ctx* ctx, const double* body_verts, const double* sigma, const double* mu,
                          int64_t nb, const double* wake_verts, const double* wake_mu, int64_t nw,
                          const double* pts, int64_t m, double* vel);
+
+/* Panel-induced stretching on m particles (pos, strength m x 3): sum over nb body
+ * triangles (vertices nb x 9, sigma, mu) of bodyPanel::partStretching and over nw wake
+ * quadrilaterals (vertices nw x 12, mu) of wakePanel::partStretching.  Device arrays. */
+int  cpg_panels_stretching(cpg_ctx* ctx, const double* body_verts, const double* sigma, const double* mu,
+                           int64_t nb, const double* wake_verts, const double* wake_mu, int64_t nw,
+                           const double* pos, const double* strength, int64_t m, double* out);
+
+/* ---- the vortex-particle case ---- */
+typedef struct cpg_vpcase cpg_vpcase;
+typedef struct {
+    double V, alpha, beta; /* free stream (degrees)                                       */
+    double dt;             /* time step; <= 0: mean trailing-edge length / V (calcTimeStep) */
+    double cref;           /* reference chord of the far-field cut-offs (12 c, 20 c)       */
+    int accelerate;        /* Barnes-Hut (inputParams::accelerateCode) or direct sums      */
+} cpg_vp_params;
+typedef struct {
+    int64_t n_body, n_w1, n_w2;   /* body panels, first and second buffer rows           */
+    int64_t n_particles;
+    int64_t timestep;             /* completed steps (the reference's timestep counter)   */
+    int64_t solver_iters;         /* BiCGSTAB iterations of the last solve                */
+    double dt;
+    int64_t n_tree_nodes;         /* octree of the last rebuild                          */
+} cpg_vp_info;
+/* Host-only build of the buffer wake (no device use): counts[3] = n_body, n_w1, n_w2 and
+ * *dt_out always; the other outputs (w1/w2 vertices n x 12, first-row interpolation
+ * columns n_w1 x 4 and coefficients, second-row parents) when non-null. */
+int  cpg_vp_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
+                     int64_t n_tris, double V, double dt, int64_t* counts, double* dt_out, double* w1_verts,
+                     double* w2_verts, int32_t* w1_idx4, double* w1_coef, int32_t* w2_parent);
+/* Mesh as in cpg_geometry_create (host arrays, 1-based triangles); no wake panels. */
+int  cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const int64_t* tris,
+                       const int32_t* ids, int64_t n_tris, const cpg_vp_params* params, cpg_vpcase** out);
+void cpg_vpcase_destroy(cpg_vpcase* c);
+int  cpg_vpcase_info_get(const cpg_vpcase* c, cpg_vp_info* info);
+/* advance nsteps time steps (step 1: steady solve; 2: first buffer convection; then the loop) */
+int  cpg_vpcase_step(cpg_vpcase* c, int nsteps);
+/* host copies: particles in shedding order (pos, strength n x 3, radius, shed step, index
+ * of the shedding second-row panel); any pointer may be null */
+int  cpg_vpcase_particles(cpg_vpcase* c, double* pos, double* strength, double* radius, int32_t* shed_time,
+                          int32_t* parent);
+int  cpg_vpcase_strengths(cpg_vpcase* c, double* sigma, double* mu, double* mu_w1, double* mu_w2);
+/* buffer-wake quadrilaterals (n_w1 x 12, n_w2 x 12 doubles) */
+int  cpg_vpcase_wake(const cpg_vpcase* c, double* w1_verts, double* w2_verts);
+/* A, B (n x n) and C (n x n_w2), column-major, host */
+int  cpg_vpcase_matrices(cpg_vpcase* c, double* A, double* B, double* C);
 
 #ifdef __cplusplus
 }

@@ -11,13 +11,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = ["cpo.cpp", "cpo_vp.cpp"]
+HEADERS = ["cpo.h", "cpo_vp.h", "cpo_pair.h", "cpo_vpcase.inc"]
 
 
 def _stale():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, "cpo.h"), os.path.join(HERE, "cpo_vp.h")]
+    deps = [os.path.join(HERE, s) for s in SOURCES] + [os.path.join(HERE, h) for h in HEADERS]
     return any(os.path.exists(d) and os.path.getmtime(d) > t for d in deps)
 
 

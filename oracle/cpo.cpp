@@ -53,8 +53,9 @@ struct Edge {
     bool TE = false;
 };
 struct Tri {  // panel::setGeom state, CPanel/panel.cpp:33-72
-    int node[3];
-    int edge[3];
+    int node[4];  // triangles use 3; the vortex-particle buffer wake uses quads
+    int edge[4];
+    int nv = 3;
     V3 center, normal, bez;
     double area = 0, longSide = 0;
     int surfID = 0, fileTri = 0;
@@ -1397,3 +1398,6 @@ int cpo_case_run(void* mp, const double* A, const double* B, const cpo_case_para
 }
 
 }  // extern "C"
+
+// vortex-particle case (buffer wake, shedding, panel stretching, time loop)
+#include "cpo_vpcase.inc"

@@ -55,6 +55,20 @@ def lib():
         L.cpo_bicgstab.argtypes = [D, C.c_int64, D, D, C.c_double, C.c_int64, I64, D, C.c_int]
         L.cpo_tri_dub_v_inf.argtypes = [D, D, D]
         L.cpo_panels_velocity.argtypes = [D, D, D, C.c_int64, D, D, C.c_int64, D, C.c_int64, D, C.c_int]
+        L.cpo_vpcase_new.restype = C.c_void_p
+        L.cpo_vpcase_new.argtypes = [D, C.c_int64, I64, I32, C.c_int64, C.c_double, C.c_double, C.c_double,
+                                     C.c_double, C.c_double, C.c_int, C.c_int]
+        L.cpo_vpcase_free.argtypes = [C.c_void_p]
+        L.cpo_vpcase_info.argtypes = [C.c_void_p, I64]
+        L.cpo_vpcase_dt.restype = C.c_double
+        L.cpo_vpcase_dt.argtypes = [C.c_void_p]
+        L.cpo_vpcase_wake.argtypes = [C.c_void_p, D, D, I32, D]
+        L.cpo_vpcase_matrices.argtypes = [C.c_void_p, D, D, D]
+        L.cpo_vpcase_step.restype = C.c_int
+        L.cpo_vpcase_step.argtypes = [C.c_void_p]
+        L.cpo_vpcase_particles.argtypes = [C.c_void_p, D, D, D, I32, I32]
+        L.cpo_vpcase_strengths.argtypes = [C.c_void_p, D, D, D, D]
+        L.cpo_panels_stretching.argtypes = [D, D, D, C.c_int64, D, D, C.c_int64, D, D, C.c_int64, D]
         L.cpo_vp_direct_velocity.argtypes = [D, D, D, C.c_int64, D, C.c_int64, C.c_int, D]
         L.cpo_vp_direct_stretch.argtypes = [D, D, D, C.c_int64, D]
         L.cpo_vp_direct_diffusion.argtypes = [D, D, D, C.c_int64, D]
@@ -319,3 +333,82 @@ class ParticleTree:
         out = np.zeros((len(self.pos), 3))
         lib().cpo_bh_diffusion(self.h, _p(out))
         return out
+
+
+def panels_stretching(bverts, sigma, mu, wverts, wmu, pos, strength):
+    """Sum of bodyPanel::partStretching (triangles) and wakePanel::partStretching (quads)."""
+    L = lib()
+    bv = np.ascontiguousarray(bverts, dtype=np.float64).reshape(-1, 9)
+    wv = np.ascontiguousarray(wverts, dtype=np.float64).reshape(-1, 12)
+    p = np.ascontiguousarray(pos, dtype=np.float64).reshape(-1, 3)
+    st = np.ascontiguousarray(strength, dtype=np.float64).reshape(-1, 3)
+    out = np.zeros((len(p), 3))
+    L.cpo_panels_stretching(_p(bv), _p(np.ascontiguousarray(sigma, dtype=np.float64)),
+                            _p(np.ascontiguousarray(mu, dtype=np.float64)), len(bv), _p(wv),
+                            _p(np.ascontiguousarray(wmu, dtype=np.float64)), len(wv), _p(p), _p(st), len(p), _p(out))
+    return out
+
+
+class VPCase:
+    """cpCaseVP on a body-only mesh: buffer wake, shedding, stretching, AB2 time loop."""
+
+    def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, num_steps=10):
+        L = lib()
+        self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+        self.tris = np.ascontiguousarray(tris, dtype=np.int64)
+        self.ids = np.ascontiguousarray(ids, dtype=np.int32)
+        self.h = L.cpo_vpcase_new(_p(self.nodes), len(self.nodes), _p(self.tris, I64), _p(self.ids, I32),
+                                  len(self.tris), V, alpha, beta, dt, cref, 1 if accelerate else 0, num_steps)
+        if not self.h:
+            raise ValueError("mesh has wake panels; the vortex-particle case builds its own")
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            lib().cpo_vpcase_free(h)
+            self.h = None
+
+    def info(self):
+        out = np.zeros(7, dtype=np.int64)
+        lib().cpo_vpcase_info(self.h, _p(out, I64))
+        return dict(n_body=int(out[0]), n_w1=int(out[1]), n_w2=int(out[2]), n_particles=int(out[3]),
+                    timestep=int(out[4]), n_nodes=int(out[5]), last_iters=int(out[6]))
+
+    @property
+    def dt(self):
+        return lib().cpo_vpcase_dt(self.h)
+
+    def wake(self):
+        i = self.info()
+        w1 = np.zeros((i["n_w1"], 12))
+        w2 = np.zeros((i["n_w2"], 12))
+        cols = np.zeros((i["n_w1"], 4), dtype=np.int32)
+        coef = np.zeros(i["n_w1"])
+        lib().cpo_vpcase_wake(self.h, _p(w1), _p(w2), _p(cols, I32), _p(coef))
+        return w1, w2, cols, coef
+
+    def matrices(self):
+        i = self.info()
+        n = i["n_body"]
+        A = np.zeros((n, n), order="F")
+        B = np.zeros((n, n), order="F")
+        Cm = np.zeros((n, i["n_w2"]), order="F")
+        lib().cpo_vpcase_matrices(self.h, _p(A), _p(B), _p(Cm))
+        return A, B, Cm
+
+    def step(self):
+        return lib().cpo_vpcase_step(self.h)
+
+    def particles(self):
+        n = self.info()["n_particles"]
+        pos, st, rad = np.zeros((n, 3)), np.zeros((n, 3)), np.zeros(n)
+        shed, parent = np.zeros(n, dtype=np.int32), np.zeros(n, dtype=np.int32)
+        lib().cpo_vpcase_particles(self.h, _p(pos), _p(st), _p(rad), _p(shed, I32), _p(parent, I32))
+        return dict(pos=pos, strength=st, radius=rad, shed_time=shed, parent=parent)
+
+    def strengths(self):
+        i = self.info()
+        sg, mu = np.zeros(i["n_body"]), np.zeros(i["n_body"])
+        m1, m2 = np.zeros(i["n_w1"]), np.zeros(i["n_w2"])
+        lib().cpo_vpcase_strengths(self.h, _p(sg), _p(mu), _p(m1), _p(m2))
+        return dict(sigma=sg, mu=mu, mu_w1=m1, mu_w2=m2)

@@ -125,3 +125,67 @@ def test_panels_velocity_matches_oracle(built):
     got = _np(vp.panels_velocity(_cuda(bv), _cuda(sigma), _cuda(mu), None, None, _cuda(pts)))
     err = np.abs(got - ref).max(axis=1) / np.maximum(np.abs(ref).max(axis=1), 1.0)
     assert err.max() < 1e-10
+
+
+# ---- vortex-particle case ----
+
+def _vp_wing(n_chord=8, n_span=6, taper=1.0, sweep=0.0):
+    from cpanel_gb300 import wing
+    spec = wing.WingSpec(m=0.04, p=0.4, t=0.12, root_chord=1.0, span=4.0, taper=taper, sweep_deg=sweep,
+                         n_chord=n_chord, n_span=n_span, wake_len=10.0, wake_dir=wing.wake_dir_for(8.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    return nodes, tris[keep], ids[keep]
+
+
+def test_panels_stretching_matches_oracle(built):
+    from cpanel_gb300 import vp
+    nodes, tris, ids = _vp_wing(10, 7)
+    m = po.Mesh(nodes, tris, ids)
+    bv = m.body_verts()
+    T = vp.vp_topology(nodes, tris, ids)
+    wv = T["w1"]
+    rng = np.random.default_rng(21)
+    sigma, mu, wmu = rng.normal(size=len(bv)), rng.normal(size=len(bv)), rng.normal(size=len(wv))
+    c = bv.reshape(-1, 3, 3).mean(axis=1)
+    pos = np.concatenate([c[::3] + rng.normal(size=(len(c[::3]), 3)) * 0.05,        # near the surface
+                          rng.normal(size=(150, 3)) * [2.0, 2.0, 0.5] + [1.2, 0, 0],  # near the buffer wake
+                          rng.normal(size=(50, 3)) * 10])                            # far field
+    st = rng.normal(size=pos.shape) * 0.01
+    ref = po.panels_stretching(bv, sigma, mu, wv, wmu, pos, st)
+    got = _np(vp.panels_stretching(_cuda(bv), _cuda(sigma), _cuda(mu), _cuda(wv), _cuda(wmu), _cuda(pos), _cuda(st)))
+    scale = np.maximum(np.abs(ref).max(axis=1), 1e-6)
+    assert (np.abs(got - ref).max(axis=1) / scale).max() < 1e-9
+
+
+def test_vp_matrices_match_oracle(built):
+    from cpanel_gb300 import vp
+    nodes, tris, ids = _vp_wing(10, 7, 0.7, 10.0)
+    S = po.VPCase(nodes, tris, ids, V=1.0, alpha=8.0)
+    G = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0)
+    Ao, Bo, Co = S.matrices()
+    Ag, Bg, Cg = G.matrices()
+    for X, Y in ((Ag, Ao), (Bg, Bo), (Cg, Co)):
+        assert np.abs(X - Y).max() <= 1e-12 * np.abs(Y).max()
+
+
+@pytest.mark.parametrize("accelerate", [True, False])
+def test_vp_time_loop_matches_oracle(built, accelerate):
+    """Nine steps of cpCaseVP::run: shedding order exact, state to 1e-9 relative."""
+    from cpanel_gb300 import vp
+    nodes, tris, ids = _vp_wing(8, 6)
+    S = po.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, accelerate=accelerate)
+    G = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, accelerate=accelerate)
+    for step in range(9):
+        S.step()
+        G.step()
+        po_, pg = S.particles(), G.particles()
+        assert len(pg["pos"]) == len(po_["pos"])
+        assert np.array_equal(pg["shed_time"], po_["shed_time"]) and np.array_equal(pg["parent"], po_["parent"])
+        if len(po_["pos"]):
+            for key in ("pos", "strength", "radius"):
+                ref = po_[key]
+                assert np.abs(pg[key] - ref).max() <= 1e-9 * max(np.abs(ref).max(), 1e-12), (step, key)
+        so, sg = S.strengths(), G.strengths()
+        for key in ("sigma", "mu", "mu_w1", "mu_w2"):
+            assert np.abs(sg[key] - so[key]).max() <= 1e-9 * max(np.abs(so[key]).max(), 1e-12), (step, key)

@@ -260,3 +260,54 @@ def test_dub_v_inf_single_triangle():
     for poi in ([2.0, 2.0, 2.0], [7.0, 7.0, 7.0], [0.1, 0.0, 0.05]):
         vs, vd = po.tri_v_inf(v9, poi)
         assert np.allclose(po.tri_dub_v_inf(v9, poi), vd, rtol=1e-12, atol=1e-15)
+
+
+# ---- vortex-particle case: the buffer wake built by the product vs the oracle ----
+
+def _vp_wing(n_chord=8, n_span=6, taper=1.0, sweep=0.0):
+    from cpanel_gb300 import wing
+    spec = wing.WingSpec(m=0.04, p=0.4, t=0.12, root_chord=1.0, span=4.0, taper=taper, sweep_deg=sweep,
+                         n_chord=n_chord, n_span=n_span, wake_len=10.0, wake_dir=wing.wake_dir_for(8.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000  # the VP case takes a body-only mesh (CPanel/geometry.cpp:270-277)
+    return nodes, tris[keep], ids[keep]
+
+
+@pytest.mark.parametrize("shape", [(8, 6, 1.0, 0.0), (10, 9, 0.7, 10.0), (14, 7, 0.6, 20.0)])
+def test_vp_buffer_wake_matches_oracle_bit_for_bit(built, shape):
+    from cpanel_gb300 import vp
+    nodes, tris, ids = _vp_wing(*shape)
+    S = po.VPCase(nodes, tris, ids, V=1.0, alpha=8.0)
+    w1, w2, cols, coef = S.wake()
+    T = vp.vp_topology(nodes, tris, ids, V=1.0)
+    assert T["dt"] == S.dt
+    assert np.array_equal(T["w1"], w1) and np.array_equal(T["w2"], w2)
+    assert np.array_equal(T["w1_idx"], cols) and np.array_equal(T["w1_coef"], coef)
+    # one first-row and one second-row quad per trailing-edge edge, second row behind the first
+    assert len(w1) == len(w2) == S.info()["n_w1"]
+    assert np.all(w2.reshape(-1, 4, 3)[:, :, 0].mean(1) > w1.reshape(-1, 4, 3)[:, :, 0].mean(1))
+
+
+def test_vp_mesh_with_wake_panels_is_rejected(built):
+    from cpanel_gb300 import vp, wing
+    spec = wing.WingSpec(m=0.0, p=0.4, t=0.12, root_chord=1.0, span=4.0, taper=1.0, sweep_deg=0.0, n_chord=8,
+                         n_span=6, wake_len=10.0, wake_dir=wing.wake_dir_for(5.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    with pytest.raises(ValueError):
+        po.VPCase(nodes, tris, ids)
+    with pytest.raises(Exception):
+        vp.vp_topology(nodes, tris, ids)
+
+
+def test_vp_oracle_sheds_one_particle_per_te_edge_in_panel_order():
+    nodes, tris, ids = _vp_wing()
+    S = po.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, accelerate=True)
+    n2 = S.info()["n_w2"]
+    for _ in range(6):
+        S.step()
+    p = S.particles()
+    # steps 1-2 shed nothing; from step 3 every second-row panel sheds once per step, in order
+    assert len(p["pos"]) == 4 * n2
+    assert list(p["shed_time"]) == [t for t in range(3, 7) for _ in range(n2)]
+    assert list(p["parent"]) == list(range(n2)) * 4
+    assert np.all(np.isfinite(p["pos"])) and np.all(p["radius"] > 0)

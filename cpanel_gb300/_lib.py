@@ -68,9 +68,21 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_particles_velocity", "cpg_particles_stretch_diff",
            "cpg_panels_velocity", "cpg_panels_stretching", "cpg_vp_topology", "cpg_vpcase_create",
            "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_particles",
-           "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices"]
+           "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices",
+           # cpanel_serve.h
+           "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint"]
 
 VEL_GAUSS_SYM, VEL_GAUSS, VEL_ALG = 1, 2, 3
+
+
+class ServerParams(C.Structure):
+    _fields_ = [("device", C.c_int), ("slots", C.c_int), ("budget_bytes", C.c_double), ("precision", C.c_int)]
+
+
+class RequestInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("n_body", C.c_int64), ("k", C.c_int), ("footprint_bytes", C.c_int64),
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double),
+                ("running_at_start", C.c_int), ("message", C.c_char * 160)]
 
 
 class VPParams(C.Structure):
@@ -134,6 +146,14 @@ def load():
     L.cpg_bh_particles.argtypes = [vp, vp, vp, vp]
     L.cpg_particles_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, C.c_int64, C.c_int, vp]
     L.cpg_particles_stretch_diff.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp]
+    L.cpg_server_create.argtypes = [C.POINTER(ServerParams), C.POINTER(vp)]
+    L.cpg_server_destroy.argtypes = [vp]
+    L.cpg_server_destroy.restype = None
+    L.cpg_server_submit.argtypes = [vp, D, C.c_int64, I64, I32, C.c_int64, C.POINTER(Flow), C.c_int, C.POINTER(Refs),
+                                    I64]
+    L.cpg_server_wait.argtypes = [vp, C.c_int64, D, D, D, C.POINTER(RequestInfo)]
+    L.cpg_server_footprint.argtypes = [C.c_int64, C.c_int, C.c_int]
+    L.cpg_server_footprint.restype = C.c_int64
     L.cpg_panels_stretching.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, vp, C.c_int64, vp]
     L.cpg_vp_topology.argtypes = [D, C.c_int64, I64, I32, C.c_int64, C.c_double, C.c_double, I64, D, D, D, I32, D, I32]
     L.cpg_vpcase_create.argtypes = [vp, D, C.c_int64, I64, I32, C.c_int64, C.POINTER(VPParams), C.POINTER(vp)]

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -129,11 +130,13 @@ __global__ void k_addf(double* __restrict__ x, const float* __restrict__ d, int6
 
 inline unsigned nb256(int64_t m) { return (unsigned)((m + 255) / 256); }
 
-bool g_attr_set = false;
+// once per device, also when several host threads start at the same time
 void set_attrs() {
-    if (g_attr_set) return;
-    cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
-    g_attr_set = true;
+    static std::once_flag once[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::call_once(once[dev & 63],
+                   [] { cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM); });
 }
 
 cublasComputeType_t lu_compute() {

@@ -5,6 +5,7 @@
 //     chain, bodyPanel::pntVelocity :490-521), Cp (:591-594), forces and moments
 //     (cpCase::compVelocity, CPanel/cpCase.cpp:342-365) and the Trefftz plane
 //     (wake::trefftzPlane / Vradial / wakeStrength, CPanel/wake.cpp:146-188,478-597).
+#include <mutex>
 #include <vector>
 
 #include "assemble.h"
@@ -17,7 +18,6 @@ namespace {
 // zero row) for N = 3 and N = 2, orders 0..3.  c_ms[N-2][order][k][d].
 __constant__ int8_t c_ms[2][4][19][3];
 __constant__ int c_t[2][4];
-bool g_tables_ready = false;
 
 void build_tables() {
     int8_t ms[2][4][19][3] = {};
@@ -72,7 +72,14 @@ void build_tables() {
         }
     cudaMemcpyToSymbol(c_ms, ms, sizeof(ms));
     cudaMemcpyToSymbol(c_t, tt, sizeof(tt));
-    g_tables_ready = true;
+}
+
+// once per device, also when several host threads start at the same time
+void ensure_tables() {
+    static std::once_flag once[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::call_once(once[dev & 63], build_tables);
 }
 
 constexpr int WPB = 2;        // warps (panels) per block
@@ -485,7 +492,7 @@ cudaError_t launch_widen(const float* a, double* b, int64_t m, cudaStream_t s) {
 }
 
 cudaError_t launch_chtls_weights(const PostTables& t, cudaStream_t s) {
-    if (!g_tables_ready) build_tables();
+    ensure_tables();
     if (t.n <= 0) return cudaSuccess;
     ProfScope ps(Prof::CHTLS, s);
     k_chtls<<<(unsigned)((t.n + WPB - 1) / WPB), 32 * WPB, 0, s>>>(t);

@@ -59,7 +59,7 @@ def config_dict(info, name="multi_rhs"):
     stations = {"multi_rhs": 61, "mid": 25}[name]
     return {"workload": "NACA4412 tapered AR6 wing, 80 pts/side x %d stations, 17 alphas (-4..12 deg)" % stations,
             "body_panels": info["n_body"], "wake_panels": info["n_wake"], "alphas": len(ALPHAS), "mach": MACH,
-            "precision": "mixed: df32 far field + FP64 near field, FP32 LU + refinement to 1e-10",
+            "precision": "mixed: df32 far field + FP64 near field, FP32 LU + refinement to 1e-12",
             "l2": "inputs larger than L2 (A = 2 x 1.49 GB)", "parallelism": "replicas"}
 
 
@@ -161,6 +161,82 @@ def cpu_cost_model(nodes, tris, ids, refs, nthreads):
     return k / t_sweep, sample
 
 
+def _wing_with(ntri_target, rng, **kw):
+    """A seeded NACA wing with about ntri_target body triangles (for the request mix)."""
+    from cpanel_gb300 import wing
+    nc = int(rng.integers(20, 101))
+    ns = int(max(15, min(400, round(ntri_target / (4.0 * (nc - 1)) + 1))))
+    taper = float(rng.uniform(0.3, 1.0))
+    span = float(rng.uniform(3, 10)) * (1 + taper) / 2
+    spec = wing.WingSpec(m=float(rng.uniform(0, 0.06)), p=float(rng.uniform(0.2, 0.5)), t=float(rng.uniform(0.08, 0.18)),
+                         root_chord=1.0, span=span, taper=taper, sweep_deg=float(rng.uniform(0, 35)), n_chord=nc,
+                         n_span=ns, wake_len=30.0, wake_dir=(1.0, 0.0, 0.0), seed=int(rng.integers(1 << 30)))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    return nodes, tris, ids, dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0.0, 0.0))
+
+
+def batched_and_served():
+    """Config 3 (64 uneven wings x 8 alphas submitted together) and a bounded sample of
+    config 5 (Poisson arrivals, 50 req/s, steady wings of 1k-40k triangles) through the
+    request loop (include/cpanel_serve.h), mixed precision, 8 and 4 slots."""
+    from cpanel_gb300 import serve, wing
+    out = {}
+    # ---- config 3
+    wings = []
+    for i in range(64):
+        spec = wing.config_random(20261203 + i)
+        nodes, tris, ids, info = wing.make_wing(spec)
+        rng = np.random.default_rng(20261203 + i)
+        flows = [(1.0, float(a), 0.0, MACH) for a in rng.uniform(-2, 10, 8)]
+        wings.append((nodes, tris, ids, flows, dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0, 0)),
+                      int(np.count_nonzero(ids <= 1000))))
+    srv = serve.Server(slots=8, budget_gb=160.0, precision="mixed")
+    srv.wait(srv.submit(*wings[0][:4], **wings[0][4]))  # warm-up: kernels, cuBLAS plans, workspaces
+    t0 = time.perf_counter()
+    tickets = [srv.submit(n_, t_, i_, f_, **r_) for n_, t_, i_, f_, r_, _ in wings]
+    res = [srv.wait(t) for t in tickets]
+    wall = time.perf_counter() - t0
+    srv.close()
+    nsol = sum(len(w[3]) for w in wings)
+    out["batched_uneven"] = {
+        "workload": "64 seeded NACA wings (config_random, seeds 20261203+i), %d-%d body panels, 8 alphas each"
+                    % (min(w[5] for w in wings), max(w[5] for w in wings)),
+        "solves": nsol, "wall_s": wall, "solves_per_s": nsol / wall,
+        "p50_ms": float(np.percentile([r["info"]["total_ms"] for r in res], 50)),
+        "max_concurrent": max(r["info"]["running_at_start"] for r in res), "slots": 8,
+        "how": "all submitted at once to the request loop; each request is assembly + LU + 8 refined solves + post"}
+    # ---- config 5 (bounded sample)
+    rng = np.random.default_rng(7)
+    nreq = 32
+    gaps = rng.exponential(1.0 / 50.0, nreq)
+    reqs = []
+    for q in range(nreq):
+        nodes, tris, ids, refs = _wing_with(float(rng.uniform(1000, 40000)), rng)
+        flows = [(1.0, float(a), 0.0, MACH) for a in rng.uniform(-2, 10, 4)]
+        reqs.append((nodes, tris, ids, flows, refs))
+    srv = serve.Server(slots=4, budget_gb=160.0, precision="mixed")
+    srv.wait(srv.submit(*reqs[0][:4], **reqs[0][4]))
+    tickets = []
+    t0 = time.perf_counter()
+    for q in range(nreq):
+        time.sleep(gaps[q])
+        tickets.append(srv.submit(*reqs[q][:4], **reqs[q][4]))
+    res = [srv.wait(t) for t in tickets]
+    wall = time.perf_counter() - t0
+    srv.close()
+    lat = [r["info"]["total_ms"] for r in res]
+    nsol = sum(len(r[3]) for r in reqs)
+    out["serving"] = {
+        "workload": "%d steady requests, Poisson arrivals at 50 req/s (seed 7), NACA wings of %d-%d body panels, "
+                    "4 alphas each; unsteady requests not included" % (nreq, min(r["info"]["n_body"] for r in res),
+                                                                     max(r["info"]["n_body"] for r in res)),
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "solves_per_s": nsol / wall, "wall_s": wall, "slots": 4,
+        "max_concurrent": max(r["info"]["running_at_start"] for r in res),
+        "latency": "submit -> results on the host (includes topology, uploads, assembly, LU, solves, post)"}
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -192,6 +268,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--workload", default="multi_rhs", choices=["multi_rhs", "mid"])
+    ap.add_argument("--no-serving", action="store_true", help="skip the batched (config 3) and served (config 5) runs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -333,6 +410,10 @@ def main():
     roof = roofs.get(dom[0])
     breakdown = {name: {"launches": int(l), "ms": round(ms, 3)} for name, (l, ms) in prof.items() if l}
 
+    extra = {}
+    if rank == 0 and world == 1 and not args.no_serving:
+        extra = batched_and_served()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         v, sample = cpu_cost_model(nodes, tris, ids, refs, os.cpu_count() or 1)
@@ -356,6 +437,7 @@ def main():
                 "solver": {"iters_max": stats["iters_max"], "refinements": stats["refinements"],
                            "residual_max": stats["residual_max"], "near_pairs": stats["n_near"]},
                 "cpu_baseline": cpu, "clocks": clk.summary(), "wall_s": wall}
+        line.update(extra)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

@@ -66,7 +66,10 @@ struct DevBuf {
 
 constexpr double kPi = 3.14159265358979323846;
 // Relative residual at which the mixed path's refinement stops (per right-hand side).
-constexpr double kMixedRefineTol = 1e-10;
+// 1e-10 (two passes) measured Cp errors of 4.9e-6 against the plain path on the 19k
+// wing: CHTLS weights of order 1/h amplify the remaining doublet error.  Three passes
+// (1e-12) give 3.6e-9.
+constexpr double kMixedRefineTol = 1e-12;
 constexpr int F_STRIDE_HOST = 16;  // double-float far-field record, F_STRIDE in common.cuh
 
 }  // namespace
@@ -412,10 +415,10 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
     } else if (precision == CPG_MIXED) {
         CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
         CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
-        CK(g->rb.ensure(sizeof(double) * 3 * n), "alloc rhs basis");
+        CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n))), "alloc rhs basis");
         CK(cpg::launch_assemble_mixed(g->rec.as<double>(), g->frec.as<float>(), n, g->wrec.as<double>(),
                                       g->widx.as<int32_t>(), g->wcoef.as<double>(), g->H.n_wake,
-                                      g->A32.as<float>(), g->Alo.as<float>(), g->rb.as<double>(),
+                                      g->A32.as<float>(), g->Alo.as<float>(), g->rb.as<double>(), g->rb.as<double>() + 3 * n,
                                       g->count.as<unsigned long long>(), s),
            "assembly (mixed)");
         g->have32 = true;

@@ -61,10 +61,12 @@ __global__ void __launch_bounds__(TI) k_assemble_fp64(const double* __restrict__
 // carries about 44 bits; the Krylov iterations read hi only, the refinement
 // residual reads both.  Instead of storing B, the source right-hand-side basis
 // rb[c*n+i] = sum_j B(i,j) * n_j[c] is accumulated (double-float per tile, FP64
-// across tiles and for near pairs).
+// across tiles and for near pairs).  Each column chunk writes its own partial sums
+// (rbp[(chunk*3 + c)*n + i]); k_rb_reduce adds the chunks in order, so the result does
+// not depend on block scheduling.
 __global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict__ rec, const float* __restrict__ frec,
                                                        int64_t n, int64_t jchunk, float* __restrict__ A32,
-                                                       float* __restrict__ Alo, double* __restrict__ rb,
+                                                       float* __restrict__ Alo, double* __restrict__ rbp,
                                                        unsigned long long* __restrict__ near_count) {
     __shared__ double s_rec[TJ * R_STRIDE];
     __shared__ float s_f[TJ * F_STRIDE];
@@ -138,9 +140,10 @@ __global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict_
         for (int c = 0; c < 3; c++) acc64[c] += df_to_double(acc[c]);
     }
     if (act) {
-        atomicAdd(rb + i, acc64[0]);
-        atomicAdd(rb + n + i, acc64[1]);
-        atomicAdd(rb + 2 * n + i, acc64[2]);
+        double* part = rbp + (int64_t)blockIdx.y * 3 * n;
+        part[i] = acc64[0];
+        part[n + i] = acc64[1];
+        part[2 * n + i] = acc64[2];
     }
     if (near_count) {
         for (int o = 16; o > 0; o >>= 1) nnear += __shfl_down_sync(0xffffffffu, nnear, o);
@@ -190,6 +193,14 @@ __global__ void k_wake_columns_split(const double* __restrict__ rec, const doubl
             Alo[o] = (float)(v - (double)hi);
         }
     }
+}
+
+__global__ void k_rb_reduce(const double* __restrict__ rbp, int64_t n, int64_t chunks, double* __restrict__ rb) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * n) return;
+    double acc = 0;
+    for (int64_t y = 0; y < chunks; y++) acc += rbp[y * 3 * n + t];
+    rb[t] = acc;
 }
 
 // panel::setGeom + getLocalSys on the device for free triangles (batched API).
@@ -364,20 +375,24 @@ cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wre
 
 cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
                                   const int32_t* widx, const double* wcoef, int64_t nw, float* A32, float* Alo,
-                                  double* rb, unsigned long long* near_count, cudaStream_t s) {
-    cudaError_t e = cudaMemsetAsync(rb, 0, sizeof(double) * 3 * n, s);
-    if (e != cudaSuccess) return e;
+                                  double* rb, double* rb_part, unsigned long long* near_count, cudaStream_t s) {
     int64_t ch = chunk_for(n);
     dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
     {
         ProfScope ps(Prof::ASSEMBLE, s);
-        k_assemble_mixed<<<grid, TI, 0, s>>>(rec, frec, n, ch, A32, Alo, rb, near_count);
+        k_assemble_mixed<<<grid, TI, 0, s>>>(rec, frec, n, ch, A32, Alo, rb_part, near_count);
+        k_rb_reduce<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(rb_part, n, (int64_t)grid.y, rb);
     }
     if (nw > 0) {
         ProfScope ps(Prof::WAKE_COLUMNS, s);
         k_wake_columns_split<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A32, Alo);
     }
     return cudaGetLastError();
+}
+
+int64_t mixed_rb_part_doubles(int64_t n) {
+    int64_t ch = chunk_for(n);
+    return ((n + ch - 1) / ch) * 3 * n;
 }
 
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,

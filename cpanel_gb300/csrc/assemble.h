@@ -45,7 +45,9 @@ cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wre
                                  unsigned long long* near_count, cudaStream_t s);
 cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
                                   const int32_t* widx, const double* wcoef, int64_t nw, float* A32, float* Alo,
-                                  double* rb, unsigned long long* near_count, cudaStream_t s);
+                                  double* rb, double* rb_part, unsigned long long* near_count, cudaStream_t s);
+// doubles of the per-chunk partial sums that launch_assemble_mixed needs in rb_part
+int64_t mixed_rb_part_doubles(int64_t n);
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,
                              cudaStream_t s);
 cudaError_t launch_v_batch(const double* verts, const double* poi, int64_t m, double* vs, double* vd, cudaStream_t s);
@@ -87,7 +89,7 @@ struct LuGraphs {
     void* workspace = nullptr;  // cuBLAS workspace (no allocation inside a capture)
     float* dinv = nullptr;      // inverses of the diagonal blocks (L then U per block)
     float* panel = nullptr;     // n x 128 staging for the panel GEMMs
-    float* tmp = nullptr;       // 128 x k staging for the substitutions
+    float* tmp = nullptr;       // n x k intermediate of the substitutions
     size_t tmp_floats = 0;
     void release();
 };

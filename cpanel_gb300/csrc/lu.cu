@@ -218,34 +218,35 @@ cudaError_t factor_body(cublasHandle_t h, float* LU, float* Dinv, float* W, int6
     return cudaGetLastError();
 }
 
-// Blocked forward and backward substitution with the diagonal-block inverses:
-// per block, T = inv(D_KK) x_K (small GEMM), x_K <- T, then the rows block K feeds
-// are updated by one GEMM.
-cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int64_t n, float* X, float* T, int k,
-                       cudaStream_t s) {
+// Blocked forward and backward substitution with the diagonal-block inverses, two
+// GEMMs per block and direction and no copies: forward, Y_K = inv(L_KK) X_K and
+// X_below -= L_below,K Y_K; backward, X_K = inv(U_KK) Y_K and Y_above -= U_above,K X_K.
+// X (n x k, ld n) ends with the solution; Y is an n x k scratch array.
+cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int64_t n, float* X, float* Y, int k) {
     const float one = 1.f, mone = -1.f, zero = 0.f;
     const int64_t nblk = (n + NB - 1) / NB;
-    for (int64_t q = 0; q < 2 * nblk; q++) {
-        bool fwd = q < nblk;
-        int64_t blk = fwd ? q : 2 * nblk - 1 - q;
+    for (int64_t blk = 0; blk < nblk; blk++) {
         int64_t K = blk * NB;
         int b = (int)std::min<int64_t>(NB, n - K);
-        const float* Di = Dinv + blk * 2 * NB * NB + (fwd ? 0 : NB * NB);
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, k, b, &one, Di, NB, X + K, (int)n, &zero, T, b) !=
+        const float* Li = Dinv + blk * 2 * NB * NB;
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, k, b, &one, Li, NB, X + K, (int)n, &zero, Y + K, (int)n) !=
             CUBLAS_STATUS_SUCCESS)
             return cudaErrorUnknown;
-        cudaError_t e = cudaMemcpy2DAsync(X + K, n * sizeof(float), T, b * sizeof(float), b * sizeof(float), k,
-                                          cudaMemcpyDeviceToDevice, s);
-        if (e != cudaSuccess) return e;
-        if (fwd) {
-            int64_t rest = n - K - b;
-            if (rest > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, b, &mone, LU + K * n + K + b,
-                                        (int)n, T, b, &one, X + K + b, (int)n) != CUBLAS_STATUS_SUCCESS)
-                return cudaErrorUnknown;
-        } else if (K > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, b, &mone, LU + K * n, (int)n, T, b,
-                                        &one, X, (int)n) != CUBLAS_STATUS_SUCCESS) {
+        int64_t rest = n - K - b;
+        if (rest > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, b, &mone, LU + K * n + K + b, (int)n,
+                                    Y + K, (int)n, &one, X + K + b, (int)n) != CUBLAS_STATUS_SUCCESS)
             return cudaErrorUnknown;
-        }
+    }
+    for (int64_t blk = nblk - 1; blk >= 0; blk--) {
+        int64_t K = blk * NB;
+        int b = (int)std::min<int64_t>(NB, n - K);
+        const float* Ui = Dinv + blk * 2 * NB * NB + NB * NB;
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, k, b, &one, Ui, NB, Y + K, (int)n, &zero, X + K, (int)n) !=
+            CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        if (K > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, b, &mone, LU + K * n, (int)n, X + K, (int)n,
+                                 &one, Y, (int)n) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
     }
     return cudaGetLastError();
 }
@@ -325,13 +326,13 @@ cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, f
     if (!G->solve || G->solve_X != X || G->solve_k != k || G->solve_LU != LU) {
         if (G->solve) cudaGraphExecDestroy(G->solve);
         G->solve = nullptr;
-        if (G->tmp_floats < (size_t)NB * k) {
+        if (G->tmp_floats < (size_t)n * k) {
             if (G->tmp) cudaFree(G->tmp);
             G->tmp = nullptr;
-            if ((e = cudaMalloc(&G->tmp, sizeof(float) * NB * k)) != cudaSuccess) return e;
-            G->tmp_floats = (size_t)NB * k;
+            if ((e = cudaMalloc(&G->tmp, sizeof(float) * n * k)) != cudaSuccess) return e;
+            G->tmp_floats = (size_t)n * k;
         }
-        e = capture(s, &G->solve, [&] { return solve_body(h, LU, G->dinv, n, X, G->tmp, k, s); });
+        e = capture(s, &G->solve, [&] { return solve_body(h, LU, G->dinv, n, X, G->tmp, k); });
         if (e != cudaSuccess) return e;
         G->solve_X = X;
         G->solve_k = k;

@@ -77,12 +77,27 @@ __global__ void k_mv_reduce(const TACC* __restrict__ P, int nchunk, int KB, int 
 }
 
 // Double-float residual chunks: exact FP32 products of A32 with x = xh + xl.
+// x is staged as (hi, lo) pairs (one 8-byte shared load per product); the matrix
+// columns are read four at a time before any arithmetic so that four loads per
+// thread are in flight.
+__device__ __forceinline__ void df_acc(float a, float al, float2 x, float& hi, float& lo) {
+    float p = __fmul_rn(a, x.x);
+    float e = __fmaf_rn(a, x.x, -p);  // exact product error
+    e = __fmaf_rn(a, x.y, e);
+    e = __fmaf_rn(al, x.x, e);
+    float s = __fadd_rn(hi, p);  // TwoSum(hi, p)
+    float bb = __fsub_rn(s, hi);
+    float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+    hi = s;
+    lo = __fadd_rn(lo, __fadd_rn(err, e));
+}
+
 template <int KB>
 __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict__ A, const float* __restrict__ Alo,
                                                          int64_t n, int64_t jchunk,
                                                          const double* __restrict__ X, int col0, int kb,
                                                          double* __restrict__ P) {
-    __shared__ float sh[MV_JT][KB], sl[MV_JT][KB];
+    __shared__ float2 sx[MV_JT][KB];
     int64_t i = (int64_t)blockIdx.x * MV_THREADS + threadIdx.x;
     int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
     double acc[KB];
@@ -95,8 +110,7 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
             int64_t j = j0 + jj;
             double xv = (j < je && c < kb) ? X[(int64_t)(col0 + c) * n + j] : 0.0;
             float h = (float)xv;
-            sh[jj][c] = h;
-            sl[jj][c] = (float)(xv - (double)h);
+            sx[jj][c] = make_float2(h, (float)(xv - (double)h));
         }
         __syncthreads();
         if (i < n) {
@@ -106,21 +120,23 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
             float hi[KB], lo[KB];
 #pragma unroll
             for (int c = 0; c < KB; c++) hi[c] = lo[c] = 0.f;
-            for (int t = 0; t < cnt; t++) {
-                float a = Ap[(int64_t)t * n];
-                float al = Lp[(int64_t)t * n];
+            int t = 0;
+            for (; t + 3 < cnt; t += 4) {
+                float a[4], al[4];
 #pragma unroll
-                for (int c = 0; c < KB; c++) {
-                    float p = __fmul_rn(a, sh[t][c]);
-                    float e = __fmaf_rn(a, sh[t][c], -p);     // exact product error
-                    e = __fmaf_rn(a, sl[t][c], e);
-                    e = __fmaf_rn(al, sh[t][c], e);
-                    float s = __fadd_rn(hi[c], p);           // TwoSum(hi, p)
-                    float bb = __fsub_rn(s, hi[c]);
-                    float err = __fadd_rn(__fsub_rn(hi[c], __fsub_rn(s, bb)), __fsub_rn(p, bb));
-                    hi[c] = s;
-                    lo[c] = __fadd_rn(lo[c], __fadd_rn(err, e));
+                for (int u = 0; u < 4; u++) {
+                    a[u] = __ldg(Ap + (int64_t)(t + u) * n);
+                    al[u] = __ldg(Lp + (int64_t)(t + u) * n);
                 }
+#pragma unroll
+                for (int u = 0; u < 4; u++)
+#pragma unroll
+                    for (int c = 0; c < KB; c++) df_acc(a[u], al[u], sx[t + u][c], hi[c], lo[c]);
+            }
+            for (; t < cnt; t++) {
+                float a = __ldg(Ap + (int64_t)t * n), al = __ldg(Lp + (int64_t)t * n);
+#pragma unroll
+                for (int c = 0; c < KB; c++) df_acc(a, al, sx[t][c], hi[c], lo[c]);
             }
 #pragma unroll
             for (int c = 0; c < KB; c++) acc[c] += (double)hi[c] + (double)lo[c];

@@ -9,7 +9,7 @@ import ctypes as C
 
 import numpy as np
 
-from . import _lib
+from . import _lib, _shutting_down_now
 from ._lib import MIXED, PLAIN_FP64, CpgError
 
 _PREC = {"mixed": MIXED, "fp64": PLAIN_FP64, "plain": PLAIN_FP64, MIXED: MIXED, PLAIN_FP64: PLAIN_FP64}
@@ -37,7 +37,6 @@ class Server:
             self.h = None
 
     def __del__(self):
-        from . import _shutting_down_now
         if not _shutting_down_now():
             self.close()
 

@@ -40,7 +40,7 @@ typedef enum {
     CPG_PLAIN_FP64 = 0,  /* the reference method in FP64: explicit A, B; BiCGSTAB to eps */
     CPG_MIXED = 1        /* double-float far field + FP64 near field, matrix kept as an
                             FP32 hi + lo pair; FP32 LU + refinement with an exact-
-                            product residual to relative residual 1e-10              */
+                            product residual to relative residual 1e-12              */
 } cpg_precision;
 
 typedef struct cpg_ctx cpg_ctx;

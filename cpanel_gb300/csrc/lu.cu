@@ -24,33 +24,41 @@ constexpr int NB = 128;   // panel width
 constexpr int P = NB + 1; // padded smem pitch (no bank conflicts on row access)
 
 constexpr int DT = 512;    // threads of the diagonal-block kernel
-constexpr int DIAG_SMEM = 3 * NB * P * 4;
+constexpr int BS = 32;     // inner block of the diagonal kernel
+constexpr int TP = BS + 1; // pitch of its 32 x 32 scratch
+constexpr int DIAG_SMEM = (3 * NB * P + 6 * BS * TP) * 4;
 
 // In-place LU (unit lower L, upper U) of the b x b block at A + K*n + K, then the
 // inverses of both triangles into Dinv (L11^{-1} then U11^{-1}, column-major, ld NB).
 // A block smaller than NB is padded with the identity, which factors and inverts to
-// itself without touching the real entries.
+// itself without touching the real entries.  Every phase below is a set of
+// independent items spread over the 512 threads; barriers separate the phases.
 //
-// Elimination: thread t owns row r = t % 128 and the columns c = t / 128 (mod 4), so
-// each of the 128 steps spreads its rank-1 update over 512 threads behind one
-// barrier.  Step j reads column j and row j and writes only rows and columns past j;
-// the multiplier l(r, j) is stored one step later, when nothing reads column j.
-// Inversion: threads 0-255 invert L and 256-511 invert U at the same time, two lanes
-// per column.  Lane `sub` sums the terms of rows with parity `sub` and is the one that
-// stores those rows of the inverse, so it only ever reads entries it wrote itself;
-// one shuffle joins the two partial sums.
+// LU: 128 right-looking steps, thread t owning row t % 128 and every fourth column;
+// step j reads column j and row j and writes only past them, and the multiplier of
+// column j is stored one step later, when nothing reads column j.
+// Inverses: the eight 32 x 32 diagonal blocks first (right-looking; U as the unit
+// upper factor of U scaled by its diagonal, then the columns divided by it), then the
+// off-diagonal blocks by distance d = 1..3 from the diagonal:
+// Linv[I][J] = -Linv[I][I] sum_{K=J}^{I-1} L[I][K] Linv[K][J] and
+// Uinv[I][J] = -Uinv[I][I] sum_{K=I+1}^{J} U[I][K] Uinv[K][J].
 __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
                                                 float* __restrict__ Dinv, int* bad) {
     extern __shared__ float sm[];
-    float* S = sm;               // S[r*P + c]
-    float* ZL = sm + NB * P;     // ZL[col*P + i] = (L^{-1})(i, col)
-    float* ZU = sm + 2 * NB * P; // ZU[col*P + i] = (U^{-1})(i, col)
+    float* S = sm;                 // S[r*P + c]
+    float* ZL = sm + NB * P;       // L^{-1}, row-major
+    float* ZU = sm + 2 * NB * P;   // U^{-1}, row-major
+    float* Tb = sm + 3 * NB * P;   // 6 scratch blocks, Tb[slot*BS*TP + r*TP + c]
     const int t = threadIdx.x;
     for (int idx = t; idx < NB * NB; idx += DT) {
         int c = idx / NB, r = idx % NB;
         S[r * P + c] = (r < b && c < b) ? A[(K + c) * n + K + r] : (r == c ? 1.f : 0.f);
+        ZL[r * P + c] = r == c ? 1.f : 0.f;
+        ZU[r * P + c] = r == c ? 1.f : 0.f;
     }
     __syncthreads();
+    // ---- LU: thread t owns row t % 128 and the columns c = t / 128 (mod 4); one barrier
+    // per step; the multiplier of column j is stored during step j + 1
     const int r = t % NB, q = t / NB;
     float lprev = 0.f;
     for (int j = 0; j < NB; j++) {
@@ -63,58 +71,109 @@ __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n
         if (r > j) {
             float l = S[r * P + j] / piv;
             int c = j + 1 + ((q - (j + 1)) & 3);
-            for (; c + 4 < NB; c += 8) {
-                float u0 = S[j * P + c], u1 = S[j * P + c + 4];
-                S[r * P + c] = __fmaf_rn(-l, u0, S[r * P + c]);
-                S[r * P + c + 4] = __fmaf_rn(-l, u1, S[r * P + c + 4]);
+            // eight columns per batch: all loads first, so that the shared-memory
+            // latencies overlap instead of chaining through the stores
+            for (; c + 28 < NB; c += 32) {
+                float u[8], v[8];
+#pragma unroll
+                for (int m = 0; m < 8; m++) {
+                    u[m] = S[j * P + c + 4 * m];
+                    v[m] = S[r * P + c + 4 * m];
+                }
+#pragma unroll
+                for (int m = 0; m < 8; m++) S[r * P + c + 4 * m] = __fmaf_rn(-l, u[m], v[m]);
             }
-            if (c < NB) S[r * P + c] = __fmaf_rn(-l, S[j * P + c], S[r * P + c]);
+            for (; c < NB; c += 4) S[r * P + c] = __fmaf_rn(-l, S[j * P + c], S[r * P + c]);
             lprev = l;
         }
         __syncthreads();
     }
-    // (the multiplier of the last step belongs to no row: r > NB - 1 never holds)
-    const int half = t / 256, u = t % 256, col = u / 2, sub = u % 2;
-    if (half == 0) {  // L z = e_col, unit lower: rows col..NB-1
-        float* Z = ZL + col * P;
-        for (int i = 0; i < NB; i++) {
-            float s0 = 0.f, s1 = 0.f;
-            if (i > col) {
-                int jj = col + ((sub - col) & 1);  // lane sub owns the rows of its parity
-                for (; jj + 2 < i; jj += 4) {
-                    s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
-                    s1 = __fmaf_rn(-S[i * P + jj + 2], Z[jj + 2], s1);
-                }
-                if (jj < i) s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
+    // ---- inverses of the 32 x 32 diagonal blocks (L: k ascending; U: unit-scaled, k descending)
+    for (int st = 0; st < BS; st++) {
+        const int kL = st, kU = BS - 1 - st;
+        const int eL = (BS - 1 - kL) * (kL + 1), eU = kU * (BS - kU);
+        for (int w = t; w < 4 * (eL + eU); w += DT) {
+            if (w < 4 * eL) {
+                const int o = BS * (w / eL), ww = w % eL;
+                const int i = kL + 1 + ww / (kL + 1), c = ww % (kL + 1);
+                ZL[(o + i) * P + o + c] =
+                    __fmaf_rn(-S[(o + i) * P + o + kL], ZL[(o + kL) * P + o + c], ZL[(o + i) * P + o + c]);
+            } else {
+                const int w2 = w - 4 * eL;
+                const int o = BS * (w2 / eU), ww = w2 % eU;
+                const int i = ww / (BS - kU), c = kU + ww % (BS - kU);
+                ZU[(o + i) * P + o + c] = __fmaf_rn(-(S[(o + i) * P + o + kU] / S[(o + i) * P + o + i]),
+                                                    ZU[(o + kU) * P + o + c], ZU[(o + i) * P + o + c]);
             }
-            float v = s0 + s1;
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            if (sub == (i & 1)) Z[i] = i < col ? 0.f : (i == col ? 1.f : v);
         }
-    } else {  // U z = e_col: rows col..0
-        float* Z = ZU + col * P;
-        for (int i = NB - 1; i >= 0; i--) {
-            float s0 = 0.f, s1 = 0.f;
-            if (i < col) {
-                int jj = i + 1 + ((sub - (i + 1)) & 1);
-                for (; jj + 2 <= col; jj += 4) {
-                    s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
-                    s1 = __fmaf_rn(-S[i * P + jj + 2], Z[jj + 2], s1);
-                }
-                if (jj <= col) s0 = __fmaf_rn(-S[i * P + jj], Z[jj], s0);
-            }
-            float v = s0 + s1;
-            v += __shfl_xor_sync(0xffffffffu, v, 1);
-            if (sub == (i & 1)) Z[i] = i > col ? 0.f : ((i == col ? 1.f : v) / S[i * P + i]);
-        }
+        __syncthreads();
+    }
+    for (int w = t; w < 4 * BS * BS; w += DT) {  // U: divide the columns by the diagonal
+        const int o = BS * (w / (BS * BS)), i = (w % (BS * BS)) / BS, c = w % BS;
+        if (c >= i) ZU[(o + i) * P + o + c] = ZU[(o + i) * P + o + c] / S[(o + c) * P + o + c];
     }
     __syncthreads();
+    // ---- off-diagonal blocks, by distance from the diagonal
+    for (int d = 1; d < NB / BS; d++) {
+        const int nL = NB / BS - d;
+        for (int w = t; w < 2 * nL * 64; w += DT) {
+            const bool isU = w >= nL * 64;
+            const int ww = w % (nL * 64), q = ww / 64, tile = ww % 64, tr = tile / 8, tc = tile % 8;
+            const int I = isU ? q : d + q, J = isU ? q + d : q;
+            const int kb = isU ? I + 1 : J, ke = isU ? J + 1 : I;
+            const float* Z = isU ? ZU : ZL;
+            float acc[4][4] = {};
+            for (int Kb = kb; Kb < ke; Kb++)
+                for (int k = 0; k < BS; k++) {
+                    const int kk = BS * Kb + k;
+                    float a[4], bb[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) a[i] = S[(BS * I + 4 * tr + i) * P + kk];
+#pragma unroll
+                    for (int x = 0; x < 4; x++) bb[x] = Z[kk * P + BS * J + 4 * tc + x];
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int x = 0; x < 4; x++) acc[i][x] = __fmaf_rn(a[i], bb[x], acc[i][x]);
+                }
+            float* Tq = Tb + (isU ? 3 + q : q) * BS * TP;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 4; x++) Tq[(4 * tr + i) * TP + 4 * tc + x] = acc[i][x];
+        }
+        __syncthreads();
+        for (int w = t; w < 2 * nL * 64; w += DT) {
+            const bool isU = w >= nL * 64;
+            const int ww = w % (nL * 64), q = ww / 64, tile = ww % 64, tr = tile / 8, tc = tile % 8;
+            const int I = isU ? q : d + q, J = isU ? q + d : q;
+            float* Z = isU ? ZU : ZL;
+            const float* Tq = Tb + (isU ? 3 + q : q) * BS * TP;
+            float acc[4][4] = {};
+            for (int k = 0; k < BS; k++) {
+                float a[4], bb[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) a[i] = Z[(BS * I + 4 * tr + i) * P + BS * I + k];
+#pragma unroll
+                for (int x = 0; x < 4; x++) bb[x] = Tq[k * TP + 4 * tc + x];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int x = 0; x < 4; x++) acc[i][x] = __fmaf_rn(a[i], bb[x], acc[i][x]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 4; x++) Z[(BS * I + 4 * tr + i) * P + BS * J + 4 * tc + x] = -acc[i][x];
+        }
+        __syncthreads();
+    }
     float* Li = Dinv + (K / NB) * 2 * NB * NB;
     float* Ui = Li + NB * NB;
     for (int idx = t; idx < NB * NB; idx += DT) {
         int c = idx / NB, rr = idx % NB;
-        Li[idx] = ZL[c * P + rr];
-        Ui[idx] = ZU[c * P + rr];
+        Li[idx] = ZL[rr * P + c];
+        Ui[idx] = ZU[rr * P + c];
         if (rr < b && c < b) A[(K + c) * n + K + rr] = S[rr * P + c];
     }
 }

@@ -237,6 +237,65 @@ def batched_and_served():
     return out
 
 
+def vortex_particles(steps=20):
+    """Config 4 (bounded sample): NACA 4412 AR 6 wing of 8,216 body triangles without wake
+    panels, alpha 8 deg, dt 0.05, Barnes-Hut on: the first `steps` steps of the VP loop, then
+    the particle operators on 40,000 particles spread behind the wing."""
+    import torch
+
+    from cpanel_gb300 import vp, wing
+    spec = wing.WingSpec(m=0.04, p=0.4, t=0.12, root_chord=1.0, span=6 * (1 + 0.6) / 2, taper=0.6, sweep_deg=0.0,
+                         n_chord=80, n_span=26, wake_len=30.0, wake_dir=(1.0, 0.0, 0.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    tris, ids = tris[keep], ids[keep]
+    S = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, dt=0.05, accelerate=True)
+    S.step(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    S.step(steps)
+    torch.cuda.synchronize()
+    t_loop = time.perf_counter() - t0
+    inf = S.info()
+    # operators at 40k particles
+    rng = np.random.default_rng(4)
+    n = 40000
+    pos = np.c_[rng.uniform(1.0, 15.0, n), rng.uniform(-2.4, 2.4, n), rng.normal(0, 0.3, n)]
+    P = torch.tensor(pos, device="cuda")
+    A = torch.tensor(rng.normal(size=(n, 3)) * 0.01, device="cuda")
+    R = torch.full((n,), 0.05, dtype=torch.float64, device="cuda")
+    verts = np.asarray(nodes)[np.asarray(tris) - 1].reshape(-1, 9)
+    BV = torch.tensor(verts, device="cuda")
+    SG = torch.tensor(rng.normal(size=len(verts)), device="cuda")
+    MU = torch.tensor(rng.normal(size=len(verts)), device="cuda")
+
+    def timed(f, reps=2):
+        f()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(reps):
+            f()
+        torch.cuda.synchronize()
+        return (time.perf_counter() - t) / reps * 1e3
+
+    t_tree = timed(lambda: vp.ParticleFMM(P, A, R))
+    tree = vp.ParticleFMM(P, A, R)
+    t_bh = timed(lambda: tree.barnesHut(True, True, True))
+    t_pv = timed(lambda: vp.panels_velocity(BV, SG, MU, None, None, P), 1)
+    t_ps = timed(lambda: vp.panels_stretching(BV, SG, MU, None, None, P, A), 1)
+    pairs = float(n) * len(verts)
+    return {"vp_unsteady": {
+        "workload": "NACA 4412 AR 6 taper 0.6, %d body triangles, no wake panels, alpha 8 deg, dt 0.05, "
+                    "Barnes-Hut theta 0.5 (FP64)" % len(verts),
+        "loop": {"steps": steps, "ms_per_step": t_loop / steps * 1e3, "particles_at_end": inf["n_particles"],
+                 "first_step": 4, "what": "cpg_vpcase_step: convection, shedding, strength update, octree, "
+                                          "source strengths, FP64 BiCGSTAB solve"},
+        "operators_40k_particles": {
+            "tree_build_ms": t_tree, "barnes_hut_vel_stretch_diff_ms": t_bh,
+            "panel_velocity_ms": t_pv, "panel_velocity_pairs_per_s": pairs / (t_pv * 1e-3),
+            "panel_stretching_ms": t_ps, "panel_stretching_pairs_per_s": pairs / (t_ps * 1e-3)}}}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -269,6 +328,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--workload", default="multi_rhs", choices=["multi_rhs", "mid"])
     ap.add_argument("--no-serving", action="store_true", help="skip the batched (config 3) and served (config 5) runs")
+    ap.add_argument("--no-vp", action="store_true", help="skip the vortex-particle sample (config 4)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -413,6 +473,8 @@ def main():
     extra = {}
     if rank == 0 and world == 1 and not args.no_serving:
         extra = batched_and_served()
+    if rank == 0 and world == 1 and not args.no_vp:
+        extra.update(vortex_particles())
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -118,8 +118,8 @@ struct cpg_vpcase {
     cpg::ParticleTree T;
     bool tree_built = false;
     Buf tnodes, tperm, tslots;
-    // device: shedding evaluation points
-    Buf spts, sout;
+    // device: shedding evaluation points; scratch of the chunked panel kernels
+    Buf spts, sout, scr;
     std::vector<double> filh;  // host copy of the filaments (8 per w2 panel)
     bool have_fil = false;
 };
@@ -208,10 +208,11 @@ cudaError_t field_at(cpg_vpcase& S, bool bh, const std::vector<double>& pts, int
     double* P = S.sout.as<double>();
     double* Q = P + 3 * m;
     if ((e = particle_term_points(S, bh, S.spts.as<double>(), m, nsrc, P)) != cudaSuccess) return e;
+    if ((e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s)) != cudaSuccess) return e;
     if ((e = cpg::vp_launch_panel_vel(S.rec.as<double>(), S.sigma.as<double>(), S.mu.as<double>(), S.n,
                                       S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.q2.as<double>(),
                                       S.mu2.as<double>(), S.n2, S.fil.as<double>(), S.have_fil ? S.n2 : 0,
-                                      S.spts.as<double>(), m, 0.0, Q, S.s)) != cudaSuccess)
+                                      S.spts.as<double>(), m, 0.0, Q, S.scr.as<double>(), S.s)) != cudaSuccess)
         return e;
     std::vector<double> h(6 * m);
     if ((e = cudaMemcpyAsync(h.data(), P, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
@@ -430,10 +431,12 @@ cudaError_t step_once(cpg_vpcase& S) {
                                         nullptr, m, c, S.tP.as<double>(), nullptr, nullptr, S.s)) != cudaSuccess)
                 return e;
         }
+        if ((e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s)) != cudaSuccess) return e;
         if ((e = cpg::vp_launch_panel_vel(S.rec.as<double>(), S.sigma.as<double>(), S.mu.as<double>(), S.n,
                                           S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.q2.as<double>(),
                                           S.mu2.as<double>(), S.n2, S.fil.as<double>(), S.have_fil ? S.n2 : 0,
-                                          S.pos.as<double>(), m, 12 * S.cref, S.tQ.as<double>(), S.s)) != cudaSuccess)
+                                          S.pos.as<double>(), m, 12 * S.cref, S.tQ.as<double>(), S.scr.as<double>(),
+                                          S.s)) != cudaSuccess)
             return e;
         if ((e = cpg::vp_launch_convect(S.pos.as<double>(), S.pvel.as<double>(), S.tP.as<double>(), S.tQ.as<double>(), m,
                                         vinf, S.cref, S.dt, S.s)) != cudaSuccess)
@@ -465,10 +468,11 @@ cudaError_t step_once(cpg_vpcase& S) {
                                         m, c, nullptr, S.tS.as<double>(), S.tD.as<double>(), S.s)) != cudaSuccess)
                 return e;
         }
+        if ((e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s)) != cudaSuccess) return e;
         if ((e = cpg::vp_launch_stretch_panels(S.rec.as<double>(), S.sigma.as<double>(), S.mu.as<double>(), S.n,
                                                S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.pos.as<double>(),
-                                               S.str.as<double>(), m, 12 * S.cref, S.tPan.as<double>(), S.s)) !=
-            cudaSuccess)
+                                               S.str.as<double>(), m, 12 * S.cref, S.tPan.as<double>(),
+                                               S.scr.as<double>(), S.s)) != cudaSuccess)
             return e;
         if ((e = cpg::vp_launch_strength(S.pos.as<double>(), S.str.as<double>(), S.pstr.as<double>(), S.tS.as<double>(),
                                          S.tD.as<double>(), S.tPan.as<double>(), m, S.cref, S.dt, S.s)) != cudaSuccess)
@@ -587,7 +591,7 @@ void cpg_vpcase_destroy(cpg_vpcase* S) {
     Buf* all[] = {&S->rec, &S->q1, &S->q2, &S->widx, &S->wcoef, &S->par, &S->A, &S->B, &S->C, &S->work,
                   &S->sigma, &S->mu, &S->mu1, &S->prev1, &S->mu2, &S->prev2, &S->rhs, &S->fil, &S->vcent,
                   &S->pos, &S->str, &S->rad, &S->pvel, &S->pstr, &S->packed, &S->tP, &S->tQ, &S->tS, &S->tD,
-                  &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout};
+                  &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr};
     for (Buf* b : all) b->release();
     delete S;
 }
@@ -718,9 +722,10 @@ int cpg_panels_stretching(cpg_ctx* ctx, const double* body_verts, const double* 
     }
     if (m == 0) return CPG_OK;
     cudaStream_t s = cpg::ctx_stream(ctx);
-    Buf rec, q;
+    Buf rec, q, scr;
     std::vector<double> hv(12 * nw), hq(cpg::QF_STRIDE * nw);
     cudaError_t e = rec.ensure(sizeof(double) * 24 * std::max<int64_t>(1, nb), s);
+    if (e == cudaSuccess) e = scr.ensure(sizeof(double) * std::max<int64_t>(1, cpg::vp_scratch_doubles(m, nb)), s);
     if (e == cudaSuccess && nb > 0) e = cpg::launch_pack_records(body_verts, nb, rec.as<double>(), s);
     if (e == cudaSuccess && nw > 0) e = cudaMemcpyAsync(hv.data(), wake_verts, sizeof(double) * 12 * nw,
                                                         cudaMemcpyDeviceToHost, s);
@@ -729,10 +734,11 @@ int cpg_panels_stretching(cpg_ctx* ctx, const double* body_verts, const double* 
     if (e == cudaSuccess) e = up(q, hq, s);
     if (e == cudaSuccess)
         e = cpg::vp_launch_stretch_panels(rec.as<double>(), sigma, mu, nb, q.as<double>(), wake_mu, nw, pos, strength, m,
-                                          0.0, out, s);
+                                          0.0, out, scr.as<double>(), s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     rec.release();
     q.release();
+    scr.release();
     if (e != cudaSuccess) {
         cpg::ctx_set_error(ctx, std::string("panel stretching: ") + cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? CPG_E_OOM : CPG_E_CUDA;

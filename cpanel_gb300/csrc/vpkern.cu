@@ -5,6 +5,8 @@
 // rounds as the host's do.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "common.cuh"
 #include "panel64.cuh"
 #include "vp.cuh"
@@ -45,23 +47,23 @@ __global__ void k_vp_cmat(const double* __restrict__ rec, int64_t n, const doubl
 // second buffer rows (mu dubVInf), filaments (vortexFil::velInfl, CPanel/vortexFil.cpp:26-40).
 // Points with |p| > skip_r (skip_r > 0) get zero: the reference returns before the panel
 // terms there (CPanel/cpCaseVP.cpp:711-715).
-__global__ void __launch_bounds__(VT) k_vp_panel_vel(const double* __restrict__ rec, const double* __restrict__ sigma,
-                                                     const double* __restrict__ mu, int64_t nb,
-                                                     const double* __restrict__ q1, const double* __restrict__ mu1,
-                                                     int64_t n1, const double* __restrict__ q2,
-                                                     const double* __restrict__ mu2, int64_t n2,
-                                                     const double* __restrict__ fil, int64_t nf,
-                                                     const double* __restrict__ pts, int64_t m, double skip_r,
-                                                     double* __restrict__ out) {
+// The body panels are split into chunks along grid.y so that a handful of points still
+// fill the GPU; k_vp_panel_vel_fin adds the chunks in order, then the quads and filaments.
+__global__ void __launch_bounds__(VT) k_vp_panel_vel_part(const double* __restrict__ rec,
+                                                          const double* __restrict__ sigma,
+                                                          const double* __restrict__ mu, int64_t nb,
+                                                          int64_t chunk, const double* __restrict__ pts, int64_t m,
+                                                          double skip_r, double* __restrict__ part) {
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool live = q < m;
     dv3 poi = live ? ld3(pts + 3 * q) : mk3(0, 0, 0);
     if (live && skip_r > 0 && norm3(poi) > skip_r) live = false;
+    const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
     dv3 acc = mk3(0, 0, 0);
-    for (int64_t b = 0; b < nb; b += TILE) {
-        int lim = (int)((nb - b) < TILE ? (nb - b) : TILE);
+    for (int64_t b = jb; b < je; b += TILE) {
+        int lim = (int)((je - b) < TILE ? (je - b) : TILE);
         __syncthreads();
         for (int k = threadIdx.x; k < lim * R_STRIDE; k += VT) tile[k] = rec[b * R_STRIDE + k];
         for (int k = threadIdx.x; k < lim; k += VT) {
@@ -77,10 +79,26 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel(const double* __restrict__ 
         }
     }
     if (q >= m) return;
-    if (!live) {
+    double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
+    o[0] = acc.x;
+    o[1] = acc.y;
+    o[2] = acc.z;
+}
+
+__global__ void k_vp_panel_vel_fin(const double* __restrict__ part, int64_t nchunk, const double* __restrict__ q1,
+                                   const double* __restrict__ mu1, int64_t n1, const double* __restrict__ q2,
+                                   const double* __restrict__ mu2, int64_t n2, const double* __restrict__ fil,
+                                   int64_t nf, const double* __restrict__ pts, int64_t m, double skip_r,
+                                   double* __restrict__ out) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    dv3 poi = ld3(pts + 3 * q);
+    if (skip_r > 0 && norm3(poi) > skip_r) {
         out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = 0;
         return;
     }
+    dv3 acc = mk3(0, 0, 0);
+    for (int64_t c = 0; c < nchunk; c++) acc = acc + ld3(part + (c * m + q) * 3);
     for (int64_t j = 0; j < n1; j++) acc = acc + mu1[j] * dub_v_inf_q(q1 + j * Q_STRIDE, poi);
     for (int64_t j = 0; j < n2; j++) acc = acc + mu2[j] * dub_v_inf_q(q2 + j * Q_STRIDE, poi);
     for (int64_t j = 0; j < nf; j++) {
@@ -95,15 +113,14 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel(const double* __restrict__ 
 
 // sum over body panels of bodyPanel::partStretching and over first-row panels of
 // wakePanel::partStretching (CPanel/bodyPanel.cpp:697-728, CPanel/wakePanel.cpp:266-289).
-// Particles with |x| > skip_x (skip_x > 0) get zero (cpCaseVP.cpp:473-499).
-__global__ void __launch_bounds__(VT) k_vp_stretch_panels(const double* __restrict__ rec,
-                                                          const double* __restrict__ sigma,
-                                                          const double* __restrict__ mu, int64_t nb,
-                                                          const double* __restrict__ q1,
-                                                          const double* __restrict__ mu1, int64_t n1,
-                                                          const double* __restrict__ pos,
-                                                          const double* __restrict__ str, int64_t m, double skip_x,
-                                                          double* __restrict__ out) {
+// Particles with |x| > skip_x (skip_x > 0) get zero (cpCaseVP.cpp:473-499).  Body
+// panels in chunks along grid.y as for the velocity.
+__global__ void __launch_bounds__(VT) k_vp_stretch_part(const double* __restrict__ rec,
+                                                        const double* __restrict__ sigma,
+                                                        const double* __restrict__ mu, int64_t nb, int64_t chunk,
+                                                        const double* __restrict__ pos,
+                                                        const double* __restrict__ str, int64_t m, double skip_x,
+                                                        double* __restrict__ part) {
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -111,9 +128,10 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_panels(const double* __restri
     dv3 x = live ? ld3(pos + 3 * q) : mk3(0, 0, 0);
     dv3 a = live ? ld3(str + 3 * q) : mk3(0, 0, 0);
     if (live && skip_x > 0 && fabs(x.x) > skip_x) live = false;
+    const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
     dv3 acc = mk3(0, 0, 0);
-    for (int64_t b = 0; b < nb; b += TILE) {
-        int lim = (int)((nb - b) < TILE ? (nb - b) : TILE);
+    for (int64_t b = jb; b < je; b += TILE) {
+        int lim = (int)((je - b) < TILE ? (je - b) : TILE);
         __syncthreads();
         for (int k = threadIdx.x; k < lim * R_STRIDE; k += VT) tile[k] = rec[b * R_STRIDE + k];
         for (int k = threadIdx.x; k < lim; k += VT) {
@@ -145,10 +163,24 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_panels(const double* __restri
         }
     }
     if (q >= m) return;
-    if (!live) {
+    double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
+    o[0] = acc.x;
+    o[1] = acc.y;
+    o[2] = acc.z;
+}
+
+__global__ void k_vp_stretch_fin(const double* __restrict__ part, int64_t nchunk, const double* __restrict__ q1,
+                                 const double* __restrict__ mu1, int64_t n1, const double* __restrict__ pos,
+                                 const double* __restrict__ str, int64_t m, double skip_x, double* __restrict__ out) {
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    dv3 x = ld3(pos + 3 * q), a = ld3(str + 3 * q);
+    if (skip_x > 0 && fabs(x.x) > skip_x) {
         out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = 0;
         return;
     }
+    dv3 acc = mk3(0, 0, 0);
+    for (int64_t c = 0; c < nchunk; c++) acc = acc + ld3(part + (c * m + q) * 3);
     for (int64_t j = 0; j < n1; j++) {
         const double* w = q1 + j * Q_STRIDE;
         dv3 c = ld3(w + Q_C);
@@ -272,20 +304,43 @@ cudaError_t vp_launch_cmat(const double* rec, int64_t n, const double* q2, int64
     if (n > 0 && n2 > 0) k_vp_cmat<<<nblk(n * n2, 256), 256, 0, s>>>(rec, n, q2, n2, C);
     return cudaGetLastError();
 }
+// chunks of body panels along grid.y: enough blocks to fill the GPU several times over
+int64_t vp_chunks(int64_t m, int64_t nb) {
+    int64_t bx = (m + VT - 1) / VT;
+    int64_t maxc = (nb + TILE - 1) / TILE;
+    int64_t c = (4 * 152 + bx - 1) / bx;
+    return std::max<int64_t>(1, std::min(c, maxc));
+}
+
+int64_t vp_scratch_doubles(int64_t m, int64_t nb) { return vp_chunks(m, nb) * m * 3; }
+
 cudaError_t vp_launch_panel_vel(const double* rec, const double* sigma, const double* mu, int64_t nb, const double* q1,
                                 const double* mu1, int64_t n1, const double* q2, const double* mu2, int64_t n2,
                                 const double* fil, int64_t nf, const double* pts, int64_t m, double skip_r,
-                                double* out, cudaStream_t s) {
-    if (m > 0)
-        k_vp_panel_vel<<<nblk(m, VT), VT, 0, s>>>(rec, sigma, mu, nb, q1, mu1, n1, q2, mu2, n2, fil, nf, pts, m, skip_r,
-                                                  out);
+                                double* out, double* scratch, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    const int64_t nc = vp_chunks(m, nb);
+    const int64_t chunk = nb > 0 ? ((nb + nc - 1) / nc + TILE - 1) / TILE * TILE : TILE;
+    const int64_t ncu = nb > 0 ? (nb + chunk - 1) / chunk : 0;
+    if (ncu > 0)
+        k_vp_panel_vel_part<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pts, m, skip_r,
+                                                                           scratch);
+    k_vp_panel_vel_fin<<<nblk(m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, q2, mu2, n2, fil, nf, pts, m, skip_r,
+                                                    out);
     return cudaGetLastError();
 }
 cudaError_t vp_launch_stretch_panels(const double* rec, const double* sigma, const double* mu, int64_t nb,
                                      const double* q1, const double* mu1, int64_t n1, const double* pos,
-                                     const double* str, int64_t m, double skip_x, double* out, cudaStream_t s) {
-    if (m > 0)
-        k_vp_stretch_panels<<<nblk(m, VT), VT, 0, s>>>(rec, sigma, mu, nb, q1, mu1, n1, pos, str, m, skip_x, out);
+                                     const double* str, int64_t m, double skip_x, double* out, double* scratch,
+                                     cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    const int64_t nc = vp_chunks(m, nb);
+    const int64_t chunk = nb > 0 ? ((nb + nc - 1) / nc + TILE - 1) / TILE * TILE : TILE;
+    const int64_t ncu = nb > 0 ? (nb + chunk - 1) / chunk : 0;
+    if (ncu > 0)
+        k_vp_stretch_part<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pos, str, m,
+                                                                         skip_x, scratch);
+    k_vp_stretch_fin<<<nblk(m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, pos, str, m, skip_x, out);
     return cudaGetLastError();
 }
 cudaError_t vp_launch_convect(double* pos, double* prevVel, const double* part, const double* pan, int64_t m,

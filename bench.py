@@ -249,7 +249,7 @@ def vortex_particles(steps=20):
     nodes, tris, ids, info = wing.make_wing(spec)
     keep = ids < 1000
     tris, ids = tris[keep], ids[keep]
-    S = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, dt=0.05, accelerate=True)
+    S = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, dt=0.05, accelerate=True, Sref=info["area"])
     S.step(3)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -257,6 +257,8 @@ def vortex_particles(steps=20):
     torch.cuda.synchronize()
     t_loop = time.perf_counter() - t0
     inf = S.info()
+    done = inf["timestep"] - 3  # fewer than `steps` once the Trefftz check has converged
+    tz = S.trefftz()
     # operators at 40k particles
     rng = np.random.default_rng(4)
     n = 40000
@@ -287,9 +289,10 @@ def vortex_particles(steps=20):
     return {"vp_unsteady": {
         "workload": "NACA 4412 AR 6 taper 0.6, %d body triangles, no wake panels, alpha 8 deg, dt 0.05, "
                     "Barnes-Hut theta 0.5 (FP64)" % len(verts),
-        "loop": {"steps": steps, "ms_per_step": t_loop / steps * 1e3, "particles_at_end": inf["n_particles"],
-                 "first_step": 4, "what": "cpg_vpcase_step: convection, shedding, strength update, octree, "
-                                          "source strengths, FP64 BiCGSTAB solve"},
+        "loop": {"steps": done, "ms_per_step": t_loop / max(done, 1) * 1e3, "particles_at_end": inf["n_particles"],
+                 "first_step": 4, "trefftz_CL": tz["CL"], "trefftz_CD": tz["CD"], "converged": tz["converged"],
+                 "what": "cpg_vpcase_step: convection, shedding, strength update, octree, source strengths, "
+                         "FP64 BiCGSTAB solve, Trefftz-plane convergence check"},
         "operators_40k_particles": {
             "tree_build_ms": t_tree, "barnes_hut_vel_stretch_diff_ms": t_bh,
             "panel_velocity_ms": t_pv, "panel_velocity_pairs_per_s": pairs / (t_pv * 1e-3),

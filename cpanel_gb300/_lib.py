@@ -67,7 +67,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_particles_velocity", "cpg_particles_stretch_diff",
            "cpg_panels_velocity", "cpg_panels_stretching", "cpg_vp_topology", "cpg_vpcase_create",
-           "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_particles",
+           "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_trefftz", "cpg_vpcase_particles",
            "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices",
            # cpanel_serve.h
            "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint"]
@@ -87,7 +87,7 @@ class RequestInfo(C.Structure):
 
 class VPParams(C.Structure):
     _fields_ = [("V", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("dt", C.c_double),
-                ("cref", C.c_double), ("accelerate", C.c_int)]
+                ("cref", C.c_double), ("accelerate", C.c_int), ("Sref", C.c_double), ("mach", C.c_double)]
 
 
 class VPInfo(C.Structure):
@@ -161,6 +161,7 @@ def load():
     L.cpg_vpcase_destroy.restype = None
     L.cpg_vpcase_info_get.argtypes = [vp, C.POINTER(VPInfo)]
     L.cpg_vpcase_step.argtypes = [vp, C.c_int]
+    L.cpg_vpcase_trefftz.argtypes = [vp, D, D, C.POINTER(C.c_int)]
     L.cpg_vpcase_particles.argtypes = [vp, D, D, D, I32, I32]
     L.cpg_vpcase_strengths.argtypes = [vp, D, D, D, D]
     L.cpg_vpcase_wake.argtypes = [vp, D, D]

@@ -1,7 +1,7 @@
 // The vortex-particle case driven step by step (include/cpanel_vp.h, cpg_vpcase_*).
 //
-// Restates cpCaseVP::run (CPanel/cpCaseVP.cpp:26-117) with the Trefftz early stop left
-// to the caller (cpg_vpcase_step advances a given number of steps).  State lives on the
+// Restates cpCaseVP::run (CPanel/cpCaseVP.cpp:26-117), including its Trefftz-plane early
+// stop (cpg_vpcase_step advances a given number of steps).  State lives on the
 // device; the host keeps the shedding bookkeeping, builds the octree after the strength
 // update (as the reference does) and solves the small sequential pieces of the shedding.
 //
@@ -122,6 +122,10 @@ struct cpg_vpcase {
     Buf spts, sout, scr;
     std::vector<double> filh;  // host copy of the filaments (8 per w2 panel)
     bool have_fil = false;
+    // Trefftz plane (cpCase CL_trefftz / CD_trefftz) and the early stop
+    double Sref = 1, PG = 1;
+    double CLt = 0, CDt = 0;
+    bool converged = false;
 };
 
 namespace {
@@ -394,6 +398,172 @@ cudaError_t build_tree(cpg_vpcase& S) {
     return cudaStreamSynchronize(S.s);
 }
 
+struct T3 {
+    double x, y, z;
+};
+inline T3 tsub(T3 a, T3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline T3 tadd(T3 a, T3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline T3 tmul(double s, T3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline double tnorm(T3 a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline T3 tunit(T3 a) {  // Eigen's normalized(): unchanged when zero
+    double z = a.x * a.x + a.y * a.y + a.z * a.z;
+    if (z > 0) {
+        double r = std::sqrt(z);
+        return {a.x / r, a.y / r, a.z / r};
+    }
+    return a;
+}
+
+// wake::wakeStrength, CPanel/wake.cpp:478-506: (mu_upper - mu_lower) interpolated in y
+// between the wake lines (wakeLine::getStrength, CPanel/wakeLine.cpp:26-29)
+double wake_strength(const cpg::VPGeom& G, const std::vector<double>& mu, double y) {
+    const size_t L = G.line_y.size();
+    size_t a = 0, b = 1;
+    if (y < G.line_y[1]) {
+        a = 0;
+        b = 1;
+    } else if (y >= G.line_y[L - 1]) {
+        a = L - 2;
+        b = L - 1;
+    } else {
+        for (size_t i = 1; i + 1 < L; i++)
+            if (G.line_y[i] <= y && G.line_y[i + 1] > y) {
+                a = i;
+                b = i + 1;
+            }
+    }
+    double interp = (y - G.line_y[a]) / (G.line_y[b] - G.line_y[a]);
+    double sa = mu[G.line_up[a]] - mu[G.line_lo[a]];
+    double sb = mu[G.line_up[b]] - mu[G.line_lo[b]];
+    return sa + interp * (sb - sa);
+}
+
+// wake::trefftzPlaneVP, CPanel/wake.cpp:191-320 (particlePntInWakeY :322-351,
+// stretchFactor :353-361) over the one buffer wake, scaled as in
+// cpCaseVP::trefftzPlaneAnalysisVP (CPanel/cpCaseVP.cpp:418-429).  The particle row shed
+// at step ceil_even(timestep)/2 + 2 is ordered by its parents' centre y and joined into
+// a curve; 3N points spaced evenly along it carry dPhi (the wake strength at the
+// interpolated parent y times the stretch of the row) and the downwash |w| of all
+// particles (Gaussian sums on the device); Simpson's rule integrates both.  A row of
+// fewer than two particles (undefined in the reference) gives zero.
+cudaError_t trefftz(cpg_vpcase& S, double& CL, double& CD) {
+    CL = CD = 0;
+    const cpg::VPGeom& G = S.G;
+    int steps = S.timestep;
+    if (steps % 2 != 0) steps++;
+    const int row = steps / 2 + 2;
+    std::vector<int64_t> unsorted;
+    for (int64_t i = 0; i < S.np; i++)
+        if (S.shed[i] == row) unsorted.push_back(i);
+    if (unsorted.size() < 2) return cudaSuccess;
+    cudaError_t e;
+    std::vector<double> hp(3 * S.np), mu(S.n);
+    if ((e = cudaMemcpyAsync(hp.data(), S.pos.p, sizeof(double) * 3 * S.np, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
+        return e;
+    if ((e = cudaMemcpyAsync(mu.data(), S.mu.p, sizeof(double) * S.n, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
+        return e;
+    if ((e = cudaStreamSynchronize(S.s)) != cudaSuccess) return e;
+    auto pos = [&](int64_t i) { return T3{hp[3 * i], hp[3 * i + 1], hp[3 * i + 2]}; };
+    auto pc = [&](int64_t i) {
+        const double* c = &G.w2[(size_t)S.parent[i] * cpg::QF_STRIDE + cpg::QF_C];
+        return T3{c[0], c[1], c[2]};
+    };
+    // repeated extraction of the lowest parent y (first one on ties)
+    std::vector<int64_t> sorted;
+    while (!unsorted.empty()) {
+        size_t li = 0;
+        double lowest = pc(unsorted[0]).y;
+        for (size_t i = 0; i < unsorted.size(); i++)
+            if (pc(unsorted[i]).y < lowest) {
+                lowest = pc(unsorted[i]).y;
+                li = i;
+            }
+        sorted.push_back(unsorted[li]);
+        unsorted.erase(unsorted.begin() + (long)li);
+    }
+    double Slen = 0;
+    for (size_t i = 0; i + 1 < sorted.size(); i++) Slen += tnorm(tsub(pos(sorted[i + 1]), pos(sorted[i])));
+    const int npts = (int)sorted.size() * 3;
+    const double step = Slen / npts;
+    std::vector<T3> pts{pos(sorted[0])};
+    std::vector<int64_t> p1{sorted[0]}, p2{sorted[1]};
+    T3 next = pos(sorted[1]);
+    size_t ni = 1;
+    T3 pt = pos(sorted[0]);
+    for (int i = 1; i < npts; i++) {
+        if (step < tnorm(tsub(next, pt))) {
+            T3 q = tadd(pt, tmul(step, tunit(tsub(next, pt))));
+            pts.push_back(q);
+            p1.push_back(sorted[ni - 1]);
+            p2.push_back(sorted[ni]);
+            pt = q;
+        } else {
+            double cov = tnorm(tsub(next, pt));
+            if (ni + 1 >= sorted.size()) break;  // rounding at the curve's end
+            pt = next;
+            next = pos(sorted[ni + 1]);
+            ni++;
+            T3 q = tadd(pt, tmul(step - cov, tunit(tsub(next, pt))));
+            pts.push_back(q);
+            p1.push_back(sorted[ni - 1]);
+            p2.push_back(sorted[ni]);
+            pt = q;
+        }
+    }
+    // downwash of all particles at the curve points (Gaussian sums, as particle::velInfl)
+    const int64_t m = (int64_t)pts.size();
+    std::vector<double> hq(3 * m), hv(3 * m);
+    for (int64_t i = 0; i < m; i++) {
+        hq[3 * i] = pts[i].x;
+        hq[3 * i + 1] = pts[i].y;
+        hq[3 * i + 2] = pts[i].z;
+    }
+    if ((e = S.spts.ensure(sizeof(double) * 3 * m, S.s)) != cudaSuccess) return e;
+    if ((e = S.sout.ensure(sizeof(double) * 6 * m, S.s)) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(S.spts.p, hq.data(), sizeof(double) * 3 * m, cudaMemcpyHostToDevice, S.s)) != cudaSuccess)
+        return e;
+    if ((e = pack_current(S)) != cudaSuccess) return e;
+    if ((e = particle_term_points(S, false, S.spts.as<double>(), m, S.np, S.sout.as<double>())) != cudaSuccess) return e;
+    if ((e = cudaMemcpyAsync(hv.data(), S.sout.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
+        return e;
+    if ((e = cudaStreamSynchronize(S.s)) != cudaSuccess) return e;
+    std::vector<double> Cl(npts + 1, 0.0), Cd(npts + 1, 0.0);
+    for (int64_t i = 1; i < m; i++) {
+        T3 A = pos(p1[i]), B = pos(p2[i]);
+        double d = tnorm(tsub(B, A)), a = tnorm(tsub(pts[i], A)), b = tnorm(tsub(B, pts[i]));
+        double yA = pc(p1[i]).y, yB = pc(p2[i]).y, y;
+        if (a < 1e-10)
+            y = yA;
+        else if (b < 1e-10)
+            y = yB;
+        else
+            y = yA + (a / d) * (yB - yA);
+        double fac = tnorm(tsub(pc(p2[i]), pc(p1[i]))) / tnorm(tsub(B, A));
+        double w = std::abs(hv[3 * i + 2]);
+        double dphi = -wake_strength(G, mu, y) * fac;
+        Cl[i] = 2 * dphi / (S.V * S.Sref);
+        Cd[i] = dphi * w / (S.V * S.V * S.Sref);
+    }
+    for (int i = 0; i < (int)Cl.size() - 2; i += 2) {
+        CL += 1.0 / 3 * step * (Cl[i] + 4 * Cl[i + 1] + Cl[i + 2]);
+        CD += 1.0 / 3 * step * (Cd[i] + 4 * Cd[i + 1] + Cd[i + 2]);
+    }
+    CL /= S.PG;
+    CD /= std::pow(S.PG, 2);
+    return cudaSuccess;
+}
+
+// cpCaseVP::solutionConvergence, CPanel/cpCaseVP.cpp:204-229 (steady case)
+cudaError_t convergence_check(cpg_vpcase& S) {
+    if (S.timestep < 5) return cudaSuccess;
+    double prevCL = S.CLt, prevCD = S.CDt;
+    cudaError_t e = trefftz(S, S.CLt, S.CDt);
+    if (e != cudaSuccess) return e;
+    double dCD = std::abs((S.CDt - prevCD) / prevCD), dCL = std::abs((S.CLt - prevCL) / prevCL);
+    S.converged = dCL < 0.0001 && dCD < 0.0001;
+    return cudaSuccess;
+}
+
 cudaError_t step_once(cpg_vpcase& S) {
     cudaError_t e;
     const double vinf[3] = {S.vinf[0], S.vinf[1], S.vinf[2]};
@@ -500,7 +670,8 @@ cudaError_t step_once(cpg_vpcase& S) {
             return e;
     }
     if ((e = solve(S, true)) != cudaSuccess) return e;
-    return cudaStreamSynchronize(S.s);
+    if ((e = cudaStreamSynchronize(S.s)) != cudaSuccess) return e;
+    return convergence_check(S);
 }
 
 }  // namespace
@@ -515,7 +686,8 @@ extern "C" {
 
 int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
                       int64_t n_tris, const cpg_vp_params* prm, cpg_vpcase** out) {
-    if (!ctx || !out || !prm || !nodes || !tris || !ids || n_nodes <= 0 || n_tris <= 0 || !(prm->V > 0)) {
+    if (!ctx || !out || !prm || !nodes || !tris || !ids || n_nodes <= 0 || n_tris <= 0 || !(prm->V > 0) ||
+        !(prm->Sref > 0) || !(std::abs(prm->mach) < 1)) {
         if (ctx) cpg::ctx_set_error(ctx, "bad argument");
         return CPG_E_INVALID;
     }
@@ -536,6 +708,8 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
     S.beta = prm->beta;
     S.cref = prm->cref > 0 ? prm->cref : 1.0;
     S.accelerate = prm->accelerate != 0;
+    S.Sref = prm->Sref;
+    S.PG = std::sqrt(1 - std::pow(prm->mach, 2));
     S.dt = S.G.dt;
     wind_to_body(S.V, S.alpha, S.beta, S.vinf);
     S.n = S.G.n_body;
@@ -612,13 +786,27 @@ int cpg_vpcase_info_get(const cpg_vpcase* S, cpg_vp_info* o) {
 int cpg_vpcase_step(cpg_vpcase* Sp, int nsteps) {
     if (!Sp || nsteps < 0) return CPG_E_INVALID;
     cpg_vpcase& S = *Sp;
-    for (int k = 0; k < nsteps; k++) {
+    for (int k = 0; k < nsteps && !S.converged; k++) {
         cudaError_t e = step_once(S);
         if (e != cudaSuccess) {
             cpg::ctx_set_error(S.ctx, std::string("vortex-particle step: ") + cudaGetErrorString(e));
             return e == cudaErrorMemoryAllocation ? CPG_E_OOM : CPG_E_CUDA;
         }
     }
+    return CPG_OK;
+}
+
+int cpg_vpcase_trefftz(cpg_vpcase* Sp, double* CL, double* CD, int* converged) {
+    if (!Sp) return CPG_E_INVALID;
+    double cl = 0, cd = 0;
+    cudaError_t e = trefftz(*Sp, cl, cd);
+    if (e != cudaSuccess) {
+        cpg::ctx_set_error(Sp->ctx, std::string("trefftz: ") + cudaGetErrorString(e));
+        return CPG_E_CUDA;
+    }
+    if (CL) *CL = cl;
+    if (CD) *CD = cd;
+    if (converged) *converged = Sp->converged ? 1 : 0;
     return CPG_OK;
 }
 

@@ -332,6 +332,11 @@ std::string build_vp_geometry(const double* nodes, int64_t nn, const int64_t* tr
         G.widx[4 * j + 3] = index[b->lo];
     }
     G.parent = parentW;
+    for (const Line& l : L) {
+        G.line_up.push_back(index[l.up]);
+        G.line_lo.push_back(index[l.lo]);
+        G.line_y.push_back(l.y);
+    }
     // shedding topology of the second row
     std::vector<int> w2pos(T.wake.size(), -1);
     for (size_t k = 0; k < w2.size(); k++) w2pos[w2[k]] = (int)k;

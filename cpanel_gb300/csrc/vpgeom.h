@@ -27,6 +27,10 @@ struct VPGeom {
     std::vector<int32_t> widx;     // 4 matrix columns per first-row panel
     std::vector<double> wcoef;     // interpolation coefficient per first-row panel
     std::vector<int32_t> parent;   // second-row panel -> its first-row parent (w1 index)
+    // wake lines sorted by y (wake::addWakeLine): upper and lower body panel (matrix
+    // order) and the y of the line's trailing-edge midpoint
+    std::vector<int32_t> line_up, line_lo;
+    std::vector<double> line_y;
     // shedding topology per second-row panel k
     std::vector<int32_t> eio;      // 4 edge ids in edgesInOrder order
     std::vector<int32_t> pio;      // 4 node ids in pointsInOrder order

@@ -218,12 +218,13 @@ def vp_topology(nodes, tris, ids, V=1.0, dt=0.0):
 class VPCase:
     """cpCaseVP on a body-only mesh, advanced step by step on the GPU."""
 
-    def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, ctx=None):
+    def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, Sref=1.0,
+                 mach=0.0, ctx=None):
         self.ctx = _ctx(ctx)
         nodes = np.ascontiguousarray(nodes, dtype=np.float64)
         tris = np.ascontiguousarray(tris, dtype=np.int64)
         ids = np.ascontiguousarray(ids, dtype=np.int32)
-        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0)
+        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0, Sref, mach)
         h = C.c_void_p()
         self.ctx.check(self.ctx.L.cpg_vpcase_create(self.ctx.h, nodes.ctypes.data_as(_lib.D), len(nodes),
                                                     tris.ctypes.data_as(_lib.I64), ids.ctypes.data_as(_lib.I32),
@@ -245,6 +246,12 @@ class VPCase:
     def step(self, n=1):
         self.ctx.check(self.ctx.L.cpg_vpcase_step(self.h, n), "step")
         return self.info()["timestep"]
+
+    def trefftz(self):
+        """Trefftz-plane CL, CD of the current state and whether the run has converged."""
+        cl, cd, cv = C.c_double(), C.c_double(), C.c_int()
+        self.ctx.check(self.ctx.L.cpg_vpcase_trefftz(self.h, C.byref(cl), C.byref(cd), C.byref(cv)), "trefftz")
+        return dict(CL=cl.value, CD=cd.value, converged=bool(cv.value))
 
     def particles(self):
         n = self.info()["n_particles"]

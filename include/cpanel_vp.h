@@ -114,6 +114,8 @@ typedef struct {
     double dt;             /* time step; <= 0: mean trailing-edge length / V (calcTimeStep) */
     double cref;           /* reference chord of the far-field cut-offs (12 c, 20 c)       */
     int accelerate;        /* Barnes-Hut (inputParams::accelerateCode) or direct sums      */
+    double Sref;           /* reference area of the Trefftz-plane coefficients (> 0)       */
+    double mach;           /* Prandtl-Glauert factor sqrt(1 - M^2) of those coefficients   */
 } cpg_vp_params;
 typedef struct {
     int64_t n_body, n_w1, n_w2;   /* body panels, first and second buffer rows           */
@@ -134,8 +136,16 @@ int  cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const
                        const int32_t* ids, int64_t n_tris, const cpg_vp_params* params, cpg_vpcase** out);
 void cpg_vpcase_destroy(cpg_vpcase* c);
 int  cpg_vpcase_info_get(const cpg_vpcase* c, cpg_vp_info* info);
-/* advance nsteps time steps (step 1: steady solve; 2: first buffer convection; then the loop) */
+/* advance nsteps time steps (step 1: steady solve; 2: first buffer convection; then the
+ * loop).  From step 5 on every step ends with the Trefftz-plane convergence check of
+ * cpCaseVP::solutionConvergence (CPanel/cpCaseVP.cpp:204-229): once CL and CD both change
+ * by less than 0.01 % the case is converged and further steps do nothing, as the
+ * reference leaves its time loop (CPanel/cpCaseVP.cpp:94-100). */
 int  cpg_vpcase_step(cpg_vpcase* c, int nsteps);
+/* Trefftz-plane CL and CD of the current state (cpCaseVP::trefftzPlaneAnalysisVP,
+ * CPanel/cpCaseVP.cpp:418-429; wake::trefftzPlaneVP, CPanel/wake.cpp:191-320) and whether
+ * the convergence check has fired.  Any pointer may be null. */
+int  cpg_vpcase_trefftz(cpg_vpcase* c, double* CL, double* CD, int* converged);
 /* host copies: particles in shedding order (pos, strength n x 3, radius, shed step, index
  * of the shedding second-row panel); any pointer may be null */
 int  cpg_vpcase_particles(cpg_vpcase* c, double* pos, double* strength, double* radius, int32_t* shed_time,

@@ -64,6 +64,8 @@ def lib():
         L.cpo_vpcase_dt.argtypes = [C.c_void_p]
         L.cpo_vpcase_wake.argtypes = [C.c_void_p, D, D, I32, D]
         L.cpo_vpcase_matrices.argtypes = [C.c_void_p, D, D, D]
+        L.cpo_vpcase_set_refs.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        L.cpo_vpcase_trefftz.argtypes = [C.c_void_p, D]
         L.cpo_vpcase_step.restype = C.c_int
         L.cpo_vpcase_step.argtypes = [C.c_void_p]
         L.cpo_vpcase_particles.argtypes = [C.c_void_p, D, D, D, I32, I32]
@@ -352,7 +354,8 @@ def panels_stretching(bverts, sigma, mu, wverts, wmu, pos, strength):
 class VPCase:
     """cpCaseVP on a body-only mesh: buffer wake, shedding, stretching, AB2 time loop."""
 
-    def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, num_steps=10):
+    def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, num_steps=10,
+                 Sref=1.0, mach=0.0):
         L = lib()
         self.nodes = np.ascontiguousarray(nodes, dtype=np.float64)
         self.tris = np.ascontiguousarray(tris, dtype=np.int64)
@@ -361,6 +364,12 @@ class VPCase:
                                   len(self.tris), V, alpha, beta, dt, cref, 1 if accelerate else 0, num_steps)
         if not self.h:
             raise ValueError("mesh has wake panels; the vortex-particle case builds its own")
+        L.cpo_vpcase_set_refs(self.h, Sref, mach)
+
+    def trefftz(self):
+        out = np.zeros(3)
+        lib().cpo_vpcase_trefftz(self.h, _p(out))
+        return dict(CL=out[0], CD=out[1], converged=bool(out[2]))
 
     def __del__(self):
         h = getattr(self, "h", None)

@@ -189,3 +189,25 @@ def test_vp_time_loop_matches_oracle(built, accelerate):
         so, sg = S.strengths(), G.strengths()
         for key in ("sigma", "mu", "mu_w1", "mu_w2"):
             assert np.abs(sg[key] - so[key]).max() <= 1e-9 * max(np.abs(so[key]).max(), 1e-12), (step, key)
+
+
+def test_vp_trefftz_and_early_stop_match_oracle(built):
+    """Trefftz plane of the particle row (wake::trefftzPlaneVP) after every step, and the
+    convergence stop of cpCaseVP::solutionConvergence at the same step."""
+    from cpanel_gb300 import vp, wing
+    spec = wing.WingSpec(m=0.0, p=0.4, t=0.12, root_chord=1.0, span=4.0, taper=1.0, sweep_deg=0.0, n_chord=6,
+                         n_span=4, wake_len=10.0, wake_dir=wing.wake_dir_for(4.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    tris, ids = tris[keep], ids[keep]
+    S = po.VPCase(nodes, tris, ids, V=1.0, alpha=4.0, Sref=info["area"], mach=0.2)
+    G = vp.VPCase(nodes, tris, ids, V=1.0, alpha=4.0, Sref=info["area"], mach=0.2)
+    for step in range(70):
+        ts_o, ts_g = S.step(), G.step()
+        assert ts_o == ts_g
+        to, tg = S.trefftz(), G.trefftz()
+        assert tg["converged"] == to["converged"], step
+        for key in ("CL", "CD"):
+            assert abs(tg[key] - to[key]) <= 1e-9 * max(abs(to[key]), 1e-12), (step, key)
+    assert to["converged"] and S.info()["timestep"] < 70
+    assert G.info()["timestep"] == S.info()["timestep"]

@@ -311,3 +311,27 @@ def test_vp_oracle_sheds_one_particle_per_te_edge_in_panel_order():
     assert list(p["shed_time"]) == [t for t in range(3, 7) for _ in range(n2)]
     assert list(p["parent"]) == list(range(n2)) * 4
     assert np.all(np.isfinite(p["pos"])) and np.all(p["radius"] > 0)
+
+
+def test_oracle_vp_converges_and_stops():
+    """cpCaseVP::solutionConvergence on the oracle: no Trefftz check before step 5, the
+    stop once CL and CD change by < 0.01 %, and no further steps after it."""
+    from cpanel_gb300 import wing
+    spec = wing.WingSpec(m=0.0, p=0.4, t=0.12, root_chord=1.0, span=4.0, taper=1.0, sweep_deg=0.0, n_chord=6,
+                         n_span=4, wake_len=10.0, wake_dir=wing.wake_dir_for(4.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    S = po.VPCase(nodes, tris[keep], ids[keep], V=1.0, alpha=4.0, Sref=info["area"])
+    hist = []
+    for _ in range(80):
+        ts = S.step()
+        t = S.trefftz()
+        hist.append((ts, t["CL"], t["CD"], t["converged"]))
+        if t["converged"]:
+            break
+    ts, CL, CD, conv = hist[-1]
+    assert conv and 5 < ts < 80
+    assert not any(h[3] for h in hist[:-1])
+    prev = hist[-2]
+    assert abs(CL - prev[1]) < 1e-4 * abs(prev[1]) and abs(CD - prev[2]) < 1e-4 * abs(prev[2])
+    assert S.step() == ts and S.info()["n_particles"] == 3 * (ts - 2)

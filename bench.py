@@ -161,8 +161,30 @@ def cpu_cost_model(nodes, tris, ids, refs, nthreads):
     return k / t_sweep, sample
 
 
+def _mesh_ok(nodes, tris, ids):
+    """The host topology check of cpg_geometry_create (no device use)."""
+    from cpanel_gb300 import _lib
+    L = _lib.load()
+    nodes = np.ascontiguousarray(nodes, dtype=np.float64)
+    tris = np.ascontiguousarray(tris, dtype=np.int64)
+    ids = np.ascontiguousarray(ids, dtype=np.int32)
+    info = _lib.GeometryInfo()
+    return L.cpg_topology(nodes.ctypes.data_as(_lib.D), len(nodes), tris.ctypes.data_as(_lib.I64),
+                          ids.ctypes.data_as(_lib.I32), len(ids), C.byref(info), None, None, None, None, None) == 0
+
+
 def _wing_with(ntri_target, rng, **kw):
-    """A seeded NACA wing with about ntri_target body triangles (for the request mix)."""
+    """A seeded NACA wing with about ntri_target body triangles (for the request mix);
+    draws again when the generator made a mesh whose topology the path rejects (a tip
+    panel at the trailing edge without a usable CHTLS neighbourhood)."""
+    for _ in range(20):
+        out = _draw_wing(ntri_target, rng)
+        if _mesh_ok(*out[:3]):
+            return out
+    raise RuntimeError("no valid wing drawn")
+
+
+def _draw_wing(ntri_target, rng):
     from cpanel_gb300 import wing
     nc = int(rng.integers(20, 101))
     ns = int(max(15, min(400, round(ntri_target / (4.0 * (nc - 1)) + 1))))
@@ -177,8 +199,9 @@ def _wing_with(ntri_target, rng, **kw):
 
 def batched_and_served():
     """Config 3 (64 uneven wings x 8 alphas submitted together) and a bounded sample of
-    config 5 (Poisson arrivals, 50 req/s, steady wings of 1k-40k triangles) through the
-    request loop (include/cpanel_serve.h), mixed precision, 8 and 4 slots."""
+    config 5 (Poisson arrivals, 50 req/s, steady wings of 1k-40k triangles and ~10%
+    unsteady 100-step particle-wake runs on ~4k-triangle wings) through the request loop
+    (include/cpanel_serve.h), mixed precision, 8 and 4 slots."""
     from cpanel_gb300 import serve, wing
     out = {}
     # ---- config 3
@@ -205,42 +228,68 @@ def batched_and_served():
         "p50_ms": float(np.percentile([r["info"]["total_ms"] for r in res], 50)),
         "max_concurrent": max(r["info"]["running_at_start"] for r in res), "slots": 8,
         "how": "all submitted at once to the request loop; each request is assembly + LU + 8 refined solves + post"}
-    # ---- config 5 (bounded sample)
+    # ---- config 5 (bounded sample): steady requests and ~10% unsteady particle-wake runs
     rng = np.random.default_rng(7)
     nreq = 32
     gaps = rng.exponential(1.0 / 50.0, nreq)
     reqs = []
     for q in range(nreq):
-        nodes, tris, ids, refs = _wing_with(float(rng.uniform(1000, 40000)), rng)
-        flows = [(1.0, float(a), 0.0, MACH) for a in rng.uniform(-2, 10, 4)]
-        reqs.append((nodes, tris, ids, flows, refs))
+        if q % 10 == 5:  # unsteady: 100 steps on a ~4k-triangle wing, body panels only
+            nodes, tris, ids, refs = _wing_with(4000.0, rng)
+            keep = ids < 1000
+            reqs.append(("vp", nodes, tris[keep], ids[keep], refs))
+        else:
+            nodes, tris, ids, refs = _wing_with(float(rng.uniform(1000, 40000)), rng)
+            flows = [(1.0, float(a), 0.0, MACH) for a in rng.uniform(-2, 10, 4)]
+            reqs.append(("steady", nodes, tris, ids, flows, refs))
+
+    def submit(srv, r):
+        if r[0] == "vp":
+            return srv.submit_vp(r[1], r[2], r[3], 100, alpha=8.0, dt=0.05, Sref=r[4]["Sref"], precision="mixed")
+        return srv.submit(*r[1:5], **r[5])
+
     srv = serve.Server(slots=4, budget_gb=160.0, precision="mixed")
-    srv.wait(srv.submit(*reqs[0][:4], **reqs[0][4]))
+    srv.wait(submit(srv, reqs[0]))  # warm-up
+    srv.wait(srv.submit_vp(*reqs[5][1:4], 4, alpha=8.0, dt=0.05, precision="mixed"))
     tickets = []
     t0 = time.perf_counter()
     for q in range(nreq):
         time.sleep(gaps[q])
-        tickets.append(srv.submit(*reqs[q][:4], **reqs[q][4]))
+        tickets.append(submit(srv, reqs[q]))
     res = [srv.wait(t) for t in tickets]
     wall = time.perf_counter() - t0
     srv.close()
+    kinds = [r[0] for r in reqs]
     lat = [r["info"]["total_ms"] for r in res]
-    nsol = sum(len(r[3]) for r in reqs)
+    lat_s = [l for l, k in zip(lat, kinds) if k == "steady"]
+    lat_u = [l for l, k in zip(lat, kinds) if k == "vp"]
+    nsol = sum(len(r[4]) for r in reqs if r[0] == "steady")
+    nb = [r["info"]["n_body"] for r, k in zip(res, kinds) if k == "steady"]
     out["serving"] = {
-        "workload": "%d steady requests, Poisson arrivals at 50 req/s (seed 7), NACA wings of %d-%d body panels, "
-                    "4 alphas each; unsteady requests not included" % (nreq, min(r["info"]["n_body"] for r in res),
-                                                                     max(r["info"]["n_body"] for r in res)),
+        "workload": "%d requests, Poisson arrivals at 50 req/s (seed 7): %d steady (NACA wings of %d-%d body panels, "
+                    "4 alphas each) and %d unsteady (vortex-particle wake, 100 steps of dt 0.05, alpha 8, "
+                    "%d-%d body panels, mixed precision)"
+                    % (nreq, len(lat_s), min(nb), max(nb), len(lat_u),
+                       min(r["info"]["n_body"] for r, k in zip(res, kinds) if k == "vp"),
+                       max(r["info"]["n_body"] for r, k in zip(res, kinds) if k == "vp")),
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-        "solves_per_s": nsol / wall, "wall_s": wall, "slots": 4,
+        "steady_p50_ms": float(np.percentile(lat_s, 50)), "steady_p99_ms": float(np.percentile(lat_s, 99)),
+        "unsteady_p50_ms": float(np.percentile(lat_u, 50)), "unsteady_max_ms": float(max(lat_u)),
+        "unsteady_particles": [int(r["n_particles"]) for r, k in zip(res, kinds) if k == "vp"],
+        "steady_solves_per_s": nsol / wall, "wall_s": wall, "slots": 4,
         "max_concurrent": max(r["info"]["running_at_start"] for r in res),
-        "latency": "submit -> results on the host (includes topology, uploads, assembly, LU, solves, post)"}
+        "latency": "submit -> results on the host (steady: topology, uploads, assembly, LU, solves, post; "
+                   "unsteady: buffer wake, matrices, LU, 100 steps)"}
     return out
 
 
 def vortex_particles(steps=20):
     """Config 4 (bounded sample): NACA 4412 AR 6 wing of 8,216 body triangles without wake
-    panels, alpha 8 deg, dt 0.05, Barnes-Hut on: the first `steps` steps of the VP loop, then
-    the particle operators on 40,000 particles spread behind the wing."""
+    panels, alpha 8 deg, dt 0.05, Barnes-Hut on: the first `steps` steps of the VP loop in
+    FP64 and in the mixed form (FP32 far fields, FP64 near fields, FP32 LU refined in
+    FP64), the particle-velocity check of the final state (mixed and FP64 octree against
+    the FP64 direct sum), then the particle operators on 40,000 particles spread behind
+    the wing in both precisions."""
     import torch
 
     from cpanel_gb300 import vp, wing
@@ -249,21 +298,44 @@ def vortex_particles(steps=20):
     nodes, tris, ids, info = wing.make_wing(spec)
     keep = ids < 1000
     tris, ids = tris[keep], ids[keep]
-    S = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, dt=0.05, accelerate=True, Sref=info["area"])
-    S.step(3)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    S.step(steps)
-    torch.cuda.synchronize()
-    t_loop = time.perf_counter() - t0
-    inf = S.info()
-    done = inf["timestep"] - 3  # fewer than `steps` once the Trefftz check has converged
-    tz = S.trefftz()
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+    loops, cases = {}, {}
+    for prec in ("plain", "mixed"):
+        t0 = time.perf_counter()
+        S = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, dt=0.05, accelerate=True, Sref=info["area"], precision=prec)
+        S.step(3)
+        torch.cuda.synchronize()
+        t_setup = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        S.step(steps)
+        torch.cuda.synchronize()
+        t_loop = time.perf_counter() - t0
+        inf = S.info()
+        done = inf["timestep"] - 3  # fewer than `steps` once the Trefftz check has converged
+        tz = S.trefftz()
+        loops[prec] = {"steps": done, "ms_per_step": t_loop / max(done, 1) * 1e3, "setup_and_first_3_steps_s": t_setup,
+                       "particles_at_end": inf["n_particles"], "trefftz_CL": tz["CL"], "trefftz_CD": tz["CD"],
+                       "converged": tz["converged"], "solve_fallbacks": inf["solve_fallbacks"]}
+        cases[prec] = S
+    P = cases["plain"]
+    v64, v32, vdir = P.velocities("plain"), P.velocities("mixed"), P.velocities("plain", direct=True)
+    check = {"particles": int(len(v64)), "mixed_vs_plain_octree": rel(v32, v64),
+             "plain_octree_vs_fp64_direct": rel(v64, vdir), "mixed_vs_fp64_direct": rel(v32, vdir),
+             "what": "max |dv| / max |v| over the convective particle velocities (Vinf + particles + panels)"}
+    pm, pp = cases["mixed"].particles(), P.particles()
+    drift = {"same_shedding": bool(np.array_equal(pm["shed_time"], pp["shed_time"])
+                                   and np.array_equal(pm["parent"], pp["parent"])),
+             "pos_rel": rel(pm["pos"], pp["pos"]), "strength_rel": rel(pm["strength"], pp["strength"]),
+             "CL_rel": abs(loops["mixed"]["trefftz_CL"] - loops["plain"]["trefftz_CL"]) / abs(loops["plain"]["trefftz_CL"])}
+    del cases, P
     # operators at 40k particles
     rng = np.random.default_rng(4)
     n = 40000
     pos = np.c_[rng.uniform(1.0, 15.0, n), rng.uniform(-2.4, 2.4, n), rng.normal(0, 0.3, n)]
-    P = torch.tensor(pos, device="cuda")
+    Pt = torch.tensor(pos, device="cuda")
     A = torch.tensor(rng.normal(size=(n, 3)) * 0.01, device="cuda")
     R = torch.full((n,), 0.05, dtype=torch.float64, device="cuda")
     verts = np.asarray(nodes)[np.asarray(tris) - 1].reshape(-1, 9)
@@ -280,23 +352,31 @@ def vortex_particles(steps=20):
         torch.cuda.synchronize()
         return (time.perf_counter() - t) / reps * 1e3
 
-    t_tree = timed(lambda: vp.ParticleFMM(P, A, R))
-    tree = vp.ParticleFMM(P, A, R)
-    t_bh = timed(lambda: tree.barnesHut(True, True, True))
-    t_pv = timed(lambda: vp.panels_velocity(BV, SG, MU, None, None, P), 1)
-    t_ps = timed(lambda: vp.panels_stretching(BV, SG, MU, None, None, P, A), 1)
     pairs = float(n) * len(verts)
+    ops, outs = {}, {}
+    tree = vp.ParticleFMM(Pt, A, R)
+    for prec in ("plain", "mixed"):
+        tree.set_precision(prec)
+        o = {"barnes_hut_vel_stretch_diff_ms": timed(lambda: tree.barnesHut(True, True, True))}
+        o["panel_velocity_ms"] = timed(lambda: vp.panels_velocity(BV, SG, MU, None, None, Pt, precision=prec), 1)
+        o["panel_stretching_ms"] = timed(lambda: vp.panels_stretching(BV, SG, MU, None, None, Pt, A, precision=prec), 1)
+        o["panel_velocity_pairs_per_s"] = pairs / (o["panel_velocity_ms"] * 1e-3)
+        o["panel_stretching_pairs_per_s"] = pairs / (o["panel_stretching_ms"] * 1e-3)
+        ops[prec] = o
+        outs[prec] = [x.cpu().numpy() for x in tree.barnesHut(True, True, True)] + [
+            vp.panels_velocity(BV, SG, MU, None, None, Pt, precision=prec).cpu().numpy(),
+            vp.panels_stretching(BV, SG, MU, None, None, Pt, A, precision=prec).cpu().numpy()]
+    names = ("bh_velocity", "bh_stretching", "bh_diffusion", "panel_velocity", "panel_stretching")
+    ops["mixed_vs_plain_rel"] = {k: rel(outs["mixed"][i], outs["plain"][i]) for i, k in enumerate(names)}
+    ops["tree_build_ms"] = timed(lambda: vp.ParticleFMM(Pt, A, R))
     return {"vp_unsteady": {
         "workload": "NACA 4412 AR 6 taper 0.6, %d body triangles, no wake panels, alpha 8 deg, dt 0.05, "
-                    "Barnes-Hut theta 0.5 (FP64)" % len(verts),
-        "loop": {"steps": done, "ms_per_step": t_loop / max(done, 1) * 1e3, "particles_at_end": inf["n_particles"],
-                 "first_step": 4, "trefftz_CL": tz["CL"], "trefftz_CD": tz["CD"], "converged": tz["converged"],
-                 "what": "cpg_vpcase_step: convection, shedding, strength update, octree, source strengths, "
-                         "FP64 BiCGSTAB solve, Trefftz-plane convergence check"},
-        "operators_40k_particles": {
-            "tree_build_ms": t_tree, "barnes_hut_vel_stretch_diff_ms": t_bh,
-            "panel_velocity_ms": t_pv, "panel_velocity_pairs_per_s": pairs / (t_pv * 1e-3),
-            "panel_stretching_ms": t_ps, "panel_stretching_pairs_per_s": pairs / (t_ps * 1e-3)}}}
+                    "Barnes-Hut theta 0.5" % len(verts),
+        "loop": loops, "first_step": 4,
+        "what": "cpg_vpcase_step: convection, shedding, strength update, octree, source strengths, solve "
+                "(plain: FP64 BiCGSTAB; mixed: FP32 LU refined in FP64), Trefftz-plane convergence check",
+        "velocity_check": check, "mixed_vs_plain_state": drift,
+        "operators_40k_particles": ops}}
 
 
 def run_reference(args):

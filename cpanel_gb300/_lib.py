@@ -65,12 +65,13 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak",
            # cpanel_vp.h
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
-           "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_particles_velocity", "cpg_particles_stretch_diff",
+           "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_ptree_set_precision", "cpg_set_particle_precision", "cpg_particles_velocity", "cpg_particles_stretch_diff",
            "cpg_panels_velocity", "cpg_panels_stretching", "cpg_vp_topology", "cpg_vpcase_create",
-           "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_trefftz", "cpg_vpcase_particles",
+           "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_trefftz", "cpg_vpcase_velocities", "cpg_vpcase_particles",
            "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices",
            # cpanel_serve.h
-           "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint"]
+           "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint",
+           "cpg_server_submit_vp", "cpg_server_wait_vp", "cpg_server_footprint_vp"]
 
 VEL_GAUSS_SYM, VEL_GAUSS, VEL_ALG = 1, 2, 3
 
@@ -85,15 +86,21 @@ class RequestInfo(C.Structure):
                 ("running_at_start", C.c_int), ("message", C.c_char * 160)]
 
 
+class VPResult(C.Structure):
+    _fields_ = [("CL", C.c_double), ("CD", C.c_double), ("steps", C.c_int64), ("n_particles", C.c_int64),
+                ("converged", C.c_int)]
+
+
 class VPParams(C.Structure):
     _fields_ = [("V", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("dt", C.c_double),
-                ("cref", C.c_double), ("accelerate", C.c_int), ("Sref", C.c_double), ("mach", C.c_double)]
+                ("cref", C.c_double), ("accelerate", C.c_int), ("Sref", C.c_double), ("mach", C.c_double),
+                ("precision", C.c_int)]
 
 
 class VPInfo(C.Structure):
     _fields_ = [("n_body", C.c_int64), ("n_w1", C.c_int64), ("n_w2", C.c_int64), ("n_particles", C.c_int64),
                 ("timestep", C.c_int64), ("solver_iters", C.c_int64), ("dt", C.c_double),
-                ("n_tree_nodes", C.c_int64)]
+                ("n_tree_nodes", C.c_int64), ("solve_fallbacks", C.c_int64)]
 
 
 class PTreeInfo(C.Structure):
@@ -154,14 +161,22 @@ def load():
     L.cpg_server_wait.argtypes = [vp, C.c_int64, D, D, D, C.POINTER(RequestInfo)]
     L.cpg_server_footprint.argtypes = [C.c_int64, C.c_int, C.c_int]
     L.cpg_server_footprint.restype = C.c_int64
+    L.cpg_server_submit_vp.argtypes = [vp, D, C.c_int64, I64, I32, C.c_int64, C.POINTER(VPParams), C.c_int,
+                                       C.POINTER(C.c_int64)]
+    L.cpg_server_wait_vp.argtypes = [vp, C.c_int64, C.POINTER(VPResult), D, C.POINTER(RequestInfo)]
+    L.cpg_server_footprint_vp.argtypes = [C.c_int64, C.c_int64, C.c_int, C.c_int]
+    L.cpg_server_footprint_vp.restype = C.c_int64
     L.cpg_panels_stretching.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, vp, C.c_int64, vp]
     L.cpg_vp_topology.argtypes = [D, C.c_int64, I64, I32, C.c_int64, C.c_double, C.c_double, I64, D, D, D, I32, D, I32]
     L.cpg_vpcase_create.argtypes = [vp, D, C.c_int64, I64, I32, C.c_int64, C.POINTER(VPParams), C.POINTER(vp)]
     L.cpg_vpcase_destroy.argtypes = [vp]
     L.cpg_vpcase_destroy.restype = None
     L.cpg_vpcase_info_get.argtypes = [vp, C.POINTER(VPInfo)]
+    L.cpg_ptree_set_precision.argtypes = [vp, C.c_int]
+    L.cpg_set_particle_precision.argtypes = [vp, C.c_int]
     L.cpg_vpcase_step.argtypes = [vp, C.c_int]
     L.cpg_vpcase_trefftz.argtypes = [vp, D, D, C.POINTER(C.c_int)]
+    L.cpg_vpcase_velocities.argtypes = [vp, C.c_int, C.c_int, D]
     L.cpg_vpcase_particles.argtypes = [vp, D, D, D, I32, I32]
     L.cpg_vpcase_strengths.argtypes = [vp, D, D, D, D]
     L.cpg_vpcase_wake.argtypes = [vp, D, D]

@@ -19,6 +19,7 @@
 #include "mesh.h"
 #include "octree.h"
 #include "particles.h"
+#include "vpkern.h"
 #include "post.h"
 
 struct cpg_ctx {
@@ -28,6 +29,7 @@ struct cpg_ctx {
     std::string err;
     cpg::Prof* prof = nullptr;  // device-time accounting, when enabled
     cublasHandle_t blas = nullptr;
+    int particle_precision = CPG_PLAIN_FP64;  // cpg_panels_velocity / cpg_panels_stretching
 };
 
 namespace {
@@ -97,7 +99,8 @@ struct cpg_geometry {
 struct cpg_ptree {
     cpg_ctx* ctx = nullptr;
     cpg::ParticleTree T;
-    DevBuf nodes, parts;
+    DevBuf nodes, parts, fnodes;
+    int precision = CPG_PLAIN_FP64;
 };
 
 namespace cpg {
@@ -105,6 +108,18 @@ void ctx_set_error(cpg_ctx* ctx, const std::string& msg) {
     if (ctx) ctx->err = msg;
 }
 cudaStream_t ctx_stream(cpg_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
+int ctx_particle_precision(cpg_ctx* ctx) { return ctx ? ctx->particle_precision : CPG_PLAIN_FP64; }
+void* ctx_blas(cpg_ctx* ctx) {
+    if (!ctx) return nullptr;
+    if (!ctx->blas) {
+        if (cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) {
+            ctx->blas = nullptr;
+            return nullptr;
+        }
+        cublasSetStream(ctx->blas, ctx->stream);
+    }
+    return ctx->blas;
+}
 }  // namespace cpg
 
 namespace {
@@ -676,6 +691,7 @@ int cpg_ptree_build(cpg_ctx* ctx, const double* pos, const double* strength, con
     }
     cpg::build_particle_tree(hp.data(), hs.data(), hr.data(), n, max_members, theta, t->T);
     cudaError_t e = upload(t->nodes, t->T.nodes, s);
+    if (e == cudaSuccess) e = upload(t->fnodes, t->T.fnodes, s);
     if (e == cudaSuccess) e = upload(t->parts, t->T.parts, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -689,6 +705,7 @@ int cpg_ptree_build(cpg_ctx* ctx, const double* pos, const double* strength, con
 void cpg_ptree_destroy(cpg_ptree* t) {
     if (!t) return;
     t->nodes.release();
+    t->fnodes.release();
     t->parts.release();
     delete t;
 }
@@ -742,11 +759,25 @@ int cpg_bh_velocity_points(cpg_ptree* t, const double* pts, int64_t m, double* v
         CK(cudaMemsetAsync(vel, 0, sizeof(double) * 3 * m, ctx->stream), "barnesHutVel");
     } else {
         cpg::ProfScope ps(cpg::Prof::PARTICLES, ctx->stream);
-        CK(cpg::launch_bh_points(t->nodes.as<cpg::BHNode>(), nn, t->parts.as<cpg::BHPart>(), t->T.theta, pts, m,
+        CK(cpg::launch_bh_points(t->nodes.as<cpg::BHNode>(),
+                                 t->precision == CPG_MIXED ? t->fnodes.as<cpg::BHNodeF>() : nullptr, nn,
+                                 t->parts.as<cpg::BHPart>(), t->T.theta, pts, m,
                                  cpg::vp_constants(), vel, ctx->stream),
            "barnesHutVel");
     }
     CK(cudaStreamSynchronize(ctx->stream), "barnesHutVel");
+    return CPG_OK;
+}
+
+int cpg_set_particle_precision(cpg_ctx* ctx, int precision) {
+    if (!ctx || (precision != CPG_PLAIN_FP64 && precision != CPG_MIXED)) return CPG_E_INVALID;
+    ctx->particle_precision = precision;
+    return CPG_OK;
+}
+
+int cpg_ptree_set_precision(cpg_ptree* t, int precision) {
+    if (!t || (precision != CPG_PLAIN_FP64 && precision != CPG_MIXED)) return CPG_E_INVALID;
+    t->precision = precision;
     return CPG_OK;
 }
 
@@ -762,7 +793,9 @@ int cpg_bh_particles(cpg_ptree* t, double* vel, double* stretch, double* diff) {
             if (o) CK(cudaMemsetAsync(o, 0, sizeof(double) * 3 * n, ctx->stream), "barnesHut");
     } else {
         cpg::ProfScope ps(cpg::Prof::PARTICLES, ctx->stream);
-        CK(cpg::launch_bh_particles(t->nodes.as<cpg::BHNode>(), nn, t->parts.as<cpg::BHPart>(), n, t->T.theta,
+        CK(cpg::launch_bh_particles(t->nodes.as<cpg::BHNode>(),
+                                    t->precision == CPG_MIXED ? t->fnodes.as<cpg::BHNodeF>() : nullptr, nn,
+                                    t->parts.as<cpg::BHPart>(), n, t->T.theta,
                                     cpg::vp_constants(), vel, stretch, diff, ctx->stream),
            "barnesHut");
     }
@@ -827,9 +860,24 @@ int cpg_panels_velocity(cpg_ctx* ctx, const double* body_verts, const double* si
     if (m == 0) return CPG_OK;
     ProfInstall pi(ctx);
     cudaStream_t s = ctx->stream;
-    DevBuf rec;
+    DevBuf rec, scr;
     CK(rec.ensure(sizeof(double) * 24 * std::max<int64_t>(1, nb + nw)), "alloc panel records");
-    {
+    if (ctx->particle_precision == CPG_MIXED) {
+        // body panels through the chunked kernel with the far field in FP32, then the wake
+        // triangles (FP64) added on top
+        CK(scr.ensure(sizeof(double) * std::max<int64_t>(cpg::vp_scratch_doubles(m, nb), 3 * m)), "alloc scratch");
+        cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
+        CK(cpg::launch_pack_records(body_verts, nb, rec.as<double>(), s), "panel records");
+        CK(cpg::vp_launch_panel_vel(rec.as<double>(), sigma, mu, nb, nullptr, nullptr, 0, nullptr, nullptr, 0, nullptr,
+                                    0, pts, m, 0.0, vel, scr.as<double>(), s, true),
+           "panel velocity");
+        if (nw > 0) {
+            CK(cpg::launch_panels_velocity(nullptr, nullptr, nullptr, 0, wake_verts, wake_mu, nw, pts, m,
+                                           rec.as<double>(), scr.as<double>(), s),
+               "wake velocity");
+            CK(cpg::vp_launch_add(vel, scr.as<double>(), 3 * m, s), "wake velocity");
+        }
+    } else {
         cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
         CK(cpg::launch_panels_velocity(body_verts, sigma, mu, nb, wake_verts, wake_mu, nw, pts, m, rec.as<double>(),
                                        vel, s),
@@ -837,6 +885,7 @@ int cpg_panels_velocity(cpg_ctx* ctx, const double* body_verts, const double* si
     }
     cudaError_t e = cudaStreamSynchronize(s);
     rec.release();
+    scr.release();
     CK(e, "panel velocity");
     return CPG_OK;
 }

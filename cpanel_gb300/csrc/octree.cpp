@@ -174,6 +174,24 @@ void build_particle_tree(const double* pos, const double* str, const double* rad
         nd.width = 2 * hh[0];
     }
     T.nodes[0].width = 2 * T.half[0];
+    T.fnodes.resize(T.nodes.size());
+    for (size_t i = 0; i < T.nodes.size(); i++) {
+        const BHNode& nd = T.nodes[i];
+        BHNodeF& f = T.fnodes[i];
+        f.hx = (float)nd.ex;
+        f.hy = (float)nd.ey;
+        f.hz = (float)nd.ez;
+        f.lx = (float)(nd.ex - (double)f.hx);
+        f.ly = (float)(nd.ey - (double)f.hy);
+        f.lz = (float)(nd.ez - (double)f.hz);
+        f.ax = (float)nd.ax;
+        f.ay = (float)nd.ay;
+        f.az = (float)nd.az;
+        f.erad = (float)nd.erad;
+        const double fr = nd.width / theta, ct = 5 * nd.erad;
+        f.far2 = (float)(fr * fr);
+        f.cut2 = (float)(ct * ct);
+    }
 }
 
 void particle_tree_table(const ParticleTree& T, double* out) {

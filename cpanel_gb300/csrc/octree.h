@@ -40,6 +40,19 @@ struct BHPart {
     double idx;  // original particle index (exact in a double)
 };
 
+// Single-precision view of a node's far-field data, for traversals that evaluate far
+// nodes in FP32 (48 bytes): expansion centre split into a high and a low float (the
+// difference to a target is then accurate to float rounding of the difference itself),
+// strength and radius, and the squared distances beyond which the node is far
+// ((width / theta)^2) and within which its stretching acts ((5 erad)^2).  The
+// traversal compares squared distances against these with a relative margin and falls
+// back to the exact FP64 test inside the margin, so every decision equals the FP64 one.
+struct BHNodeF {
+    float hx, hy, hz, lx;
+    float ly, lz, ax, ay;
+    float az, erad, far2, cut2;
+};
+
 constexpr int kBHMaxLevel = 32;  // a node at this level stays a leaf (reference: unbounded)
 constexpr int kBHNodeFields = 24;
 
@@ -52,6 +65,7 @@ struct ParticleTree {
     std::vector<double> origin, half;  // 3 per node
     std::vector<int32_t> level, child;  // child: 8 per node (pre-order index or -1)
     std::vector<BHNode> nodes;
+    std::vector<BHNodeF> fnodes;  // FP32 view of nodes (same order)
     std::vector<int64_t> perm;  // slot -> particle index (leaves in pre-order)
     std::vector<BHPart> parts;  // slot order
 };

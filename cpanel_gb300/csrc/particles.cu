@@ -17,6 +17,9 @@
 // |x_s - x_t| > 5 r_s, zero distance) are computed with explicitly rounded
 // intrinsics, so they match the host exactly although this file keeps FMA
 // contraction for the pair arithmetic.
+//
+// The *_f32 traversals are the mixed-precision form: far nodes in FP32, leaves (the
+// direct near field) in FP64, the same decisions as the FP64 traversal.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -132,6 +135,179 @@ __device__ __forceinline__ Tgt load_part_g(const BHPart* __restrict__ parts, int
     return Tgt{mk3(a0.x, a0.y, a1.x), a1.y, mk3(b0.x, b0.y, b1.x), b1.y};
 }
 
+// ---- FP32 far field ----
+// A far node's interaction is evaluated in FP32 from the node's float view (BHNodeF)
+// and a target split into high and low floats; the near field (leaf members) stays
+// FP64.  Far/near and stretching cut-off decisions compare float squared distances
+// with a relative margin of 1e-5 (far beyond any float rounding of the distance) and
+// take the exact FP64 test inside it, so the traversal visits the same nodes in the
+// same order as the FP64 one.  Far contributions are summed with compensation
+// (Kahan) in float and added to the FP64 accumulators once per target.
+
+constexpr float kBandLo = 1.0f - 1e-5f, kBandHi = 1.0f + 1e-5f;
+
+struct TgtF {
+    float hx, hy, hz, lx, ly, lz;
+    float r, ax, ay, az;
+};
+
+__device__ __forceinline__ TgtF split_tgt(const Tgt& t) {
+    TgtF f;
+    f.hx = __double2float_rn(t.x.x);
+    f.hy = __double2float_rn(t.x.y);
+    f.hz = __double2float_rn(t.x.z);
+    f.lx = __double2float_rn(t.x.x - (double)f.hx);
+    f.ly = __double2float_rn(t.x.y - (double)f.hy);
+    f.lz = __double2float_rn(t.x.z - (double)f.hz);
+    f.r = __double2float_rn(t.r);
+    f.ax = __double2float_rn(t.a.x);
+    f.ay = __double2float_rn(t.a.y);
+    f.az = __double2float_rn(t.a.z);
+    return f;
+}
+
+__device__ __forceinline__ BHNodeF load_fnode(const BHNodeF* __restrict__ f, int i) {
+    const float4* p = reinterpret_cast<const float4*>(f + i);
+    float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
+    return BHNodeF{a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x, c.y, c.z, c.w};
+}
+
+__device__ __forceinline__ int4 load_links(const BHNode* __restrict__ nodes, int i) {
+    return __ldg(reinterpret_cast<const int4*>(nodes + i) + 4);  // first, count, skip, leaf
+}
+
+struct KSum {  // compensated float sum of a 3-vector
+    float x = 0, y = 0, z = 0, cx = 0, cy = 0, cz = 0;
+    __device__ __forceinline__ void add1(float& s, float& c, float v) {
+        float y_ = v - c;
+        float t = s + y_;
+        c = (t - s) - y_;
+        s = t;
+    }
+    __device__ __forceinline__ void add(float vx, float vy, float vz) {
+        add1(x, cx, vx);
+        add1(y, cy, vy);
+        add1(z, cz, vz);
+    }
+    __device__ __forceinline__ dv3 value() const {
+        return mk3((double)x - (double)cx, (double)y - (double)cy, (double)z - (double)cz);
+    }
+};
+
+struct VPConstF {
+    float inv_four_pi, inv_sqrt2, c15, four_pi_3, two_nu;
+};
+
+__device__ __forceinline__ VPConstF fconst(const VPConst& c) {
+    return VPConstF{(float)c.inv_four_pi, (float)(1.0 / c.sqrt2), (float)c.c15, (float)c.four_pi_3, (float)(2 * c.nu)};
+}
+
+// far node f acting on target t; (dx, dy, dz) = target - expansion centre, d2 = |.|^2.
+// V: symmetrised Gaussian velocity; S: stretching with `this` = the node (acts only when
+// stretch_on); D: diffusion with `this` = the node.
+template <bool V, bool S, bool D>
+__device__ __forceinline__ void far_pair_f(const BHNodeF& f, const TgtF& t, float dx, float dy, float dz, float d2,
+                                           bool stretch_on, const VPConstF& c, KSum& v, KSum& s, KSum& dd) {
+    const float a = 1.5f * f.erad, b = 1.5f * t.r;
+    const float sig = sqrtf(a * a + b * b) * c.inv_sqrt2;
+    const float isig = 1.0f / sig;
+    const float rho = sqrtf(d2) * isig;
+    const float rho2 = rho * rho;
+    const float ex = expf(-0.5f * rho2);
+    const float xi = c.c15 * ex;
+    const float isig3 = isig * isig * isig;
+    float K = 0;
+    if (V || S) {
+        const float G = erff(rho * c.inv_sqrt2) * c.inv_four_pi / rho;
+        K = (G - xi) / rho2;
+    }
+    if (V) {
+        const float k = -K * isig3;  // -(K / sig^3) (d x a_node)
+        v.add(k * (dy * f.az - dz * f.ay), k * (dz * f.ax - dx * f.az), k * (dx * f.ay - dy * f.ax));
+    }
+    if (S && stretch_on) {
+        const float F = (3 * K - xi) / rho2;
+        const float da = dx * f.ax + dy * f.ay + dz * f.az;
+        const float g = F * isig * isig * da;
+        const float mx = K * f.ax - g * dx, my = K * f.ay - g * dy, mz = K * f.az - g * dz;
+        s.add(isig3 * (t.ay * mz - t.az * my), isig3 * (t.az * mx - t.ax * mz), isig3 * (t.ax * my - t.ay * mx));
+    }
+    if (D) {
+        const float vi = c.four_pi_3 * (f.erad * f.erad * f.erad), vj = c.four_pi_3 * (t.r * t.r * t.r);
+        const float k = c.two_nu * isig * isig * (xi / (rho2 * rho));
+        dd.add(k * (vi * t.ax - vj * f.ax), k * (vi * t.ay - vj * f.ay), k * (vi * t.az - vj * f.az));
+    }
+}
+
+// float difference target - node centre
+__device__ __forceinline__ float3 diff_f(const TgtF& t, const BHNodeF& f) {
+    return make_float3((t.hx - f.hx) + (t.lx - f.lx), (t.hy - f.hy) + (t.ly - f.ly), (t.hz - f.hz) + (t.lz - f.lz));
+}
+
+// exact FP64 tests of node i (used inside the margin only)
+__device__ __forceinline__ bool far_exact(const BHNode* __restrict__ nodes, int i, dv3 x, double theta) {
+    return far_field(load_node(nodes, i), x, theta);
+}
+// stretching of node i acts on x: not (|x_exp - x| > 5 erad), as in stretch()
+__device__ __forceinline__ bool cut_exact(const BHNode* __restrict__ nodes, int i, dv3 x) {
+    const BHNode nd = load_node(nodes, i);
+    return !(exact_norm(nd.ex - x.x, nd.ey - x.y, nd.ez - x.z) > __dmul_rn(5.0, nd.erad));
+}
+
+// one traversal with FP32 far nodes for target t; `self` skips the member with the
+// target's index.  Accumulates into v, s, d (FP64).
+template <bool V, bool S, bool D>
+__device__ __forceinline__ void traverse_f32(const BHNode* __restrict__ nodes, const BHNodeF* __restrict__ fn, int nn,
+                                             const BHPart* __restrict__ parts, double theta, const Tgt& t,
+                                             const VPConst& c, dv3& v, dv3& s, dv3& d) {
+    const TgtF tf = split_tgt(t);
+    const VPConstF cf = fconst(c);
+    KSum fv, fs, fd;
+    int i = 1;
+    while (i < nn) {
+        const int4 L = load_links(nodes, i);
+        if (L.w) {
+            for (int32_t k = L.x; k < L.x + L.y; k++) {
+                const Tgt m = load_part_g(parts, k);
+                if (m.idx == t.idx) continue;
+                if (V) v = v + vel_gauss_sym(m, t, c);
+                if (S) s = s + stretch(m, t, c);
+                if (D) d = d + diffusion(m, t, c);
+            }
+            i++;
+            continue;
+        }
+        const BHNodeF f = load_fnode(fn, i);
+        const float3 dl = diff_f(tf, f);
+        const float d2 = dl.x * dl.x + dl.y * dl.y + dl.z * dl.z;
+        bool far;
+        if (d2 > f.far2 * kBandHi)
+            far = true;
+        else if (d2 < f.far2 * kBandLo)
+            far = false;
+        else
+            far = far_exact(nodes, i, t.x, theta);
+        if (!far) {
+            i++;
+            continue;
+        }
+        bool on = false;
+        if (S) {
+            if (d2 < f.cut2 * kBandLo)
+                on = true;
+            else if (d2 > f.cut2 * kBandHi)
+                on = false;
+            else
+                on = cut_exact(nodes, i, t.x);
+        }
+        far_pair_f<V, S, D>(f, tf, dl.x, dl.y, dl.z, d2, on, cf, fv, fs, fd);
+        i = L.z;
+    }
+    if (V) v = v + fv.value();
+    if (S) s = s + fs.value();
+    if (D) d = d + fd.value();
+}
+
 // particleFMM::barnesHutVel(part) / barnesHutStretch / barnesHutDiff for every particle.
 // Thread q handles the particle in slot q (leaf order: neighbouring threads traverse
 // neighbouring paths).  Leaves: `this` = member (node.h:274-276, 307-309, 341-343).
@@ -211,6 +387,41 @@ __global__ void __launch_bounds__(128) k_bh_targets(const BHNode* __restrict__ n
     if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
 }
 
+// k_bh_particles / k_bh_targets with far nodes in FP32 (near field FP64)
+template <bool V, bool S, bool D>
+__global__ void __launch_bounds__(128) k_bh_particles_f32(const BHNode* __restrict__ nodes,
+                                                          const BHNodeF* __restrict__ fn, int nn,
+                                                          const BHPart* __restrict__ parts, int64_t n, double theta,
+                                                          VPConst c, double* __restrict__ vel,
+                                                          double* __restrict__ str, double* __restrict__ dif) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const Tgt t = load_part_g(parts, q);
+    dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
+    traverse_f32<V, S, D>(nodes, fn, nn, parts, theta, t, c, v, s, d);
+    int64_t o = 3 * (int64_t)t.idx;
+    if (V) { vel[o] = v.x; vel[o + 1] = v.y; vel[o + 2] = v.z; }
+    if (S) { str[o] = s.x; str[o + 1] = s.y; str[o + 2] = s.z; }
+    if (D) { dif[o] = d.x; dif[o + 1] = d.y; dif[o + 2] = d.z; }
+}
+
+template <bool V, bool S, bool D>
+__global__ void __launch_bounds__(128) k_bh_targets_f32(const BHNode* __restrict__ nodes,
+                                                        const BHNodeF* __restrict__ fn, int nn,
+                                                        const BHPart* __restrict__ slots, double theta,
+                                                        const BHPart* __restrict__ tgt, int64_t m, VPConst c,
+                                                        double* __restrict__ vel, double* __restrict__ str,
+                                                        double* __restrict__ dif) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    const Tgt t = load_part_g(tgt, q);
+    dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
+    traverse_f32<V, S, D>(nodes, fn, nn, slots, theta, t, c, v, s, d);
+    if (V) { vel[3 * q] = v.x; vel[3 * q + 1] = v.y; vel[3 * q + 2] = v.z; }
+    if (S) { str[3 * q] = s.x; str[3 * q + 1] = s.y; str[3 * q + 2] = s.z; }
+    if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
+}
+
 // slots[q] <- the current state of particle perm[q]
 __global__ void k_refresh_slots(const int64_t* __restrict__ perm, int64_t ns, const double* __restrict__ pos,
                                 const double* __restrict__ str, const double* __restrict__ rad,
@@ -245,6 +456,54 @@ __global__ void __launch_bounds__(128) k_bh_points(const BHNode* __restrict__ no
             i++;
         }
     }
+    vel[3 * q] = v.x;
+    vel[3 * q + 1] = v.y;
+    vel[3 * q + 2] = v.z;
+}
+
+// k_bh_points with far nodes in FP32 (algebraic core; leaves FP64)
+__global__ void __launch_bounds__(128) k_bh_points_f32(const BHNode* __restrict__ nodes,
+                                                       const BHNodeF* __restrict__ fn, int nn,
+                                                       const BHPart* __restrict__ parts, double theta,
+                                                       const double* __restrict__ pts, int64_t m, VPConst c,
+                                                       double* __restrict__ vel) {
+    int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (q >= m) return;
+    const dv3 x = ld3(pts + 3 * q);
+    const Tgt t{x, 0.0, mk3(0, 0, 0), -1.0};
+    const TgtF tf = split_tgt(t);
+    const float i4p = (float)c.inv_four_pi;
+    dv3 v = mk3(0, 0, 0);
+    KSum fv;
+    int i = 1;
+    while (i < nn) {
+        const int4 L = load_links(nodes, i);
+        if (L.w) {
+            for (int32_t k = L.x; k < L.x + L.y; k++) v = v + vel_alg(load_part_g(parts, k), x, c);
+            i++;
+            continue;
+        }
+        const BHNodeF f = load_fnode(fn, i);
+        const float3 dl = diff_f(tf, f);
+        const float d2 = dl.x * dl.x + dl.y * dl.y + dl.z * dl.z;
+        bool far;
+        if (d2 > f.far2 * kBandHi)
+            far = true;
+        else if (d2 < f.far2 * kBandLo)
+            far = false;
+        else
+            far = far_exact(nodes, i, x, theta);
+        if (!far) {
+            i++;
+            continue;
+        }
+        const float sg = 1.5f * f.erad, sg2 = sg * sg;
+        const float qq = d2 + sg2;
+        const float k = -i4p * (d2 + 2.5f * sg2) / (qq * qq * sqrtf(qq));
+        fv.add(k * (dl.y * f.az - dl.z * f.ay), k * (dl.z * f.ax - dl.x * f.az), k * (dl.x * f.ay - dl.y * f.ax));
+        i = L.z;
+    }
+    v = v + fv.value();
     vel[3 * q] = v.x;
     vel[3 * q + 1] = v.y;
     vel[3 * q + 2] = v.z;
@@ -306,11 +565,28 @@ unsigned blocks(int64_t m, int t) { return (unsigned)((m + t - 1) / t); }
 
 }  // namespace
 
-cudaError_t launch_bh_particles(const BHNode* nodes, int nn, const BHPart* parts, int64_t n, double theta,
-                                const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s) {
+cudaError_t launch_bh_particles(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, int64_t n,
+                                double theta, const VPConst& c, double* vel, double* str, double* dif,
+                                cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     int mask = (vel ? 1 : 0) | (str ? 2 : 0) | (dif ? 4 : 0);
     dim3 g(blocks(n, 128)), b(128);
+    if (fnodes) {
+#define CPG_BHF(V_, S_, D_) \
+    k_bh_particles_f32<V_, S_, D_><<<g, b, 0, s>>>(nodes, fnodes, nn, parts, n, theta, c, vel, str, dif)
+        switch (mask) {
+            case 1: CPG_BHF(true, false, false); break;
+            case 2: CPG_BHF(false, true, false); break;
+            case 3: CPG_BHF(true, true, false); break;
+            case 4: CPG_BHF(false, false, true); break;
+            case 5: CPG_BHF(true, false, true); break;
+            case 6: CPG_BHF(false, true, true); break;
+            case 7: CPG_BHF(true, true, true); break;
+            default: return cudaSuccess;
+        }
+#undef CPG_BHF
+        return cudaGetLastError();
+    }
     switch (mask) {
         case 1: k_bh_particles<true, false, false><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
         case 2: k_bh_particles<false, true, false><<<g, b, 0, s>>>(nodes, nn, parts, n, theta, c, vel, str, dif); break;
@@ -324,11 +600,21 @@ cudaError_t launch_bh_particles(const BHNode* nodes, int nn, const BHPart* parts
     return cudaGetLastError();
 }
 
-cudaError_t launch_bh_targets(const BHNode* nodes, int nn, const BHPart* slots, double theta, const BHPart* tgt,
-                              int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s) {
+cudaError_t launch_bh_targets(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* slots, double theta,
+                              const BHPart* tgt, int64_t m, const VPConst& c, double* vel, double* str, double* dif,
+                              cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
     int mask = (vel ? 1 : 0) | (str ? 2 : 0) | (dif ? 4 : 0);
     dim3 g(blocks(m, 128)), b(128);
+    if (fnodes) {
+        switch (mask) {
+            case 1: k_bh_targets_f32<true, false, false><<<g, b, 0, s>>>(nodes, fnodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
+            case 6: k_bh_targets_f32<false, true, true><<<g, b, 0, s>>>(nodes, fnodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
+            case 7: k_bh_targets_f32<true, true, true><<<g, b, 0, s>>>(nodes, fnodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
+            default: return cudaErrorInvalidValue;
+        }
+        return cudaGetLastError();
+    }
     switch (mask) {
         case 1: k_bh_targets<true, false, false><<<g, b, 0, s>>>(nodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
         case 6: k_bh_targets<false, true, true><<<g, b, 0, s>>>(nodes, nn, slots, theta, tgt, m, c, vel, str, dif); break;
@@ -345,10 +631,13 @@ cudaError_t launch_refresh_slots(const int64_t* perm, int64_t ns, const double* 
     return cudaGetLastError();
 }
 
-cudaError_t launch_bh_points(const BHNode* nodes, int nn, const BHPart* parts, double theta, const double* pts,
-                             int64_t m, const VPConst& c, double* vel, cudaStream_t s) {
+cudaError_t launch_bh_points(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, double theta,
+                             const double* pts, int64_t m, const VPConst& c, double* vel, cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
-    k_bh_points<<<blocks(m, 128), 128, 0, s>>>(nodes, nn, parts, theta, pts, m, c, vel);
+    if (fnodes)
+        k_bh_points_f32<<<blocks(m, 128), 128, 0, s>>>(nodes, fnodes, nn, parts, theta, pts, m, c, vel);
+    else
+        k_bh_points<<<blocks(m, 128), 128, 0, s>>>(nodes, nn, parts, theta, pts, m, c, vel);
     return cudaGetLastError();
 }
 

@@ -16,17 +16,21 @@ VPConst vp_constants();
 
 cudaError_t launch_pack_parts(const double* pos, const double* str, const double* rad, int64_t n, BHPart* out,
                               cudaStream_t s);
+// Barnes-Hut traversals.  fnodes (the tree's BHNodeF view on the device) selects far
+// nodes in FP32 with the near field in FP64; null: everything in FP64.
 // any of vel/str/dif may be null; outputs indexed by original particle index
-cudaError_t launch_bh_particles(const BHNode* nodes, int nn, const BHPart* parts, int64_t n, double theta,
-                                const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s);
+cudaError_t launch_bh_particles(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, int64_t n,
+                                double theta, const VPConst& c, double* vel, double* str, double* dif,
+                                cudaStream_t s);
 // traversal for explicit targets (original order; outputs by target position); vel / str+dif / all
-cudaError_t launch_bh_targets(const BHNode* nodes, int nn, const BHPart* slots, double theta, const BHPart* tgt,
-                              int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s);
+cudaError_t launch_bh_targets(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* slots, double theta,
+                              const BHPart* tgt, int64_t m, const VPConst& c, double* vel, double* str, double* dif,
+                              cudaStream_t s);
 // slots[q] <- current state of particle perm[q]
 cudaError_t launch_refresh_slots(const int64_t* perm, int64_t ns, const double* pos, const double* str,
                                  const double* rad, BHPart* slots, cudaStream_t s);
-cudaError_t launch_bh_points(const BHNode* nodes, int nn, const BHPart* parts, double theta, const double* pts,
-                             int64_t m, const VPConst& c, double* vel, cudaStream_t s);
+cudaError_t launch_bh_points(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, double theta,
+                             const double* pts, int64_t m, const VPConst& c, double* vel, cudaStream_t s);
 // vk: 0 none, 1 symmetrised Gaussian (particle targets), 2 Gaussian at points, 3 algebraic
 cudaError_t launch_direct(int vk, bool S, bool D, const BHPart* src, int64_t n, const BHPart* tgt, const double* pts,
                           int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s);

@@ -1,4 +1,5 @@
-// Request loop (include/cpanel_serve.h): a pool of slots, each with its own context,
+// Request loop (include/cpanel_serve.h): steady and unsteady (vortex-particle) requests
+// on a pool of slots, each with its own context,
 // taking queued requests in arrival order whenever a slot is idle and the request fits
 // in the free memory budget (a later, smaller request may start ahead of an earlier one
 // that does not fit yet).
@@ -17,6 +18,8 @@
 
 #include "../../include/cpanel_gpu.h"
 #include "../../include/cpanel_serve.h"
+#include "../../include/cpanel_vp.h"
+#include "vpgeom.h"
 
 namespace {
 
@@ -37,6 +40,12 @@ struct Request {
     int status = CPG_OK;
     std::string message;
     std::vector<double> cp, CL, CDi;
+    // unsteady request
+    bool vp = false;
+    cpg_vp_params vprm{};
+    int nsteps = 0;
+    cpg_vp_result vres{};
+    std::vector<double> mu;
 };
 
 double ms(Clock::time_point a, Clock::time_point b) {
@@ -88,6 +97,26 @@ void run_request(cpg_ctx* ctx, int precision, Request& r) {
     if (g) cpg_geometry_destroy(g);
 }
 
+void run_request_vp(cpg_ctx* ctx, Request& r) {
+    cpg_vpcase* c = nullptr;
+    int rc = cpg_vpcase_create(ctx, r.nodes.data(), (int64_t)r.nodes.size() / 3, r.tris.data(), r.ids.data(),
+                               (int64_t)r.ids.size(), &r.vprm, &c);
+    if (rc == CPG_OK) rc = cpg_vpcase_step(c, r.nsteps);
+    if (rc == CPG_OK) rc = cpg_vpcase_trefftz(c, &r.vres.CL, &r.vres.CD, &r.vres.converged);
+    if (rc == CPG_OK) {
+        cpg_vp_info vi;
+        cpg_vpcase_info_get(c, &vi);
+        r.vres.steps = vi.timestep;
+        r.vres.n_particles = vi.n_particles;
+        r.n_body = vi.n_body;
+        r.mu.assign(vi.n_body, 0.0);
+        rc = cpg_vpcase_strengths(c, nullptr, r.mu.data(), nullptr, nullptr);
+    }
+    if (rc != CPG_OK) r.message = cpg_last_error(ctx);
+    r.status = rc;
+    if (c) cpg_vpcase_destroy(c);
+}
+
 void worker(cpg_server* S) {
     cpg_ctx* ctx = nullptr;
     int rc = cpg_create(&ctx, S->p.device);
@@ -119,7 +148,10 @@ void worker(cpg_server* S) {
             r->running_at_start = S->running;
             r->t_start = Clock::now();
         }
-        run_request(ctx, S->p.precision, *r);
+        if (r->vp)
+            run_request_vp(ctx, *r);
+        else
+            run_request(ctx, S->p.precision, *r);
         {
             std::lock_guard<std::mutex> lk(S->mu);
             r->t_done = Clock::now();
@@ -135,6 +167,33 @@ void worker(cpg_server* S) {
 
 }  // namespace
 
+namespace {
+// blocks until request `ticket` is done and takes it out of the table
+std::shared_ptr<Request> take_done(cpg_server* S, int64_t ticket) {
+    std::unique_lock<std::mutex> lk(S->mu);
+    auto it = S->all.find(ticket);
+    if (it == S->all.end()) return nullptr;
+    std::shared_ptr<Request> r = it->second;
+    S->cv_done.wait(lk, [&] { return r->done || S->stop; });
+    if (!r->done) return nullptr;
+    S->all.erase(ticket);
+    return r;
+}
+
+void fill_info(const Request& r, cpg_request_info* info) {
+    if (!info) return;
+    info->status = r.status;
+    info->n_body = r.n_body;
+    info->k = (int)r.flows.size();
+    info->footprint_bytes = r.footprint;
+    info->queue_ms = ms(r.t_submit, r.t_start);
+    info->run_ms = ms(r.t_start, r.t_done);
+    info->total_ms = ms(r.t_submit, r.t_done);
+    info->running_at_start = r.running_at_start;
+    std::snprintf(info->message, sizeof(info->message), "%s", r.message.c_str());
+}
+}  // namespace
+
 extern "C" {
 
 int64_t cpg_server_footprint(int64_t n, int k, int precision) {
@@ -143,6 +202,16 @@ int64_t cpg_server_footprint(int64_t n, int k, int precision) {
     const int64_t nn = n * n;
     int64_t mats = precision == CPG_PLAIN_FP64 ? 16 * nn : 12 * nn + (int64_t)n * 128 * 4 + ((int64_t)256 << 20);
     return mats + (int64_t)n * (int64_t)(2000 + 64 * k) + ((int64_t)64 << 20);
+}
+
+int64_t cpg_server_footprint_vp(int64_t n, int64_t n2, int nsteps, int precision) {
+    // A and B (FP64), C; for CPG_MIXED the float pair of A, its LU and the LU's staging;
+    // per particle its state, tree slot, step scratch and the panel kernels' partial sums
+    const int64_t nn = n * n;
+    int64_t mats = 16 * nn + 8 * n * n2;
+    if (precision == CPG_MIXED) mats += 12 * nn + n * 128 * 4 + ((int64_t)256 << 20);
+    const int64_t np = n2 * (int64_t)(nsteps > 0 ? nsteps : 0);
+    return mats + n * 4000 + np * 4096 + ((int64_t)64 << 20);
 }
 
 int cpg_server_create(const cpg_server_params* p, cpg_server** out) {
@@ -205,32 +274,65 @@ int cpg_server_submit(cpg_server* S, const double* nodes, int64_t n_nodes, const
     return CPG_OK;
 }
 
+int cpg_server_submit_vp(cpg_server* S, const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
+                         int64_t n_tris, const cpg_vp_params* prm, int nsteps, int64_t* ticket) {
+    if (!S || !nodes || !tris || !ids || !prm || !ticket || n_nodes <= 0 || n_tris <= 0 || nsteps < 0)
+        return CPG_E_INVALID;
+    // the buffer wake's size sets the particle count: build it on the host now (this also
+    // rejects a mesh the case cannot take before it is queued)
+    cpg::VPGeom G;
+    if (!cpg::build_vp_geometry(nodes, n_nodes, tris, ids, n_tris, prm->V, prm->dt, G).empty()) return CPG_E_BAD_MESH;
+    auto r = std::make_shared<Request>();
+    r->vp = true;
+    r->nodes.assign(nodes, nodes + 3 * n_nodes);
+    r->tris.assign(tris, tris + 3 * n_tris);
+    r->ids.assign(ids, ids + n_tris);
+    r->vprm = *prm;
+    r->nsteps = nsteps;
+    r->n_body = G.n_body;
+    r->footprint = cpg_server_footprint_vp(G.n_body, G.n_w2, nsteps, prm->precision);
+    if ((double)r->footprint > S->p.budget_bytes) return CPG_E_OOM;
+    r->t_submit = Clock::now();
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        r->id = S->next_id++;
+        S->all[r->id] = r;
+        S->queue.push_back(r);
+        *ticket = r->id;
+    }
+    S->cv_work.notify_one();
+    return CPG_OK;
+}
+
+
+int cpg_server_wait_vp(cpg_server* S, int64_t ticket, cpg_vp_result* res, double* mu, cpg_request_info* info) {
+    if (!S) return CPG_E_INVALID;
+    {
+        std::lock_guard<std::mutex> lk(S->mu);
+        auto it = S->all.find(ticket);
+        if (it == S->all.end() || !it->second->vp) return CPG_E_INVALID;
+    }
+    std::shared_ptr<Request> r = take_done(S, ticket);
+    if (!r) return CPG_E_INVALID;
+    if (res) *res = r->vres;
+    if (mu && !r->mu.empty()) std::memcpy(mu, r->mu.data(), sizeof(double) * r->mu.size());
+    fill_info(*r, info);
+    return r->status;
+}
+
 int cpg_server_wait(cpg_server* S, int64_t ticket, double* cp, double* CL, double* CDi, cpg_request_info* info) {
     if (!S) return CPG_E_INVALID;
-    std::shared_ptr<Request> r;
     {
-        std::unique_lock<std::mutex> lk(S->mu);
+        std::lock_guard<std::mutex> lk(S->mu);
         auto it = S->all.find(ticket);
-        if (it == S->all.end()) return CPG_E_INVALID;
-        r = it->second;
-        S->cv_done.wait(lk, [&] { return r->done || S->stop; });
-        if (!r->done) return CPG_E_INVALID;
-        S->all.erase(ticket);
+        if (it == S->all.end() || it->second->vp) return CPG_E_INVALID;
     }
+    std::shared_ptr<Request> r = take_done(S, ticket);
+    if (!r) return CPG_E_INVALID;
     if (cp && !r->cp.empty()) std::memcpy(cp, r->cp.data(), sizeof(double) * r->cp.size());
     if (CL && !r->CL.empty()) std::memcpy(CL, r->CL.data(), sizeof(double) * r->CL.size());
     if (CDi && !r->CDi.empty()) std::memcpy(CDi, r->CDi.data(), sizeof(double) * r->CDi.size());
-    if (info) {
-        info->status = r->status;
-        info->n_body = r->n_body;
-        info->k = (int)r->flows.size();
-        info->footprint_bytes = r->footprint;
-        info->queue_ms = ms(r->t_submit, r->t_start);
-        info->run_ms = ms(r->t_start, r->t_done);
-        info->total_ms = ms(r->t_submit, r->t_done);
-        info->running_at_start = r->running_at_start;
-        std::snprintf(info->message, sizeof(info->message), "%s", r->message.c_str());
-    }
+    fill_info(*r, info);
     return r->status;
 }
 

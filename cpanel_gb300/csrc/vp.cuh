@@ -170,12 +170,14 @@ __device__ bool hull_is_nodes(const dv3* pts, int np) {
 }
 
 // panel::onPanelCheck / inPanelProjection, CPanel/panel.cpp:113-153 (np vertices at v)
+// The height test is taken first: the hull is only built when it can matter.
 __device__ __forceinline__ bool on_panel_check(const double* v, int np, dv3 c, dv3 n, dv3 l, dv3 m, double longSide,
                                                dv3 poi) {
     dv3 pts[5];
-    for (int i = 0; i < np; i++) pts[i] = to_local(c, l, m, n, ld3(v + 3 * i));
     pts[np] = to_local(c, l, m, n, poi);
-    return hull_is_nodes(pts, np) && (pts[np].z < 0.05 * longSide);
+    if (!(pts[np].z < 0.05 * longSide)) return false;
+    for (int i = 0; i < np; i++) pts[i] = to_local(c, l, m, n, ld3(v + 3 * i));
+    return hull_is_nodes(pts, np);
 }
 
 // panel::nearFilamentCheck, CPanel/panel.cpp:939-966

@@ -5,6 +5,14 @@
 // device; the host keeps the shedding bookkeeping, builds the octree after the strength
 // update (as the reference does) and solves the small sequential pieces of the shedding.
 //
+// Precision: CPG_PLAIN_FP64 is the reference method in FP64.  CPG_MIXED evaluates far
+// particle nodes and far panels in FP32 (the near field -- leaf members, panels within
+// five lengths -- stays FP64, and every near/far decision equals the FP64 one) and
+// replaces the per-step BiCGSTAB by the FP32 LU of A (factored once; A does not change)
+// refined against the FP64 matrix, held as a float pair, to a relative residual of
+// 1e-12, falling back to BiCGSTAB for a step whose refinement stalls.  The shedding
+// and its bookkeeping are the same in both.
+//
 // Per step (timestep >= 3):
 //   convectParticles   particle term (Barnes-Hut on the previous step's tree, or direct
 //                      Gaussian sums) + panel/filament term, AB2 (k_vp_convect);
@@ -24,6 +32,8 @@
 #include <string>
 #include <vector>
 
+#include <cublas_v2.h>
+
 #include "../../include/cpanel_gpu.h"
 #include "../../include/cpanel_vp.h"
 #include "assemble.h"
@@ -32,6 +42,15 @@
 #include "particles.h"
 #include "vpgeom.h"
 #include "vpkern.h"
+
+namespace cpg {
+// context accessors (api.cpp): last error message, stream, cuBLAS handle (created on
+// first use; null if that fails)
+void ctx_set_error(cpg_ctx* ctx, const std::string& msg);
+cudaStream_t ctx_stream(cpg_ctx* ctx);
+void* ctx_blas(cpg_ctx* ctx);
+int ctx_particle_precision(cpg_ctx* ctx);
+}  // namespace cpg
 
 namespace {
 
@@ -126,6 +145,13 @@ struct cpg_vpcase {
     double Sref = 1, PG = 1;
     double CLt = 0, CDt = 0;
     bool converged = false;
+    // mixed precision: FP32 far fields, LU-refined solve
+    int precision = CPG_PLAIN_FP64;
+    Buf fnodes, A32, Alo, LU, bad;
+    cpg::LuGraphs lug;
+    int64_t fallbacks = 0;  // steps whose refinement stalled and that BiCGSTAB solved
+    bool mixed() const { return precision == CPG_MIXED; }
+    const cpg::BHNodeF* fn() const { return mixed() ? fnodes.as<cpg::BHNodeF>() : nullptr; }
 };
 
 namespace {
@@ -161,7 +187,7 @@ cudaError_t particle_term_points(cpg_vpcase& S, bool bh, const double* pts, int6
         if (nn <= 1) return cudaMemsetAsync(out, 0, sizeof(double) * 3 * m, S.s);
         cudaError_t e = refresh_slots(S);
         if (e != cudaSuccess) return e;
-        return cpg::launch_bh_points(S.tnodes.as<cpg::BHNode>(), nn, S.tslots.as<cpg::BHPart>(), S.T.theta, pts, m,
+        return cpg::launch_bh_points(S.tnodes.as<cpg::BHNode>(), S.fn(), nn, S.tslots.as<cpg::BHPart>(), S.T.theta, pts, m,
                                      cpg::vp_constants(), out, S.s);
     }
     if (nsrc <= 0) return cudaMemsetAsync(out, 0, sizeof(double) * 3 * m, S.s);
@@ -181,6 +207,8 @@ cudaError_t ensure_particles(cpg_vpcase& S, int64_t cap) {
     return cudaSuccess;
 }
 
+constexpr double kVPRefineTol = 1e-12;
+
 // solveMatrixEq / solveVPmatrixEq, CPanel/cpCaseVP.cpp:231-301
 cudaError_t solve(cpg_vpcase& S, bool with_c) {
     cudaError_t e = cpg::gemm_fp64_nk(S.B.as<double>(), S.n, 1, S.sigma.as<double>(), S.rhs.as<double>(), -1.0,
@@ -190,10 +218,22 @@ cudaError_t solve(cpg_vpcase& S, bool with_c) {
                       cudaSuccess)
         return e;
     cpg::SolveStats st;
-    e = cpg::solve_fp64(S.A.as<double>(), S.n, 1, S.rhs.as<double>(), S.mu.as<double>(), S.work.p,
-                        2.220446049250313e-16, 2 * S.n, &st, S.s);
-    if (e != cudaSuccess) return e;
-    S.last_iters = st.iters_max;
+    bool done = false;
+    if (S.mixed()) {
+        e = cpg::solve_lu_refined(cpg::ctx_blas(S.ctx), &S.lug, S.A32.as<float>(), S.Alo.as<float>(), S.LU.as<float>(),
+                                  S.n, 1, S.rhs.as<double>(), S.mu.as<double>(), S.work.p, kVPRefineTol, 8, &st, S.s);
+        if (e != cudaSuccess) return e;
+        done = st.residual_max <= kVPRefineTol;
+        S.last_iters = st.refinements;
+        if (!done) S.fallbacks++;
+    }
+    if (!done) {
+        st = cpg::SolveStats();
+        e = cpg::solve_fp64(S.A.as<double>(), S.n, 1, S.rhs.as<double>(), S.mu.as<double>(), S.work.p,
+                            2.220446049250313e-16, 2 * S.n, &st, S.s);
+        if (e != cudaSuccess) return e;
+        S.last_iters = st.iters_max;
+    }
     return cpg::vp_launch_wake_mu(S.mu.as<double>(), S.widx.as<int32_t>(), S.wcoef.as<double>(), S.n1,
                                   S.mu1.as<double>(), S.prev1.as<double>(), with_c ? 1 : 0, S.s);
 }
@@ -392,6 +432,7 @@ cudaError_t build_tree(cpg_vpcase& S) {
     }
     cpg::build_particle_tree(hp.data(), hs.data(), hr.data(), S.np, 10, 0.5, S.T);
     if ((e = up(S.tnodes, S.T.nodes, S.s)) != cudaSuccess) return e;
+    if ((e = up(S.fnodes, S.T.fnodes, S.s)) != cudaSuccess) return e;
     if ((e = up(S.tperm, S.T.perm, S.s)) != cudaSuccess) return e;
     if ((e = S.tslots.ensure(sizeof(cpg::BHPart) * std::max<int64_t>(1, S.np), S.s)) != cudaSuccess) return e;
     S.tree_built = true;
@@ -590,7 +631,7 @@ cudaError_t step_once(cpg_vpcase& S) {
         const int64_t m = S.np;
         if (S.accelerate && S.timestep > 2 && S.tree_built && S.T.nodes.size() > 1) {
             if ((e = refresh_slots(S)) != cudaSuccess) return e;
-            if ((e = cpg::launch_bh_targets(S.tnodes.as<cpg::BHNode>(), (int)S.T.nodes.size(),
+            if ((e = cpg::launch_bh_targets(S.tnodes.as<cpg::BHNode>(), S.fn(), (int)S.T.nodes.size(),
                                             S.tslots.as<cpg::BHPart>(), S.T.theta, S.packed.as<cpg::BHPart>(), m, c,
                                             S.tP.as<double>(), nullptr, nullptr, S.s)) != cudaSuccess)
                 return e;
@@ -606,7 +647,7 @@ cudaError_t step_once(cpg_vpcase& S) {
                                           S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.q2.as<double>(),
                                           S.mu2.as<double>(), S.n2, S.fil.as<double>(), S.have_fil ? S.n2 : 0,
                                           S.pos.as<double>(), m, 12 * S.cref, S.tQ.as<double>(), S.scr.as<double>(),
-                                          S.s)) != cudaSuccess)
+                                          S.s, S.mixed())) != cudaSuccess)
             return e;
         if ((e = cpg::vp_launch_convect(S.pos.as<double>(), S.pvel.as<double>(), S.tP.as<double>(), S.tQ.as<double>(), m,
                                         vinf, S.cref, S.dt, S.s)) != cudaSuccess)
@@ -626,7 +667,7 @@ cudaError_t step_once(cpg_vpcase& S) {
         bool bh = S.accelerate && S.timestep > 3 && S.tree_built;
         if (bh && S.T.nodes.size() > 1) {
             if ((e = refresh_slots(S)) != cudaSuccess) return e;
-            if ((e = cpg::launch_bh_targets(S.tnodes.as<cpg::BHNode>(), (int)S.T.nodes.size(),
+            if ((e = cpg::launch_bh_targets(S.tnodes.as<cpg::BHNode>(), S.fn(), (int)S.T.nodes.size(),
                                             S.tslots.as<cpg::BHPart>(), S.T.theta, S.packed.as<cpg::BHPart>(), m, c,
                                             nullptr, S.tS.as<double>(), S.tD.as<double>(), S.s)) != cudaSuccess)
                 return e;
@@ -642,7 +683,7 @@ cudaError_t step_once(cpg_vpcase& S) {
         if ((e = cpg::vp_launch_stretch_panels(S.rec.as<double>(), S.sigma.as<double>(), S.mu.as<double>(), S.n,
                                                S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.pos.as<double>(),
                                                S.str.as<double>(), m, 12 * S.cref, S.tPan.as<double>(),
-                                               S.scr.as<double>(), S.s)) != cudaSuccess)
+                                               S.scr.as<double>(), S.s, S.mixed())) != cudaSuccess)
             return e;
         if ((e = cpg::vp_launch_strength(S.pos.as<double>(), S.str.as<double>(), S.pstr.as<double>(), S.tS.as<double>(),
                                          S.tD.as<double>(), S.tPan.as<double>(), m, S.cref, S.dt, S.s)) != cudaSuccess)
@@ -676,18 +717,13 @@ cudaError_t step_once(cpg_vpcase& S) {
 
 }  // namespace
 
-namespace cpg {
-// set the context's last error message (api.cpp)
-void ctx_set_error(cpg_ctx* ctx, const std::string& msg);
-cudaStream_t ctx_stream(cpg_ctx* ctx);
-}  // namespace cpg
-
 extern "C" {
 
 int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
                       int64_t n_tris, const cpg_vp_params* prm, cpg_vpcase** out) {
     if (!ctx || !out || !prm || !nodes || !tris || !ids || n_nodes <= 0 || n_tris <= 0 || !(prm->V > 0) ||
-        !(prm->Sref > 0) || !(std::abs(prm->mach) < 1)) {
+        !(prm->Sref > 0) || !(std::abs(prm->mach) < 1) ||
+        (prm->precision != CPG_PLAIN_FP64 && prm->precision != CPG_MIXED)) {
         if (ctx) cpg::ctx_set_error(ctx, "bad argument");
         return CPG_E_INVALID;
     }
@@ -709,6 +745,7 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
     S.cref = prm->cref > 0 ? prm->cref : 1.0;
     S.accelerate = prm->accelerate != 0;
     S.Sref = prm->Sref;
+    S.precision = prm->precision;
     S.PG = std::sqrt(1 - std::pow(prm->mach, 2));
     S.dt = S.G.dt;
     wind_to_body(S.V, S.alpha, S.beta, S.vinf);
@@ -733,7 +770,9 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
         if ((e = b->ensure(sizeof(double) * n * n, S.s)) != cudaSuccess) return fail_cuda(e, "alloc matrices");
     if ((e = S.C.ensure(sizeof(double) * std::max<int64_t>(1, n * S.n2), S.s)) != cudaSuccess)
         return fail_cuda(e, "alloc C");
-    if ((e = S.work.ensure(cpg::solve_fp64_work_bytes(n, 1), S.s)) != cudaSuccess) return fail_cuda(e, "alloc work");
+    if ((e = S.work.ensure(std::max(cpg::solve_fp64_work_bytes(n, 1), cpg::solve_lu_work_bytes(n, 1)), S.s)) !=
+        cudaSuccess)
+        return fail_cuda(e, "alloc work");
     Buf* vec[] = {&S.sigma, &S.mu, &S.rhs};
     for (Buf* b : vec)
         if ((e = b->ensure(sizeof(double) * n, S.s)) != cudaSuccess) return fail_cuda(e, "alloc");
@@ -755,6 +794,27 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
         return fail_cuda(e, "wake columns");
     if ((e = cpg::vp_launch_cmat(S.rec.as<double>(), n, S.q2.as<double>(), S.n2, S.C.as<double>(), S.s)) != cudaSuccess)
         return fail_cuda(e, "C matrix");
+    if (S.mixed()) {  // A as a float pair and its FP32 LU, once (A is the same every step)
+        void* blas = cpg::ctx_blas(ctx);
+        if (!blas) {
+            cpg::ctx_set_error(ctx, "cublasCreate failed");
+            cpg_vpcase_destroy(Sp);
+            return CPG_E_CUDA;
+        }
+        const size_t nn = (size_t)n * n;
+        Buf* f32[] = {&S.A32, &S.Alo, &S.LU};
+        for (Buf* b : f32)
+            if ((e = b->ensure(sizeof(float) * nn, S.s)) != cudaSuccess) return fail_cuda(e, "alloc LU");
+        if ((e = S.bad.ensure(sizeof(int), S.s)) != cudaSuccess) return fail_cuda(e, "alloc LU");
+        if ((e = cudaMemsetAsync(S.bad.p, 0, sizeof(int), S.s)) != cudaSuccess) return fail_cuda(e, "LU");
+        if ((e = cpg::vp_launch_split(S.A.as<double>(), (int64_t)nn, S.A32.as<float>(), S.Alo.as<float>(), S.s)) !=
+            cudaSuccess)
+            return fail_cuda(e, "split A");
+        if ((e = cudaMemcpyAsync(S.LU.p, S.A32.p, sizeof(float) * nn, cudaMemcpyDeviceToDevice, S.s)) != cudaSuccess)
+            return fail_cuda(e, "LU");
+        if ((e = cpg::lu_factor_fp32(blas, &S.lug, S.LU.as<float>(), n, S.bad.as<int>(), S.s)) != cudaSuccess)
+            return fail_cuda(e, "LU factorization");
+    }
     if ((e = cudaStreamSynchronize(S.s)) != cudaSuccess) return fail_cuda(e, "assembly");
     *out = Sp;
     return CPG_OK;
@@ -765,8 +825,10 @@ void cpg_vpcase_destroy(cpg_vpcase* S) {
     Buf* all[] = {&S->rec, &S->q1, &S->q2, &S->widx, &S->wcoef, &S->par, &S->A, &S->B, &S->C, &S->work,
                   &S->sigma, &S->mu, &S->mu1, &S->prev1, &S->mu2, &S->prev2, &S->rhs, &S->fil, &S->vcent,
                   &S->pos, &S->str, &S->rad, &S->pvel, &S->pstr, &S->packed, &S->tP, &S->tQ, &S->tS, &S->tD,
-                  &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr};
+                  &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr,
+                  &S->fnodes, &S->A32, &S->Alo, &S->LU, &S->bad};
     for (Buf* b : all) b->release();
+    S->lug.release();
     delete S;
 }
 
@@ -780,6 +842,7 @@ int cpg_vpcase_info_get(const cpg_vpcase* S, cpg_vp_info* o) {
     o->solver_iters = S->last_iters;
     o->dt = S->dt;
     o->n_tree_nodes = (int64_t)S->T.nodes.size();
+    o->solve_fallbacks = S->fallbacks;
     return CPG_OK;
 }
 
@@ -807,6 +870,63 @@ int cpg_vpcase_trefftz(cpg_vpcase* Sp, double* CL, double* CD, int* converged) {
     if (CL) *CL = cl;
     if (CD) *CD = cd;
     if (converged) *converged = Sp->converged ? 1 : 0;
+    return CPG_OK;
+}
+
+int cpg_vpcase_velocities(cpg_vpcase* Sp, int precision, int direct, double* vel) {
+    if (!Sp || (precision != CPG_PLAIN_FP64 && precision != CPG_MIXED)) return CPG_E_INVALID;
+    cpg_vpcase& S = *Sp;
+    const int64_t m = S.np;
+    if (m == 0) return CPG_OK;
+    if (!vel) return CPG_E_INVALID;
+    const bool f32 = precision == CPG_MIXED;
+    const cpg::VPConst c = cpg::vp_constants();
+    cudaError_t e = pack_current(S);
+    // particle term as convectParticles takes it (or the FP64 direct sum)
+    if (e == cudaSuccess) {
+        if (direct)
+            e = cpg::launch_direct(1, false, false, S.packed.as<cpg::BHPart>(), m, S.packed.as<cpg::BHPart>(), nullptr,
+                                   m, c, S.tP.as<double>(), nullptr, nullptr, S.s);
+        else if (S.accelerate && S.tree_built && S.T.nodes.size() > 1) {
+            e = refresh_slots(S);
+            if (e == cudaSuccess)
+                e = cpg::launch_bh_targets(S.tnodes.as<cpg::BHNode>(), f32 ? S.fnodes.as<cpg::BHNodeF>() : nullptr,
+                                           (int)S.T.nodes.size(), S.tslots.as<cpg::BHPart>(), S.T.theta,
+                                           S.packed.as<cpg::BHPart>(), m, c, S.tP.as<double>(), nullptr, nullptr, S.s);
+        } else if (S.accelerate)
+            e = cudaMemsetAsync(S.tP.p, 0, sizeof(double) * 3 * m, S.s);
+        else
+            e = cpg::launch_direct(2, false, false, S.packed.as<cpg::BHPart>(), m, S.packed.as<cpg::BHPart>(), nullptr,
+                                   m, c, S.tP.as<double>(), nullptr, nullptr, S.s);
+    }
+    if (e == cudaSuccess) e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s);
+    if (e == cudaSuccess)
+        e = cpg::vp_launch_panel_vel(S.rec.as<double>(), S.sigma.as<double>(), S.mu.as<double>(), S.n,
+                                     S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.q2.as<double>(),
+                                     S.mu2.as<double>(), S.n2, S.fil.as<double>(), S.have_fil ? S.n2 : 0,
+                                     S.pos.as<double>(), m, 12 * S.cref, S.tQ.as<double>(), S.scr.as<double>(), S.s,
+                                     f32);
+    std::vector<double> hp(3 * m), hq(3 * m), hx(3 * m);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp.data(), S.tP.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, S.s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hq.data(), S.tQ.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, S.s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hx.data(), S.pos.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, S.s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(S.s);
+    if (e != cudaSuccess) {
+        cpg::ctx_set_error(S.ctx, std::string("velocities: ") + cudaGetErrorString(e));
+        return CPG_E_CUDA;
+    }
+    // the sum of k_vp_convect, with its 20 cref / 12 cref cut-offs
+    for (int64_t i = 0; i < m; i++) {
+        const double r = std::sqrt(hx[3 * i] * hx[3 * i] + hx[3 * i + 1] * hx[3 * i + 1] + hx[3 * i + 2] * hx[3 * i + 2]);
+        for (int k = 0; k < 3; k++) {
+            double v = S.vinf[k];
+            if (!(r > 20 * S.cref)) {
+                v = v + hp[3 * i + k];
+                if (!(r > 12 * S.cref)) v = v + hq[3 * i + k];
+            }
+            vel[3 * i + k] = v;
+        }
+    }
     return CPG_OK;
 }
 
@@ -922,7 +1042,8 @@ int cpg_panels_stretching(cpg_ctx* ctx, const double* body_verts, const double* 
     if (e == cudaSuccess) e = up(q, hq, s);
     if (e == cudaSuccess)
         e = cpg::vp_launch_stretch_panels(rec.as<double>(), sigma, mu, nb, q.as<double>(), wake_mu, nw, pos, strength, m,
-                                          0.0, out, scr.as<double>(), s);
+                                          0.0, out, scr.as<double>(), s,
+                                          cpg::ctx_particle_precision(ctx) == CPG_MIXED);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     rec.release();
     q.release();

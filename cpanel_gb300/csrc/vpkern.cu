@@ -1,6 +1,6 @@
 // Kernels of the vortex-particle case that involve panels: buffer-wake assembly
 // columns, the C matrix, panel and filament velocity at points, panel-to-particle
-// stretching, and the per-step updates.  Compiled with --fmad=false so that every
+// stretching (FP64, or with the far field in FP32), and the per-step updates.  Compiled with --fmad=false so that every
 // branch (near/far, on-panel, near-filament, the AB2 start test) and every update
 // rounds as the host's do.
 #include <cuda_runtime.h>
@@ -85,30 +85,51 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part(const double* __restri
     o[2] = acc.z;
 }
 
+__device__ __forceinline__ dv3 warp_sum3(dv3 v) {  // fixed butterfly: deterministic
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+    }
+    return v;
+}
+
+// one warp per point: lanes share the quads and filaments, lane 0 adds the body chunks
+// in order and the warp's sum
 __global__ void k_vp_panel_vel_fin(const double* __restrict__ part, int64_t nchunk, const double* __restrict__ q1,
                                    const double* __restrict__ mu1, int64_t n1, const double* __restrict__ q2,
                                    const double* __restrict__ mu2, int64_t n2, const double* __restrict__ fil,
                                    int64_t nf, const double* __restrict__ pts, int64_t m, double skip_r,
                                    double* __restrict__ out) {
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= m) return;
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= m) return;  // uniform across the warp
     dv3 poi = ld3(pts + 3 * q);
     if (skip_r > 0 && norm3(poi) > skip_r) {
-        out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = 0;
+        if (lane == 0) out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = 0;
         return;
     }
     dv3 acc = mk3(0, 0, 0);
-    for (int64_t c = 0; c < nchunk; c++) acc = acc + ld3(part + (c * m + q) * 3);
-    for (int64_t j = 0; j < n1; j++) acc = acc + mu1[j] * dub_v_inf_q(q1 + j * Q_STRIDE, poi);
-    for (int64_t j = 0; j < n2; j++) acc = acc + mu2[j] * dub_v_inf_q(q2 + j * Q_STRIDE, poi);
-    for (int64_t j = 0; j < nf; j++) {
-        const double* f = fil + 8 * j;
-        dv3 p1 = ld3(f), p2 = ld3(f + 3);
-        acc = acc + (f[6] * vortex_v(poi - p1, poi - p2, p2 - p1)) / CPG_FOUR_PI;
+    for (int64_t j = lane; j < n1 + n2 + nf; j += 32) {
+        if (j < n1) {
+            acc = acc + mu1[j] * dub_v_inf_q(q1 + j * Q_STRIDE, poi);
+        } else if (j < n1 + n2) {
+            acc = acc + mu2[j - n1] * dub_v_inf_q(q2 + (j - n1) * Q_STRIDE, poi);
+        } else {
+            const double* f = fil + 8 * (j - n1 - n2);
+            dv3 p1 = ld3(f), p2 = ld3(f + 3);
+            acc = acc + (f[6] * vortex_v(poi - p1, poi - p2, p2 - p1)) / CPG_FOUR_PI;
+        }
     }
-    out[3 * q] = acc.x;
-    out[3 * q + 1] = acc.y;
-    out[3 * q + 2] = acc.z;
+    acc = warp_sum3(acc);
+    if (lane != 0) return;
+    dv3 tot = mk3(0, 0, 0);
+    for (int64_t c = 0; c < nchunk; c++) tot = tot + ld3(part + (c * m + q) * 3);
+    tot = tot + acc;
+    out[3 * q] = tot.x;
+    out[3 * q + 1] = tot.y;
+    out[3 * q + 2] = tot.z;
 }
 
 // sum over body panels of bodyPanel::partStretching and over first-row panels of
@@ -169,19 +190,238 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part(const double* __restrict
     o[2] = acc.z;
 }
 
+// ---- FP32 far field (the mixed-precision form of the two panel kernels) ----
+// Pairs beyond five panel lengths (the reference's point-source/point-doublet branch)
+// are evaluated in FP32 from a float view of the tile: panel centre split into high
+// and low floats, normal, sigma area / 4 pi, mu area / 4 pi and (5 longSide)^2.  The
+// near/far decision compares the float squared distance with a relative margin of 1e-5
+// and takes the FP64 test inside it, so every pair takes the same branch as in FP64;
+// near pairs run the FP64 code above.  Far terms are summed with compensation in float.
+constexpr float kBandLo = 1.0f - 1e-5f, kBandHi = 1.0f + 1e-5f;
+enum { FT_CH = 0, FT_CL = 3, FT_N = 6, FT_AS = 9, FT_AD = 10, FT_T2 = 11, FT_STRIDE = 12 };
+
+struct KSum3 {
+    float x = 0, y = 0, z = 0, cx = 0, cy = 0, cz = 0;
+    __device__ __forceinline__ static void add1(float& s, float& c, float v) {
+        float y_ = v - c;
+        float t = s + y_;
+        c = (t - s) - y_;
+        s = t;
+    }
+    __device__ __forceinline__ void add(float vx, float vy, float vz) {
+        add1(x, cx, vx);
+        add1(y, cy, vy);
+        add1(z, cz, vz);
+    }
+    __device__ __forceinline__ dv3 value() const {
+        return mk3((double)x - (double)cx, (double)y - (double)cy, (double)z - (double)cz);
+    }
+};
+
+// float view of panel b + k (thread-strided fill of a tile)
+__device__ __forceinline__ void fill_ftile(const double* __restrict__ r, double sigma, double mu, float* __restrict__ f) {
+    const double inv4pi = 1.0 / CPG_FOUR_PI;
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+        const double c = r[R_C + q];
+        const float h = __double2float_rn(c);
+        f[FT_CH + q] = h;
+        f[FT_CL + q] = __double2float_rn(c - (double)h);
+        f[FT_N + q] = __double2float_rn(r[R_N + q]);
+    }
+    f[FT_AS] = __double2float_rn(sigma * r[R_AREA] * inv4pi);
+    f[FT_AD] = __double2float_rn(mu * r[R_AREA] * inv4pi);
+    const double t = 5 * r[R_LONG];
+    f[FT_T2] = __double2float_rn(t * t);
+}
+
+struct PtF {
+    float hx, hy, hz, lx, ly, lz;
+};
+__device__ __forceinline__ PtF split_pt(dv3 p) {
+    PtF f;
+    f.hx = __double2float_rn(p.x);
+    f.hy = __double2float_rn(p.y);
+    f.hz = __double2float_rn(p.z);
+    f.lx = __double2float_rn(p.x - (double)f.hx);
+    f.ly = __double2float_rn(p.y - (double)f.hy);
+    f.lz = __double2float_rn(p.z - (double)f.hz);
+    return f;
+}
+
+// 1: far (point formulas), 0: near; p - centre in (dx, dy, dz), squared norm d2
+__device__ __forceinline__ bool far_pair(const PtF& p, const float* __restrict__ f, const double* __restrict__ r,
+                                         dv3 poi, float& dx, float& dy, float& dz, float& d2) {
+    dx = (p.hx - f[FT_CH]) + (p.lx - f[FT_CL]);
+    dy = (p.hy - f[FT_CH + 1]) + (p.ly - f[FT_CL + 1]);
+    dz = (p.hz - f[FT_CH + 2]) + (p.lz - f[FT_CL + 2]);
+    d2 = dx * dx + dy * dy + dz * dz;
+    const float t2 = f[FT_T2];
+    if (d2 > t2 * kBandHi) return true;
+    if (d2 < t2 * kBandLo) return false;
+    return norm3(poi - ld3(r + R_C)) / r[R_LONG] > 5;  // the FP64 test of panel_v_inf / stretching
+}
+
+__global__ void __launch_bounds__(VT) k_vp_panel_vel_part_f32(const double* __restrict__ rec,
+                                                              const double* __restrict__ sigma,
+                                                              const double* __restrict__ mu, int64_t nb,
+                                                              int64_t chunk, const double* __restrict__ pts,
+                                                              int64_t m, double skip_r, double* __restrict__ part) {
+    __shared__ double tile[TILE * R_STRIDE];
+    __shared__ double ts[TILE], tm[TILE];
+    __shared__ float ft[TILE * FT_STRIDE];
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = q < m;
+    dv3 poi = live ? ld3(pts + 3 * q) : mk3(0, 0, 0);
+    if (live && skip_r > 0 && norm3(poi) > skip_r) live = false;
+    const PtF pf = split_pt(poi);
+    const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
+    dv3 acc = mk3(0, 0, 0);
+    KSum3 fa;
+    for (int64_t b = jb; b < je; b += TILE) {
+        int lim = (int)((je - b) < TILE ? (je - b) : TILE);
+        __syncthreads();
+        for (int k = threadIdx.x; k < lim * R_STRIDE; k += VT) tile[k] = rec[b * R_STRIDE + k];
+        for (int k = threadIdx.x; k < lim; k += VT) {
+            ts[k] = sigma[b + k];
+            tm[k] = mu[b + k];
+            fill_ftile(rec + (b + k) * R_STRIDE, ts[k], tm[k], ft + k * FT_STRIDE);
+        }
+        __syncthreads();
+        if (!live) continue;
+        for (int k = 0; k < lim; k++) {
+            const float* f = ft + k * FT_STRIDE;
+            float dx, dy, dz, d2;
+            if (far_pair(pf, f, tile + k * R_STRIDE, poi, dx, dy, dz, d2)) {
+                // sigma vSrc + mu vDub = (3 ad pn / d^2 - as) / d^3 (p - c) - ad / d^3 n
+                const float inv = rsqrtf(d2), i2 = inv * inv, i3 = i2 * inv;
+                const float nx = f[FT_N], ny = f[FT_N + 1], nz = f[FT_N + 2];
+                const float pn = dx * nx + dy * ny + dz * nz;
+                const float ad = f[FT_AD];
+                const float cp = (3 * ad * pn * i2 - f[FT_AS]) * i3, cn = ad * i3;
+                fa.add(cp * dx - cn * nx, cp * dy - cn * ny, cp * dz - cn * nz);
+            } else {
+                dv3 vs, vd;
+                panel_v_inf(tile + k * R_STRIDE, poi, vs, vd);
+                acc = acc + (ts[k] * vs + tm[k] * vd);
+            }
+        }
+    }
+    if (q >= m) return;
+    acc = acc + fa.value();
+    double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
+    o[0] = acc.x;
+    o[1] = acc.y;
+    o[2] = acc.z;
+}
+
+__global__ void __launch_bounds__(VT) k_vp_stretch_part_f32(const double* __restrict__ rec,
+                                                            const double* __restrict__ sigma,
+                                                            const double* __restrict__ mu, int64_t nb, int64_t chunk,
+                                                            const double* __restrict__ pos,
+                                                            const double* __restrict__ str, int64_t m,
+                                                            double skip_x, double* __restrict__ part) {
+    __shared__ double tile[TILE * R_STRIDE];
+    __shared__ double ts[TILE], tm[TILE];
+    __shared__ float ft[TILE * FT_STRIDE];
+    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = q < m;
+    dv3 x = live ? ld3(pos + 3 * q) : mk3(0, 0, 0);
+    dv3 a = live ? ld3(str + 3 * q) : mk3(0, 0, 0);
+    if (live && skip_x > 0 && fabs(x.x) > skip_x) live = false;
+    const PtF pf = split_pt(x);
+    const float ax = (float)a.x, ay = (float)a.y, az = (float)a.z;
+    const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
+    dv3 acc = mk3(0, 0, 0);
+    KSum3 fa;
+    for (int64_t b = jb; b < je; b += TILE) {
+        int lim = (int)((je - b) < TILE ? (je - b) : TILE);
+        __syncthreads();
+        for (int k = threadIdx.x; k < lim * R_STRIDE; k += VT) tile[k] = rec[b * R_STRIDE + k];
+        for (int k = threadIdx.x; k < lim; k += VT) {
+            ts[k] = sigma[b + k];
+            tm[k] = mu[b + k];
+            fill_ftile(rec + (b + k) * R_STRIDE, ts[k], tm[k], ft + k * FT_STRIDE);
+        }
+        __syncthreads();
+        if (!live) continue;
+        for (int k = 0; k < lim; k++) {
+            const float* f = ft + k * FT_STRIDE;
+            const double* r = tile + k * R_STRIDE;
+            float ddx, ddy, ddz, d2;
+            if (far_pair(pf, f, r, x, ddx, ddy, ddz, d2)) {
+                // velocityGradientPointSource + velocityGradientPointDoublet in FP32, with
+                // the reference's terms: dx = c.x - x, dy = c.y - y, z = c.z, z - z0 = c.z - x.z
+                const float dx = -ddx, dy = -ddy, zz = -ddz;
+                const float z = f[FT_CH + 2] + f[FT_CL + 2];
+                const float dx2 = dx * dx, dy2 = dy * dy, z2 = z * z;
+                const float bb = dx2 + dy2 + z2;
+                const float sb = sqrtf(bb);
+                const float is = f[FT_AS] / (bb * bb * sb);          // sigma area / 4 pi / sdd
+                const float id = 1.0f / (bb * bb * bb * sb);          // 1 / ddd
+                const float uv = 3 * f[FT_AD] * id, w = -f[FT_AD] * id;
+                const float e = dx2 + dy2 - 4 * z2;
+                float G00 = is * (-2 * dx2 + dy2 + z2) + uv * z * (-4 * dx2 + dy2 + z2);
+                float G10 = is * (-3 * dx * dy) + uv * (-5) * z * dy * dx;
+                float G20 = is * (-3 * dx * z) + uv * dx * e;
+                float G01 = is * (-3 * dx * dy) + uv * (-5) * dx * dy * z;
+                float G11 = is * (dx2 - dy2 + z2) + uv * z * (dx2 - 4 * dy2 + z2);
+                float G21 = is * (-3 * z * dy) + uv * dy * e;
+                float G02 = is * (-3 * dx * zz) + w * (-3) * dx * e;
+                float G12 = is * (-3 * dy * zz) + w * (-3) * dy * e;
+                float G22 = is * (-3 * z * zz + bb) + w * (-3) * z * (3 * dx2 + 3 * dy2 - 2 * z2);
+                fa.add(G00 * ax + G01 * ay + G02 * az, G10 * ax + G11 * ay + G12 * az, G20 * ax + G21 * ay + G22 * az);
+            } else {
+                dv3 c = ld3(r + R_C);
+                dm3 g1 = vel_grad_tri_source(r, ts[k], x);
+                dm3 g2 = vel_grad_doublet(r, 3, c, ld3(r + R_N), ld3(r + R_L), ld3(r + R_M), r[R_LONG], tm[k], x);
+                dm3 G;
+#pragma unroll
+                for (int i = 0; i < 3; i++)
+#pragma unroll
+                    for (int j = 0; j < 3; j++) G.a[i][j] = (0 + g1.a[i][j]) + g2.a[i][j];
+                acc = acc + mul_m3(G, a);
+            }
+        }
+    }
+    if (q >= m) return;
+    acc = acc + fa.value();
+    double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
+    o[0] = acc.x;
+    o[1] = acc.y;
+    o[2] = acc.z;
+}
+
+// A = A32 + Alo: the FP64 matrix as a float pair (the mixed-precision solve factors A32
+// and refines against both)
+__global__ void k_vp_split(const double* __restrict__ A, int64_t nn, float* __restrict__ A32, float* __restrict__ Alo) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nn) return;
+    const double a = A[i];
+    const float h = __double2float_rn(a);
+    A32[i] = h;
+    Alo[i] = __double2float_rn(a - (double)h);
+}
+
+__global__ void k_vp_add(double* __restrict__ y, const double* __restrict__ x, int64_t n) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = y[i] + x[i];
+}
+
+// one warp per particle: lanes share the first-row quads (wakePanel::partStretching)
 __global__ void k_vp_stretch_fin(const double* __restrict__ part, int64_t nchunk, const double* __restrict__ q1,
                                  const double* __restrict__ mu1, int64_t n1, const double* __restrict__ pos,
                                  const double* __restrict__ str, int64_t m, double skip_x, double* __restrict__ out) {
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= m) return;
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= m) return;  // uniform across the warp
     dv3 x = ld3(pos + 3 * q), a = ld3(str + 3 * q);
     if (skip_x > 0 && fabs(x.x) > skip_x) {
-        out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = 0;
+        if (lane == 0) out[3 * q] = out[3 * q + 1] = out[3 * q + 2] = 0;
         return;
     }
     dv3 acc = mk3(0, 0, 0);
-    for (int64_t c = 0; c < nchunk; c++) acc = acc + ld3(part + (c * m + q) * 3);
-    for (int64_t j = 0; j < n1; j++) {
+    for (int64_t j = lane; j < n1; j += 32) {
         const double* w = q1 + j * Q_STRIDE;
         dv3 c = ld3(w + Q_C);
         dm3 G = norm3(x - c) / w[Q_LONG] > 5
@@ -189,9 +429,14 @@ __global__ void k_vp_stretch_fin(const double* __restrict__ part, int64_t nchunk
                     : vel_grad_doublet(w, 4, c, ld3(w + Q_N), ld3(w + Q_L), ld3(w + Q_M), w[Q_LONG], mu1[j], x);
         acc = acc + mul_m3(G, a);
     }
-    out[3 * q] = acc.x;
-    out[3 * q + 1] = acc.y;
-    out[3 * q + 2] = acc.z;
+    acc = warp_sum3(acc);
+    if (lane != 0) return;
+    dv3 tot = mk3(0, 0, 0);
+    for (int64_t c = 0; c < nchunk; c++) tot = tot + ld3(part + (c * m + q) * 3);
+    tot = tot + acc;
+    out[3 * q] = tot.x;
+    out[3 * q + 1] = tot.y;
+    out[3 * q + 2] = tot.z;
 }
 
 // Eigen's isZero(): every |component| <= 1e-12
@@ -300,16 +545,31 @@ cudaError_t vp_launch_wake_columns(const double* rec, int64_t n, const double* q
     if (n > 0 && n1 > 0) k_vp_wake_columns<<<nblk(n, VT), VT, 0, s>>>(rec, n, q1, widx, wcoef, n1, A);
     return cudaGetLastError();
 }
+cudaError_t vp_launch_add(double* y, const double* x, int64_t n, cudaStream_t s) {
+    if (n > 0) k_vp_add<<<nblk(n, 256), 256, 0, s>>>(y, x, n);
+    return cudaGetLastError();
+}
+cudaError_t vp_launch_split(const double* A, int64_t nn, float* A32, float* Alo, cudaStream_t s) {
+    if (nn > 0) k_vp_split<<<nblk(nn, 256), 256, 0, s>>>(A, nn, A32, Alo);
+    return cudaGetLastError();
+}
 cudaError_t vp_launch_cmat(const double* rec, int64_t n, const double* q2, int64_t n2, double* C, cudaStream_t s) {
     if (n > 0 && n2 > 0) k_vp_cmat<<<nblk(n * n2, 256), 256, 0, s>>>(rec, n, q2, n2, C);
     return cudaGetLastError();
 }
 // chunks of body panels along grid.y: enough blocks to fill the GPU several times over
+// panel chunks along grid.y: about 4 blocks per SM in all, chunks of at least CHUNK_MIN
+// panels (a handful of points then still spreads over the SMs)
+constexpr int CHUNK_MIN = 16;
 int64_t vp_chunks(int64_t m, int64_t nb) {
     int64_t bx = (m + VT - 1) / VT;
-    int64_t maxc = (nb + TILE - 1) / TILE;
+    int64_t maxc = (nb + CHUNK_MIN - 1) / CHUNK_MIN;
     int64_t c = (4 * 152 + bx - 1) / bx;
     return std::max<int64_t>(1, std::min(c, maxc));
+}
+int64_t vp_chunk_size(int64_t m, int64_t nb) {
+    const int64_t nc = vp_chunks(m, nb);
+    return nb > 0 ? ((nb + nc - 1) / nc + CHUNK_MIN - 1) / CHUNK_MIN * CHUNK_MIN : CHUNK_MIN;
 }
 
 int64_t vp_scratch_doubles(int64_t m, int64_t nb) { return vp_chunks(m, nb) * m * 3; }
@@ -317,30 +577,34 @@ int64_t vp_scratch_doubles(int64_t m, int64_t nb) { return vp_chunks(m, nb) * m 
 cudaError_t vp_launch_panel_vel(const double* rec, const double* sigma, const double* mu, int64_t nb, const double* q1,
                                 const double* mu1, int64_t n1, const double* q2, const double* mu2, int64_t n2,
                                 const double* fil, int64_t nf, const double* pts, int64_t m, double skip_r,
-                                double* out, double* scratch, cudaStream_t s) {
+                                double* out, double* scratch, cudaStream_t s, bool far_f32) {
     if (m <= 0) return cudaSuccess;
-    const int64_t nc = vp_chunks(m, nb);
-    const int64_t chunk = nb > 0 ? ((nb + nc - 1) / nc + TILE - 1) / TILE * TILE : TILE;
+    const int64_t chunk = vp_chunk_size(m, nb);
     const int64_t ncu = nb > 0 ? (nb + chunk - 1) / chunk : 0;
-    if (ncu > 0)
+    if (ncu > 0 && far_f32)
+        k_vp_panel_vel_part_f32<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pts, m,
+                                                                               skip_r, scratch);
+    else if (ncu > 0)
         k_vp_panel_vel_part<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pts, m, skip_r,
                                                                            scratch);
-    k_vp_panel_vel_fin<<<nblk(m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, q2, mu2, n2, fil, nf, pts, m, skip_r,
+    k_vp_panel_vel_fin<<<nblk(32 * m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, q2, mu2, n2, fil, nf, pts, m, skip_r,
                                                     out);
     return cudaGetLastError();
 }
 cudaError_t vp_launch_stretch_panels(const double* rec, const double* sigma, const double* mu, int64_t nb,
                                      const double* q1, const double* mu1, int64_t n1, const double* pos,
                                      const double* str, int64_t m, double skip_x, double* out, double* scratch,
-                                     cudaStream_t s) {
+                                     cudaStream_t s, bool far_f32) {
     if (m <= 0) return cudaSuccess;
-    const int64_t nc = vp_chunks(m, nb);
-    const int64_t chunk = nb > 0 ? ((nb + nc - 1) / nc + TILE - 1) / TILE * TILE : TILE;
+    const int64_t chunk = vp_chunk_size(m, nb);
     const int64_t ncu = nb > 0 ? (nb + chunk - 1) / chunk : 0;
-    if (ncu > 0)
+    if (ncu > 0 && far_f32)
+        k_vp_stretch_part_f32<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pos, str, m,
+                                                                             skip_x, scratch);
+    else if (ncu > 0)
         k_vp_stretch_part<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pos, str, m,
                                                                          skip_x, scratch);
-    k_vp_stretch_fin<<<nblk(m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, pos, str, m, skip_x, out);
+    k_vp_stretch_fin<<<nblk(32 * m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, pos, str, m, skip_x, out);
     return cudaGetLastError();
 }
 cudaError_t vp_launch_convect(double* pos, double* prevVel, const double* part, const double* pan, int64_t m,

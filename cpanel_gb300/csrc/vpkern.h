@@ -10,17 +10,22 @@ namespace cpg {
 
 cudaError_t vp_launch_wake_columns(const double* rec, int64_t n, const double* q1, const int32_t* widx,
                                    const double* wcoef, int64_t n1, double* A, cudaStream_t s);
+// y += x over n doubles
+cudaError_t vp_launch_add(double* y, const double* x, int64_t n, cudaStream_t s);
+// A32 = fl(A), Alo = fl(A - A32) elementwise over nn entries
+cudaError_t vp_launch_split(const double* A, int64_t nn, float* A32, float* Alo, cudaStream_t s);
 cudaError_t vp_launch_cmat(const double* rec, int64_t n, const double* q2, int64_t n2, double* C, cudaStream_t s);
-// scratch of the two panel kernels below: vp_scratch_doubles(m, nb) doubles
+// scratch of the two panel kernels below: vp_scratch_doubles(m, nb) doubles.  far_f32:
+// panel pairs beyond five panel lengths in FP32 (same near/far split as FP64).
 int64_t vp_scratch_doubles(int64_t m, int64_t nb);
 cudaError_t vp_launch_panel_vel(const double* rec, const double* sigma, const double* mu, int64_t nb, const double* q1,
                                 const double* mu1, int64_t n1, const double* q2, const double* mu2, int64_t n2,
                                 const double* fil, int64_t nf, const double* pts, int64_t m, double skip_r,
-                                double* out, double* scratch, cudaStream_t s);
+                                double* out, double* scratch, cudaStream_t s, bool far_f32 = false);
 cudaError_t vp_launch_stretch_panels(const double* rec, const double* sigma, const double* mu, int64_t nb,
                                      const double* q1, const double* mu1, int64_t n1, const double* pos,
                                      const double* str, int64_t m, double skip_x, double* out, double* scratch,
-                                     cudaStream_t s);
+                                     cudaStream_t s, bool far_f32 = false);
 cudaError_t vp_launch_convect(double* pos, double* prevVel, const double* part, const double* pan, int64_t m,
                               const double vinf[3], double cref, double dt, cudaStream_t s);
 cudaError_t vp_launch_strength(const double* pos, double* str, double* prevStr, const double* dstr,

@@ -45,10 +45,14 @@ def _sync():
     torch.cuda.synchronize()
 
 
+def _precision(p):
+    return {"plain": _lib.PLAIN_FP64, "mixed": _lib.MIXED}[p]
+
+
 class ParticleFMM:
     """Barnes-Hut octree over one particle set (fresh build, as the VP loop does every step)."""
 
-    def __init__(self, pos, strength, radius, max_members=10, theta=0.5, ctx=None):
+    def __init__(self, pos, strength, radius, max_members=10, theta=0.5, precision="plain", ctx=None):
         self.ctx = _ctx(ctx)
         self.pos, self.strength, self.radius = _dev(pos, 3), _dev(strength, 3), _dev(radius).reshape(-1)
         self.n = self.pos.shape[0]
@@ -57,6 +61,13 @@ class ParticleFMM:
         self.ctx.check(self.ctx.L.cpg_ptree_build(self.ctx.h, _ptr(self.pos), _ptr(self.strength), _ptr(self.radius),
                                                   self.n, max_members, theta, C.byref(h)), "particle tree")
         self.h = h
+        self.set_precision(precision)
+
+    def set_precision(self, precision):
+        """"plain": every interaction in FP64; "mixed": far nodes in FP32, leaves (the
+        direct near field) in FP64, the same traversal decisions."""
+        code = _precision(precision)
+        self.ctx.check(self.ctx.L.cpg_ptree_set_precision(self.h, code), "tree precision")
 
     def __del__(self):
         h = getattr(self, "h", None)
@@ -161,7 +172,22 @@ def particles_stretch_diff(pos, strength, radius, ctx=None):
     return s, d
 
 
-def panels_velocity(body_verts, sigma, mu, wake_verts, wake_mu, points, ctx=None):
+class _OperatorPrecision:
+    """Sets the context's panel-particle operator precision for one call."""
+
+    def __init__(self, ctx, precision):
+        self.ctx, self.code = ctx, _precision(precision)
+
+    def __enter__(self):
+        self.ctx.check(self.ctx.L.cpg_set_particle_precision(self.ctx.h, self.code), "operator precision")
+
+    def __exit__(self, *a):
+        self.ctx.L.cpg_set_particle_precision(self.ctx.h, _lib.PLAIN_FP64)
+
+
+def panels_velocity(body_verts, sigma, mu, wake_verts, wake_mu, points, precision="plain", ctx=None):
+    """Sum of bodyPanel::panelV (triangles) and wake-triangle dubVInf at points; "mixed"
+    evaluates body pairs beyond five panel lengths in FP32."""
     import torch
     ctx = _ctx(ctx)
     bv = _dev(body_verts, 9)
@@ -172,13 +198,15 @@ def panels_velocity(body_verts, sigma, mu, wake_verts, wake_mu, points, ctx=None
     pts = _dev(points, 3)
     vel = torch.empty_like(pts)
     _sync()
-    ctx.check(ctx.L.cpg_panels_velocity(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm), nw,
-                                        _ptr(pts), pts.shape[0], _ptr(vel)), "panel velocity")
+    with _OperatorPrecision(ctx, precision):
+        ctx.check(ctx.L.cpg_panels_velocity(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm), nw,
+                                            _ptr(pts), pts.shape[0], _ptr(vel)), "panel velocity")
     return vel
 
 
-def panels_stretching(body_verts, sigma, mu, wake_verts, wake_mu, pos, strength, ctx=None):
-    """Sum of bodyPanel::partStretching (triangles) and wakePanel::partStretching (quads)."""
+def panels_stretching(body_verts, sigma, mu, wake_verts, wake_mu, pos, strength, precision="plain", ctx=None):
+    """Sum of bodyPanel::partStretching (triangles) and wakePanel::partStretching (quads);
+    "mixed" evaluates body pairs beyond five panel lengths in FP32."""
     import torch
     ctx = _ctx(ctx)
     bv = _dev(body_verts, 9)
@@ -189,8 +217,9 @@ def panels_stretching(body_verts, sigma, mu, wake_verts, wake_mu, pos, strength,
     p, st = _dev(pos, 3), _dev(strength, 3)
     out = torch.empty_like(p)
     _sync()
-    ctx.check(ctx.L.cpg_panels_stretching(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm), nw,
-                                          _ptr(p), _ptr(st), p.shape[0], _ptr(out)), "panel stretching")
+    with _OperatorPrecision(ctx, precision):
+        ctx.check(ctx.L.cpg_panels_stretching(ctx.h, _ptr(bv), _ptr(sg), _ptr(mu_), bv.shape[0], _ptr(wv), _ptr(wm),
+                                              nw, _ptr(p), _ptr(st), p.shape[0], _ptr(out)), "panel stretching")
     return out
 
 
@@ -219,12 +248,12 @@ class VPCase:
     """cpCaseVP on a body-only mesh, advanced step by step on the GPU."""
 
     def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, Sref=1.0,
-                 mach=0.0, ctx=None):
+                 mach=0.0, precision="plain", ctx=None):
         self.ctx = _ctx(ctx)
         nodes = np.ascontiguousarray(nodes, dtype=np.float64)
         tris = np.ascontiguousarray(tris, dtype=np.int64)
         ids = np.ascontiguousarray(ids, dtype=np.int32)
-        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0, Sref, mach)
+        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0, Sref, mach, _precision(precision))
         h = C.c_void_p()
         self.ctx.check(self.ctx.L.cpg_vpcase_create(self.ctx.h, nodes.ctypes.data_as(_lib.D), len(nodes),
                                                     tris.ctypes.data_as(_lib.I64), ids.ctypes.data_as(_lib.I32),
@@ -252,6 +281,14 @@ class VPCase:
         cl, cd, cv = C.c_double(), C.c_double(), C.c_int()
         self.ctx.check(self.ctx.L.cpg_vpcase_trefftz(self.h, C.byref(cl), C.byref(cd), C.byref(cv)), "trefftz")
         return dict(CL=cl.value, CD=cd.value, converged=bool(cv.value))
+
+    def velocities(self, precision="plain", direct=False):
+        """Convective velocity of every particle at the current state (n x 3)."""
+        n = self.info()["n_particles"]
+        out = np.zeros((n, 3))
+        self.ctx.check(self.ctx.L.cpg_vpcase_velocities(self.h, _precision(precision), 1 if direct else 0,
+                                                        out.ctypes.data_as(_lib.D)), "velocities")
+        return out
 
     def particles(self):
         n = self.info()["n_particles"]

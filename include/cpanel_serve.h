@@ -1,6 +1,7 @@
 /*
- * cpanel_serve.h -- request loop of the GB300 panel path: steady solves of different
- * meshes admitted by device-memory footprint and run concurrently (sm_103a).
+ * cpanel_serve.h -- request loop of the GB300 panel path: steady solves and unsteady
+ * vortex-particle runs of different meshes admitted by device-memory footprint and run
+ * concurrently (sm_103a).
  *
  * No counterpart in the reference, which runs one case at a time from its CLI
  * (CPanel/cpanel.cpp, CPanel/CPanelMgr.cpp:90-167).  Each request is what
@@ -18,6 +19,7 @@
 #include <stdint.h>
 
 #include "cpanel_gpu.h"
+#include "cpanel_vp.h"
 
 #ifdef __cplusplus
 extern "C" {
@@ -35,7 +37,7 @@ typedef struct {
 typedef struct {
     int status;              /* cpg_status of the request                              */
     int64_t n_body;
-    int k;                   /* flow conditions                                        */
+    int k;                   /* flow conditions (unsteady: 0)                          */
     int64_t footprint_bytes; /* admission estimate                                     */
     double queue_ms;         /* submit -> start (host clock)                           */
     double run_ms;           /* start -> done                                          */
@@ -57,6 +59,24 @@ int  cpg_server_submit(cpg_server* s, const double* nodes, int64_t n_nodes, cons
 int  cpg_server_wait(cpg_server* s, int64_t ticket, double* cp, double* CL, double* CDi, cpg_request_info* info);
 /* Device-memory estimate of one request (the admission rule). */
 int64_t cpg_server_footprint(int64_t n_body, int k, int precision);
+
+/* Unsteady request: the vortex-particle case of cpg_vpcase_create on this mesh (body
+ * panels only), advanced nsteps time steps or until its Trefftz-plane check converges. */
+typedef struct {
+    double CL, CD;        /* Trefftz plane of the final state                          */
+    int64_t steps;        /* time steps taken                                           */
+    int64_t n_particles;
+    int converged;
+} cpg_vp_result;
+int  cpg_server_submit_vp(cpg_server* s, const double* nodes, int64_t n_nodes, const int64_t* tris,
+                          const int32_t* ids, int64_t n_tris, const cpg_vp_params* params, int nsteps,
+                          int64_t* ticket);
+/* Blocks until the unsteady request is done; mu (n_body, may be null): the final body
+ * doublet strengths.  Returns the request's status. */
+int  cpg_server_wait_vp(cpg_server* s, int64_t ticket, cpg_vp_result* result, double* mu, cpg_request_info* info);
+/* Device-memory estimate of an unsteady request: n_w2 second-row buffer panels (one
+ * particle each per step), nsteps steps. */
+int64_t cpg_server_footprint_vp(int64_t n_body, int64_t n_w2, int nsteps, int precision);
 
 #ifdef __cplusplus
 }

@@ -28,7 +28,9 @@
  *                              CPanel/geometry.cpp:261-400,1313-1345, and cpCaseVP::run,
  *                              CPanel/cpCaseVP.cpp:26-117 (convection, shedding, strength
  *                              update, octree rebuild, source strengths, solve) one step
- *                              at a time; the Trefftz-plane early stop is the caller's
+ *                              at a time, with the Trefftz-plane early stop
+ *                              (cpCaseVP::solutionConvergence, CPanel/cpCaseVP.cpp:204-229;
+ *                              wake::trefftzPlaneVP, CPanel/wake.cpp:191-361)
  */
 #ifndef CPANEL_VP_H
 #define CPANEL_VP_H
@@ -77,6 +79,11 @@ int  cpg_ptree_table(const cpg_ptree* t, double* nodes, int64_t* leaf_members);
 int  cpg_ptree_host_table(const double* pos, const double* strength, const double* radius, int64_t n,
                           int64_t max_members, double* nodes, int64_t cap_nodes, int64_t* leaf_members,
                           cpg_ptree_info* info);
+/* Precision of this tree's traversals: CPG_PLAIN_FP64 (default; every interaction in
+ * FP64) or CPG_MIXED (far nodes in FP32 from a float view of their expansions, leaf
+ * members -- the direct near field -- in FP64; far/near and cut-off decisions equal the
+ * FP64 ones, so the same nodes are visited). */
+int  cpg_ptree_set_precision(cpg_ptree* t, int precision);
 /* barnesHutVel(POI) at m points (device pts m x 3 -> vel m x 3) */
 int  cpg_bh_velocity_points(cpg_ptree* t, const double* pts, int64_t m, double* vel);
 /* barnesHutVel(particle*), barnesHutStretch, barnesHutDiff for every particle of the
@@ -92,6 +99,12 @@ int  cpg_particles_velocity(cpg_ctx* ctx, const double* pos, const double* stren
  * output may be null. */
 int  cpg_particles_stretch_diff(cpg_ctx* ctx, const double* pos, const double* strength, const double* radius,
                                 int64_t n, double* stretch, double* diff);
+
+/* Precision of this context's panel-particle operators (cpg_panels_velocity,
+ * cpg_panels_stretching): CPG_PLAIN_FP64 (default) or CPG_MIXED (body-panel pairs
+ * beyond five panel lengths -- the point-source/point-doublet branch -- in FP32, the
+ * rest in FP64, the same near/far split). */
+int  cpg_set_particle_precision(cpg_ctx* ctx, int precision);
 
 /* Panel-induced velocity at m points: sum over nb body triangles (vertices nb x 9)
  * of sigma_j vSrc + mu_j vDub, then over nw wake triangles of mu_w dubVInf.
@@ -116,14 +129,21 @@ typedef struct {
     int accelerate;        /* Barnes-Hut (inputParams::accelerateCode) or direct sums      */
     double Sref;           /* reference area of the Trefftz-plane coefficients (> 0)       */
     double mach;           /* Prandtl-Glauert factor sqrt(1 - M^2) of those coefficients   */
+    int precision;         /* CPG_PLAIN_FP64: the reference method in FP64.  CPG_MIXED:
+                              particle-node and panel far fields in FP32 (near fields, and
+                              every near/far decision, as in FP64) and the FP32 LU of A,
+                              factored once, refined against FP64 A to 1e-12 each step
+                              (BiCGSTAB for a step whose refinement stalls)            */
 } cpg_vp_params;
 typedef struct {
     int64_t n_body, n_w1, n_w2;   /* body panels, first and second buffer rows           */
     int64_t n_particles;
     int64_t timestep;             /* completed steps (the reference's timestep counter)   */
-    int64_t solver_iters;         /* BiCGSTAB iterations of the last solve                */
+    int64_t solver_iters;         /* BiCGSTAB iterations (CPG_MIXED: refinement steps) of
+                                     the last solve                                      */
     double dt;
     int64_t n_tree_nodes;         /* octree of the last rebuild                          */
+    int64_t solve_fallbacks;      /* CPG_MIXED: steps whose refinement stalled            */
 } cpg_vp_info;
 /* Host-only build of the buffer wake (no device use): counts[3] = n_body, n_w1, n_w2 and
  * *dt_out always; the other outputs (w1/w2 vertices n x 12, first-row interpolation
@@ -146,6 +166,12 @@ int  cpg_vpcase_step(cpg_vpcase* c, int nsteps);
  * CPanel/cpCaseVP.cpp:418-429; wake::trefftzPlaneVP, CPanel/wake.cpp:191-320) and whether
  * the convergence check has fired.  Any pointer may be null. */
 int  cpg_vpcase_trefftz(cpg_vpcase* c, double* CL, double* CD, int* converged);
+/* Convective velocity of every particle at the current state (host vel n_particles x 3):
+ * Vinf + particle term + panel/filament term (the latter zero beyond 12 cref), as the
+ * next step's convection evaluates it (cpCaseVP::convectParticles, CPanel/cpCaseVP.cpp:
+ * 370-391).  precision CPG_PLAIN_FP64 or CPG_MIXED; direct != 0 replaces the octree by
+ * the FP64 direct sum over all particles (symmetrised Gaussian core, self excluded). */
+int  cpg_vpcase_velocities(cpg_vpcase* c, int precision, int direct, double* vel);
 /* host copies: particles in shedding order (pos, strength n x 3, radius, shed step, index
  * of the shedding second-row panel); any pointer may be null */
 int  cpg_vpcase_particles(cpg_vpcase* c, double* pos, double* strength, double* radius, int32_t* shed_time,

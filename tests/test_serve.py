@@ -64,3 +64,42 @@ def test_admission_by_budget_serialises_large_requests(built):
     srv.close()
     assert all(r["info"]["running_at_start"] == 1 for r in res)
     assert all(r["info"]["status"] == 0 for r in res)
+
+
+def test_footprint_rule_unsteady(built):
+    from cpanel_gb300 import serve
+    a = serve.footprint_vp(4000, 40, 100, "plain")
+    b = serve.footprint_vp(4000, 40, 100, "mixed")
+    assert a > 16 * 4000**2 + 8 * 4000 * 40 and b > a + 12 * 4000**2
+    assert serve.footprint_vp(4000, 40, 200, "plain") > a
+
+
+@pytest.mark.gpu
+def test_unsteady_requests_alone_equal_in_the_mix(built):
+    """Vortex-particle runs beside steady solves: the same particles, strengths and
+    Trefftz plane as when run alone."""
+    from cpanel_gb300 import serve, wing
+    spec = wing.WingSpec(m=0.02, p=0.4, t=0.12, root_chord=1.0, span=4.0, taper=0.8, sweep_deg=0.0, n_chord=10,
+                         n_span=6, wake_len=10.0, wake_dir=(1.0, 0.0, 0.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    tris, ids = tris[keep], ids[keep]
+    steady = _mix()[:3]
+    srv = serve.Server(slots=4, budget_gb=40.0, precision="mixed")
+    alone = {p: srv.wait(srv.submit_vp(nodes, tris, ids, 12, alpha=6.0, Sref=info["area"], precision=p))
+             for p in ("plain", "mixed")}
+    tickets = []
+    for p in ("plain", "mixed"):
+        tickets += [srv.submit(*r[:4], **r[4]) for r in steady]
+        tickets.append((p, srv.submit_vp(nodes, tris, ids, 12, alpha=6.0, Sref=info["area"], precision=p)))
+    res = [(t[0], srv.wait(t[1])) if isinstance(t, tuple) else (None, srv.wait(t)) for t in tickets]
+    srv.close()
+    for p, r in res:
+        if p is None:
+            continue
+        a = alone[p]
+        assert r["steps"] == a["steps"] == 12 and r["n_particles"] == a["n_particles"] > 0
+        assert np.abs(r["mu"] - a["mu"]).max() <= 1e-12 * np.abs(a["mu"]).max()
+        assert abs(r["CL"] - a["CL"]) <= 1e-12 * abs(a["CL"]) and abs(r["CD"] - a["CD"]) <= 1e-12 * abs(a["CD"])
+    assert max(r["info"]["running_at_start"] for _, r in res) > 1
+    assert abs(alone["mixed"]["CL"] - alone["plain"]["CL"]) <= 1e-6 * abs(alone["plain"]["CL"])

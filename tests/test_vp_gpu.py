@@ -211,3 +211,81 @@ def test_vp_trefftz_and_early_stop_match_oracle(built):
             assert abs(tg[key] - to[key]) <= 1e-9 * max(abs(to[key]), 1e-12), (step, key)
     assert to["converged"] and S.info()["timestep"] < 70
     assert G.info()["timestep"] == S.info()["timestep"]
+
+
+# ---- mixed precision: FP32 far field, FP64 near field, same decisions ----
+MIXED_TOL = 1e-5  # max |mixed - FP64| / max |FP64|, per output
+
+
+@pytest.mark.parametrize("clustered", [False, True])
+def test_barnes_hut_mixed_precision(built, clustered):
+    from cpanel_gb300 import vp
+    pos, st, rad = _cloud(5000, 31, clustered)
+    if not clustered:
+        pos *= 0.3
+    tree = vp.ParticleFMM(_cuda(pos), _cuda(st), _cuda(rad))
+    ref = [_np(x) for x in tree.barnesHut()]
+    rng = np.random.default_rng(32)
+    pts = _cuda(np.concatenate([rng.normal(size=(800, 3)), pos[:10]]))
+    ref_pts = _np(tree.barnesHutVel(pts))
+    tree.set_precision("mixed")
+    got = [_np(x) for x in tree.barnesHut()]
+    for r, g in zip(ref, got):
+        assert _rel(g, r) < MIXED_TOL
+        assert _rel(g, r) > 0 or np.abs(r).max() == 0  # the far field did run in FP32
+    assert _rel(_np(tree.barnesHutVel(pts)), ref_pts) < MIXED_TOL
+    # single outputs take the same decisions
+    assert _rel(_np(tree.barnesHutStretch()), ref[1]) < MIXED_TOL
+
+
+def test_panel_operators_mixed_precision(built):
+    from cpanel_gb300 import vp
+    nodes, tris, ids = _vp_wing(10, 7)
+    m = po.Mesh(nodes, tris, ids)
+    bv = m.body_verts()
+    T = vp.vp_topology(nodes, tris, ids)
+    wv = T["w1"]
+    rng = np.random.default_rng(41)
+    sigma, mu, wmu = rng.normal(size=len(bv)), rng.normal(size=len(bv)), rng.normal(size=len(wv))
+    c = bv.reshape(-1, 3, 3).mean(axis=1)
+    pos = np.concatenate([c[::3] + rng.normal(size=(len(c[::3]), 3)) * 0.05,
+                          rng.normal(size=(3000, 3)) * [3.0, 2.0, 0.5] + [2.0, 0, 0],
+                          rng.normal(size=(500, 3)) * 10])
+    st = rng.normal(size=pos.shape) * 0.01
+    args = (_cuda(bv), _cuda(sigma), _cuda(mu))
+    for wverts, wm in ((None, None), (m.wake_verts(), rng.normal(size=len(m.wake_verts())))):
+        w = (None, None) if wverts is None else (_cuda(wverts), _cuda(wm))
+        ref = _np(vp.panels_velocity(*args, *w, _cuda(pos)))
+        got = _np(vp.panels_velocity(*args, *w, _cuda(pos), precision="mixed"))
+        assert 0 < _rel(got, ref) < MIXED_TOL
+    ref = _np(vp.panels_stretching(*args, _cuda(wv), _cuda(wmu), _cuda(pos), _cuda(st)))
+    got = _np(vp.panels_stretching(*args, _cuda(wv), _cuda(wmu), _cuda(pos), _cuda(st), precision="mixed"))
+    assert 0 < _rel(got, ref) < MIXED_TOL
+
+
+def test_vp_mixed_velocities_and_loop(built):
+    """Particle velocities of one state in both precisions (and against the FP64 direct
+    sum), then the mixed loop against the FP64 loop: same shedding, close states."""
+    from cpanel_gb300 import vp
+    nodes, tris, ids = _vp_wing(8, 6)
+    P = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0)
+    M = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, precision="mixed")
+    for step in range(14):
+        P.step()
+        M.step()
+    vp64 = P.velocities("plain")
+    vp32 = P.velocities("mixed")
+    vdir = P.velocities("plain", direct=True)
+    assert _rel(vp32, vp64) < MIXED_TOL
+    per = np.linalg.norm(vp32 - vp64, axis=1) / np.linalg.norm(vp64, axis=1)
+    assert per.max() < MIXED_TOL
+    assert _rel(vdir, vp64) < 1e-2  # the octree's own approximation, for scale
+    pp, pm = P.particles(), M.particles()
+    assert np.array_equal(pp["shed_time"], pm["shed_time"]) and np.array_equal(pp["parent"], pm["parent"])
+    assert _rel(pm["pos"], pp["pos"]) < 1e-6
+    assert _rel(pm["strength"], pp["strength"]) < 1e-4
+    sp, sm = P.strengths(), M.strengths()
+    assert _rel(sm["mu"], sp["mu"]) < 1e-5
+    assert M.info()["solve_fallbacks"] == 0
+    tp, tm = P.trefftz(), M.trefftz()
+    assert abs(tm["CL"] - tp["CL"]) <= 1e-5 * abs(tp["CL"])

@@ -72,7 +72,7 @@ constexpr double kPi = 3.14159265358979323846;
 // wing: CHTLS weights of order 1/h amplify the remaining doublet error.  Three passes
 // (1e-12) give 3.6e-9.
 constexpr double kMixedRefineTol = 1e-12;
-constexpr int F_STRIDE_HOST = 16;  // double-float far-field record, F_STRIDE in common.cuh
+constexpr int F_STRIDE_HOST = 64;  // double-float record of the mixed assembly, F_STRIDE in common.cuh
 
 }  // namespace
 
@@ -84,6 +84,8 @@ struct cpg_geometry {
     cpg_ctx* ctx = nullptr;
     cpg::HostMesh H;
     DevBuf rec, frec, bez, clp, cli, tip, ts, wrec, widx, wcoef, tzst, tzln, tzpts, G, F3, F2, mode;
+    DevBuf order;  // block schedule of the mixed assembly
+    int64_t order_n = -1;
     DevBuf A64, B64, A32, Alo, rb, count;
     DevBuf LU, bad;
     cpg::LuGraphs graphs;
@@ -311,6 +313,22 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
         }
         split(r[cpg::PF_AREA], o + 12, o + 13);
         o[14] = (float)r[cpg::PF_LONG];
+        // exact-formula band: vertices about the centroid, n x s_k, |s_k|, 1/|s_k|
+        const double* c = r + cpg::PF_C;
+        const double* nv = r + cpg::PF_N;
+        for (int k = 0; k < 3; k++) {
+            const double* v = r + cpg::PF_V0 + 3 * k;
+            const double* w = r + cpg::PF_V0 + 3 * ((k + 1) % 3);
+            double sv[3] = {w[0] - v[0], w[1] - v[1], w[2] - v[2]};
+            double ns[3] = {nv[1] * sv[2] - nv[2] * sv[1], nv[2] * sv[0] - nv[0] * sv[2], nv[0] * sv[1] - nv[1] * sv[0]};
+            double S = std::sqrt(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]);
+            for (int q = 0; q < 3; q++) {
+                split(v[q] - c[q], o + 16 + 2 * (3 * k + q), o + 17 + 2 * (3 * k + q));
+                split(ns[q], o + 34 + 2 * (3 * k + q), o + 35 + 2 * (3 * k + q));
+            }
+            split(S, o + 52 + 2 * k, o + 53 + 2 * k);
+            split(1.0 / S, o + 58 + 2 * k, o + 59 + 2 * k);
+        }
     }
     cudaError_t e;
     if ((e = upload(g->rec, H.body, s)) != cudaSuccess || (e = upload(g->frec, fr, s)) != cudaSuccess ||
@@ -331,7 +349,8 @@ void cpg_geometry_destroy(cpg_geometry* g) {
     if (!g) return;
     DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
                       &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
-                      &g->B64, &g->A32, &g->Alo, &g->rb, &g->LU, &g->bad, &g->count, &g->work, &g->post_work, &g->cases, &g->outs};
+                      &g->B64, &g->A32, &g->Alo, &g->rb, &g->LU, &g->bad, &g->count, &g->work, &g->post_work, &g->cases, &g->outs,
+                      &g->order};
     // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
     g->graphs.release();
@@ -431,8 +450,14 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
         CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
         CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
         CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n))), "alloc rhs basis");
+        if (g->order_n != n) {  // block schedule, once per geometry
+            std::vector<int> ord;
+            cpg::mixed_block_order(n, ord);
+            CK(upload(g->order, ord, s), "upload block order");
+            g->order_n = n;
+        }
         CK(cpg::launch_assemble_mixed(g->rec.as<double>(), g->frec.as<float>(), n, g->wrec.as<double>(),
-                                      g->widx.as<int32_t>(), g->wcoef.as<double>(), g->H.n_wake,
+                                      g->widx.as<int32_t>(), g->wcoef.as<double>(), g->H.n_wake, g->order.as<int>(),
                                       g->A32.as<float>(), g->Alo.as<float>(), g->rb.as<double>(), g->rb.as<double>() + 3 * n,
                                       g->count.as<unsigned long long>(), s),
            "assembly (mixed)");
@@ -464,7 +489,8 @@ int cpg_get_A(cpg_geometry* g, double* host) {
     } else if (g->have32) {
         DevBuf tmp;
         CK(tmp.ensure(sizeof(double) * nn), "alloc");
-        CK(cpg::launch_widen(g->A32.as<float>(), tmp.as<double>(), (int64_t)nn, ctx->stream), "widen");
+        CK(cpg::launch_widen(g->A32.as<float>(), g->Alo.as<float>(), tmp.as<double>(), (int64_t)nn, ctx->stream),
+           "widen");
         CK(cudaMemcpyAsync(host, tmp.p, sizeof(double) * nn, cudaMemcpyDeviceToHost, ctx->stream), "copy A");
         CK(cudaStreamSynchronize(ctx->stream), "copy A");
         tmp.release();

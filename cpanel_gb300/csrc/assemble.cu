@@ -5,7 +5,10 @@
 // j = source panel.  A block owns 128 consecutive targets and a contiguous range of
 // source panels, staged 32 at a time in shared memory; each store instruction of
 // a warp writes 32 consecutive rows of one column.
+#include <algorithm>
 #include <mutex>
+#include <utility>
+#include <vector>
 
 #include "../../include/cpanel_gpu.h"
 #include "assemble.h"
@@ -56,27 +59,131 @@ __global__ void __launch_bounds__(TI) k_assemble_fp64(const double* __restrict__
     }
 }
 
-// Mixed: double-float far field, FP64 near field (the reference's own near set,
-// |pjk| <= 5 longSide).  A is stored as two FP32 matrices, hi and lo, whose sum
-// carries about 44 bits; the Krylov iterations read hi only, the refinement
-// residual reads both.  Instead of storing B, the source right-hand-side basis
-// rb[c*n+i] = sum_j B(i,j) * n_j[c] is accumulated (double-float per tile, FP64
-// across tiles and for near pairs).  Each column chunk writes its own partial sums
+// panelPhiInf (CPanel/bodyPanel.cpp:132-190) for a target between 3 and 5 longSide of the
+// source, in double-float.  The three edge angles of vortexPhi sum to minus the solid angle
+// of the triangle, taken here as 2 atan(N / D) (Van Oosterom and Strackee, 1983) with
+// N = -2 area PN and D = |a0||a1||a2| + (a0.a1)|a2| + (a0.a2)|a1| + (a1.a2)|a0| (a_k = poi - v_k);
+// there |N / D| < 0.02, so atan is a short odd series.  Each edge's log term is
+// log((A+B+S)/(A+B-S)) = 2 atanh(S / (A+B)) with S / (A+B) < 0.25, also a series.  The
+// edge sum of the reference loses accuracy for nearly coplanar pairs (|N / D| < 1e-6: up
+// to 3e-11 absolute on the test wings); those, and anything outside the series' ranges,
+// return false and take the FP64 formula.  d: poi - centroid; f: the panel's record.
+struct BandPhi {
+    df32 src, dub;
+    bool ok;
+};
+__device__ __noinline__ BandPhi band_phi_df(df32 d0, df32 d1, df32 d2, const float* __restrict__ f) {
+    BandPhi out{{0, 0}, {0, 0}, false};
+    const df32 d[3] = {d0, d1, d2};
+    const df32 nv[3] = {{f[F_NHI], f[F_NLO]}, {f[F_NHI + 1], f[F_NLO + 1]}, {f[F_NHI + 2], f[F_NLO + 2]}};
+    const df32 PN = df_add(df_add(df_mul(d[0], nv[0]), df_mul(d[1], nv[1])), df_mul(d[2], nv[2]));
+    df32 a[3][3], A[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+#pragma unroll
+        for (int c = 0; c < 3; c++) a[k][c] = df_sub(d[c], df32{f[F_VC + 2 * (3 * k + c)], f[F_VC + 2 * (3 * k + c) + 1]});
+        A[k] = df_sqrt(df_add(df_add(df_mul(a[k][0], a[k][0]), df_mul(a[k][1], a[k][1])), df_mul(a[k][2], a[k][2])));
+    }
+    auto dot = [&](int i, int j) {
+        return df_add(df_add(df_mul(a[i][0], a[j][0]), df_mul(a[i][1], a[j][1])), df_mul(a[i][2], a[j][2]));
+    };
+    df32 D = df_mul(df_mul(A[0], A[1]), A[2]);
+    D = df_add(D, df_mul(dot(0, 1), A[2]));
+    D = df_add(D, df_mul(dot(0, 2), A[1]));
+    D = df_add(D, df_mul(dot(1, 2), A[0]));
+    if (!(D.hi > 0.f)) return out;
+    const df32 N = df_neg(df_mul(df32{2.f * f[F_AHI], 2.f * f[F_ALO]}, PN));
+    const df32 x = df_div(N, D);
+    const float ax = fabsf(x.hi);
+    if (ax < 1e-6f || ax > 0.02f) return out;
+    // atan(x) = x (1 - u/3 + u^2/5 - ... - u^5/11), u = x^2 (next term below 2e-20 x)
+    const df32 u = df_mul(x, x);
+    df32 p = CPG_DFK(-1.0 / 11);
+    p = df_add(df_mul(p, u), CPG_DFK(1.0 / 9));
+    p = df_add(df_mul(p, u), CPG_DFK(-1.0 / 7));
+    p = df_add(df_mul(p, u), CPG_DFK(1.0 / 5));
+    p = df_add(df_mul(p, u), CPG_DFK(-1.0 / 3));
+    p = df_add(df_mul(p, u), df32{1.f, 0.f});
+    const df32 at = df_mul(x, p);
+    const df32 dubs = df32{-2.f * at.hi, -2.f * at.lo};  // sum of the three edge angles
+    df32 ss = {0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        const int k1 = k == 2 ? 0 : k + 1;
+        const df32 S = {f[F_S + 2 * k], f[F_S + 2 * k + 1]}, IS = {f[F_IS + 2 * k], f[F_IS + 2 * k + 1]};
+        const df32 t = df_div(S, df_add(A[k], A[k1]));
+        if (!(t.hi < 0.25f)) return out;
+        // atanh(t) = t (1 + w/3 + w^2/5 + ... + w^12/25), w = t^2 (next term below 1e-16 t)
+        const df32 w = df_mul(t, t);
+        df32 q = CPG_DFK(1.0 / 25);
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 23));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 21));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 19));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 17));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 15));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 13));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 11));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 9));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 7));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 5));
+        q = df_add(df_mul(q, w), CPG_DFK(1.0 / 3));
+        q = df_add(df_mul(q, w), df32{1.f, 0.f});
+        const df32 at2 = df_mul(t, q);
+        const df32 ns[3] = {{f[F_NS + 2 * (3 * k)], f[F_NS + 2 * (3 * k) + 1]},
+                            {f[F_NS + 2 * (3 * k + 1)], f[F_NS + 2 * (3 * k + 1) + 1]},
+                            {f[F_NS + 2 * (3 * k + 2)], f[F_NS + 2 * (3 * k + 2) + 1]}};
+        const df32 Al = df_add(df_add(df_mul(ns[0], a[k][0]), df_mul(ns[1], a[k][1])), df_mul(ns[2], a[k][2]));
+        // Al * GL with GL = 2 atanh(t) / S
+        ss = df_add(ss, df_mul(Al, df_mul(df32{2.f * at2.hi, 2.f * at2.lo}, IS)));
+    }
+    const double q4 = 1.0 / CPG_FOUR_PI;
+    const df32 inv4pi = df32{(float)q4, (float)(q4 - (double)(float)q4)};
+    out.src = df_mul(df_sub(ss, df_mul(PN, dubs)), inv4pi);
+    out.dub = df_mul(dubs, inv4pi);
+    out.ok = true;
+    return out;
+}
+
+// Mixed assembly.  Per (target, source) pair: far field (beyond 5 longSide, decided
+// exactly as the reference) in double-float; between 3 and 5 longSide the exact formulas
+// in double-float (band_phi_df); nearer, the FP64 formulas.  A is stored as two FP32
+// matrices, hi and lo, whose sum carries about 44 bits; the factorization reads hi, the
+// refinement residual both.  Instead of storing B, the source right-hand-side basis
+// rb[c*n+i] = sum_j B(i,j) * n_j[c] is accumulated (double-float per tile, FP64 across
+// tiles and for near pairs).  Each source chunk writes its own partial sums
 // (rbp[(chunk*3 + c)*n + i]); k_rb_reduce adds the chunks in order, so the result does
-// not depend on block scheduling.
-__global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict__ rec, const float* __restrict__ frec,
-                                                       int64_t n, int64_t jchunk, float* __restrict__ A32,
-                                                       float* __restrict__ Alo, double* __restrict__ rbp,
-                                                       unsigned long long* __restrict__ near_count) {
+// not depend on block scheduling.  The FP64 pairs of a warp are
+// queued per source tile (in tile order, then lane order) and evaluated by the whole warp,
+// one pair per lane, so a warp with a few near lanes does not idle the others; each target
+// then adds its own queued results in queue order (the same order on every run).
+constexpr int WARPS_PER_BLOCK = TI / 32;
+__global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restrict__ rec,
+                                                          const float* __restrict__ frec, int64_t n, int64_t jchunk,
+                                                          const int* __restrict__ order, float* __restrict__ A32,
+                                                          float* __restrict__ Alo, double* __restrict__ rbp,
+                                                          unsigned long long* __restrict__ near_count) {
+    // block b works on row block order[2b] and source chunk order[2b+1] (the costly
+    // near-diagonal blocks first, so that they do not form the tail)
+    const int64_t bx = order[2 * blockIdx.x], by = order[2 * blockIdx.x + 1];
     __shared__ double s_rec[TJ * R_STRIDE];
     __shared__ float s_f[TJ * F_STRIDE];
-    int64_t i = (int64_t)blockIdx.x * TI + threadIdx.x;
+    __shared__ unsigned short s_q[WARPS_PER_BLOCK][TJ * 32];  // (tile index << 5) | lane
+    __shared__ double s_res[WARPS_PER_BLOCK][32][3];
+    __shared__ int s_own[WARPS_PER_BLOCK][32];
+    __shared__ double s_poi[WARPS_PER_BLOCK][32][3];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    int64_t i = bx * TI + threadIdx.x;
+    const int64_t iw = bx * TI + 32 * w;  // first target of this warp
     bool act = i < n;
     dv3 poi = act ? ld3(rec + i * R_STRIDE + R_C) : mk3(0, 0, 0);
+    s_poi[w][lane][0] = poi.x;
+    s_poi[w][lane][1] = poi.y;
+    s_poi[w][lane][2] = poi.z;
     df32 ci[3] = {{0, 0}, {0, 0}, {0, 0}};
     if (act)
         for (int c = 0; c < 3; c++) ci[c] = df32{frec[i * F_STRIDE + F_CHI + c], frec[i * F_STRIDE + F_CLO + c]};
-    int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
+    int64_t jb = by * jchunk, je = min(n, jb + jchunk);
     double acc64[3] = {0, 0, 0};
     unsigned nnear = 0;
     const double q4 = 1.0 / CPG_FOUR_PI;
@@ -90,57 +197,95 @@ __global__ void __launch_bounds__(TI) k_assemble_mixed(const double* __restrict_
         }
         __syncthreads();
         int cnt = (int)min((int64_t)TJ, je - j0);
-        if (!act) continue;
         df32 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+        int qn = 0;  // warp-uniform queue length
         for (int t = 0; t < cnt; t++) {
             int64_t j = j0 + t;
             const float* f = s_f + t * F_STRIDE;
-            df32 d[3];
+            bool near64 = false;
+            if (act) {
+                df32 d[3];
 #pragma unroll
-            for (int c = 0; c < 3; c++) d[c] = df_sub(ci[c], df32{f[F_CHI + c], f[F_CLO + c]});
-            float r2f = __fmaf_rn(d[2].hi, d[2].hi, __fmaf_rn(d[1].hi, d[1].hi, __fmul_rn(d[0].hi, d[0].hi)));
-            float L = f[F_LONG];
-            float lim = __fmul_rn(25.f, __fmul_rn(L, L));
-            bool far;
-            if (r2f > __fmul_rn(lim, 1.00001f))
-                far = true;
-            else if (r2f < __fmul_rn(lim, 0.99999f))
-                far = false;
-            else {  // guard band: decide exactly as the FP64 reference does
-                const double* r = s_rec + t * R_STRIDE;
-                double dd = norm3(poi - ld3(r + R_C));
-                far = dd / r[R_LONG] > 5;
-            }
-            if (far) {
-                // pntSrcPhi / pntDubPhi (CPanel/bodyPanel.cpp:392-395, panel.cpp:737-740) in double-float
-                df32 r2 = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
-                df32 rinv = df_rsqrt(r2);
-                df32 src = df_mul(df_mul(df32{f[F_AHI], f[F_ALO]}, rinv), inv4pi);
+                for (int c = 0; c < 3; c++) d[c] = df_sub(ci[c], df32{f[F_CHI + c], f[F_CLO + c]});
+                float r2f = __fmaf_rn(d[2].hi, d[2].hi, __fmaf_rn(d[1].hi, d[1].hi, __fmul_rn(d[0].hi, d[0].hi)));
+                float L = f[F_LONG];
+                float lim = __fmul_rn(25.f, __fmul_rn(L, L));
+                bool far;
+                if (r2f > __fmul_rn(lim, 1.00001f))
+                    far = true;
+                else if (r2f < __fmul_rn(lim, 0.99999f))
+                    far = false;
+                else {  // guard band: decide exactly as the FP64 reference does
+                    const double* r = s_rec + t * R_STRIDE;
+                    double dd = norm3(poi - ld3(r + R_C));
+                    far = dd / r[R_LONG] > 5;
+                }
                 df32 nv[3] = {{f[F_NHI], f[F_NLO]}, {f[F_NHI + 1], f[F_NLO + 1]}, {f[F_NHI + 2], f[F_NLO + 2]}};
-                df32 pn = df_add(df_add(df_mul(d[0], nv[0]), df_mul(d[1], nv[1])), df_mul(d[2], nv[2]));
-                df32 dub = df_mul(df_mul(pn, df_mul(rinv, rinv)), src);
-                A32[j * n + i] = dub.hi;
-                Alo[j * n + i] = dub.lo;
+                if (far) {
+                    // pntSrcPhi / pntDubPhi (CPanel/bodyPanel.cpp:392-395, panel.cpp:737-740) in double-float
+                    df32 r2 = df_add(df_add(df_mul(d[0], d[0]), df_mul(d[1], d[1])), df_mul(d[2], d[2]));
+                    df32 rinv = df_rsqrt(r2);
+                    df32 src = df_mul(df_mul(df32{f[F_AHI], f[F_ALO]}, rinv), inv4pi);
+                    df32 pn = df_add(df_add(df_mul(d[0], nv[0]), df_mul(d[1], nv[1])), df_mul(d[2], nv[2]));
+                    df32 dub = df_mul(df_mul(pn, df_mul(rinv, rinv)), src);
+                    A32[j * n + i] = dub.hi;
+                    Alo[j * n + i] = dub.lo;
 #pragma unroll
-                for (int c = 0; c < 3; c++) acc[c] = df_add(acc[c], df_mul(src, nv[c]));
-            } else {
-                double src = 0, dub = 0;
-                const double* r = s_rec + t * R_STRIDE;
-                panel_phi_inf(r, poi, src, dub);
-                nnear++;
-                float hi = (float)dub;
-                A32[j * n + i] = hi;
-                Alo[j * n + i] = (float)(dub - (double)hi);  // FP64 value = hi + lo to 2^-48
-                acc64[0] += src * r[R_N + 0];
-                acc64[1] += src * r[R_N + 1];
-                acc64[2] += src * r[R_N + 2];
+                    for (int c = 0; c < 3; c++) acc[c] = df_add(acc[c], df_mul(src, nv[c]));
+                } else {
+                    // beyond 3 longSide the exact formulas run in double-float (band_phi_df)
+                    BandPhi bp{{0, 0}, {0, 0}, false};
+                    if (r2f > __fmul_rn(9.f, __fmul_rn(L, L))) bp = band_phi_df(d[0], d[1], d[2], f);
+                    if (bp.ok) {
+                        A32[j * n + i] = bp.dub.hi;
+                        Alo[j * n + i] = bp.dub.lo;
+#pragma unroll
+                        for (int c = 0; c < 3; c++) acc[c] = df_add(acc[c], df_mul(bp.src, nv[c]));
+                    } else {
+                        near64 = true;
+                    }
+                }
             }
+            const unsigned qm = __ballot_sync(0xffffffffu, near64);
+            if (near64) s_q[w][qn + __popc(qm & lt_mask)] = (unsigned short)((t << 5) | lane);
+            qn += __popc(qm);
+        }
+        __syncwarp();
+        // the warp's FP64 pairs, one per lane
+        for (int base = 0; base < qn; base += 32) {
+            const int e = base + lane;
+            if (e < qn) {
+                const int ent = s_q[w][e];
+                const int tt = ent >> 5, ln = ent & 31;
+                const double* r = s_rec + tt * R_STRIDE;
+                const dv3 pe = mk3(s_poi[w][ln][0], s_poi[w][ln][1], s_poi[w][ln][2]);
+                double src = 0, dub = 0;
+                panel_phi_inf(r, pe, src, dub);
+                const int64_t ie = iw + ln, je_ = j0 + tt;
+                float hi = (float)dub;
+                A32[je_ * n + ie] = hi;
+                Alo[je_ * n + ie] = (float)(dub - (double)hi);  // FP64 value = hi + lo to 2^-48
+                s_res[w][lane][0] = src * r[R_N + 0];
+                s_res[w][lane][1] = src * r[R_N + 1];
+                s_res[w][lane][2] = src * r[R_N + 2];
+                s_own[w][lane] = ln;
+                nnear++;
+            }
+            __syncwarp();
+            const int m = min(32, qn - base);
+            for (int k = 0; k < m; k++)
+                if (s_own[w][k] == lane) {
+                    acc64[0] += s_res[w][k][0];
+                    acc64[1] += s_res[w][k][1];
+                    acc64[2] += s_res[w][k][2];
+                }
+            __syncwarp();
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) acc64[c] += df_to_double(acc[c]);
     }
     if (act) {
-        double* part = rbp + (int64_t)blockIdx.y * 3 * n;
+        double* part = rbp + by * 3 * n;
         part[i] = acc64[0];
         part[n + i] = acc64[1];
         part[2 * n + i] = acc64[2];
@@ -373,15 +518,33 @@ cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wre
     return cudaGetLastError();
 }
 
+void mixed_block_order(int64_t n, std::vector<int>& out) {
+    const int64_t ch = chunk_for(n);
+    const int64_t nbx = (n + TI - 1) / TI, nby = (n + ch - 1) / ch;
+    std::vector<std::pair<int64_t, int64_t>> key;  // (distance of the index ranges' centres, block)
+    for (int64_t by = 0; by < nby; by++)
+        for (int64_t bx = 0; bx < nbx; bx++) {
+            int64_t rc = bx * TI + TI / 2, cc = by * ch + ch / 2;
+            key.push_back({rc > cc ? rc - cc : cc - rc, by * nbx + bx});
+        }
+    std::sort(key.begin(), key.end());
+    out.resize(2 * key.size());
+    for (size_t b = 0; b < key.size(); b++) {
+        out[2 * b] = (int)(key[b].second % nbx);
+        out[2 * b + 1] = (int)(key[b].second / nbx);
+    }
+}
+
 cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
-                                  const int32_t* widx, const double* wcoef, int64_t nw, float* A32, float* Alo,
-                                  double* rb, double* rb_part, unsigned long long* near_count, cudaStream_t s) {
+                                  const int32_t* widx, const double* wcoef, int64_t nw, const int* order, float* A32,
+                                  float* Alo, double* rb, double* rb_part, unsigned long long* near_count,
+                                  cudaStream_t s) {
     int64_t ch = chunk_for(n);
-    dim3 grid((unsigned)((n + TI - 1) / TI), (unsigned)((n + ch - 1) / ch));
+    const int64_t nbx = (n + TI - 1) / TI, nby = (n + ch - 1) / ch;
     {
         ProfScope ps(Prof::ASSEMBLE, s);
-        k_assemble_mixed<<<grid, TI, 0, s>>>(rec, frec, n, ch, A32, Alo, rb_part, near_count);
-        k_rb_reduce<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(rb_part, n, (int64_t)grid.y, rb);
+        k_assemble_mixed<<<(unsigned)(nbx * nby), TI, 0, s>>>(rec, frec, n, ch, order, A32, Alo, rb_part, near_count);
+        k_rb_reduce<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(rb_part, n, nby, rb);
     }
     if (nw > 0) {
         ProfScope ps(Prof::WAKE_COLUMNS, s);

@@ -43,9 +43,14 @@ struct ProfScope {
 cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wrec, const int32_t* widx,
                                  const double* wcoef, int64_t nw, double* A, double* B,
                                  unsigned long long* near_count, cudaStream_t s);
+// order: mixed_block_order(n) on the device (2 ints per block: row block, source chunk)
 cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
-                                  const int32_t* widx, const double* wcoef, int64_t nw, float* A32, float* Alo,
-                                  double* rb, double* rb_part, unsigned long long* near_count, cudaStream_t s);
+                                  const int32_t* widx, const double* wcoef, int64_t nw, const int* order, float* A32,
+                                  float* Alo, double* rb, double* rb_part, unsigned long long* near_count,
+                                  cudaStream_t s);
+// block schedule of the mixed assembly: blocks sorted by the distance between their row
+// and source index ranges (near-field-heavy blocks first)
+void mixed_block_order(int64_t n, std::vector<int>& out);
 // doubles of the per-chunk partial sums that launch_assemble_mixed needs in rb_part
 int64_t mixed_rb_part_doubles(int64_t n);
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,

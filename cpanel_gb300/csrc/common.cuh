@@ -24,8 +24,13 @@ __device__ __forceinline__ dv3 ld3(const double* p) { return dv3{p[0], p[1], p[2
 // Packed panel record layout (must match cpg::PanelField in mesh.h).
 enum { R_V0 = 0, R_V1 = 3, R_V2 = 6, R_C = 9, R_N = 12, R_L = 15, R_M = 18, R_AREA = 21, R_LONG = 22, R_STRIDE = 24 };
 
-// Per-panel double-float record used by the mixed far field (FP32 pairs):
-// [c_hi(3) c_lo(3) n_hi(3) n_lo(3) area_hi area_lo longSide pad]
-enum { F_CHI = 0, F_CLO = 3, F_NHI = 6, F_NLO = 9, F_AHI = 12, F_ALO = 13, F_LONG = 14, F_STRIDE = 16 };
+// Per-panel double-float record of the mixed assembly (FP32 pairs):
+// [c_hi(3) c_lo(3) n_hi(3) n_lo(3) area_hi area_lo longSide pad] for the far field, then for
+// the exact formulas between 3 and 5 longSide, as (hi, lo) pairs: vertices minus centroid
+// (3 x 3), n x s_k for the edges s_k = v_{k+1} - v_k (3 x 3), |s_k| (3), 1/|s_k| (3).
+enum {
+    F_CHI = 0, F_CLO = 3, F_NHI = 6, F_NLO = 9, F_AHI = 12, F_ALO = 13, F_LONG = 14,
+    F_VC = 16, F_NS = 34, F_S = 52, F_IS = 58, F_STRIDE = 64
+};
 
 #define CPG_CUDA_OK(x) ((x) == cudaSuccess)

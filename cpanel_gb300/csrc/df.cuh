@@ -45,3 +45,15 @@ __device__ __forceinline__ df32 df_rsqrt(df32 x) {
     return df_fast_two_sum(y, __fmul_rn(__fmul_rn(y, r), 0.5f));
 }
 __device__ __forceinline__ double df_to_double(df32 x) { return (double)x.hi + (double)x.lo; }
+__device__ __forceinline__ df32 df_neg(df32 x) { return df32{-x.hi, -x.lo}; }
+// sqrt(x) = x / sqrt(x) for x > 0
+__device__ __forceinline__ df32 df_sqrt(df32 x) { return df_mul(x, df_rsqrt(x)); }
+// a / b: a float quotient, then the quotient of the double-float remainder
+__device__ __forceinline__ df32 df_div(df32 a, df32 b) {
+    float q1 = __fdiv_rn(a.hi, b.hi);
+    df32 r = df_sub(a, df_mul(df32{q1, 0.f}, b));
+    float q2 = __fdiv_rn(r.hi, b.hi);
+    return df_fast_two_sum(q1, q2);
+}
+// a double-precision constant as a double-float (folded at compile time)
+#define CPG_DFK(v) df32{(float)(v), (float)((v) - (double)(float)(v))}

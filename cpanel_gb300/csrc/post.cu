@@ -464,9 +464,9 @@ __global__ void k_rhs_basis(const double* __restrict__ rb, int64_t n, int k, con
     rhs[t] = V[0] * rb[i] + V[1] * rb[n + i] + V[2] * rb[2 * n + i];
 }
 
-__global__ void k_widen(const float* __restrict__ a, double* __restrict__ b, int64_t m) {
+__global__ void k_widen(const float* __restrict__ a, const float* __restrict__ lo, double* __restrict__ b, int64_t m) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < m) b[t] = (double)a[t];
+    if (t < m) b[t] = lo ? (double)a[t] + (double)lo[t] : (double)a[t];
 }
 
 }  // namespace
@@ -485,9 +485,9 @@ cudaError_t launch_rhs_basis(const double* rb, int64_t n, int k, const CaseScala
     return cudaGetLastError();
 }
 
-cudaError_t launch_widen(const float* a, double* b, int64_t m, cudaStream_t s) {
+cudaError_t launch_widen(const float* a, const float* lo, double* b, int64_t m, cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
-    k_widen<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(a, b, m);
+    k_widen<<<(unsigned)((m + 255) / 256), 256, 0, s>>>(a, lo, b, m);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,7 @@ cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs_dev, c
 
 cudaError_t launch_sigma(const double* rec, int64_t n, int k, const CaseScalars* cs, double* sigma, cudaStream_t s);
 cudaError_t launch_rhs_basis(const double* rb, int64_t n, int k, const CaseScalars* cs, double* rhs, cudaStream_t s);
-cudaError_t launch_widen(const float* a, double* b, int64_t m, cudaStream_t s);
+// b = a (+ lo when lo is not null), FP32 -> FP64
+cudaError_t launch_widen(const float* a, const float* lo, double* b, int64_t m, cudaStream_t s);
 
 }  // namespace cpg

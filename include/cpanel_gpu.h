@@ -123,7 +123,8 @@ int  cpg_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, con
  * source right-hand-side basis vectors (B is never stored). */
 int  cpg_set_inf_coeff(cpg_geometry* g, int precision);
 /* Copy the assembled matrices to host column-major buffers (n*n doubles).
- * cpg_get_A works for both precisions (FP32 values widened for CPG_MIXED). */
+ * cpg_get_A works for both precisions (CPG_MIXED: the float pair hi + lo as FP64, the
+ * matrix its refinement solves with). */
 int  cpg_get_A(cpg_geometry* g, double* host);
 int  cpg_get_B(cpg_geometry* g, double* host);
 

@@ -575,7 +575,7 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
         CK(cpg::solve_lu_refined(ctx->blas, &g->graphs, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(),
                                  n, k, rhs, mu,
-                                 g->work.p, kMixedRefineTol, 8, &st, s),
+                                 g->work.p, kMixedRefineTol, 16, &st, s),
            "refined solve (mixed)");
     }
     CK(cudaEventRecord(e1, s), "event");

@@ -198,9 +198,14 @@ void set_attrs() {
                    [] { cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM); });
 }
 
+// GEMM arithmetic of the factorization: BF16x9 emulation of FP32 on the tensor cores by
+// default; CPG_LU_GEMM=sgemm (FP32 SIMT), tf32 or bf16 (one tensor-core pass, fewer
+// correct bits: the refinement then takes more passes) for comparison.
 cublasComputeType_t lu_compute() {
     const char* e = std::getenv("CPG_LU_GEMM");
     if (e && std::string(e) == "sgemm") return CUBLAS_COMPUTE_32F;
+    if (e && std::string(e) == "tf32") return CUBLAS_COMPUTE_32F_FAST_TF32;
+    if (e && std::string(e) == "bf16") return CUBLAS_COMPUTE_32F_FAST_16BF;
     return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
 }
 
@@ -226,27 +231,34 @@ cudaError_t prepare_blas(cublasHandle_t h, LuGraphs* G, cudaStream_t s) {
     return cudaSuccess;
 }
 
-// The two panel solves of block K as GEMMs through W (copied back):
-//   L21 = A21 U_KK^{-1},  U12 = L_KK^{-1} A12.
-cudaError_t panel_gemms(cublasHandle_t h, float* LU, const float* Dinv, float* W, int64_t n, int64_t K,
-                        cudaStream_t s) {
+// L21 = A21 U_KK^{-1} for all rows below block K, as a GEMM through W (copied back).
+cudaError_t column_solve(cublasHandle_t h, float* LU, const float* Dinv, float* W, int64_t n, int64_t K,
+                         cudaStream_t s) {
     const float one = 1.f, zero = 0.f;
-    cublasComputeType_t ct = lu_compute();
     int b = (int)std::min<int64_t>(NB, n - K);
-    const float* Li = Dinv + (K / NB) * 2 * NB * NB;
-    const float* Ui = Li + NB * NB;
+    const float* Ui = Dinv + (K / NB) * 2 * NB * NB + NB * NB;
     int64_t rest = n - K - b;
     if (rest <= 0) return cudaSuccess;
     if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, b, b, &one, LU + K * n + K + b, CUDA_R_32F, (int)n, Ui,
-                     CUDA_R_32F, NB, &zero, W, CUDA_R_32F, (int)rest, ct, CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+                     CUDA_R_32F, NB, &zero, W, CUDA_R_32F, (int)rest, lu_compute(), CUBLAS_GEMM_DEFAULT) !=
+        CUBLAS_STATUS_SUCCESS)
         return cudaErrorUnknown;
-    cudaError_t e = cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float),
-                                      rest * sizeof(float), b, cudaMemcpyDeviceToDevice, s);
-    if (e != cudaSuccess) return e;
-    if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)rest, b, &one, Li, CUDA_R_32F, NB, LU + (K + b) * n + K,
-                     CUDA_R_32F, (int)n, &zero, W, CUDA_R_32F, b, ct, CUBLAS_GEMM_DEFAULT) != CUBLAS_STATUS_SUCCESS)
+    return cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float), rest * sizeof(float), b,
+                             cudaMemcpyDeviceToDevice, s);
+}
+
+// U(K..K+b, c0..c0+nc) = L_KK^{-1} A(K..K+b, c0..c0+nc), as a GEMM through W (copied back).
+cudaError_t row_solve(cublasHandle_t h, float* LU, const float* Dinv, float* W, int64_t n, int64_t K, int64_t c0,
+                      int64_t nc, cudaStream_t s) {
+    if (nc <= 0) return cudaSuccess;
+    const float one = 1.f, zero = 0.f;
+    int b = (int)std::min<int64_t>(NB, n - K);
+    const float* Li = Dinv + (K / NB) * 2 * NB * NB;
+    if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)nc, b, &one, Li, CUDA_R_32F, NB, LU + c0 * n + K,
+                     CUDA_R_32F, (int)n, &zero, W, CUDA_R_32F, b, lu_compute(), CUBLAS_GEMM_DEFAULT) !=
+        CUBLAS_STATUS_SUCCESS)
         return cudaErrorUnknown;
-    return cudaMemcpy2DAsync(LU + (K + b) * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), rest,
+    return cudaMemcpy2DAsync(LU + c0 * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), nc,
                              cudaMemcpyDeviceToDevice, s);
 }
 
@@ -261,18 +273,41 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
     return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
 }
 
-// Right-looking blocked LU: per block, the diagonal kernel, the two panel GEMMs, then
-// one trailing-update GEMM over the whole remaining matrix.  (Factoring the next
-// diagonal block on a side stream beside the trailing GEMM was measured slower here:
-// the split GEMMs cost more than the overlap recovered.)
+// Two-level right-looking blocked LU.  Inner blocks of NB columns are factored within an
+// outer panel of OB columns: per inner block the diagonal kernel, L21 for all rows
+// below, U12 and the trailing update only inside the outer panel (an (n - K) x < OB
+// update that stays in L2).  After the panel, its U rows right of it come from a
+// blocked forward substitution and the rest of the matrix from one rank-OB update, so the
+// large trailing matrix is read and written once per OB columns instead of once per NB.
+// (Factoring the next diagonal block on a side stream beside the trailing GEMM was
+// measured slower: the split GEMMs cost more than the overlap recovered.)
+// outer panel width: OB_BLOCKS inner blocks (CPG_LU_OUTER overrides, 1..16)
+constexpr int OB_BLOCKS = 8;
+int64_t outer_width() {
+    const char* e = std::getenv("CPG_LU_OUTER");
+    int k = e ? std::atoi(e) : OB_BLOCKS;
+    return (int64_t)NB * (k >= 1 && k <= 16 ? k : OB_BLOCKS);
+}
 cudaError_t factor_body(cublasHandle_t h, float* LU, float* Dinv, float* W, int64_t n, int* bad, cudaStream_t s) {
-    for (int64_t K = 0; K < n; K += NB) {
-        int b = (int)std::min<int64_t>(NB, n - K);
-        k_lu_diag<<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, Dinv, bad);
-        cudaError_t e = panel_gemms(h, LU, Dinv, W, n, K, s);
-        if (e != cudaSuccess) return e;
-        int64_t K1 = K + b, rest = n - K1;
-        if (rest > 0 && (e = trailing(h, LU, n, K, b, K1, rest, K1, rest)) != cudaSuccess) return e;
+    cudaError_t e;
+    const int64_t OB = outer_width();
+    for (int64_t KO = 0; KO < n; KO += OB) {
+        const int64_t KE = std::min<int64_t>(KO + OB, n);
+        for (int64_t K = KO; K < KE; K += NB) {
+            const int b = (int)std::min<int64_t>(NB, n - K);
+            k_lu_diag<<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, Dinv, bad);
+            if ((e = column_solve(h, LU, Dinv, W, n, K, s)) != cudaSuccess) return e;
+            const int64_t K1 = K + b;
+            if ((e = row_solve(h, LU, Dinv, W, n, K, K1, KE - K1, s)) != cudaSuccess) return e;
+            if ((e = trailing(h, LU, n, K, b, K1, n - K1, K1, KE - K1)) != cudaSuccess) return e;
+        }
+        if (KE >= n) break;
+        for (int64_t K = KO; K < KE; K += NB) {  // U(KO..KE, KE..n): forward substitution by blocks
+            const int b = (int)std::min<int64_t>(NB, n - K);
+            if ((e = row_solve(h, LU, Dinv, W, n, K, KE, n - KE, s)) != cudaSuccess) return e;
+            if ((e = trailing(h, LU, n, K, b, K + b, KE - K - b, KE, n - KE)) != cudaSuccess) return e;
+        }
+        if ((e = trailing(h, LU, n, KO, (int)(KE - KO), KE, n - KE, KE, n - KE)) != cudaSuccess) return e;
     }
     return cudaGetLastError();
 }

@@ -92,6 +92,9 @@ struct LuGraphs {
     const float* solve_X = nullptr;
     int solve_k = 0;
     void* workspace = nullptr;  // cuBLAS workspace (no allocation inside a capture)
+    void* workspace2 = nullptr; // cuBLAS workspace of the panel stream
+    cudaStream_t panel_stream = nullptr;  // high-priority stream of the panel factorizations
+    cudaEvent_t ev_update = nullptr, ev_panel = nullptr;  // fork / join inside the capture
     float* dinv = nullptr;      // inverses of the diagonal blocks (L then U per block)
     float* panel = nullptr;     // n x 128 staging for the panel GEMMs
     float* tmp = nullptr;       // n x k intermediate of the substitutions

@@ -279,8 +279,11 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
 // update that stays in L2).  After the panel, its U rows right of it come from a
 // blocked forward substitution and the rest of the matrix from one rank-OB update, so the
 // large trailing matrix is read and written once per OB columns instead of once per NB.
-// (Factoring the next diagonal block on a side stream beside the trailing GEMM was
-// measured slower: the split GEMMs cost more than the overlap recovered.)
+// Look-ahead: the rank-OB update is split into the next panel's columns and the rest;
+// the next panel is factored on a high-priority stream while the rest of the update
+// runs.  (Measured: about 1 ms of 56 on the 19k wing.  cuBLAS's large GEMM holds every
+// SM until it ends, and keeping 8-32 SMs out of it for the panel measured 0.6-5 ms
+// slower.)
 // outer panel width: OB_BLOCKS inner blocks (CPG_LU_OUTER overrides, 1..16)
 constexpr int OB_BLOCKS = 8;
 int64_t outer_width() {
@@ -288,27 +291,64 @@ int64_t outer_width() {
     int k = e ? std::atoi(e) : OB_BLOCKS;
     return (int64_t)NB * (k >= 1 && k <= 16 ? k : OB_BLOCKS);
 }
-cudaError_t factor_body(cublasHandle_t h, float* LU, float* Dinv, float* W, int64_t n, int* bad, cudaStream_t s) {
+
+struct Streams {  // where the next cuBLAS calls go
+    cublasHandle_t h;
+    cudaStream_t main, panel;
+    void *ws_main, *ws_panel;
+    cudaError_t use(bool on_panel) const {
+        if (cublasSetStream(h, on_panel ? panel : main) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+        if (cublasSetWorkspace(h, on_panel ? ws_panel : ws_main, kBlasWorkspace) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        return cudaSuccess;
+    }
+};
+
+// factorization of the outer panel [KO, KE) (on st.panel)
+cudaError_t factor_panel(const Streams& st, float* LU, float* Dinv, float* W, int64_t n, int* bad, int64_t KO,
+                         int64_t KE) {
+    cudaError_t e;
+    if ((e = st.use(true)) != cudaSuccess) return e;
+    for (int64_t K = KO; K < KE; K += NB) {
+        const int b = (int)std::min<int64_t>(NB, n - K);
+        k_lu_diag<<<1, DT, DIAG_SMEM, st.panel>>>(LU, n, K, b, Dinv, bad);
+        if ((e = column_solve(st.h, LU, Dinv, W, n, K, st.panel)) != cudaSuccess) return e;
+        const int64_t K1 = K + b;
+        if ((e = row_solve(st.h, LU, Dinv, W, n, K, K1, KE - K1, st.panel)) != cudaSuccess) return e;
+        if ((e = trailing(st.h, LU, n, K, b, K1, n - K1, K1, KE - K1)) != cudaSuccess) return e;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t factor_body(const Streams& st, LuGraphs* G, float* LU, float* Dinv, float* W, int64_t n, int* bad) {
     cudaError_t e;
     const int64_t OB = outer_width();
+    // first panel
+    if ((e = cudaEventRecord(G->ev_update, st.main)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st.panel, G->ev_update, 0)) != cudaSuccess) return e;
+    if ((e = factor_panel(st, LU, Dinv, W, n, bad, 0, std::min<int64_t>(OB, n))) != cudaSuccess) return e;
     for (int64_t KO = 0; KO < n; KO += OB) {
         const int64_t KE = std::min<int64_t>(KO + OB, n);
-        for (int64_t K = KO; K < KE; K += NB) {
-            const int b = (int)std::min<int64_t>(NB, n - K);
-            k_lu_diag<<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, Dinv, bad);
-            if ((e = column_solve(h, LU, Dinv, W, n, K, s)) != cudaSuccess) return e;
-            const int64_t K1 = K + b;
-            if ((e = row_solve(h, LU, Dinv, W, n, K, K1, KE - K1, s)) != cudaSuccess) return e;
-            if ((e = trailing(h, LU, n, K, b, K1, n - K1, K1, KE - K1)) != cudaSuccess) return e;
-        }
+        // this panel done (the main stream has finished the rest of the previous update)
+        if ((e = cudaEventRecord(G->ev_panel, st.panel)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st.main, G->ev_panel, 0)) != cudaSuccess) return e;
         if (KE >= n) break;
+        if ((e = st.use(false)) != cudaSuccess) return e;
         for (int64_t K = KO; K < KE; K += NB) {  // U(KO..KE, KE..n): forward substitution by blocks
             const int b = (int)std::min<int64_t>(NB, n - K);
-            if ((e = row_solve(h, LU, Dinv, W, n, K, KE, n - KE, s)) != cudaSuccess) return e;
-            if ((e = trailing(h, LU, n, K, b, K + b, KE - K - b, KE, n - KE)) != cudaSuccess) return e;
+            if ((e = row_solve(st.h, LU, Dinv, W, n, K, KE, n - KE, st.main)) != cudaSuccess) return e;
+            if ((e = trailing(st.h, LU, n, K, b, K + b, KE - K - b, KE, n - KE)) != cudaSuccess) return e;
         }
-        if ((e = trailing(h, LU, n, KO, (int)(KE - KO), KE, n - KE, KE, n - KE)) != cudaSuccess) return e;
+        const int64_t KE2 = std::min<int64_t>(KE + OB, n);
+        // rank-OB update of the next panel's columns, then the next panel on its stream
+        // beside the update of the remaining columns
+        if ((e = trailing(st.h, LU, n, KO, (int)(KE - KO), KE, n - KE, KE, KE2 - KE)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(G->ev_update, st.main)) != cudaSuccess) return e;
+        if ((e = trailing(st.h, LU, n, KO, (int)(KE - KO), KE, n - KE, KE2, n - KE2)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(st.panel, G->ev_update, 0)) != cudaSuccess) return e;
+        if ((e = factor_panel(st, LU, Dinv, W, n, bad, KE, KE2)) != cudaSuccess) return e;
     }
+    if ((e = st.use(false)) != cudaSuccess) return e;
     return cudaGetLastError();
 }
 
@@ -347,7 +387,7 @@ cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int
 
 // Capture body() on s into a graph (no profiler events inside the capture).
 template <class F>
-cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body) {
+cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body, unsigned long long flags = 0) {
     Prof* saved = g_prof;
     g_prof = nullptr;
     cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
@@ -364,7 +404,7 @@ cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body) {
         return eb;
     }
     if (e != cudaSuccess) return e;
-    e = cudaGraphInstantiate(out, graph, 0);
+    e = cudaGraphInstantiateWithFlags(out, graph, flags);
     cudaGraphDestroy(graph);
     return e;
 }
@@ -375,6 +415,13 @@ void LuGraphs::release() {
     if (factor) cudaGraphExecDestroy(factor);
     if (solve) cudaGraphExecDestroy(solve);
     if (workspace) cudaFree(workspace);
+    if (workspace2) cudaFree(workspace2);
+    if (panel_stream) cudaStreamDestroy(panel_stream);
+    if (ev_update) cudaEventDestroy(ev_update);
+    if (ev_panel) cudaEventDestroy(ev_panel);
+    workspace2 = nullptr;
+    panel_stream = nullptr;
+    ev_update = ev_panel = nullptr;
     if (dinv) cudaFree(dinv);
     if (panel) cudaFree(panel);
     if (tmp) cudaFree(tmp);
@@ -401,7 +448,18 @@ cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* b
         size_t nb = (size_t)((n + NB - 1) / NB);
         if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&G->panel, sizeof(float) * (size_t)n * NB)) != cudaSuccess) return e;
-        e = capture(s, &G->factor, [&] { return factor_body(h, LU, G->dinv, G->panel, n, bad, s); });
+        if (!G->panel_stream) {
+            int least = 0, greatest = 0;
+            cudaDeviceGetStreamPriorityRange(&least, &greatest);
+            if ((e = cudaStreamCreateWithPriority(&G->panel_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
+                return e;
+            if ((e = cudaEventCreateWithFlags(&G->ev_update, cudaEventDisableTiming)) != cudaSuccess) return e;
+            if ((e = cudaEventCreateWithFlags(&G->ev_panel, cudaEventDisableTiming)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&G->workspace2, kBlasWorkspace)) != cudaSuccess) return e;
+        }
+        const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
+        e = capture(s, &G->factor, [&] { return factor_body(st, G, LU, G->dinv, G->panel, n, bad); },
+                    cudaGraphInstantiateFlagUseNodePriority);
         if (e != cudaSuccess) return e;
         G->factor_LU = LU;
         G->factor_n = n;

@@ -379,6 +379,27 @@ def vortex_particles(steps=20):
         "operators_40k_particles": ops}}
 
 
+def vp_loop_only(precision, steps):
+    """The config-4 loop alone (profiling aid): case creation, 3 steps, `steps` timed steps."""
+    import torch
+
+    from cpanel_gb300 import vp, wing
+    spec = wing.WingSpec(m=0.04, p=0.4, t=0.12, root_chord=1.0, span=6 * (1 + 0.6) / 2, taper=0.6, sweep_deg=0.0,
+                         n_chord=80, n_span=26, wake_len=30.0, wake_dir=(1.0, 0.0, 0.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    S = vp.VPCase(nodes, tris[keep], ids[keep], V=1.0, alpha=8.0, dt=0.05, accelerate=True, Sref=info["area"],
+                  precision=precision)
+    S.step(3)
+    torch.cuda.synchronize()
+    ms = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        S.step(1)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    print(json.dumps({"vp_loop": precision, "ms_per_step": [round(t, 2) for t in ms], "info": S.info()}))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -412,9 +433,14 @@ def main():
     ap.add_argument("--workload", default="multi_rhs", choices=["multi_rhs", "mid"])
     ap.add_argument("--no-serving", action="store_true", help="skip the batched (config 3) and served (config 5) runs")
     ap.add_argument("--no-vp", action="store_true", help="skip the vortex-particle sample (config 4)")
+    ap.add_argument("--vp-loop", choices=["plain", "mixed"],
+                    help="only the config-4 vortex-particle loop in this precision: 3 steps, then --steps timed "
+                         "steps (one JSON line; for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.vp_loop:
+        return vp_loop_only(args.vp_loop, args.steps)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -95,8 +95,8 @@ __device__ __forceinline__ dv3 warp_sum3(dv3 v) {  // fixed butterfly: determini
     return v;
 }
 
-// one warp per point: lanes share the quads and filaments, lane 0 adds the body chunks
-// in order and the warp's sum
+// one warp per point: lanes share the body chunks' partial sums and the quads and
+// filaments, each set reduced by a fixed butterfly
 __global__ void k_vp_panel_vel_fin(const double* __restrict__ part, int64_t nchunk, const double* __restrict__ q1,
                                    const double* __restrict__ mu1, int64_t n1, const double* __restrict__ q2,
                                    const double* __restrict__ mu2, int64_t n2, const double* __restrict__ fil,
@@ -122,11 +122,13 @@ __global__ void k_vp_panel_vel_fin(const double* __restrict__ part, int64_t nchu
             acc = acc + (f[6] * vortex_v(poi - p1, poi - p2, p2 - p1)) / CPG_FOUR_PI;
         }
     }
+    // body chunks: lane l adds chunks l, l+32, ... (then the same butterfly)
+    dv3 body = mk3(0, 0, 0);
+    for (int64_t c = lane; c < nchunk; c += 32) body = body + ld3(part + (c * m + q) * 3);
+    body = warp_sum3(body);
     acc = warp_sum3(acc);
     if (lane != 0) return;
-    dv3 tot = mk3(0, 0, 0);
-    for (int64_t c = 0; c < nchunk; c++) tot = tot + ld3(part + (c * m + q) * 3);
-    tot = tot + acc;
+    const dv3 tot = body + acc;
     out[3 * q] = tot.x;
     out[3 * q + 1] = tot.y;
     out[3 * q + 2] = tot.z;
@@ -429,11 +431,13 @@ __global__ void k_vp_stretch_fin(const double* __restrict__ part, int64_t nchunk
                     : vel_grad_doublet(w, 4, c, ld3(w + Q_N), ld3(w + Q_L), ld3(w + Q_M), w[Q_LONG], mu1[j], x);
         acc = acc + mul_m3(G, a);
     }
+    // body chunks: lane l adds chunks l, l+32, ... (then the same butterfly)
+    dv3 body = mk3(0, 0, 0);
+    for (int64_t c = lane; c < nchunk; c += 32) body = body + ld3(part + (c * m + q) * 3);
+    body = warp_sum3(body);
     acc = warp_sum3(acc);
     if (lane != 0) return;
-    dv3 tot = mk3(0, 0, 0);
-    for (int64_t c = 0; c < nchunk; c++) tot = tot + ld3(part + (c * m + q) * 3);
-    tot = tot + acc;
+    const dv3 tot = body + acc;
     out[3 * q] = tot.x;
     out[3 * q + 1] = tot.y;
     out[3 * q + 2] = tot.z;

@@ -85,6 +85,7 @@ struct cpg_geometry {
     cpg::HostMesh H;
     DevBuf rec, frec, bez, clp, cli, tip, ts, wrec, widx, wcoef, tzst, tzln, tzpts, G, F3, F2, mode;
     DevBuf order;  // block schedule of the mixed assembly
+    DevBuf erec;   // FP64 edge constants of the mixed near field
     int64_t order_n = -1;
     DevBuf A64, B64, A32, Alo, rb, count;
     DevBuf LU, bad;
@@ -330,8 +331,25 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
             split(1.0 / S, o + 58 + 2 * k, o + 59 + 2 * k);
         }
     }
+    // FP64 edge constants of the mixed near field: |s_k|, 1/|s_k|, s_k.m (E_STRIDE = 12 per panel),
+    // rounded exactly as the device would form them (no contraction in this file)
+    std::vector<double> er(n * 12, 0.0);
+    for (int64_t i = 0; i < n; i++) {
+        const double* r = &H.body[i * cpg::PF_STRIDE];
+        const double* m = r + cpg::PF_M;
+        for (int k = 0; k < 3; k++) {
+            const double* v = r + cpg::PF_V0 + 3 * k;
+            const double* w = r + cpg::PF_V0 + 3 * ((k + 1) % 3);
+            const double sx = w[0] - v[0], sy = w[1] - v[1], sz = w[2] - v[2];
+            const double S = std::sqrt(sx * sx + sy * sy + sz * sz);
+            er[i * 12 + k] = S;
+            er[i * 12 + 3 + k] = 1 / S;
+            er[i * 12 + 6 + k] = sx * m[0] + sy * m[1] + sz * m[2];
+        }
+    }
     cudaError_t e;
     if ((e = upload(g->rec, H.body, s)) != cudaSuccess || (e = upload(g->frec, fr, s)) != cudaSuccess ||
+        (e = upload(g->erec, er, s)) != cudaSuccess ||
         (e = upload(g->bez, H.bez, s)) != cudaSuccess || (e = upload(g->clp, H.cl_ptr, s)) != cudaSuccess ||
         (e = upload(g->cli, H.cl_idx, s)) != cudaSuccess || (e = upload(g->tip, H.tip, s)) != cudaSuccess ||
         (e = upload(g->ts, H.tsorder, s)) != cudaSuccess || (e = upload(g->wrec, H.wake, s)) != cudaSuccess ||
@@ -350,7 +368,7 @@ void cpg_geometry_destroy(cpg_geometry* g) {
     DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
                       &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
                       &g->B64, &g->A32, &g->Alo, &g->rb, &g->LU, &g->bad, &g->count, &g->work, &g->post_work, &g->cases, &g->outs,
-                      &g->order};
+                      &g->order, &g->erec};
     // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
     g->graphs.release();
@@ -456,7 +474,8 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
             CK(upload(g->order, ord, s), "upload block order");
             g->order_n = n;
         }
-        CK(cpg::launch_assemble_mixed(g->rec.as<double>(), g->frec.as<float>(), n, g->wrec.as<double>(),
+        CK(cpg::launch_assemble_mixed(g->rec.as<double>(), g->frec.as<float>(), g->erec.as<double>(), n,
+                                      g->wrec.as<double>(),
                                       g->widx.as<int32_t>(), g->wcoef.as<double>(), g->H.n_wake, g->order.as<int>(),
                                       g->A32.as<float>(), g->Alo.as<float>(), g->rb.as<double>(), g->rb.as<double>() + 3 * n,
                                       g->count.as<unsigned long long>(), s),

@@ -158,7 +158,8 @@ __device__ __noinline__ BandPhi band_phi_df(df32 d0, df32 d1, df32 d2, const flo
 // then adds its own queued results in queue order (the same order on every run).
 constexpr int WARPS_PER_BLOCK = TI / 32;
 __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restrict__ rec,
-                                                          const float* __restrict__ frec, int64_t n, int64_t jchunk,
+                                                          const float* __restrict__ frec,
+                                                          const double* __restrict__ erec, int64_t n, int64_t jchunk,
                                                           const int* __restrict__ order, float* __restrict__ A32,
                                                           float* __restrict__ Alo, double* __restrict__ rbp,
                                                           unsigned long long* __restrict__ near_count) {
@@ -167,6 +168,7 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
     const int64_t bx = order[2 * blockIdx.x], by = order[2 * blockIdx.x + 1];
     __shared__ double s_rec[TJ * R_STRIDE];
     __shared__ float s_f[TJ * F_STRIDE];
+    __shared__ double s_e[TJ * E_STRIDE];
     __shared__ unsigned short s_q[WARPS_PER_BLOCK][TJ * 32];  // (tile index << 5) | lane
     __shared__ double s_res[WARPS_PER_BLOCK][32][3];
     __shared__ int s_own[WARPS_PER_BLOCK][32];
@@ -194,6 +196,10 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
         for (int t = threadIdx.x; t < TJ * F_STRIDE; t += blockDim.x) {
             int64_t j = j0 + t / F_STRIDE;
             s_f[t] = j < n ? frec[j0 * F_STRIDE + t] : 0.f;
+        }
+        for (int t = threadIdx.x; t < TJ * E_STRIDE; t += blockDim.x) {
+            int64_t j = j0 + t / E_STRIDE;
+            s_e[t] = j < n ? erec[j0 * E_STRIDE + t] : 0.0;
         }
         __syncthreads();
         int cnt = (int)min((int64_t)TJ, je - j0);
@@ -260,7 +266,7 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
                 const double* r = s_rec + tt * R_STRIDE;
                 const dv3 pe = mk3(s_poi[w][ln][0], s_poi[w][ln][1], s_poi[w][ln][2]);
                 double src = 0, dub = 0;
-                panel_phi_inf(r, pe, src, dub);
+                panel_phi_inf_pre(r, s_e + tt * E_STRIDE, pe, src, dub);
                 const int64_t ie = iw + ln, je_ = j0 + tt;
                 float hi = (float)dub;
                 A32[je_ * n + ie] = hi;
@@ -535,15 +541,16 @@ void mixed_block_order(int64_t n, std::vector<int>& out) {
     }
 }
 
-cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
-                                  const int32_t* widx, const double* wcoef, int64_t nw, const int* order, float* A32,
-                                  float* Alo, double* rb, double* rb_part, unsigned long long* near_count,
-                                  cudaStream_t s) {
+cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const double* erec, int64_t n,
+                                  const double* wrec, const int32_t* widx, const double* wcoef, int64_t nw,
+                                  const int* order, float* A32, float* Alo, double* rb, double* rb_part,
+                                  unsigned long long* near_count, cudaStream_t s) {
     int64_t ch = chunk_for(n);
     const int64_t nbx = (n + TI - 1) / TI, nby = (n + ch - 1) / ch;
     {
         ProfScope ps(Prof::ASSEMBLE, s);
-        k_assemble_mixed<<<(unsigned)(nbx * nby), TI, 0, s>>>(rec, frec, n, ch, order, A32, Alo, rb_part, near_count);
+        k_assemble_mixed<<<(unsigned)(nbx * nby), TI, 0, s>>>(rec, frec, erec, n, ch, order, A32, Alo, rb_part,
+                                                              near_count);
         k_rb_reduce<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(rb_part, n, nby, rb);
     }
     if (nw > 0) {

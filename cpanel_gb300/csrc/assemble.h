@@ -43,11 +43,13 @@ struct ProfScope {
 cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wrec, const int32_t* widx,
                                  const double* wcoef, int64_t nw, double* A, double* B,
                                  unsigned long long* near_count, cudaStream_t s);
-// order: mixed_block_order(n) on the device (2 ints per block: row block, source chunk)
-cudaError_t launch_assemble_mixed(const double* rec, const float* frec, int64_t n, const double* wrec,
-                                  const int32_t* widx, const double* wcoef, int64_t nw, const int* order, float* A32,
-                                  float* Alo, double* rb, double* rb_part, unsigned long long* near_count,
-                                  cudaStream_t s);
+// order: mixed_block_order(n) on the device (2 ints per block: row block, source chunk);
+// erec: per-panel FP64 edge constants of the near field (E_STRIDE doubles per body panel:
+// |s_k|, 1/|s_k|, s_k.m with s_k = v_{k+1} - v_k, rounded as the device rounds them)
+cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const double* erec, int64_t n,
+                                  const double* wrec, const int32_t* widx, const double* wcoef, int64_t nw,
+                                  const int* order, float* A32, float* Alo, double* rb, double* rb_part,
+                                  unsigned long long* near_count, cudaStream_t s);
 // block schedule of the mixed assembly: blocks sorted by the distance between their row
 // and source index ranges (near-field-heavy blocks first)
 void mixed_block_order(int64_t n, std::vector<int>& out);

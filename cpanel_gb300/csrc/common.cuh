@@ -33,4 +33,8 @@ enum {
     F_VC = 16, F_NS = 34, F_S = 52, F_IS = 58, F_STRIDE = 64
 };
 
+// Per-panel FP64 edge constants of the mixed assembly's near field:
+// [|s_k| (3), 1/|s_k| (3), s_k.m (3), pad (3)] with s_k = v_{k+1} - v_k.
+enum { E_S = 0, E_IS = 3, E_SM = 6, E_STRIDE = 12 };
+
 #define CPG_CUDA_OK(x) ((x) == cudaSuccess)

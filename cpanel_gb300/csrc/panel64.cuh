@@ -63,6 +63,52 @@ __device__ __forceinline__ int panel_phi_inf(const double* r, dv3 poi, double& p
     return 1;
 }
 
+// panel_phi_inf for a near pair with the panel's per-edge constants precomputed (ec: |s_k|,
+// 1/|s_k|, s_k.m for k = 0..2, computed on the host with the same rounded operations) and
+// the three vertex distances formed once per pair (edge k's |b| is edge k+1's |a|).  Every
+// value, and so every branch, equals panel_phi_inf's; only repeated work is gone.
+__device__ __forceinline__ void panel_phi_inf_pre(const double* r, const double* ec, dv3 poi, double& phiSrc,
+                                                  double& phiDub) {
+    dv3 c = ld3(r + R_C);
+    dv3 pjk = poi - c;
+    double d = norm3(pjk);
+    bool itself = d < 1e-10;
+    dv3 n = ld3(r + R_N);
+    double PN = dot3(pjk, n);
+    dv3 l = ld3(r + R_L);
+    dv3 p[3] = {ld3(r + R_V0), ld3(r + R_V1), ld3(r + R_V2)};
+    dv3 av[3] = {poi - p[0], poi - p[1], poi - p[2]};
+    double dn[3] = {norm3(av[0]), norm3(av[1]), norm3(av[2])};
+    double src = 0, dub = 0, phiV = 0;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const int i2 = i == 2 ? 0 : i + 1;
+        dv3 a = av[i], s = p[i2] - p[i];
+        double Al = dot3(n, cross3(s, a));
+        const double na = dn[i], nb = dn[i2];
+        if (!itself) {  // vortex_phi with sm and the norms supplied
+            const double eps = 1e-15;
+            double PA = dot3(a, cross3(l, cross3(a, s)));
+            double sm = ec[6 + i];
+            double PB = PA - Al * sm;
+            double num = sm * PN * (nb * PA - na * PB);
+            double denom = PA * PB + (PN * PN) * na * nb * (sm * sm);
+            if (denom == 0.0 && fabs(PN) < eps)
+                phiV = PN >= 0 ? 0.5 * CPG_PI : -0.5 * CPG_PI;
+            else
+                phiV = atan2(num, denom);
+            dub += phiV;
+        }
+        // src_gl with S and 1/S supplied
+        const double S = ec[i];
+        double GL = 0;
+        if (fabs(na + nb - S) > 0 && S > 0) GL = ec[3 + i] * log(fabs((na + nb + S) / (na + nb - S)));
+        src += Al * GL - PN * phiV;
+    }
+    phiSrc = src / CPG_FOUR_PI;
+    phiDub = itself ? -0.5 : dub / CPG_FOUR_PI;
+}
+
 // panel::dubPhiInf, CPanel/panel.cpp:208-252
 __device__ __forceinline__ double dub_phi_inf(const double* r, dv3 poi) {
     dv3 c = ld3(r + R_C);

@@ -37,9 +37,10 @@ constexpr int DIAG_SMEM = (3 * NB * P + 6 * BS * TP) * 4;
 // LU: 128 right-looking steps, thread t owning row t % 128 and every fourth column;
 // step j reads column j and row j and writes only past them, and the multiplier of
 // column j is stored one step later, when nothing reads column j.
-// Inverses: the eight 32 x 32 diagonal blocks first (right-looking; U as the unit
-// upper factor of U scaled by its diagonal, then the columns divided by it), then the
-// off-diagonal blocks by distance d = 1..3 from the diagonal:
+// Inverses: the eight 32 x 32 diagonal blocks first, one warp each with a column per
+// lane in registers (right-looking; U as the unit upper factor of U scaled by its
+// diagonal, then the columns divided by it), then the off-diagonal blocks by distance
+// d = 1..3 from the diagonal:
 // Linv[I][J] = -Linv[I][I] sum_{K=J}^{I-1} L[I][K] Linv[K][J] and
 // Uinv[I][J] = -Uinv[I][I] sum_{K=I+1}^{J} U[I][K] Uinv[K][J].
 __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
@@ -88,29 +89,43 @@ __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n
         }
         __syncthreads();
     }
-    // ---- inverses of the 32 x 32 diagonal blocks (L: k ascending; U: unit-scaled, k descending)
-    for (int st = 0; st < BS; st++) {
-        const int kL = st, kU = BS - 1 - st;
-        const int eL = (BS - 1 - kL) * (kL + 1), eU = kU * (BS - kU);
-        for (int w = t; w < 4 * (eL + eU); w += DT) {
-            if (w < 4 * eL) {
-                const int o = BS * (w / eL), ww = w % eL;
-                const int i = kL + 1 + ww / (kL + 1), c = ww % (kL + 1);
-                ZL[(o + i) * P + o + c] =
-                    __fmaf_rn(-S[(o + i) * P + o + kL], ZL[(o + kL) * P + o + c], ZL[(o + i) * P + o + c]);
-            } else {
-                const int w2 = w - 4 * eL;
-                const int o = BS * (w2 / eU), ww = w2 % eU;
-                const int i = ww / (BS - kU), c = kU + ww % (BS - kU);
-                ZU[(o + i) * P + o + c] = __fmaf_rn(-(S[(o + i) * P + o + kU] / S[(o + i) * P + o + i]),
-                                                    ZU[(o + kU) * P + o + c], ZU[(o + i) * P + o + c]);
+    // ---- inverses of the 32 x 32 diagonal blocks, one warp each (warps 0-3: L, 4-7: U);
+    // lane c holds column c.  L: right-looking over k.  U: the unit upper factor of U
+    // (rows scaled by the diagonal, staged in Tb) inverted from the last column back,
+    // then the columns divided by the diagonal.
+    {
+        const int w = t >> 5, c = t & 31;
+        if (w < 4) {
+            const int o = BS * w;
+            float x[32];
+#pragma unroll
+            for (int i = 0; i < 32; i++) x[i] = i == c ? 1.f : 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; k++) {
+                const float xk = x[k];
+#pragma unroll
+                for (int i = k + 1; i < 32; i++) x[i] = __fmaf_rn(-S[(o + i) * P + o + k], xk, x[i]);
             }
+#pragma unroll
+            for (int i = 0; i < 32; i++) ZL[(o + i) * P + o + c] = x[i];
+        } else if (w < 8) {
+            const int o = BS * (w - 4);
+            float* Us = Tb + 2 * NB + (w - 4) * BS * TP;  // Us[i * TP + k] = S[i][k] / S[i][i]
+            for (int i = 0; i < 32; i++) Us[i * TP + c] = S[(o + i) * P + o + c] / S[(o + i) * P + o + i];
+            __syncwarp();
+            float y[32];
+#pragma unroll
+            for (int i = 0; i < 32; i++) y[i] = i == c ? 1.f : 0.f;
+#pragma unroll
+            for (int k = 31; k >= 0; k--) {
+                const float yk = y[k];
+#pragma unroll
+                for (int i = 0; i < k; i++) y[i] = __fmaf_rn(-Us[i * TP + k], yk, y[i]);
+            }
+            const float dc = S[(o + c) * P + o + c];
+#pragma unroll
+            for (int i = 0; i < 32; i++) ZU[(o + i) * P + o + c] = i <= c ? y[i] / dc : y[i];
         }
-        __syncthreads();
-    }
-    for (int w = t; w < 4 * BS * BS; w += DT) {  // U: divide the columns by the diagonal
-        const int o = BS * (w / (BS * BS)), i = (w % (BS * BS)) / BS, c = w % BS;
-        if (c >= i) ZU[(o + i) * P + o + c] = ZU[(o + i) * P + o + c] / S[(o + c) * P + o + c];
     }
     __syncthreads();
     // ---- off-diagonal blocks, by distance from the diagonal

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <thread>
 #include <unordered_map>
 
 namespace cpg {
@@ -266,6 +267,8 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
     // createSurfaces, CPanel/geometry.cpp:712-747
     std::vector<std::vector<int>> surfPans;
     B.pan.reserve(nt);
+    B.E.reserve(2 * nt + 16);
+    B.emap.reserve(2 * nt + 16);
     for (int64_t i = 0; i < nt; i++) {
         Panel p;
         for (int k = 0; k < 3; k++) p.nd[k] = (int)conn[3 * i + k];
@@ -379,8 +382,10 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
         }
         p.tip = count >= 2;
     }
-    // bodyPanel::setCluster / clusterTest, CPanel/bodyPanel.cpp:402-487,617-640
-    for (int self : bp) {
+    // bodyPanel::setCluster / clusterTest, CPanel/bodyPanel.cpp:402-487,617-640.  Each panel's
+    // cluster depends only on the (fixed) panel data, so the panels are split over host
+    // threads; the first failing panel in matrix order is reported, as a sequential loop would.
+    auto cluster_of = [&](int self) -> int {  // 0 ok, 1 no neighbourhood, 2 too large
         Panel& p = B.pan[self];
         int dim = p.tip ? 2 : 3;
         size_t buffer = 10;
@@ -390,10 +395,11 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
         p.cluster.push_back(self);
         bool upF = p.upper, loF = p.lower;
         auto inCluster = [&](int q) { return std::find(p.cluster.begin(), p.cluster.end(), q) != p.cluster.end(); };
+        std::vector<int> add;
         while (p.cluster.size() < nP) {
-            std::vector<int> add;
+            add.clear();
             for (size_t i = old; i < p.cluster.size(); i++) {
-                const std::vector<int> nb = B.pan[p.cluster[i]].nbr;
+                const std::vector<int>& nb = B.pan[p.cluster[i]].nbr;
                 for (int q : nb) {
                     const Panel& o = B.pan[q];
                     bool ok = !((upF && o.lower) || (loF && o.upper)) && p.tip == o.tip;
@@ -425,8 +431,25 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
                 if (p.cluster.size() == nP + 1) break;
             }
         }
-        if (p.ts < 1 || p.cluster.size() < 2) return "a body panel has no usable CHTLS neighbourhood";
-        if (p.cluster.size() > 32) return "CHTLS cluster larger than 32 panels";
+        if (p.ts < 1 || p.cluster.size() < 2) return 1;
+        if (p.cluster.size() > 32) return 2;
+        return 0;
+    };
+    {
+        const size_t np = bp.size();
+        std::vector<int> status(np, 0);
+        unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        if (np < 2048) nth = 1;
+        std::vector<std::thread> pool;
+        for (unsigned w = 0; w < nth; w++)
+            pool.emplace_back([&, w] {
+                for (size_t i = w; i < np; i += nth) status[i] = cluster_of(bp[i]);
+            });
+        for (auto& th : pool) th.join();
+        for (size_t i = 0; i < np; i++) {
+            if (status[i] == 1) return "a body panel has no usable CHTLS neighbourhood";
+            if (status[i] == 2) return "CHTLS cluster larger than 32 panels";
+        }
     }
 
     // ---- flatten ----
@@ -443,7 +466,9 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
     H.surf_id.resize(H.n_body);
     H.file_tri.resize(H.n_body);
     H.cl_ptr.assign(1, 0);
+    H.cl_ptr.reserve(H.n_body + 1);
     H.cl_idx.clear();
+    H.cl_idx.reserve(H.n_body * 16);
     H.n_tip = 0;
     auto pack = [&](const Panel& p, double* o) {
         for (int k = 0; k < 3; k++) {

@@ -84,11 +84,10 @@ double measure_fp64_tflops(cudaStream_t s);
 cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, double* dd, double* host, cudaStream_t s);
 
 // lu.cu: FP32 LU without pivoting (blocked, cuBLAS trailing GEMM) and the refined
-// solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.  The blocked
-// loops are captured once into CUDA graphs held in LuGraphs and replayed.
+// solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.  The substitutions
+// are captured once into a CUDA graph held in LuGraphs and replayed.
 struct LuGraphs {
-    cudaGraphExec_t factor = nullptr, solve = nullptr;
-    const float* factor_LU = nullptr;
+    cudaGraphExec_t solve = nullptr;
     int64_t factor_n = 0;
     const float* solve_LU = nullptr;
     const float* solve_X = nullptr;

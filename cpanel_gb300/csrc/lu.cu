@@ -427,7 +427,6 @@ cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body, unsigned long 
 }  // namespace
 
 void LuGraphs::release() {
-    if (factor) cudaGraphExecDestroy(factor);
     if (solve) cudaGraphExecDestroy(solve);
     if (workspace) cudaFree(workspace);
     if (workspace2) cudaFree(workspace2);
@@ -440,47 +439,46 @@ void LuGraphs::release() {
     if (dinv) cudaFree(dinv);
     if (panel) cudaFree(panel);
     if (tmp) cudaFree(tmp);
-    factor = solve = nullptr;
+    solve = nullptr;
     workspace = nullptr;
     dinv = panel = tmp = nullptr;
     tmp_floats = 0;
     solve_X = nullptr;
     solve_k = 0;
-    factor_LU = nullptr;
+    factor_n = 0;
 }
 
+// Launched directly (not from a graph): a geometry is factored once, and its ~3,000
+// launches are each longer than their host-side cost, so a captured graph would only
+// add the capture and instantiation to every new geometry.
 cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s) {
     set_attrs();
     cublasHandle_t h = (cublasHandle_t)blas;
     cudaError_t e = prepare_blas(h, G, s);
     if (e != cudaSuccess) return e;
-    if (!G->factor || G->factor_LU != LU || G->factor_n != n) {
-        if (G->factor) cudaGraphExecDestroy(G->factor);
-        G->factor = nullptr;
+    if (G->factor_n != n || !G->dinv) {
+        if (G->solve) cudaGraphExecDestroy(G->solve);  // it holds the old Dinv
+        G->solve = nullptr;
         if (G->dinv) cudaFree(G->dinv);
         if (G->panel) cudaFree(G->panel);
         G->dinv = G->panel = nullptr;
         size_t nb = (size_t)((n + NB - 1) / NB);
         if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&G->panel, sizeof(float) * (size_t)n * NB)) != cudaSuccess) return e;
-        if (!G->panel_stream) {
-            int least = 0, greatest = 0;
-            cudaDeviceGetStreamPriorityRange(&least, &greatest);
-            if ((e = cudaStreamCreateWithPriority(&G->panel_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
-                return e;
-            if ((e = cudaEventCreateWithFlags(&G->ev_update, cudaEventDisableTiming)) != cudaSuccess) return e;
-            if ((e = cudaEventCreateWithFlags(&G->ev_panel, cudaEventDisableTiming)) != cudaSuccess) return e;
-            if ((e = cudaMalloc(&G->workspace2, kBlasWorkspace)) != cudaSuccess) return e;
-        }
-        const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
-        e = capture(s, &G->factor, [&] { return factor_body(st, G, LU, G->dinv, G->panel, n, bad); },
-                    cudaGraphInstantiateFlagUseNodePriority);
-        if (e != cudaSuccess) return e;
-        G->factor_LU = LU;
         G->factor_n = n;
     }
+    if (!G->panel_stream) {
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        if ((e = cudaStreamCreateWithPriority(&G->panel_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
+            return e;
+        if ((e = cudaEventCreateWithFlags(&G->ev_update, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if ((e = cudaEventCreateWithFlags(&G->ev_panel, cudaEventDisableTiming)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&G->workspace2, kBlasWorkspace)) != cudaSuccess) return e;
+    }
+    const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
     ProfScope ps(Prof::LU_FACTOR, s);
-    return cudaGraphLaunch(G->factor, s);
+    return factor_body(st, G, LU, G->dinv, G->panel, n, bad);
 }
 
 // X (n x k, ld n) <- U^{-1} L^{-1} X

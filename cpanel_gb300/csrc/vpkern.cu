@@ -264,6 +264,48 @@ __device__ __forceinline__ bool far_pair(const PtF& p, const float* __restrict__
     return norm3(poi - ld3(r + R_C)) / r[R_LONG] > 5;  // the FP64 test of panel_v_inf / stretching
 }
 
+// Per-warp queue of the FP64 near pairs of one panel tile: entries (panel << 5) | lane in
+// tile order, then lane order; the warp evaluates them one per lane and each target adds
+// its own results in queue order (the same order on every run).
+struct NearQueue {
+    unsigned short q[VT / 32][TILE * 32];
+    double tgt[VT / 32][32][6];  // the warp's targets: position, strength
+    double res[VT / 32][32][3];
+    int own[VT / 32][32];
+    __device__ __forceinline__ void put_target(int w, int lane, dv3 x, dv3 a) {
+        tgt[w][lane][0] = x.x; tgt[w][lane][1] = x.y; tgt[w][lane][2] = x.z;
+        tgt[w][lane][3] = a.x; tgt[w][lane][4] = a.y; tgt[w][lane][5] = a.z;
+    }
+    __device__ __forceinline__ dv3 tx(int w, int ln) const { return mk3(tgt[w][ln][0], tgt[w][ln][1], tgt[w][ln][2]); }
+    __device__ __forceinline__ dv3 ta(int w, int ln) const { return mk3(tgt[w][ln][3], tgt[w][ln][4], tgt[w][ln][5]); }
+    // all lanes call; returns the new (warp-uniform) length
+    __device__ __forceinline__ int push(int w, int lane, bool near, int k, int qn) {
+        const unsigned m = __ballot_sync(0xffffffffu, near);
+        if (near) q[w][qn + __popc(m & ((1u << lane) - 1u))] = (unsigned short)((k << 5) | lane);
+        return qn + __popc(m);
+    }
+    __device__ __forceinline__ bool take(int w, int e, int qn, int& k, int& ln) const {
+        if (e >= qn) return false;
+        const int ent = q[w][e];
+        k = ent >> 5;
+        ln = ent & 31;
+        return true;
+    }
+    __device__ __forceinline__ void put_result(int w, int lane, int ln, dv3 v) {
+        res[w][lane][0] = v.x; res[w][lane][1] = v.y; res[w][lane][2] = v.z;
+        own[w][lane] = ln;
+    }
+    // all lanes call after their take/put_result: adds this chunk's results to their owners
+    __device__ __forceinline__ dv3 gather(int w, int lane, int base, int qn, dv3 acc) {
+        __syncwarp();
+        const int cnt = min(32, qn - base);
+        for (int j = 0; j < cnt; j++)
+            if (own[w][j] == lane) acc = acc + mk3(res[w][j][0], res[w][j][1], res[w][j][2]);
+        __syncwarp();
+        return acc;
+    }
+};
+
 __global__ void __launch_bounds__(VT) k_vp_panel_vel_part_f32(const double* __restrict__ rec,
                                                               const double* __restrict__ sigma,
                                                               const double* __restrict__ mu, int64_t nb,
@@ -272,10 +314,13 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part_f32(const double* __re
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
     __shared__ float ft[TILE * FT_STRIDE];
+    __shared__ NearQueue nq;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool live = q < m;
     dv3 poi = live ? ld3(pts + 3 * q) : mk3(0, 0, 0);
     if (live && skip_r > 0 && norm3(poi) > skip_r) live = false;
+    nq.put_target(w, lane, poi, mk3(0, 0, 0));
     const PtF pf = split_pt(poi);
     const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
     dv3 acc = mk3(0, 0, 0);
@@ -290,23 +335,35 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part_f32(const double* __re
             fill_ftile(rec + (b + k) * R_STRIDE, ts[k], tm[k], ft + k * FT_STRIDE);
         }
         __syncthreads();
-        if (!live) continue;
+        int qn = 0;
         for (int k = 0; k < lim; k++) {
-            const float* f = ft + k * FT_STRIDE;
-            float dx, dy, dz, d2;
-            if (far_pair(pf, f, tile + k * R_STRIDE, poi, dx, dy, dz, d2)) {
-                // sigma vSrc + mu vDub = (3 ad pn / d^2 - as) / d^3 (p - c) - ad / d^3 n
-                const float inv = rsqrtf(d2), i2 = inv * inv, i3 = i2 * inv;
-                const float nx = f[FT_N], ny = f[FT_N + 1], nz = f[FT_N + 2];
-                const float pn = dx * nx + dy * ny + dz * nz;
-                const float ad = f[FT_AD];
-                const float cp = (3 * ad * pn * i2 - f[FT_AS]) * i3, cn = ad * i3;
-                fa.add(cp * dx - cn * nx, cp * dy - cn * ny, cp * dz - cn * nz);
-            } else {
-                dv3 vs, vd;
-                panel_v_inf(tile + k * R_STRIDE, poi, vs, vd);
-                acc = acc + (ts[k] * vs + tm[k] * vd);
+            bool near = false;
+            if (live) {
+                const float* f = ft + k * FT_STRIDE;
+                float dx, dy, dz, d2;
+                if (far_pair(pf, f, tile + k * R_STRIDE, poi, dx, dy, dz, d2)) {
+                    // sigma vSrc + mu vDub = (3 ad pn / d^2 - as) / d^3 (p - c) - ad / d^3 n
+                    const float inv = rsqrtf(d2), i2 = inv * inv, i3 = i2 * inv;
+                    const float nx = f[FT_N], ny = f[FT_N + 1], nz = f[FT_N + 2];
+                    const float pn = dx * nx + dy * ny + dz * nz;
+                    const float ad = f[FT_AD];
+                    const float cp = (3 * ad * pn * i2 - f[FT_AS]) * i3, cn = ad * i3;
+                    fa.add(cp * dx - cn * nx, cp * dy - cn * ny, cp * dz - cn * nz);
+                } else {
+                    near = true;
+                }
             }
+            qn = nq.push(w, lane, near, k, qn);
+        }
+        __syncwarp();
+        for (int base = 0; base < qn; base += 32) {  // FP64 near pairs, one per lane
+            int kk, ln;
+            if (nq.take(w, base + lane, qn, kk, ln)) {
+                dv3 vs, vd;
+                panel_v_inf(tile + kk * R_STRIDE, nq.tx(w, ln), vs, vd);
+                nq.put_result(w, lane, ln, ts[kk] * vs + tm[kk] * vd);
+            }
+            acc = nq.gather(w, lane, base, qn, acc);
         }
     }
     if (q >= m) return;
@@ -326,11 +383,14 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part_f32(const double* __rest
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
     __shared__ float ft[TILE * FT_STRIDE];
+    __shared__ NearQueue nq;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     bool live = q < m;
     dv3 x = live ? ld3(pos + 3 * q) : mk3(0, 0, 0);
     dv3 a = live ? ld3(str + 3 * q) : mk3(0, 0, 0);
     if (live && skip_x > 0 && fabs(x.x) > skip_x) live = false;
+    nq.put_target(w, lane, x, a);
     const PtF pf = split_pt(x);
     const float ax = (float)a.x, ay = (float)a.y, az = (float)a.z;
     const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
@@ -346,44 +406,60 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part_f32(const double* __rest
             fill_ftile(rec + (b + k) * R_STRIDE, ts[k], tm[k], ft + k * FT_STRIDE);
         }
         __syncthreads();
-        if (!live) continue;
+        int qn = 0;  // warp-uniform: near pairs of this warp in this tile
         for (int k = 0; k < lim; k++) {
-            const float* f = ft + k * FT_STRIDE;
-            const double* r = tile + k * R_STRIDE;
-            float ddx, ddy, ddz, d2;
-            if (far_pair(pf, f, r, x, ddx, ddy, ddz, d2)) {
-                // velocityGradientPointSource + velocityGradientPointDoublet in FP32, with
-                // the reference's terms: dx = c.x - x, dy = c.y - y, z = c.z, z - z0 = c.z - x.z
-                const float dx = -ddx, dy = -ddy, zz = -ddz;
-                const float z = f[FT_CH + 2] + f[FT_CL + 2];
-                const float dx2 = dx * dx, dy2 = dy * dy, z2 = z * z;
-                const float bb = dx2 + dy2 + z2;
-                const float sb = sqrtf(bb);
-                const float is = f[FT_AS] / (bb * bb * sb);          // sigma area / 4 pi / sdd
-                const float id = 1.0f / (bb * bb * bb * sb);          // 1 / ddd
-                const float uv = 3 * f[FT_AD] * id, w = -f[FT_AD] * id;
-                const float e = dx2 + dy2 - 4 * z2;
-                float G00 = is * (-2 * dx2 + dy2 + z2) + uv * z * (-4 * dx2 + dy2 + z2);
-                float G10 = is * (-3 * dx * dy) + uv * (-5) * z * dy * dx;
-                float G20 = is * (-3 * dx * z) + uv * dx * e;
-                float G01 = is * (-3 * dx * dy) + uv * (-5) * dx * dy * z;
-                float G11 = is * (dx2 - dy2 + z2) + uv * z * (dx2 - 4 * dy2 + z2);
-                float G21 = is * (-3 * z * dy) + uv * dy * e;
-                float G02 = is * (-3 * dx * zz) + w * (-3) * dx * e;
-                float G12 = is * (-3 * dy * zz) + w * (-3) * dy * e;
-                float G22 = is * (-3 * z * zz + bb) + w * (-3) * z * (3 * dx2 + 3 * dy2 - 2 * z2);
-                fa.add(G00 * ax + G01 * ay + G02 * az, G10 * ax + G11 * ay + G12 * az, G20 * ax + G21 * ay + G22 * az);
-            } else {
+            bool near = false;
+            if (live) {
+                const float* f = ft + k * FT_STRIDE;
+                const double* r = tile + k * R_STRIDE;
+                float ddx, ddy, ddz, d2;
+                if (far_pair(pf, f, r, x, ddx, ddy, ddz, d2)) {
+                    // velocityGradientPointSource + velocityGradientPointDoublet in FP32, with
+                    // the reference's terms: dx = c.x - x, dy = c.y - y, z = c.z, z - z0 = c.z - x.z
+                    const float dx = -ddx, dy = -ddy, zz = -ddz;
+                    const float z = f[FT_CH + 2] + f[FT_CL + 2];
+                    const float dx2 = dx * dx, dy2 = dy * dy, z2 = z * z;
+                    const float bb = dx2 + dy2 + z2;
+                    const float sb = sqrtf(bb);
+                    const float is = f[FT_AS] / (bb * bb * sb);          // sigma area / 4 pi / sdd
+                    const float id = 1.0f / (bb * bb * bb * sb);          // 1 / ddd
+                    const float uv = 3 * f[FT_AD] * id, wd = -f[FT_AD] * id;
+                    const float e = dx2 + dy2 - 4 * z2;
+                    float G00 = is * (-2 * dx2 + dy2 + z2) + uv * z * (-4 * dx2 + dy2 + z2);
+                    float G10 = is * (-3 * dx * dy) + uv * (-5) * z * dy * dx;
+                    float G20 = is * (-3 * dx * z) + uv * dx * e;
+                    float G01 = is * (-3 * dx * dy) + uv * (-5) * dx * dy * z;
+                    float G11 = is * (dx2 - dy2 + z2) + uv * z * (dx2 - 4 * dy2 + z2);
+                    float G21 = is * (-3 * z * dy) + uv * dy * e;
+                    float G02 = is * (-3 * dx * zz) + wd * (-3) * dx * e;
+                    float G12 = is * (-3 * dy * zz) + wd * (-3) * dy * e;
+                    float G22 = is * (-3 * z * zz + bb) + wd * (-3) * z * (3 * dx2 + 3 * dy2 - 2 * z2);
+                    fa.add(G00 * ax + G01 * ay + G02 * az, G10 * ax + G11 * ay + G12 * az,
+                           G20 * ax + G21 * ay + G22 * az);
+                } else {
+                    near = true;
+                }
+            }
+            qn = nq.push(w, lane, near, k, qn);
+        }
+        __syncwarp();
+        // the warp's FP64 near pairs, one per lane (bodyPanel::partStretching near branch)
+        for (int base = 0; base < qn; base += 32) {
+            int kk, ln;
+            if (nq.take(w, base + lane, qn, kk, ln)) {
+                const double* r = tile + kk * R_STRIDE;
+                const dv3 xe = nq.tx(w, ln), ae = nq.ta(w, ln);
                 dv3 c = ld3(r + R_C);
-                dm3 g1 = vel_grad_tri_source(r, ts[k], x);
-                dm3 g2 = vel_grad_doublet(r, 3, c, ld3(r + R_N), ld3(r + R_L), ld3(r + R_M), r[R_LONG], tm[k], x);
+                dm3 g1 = vel_grad_tri_source(r, ts[kk], xe);
+                dm3 g2 = vel_grad_doublet(r, 3, c, ld3(r + R_N), ld3(r + R_L), ld3(r + R_M), r[R_LONG], tm[kk], xe);
                 dm3 G;
 #pragma unroll
                 for (int i = 0; i < 3; i++)
 #pragma unroll
                     for (int j = 0; j < 3; j++) G.a[i][j] = (0 + g1.a[i][j]) + g2.a[i][j];
-                acc = acc + mul_m3(G, a);
+                nq.put_result(w, lane, ln, mul_m3(G, ae));
             }
+            acc = nq.gather(w, lane, base, qn, acc);
         }
     }
     if (q >= m) return;

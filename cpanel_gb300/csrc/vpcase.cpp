@@ -256,7 +256,8 @@ cudaError_t field_at(cpg_vpcase& S, bool bh, const std::vector<double>& pts, int
     if ((e = cpg::vp_launch_panel_vel(S.rec.as<double>(), S.sigma.as<double>(), S.mu.as<double>(), S.n,
                                       S.q1.as<double>(), S.mu1.as<double>(), S.n1, S.q2.as<double>(),
                                       S.mu2.as<double>(), S.n2, S.fil.as<double>(), S.have_fil ? S.n2 : 0,
-                                      S.spts.as<double>(), m, 0.0, Q, S.scr.as<double>(), S.s)) != cudaSuccess)
+                                      S.spts.as<double>(), m, 0.0, Q, S.scr.as<double>(), S.s, S.mixed())) !=
+        cudaSuccess)
         return e;
     std::vector<double> h(6 * m);
     if ((e = cudaMemcpyAsync(h.data(), P, sizeof(double) * 6 * m, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)

@@ -105,9 +105,14 @@ struct LuGraphs {
 cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);
 cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
 size_t solve_lu_work_bytes(int64_t n, int k);
+// Ainv (optional): an FP32 inverse of A; the correction of each pass is then Ainv r
+// instead of the two substitutions with LU (LU may be null).
 cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n,
                              int k, const double* rhs, double* x, void* work, double tol, int max_steps,
-                             SolveStats* st, cudaStream_t s);
+                             SolveStats* st, cudaStream_t s, const float* Ainv = nullptr);
+// Ainv (n x n) = U^{-1} L^{-1} from the factors (n substitutions at once); frees the
+// n x n scratch afterwards.
+cudaError_t lu_invert_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* Ainv, cudaStream_t s);
 
 // y(k x n) = alpha * M x(k x n) for column-major FP64 M (used for -B sigma).
 cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, double* y, double alpha, void* work,

@@ -507,15 +507,36 @@ cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, f
     return cudaGraphLaunch(G->solve, s);
 }
 
+__global__ void k_identity(float* __restrict__ X, int64_t n) {
+    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n * n) X[t] = (t / n == t % n) ? 1.f : 0.f;
+}
+
+cudaError_t lu_invert_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* Ainv, cudaStream_t s) {
+    k_identity<<<nb256(n * n), 256, 0, s>>>(Ainv, n);
+    cudaError_t e = lu_solve_fp32(blas, G, LU, n, Ainv, (int)n, s);
+    if (e != cudaSuccess) return e;
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
+    // the n-column substitution graph and its n x n scratch are not needed again
+    if (G->solve) cudaGraphExecDestroy(G->solve);
+    G->solve = nullptr;
+    G->solve_X = nullptr;
+    G->solve_k = 0;
+    if (G->tmp) cudaFree(G->tmp);
+    G->tmp = nullptr;
+    G->tmp_floats = 0;
+    return cudaSuccess;
+}
+
 size_t solve_lu_work_bytes(int64_t n, int k) {
     size_t kn = (size_t)k * n;
-    return sizeof(double) * (2 * kn + 2 * (size_t)k * 64 + 2 * (size_t)k) + sizeof(float) * kn +
+    return sizeof(double) * (2 * kn + 2 * (size_t)k * 64 + 2 * (size_t)k) + 2 * sizeof(float) * kn +
            sizeof(double) * (size_t)residual_chunks(n) * 17 * (size_t)n + 64 * 1024;
 }
 
 cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n,
                              int k, const double* rhs, double* x, void* work, double tol, int max_steps,
-                             SolveStats* st, cudaStream_t s) {
+                             SolveStats* st, cudaStream_t s, const float* Ainv) {
     char* p = (char*)work;
     auto take = [&](size_t bytes) {
         char* r = p;
@@ -525,6 +546,7 @@ cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const fl
     const size_t kn = (size_t)k * n;
     double* r64 = (double*)take(sizeof(double) * kn);
     float* d32 = (float*)take(sizeof(float) * kn);
+    float* e32 = (float*)take(sizeof(float) * kn);  // Ainv r
     double* P64 = (double*)take(sizeof(double) * (size_t)residual_chunks(n) * 17 * n);
     double* part = (double*)take(sizeof(double) * 2 * k * 64);
     double* dd = (double*)take(sizeof(double) * 2 * k);
@@ -538,8 +560,20 @@ cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const fl
     int steps = 0;
     for (; steps < max_steps; steps++) {
         k_d2f<<<nb256(kn), 256, 0, s>>>(r64, d32, kn);
-        if ((e = lu_solve_fp32(blas, G, LU, n, d32, k, s)) != cudaSuccess) return e;
-        k_addf<<<nb256(kn), 256, 0, s>>>(x, d32, kn);
+        if (Ainv) {  // correction = Ainv r (one product instead of the two substitutions)
+            cublasHandle_t h = (cublasHandle_t)blas;
+            if ((e = prepare_blas(h, G, s)) != cudaSuccess) return e;
+            const float one = 1.f, zero = 0.f;
+            cublasStatus_t bs = k == 1 ? cublasSgemv(h, CUBLAS_OP_N, (int)n, (int)n, &one, Ainv, (int)n, d32, 1, &zero,
+                                                     e32, 1)
+                                       : cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, (int)n, &one, Ainv,
+                                                     (int)n, d32, (int)n, &zero, e32, (int)n);
+            if (bs != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+            k_addf<<<nb256(kn), 256, 0, s>>>(x, e32, kn);
+        } else {
+            if ((e = lu_solve_fp32(blas, G, LU, n, d32, k, s)) != cudaSuccess) return e;
+            k_addf<<<nb256(kn), 256, 0, s>>>(x, d32, kn);
+        }
         if ((e = residual_df(A32, Alo, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;
         if ((e = column_norms2(r64, n, k, part, dd, hd.data(), s)) != cudaSuccess) return e;
         worst = 0;

@@ -422,6 +422,165 @@ __global__ void __launch_bounds__(128) k_bh_targets_f32(const BHNode* __restrict
     if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
 }
 
+// ---- one warp per target (small target counts) ----
+// With few targets, one thread per target leaves most SMs idle while each thread runs
+// a long FP64 traversal.  Here the 32 lanes of a warp share one target: all lanes take
+// the same far/near decisions, split each leaf's members between them and take the far
+// nodes in turn; the lanes' sums are added by a fixed butterfly at the end.
+__device__ __forceinline__ dv3 warp_sum3(dv3 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+        v.z += __shfl_xor_sync(0xffffffffu, v.z, o);
+    }
+    return v;
+}
+
+// far decision of internal node i for target x (FP32 band test with the FP64 test inside
+// the margin when fn is given, else the FP64 test); d: float target - centre, d2 = |d|^2
+template <bool F32>
+__device__ __forceinline__ bool far_decide(const BHNode* __restrict__ nodes, const BHNodeF* __restrict__ fn, int i,
+                                           dv3 x, const TgtF& tf, double theta, BHNodeF& f, float3& dl, float& d2) {
+    if (F32) {
+        f = load_fnode(fn, i);
+        dl = diff_f(tf, f);
+        d2 = dl.x * dl.x + dl.y * dl.y + dl.z * dl.z;
+        if (d2 > f.far2 * kBandHi) return true;
+        if (d2 < f.far2 * kBandLo) return false;
+        return far_exact(nodes, i, x, theta);
+    }
+    return far_exact(nodes, i, x, theta);
+}
+
+template <bool V, bool S, bool D, bool F32>
+__global__ void __launch_bounds__(128) k_bh_targets_w(const BHNode* __restrict__ nodes,
+                                                      const BHNodeF* __restrict__ fn, int nn,
+                                                      const BHPart* __restrict__ slots, double theta,
+                                                      const BHPart* __restrict__ tgt, int64_t m, VPConst c,
+                                                      double* __restrict__ vel, double* __restrict__ str,
+                                                      double* __restrict__ dif) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= m) return;  // uniform across the warp
+    const Tgt t = load_part_g(tgt, q);
+    TgtF tf{};
+    if (F32) tf = split_tgt(t);
+    const VPConstF cf = fconst(c);
+    dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
+    KSum fv, fs, fd;
+    int i = 1, nfar = 0;
+    while (i < nn) {
+        const int4 L = load_links(nodes, i);
+        if (L.w) {
+            for (int32_t k = L.x + lane; k < L.x + L.y; k += 32) {
+                const Tgt mb = load_part_g(slots, k);
+                if (mb.idx == t.idx) continue;
+                if (V) v = v + vel_gauss_sym(mb, t, c);
+                if (S) s = s + stretch(mb, t, c);
+                if (D) d = d + diffusion(mb, t, c);
+            }
+            i++;
+            continue;
+        }
+        BHNodeF f{};
+        float3 dl = make_float3(0.f, 0.f, 0.f);
+        float d2 = 0.f;
+        if (!far_decide<F32>(nodes, fn, i, t.x, tf, theta, f, dl, d2)) {
+            i++;
+            continue;
+        }
+        if ((nfar & 31) == lane) {
+            if (F32) {
+                bool on = false;
+                if (S) {
+                    if (d2 < f.cut2 * kBandLo)
+                        on = true;
+                    else if (d2 > f.cut2 * kBandHi)
+                        on = false;
+                    else
+                        on = cut_exact(nodes, i, t.x);
+                }
+                far_pair_f<V, S, D>(f, tf, dl.x, dl.y, dl.z, d2, on, cf, fv, fs, fd);
+            } else {
+                const BHNode nd = load_node(nodes, i);
+                const Tgt e{mk3(nd.ex, nd.ey, nd.ez), nd.erad, mk3(nd.ax, nd.ay, nd.az), -1.0};
+                if (V) v = v + vel_gauss_sym(e, t, c);
+                if (S) s = s + stretch(e, t, c);
+                if (D) d = d + diffusion(e, t, c);
+            }
+        }
+        nfar++;
+        i = L.z;
+    }
+    if (F32) {
+        if (V) v = v + fv.value();
+        if (S) s = s + fs.value();
+        if (D) d = d + fd.value();
+    }
+    if (V) v = warp_sum3(v);
+    if (S) s = warp_sum3(s);
+    if (D) d = warp_sum3(d);
+    if (lane != 0) return;
+    if (V) { vel[3 * q] = v.x; vel[3 * q + 1] = v.y; vel[3 * q + 2] = v.z; }
+    if (S) { str[3 * q] = s.x; str[3 * q + 1] = s.y; str[3 * q + 2] = s.z; }
+    if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
+}
+
+// barnesHutVel(POI) with one warp per point (algebraic core)
+template <bool F32>
+__global__ void __launch_bounds__(128) k_bh_points_w(const BHNode* __restrict__ nodes, const BHNodeF* __restrict__ fn,
+                                                     int nn, const BHPart* __restrict__ parts, double theta,
+                                                     const double* __restrict__ pts, int64_t m, VPConst c,
+                                                     double* __restrict__ vel) {
+    const int64_t q = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= m) return;
+    const dv3 x = ld3(pts + 3 * q);
+    const Tgt t{x, 0.0, mk3(0, 0, 0), -1.0};
+    TgtF tf{};
+    if (F32) tf = split_tgt(t);
+    const float i4p = (float)c.inv_four_pi;
+    dv3 v = mk3(0, 0, 0);
+    KSum fv;
+    int i = 1, nfar = 0;
+    while (i < nn) {
+        const int4 L = load_links(nodes, i);
+        if (L.w) {
+            for (int32_t k = L.x + lane; k < L.x + L.y; k += 32) v = v + vel_alg(load_part_g(parts, k), x, c);
+            i++;
+            continue;
+        }
+        BHNodeF f{};
+        float3 dl = make_float3(0.f, 0.f, 0.f);
+        float d2 = 0.f;
+        if (!far_decide<F32>(nodes, fn, i, x, tf, theta, f, dl, d2)) {
+            i++;
+            continue;
+        }
+        if ((nfar & 31) == lane) {
+            if (F32) {
+                const float sg = 1.5f * f.erad, sg2 = sg * sg;
+                const float qq = d2 + sg2;
+                const float k = -i4p * (d2 + 2.5f * sg2) / (qq * qq * sqrtf(qq));
+                fv.add(k * (dl.y * f.az - dl.z * f.ay), k * (dl.z * f.ax - dl.x * f.az), k * (dl.x * f.ay - dl.y * f.ax));
+            } else {
+                const BHNode nd = load_node(nodes, i);
+                const Tgt e{mk3(nd.ex, nd.ey, nd.ez), nd.erad, mk3(nd.ax, nd.ay, nd.az), -1.0};
+                v = v + vel_alg(e, x, c);
+            }
+        }
+        nfar++;
+        i = L.z;
+    }
+    if (F32) v = v + fv.value();
+    v = warp_sum3(v);
+    if (lane != 0) return;
+    vel[3 * q] = v.x;
+    vel[3 * q + 1] = v.y;
+    vel[3 * q + 2] = v.z;
+}
+
 // slots[q] <- the current state of particle perm[q]
 __global__ void k_refresh_slots(const int64_t* __restrict__ perm, int64_t ns, const double* __restrict__ pos,
                                 const double* __restrict__ str, const double* __restrict__ rad,
@@ -563,6 +722,10 @@ __global__ void k_pack_parts(const double* __restrict__ pos, const double* __res
 
 unsigned blocks(int64_t m, int t) { return (unsigned)((m + t - 1) / t); }
 
+// up to this many targets a traversal runs one warp per target (k_bh_targets_w,
+// k_bh_points_w); above, one thread per target fills the GPU on its own
+constexpr int64_t kWarpPerTargetMax = 16384;
+
 }  // namespace
 
 cudaError_t launch_bh_particles(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, int64_t n,
@@ -605,6 +768,28 @@ cudaError_t launch_bh_targets(const BHNode* nodes, const BHNodeF* fnodes, int nn
                               cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
     int mask = (vel ? 1 : 0) | (str ? 2 : 0) | (dif ? 4 : 0);
+    if (m <= kWarpPerTargetMax) {
+        dim3 gw(blocks(32 * m, 128)), bw(128);
+#define CPG_BHW(V_, S_, D_, F_) \
+    k_bh_targets_w<V_, S_, D_, F_><<<gw, bw, 0, s>>>(nodes, fnodes, nn, slots, theta, tgt, m, c, vel, str, dif)
+        if (fnodes) {
+            switch (mask) {
+                case 1: CPG_BHW(true, false, false, true); break;
+                case 6: CPG_BHW(false, true, true, true); break;
+                case 7: CPG_BHW(true, true, true, true); break;
+                default: return cudaErrorInvalidValue;
+            }
+        } else {
+            switch (mask) {
+                case 1: CPG_BHW(true, false, false, false); break;
+                case 6: CPG_BHW(false, true, true, false); break;
+                case 7: CPG_BHW(true, true, true, false); break;
+                default: return cudaErrorInvalidValue;
+            }
+        }
+#undef CPG_BHW
+        return cudaGetLastError();
+    }
     dim3 g(blocks(m, 128)), b(128);
     if (fnodes) {
         switch (mask) {
@@ -634,6 +819,13 @@ cudaError_t launch_refresh_slots(const int64_t* perm, int64_t ns, const double* 
 cudaError_t launch_bh_points(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, double theta,
                              const double* pts, int64_t m, const VPConst& c, double* vel, cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
+    if (m <= kWarpPerTargetMax) {
+        if (fnodes)
+            k_bh_points_w<true><<<blocks(32 * m, 128), 128, 0, s>>>(nodes, fnodes, nn, parts, theta, pts, m, c, vel);
+        else
+            k_bh_points_w<false><<<blocks(32 * m, 128), 128, 0, s>>>(nodes, fnodes, nn, parts, theta, pts, m, c, vel);
+        return cudaGetLastError();
+    }
     if (fnodes)
         k_bh_points_f32<<<blocks(m, 128), 128, 0, s>>>(nodes, fnodes, nn, parts, theta, pts, m, c, vel);
     else

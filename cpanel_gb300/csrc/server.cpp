@@ -209,7 +209,7 @@ int64_t cpg_server_footprint_vp(int64_t n, int64_t n2, int nsteps, int precision
     // per particle its state, tree slot, step scratch and the panel kernels' partial sums
     const int64_t nn = n * n;
     int64_t mats = 16 * nn + 8 * n * n2;
-    if (precision == CPG_MIXED) mats += 12 * nn + n * 128 * 4 + ((int64_t)256 << 20);
+    if (precision == CPG_MIXED) mats += 20 * nn + n * 128 * 4 + ((int64_t)256 << 20);  // + inverse and its scratch
     const int64_t np = n2 * (int64_t)(nsteps > 0 ? nsteps : 0);
     return mats + n * 4000 + np * 4096 + ((int64_t)64 << 20);
 }

@@ -10,7 +10,8 @@
 // five lengths -- stays FP64, and every near/far decision equals the FP64 one) and
 // replaces the per-step BiCGSTAB by the FP32 LU of A (factored once; A does not change)
 // refined against the FP64 matrix, held as a float pair, to a relative residual of
-// 1e-12, falling back to BiCGSTAB for a step whose refinement stalls.  The shedding
+// 1e-12 (the LU is turned once into an FP32 inverse, so each pass is one matrix-vector
+// product), falling back to BiCGSTAB for a step whose refinement stalls.  The shedding
 // and its bookkeeping are the same in both.
 //
 // Per step (timestep >= 3):
@@ -147,7 +148,7 @@ struct cpg_vpcase {
     bool converged = false;
     // mixed precision: FP32 far fields, LU-refined solve
     int precision = CPG_PLAIN_FP64;
-    Buf fnodes, A32, Alo, LU, bad;
+    Buf fnodes, A32, Alo, LU, bad, Ainv;
     cpg::LuGraphs lug;
     int64_t fallbacks = 0;  // steps whose refinement stalled and that BiCGSTAB solved
     bool mixed() const { return precision == CPG_MIXED; }
@@ -220,8 +221,9 @@ cudaError_t solve(cpg_vpcase& S, bool with_c) {
     cpg::SolveStats st;
     bool done = false;
     if (S.mixed()) {
-        e = cpg::solve_lu_refined(cpg::ctx_blas(S.ctx), &S.lug, S.A32.as<float>(), S.Alo.as<float>(), S.LU.as<float>(),
-                                  S.n, 1, S.rhs.as<double>(), S.mu.as<double>(), S.work.p, kVPRefineTol, 8, &st, S.s);
+        e = cpg::solve_lu_refined(cpg::ctx_blas(S.ctx), &S.lug, S.A32.as<float>(), S.Alo.as<float>(), nullptr, S.n, 1,
+                                  S.rhs.as<double>(), S.mu.as<double>(), S.work.p, kVPRefineTol, 8, &st, S.s,
+                                  S.Ainv.as<float>());
         if (e != cudaSuccess) return e;
         done = st.residual_max <= kVPRefineTol;
         S.last_iters = st.refinements;
@@ -815,6 +817,12 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
             return fail_cuda(e, "LU");
         if ((e = cpg::lu_factor_fp32(blas, &S.lug, S.LU.as<float>(), n, S.bad.as<int>(), S.s)) != cudaSuccess)
             return fail_cuda(e, "LU factorization");
+        // every step solves with the same A: its FP32 inverse makes each refinement pass one
+        // matrix-vector product (the factors are not needed after this)
+        if ((e = S.Ainv.ensure(sizeof(float) * nn, S.s)) != cudaSuccess) return fail_cuda(e, "alloc inverse");
+        if ((e = cpg::lu_invert_fp32(blas, &S.lug, S.LU.as<float>(), n, S.Ainv.as<float>(), S.s)) != cudaSuccess)
+            return fail_cuda(e, "inverse");
+        S.LU.release();
     }
     if ((e = cudaStreamSynchronize(S.s)) != cudaSuccess) return fail_cuda(e, "assembly");
     *out = Sp;
@@ -827,7 +835,7 @@ void cpg_vpcase_destroy(cpg_vpcase* S) {
                   &S->sigma, &S->mu, &S->mu1, &S->prev1, &S->mu2, &S->prev2, &S->rhs, &S->fil, &S->vcent,
                   &S->pos, &S->str, &S->rad, &S->pvel, &S->pstr, &S->packed, &S->tP, &S->tQ, &S->tS, &S->tD,
                   &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr,
-                  &S->fnodes, &S->A32, &S->Alo, &S->LU, &S->bad};
+                  &S->fnodes, &S->A32, &S->Alo, &S->LU, &S->bad, &S->Ainv};
     for (Buf* b : all) b->release();
     S->lug.release();
     delete S;

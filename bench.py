@@ -559,7 +559,7 @@ def main():
     if g_l:
         fl = 2.0 / 3.0 * n ** 3  # per factorization (one graph launch)
         ach = fl / (g_ms / g_l * 1e-3) / 1e12
-        roofs["lu_factor"] = {"bound": "tensor", "kernel": "blocked LU graph: panels + cuBLAS BF16x9 trailing GEMMs",
+        roofs["lu_factor"] = {"bound": "tensor", "kernel": "two-level blocked LU: diagonal-block kernel + cuBLAS BF16x9 panel and trailing GEMMs",
                               "achieved": ach, "unit": "TFLOP/s (FP32-equivalent)", "peak": 1963.8 / 9,
                               "frac": ach / (1963.8 / 9), "peak_source": "measured bf16 / 9 BF16 products",
                               "traffic": None, "avg_launch_ms": g_ms / g_l, "launches": g_l}

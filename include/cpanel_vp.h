@@ -131,9 +131,10 @@ typedef struct {
     double mach;           /* Prandtl-Glauert factor sqrt(1 - M^2) of those coefficients   */
     int precision;         /* CPG_PLAIN_FP64: the reference method in FP64.  CPG_MIXED:
                               particle-node and panel far fields in FP32 (near fields, and
-                              every near/far decision, as in FP64) and the FP32 LU of A,
-                              factored once, refined against FP64 A to 1e-12 each step
-                              (BiCGSTAB for a step whose refinement stalls)            */
+                              every near/far decision, as in FP64) and refinement against
+                              FP64 A to 1e-12 each step with an FP32 inverse of A formed
+                              once from its LU (BiCGSTAB for a step whose refinement
+                              stalls)                                                  */
 } cpg_vp_params;
 typedef struct {
     int64_t n_body, n_w1, n_w2;   /* body panels, first and second buffer rows           */

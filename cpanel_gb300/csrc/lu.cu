@@ -223,6 +223,13 @@ cublasComputeType_t lu_compute() {
     if (e && std::string(e) == "bf16") return CUBLAS_COMPUTE_32F_FAST_16BF;
     return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
 }
+// the panel-sized GEMMs (inner dimension 128): FP32 SIMT by default (one kernel each,
+// where the BF16x9 emulation launches three); CPG_LU_SMALL=bf16x9 for the emulation
+cublasComputeType_t lu_compute_small() {
+    const char* e = std::getenv("CPG_LU_SMALL");
+    if (e && std::string(e) == "bf16x9") return lu_compute();
+    return CUBLAS_COMPUTE_32F;
+}
 
 }  // namespace
 
@@ -255,7 +262,7 @@ cudaError_t column_solve(cublasHandle_t h, float* LU, const float* Dinv, float* 
     int64_t rest = n - K - b;
     if (rest <= 0) return cudaSuccess;
     if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, b, b, &one, LU + K * n + K + b, CUDA_R_32F, (int)n, Ui,
-                     CUDA_R_32F, NB, &zero, W, CUDA_R_32F, (int)rest, lu_compute(), CUBLAS_GEMM_DEFAULT) !=
+                     CUDA_R_32F, NB, &zero, W, CUDA_R_32F, (int)rest, lu_compute_small(), CUBLAS_GEMM_DEFAULT) !=
         CUBLAS_STATUS_SUCCESS)
         return cudaErrorUnknown;
     return cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float), rest * sizeof(float), b,
@@ -270,7 +277,7 @@ cudaError_t row_solve(cublasHandle_t h, float* LU, const float* Dinv, float* W, 
     int b = (int)std::min<int64_t>(NB, n - K);
     const float* Li = Dinv + (K / NB) * 2 * NB * NB;
     if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)nc, b, &one, Li, CUDA_R_32F, NB, LU + c0 * n + K,
-                     CUDA_R_32F, (int)n, &zero, W, CUDA_R_32F, b, lu_compute(), CUBLAS_GEMM_DEFAULT) !=
+                     CUDA_R_32F, (int)n, &zero, W, CUDA_R_32F, b, lu_compute_small(), CUBLAS_GEMM_DEFAULT) !=
         CUBLAS_STATUS_SUCCESS)
         return cudaErrorUnknown;
     return cudaMemcpy2DAsync(LU + c0 * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), nc,
@@ -284,7 +291,8 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
     const float one = 1.f, mone = -1.f;
     cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)nc, b, &mone, LU + K * n + r0,
                                      CUDA_R_32F, (int)n, LU + c0 * n + K, CUDA_R_32F, (int)n, &one, LU + c0 * n + r0,
-                                     CUDA_R_32F, (int)n, lu_compute(), CUBLAS_GEMM_DEFAULT);
+                                     CUDA_R_32F, (int)n, b <= NB ? lu_compute_small() : lu_compute(),
+                                     CUBLAS_GEMM_DEFAULT);
     return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
 }
 

@@ -26,6 +26,7 @@ struct cpg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    cudaStream_t aux = nullptr;  // per-geometry tables built beside the solve
     std::string err;
     cpg::Prof* prof = nullptr;  // device-time accounting, when enabled
     cublasHandle_t blas = nullptr;
@@ -93,6 +94,7 @@ struct cpg_geometry {
     bool lu_ready = false;
     DevBuf work, post_work, cases, outs;
     bool have64 = false, have32 = false, post_ready = false;
+    cudaEvent_t post_ev = nullptr;  // recorded on the aux stream when the post tables are built
     int64_t h2d_bytes = 0;
     int64_t n_near64 = 0, n_near32 = 0;
     cpg::PostTables T;
@@ -168,10 +170,17 @@ void case_scalars(const cpg_flow& f, const cpg_refs& r, cpg::CaseScalars& cs) {
     for (int q = 0; q < 3; q++) cs.cg[q] = r.cg[q];
 }
 
+// The post-processing tables (CHTLS weights, Trefftz operator) do not depend on the
+// solve, so they are built on the context's aux stream while the main stream assembles,
+// factors and solves; launch_post waits for g->post_ev.
 int prepare_post(cpg_geometry* g) {
     cpg_ctx* ctx = g->ctx;
     if (g->post_ready) return CPG_OK;
-    cudaStream_t s = ctx->stream;
+    if (!ctx->aux) CK(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking), "aux stream");
+    if (!g->post_ev) CK(cudaEventCreateWithFlags(&g->post_ev, cudaEventDisableTiming), "event");
+    CK(cudaEventRecord(g->post_ev, ctx->stream), "event");  // the geometry's uploads
+    CK(cudaStreamWaitEvent(ctx->aux, g->post_ev, 0), "event");
+    cudaStream_t s = ctx->aux;
     const cpg::HostMesh& H = g->H;
     int64_t n = H.n_body;
     CK(g->F3.ensure(sizeof(double) * n * 3 * (cpg::kClMax - 1)), "alloc F3");
@@ -225,6 +234,7 @@ int prepare_post(cpg_geometry* g) {
     T.tz_station = g->tzst.as<double>();
     T.tz_lines = g->tzln.as<int32_t>();
     T.G = g->G.as<double>();
+    CK(cudaEventRecord(g->post_ev, s), "event");
     g->post_ready = true;
     return CPG_OK;
 }
@@ -256,6 +266,7 @@ void cpg_destroy(cpg_ctx* c) {
     delete c->prof;
     if (c->blas) cublasDestroy(c->blas);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    if (c->aux) cudaStreamDestroy(c->aux);
     delete c;
 }
 
@@ -372,6 +383,7 @@ void cpg_geometry_destroy(cpg_geometry* g) {
     // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
     g->graphs.release();
+    if (g->post_ev) cudaEventDestroy(g->post_ev);
     delete g;
 }
 
@@ -599,6 +611,7 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     }
     CK(cudaEventRecord(e1, s), "event");
     CK(g->post_work.ensure(cpg::post_work_bytes(g->T, k)), "alloc post workspace");
+    CK(cudaStreamWaitEvent(s, g->post_ev, 0), "wait for the post tables");
     CK(cpg::launch_post(g->T, k, dcs, mu, phi, vel, cp, forces, tz, wmu, g->post_work.p, s), "post");
     CK(cudaEventRecord(e2, s), "event");
     // host outputs

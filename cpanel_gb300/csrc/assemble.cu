@@ -204,11 +204,11 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
         __syncthreads();
         int cnt = (int)min((int64_t)TJ, je - j0);
         df32 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
-        int qn = 0;  // warp-uniform queue length
+        int qn = 0, qfar = 0;  // warp-uniform queue lengths (front and back class)
         for (int t = 0; t < cnt; t++) {
             int64_t j = j0 + t;
             const float* f = s_f + t * F_STRIDE;
-            bool near64 = false;
+            bool near64 = false, close = false;
             if (act) {
                 df32 d[3];
 #pragma unroll
@@ -249,19 +249,26 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
                         for (int c = 0; c < 3; c++) acc[c] = df_add(acc[c], df_mul(bp.src, nv[c]));
                     } else {
                         near64 = true;
+                        close = r2f < __fmul_rn(L, L);
                     }
                 }
             }
-            const unsigned qm = __ballot_sync(0xffffffffu, near64);
-            if (near64) s_q[w][qn + __popc(qm & lt_mask)] = (unsigned short)((t << 5) | lane);
-            qn += __popc(qm);
+            // two classes, so that a chunk of the queue takes one branch of panel_phi_inf_pre:
+            // within one longSide (edge sums) from the front, farther (one atan2) from the back
+            const unsigned qc = __ballot_sync(0xffffffffu, close);
+            const unsigned qf = __ballot_sync(0xffffffffu, near64 && !close);
+            if (close) s_q[w][qn + __popc(qc & lt_mask)] = (unsigned short)((t << 5) | lane);
+            if (near64 && !close) s_q[w][TJ * 32 - 1 - (qfar + __popc(qf & lt_mask))] = (unsigned short)((t << 5) | lane);
+            qn += __popc(qc);
+            qfar += __popc(qf);
         }
         __syncwarp();
-        // the warp's FP64 pairs, one per lane
-        for (int base = 0; base < qn; base += 32) {
+        // the warp's FP64 pairs, one per lane: the front class, then the back class
+        const int qtot = qn + qfar;
+        for (int base = 0; base < qtot; base += 32) {
             const int e = base + lane;
-            if (e < qn) {
-                const int ent = s_q[w][e];
+            if (e < qtot) {
+                const int ent = e < qn ? s_q[w][e] : s_q[w][TJ * 32 - 1 - (e - qn)];
                 const int tt = ent >> 5, ln = ent & 31;
                 const double* r = s_rec + tt * R_STRIDE;
                 const dv3 pe = mk3(s_poi[w][ln][0], s_poi[w][ln][1], s_poi[w][ln][2]);
@@ -278,7 +285,7 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
                 nnear++;
             }
             __syncwarp();
-            const int m = min(32, qn - base);
+            const int m = min(32, qtot - base);
             for (int k = 0; k < m; k++)
                 if (s_own[w][k] == lane) {
                     acc64[0] += s_res[w][k][0];

@@ -63,10 +63,15 @@ __device__ __forceinline__ int panel_phi_inf(const double* r, dv3 poi, double& p
     return 1;
 }
 
-// panel_phi_inf for a near pair with the panel's per-edge constants precomputed (ec: |s_k|,
-// 1/|s_k|, s_k.m for k = 0..2, computed on the host with the same rounded operations) and
-// the three vertex distances formed once per pair (edge k's |b| is edge k+1's |a|).  Every
-// value, and so every branch, equals panel_phi_inf's; only repeated work is gone.
+// panel_phi_inf for a near pair of the mixed path, with the panel's per-edge constants
+// precomputed (ec: |s_k|, 1/|s_k|, s_k.m for k = 0..2, rounded as the device would form
+// them) and the three vertex distances formed once per pair (edge k's |b| is edge k+1's
+// |a|).  The three vortexPhi edge angles sum to the triangle's solid angle with the
+// opposite sign; from one longSide out, unless the target lies within 1e-12 of its
+// distance from the panel plane (where the reference's coplanar branch applies), that sum
+// is taken as 2 atan2(a0.(a1 x a2), D) (Van Oosterom and Strackee), one atan2 instead
+// of three.  On the test wings the two differ by at most 1.3e-13 there; closer in (up to
+// 7e-12 for the nearest neighbours, amplified by the CHTLS weights) the edge sum is kept.
 __device__ __forceinline__ void panel_phi_inf_pre(const double* r, const double* ec, dv3 poi, double& phiSrc,
                                                   double& phiDub) {
     dv3 c = ld3(r + R_C);
@@ -75,19 +80,20 @@ __device__ __forceinline__ void panel_phi_inf_pre(const double* r, const double*
     bool itself = d < 1e-10;
     dv3 n = ld3(r + R_N);
     double PN = dot3(pjk, n);
-    dv3 l = ld3(r + R_L);
     dv3 p[3] = {ld3(r + R_V0), ld3(r + R_V1), ld3(r + R_V2)};
     dv3 av[3] = {poi - p[0], poi - p[1], poi - p[2]};
     double dn[3] = {norm3(av[0]), norm3(av[1]), norm3(av[2])};
-    double src = 0, dub = 0, phiV = 0;
+    const bool edge_sum = !itself && (!(fabs(PN) >= 1e-12 * d) || d < r[R_LONG]);
+    double ss = 0, dub = 0, phiV = 0, src = 0;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
         const int i2 = i == 2 ? 0 : i + 1;
         dv3 a = av[i], s = p[i2] - p[i];
         double Al = dot3(n, cross3(s, a));
         const double na = dn[i], nb = dn[i2];
-        if (!itself) {  // vortex_phi with sm and the norms supplied
+        if (edge_sum) {  // vortex_phi with sm and the norms supplied
             const double eps = 1e-15;
+            const dv3 l = ld3(r + R_L);
             double PA = dot3(a, cross3(l, cross3(a, s)));
             double sm = ec[6 + i];
             double PB = PA - Al * sm;
@@ -103,7 +109,19 @@ __device__ __forceinline__ void panel_phi_inf_pre(const double* r, const double*
         const double S = ec[i];
         double GL = 0;
         if (fabs(na + nb - S) > 0 && S > 0) GL = ec[3 + i] * log(fabs((na + nb + S) / (na + nb - S)));
-        src += Al * GL - PN * phiV;
+        if (edge_sum)
+            src += Al * GL - PN * phiV;
+        else
+            ss += Al * GL;
+    }
+    if (!edge_sum && !itself) {
+        const double N3 = dot3(av[0], cross3(av[1], av[2]));
+        const double D = dn[0] * dn[1] * dn[2] + dot3(av[0], av[1]) * dn[2] + dot3(av[0], av[2]) * dn[1] +
+                         dot3(av[1], av[2]) * dn[0];
+        dub = 2 * atan2(N3, D);
+        src = ss - PN * dub;
+    } else if (itself) {
+        src = ss;  // phiV stays 0 for the panel's own centroid
     }
     phiSrc = src / CPG_FOUR_PI;
     phiDub = itself ? -0.5 : dub / CPG_FOUR_PI;

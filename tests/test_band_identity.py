@@ -61,3 +61,28 @@ def test_band_identity_matches_the_reference_formulas():
         checked += 1
     assert checked > 500
     assert worst_src < 1e-15 and worst_dub < 1e-14
+
+
+def test_solid_angle_form_of_the_near_field():
+    """Within 3 panel lengths the mixed path keeps FP64 but takes the three vortexPhi edge
+    angles as one solid angle, 2 atan2(a0.(a1 x a2), D), from one panel length out (closer
+    in the edge sum is kept).  Checked in FP64 against the oracle's edge sum."""
+    nodes, tris, ids, info, spec = small_wing(n_chord=16, n_span=9)
+    m = po.Mesh(nodes, tris, ids)
+    bv = m.body_verts().reshape(-1, 3, 3)
+    c = bv.mean(axis=1)
+    L = np.max([np.linalg.norm(bv[:, (k + 1) % 3] - bv[:, k], axis=1) for k in range(3)], axis=0)
+    rng = np.random.default_rng(4)
+    worst, checked = 0.0, 0
+    for i in rng.integers(len(c), size=120):
+        r = np.linalg.norm(c - c[i], axis=1) / L
+        for j in np.where((r >= 1) & (r <= 3))[0][:40]:
+            a = [c[i] - bv[j][k] for k in range(3)]
+            A = [np.linalg.norm(x) for x in a]
+            D = A[0] * A[1] * A[2] + (a[0] @ a[1]) * A[2] + (a[0] @ a[2]) * A[1] + (a[1] @ a[2]) * A[0]
+            dub = 2 * np.arctan2(a[0] @ np.cross(a[1], a[2]), D) / (4 * np.pi)
+            _, d_ref = po.tri_phi_inf(bv[j].reshape(9), c[i])
+            worst = max(worst, abs(dub - d_ref))
+            checked += 1
+    assert checked > 1000
+    assert worst < 1e-12

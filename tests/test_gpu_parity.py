@@ -60,13 +60,14 @@ def test_assembly_fp64_4412_matches_oracle(cg, case4412):
 
 
 def test_assembly_mixed_is_close(small):
-    """The mixed matrix (hi + lo): near field within 3 longSide in FP64, the exact formulas
-    between 3 and 5 longSide and the far field in double-float."""
+    """The mixed matrix (hi + lo): near field within 3 longSide in FP64 (the solid angle in
+    one atan2), the exact formulas between 3 and 5 longSide and the far field in
+    double-float."""
     g, m, Ao, Bo, refs = small
     g.setInfCoeff("mixed")
     A = g.getA()
     assert _matrix_rel_err(A, Ao) < 1e-11
-    assert np.abs(A - Ao).max() < 1e-12
+    assert np.abs(A - Ao).max() < 1e-11
 
 
 def test_influence_operators_match_oracle(cg):

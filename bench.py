@@ -198,13 +198,14 @@ def _draw_wing(ntri_target, rng):
 
 
 def batched_and_served():
-    """Config 3 (64 uneven wings x 8 alphas submitted together) and a bounded sample of
-    config 5 (Poisson arrivals, 50 req/s, steady wings of 1k-40k triangles and ~10%
-    unsteady 100-step particle-wake runs on ~4k-triangle wings) through the request loop
-    (include/cpanel_serve.h), mixed precision, 8 and 4 slots."""
+    """The uneven batch (64 seeded wings x 8 alphas) through the grouped batch solve
+    (include/cpanel_batch.h) and, for comparison, through the request loop with 8 slots; and
+    a bounded sample of the served stream (Poisson arrivals, 50 req/s, steady wings of
+    1k-40k triangles and ~10% unsteady 100-step particle-wake runs on ~4k-triangle wings)
+    through the request loop (include/cpanel_serve.h) with 4 slots, mixed precision."""
     from cpanel_gb300 import serve, wing
     out = {}
-    # ---- config 3
+    # ---- the uneven batch: 64 wings x 8 alphas
     wings = []
     for i in range(64):
         spec = wing.config_random(20261203 + i)
@@ -213,6 +214,29 @@ def batched_and_served():
         flows = [(1.0, float(a), 0.0, MACH) for a in rng.uniform(-2, 10, 8)]
         wings.append((nodes, tris, ids, flows, dict(Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0, 0)),
                       int(np.count_nonzero(ids <= 1000))))
+    nsol = sum(len(w[3]) for w in wings)
+    label = ("64 seeded NACA wings (config_random, seeds 20261203+i), %d-%d body panels, 8 alphas each"
+             % (min(w[5] for w in wings), max(w[5] for w in wings)))
+    # grouped batch (include/cpanel_batch.h): one persistent assembly launch for all 64 meshes,
+    # work shape from the autotuner (tuned during the warm-up call, cached for the timed one)
+    from cpanel_gb300 import batch
+    meshes = [dict(nodes=n_, tris=t_, ids=i_, flows=f_, **r_) for n_, t_, i_, f_, r_, _ in wings]
+    _, st_warm = batch.batch_solve(meshes, workers=8, tune="auto")
+    t0 = time.perf_counter()
+    _, st = batch.batch_solve(meshes, workers=8, tune="auto")
+    wall = time.perf_counter() - t0
+    out["batched_uneven"] = {
+        "workload": label, "solves": nsol, "wall_s": wall, "solves_per_s": nsol / wall,
+        "ms_topology": st["ms_topology"], "ms_grouped_assembly": st["ms_assembly"], "ms_solve": st["ms_solve"],
+        "grouped_launch": {"items": st["group"]["items"], "pairs": st["group"]["pairs"],
+                           "near_pairs_fp64": st["group"]["near_pairs"], "shape": st["group"]["shape"],
+                           "tuned_in_warmup": st_warm["group"]["tuned"] == 1,
+                           "candidates_timed": st_warm["group"]["candidates"],
+                           "gpairs_per_s": st["group"]["pairs"] / st["group"]["ms"] / 1e6},
+        "workers": 8,
+        "how": "cpg_batch_solve: topology on 8 worker threads, one grouped persistent assembly launch, then "
+               "each mesh's LU + 8 refined solves + post on its worker's stream"}
+    # the same 64 wings through the request loop (one assembly launch per mesh), for comparison
     srv = serve.Server(slots=8, budget_gb=160.0, precision="mixed")
     srv.wait(srv.submit(*wings[0][:4], **wings[0][4]))  # warm-up: kernels, cuBLAS plans, workspaces
     t0 = time.perf_counter()
@@ -220,15 +244,12 @@ def batched_and_served():
     res = [srv.wait(t) for t in tickets]
     wall = time.perf_counter() - t0
     srv.close()
-    nsol = sum(len(w[3]) for w in wings)
-    out["batched_uneven"] = {
-        "workload": "64 seeded NACA wings (config_random, seeds 20261203+i), %d-%d body panels, 8 alphas each"
-                    % (min(w[5] for w in wings), max(w[5] for w in wings)),
-        "solves": nsol, "wall_s": wall, "solves_per_s": nsol / wall,
+    out["batched_uneven_request_loop"] = {
+        "workload": label, "solves": nsol, "wall_s": wall, "solves_per_s": nsol / wall,
         "p50_ms": float(np.percentile([r["info"]["total_ms"] for r in res], 50)),
         "max_concurrent": max(r["info"]["running_at_start"] for r in res), "slots": 8,
         "how": "all submitted at once to the request loop; each request is assembly + LU + 8 refined solves + post"}
-    # ---- config 5 (bounded sample): steady requests and ~10% unsteady particle-wake runs
+    # ---- the served stream (bounded sample): steady requests and ~10% unsteady particle-wake runs
     rng = np.random.default_rng(7)
     nreq = 32
     gaps = rng.exponential(1.0 / 50.0, nreq)
@@ -284,7 +305,7 @@ def batched_and_served():
 
 
 def vortex_particles(steps=20):
-    """Config 4 (bounded sample): NACA 4412 AR 6 wing of 8,216 body triangles without wake
+    """Unsteady vortex-particle wake (bounded sample): NACA 4412 AR 6 wing of 8,216 body triangles without wake
     panels, alpha 8 deg, dt 0.05, Barnes-Hut on: the first `steps` steps of the VP loop in
     FP64 and in the mixed form (FP32 far fields, FP64 near fields, FP32 LU refined in
     FP64), the particle-velocity check of the final state (mixed and FP64 octree against
@@ -380,7 +401,7 @@ def vortex_particles(steps=20):
 
 
 def vp_loop_only(precision, steps):
-    """The config-4 loop alone (profiling aid): case creation, 3 steps, `steps` timed steps."""
+    """The vortex-particle loop alone (profiling aid): case creation, 3 steps, `steps` timed steps."""
     import torch
 
     from cpanel_gb300 import vp, wing
@@ -431,10 +452,10 @@ def main():
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--workload", default="multi_rhs", choices=["multi_rhs", "mid"])
-    ap.add_argument("--no-serving", action="store_true", help="skip the batched (config 3) and served (config 5) runs")
-    ap.add_argument("--no-vp", action="store_true", help="skip the vortex-particle sample (config 4)")
+    ap.add_argument("--no-serving", action="store_true", help="skip the uneven-batch and served-stream runs")
+    ap.add_argument("--no-vp", action="store_true", help="skip the vortex-particle sample")
     ap.add_argument("--vp-loop", choices=["plain", "mixed"],
-                    help="only the config-4 vortex-particle loop in this precision: 3 steps, then --steps timed "
+                    help="only the vortex-particle loop in this precision: 3 steps, then --steps timed "
                          "steps (one JSON line; for profiling)")
     args = ap.parse_args()
     if args.impl == "reference":

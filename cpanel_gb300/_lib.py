@@ -71,7 +71,11 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices",
            # cpanel_serve.h
            "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint",
-           "cpg_server_submit_vp", "cpg_server_wait_vp", "cpg_server_footprint_vp"]
+           "cpg_server_submit_vp", "cpg_server_wait_vp", "cpg_server_footprint_vp",
+           # cpanel_batch.h
+           "cpg_group_default_shape", "cpg_set_inf_coeff_grouped", "cpg_group_schedule", "cpg_batch_solve"]
+
+TUNE_OFF, TUNE_AUTO, TUNE_FORCE = 0, 1, 2
 
 VEL_GAUSS_SYM, VEL_GAUSS, VEL_ALG = 1, 2, 3
 
@@ -106,6 +110,31 @@ class VPInfo(C.Structure):
 class PTreeInfo(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_nodes", C.c_int64), ("n_leaves", C.c_int64),
                 ("n_levels", C.c_int64)]
+
+
+class GroupShape(C.Structure):
+    _fields_ = [("chunks_per_item", C.c_int), ("near_band", C.c_int), ("blocks_per_sm", C.c_int)]
+
+
+class GroupReport(C.Structure):
+    _fields_ = [("shape", GroupShape), ("tuned", C.c_int), ("candidates", C.c_int), ("items", C.c_int64),
+                ("pairs", C.c_int64), ("near_pairs", C.c_int64), ("ms", C.c_double)]
+
+
+class BatchMesh(C.Structure):
+    _fields_ = [("nodes", D), ("n_nodes", C.c_int64), ("tris", I64), ("ids", I32), ("n_tris", C.c_int64),
+                ("flows", C.POINTER(Flow)), ("k", C.c_int), ("refs", Refs), ("cp", D), ("mu", D), ("CL", D),
+                ("CDi", D), ("status", C.c_int), ("n_body", C.c_int64)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("workers", C.c_int), ("tune", C.c_int), ("budget_bytes", C.c_double)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("ms_total", C.c_double), ("ms_topology", C.c_double), ("ms_assembly", C.c_double),
+                ("ms_solve", C.c_double), ("waves", C.c_int), ("solves", C.c_int64), ("failed", C.c_int),
+                ("group", GroupReport)]
 
 
 def load():
@@ -182,5 +211,10 @@ def load():
     L.cpg_vpcase_wake.argtypes = [vp, D, D]
     L.cpg_vpcase_matrices.argtypes = [vp, D, D, D]
     L.cpg_panels_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, C.c_int64, vp]
+    L.cpg_group_default_shape.argtypes = [C.POINTER(GroupShape)]
+    L.cpg_set_inf_coeff_grouped.argtypes = [C.POINTER(vp), C.c_int, C.c_int, C.POINTER(GroupShape),
+                                            C.POINTER(GroupReport)]
+    L.cpg_group_schedule.argtypes = [I64, C.c_int, C.POINTER(GroupShape), I32, C.c_int64, I64, I64]
+    L.cpg_batch_solve.argtypes = [vp, C.POINTER(BatchMesh), C.c_int, C.POINTER(BatchParams), C.POINTER(BatchStats)]
     _lib = L
     return L

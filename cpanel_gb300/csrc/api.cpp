@@ -9,10 +9,14 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <string>
 #include <vector>
 
+#include "../../include/cpanel_batch.h"
 #include "../../include/cpanel_gpu.h"
 #include "../../include/cpanel_vp.h"
 #include "assemble.h"
@@ -31,6 +35,7 @@ struct cpg_ctx {
     cpg::Prof* prof = nullptr;  // device-time accounting, when enabled
     cublasHandle_t blas = nullptr;
     int particle_precision = CPG_PLAIN_FP64;  // cpg_panels_velocity / cpg_panels_stretching
+    std::vector<cpg_ctx*> workers;  // contexts of cpg_batch_solve, created on first use
 };
 
 namespace {
@@ -124,6 +129,18 @@ void* ctx_blas(cpg_ctx* ctx) {
         cublasSetStream(ctx->blas, ctx->stream);
     }
     return ctx->blas;
+}
+int ctx_device(cpg_ctx* ctx) { return ctx ? ctx->device : 0; }
+// the first w worker contexts of ctx (created on first use, destroyed with ctx)
+int ctx_workers(cpg_ctx* ctx, int w, std::vector<cpg_ctx*>& out) {
+    while ((int)ctx->workers.size() < w) {
+        cpg_ctx* c = nullptr;
+        int rc = cpg_create(&c, ctx->device);
+        if (rc != CPG_OK) return rc;
+        ctx->workers.push_back(c);
+    }
+    out.assign(ctx->workers.begin(), ctx->workers.begin() + w);
+    return CPG_OK;
 }
 }  // namespace cpg
 
@@ -263,6 +280,7 @@ int cpg_create(cpg_ctx** out, int device) {
 
 void cpg_destroy(cpg_ctx* c) {
     if (!c) return;
+    for (cpg_ctx* w : c->workers) cpg_destroy(w);
     delete c->prof;
     if (c->blas) cublasDestroy(c->blas);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -945,6 +963,242 @@ int cpg_panels_velocity(cpg_ctx* ctx, const double* body_verts, const double* si
     rec.release();
     scr.release();
     CK(e, "panel velocity");
+    return CPG_OK;
+}
+
+
+// ---- grouped assembly of many geometries (include/cpanel_batch.h) ----
+
+int cpg_group_default_shape(cpg_group_shape* sh) {
+    if (!sh) return CPG_E_INVALID;
+    sh->chunks_per_item = 2;
+    sh->near_band = 1;
+    sh->blocks_per_sm = 0;  // the occupancy limit
+    return CPG_OK;
+}
+
+static bool group_shape_valid(const cpg_group_shape& s) {
+    return s.chunks_per_item >= 1 && s.chunks_per_item <= 16 && s.near_band >= 0 && s.near_band <= 64 &&
+           s.blocks_per_sm >= 0 && s.blocks_per_sm <= 64;
+}
+
+int cpg_group_schedule(const int64_t* n_body, int m, const cpg_group_shape* shape, int32_t* items, int64_t cap,
+                       int64_t* count, int64_t* chunk_len) {
+    if (!n_body || m <= 0 || !count) return CPG_E_INVALID;
+    cpg_group_shape sh;
+    cpg_group_default_shape(&sh);
+    if (shape) sh = *shape;
+    if (!group_shape_valid(sh)) return CPG_E_INVALID;
+    for (int q = 0; q < m; q++)
+        if (n_body[q] < 1) return CPG_E_INVALID;
+    std::vector<int> it;
+    int64_t ni = cpg::group_schedule(n_body, m, sh.chunks_per_item, sh.near_band, it);
+    *count = ni;
+    if (chunk_len)
+        for (int q = 0; q < m; q++) chunk_len[q] = cpg::mixed_chunk(n_body[q]);
+    if (items) {
+        if (cap < ni) return CPG_E_INVALID;
+        for (size_t t = 0; t < it.size(); t++) items[t] = (int32_t)it[t];
+    }
+    return CPG_OK;
+}
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int>, cpg_group_shape> g_tune_cache;  // (device, log2 m, 2 log2 pairs)
+}  // namespace
+
+int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cpg_group_shape* shape,
+                              cpg_group_report* rep) {
+    if (!gs || m <= 0) return CPG_E_INVALID;
+    for (int q = 0; q < m; q++)
+        if (!gs[q]) return CPG_E_INVALID;
+    cpg_ctx* ctx = gs[0]->ctx;
+    ProfInstall pi(ctx);
+    for (int q = 0; q < m; q++)
+        if (gs[q]->ctx->device != ctx->device) return fail(ctx, CPG_E_INVALID, "geometries on different devices");
+    if (tune < CPG_TUNE_OFF || tune > CPG_TUNE_FORCE) return fail(ctx, CPG_E_INVALID, "unknown tune mode");
+    if (tune == CPG_TUNE_OFF && shape && !group_shape_valid(*shape)) return fail(ctx, CPG_E_INVALID, "bad shape");
+    CK(cudaSetDevice(ctx->device), "device");
+    cudaStream_t s = ctx->stream;
+    // the launch follows the work already queued on every geometry's stream (its uploads)
+    std::vector<cpg_ctx*> others;
+    for (int q = 0; q < m; q++)
+        if (gs[q]->ctx != ctx && std::find(others.begin(), others.end(), gs[q]->ctx) == others.end())
+            others.push_back(gs[q]->ctx);
+    cudaEvent_t join, e0, e1;
+    CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "event");
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    struct EvGuard {
+        cudaEvent_t a, b, c;
+        ~EvGuard() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            cudaEventDestroy(c);
+        }
+    } evg{join, e0, e1};
+    for (cpg_ctx* c : others) {
+        CK(cudaEventRecord(join, c->stream), "event");
+        CK(cudaStreamWaitEvent(s, join, 0), "join");
+    }
+    std::vector<cpg::MixedMeshDesc> desc(m);
+    std::vector<int64_t> ns(m);
+    int64_t rows = 0;
+    double pairs = 0;
+    bool any_wake = false;
+    for (int q = 0; q < m; q++) {
+        cpg_geometry* g = gs[q];
+        const int64_t n = g->H.n_body;
+        const size_t nn = (size_t)n * n;
+        CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
+        CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
+        CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n))), "alloc rhs basis");
+        desc[q] = cpg::MixedMeshDesc{g->rec.as<double>(), g->frec.as<float>(), g->erec.as<double>(), n,
+                                     cpg::mixed_chunk(n), g->A32.as<float>(), g->Alo.as<float>(),
+                                     g->rb.as<double>() + 3 * n, g->rb.as<double>(),
+                                     g->count.as<unsigned long long>(), g->wrec.as<double>(), g->widx.as<int32_t>(),
+                                     g->wcoef.as<double>(), g->H.n_wake, rows};
+        ns[q] = n;
+        rows += n;
+        pairs += (double)n * (double)n;
+        any_wake = any_wake || g->H.n_wake > 0;
+    }
+    int nsm = 0;
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+    const int maxb = cpg::assemble_mixed_grouped_max_blocks_per_sm();
+    // queue capacity: one chunk per item is the longest queue of any shape
+    std::vector<int> items;
+    const int64_t max_items = cpg::group_schedule(ns.data(), m, 1, 0, items);
+    cpg::MixedMeshDesc* ddesc = nullptr;
+    int* ditems = nullptr;
+    int* dnext = nullptr;
+    CK(cudaMallocAsync((void**)&ddesc, sizeof(cpg::MixedMeshDesc) * m, s), "alloc group descriptors");
+    struct FreeGuard {
+        void *a, *b, *c;
+        cudaStream_t s;
+        ~FreeGuard() {
+            if (a) cudaFreeAsync(a, s);
+            if (b) cudaFreeAsync(b, s);
+            if (c) cudaFreeAsync(c, s);
+        }
+    } fg{ddesc, nullptr, nullptr, s};
+    CK(cudaMallocAsync((void**)&ditems, sizeof(int) * 4 * std::max<int64_t>(1, max_items), s), "alloc work queue");
+    fg.b = ditems;
+    CK(cudaMallocAsync((void**)&dnext, sizeof(int), s), "alloc queue counter");
+    fg.c = dnext;
+    CK(cudaMemcpyAsync(ddesc, desc.data(), sizeof(cpg::MixedMeshDesc) * m, cudaMemcpyHostToDevice, s), "descriptors");
+    auto resolve = [&](cpg_group_shape sh) {
+        if (sh.blocks_per_sm <= 0 || sh.blocks_per_sm > maxb) sh.blocks_per_sm = maxb;
+        return sh;
+    };
+    // queue one shape: upload its items and launch the persistent assembly kernel
+    int64_t nitems = 0;
+    auto launch_core = [&](const cpg_group_shape& sh) -> cudaError_t {
+        nitems = cpg::group_schedule(ns.data(), m, sh.chunks_per_item, sh.near_band, items);
+        cudaError_t e = cudaMemcpyAsync(ditems, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return e;
+        return cpg::launch_assemble_mixed_grouped_core(ddesc, ditems, (int)nitems, sh.blocks_per_sm * nsm, dnext, s);
+    };
+    cpg_group_shape use;
+    cpg_group_default_shape(&use);
+    int tuned = 0, candidates = 0;
+    const auto key = std::make_tuple(ctx->device, (int)std::floor(std::log2((double)m)),
+                                     (int)std::floor(2.0 * std::log2(std::max(1.0, pairs))));
+    bool have = false;
+    if (tune == CPG_TUNE_OFF) {
+        if (shape) use = *shape;
+        have = true;
+    } else if (tune == CPG_TUNE_AUTO) {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            use = it->second;
+            have = true;
+            tuned = 2;
+        }
+    }
+    use = resolve(use);
+    if (!have) {
+        // coordinate search over shapes that all give the same bits: chunks per far item,
+        // then the near band, then the resident blocks per SM; one timed launch each
+        cpg::Prof* saved = cpg::g_prof;
+        cpg::g_prof = nullptr;  // tuning launches are not part of the profile
+        auto timed = [&](const cpg_group_shape& sh, float* ms) -> cudaError_t {
+            cudaError_t e;
+            if ((e = cudaEventRecord(e0, s)) != cudaSuccess) return e;
+            if ((e = launch_core(sh)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(e1, s)) != cudaSuccess) return e;
+            if ((e = cudaEventSynchronize(e1)) != cudaSuccess) return e;
+            candidates++;
+            return cudaEventElapsedTime(ms, e0, e1);
+        };
+        cudaError_t e = cudaSuccess;
+        float best_ms = 0, t = 0;
+        cpg_group_shape best = use;
+        if (e == cudaSuccess) e = timed(best, &t);  // warm-up: first touch of the matrices
+        if (e == cudaSuccess) e = timed(best, &best_ms);
+        const int chunk_opts[] = {1, 4, 8};
+        for (int c : chunk_opts) {
+            if (e != cudaSuccess) break;
+            cpg_group_shape sh = best;
+            sh.chunks_per_item = c;
+            if ((e = timed(sh, &t)) == cudaSuccess && t < best_ms) best_ms = t, best = sh;
+        }
+        const int band_opts[] = {0, 2, 4};
+        for (int b : band_opts) {
+            if (e != cudaSuccess) break;
+            if (b == best.near_band) continue;
+            cpg_group_shape sh = best;
+            sh.near_band = b;
+            if ((e = timed(sh, &t)) == cudaSuccess && t < best_ms) best_ms = t, best = sh;
+        }
+        const int bps_opts[] = {maxb - 1, maxb / 2};
+        for (int bp : bps_opts) {
+            if (e != cudaSuccess) break;
+            if (bp < 1 || bp == best.blocks_per_sm || (bp == maxb / 2 && maxb / 2 == maxb - 1)) continue;
+            cpg_group_shape sh = best;
+            sh.blocks_per_sm = bp;
+            if ((e = timed(sh, &t)) == cudaSuccess && t < best_ms) best_ms = t, best = sh;
+        }
+        cpg::g_prof = saved;
+        CK(e, "assembly shape tuning");
+        use = best;
+        tuned = 1;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[key] = use;
+    }
+    for (int q = 0; q < m; q++) CK(cudaMemsetAsync(gs[q]->count.p, 0, sizeof(unsigned long long), s), "clear counter");
+    CK(cudaEventRecord(e0, s), "event");
+    CK(launch_core(use), "grouped assembly (mixed)");
+    CK(cpg::launch_assemble_mixed_grouped_finish(ddesc, m, rows, any_wake, s), "grouped sums and wake columns");
+    CK(cudaEventRecord(e1, s), "event");
+    // every geometry's stream continues after the grouped launch
+    for (cpg_ctx* c : others) CK(cudaStreamWaitEvent(c->stream, e1, 0), "join");
+    std::vector<unsigned long long> cnt(m, 0);
+    for (int q = 0; q < m; q++)
+        CK(cudaMemcpyAsync(&cnt[q], gs[q]->count.p, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s), "counter");
+    CK(cudaStreamSynchronize(s), "grouped assembly");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    int64_t near = 0;
+    for (int q = 0; q < m; q++) {
+        cpg_geometry* g = gs[q];
+        g->have32 = true;
+        g->lu_ready = false;
+        g->n_near32 = (int64_t)cnt[q];
+        g->ms_asm = (float)(ms * ((double)ns[q] * (double)ns[q]) / pairs);  // its share of the launch
+        near += (int64_t)cnt[q];
+    }
+    if (rep) {
+        rep->shape = use;
+        rep->tuned = tuned;
+        rep->candidates = candidates;
+        rep->items = nitems;
+        rep->pairs = (int64_t)pairs;
+        rep->near_pairs = near;
+        rep->ms = ms;
+    }
     return CPG_OK;
 }
 

@@ -157,31 +157,33 @@ __device__ __noinline__ BandPhi band_phi_df(df32 d0, df32 d1, df32 d2, const flo
 // one pair per lane, so a warp with a few near lanes does not idle the others; each target
 // then adds its own queued results in queue order (the same order on every run).
 constexpr int WARPS_PER_BLOCK = TI / 32;
-__global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restrict__ rec,
-                                                          const float* __restrict__ frec,
-                                                          const double* __restrict__ erec, int64_t n, int64_t jchunk,
-                                                          const int* __restrict__ order, float* __restrict__ A32,
-                                                          float* __restrict__ Alo, double* __restrict__ rbp,
-                                                          unsigned long long* __restrict__ near_count) {
-    // block b works on row block order[2b] and source chunk order[2b+1] (the costly
-    // near-diagonal blocks first, so that they do not form the tail)
-    const int64_t bx = order[2 * blockIdx.x], by = order[2 * blockIdx.x + 1];
-    __shared__ double s_rec[TJ * R_STRIDE];
-    __shared__ float s_f[TJ * F_STRIDE];
-    __shared__ double s_e[TJ * E_STRIDE];
-    __shared__ unsigned short s_q[WARPS_PER_BLOCK][TJ * 32];  // (tile index << 5) | lane
-    __shared__ double s_res[WARPS_PER_BLOCK][32][3];
-    __shared__ int s_own[WARPS_PER_BLOCK][32];
-    __shared__ double s_poi[WARPS_PER_BLOCK][32][3];
+struct MixedSmem {
+    double rec[TJ * R_STRIDE];
+    float f[TJ * F_STRIDE];
+    double e[TJ * E_STRIDE];
+    unsigned short q[WARPS_PER_BLOCK][TJ * 32];  // (tile index << 5) | lane
+    double res[WARPS_PER_BLOCK][32][3];
+    int own[WARPS_PER_BLOCK][32];
+    double poi[WARPS_PER_BLOCK][32][3];
+};
+
+// One (row block bx, source chunk by) of the mixed assembly: targets bx*TI .. bx*TI+TI-1,
+// sources by*jchunk .. min(n, (by+1)*jchunk)-1.  Safe to call back to back from one block
+// (every shared tile is refilled behind a barrier; the queue arrays are per warp).
+__device__ __forceinline__ void mixed_block(MixedSmem& S, const double* __restrict__ rec,
+                                            const float* __restrict__ frec, const double* __restrict__ erec,
+                                            int64_t n, int64_t jchunk, int64_t bx, int64_t by,
+                                            float* __restrict__ A32, float* __restrict__ Alo,
+                                            double* __restrict__ rbp, unsigned long long* __restrict__ near_count) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     int64_t i = bx * TI + threadIdx.x;
     const int64_t iw = bx * TI + 32 * w;  // first target of this warp
     bool act = i < n;
     dv3 poi = act ? ld3(rec + i * R_STRIDE + R_C) : mk3(0, 0, 0);
-    s_poi[w][lane][0] = poi.x;
-    s_poi[w][lane][1] = poi.y;
-    s_poi[w][lane][2] = poi.z;
+    S.poi[w][lane][0] = poi.x;
+    S.poi[w][lane][1] = poi.y;
+    S.poi[w][lane][2] = poi.z;
     df32 ci[3] = {{0, 0}, {0, 0}, {0, 0}};
     if (act)
         for (int c = 0; c < 3; c++) ci[c] = df32{frec[i * F_STRIDE + F_CHI + c], frec[i * F_STRIDE + F_CLO + c]};
@@ -192,14 +194,14 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
     const df32 inv4pi = df32{(float)q4, (float)(q4 - (double)(float)q4)};
     for (int64_t j0 = jb; j0 < je; j0 += TJ) {
         __syncthreads();
-        load_tile(s_rec, rec, j0, n);
+        load_tile(S.rec, rec, j0, n);
         for (int t = threadIdx.x; t < TJ * F_STRIDE; t += blockDim.x) {
             int64_t j = j0 + t / F_STRIDE;
-            s_f[t] = j < n ? frec[j0 * F_STRIDE + t] : 0.f;
+            S.f[t] = j < n ? frec[j0 * F_STRIDE + t] : 0.f;
         }
         for (int t = threadIdx.x; t < TJ * E_STRIDE; t += blockDim.x) {
             int64_t j = j0 + t / E_STRIDE;
-            s_e[t] = j < n ? erec[j0 * E_STRIDE + t] : 0.0;
+            S.e[t] = j < n ? erec[j0 * E_STRIDE + t] : 0.0;
         }
         __syncthreads();
         int cnt = (int)min((int64_t)TJ, je - j0);
@@ -207,7 +209,7 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
         int qn = 0, qfar = 0;  // warp-uniform queue lengths (front and back class)
         for (int t = 0; t < cnt; t++) {
             int64_t j = j0 + t;
-            const float* f = s_f + t * F_STRIDE;
+            const float* f = S.f + t * F_STRIDE;
             bool near64 = false, close = false;
             if (act) {
                 df32 d[3];
@@ -222,7 +224,7 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
                 else if (r2f < __fmul_rn(lim, 0.99999f))
                     far = false;
                 else {  // guard band: decide exactly as the FP64 reference does
-                    const double* r = s_rec + t * R_STRIDE;
+                    const double* r = S.rec + t * R_STRIDE;
                     double dd = norm3(poi - ld3(r + R_C));
                     far = dd / r[R_LONG] > 5;
                 }
@@ -257,8 +259,8 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
             // within one longSide (edge sums) from the front, farther (one atan2) from the back
             const unsigned qc = __ballot_sync(0xffffffffu, close);
             const unsigned qf = __ballot_sync(0xffffffffu, near64 && !close);
-            if (close) s_q[w][qn + __popc(qc & lt_mask)] = (unsigned short)((t << 5) | lane);
-            if (near64 && !close) s_q[w][TJ * 32 - 1 - (qfar + __popc(qf & lt_mask))] = (unsigned short)((t << 5) | lane);
+            if (close) S.q[w][qn + __popc(qc & lt_mask)] = (unsigned short)((t << 5) | lane);
+            if (near64 && !close) S.q[w][TJ * 32 - 1 - (qfar + __popc(qf & lt_mask))] = (unsigned short)((t << 5) | lane);
             qn += __popc(qc);
             qfar += __popc(qf);
         }
@@ -268,29 +270,29 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
         for (int base = 0; base < qtot; base += 32) {
             const int e = base + lane;
             if (e < qtot) {
-                const int ent = e < qn ? s_q[w][e] : s_q[w][TJ * 32 - 1 - (e - qn)];
+                const int ent = e < qn ? S.q[w][e] : S.q[w][TJ * 32 - 1 - (e - qn)];
                 const int tt = ent >> 5, ln = ent & 31;
-                const double* r = s_rec + tt * R_STRIDE;
-                const dv3 pe = mk3(s_poi[w][ln][0], s_poi[w][ln][1], s_poi[w][ln][2]);
+                const double* r = S.rec + tt * R_STRIDE;
+                const dv3 pe = mk3(S.poi[w][ln][0], S.poi[w][ln][1], S.poi[w][ln][2]);
                 double src = 0, dub = 0;
-                panel_phi_inf_pre(r, s_e + tt * E_STRIDE, pe, src, dub);
+                panel_phi_inf_pre(r, S.e + tt * E_STRIDE, pe, src, dub);
                 const int64_t ie = iw + ln, je_ = j0 + tt;
                 float hi = (float)dub;
                 A32[je_ * n + ie] = hi;
                 Alo[je_ * n + ie] = (float)(dub - (double)hi);  // FP64 value = hi + lo to 2^-48
-                s_res[w][lane][0] = src * r[R_N + 0];
-                s_res[w][lane][1] = src * r[R_N + 1];
-                s_res[w][lane][2] = src * r[R_N + 2];
-                s_own[w][lane] = ln;
+                S.res[w][lane][0] = src * r[R_N + 0];
+                S.res[w][lane][1] = src * r[R_N + 1];
+                S.res[w][lane][2] = src * r[R_N + 2];
+                S.own[w][lane] = ln;
                 nnear++;
             }
             __syncwarp();
             const int m = min(32, qtot - base);
             for (int k = 0; k < m; k++)
-                if (s_own[w][k] == lane) {
-                    acc64[0] += s_res[w][k][0];
-                    acc64[1] += s_res[w][k][1];
-                    acc64[2] += s_res[w][k][2];
+                if (S.own[w][k] == lane) {
+                    acc64[0] += S.res[w][k][0];
+                    acc64[1] += S.res[w][k][1];
+                    acc64[2] += S.res[w][k][2];
                 }
             __syncwarp();
         }
@@ -307,6 +309,19 @@ __global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restri
         for (int o = 16; o > 0; o >>= 1) nnear += __shfl_down_sync(0xffffffffu, nnear, o);
         if ((threadIdx.x & 31) == 0) atomicAdd(near_count, (unsigned long long)nnear);
     }
+}
+
+__global__ void __launch_bounds__(TI, 4) k_assemble_mixed(const double* __restrict__ rec,
+                                                          const float* __restrict__ frec,
+                                                          const double* __restrict__ erec, int64_t n, int64_t jchunk,
+                                                          const int* __restrict__ order, float* __restrict__ A32,
+                                                          float* __restrict__ Alo, double* __restrict__ rbp,
+                                                          unsigned long long* __restrict__ near_count) {
+    // block b works on row block order[2b] and source chunk order[2b+1] (the costly
+    // near-diagonal blocks first, so that they do not form the tail)
+    __shared__ MixedSmem S;
+    mixed_block(S, rec, frec, erec, n, jchunk, order[2 * blockIdx.x], order[2 * blockIdx.x + 1], A32, Alo, rbp,
+                near_count);
 }
 
 // Wake doublet columns, CPanel/geometry.cpp:853-873.  One thread per target row
@@ -331,12 +346,11 @@ __global__ void k_wake_columns(const double* __restrict__ rec, const double* __r
     }
 }
 
-// Wake columns for the split (hi + lo) FP32 storage of the mixed path.
-__global__ void k_wake_columns_split(const double* __restrict__ rec, const double* __restrict__ wrec,
-                                     const int32_t* __restrict__ widx, const double* __restrict__ wcoef, int64_t n,
-                                     int64_t nw, float* __restrict__ Ahi, float* __restrict__ Alo) {
-    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// Wake columns for the split (hi + lo) FP32 storage of the mixed path: row i.
+__device__ __forceinline__ void wake_row_split(const double* __restrict__ rec, const double* __restrict__ wrec,
+                                               const int32_t* __restrict__ widx, const double* __restrict__ wcoef,
+                                               int64_t n, int64_t nw, float* __restrict__ Ahi,
+                                               float* __restrict__ Alo, int64_t i) {
     dv3 poi = ld3(rec + i * R_STRIDE + R_C);
     for (int64_t j = 0; j < nw; j++) {
         double infl = dub_phi_inf(wrec + j * R_STRIDE, poi);
@@ -353,12 +367,74 @@ __global__ void k_wake_columns_split(const double* __restrict__ rec, const doubl
     }
 }
 
+__global__ void k_wake_columns_split(const double* __restrict__ rec, const double* __restrict__ wrec,
+                                     const int32_t* __restrict__ widx, const double* __restrict__ wcoef, int64_t n,
+                                     int64_t nw, float* __restrict__ Ahi, float* __restrict__ Alo) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    wake_row_split(rec, wrec, widx, wcoef, n, nw, Ahi, Alo, i);
+}
+
 __global__ void k_rb_reduce(const double* __restrict__ rbp, int64_t n, int64_t chunks, double* __restrict__ rb) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * n) return;
     double acc = 0;
     for (int64_t y = 0; y < chunks; y++) acc += rbp[y * 3 * n + t];
     rb[t] = acc;
+}
+
+// ---- grouped launch: the mixed assembly of many meshes at once.
+// The work queue holds items (mesh, row block, first source chunk, chunk count); the
+// chunk length of a mesh is the one its single-mesh launch uses (chunk_for), and every
+// chunk still writes its own partial sums, so any queue order and any grouping of chunks
+// into items gives the same bits as the single-mesh launch.  Persistent: each block
+// takes the next item from a counter until the queue is empty.
+__global__ void __launch_bounds__(TI, 4) k_assemble_mixed_grouped(const cpg::MixedMeshDesc* __restrict__ meshes,
+                                                                  const int4* __restrict__ items, int nitems,
+                                                                  int* __restrict__ next) {
+    __shared__ MixedSmem S;
+    __shared__ int s_item;
+    for (;;) {
+        __syncthreads();  // every thread has read the previous s_item
+        if (threadIdx.x == 0) s_item = atomicAdd(next, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) return;
+        const int4 w = items[it];
+        const cpg::MixedMeshDesc& d = meshes[w.x];
+        for (int c = 0; c < w.w; c++)
+            mixed_block(S, d.rec, d.frec, d.erec, d.n, d.jchunk, w.y, w.z + c, d.A32, d.Alo, d.rbp, d.near_count);
+    }
+}
+
+// mesh of flattened row r (meshes sorted by row0)
+__device__ __forceinline__ int mesh_of_row(const cpg::MixedMeshDesc* __restrict__ meshes, int m, int64_t r) {
+    int lo = 0, hi = m - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (meshes[mid].row0 <= r) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// k_rb_reduce for every mesh of a group (same order of additions)
+__global__ void k_rb_reduce_grouped(const cpg::MixedMeshDesc* __restrict__ meshes, int m, int64_t rows) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const cpg::MixedMeshDesc& d = meshes[mesh_of_row(meshes, m, r)];
+    const int64_t i = r - d.row0, n = d.n, chunks = (n + d.jchunk - 1) / d.jchunk;
+    for (int c = 0; c < 3; c++) {
+        double acc = 0;
+        for (int64_t y = 0; y < chunks; y++) acc += d.rbp[y * 3 * n + c * n + i];
+        d.rb[c * n + i] = acc;
+    }
+}
+
+__global__ void k_wake_columns_grouped(const cpg::MixedMeshDesc* __restrict__ meshes, int m, int64_t rows) {
+    int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= rows) return;
+    const cpg::MixedMeshDesc& d = meshes[mesh_of_row(meshes, m, r)];
+    if (d.nw > 0) wake_row_split(d.rec, d.wrec, d.widx, d.wcoef, d.n, d.nw, d.A32, d.Alo, r - d.row0);
 }
 
 // panel::setGeom + getLocalSys on the device for free triangles (batched API).
@@ -570,6 +646,89 @@ cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const do
 int64_t mixed_rb_part_doubles(int64_t n) {
     int64_t ch = chunk_for(n);
     return ((n + ch - 1) / ch) * 3 * n;
+}
+
+int64_t mixed_chunk(int64_t n) { return chunk_for(n); }
+
+int64_t group_schedule(const int64_t* n, int m, int chunks_per_item, int near_band, std::vector<int>& items) {
+    // an item's cost estimate: its pairs, weighted 16x when the row and source index
+    // ranges lie within near_band chunk lengths of each other (near-diagonal items hold
+    // most of the FP64 near field); near items keep one chunk each, the rest are grouped
+    // chunks_per_item at a time, and the queue runs from the costliest item down
+    struct It {
+        double cost;
+        int q, bx, by, g;
+    };
+    std::vector<It> v;
+    if (chunks_per_item < 1) chunks_per_item = 1;
+    for (int q = 0; q < m; q++) {
+        const int64_t nn = n[q];
+        if (nn <= 0) continue;
+        const int64_t ch = chunk_for(nn), nbx = (nn + TI - 1) / TI, nby = (nn + ch - 1) / ch;
+        const int64_t band = (int64_t)near_band * ch;
+        for (int64_t bx = 0; bx < nbx; bx++) {
+            const int64_t r0 = bx * TI, r1 = std::min(nn, r0 + TI);
+            int64_t by = 0;
+            while (by < nby) {
+                const int64_t c0 = by * ch, c1 = std::min(nn, c0 + ch);
+                const int64_t gap = c0 >= r1 ? c0 - r1 : (r0 >= c1 ? r0 - c1 : 0);
+                const bool near_item = gap <= band;
+                int g = 1;
+                if (!near_item) {
+                    while (g < chunks_per_item && by + g < nby) {  // extend while the next chunk is far too
+                        const int64_t d0 = (by + g) * ch, d1 = std::min(nn, d0 + ch);
+                        const int64_t gp = d0 >= r1 ? d0 - r1 : (r0 >= d1 ? r0 - d1 : 0);
+                        if (gp <= band) break;
+                        g++;
+                    }
+                }
+                const int64_t e1 = std::min(nn, (by + g) * ch);
+                const double pairs = (double)(r1 - r0) * (double)(e1 - c0);
+                v.push_back({pairs * (near_item ? 16.0 : 1.0), q, (int)bx, (int)by, g});
+                by += g;
+            }
+        }
+    }
+    std::stable_sort(v.begin(), v.end(), [](const It& a, const It& b) { return a.cost > b.cost; });
+    items.resize(4 * v.size());
+    for (size_t t = 0; t < v.size(); t++) {
+        items[4 * t] = v[t].q;
+        items[4 * t + 1] = v[t].bx;
+        items[4 * t + 2] = v[t].by;
+        items[4 * t + 3] = v[t].g;
+    }
+    return (int64_t)v.size();
+}
+
+cudaError_t launch_assemble_mixed_grouped_core(const MixedMeshDesc* meshes, const int* items, int nitems,
+                                               int blocks, int* next, cudaStream_t s) {
+    if (nitems <= 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(next, 0, sizeof(int), s);
+    if (e != cudaSuccess) return e;
+    ProfScope ps(Prof::ASSEMBLE, s);
+    k_assemble_mixed_grouped<<<(unsigned)blocks, TI, 0, s>>>(meshes, (const int4*)items, nitems, next);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, int m, int64_t rows, bool any_wake,
+                                                 cudaStream_t s) {
+    if (rows <= 0) return cudaSuccess;
+    const unsigned g = (unsigned)((rows + 127) / 128);
+    {
+        ProfScope ps(Prof::ASSEMBLE, s);
+        k_rb_reduce_grouped<<<g, 128, 0, s>>>(meshes, m, rows);
+    }
+    if (any_wake) {
+        ProfScope ps(Prof::WAKE_COLUMNS, s);
+        k_wake_columns_grouped<<<g, 128, 0, s>>>(meshes, m, rows);
+    }
+    return cudaGetLastError();
+}
+
+int assemble_mixed_grouped_max_blocks_per_sm() {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_assemble_mixed_grouped, TI, 0) != cudaSuccess) return 1;
+    return nb < 1 ? 1 : nb;
 }
 
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,

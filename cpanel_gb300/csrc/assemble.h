@@ -53,6 +53,41 @@ cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const do
 // block schedule of the mixed assembly: blocks sorted by the distance between their row
 // and source index ranges (near-field-heavy blocks first)
 void mixed_block_order(int64_t n, std::vector<int>& out);
+
+// Grouped mixed assembly of many meshes in one persistent launch.  One descriptor per
+// mesh (device copy); row0 = first row of the mesh in the group's flattened rows, the
+// descriptors sorted by row0.  jchunk must be mixed_chunk(n): the partial sums of the
+// right-hand-side basis are then split exactly as in the single-mesh launch, so the
+// results are bit-identical to launch_assemble_mixed whatever the schedule.
+struct MixedMeshDesc {
+    const double* rec;
+    const float* frec;
+    const double* erec;
+    int64_t n, jchunk;
+    float* A32;
+    float* Alo;
+    double* rbp;  // mixed_rb_part_doubles(n)
+    double* rb;   // 3n
+    unsigned long long* near_count;  // may be null
+    const double* wrec;
+    const int32_t* widx;
+    const double* wcoef;
+    int64_t nw;
+    int64_t row0;
+};
+int64_t mixed_chunk(int64_t n);
+// Work queue of a grouped launch: 4 ints per item (mesh, row block, first chunk, chunk
+// count), costliest first.  Items whose row and source ranges lie within near_band chunk
+// lengths hold one chunk; the others up to chunks_per_item.  Returns the item count.
+int64_t group_schedule(const int64_t* n, int m, int chunks_per_item, int near_band, std::vector<int>& items);
+// The persistent assembly kernel over the queue (blocks = resident blocks in total;
+// next: one device int, cleared here), then the partial-sum reduction and the wake
+// columns of every mesh (rows = the group's flattened row count).
+cudaError_t launch_assemble_mixed_grouped_core(const MixedMeshDesc* meshes, const int* items, int nitems,
+                                               int blocks, int* next, cudaStream_t s);
+cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, int m, int64_t rows, bool any_wake,
+                                                 cudaStream_t s);
+int assemble_mixed_grouped_max_blocks_per_sm();
 // doubles of the per-chunk partial sums that launch_assemble_mixed needs in rb_part
 int64_t mixed_rb_part_doubles(int64_t n);
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,

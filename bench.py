@@ -221,21 +221,46 @@ def batched_and_served():
     # work shape from the autotuner (tuned during the warm-up call, cached for the timed one)
     from cpanel_gb300 import batch
     meshes = [dict(nodes=n_, tris=t_, ids=i_, flows=f_, **r_) for n_, t_, i_, f_, r_, _ in wings]
-    _, st_warm = batch.batch_solve(meshes, workers=8, tune="auto")
+    _, st_warm = batch.batch_solve(meshes, workers=8, tune="auto", lockstep=True)
     t0 = time.perf_counter()
-    _, st = batch.batch_solve(meshes, workers=8, tune="auto")
+    bres, st = batch.batch_solve(meshes, workers=8, tune="auto", lockstep=True, want=("cp", "CL", "CDi"))
     wall = time.perf_counter() - t0
+    # accuracy against the plain FP64 GPU path on a sample of the batch (outside the timing)
+    import cpanel_gb300 as cg
+    acc = {"meshes": [0, 16, 32, 48], "cp_max_abs": 0.0, "cp_max_abs_regular_panels": 0.0, "cp_max_rel": 0.0,
+           "CL_max_rel": 0.0, "CDi_max_rel": 0.0, "degenerate_panels": 0}
+    for q in acc["meshes"]:
+        g = cg.Geometry(meshes[q]["nodes"], meshes[q]["tris"], meshes[q]["ids"])
+        ref = cg.solve_cases(g, meshes[q]["flows"], Sref=meshes[q]["Sref"], bref=meshes[q]["bref"],
+                             cref=meshes[q]["cref"], cg=meshes[q]["cg"], precision="fp64", want=("cp",))
+        del g
+        dcp = np.abs(bres[q]["cp"] - ref["cp"])
+        regular = np.abs(ref["cp"]) <= 100.0
+        acc["cp_max_abs"] = max(acc["cp_max_abs"], float(dcp.max()))
+        acc["cp_max_abs_regular_panels"] = max(acc["cp_max_abs_regular_panels"], float(dcp[regular].max()))
+        acc["cp_max_rel"] = max(acc["cp_max_rel"], float((dcp / np.maximum(1.0, np.abs(ref["cp"]))).max()))
+        acc["CL_max_rel"] = max(acc["CL_max_rel"], float((np.abs(bres[q]["CL"] - ref["CL"]) / np.abs(ref["CL"])).max()))
+        acc["CDi_max_rel"] = max(acc["CDi_max_rel"],
+                                 float((np.abs(bres[q]["CDi"] - ref["CDi"]) / np.abs(ref["CDi"])).max()))
+        acc["degenerate_panels"] += int(np.count_nonzero(~regular[0]))
+    acc["note"] = ("cp_max_rel = max |dCp| / max(1, |Cp_plain|); regular panels: |Cp_plain| <= 100. The random wings' "
+                   "fan-triangulated tip caps hold sliver panels whose CHTLS fit gives |Cp| up to 4e8 in the plain path "
+                   "as in the reference method, where a 1e-10 relative change of mu moves Cp by ~0.1")
     out["batched_uneven"] = {
         "workload": label, "solves": nsol, "wall_s": wall, "solves_per_s": nsol / wall,
-        "ms_topology": st["ms_topology"], "ms_grouped_assembly": st["ms_assembly"], "ms_solve": st["ms_solve"],
+        "ms_topology": st["ms_topology"], "ms_grouped_assembly": st["ms_assembly"],
+        "ms_lockstep_factorization": st["ms_factor"], "ms_lockstep_solves_and_post": st["ms_solve"],
+        "accuracy_vs_plain_fp64": acc,
         "grouped_launch": {"items": st["group"]["items"], "pairs": st["group"]["pairs"],
                            "near_pairs_fp64": st["group"]["near_pairs"], "shape": st["group"]["shape"],
                            "tuned_in_warmup": st_warm["group"]["tuned"] == 1,
                            "candidates_timed": st_warm["group"]["candidates"],
                            "gpairs_per_s": st["group"]["pairs"] / st["group"]["ms"] / 1e6},
         "workers": 8,
-        "how": "cpg_batch_solve: topology on 8 worker threads, one grouped persistent assembly launch, then "
-               "each mesh's LU + 8 refined solves + post on its worker's stream"}
+        "how": "cpg_batch_solve(lockstep=1): topology and post tables on 8 worker threads, one grouped persistent "
+               "assembly launch, the 64 LU factorizations in lockstep (one diagonal-block launch per block step for "
+               "all meshes), the 64 x 8 refined solves in lockstep (one launch per substitution block step), each "
+               "mesh's residuals and post on its worker's stream"}
     # the same 64 wings through the request loop (one assembly launch per mesh), for comparison
     srv = serve.Server(slots=8, budget_gb=160.0, precision="mixed")
     srv.wait(srv.submit(*wings[0][:4], **wings[0][4]))  # warm-up: kernels, cuBLAS plans, workspaces

@@ -73,7 +73,8 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint",
            "cpg_server_submit_vp", "cpg_server_wait_vp", "cpg_server_footprint_vp",
            # cpanel_batch.h
-           "cpg_group_default_shape", "cpg_set_inf_coeff_grouped", "cpg_group_schedule", "cpg_batch_solve"]
+           "cpg_group_default_shape", "cpg_set_inf_coeff_grouped", "cpg_group_schedule", "cpg_batch_solve",
+           "cpg_lu_factor_grouped"]
 
 TUNE_OFF, TUNE_AUTO, TUNE_FORCE = 0, 1, 2
 
@@ -128,12 +129,12 @@ class BatchMesh(C.Structure):
 
 
 class BatchParams(C.Structure):
-    _fields_ = [("workers", C.c_int), ("tune", C.c_int), ("budget_bytes", C.c_double)]
+    _fields_ = [("workers", C.c_int), ("tune", C.c_int), ("budget_bytes", C.c_double), ("lockstep", C.c_int)]
 
 
 class BatchStats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_topology", C.c_double), ("ms_assembly", C.c_double),
-                ("ms_solve", C.c_double), ("waves", C.c_int), ("solves", C.c_int64), ("failed", C.c_int),
+                ("ms_factor", C.c_double), ("ms_solve", C.c_double), ("waves", C.c_int), ("solves", C.c_int64), ("failed", C.c_int),
                 ("group", GroupReport)]
 
 
@@ -216,5 +217,6 @@ def load():
                                             C.POINTER(GroupReport)]
     L.cpg_group_schedule.argtypes = [I64, C.c_int, C.POINTER(GroupShape), I32, C.c_int64, I64, I64]
     L.cpg_batch_solve.argtypes = [vp, C.POINTER(BatchMesh), C.c_int, C.POINTER(BatchParams), C.POINTER(BatchStats)]
+    L.cpg_lu_factor_grouped.argtypes = [C.POINTER(vp), C.c_int, D]
     _lib = L
     return L

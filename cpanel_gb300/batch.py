@@ -3,8 +3,11 @@ assembly with its work-shape autotuner, and the batch solve of uneven meshes.
 
 The reference solves one mesh per process (geometry::readTri -> setInfCoeff,
 CPanel/geometry.cpp:607-621; CPanelMgr::run -> cpCase::run per flow condition,
-CPanel/CPanelMgr.cpp:90-167).  Here m meshes share one launch; per mesh the results are
-bit-identical to ``solve_cases(geom, ..., precision="mixed")``.
+CPanel/CPanelMgr.cpp:90-167).  Here m meshes share one assembly launch (bit-identical to
+each mesh's own); their factorizations and refined solves run either side by side on
+worker streams (bit-identical to each mesh alone) or in lockstep, one launch per block
+step for all meshes (the same factors up to FP32 rounding, so the refined solutions agree
+within the refinement tolerance).
 """
 import ctypes as C
 
@@ -73,8 +76,23 @@ def set_inf_coeff_grouped(geoms, tune="off", shape=None):
     return _report(rep)
 
 
-def batch_solve(meshes, workers=8, tune="auto", budget_gb=0.0, want=("cp", "CL", "CDi"), ctx=None):
-    """Steady mixed-precision solves of many meshes.
+def lu_factor_grouped(geoms):
+    """The mixed path's FP32 LU factorizations of every geometry at once (lockstep block
+    steps); the geometries must hold their mixed matrices.  Returns the device time (ms)."""
+    if not geoms:
+        raise ValueError("no geometries")
+    ctx = geoms[0].ctx
+    arr = (C.c_void_p * len(geoms))(*[g.h.value for g in geoms])
+    ms = C.c_double()
+    ctx.check(ctx.L.cpg_lu_factor_grouped(arr, len(geoms), C.byref(ms)), "cpg_lu_factor_grouped")
+    return ms.value
+
+
+def batch_solve(meshes, workers=8, tune="auto", budget_gb=0.0, want=("cp", "CL", "CDi"), lockstep=False,
+                ctx=None):
+    """Steady mixed-precision solves of many meshes.  lockstep: False = each mesh's LU,
+    refined solves and post on its worker (bit-identical to solve_cases); True = a wave's
+    factorizations and refined solves together, block step by block step.
 
     meshes: list of dicts with nodes, tris, ids, flows [(V, alpha, beta, mach), ...] and
     optional Sref, bref, cref, cg.  Returns (results, stats): one dict per mesh with the
@@ -111,7 +129,7 @@ def batch_solve(meshes, workers=8, tune="auto", budget_gb=0.0, want=("cp", "CL",
         for name in ("cp", "mu", "CL", "CDi"):
             setattr(b, name, _p(o[name]) if name in o else None)
         outs.append(o)
-    prm = _lib.BatchParams(workers, TUNE[tune], budget_gb * 1e9)
+    prm = _lib.BatchParams(workers, TUNE[tune], budget_gb * 1e9, 1 if lockstep else 0)
     st = _lib.BatchStats()
     rc = L.cpg_batch_solve(ctx.h, arr, m, C.byref(prm), C.byref(st))
     res = []
@@ -119,10 +137,12 @@ def batch_solve(meshes, workers=8, tune="auto", budget_gb=0.0, want=("cp", "CL",
         o["status"] = arr[i].status
         o["n_body"] = arr[i].n_body
         for name in ("cp", "mu"):
-            if name in o:
-                o[name] = o[name][:, :arr[i].n_body]
+            if name in o:  # written packed as k x n_body
+                k = o[name].shape[0]
+                o[name] = o[name].ravel()[:k * arr[i].n_body].reshape(k, arr[i].n_body)
         res.append(o)
-    stats = dict(ms_total=st.ms_total, ms_topology=st.ms_topology, ms_assembly=st.ms_assembly, ms_solve=st.ms_solve,
+    stats = dict(ms_total=st.ms_total, ms_topology=st.ms_topology, ms_assembly=st.ms_assembly,
+                 ms_factor=st.ms_factor, ms_solve=st.ms_solve,
                  waves=st.waves, solves=st.solves, failed=st.failed, group=_report(st.group))
     if rc not in (0, 5):
         ctx.check(rc, "cpg_batch_solve")

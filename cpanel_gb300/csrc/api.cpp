@@ -218,8 +218,8 @@ int prepare_post(cpg_geometry* g) {
     T.F3 = g->F3.as<double>();
     T.F2 = g->F2.as<double>();
     T.mode = g->mode.as<int32_t>();
-    CK(cpg::launch_chtls_weights(T, s), "CHTLS weights");
-    // Trefftz tables
+    // Trefftz tables (uploaded before the kernels below: a pageable copy waits for the
+    // work queued before it on its stream)
     std::vector<double> st;
     std::vector<int32_t> ln;
     int nst = 0;
@@ -244,6 +244,7 @@ int prepare_post(cpg_geometry* g) {
     CK(upload(g->tzst, st, s), "upload Trefftz");
     CK(upload(g->tzln, ln, s), "upload Trefftz");
     CK(upload(g->tzpts, H.tz_pts, s), "upload Trefftz");
+    CK(cpg::launch_chtls_weights(T, s), "CHTLS weights");
     CK(g->G.ensure(std::max<size_t>(8, sizeof(double) * T.n_pts * H.n_wake)), "alloc G");
     CK(cpg::launch_wake_potential_op(g->wrec.as<double>(), H.n_wake, g->tzpts.as<double>(), T.n_pts,
                                      g->G.as<double>(), s),
@@ -1202,4 +1203,192 @@ int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cp
     return CPG_OK;
 }
 
+int cpg_lu_factor_grouped(cpg_geometry* const* gs, int m, double* ms_out) {
+    if (!gs || m <= 0) return CPG_E_INVALID;
+    for (int q = 0; q < m; q++)
+        if (!gs[q]) return CPG_E_INVALID;
+    cpg_ctx* ctx = gs[0]->ctx;
+    ProfInstall pi(ctx);
+    for (int q = 0; q < m; q++) {
+        if (gs[q]->ctx->device != ctx->device) return fail(ctx, CPG_E_INVALID, "geometries on different devices");
+        if (!gs[q]->have32) return fail(ctx, CPG_E_INVALID, "no CPG_MIXED matrix: assemble first");
+    }
+    CK(cudaSetDevice(ctx->device), "device");
+    cudaStream_t s = ctx->stream;
+    void* blas = cpg::ctx_blas(ctx);
+    if (!blas) return fail(ctx, CPG_E_CUDA, "cublasCreate failed");
+    std::vector<cpg_ctx*> others;
+    for (int q = 0; q < m; q++)
+        if (gs[q]->ctx != ctx && std::find(others.begin(), others.end(), gs[q]->ctx) == others.end())
+            others.push_back(gs[q]->ctx);
+    cudaEvent_t join, e0, e1;
+    CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "event");
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    struct EvGuard {
+        cudaEvent_t a, b, c;
+        ~EvGuard() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+            cudaEventDestroy(c);
+        }
+    } evg{join, e0, e1};
+    for (cpg_ctx* c : others) {
+        CK(cudaEventRecord(join, c->stream), "event");
+        CK(cudaStreamWaitEvent(s, join, 0), "join");
+    }
+    std::vector<cpg::LuGraphs*> G(m);
+    std::vector<float*> LU(m);
+    std::vector<int64_t> ns(m);
+    std::vector<int*> bad(m);
+    for (int q = 0; q < m; q++) {
+        cpg_geometry* g = gs[q];
+        const int64_t n = g->H.n_body;
+        CK(g->LU.ensure(sizeof(float) * (size_t)n * n), "alloc LU");
+        CK(g->bad.ensure(sizeof(int)), "alloc flag");
+        CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
+        CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");
+        G[q] = &g->graphs;
+        LU[q] = g->LU.as<float>();
+        ns[q] = n;
+        bad[q] = g->bad.as<int>();
+    }
+    CK(cudaEventRecord(e0, s), "event");
+    CK(cpg::lu_factor_batched(blas, G.data(), LU.data(), ns.data(), bad.data(), m, s), "grouped LU factorization");
+    CK(cudaEventRecord(e1, s), "event");
+    for (cpg_ctx* c : others) CK(cudaStreamWaitEvent(c->stream, e1, 0), "join");
+    CK(cudaEventSynchronize(e1), "grouped LU factorization");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_out) *ms_out = ms;
+    for (int q = 0; q < m; q++) gs[q]->lu_ready = true;
+    return CPG_OK;
+}
+
 }  // extern "C"
+
+// ---- grouped solves of the batch path (csrc/batch.cpp) ----
+namespace cpg {
+
+int geometry_prepare_post(cpg_geometry* g) { return g ? prepare_post(g) : CPG_E_INVALID; }
+
+// cpg_solve_cases (CPG_MIXED) for m geometries that hold their mixed matrices and LU factors
+// (cpg_set_inf_coeff_grouped, cpg_lu_factor_grouped): right-hand sides per geometry, the
+// refined solves of all of them in lockstep (substitutions on gs[0]'s context stream), then
+// each one's post-processing; each geometry's own work runs on its context's stream.  status[q]: each geometry's cpg_status; returns the first failure.
+int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* flows, const int* ks,
+                        const cpg_refs* refs, const cpg_case_out* outs, int* status) {
+    if (!gs || m <= 0) return CPG_E_INVALID;
+    cpg_ctx* ctx = gs[0]->ctx;
+    ProfInstall pi(ctx);
+    CK(cudaSetDevice(ctx->device), "device");
+    cudaStream_t s = ctx->stream;
+    cudaEvent_t join;
+    CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "event");
+    for (int q = 0; q < m; q++)
+        if (gs[q]->ctx != ctx) {
+            CK(cudaEventRecord(join, gs[q]->ctx->stream), "event");
+            CK(cudaStreamWaitEvent(s, join, 0), "join");
+        }
+    struct Out {
+        double *mu, *sigma, *rhs, *phi, *cp, *vel, *forces, *tz, *wmu;
+    };
+    std::vector<Out> O(m);
+    std::vector<cpg::RefineMesh> rm(m);
+    for (int q = 0; q < m; q++) {
+        cpg_geometry* g = gs[q];
+        const int k = ks[q];
+        const int64_t n = g->H.n_body, nw = g->H.n_wake;
+        if (!g->have32 || !g->lu_ready || k < 1 || k > 4096) {
+            cudaEventDestroy(join);
+            return fail(ctx, CPG_E_INVALID, "grouped solve: geometry without mixed matrix or factors, or bad k");
+        }
+        int rc = prepare_post(g);
+        if (rc != CPG_OK) {
+            cudaEventDestroy(join);
+            return rc;
+        }
+        cudaStream_t t = g->ctx->stream;  // this geometry's own work
+        std::vector<cpg::CaseScalars> cs(k);
+        for (int c = 0; c < k; c++) case_scalars(flows[q][c], refs[q], cs[c]);
+        CK(upload(g->cases, cs, t), "upload cases");
+        const size_t kn = (size_t)k * n;
+        const size_t need = sizeof(double) * (8 * kn + 9 * (size_t)k + 2 * (size_t)k + (size_t)k * nw) + 8 * 256;
+        CK(g->outs.ensure(need), "alloc outputs");
+        Out& o = O[q];
+        o.mu = g->outs.as<double>();
+        o.sigma = o.mu + kn;
+        o.rhs = o.sigma + kn;
+        o.phi = o.rhs + kn;
+        o.cp = o.phi + kn;
+        o.vel = o.cp + kn;
+        o.forces = o.vel + 3 * kn;
+        o.tz = o.forces + 9 * (size_t)k;
+        o.wmu = o.tz + 2 * (size_t)k;
+        CK(g->work.ensure(cpg::solve_lu_work_bytes(n, k)), "alloc solver workspace");
+        const cpg::CaseScalars* dcs = g->cases.as<cpg::CaseScalars>();
+        CK(cpg::launch_sigma(g->rec.as<double>(), n, k, dcs, o.sigma, t), "sigma");
+        CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, o.rhs, t), "rhs");
+        rm[q] = cpg::RefineMesh{g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(), g->graphs.dinv, n, k,
+                                o.rhs, o.mu, g->work.p, t};
+    }
+    cudaEventDestroy(join);
+    std::vector<cpg::SolveStats> st(m);
+    CK(cpg::solve_lu_refined_batched(rm.data(), m, kMixedRefineTol, 16, st.data(), s), "refined solves (grouped)");
+    for (int q = 0; q < m; q++) {
+        cpg_geometry* g = gs[q];
+        const int k = ks[q];
+        cudaStream_t t = g->ctx->stream;
+        CK(g->post_work.ensure(cpg::post_work_bytes(g->T, k)), "alloc post workspace");
+        CK(cudaStreamWaitEvent(t, g->post_ev, 0), "wait for the post tables");
+        const Out& o = O[q];
+        CK(cpg::launch_post(g->T, k, g->cases.as<cpg::CaseScalars>(), o.mu, o.phi, o.vel, o.cp, o.forces, o.tz, o.wmu,
+                            g->post_work.p, t),
+           "post");
+    }
+    std::vector<std::vector<double>> hf(m), ht(m);
+    for (int q = 0; q < m; q++) {
+        const int k = ks[q];
+        const size_t kn = (size_t)k * gs[q]->H.n_body;
+        const Out& o = O[q];
+        const cpg_case_out* co = outs ? &outs[q] : nullptr;
+        cudaStream_t t = gs[q]->ctx->stream;
+        auto copy = [&](double* dst, const double* src, size_t cnt) -> cudaError_t {
+            if (!dst) return cudaSuccess;
+            return cudaMemcpyAsync(dst, src, sizeof(double) * cnt, cudaMemcpyDeviceToHost, t);
+        };
+        if (co) {
+            CK(copy(co->mu, o.mu, kn), "copy mu");
+            CK(copy(co->sigma, o.sigma, kn), "copy sigma");
+            CK(copy(co->phi, o.phi, kn), "copy phi");
+            CK(copy(co->vel, o.vel, 3 * kn), "copy vel");
+            CK(copy(co->cp, o.cp, kn), "copy cp");
+        }
+        hf[q].resize(9 * (size_t)k);
+        ht[q].resize(2 * (size_t)k);
+        CK(cudaMemcpyAsync(hf[q].data(), o.forces, sizeof(double) * 9 * k, cudaMemcpyDeviceToHost, t), "copy forces");
+        CK(cudaMemcpyAsync(ht[q].data(), o.tz, sizeof(double) * 2 * k, cudaMemcpyDeviceToHost, t), "copy CL");
+    }
+    for (int q = 0; q < m; q++) CK(cudaStreamSynchronize(gs[q]->ctx->stream), "grouped solves");
+    int first = CPG_OK;
+    for (int q = 0; q < m; q++) {
+        const int k = ks[q];
+        const cpg_case_out* co = outs ? &outs[q] : nullptr;
+        if (co)
+            for (int c = 0; c < k; c++) {
+                if (co->CL) co->CL[c] = ht[q][2 * c];
+                if (co->CDi) co->CDi[c] = ht[q][2 * c + 1];
+                for (int a = 0; a < 3; a++) {
+                    if (co->Fbody) co->Fbody[3 * c + a] = hf[q][9 * c + a];
+                    if (co->Fwind) co->Fwind[3 * c + a] = hf[q][9 * c + 3 + a];
+                    if (co->CM) co->CM[3 * c + a] = hf[q][9 * c + 6 + a];
+                }
+            }
+        status[q] = st[q].residual_max > 1e-9 ? CPG_E_NOT_CONVERGED : CPG_OK;
+        if (status[q] != CPG_OK && first == CPG_OK) first = status[q];
+    }
+    if (first != CPG_OK) ctx_set_error(ctx, "grouped solve: a system stopped above tolerance");
+    return first;
+}
+
+}  // namespace cpg

@@ -117,6 +117,8 @@ cudaError_t residual_df(const float* A32, const float* Alo, int64_t n, int k, co
 double measure_fp64_tflops(cudaStream_t s);
 // Squared column norms of a k x n case-major FP64 block, copied to host[0..k).
 cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, double* dd, double* host, cudaStream_t s);
+// The same into dd[0..k) on the device (no copy, no synchronization).
+cudaError_t column_norms2_device(const double* v, int64_t n, int k, double* part, double* dd, cudaStream_t s);
 
 // lu.cu: FP32 LU without pivoting (blocked, cuBLAS trailing GEMM) and the refined
 // solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.  The substitutions
@@ -138,6 +140,41 @@ struct LuGraphs {
     void release();
 };
 cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);
+// One matrix of a lockstep factorization (device copy).
+struct LuBatchMesh {
+    float* LU;
+    float* dinv;
+    int64_t n;
+    int* bad;
+};
+// The factorization of lu_factor_fp32 for m matrices at once (LUs[q]: n_q x n_q, A32 copied
+// in; Gs[q] receives the diagonal-block inverses the substitutions use), every block step
+// taken for all matrices in one launch.  Issued on s with the cuBLAS handle blas.
+cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs, const int64_t* ns,
+                              int* const* bads, int m, cudaStream_t s);
+// One system of a lockstep refined solve: A = A32 + Alo (n x n), its FP32 factors LU with
+// the diagonal-block inverses dinv (from lu_factor_fp32 or lu_factor_batched), k right-hand
+// sides rhs (k x n) -> x; work: solve_lu_work_bytes(n, k) bytes.
+struct RefineMesh {
+    const float* A32;
+    const float* Alo;
+    const float* LU;
+    const float* dinv;
+    int64_t n;
+    int k;
+    const double* rhs;
+    double* x;
+    void* work;
+    cudaStream_t stream;  // this system's own work (null: the driver's stream)
+};
+// solve_lu_refined for m systems at once: every refinement pass does the forward and
+// backward block substitutions of all systems still above tol together (one launch per
+// block step and direction for all of them), then each system's exact-product residual.
+// Each system stops at relative residual tol (or max_steps passes) as solve_lu_refined does;
+// st[q] receives its pass count and final residual.  The substitutions run on s, each
+// system's conversions, residual and norms on its own stream (joined and forked by events).
+cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, int max_steps, SolveStats* st,
+                                     cudaStream_t s);
 cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
 size_t solve_lu_work_bytes(int64_t n, int k);
 // Ainv (optional): an FP32 inverse of A; the correction of each pass is then Ainv r

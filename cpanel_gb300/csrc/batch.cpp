@@ -4,12 +4,16 @@
 // calls setInfCoeff (CPanel/geometry.cpp:607-621), then CPanelMgr::run runs cpCase::run
 // once per flow condition (CPanel/CPanelMgr.cpp:90-167, CPanel/cpCase.cpp:31-139).
 // Here m meshes run together on one GPU:
-//   1. topology and uploads on worker threads, one context (stream, cuBLAS handle) each,
-//      the meshes dealt out costliest first to the least loaded worker;
+//   1. topology, uploads and the post-processing tables (CHTLS weights, Trefftz operator)
+//      on worker threads, one context (stream, cuBLAS handle) each, the meshes dealt out
+//      costliest first to the least loaded worker;
 //   2. one grouped, persistent mixed-precision assembly per wave of meshes that fits the
 //      memory budget (cpg_set_inf_coeff_grouped);
-//   3. each mesh's FP32 LU, refined solves and post-processing (cpg_solve_cases) on its
-//      worker's stream, the workers side by side;
+//   3. either each mesh's FP32 LU, refined solves and post-processing (cpg_solve_cases) on
+//      its worker's stream, the workers side by side; or (lockstep) the wave's
+//      factorizations together (cpg_lu_factor_grouped: one diagonal-block launch per block
+//      step for every mesh), then the wave's refined solves together (one launch per
+//      substitution block step for every mesh) and each mesh's post-processing;
 //   4. the wave's device memory released once every worker of the wave is done (a
 //      cudaFree synchronizes the device, so none runs while other workers compute).
 #include <cuda_runtime.h>
@@ -26,6 +30,9 @@
 
 namespace cpg {
 int ctx_workers(cpg_ctx* ctx, int w, std::vector<cpg_ctx*>& out);
+int geometry_prepare_post(cpg_geometry* g);
+int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* flows, const int* ks,
+                        const cpg_refs* refs, const cpg_case_out* outs, int* status);
 int ctx_device(cpg_ctx* ctx);
 void ctx_set_error(cpg_ctx* ctx, const std::string& msg);
 }  // namespace cpg
@@ -58,6 +65,7 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
     int W = (p && p->workers > 0) ? p->workers : 8;
     W = std::max(1, std::min({W, m, 64}));
     const int tune = p ? p->tune : CPG_TUNE_AUTO;
+    const bool lockstep = p && p->lockstep != 0;
     if (tune < CPG_TUNE_OFF || tune > CPG_TUNE_FORCE) {
         cpg::ctx_set_error(ctx, "unknown tune mode");
         return CPG_E_INVALID;
@@ -102,6 +110,13 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
                 cpg_geometry_info_get(gi, &info);
                 M[i].n_body = info.n_body;
                 g[i] = gi;
+                // CHTLS weights and the Trefftz operator on the worker's second stream,
+                // beside the grouped assembly
+                M[i].status = r = cpg::geometry_prepare_post(gi);
+                if (r != CPG_OK) {
+                    cpg_geometry_destroy(gi);
+                    g[i] = nullptr;
+                }
             }
         }
     });
@@ -130,7 +145,7 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
         waves.back().push_back(i);
         used += fp;
     }
-    double ms_assembly = 0, ms_solve = 0;
+    double ms_assembly = 0, ms_factor = 0, ms_solve = 0;
     cpg_group_report last{};
     for (const std::vector<int>& wave : waves) {
         std::vector<cpg_geometry*> gs;
@@ -142,6 +157,37 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
         } else {
             ms_assembly += rep.ms;
             last = rep;
+            if (lockstep) {  // the wave's factorizations and refined solves in lockstep
+                double fms = 0;
+                r = cpg_lu_factor_grouped(gs.data(), (int)gs.size(), &fms);
+                ms_factor += fms;
+                if (r != CPG_OK)
+                    for (int i : wave) M[i].status = r;
+            }
+        }
+        if (r == CPG_OK && lockstep) {
+            const auto T1 = std::chrono::steady_clock::now();
+            std::vector<const cpg_flow*> fl;
+            std::vector<int> ks, stv(wave.size(), CPG_OK);
+            std::vector<cpg_refs> rf;
+            std::vector<cpg_case_out> outs(wave.size());
+            for (size_t j = 0; j < wave.size(); j++) {
+                const cpg_batch_mesh& b = M[wave[j]];
+                fl.push_back(b.flows);
+                ks.push_back(b.k);
+                rf.push_back(b.refs);
+                outs[j] = cpg_case_out{};
+                outs[j].mu = b.mu;
+                outs[j].cp = b.cp;
+                outs[j].CL = b.CL;
+                outs[j].CDi = b.CDi;
+            }
+            const int rs = cpg::solve_cases_grouped(gs.data(), (int)gs.size(), fl.data(), ks.data(), rf.data(),
+                                                    outs.data(), stv.data());
+            for (size_t j = 0; j < wave.size(); j++)
+                M[wave[j]].status = (rs != CPG_OK && rs != CPG_E_NOT_CONVERGED) ? rs : stv[j];
+            ms_solve += ms_since(T1);
+        } else if (r == CPG_OK) {
             // 3. factorizations, refined solves and post on the workers
             const auto T1 = std::chrono::steady_clock::now();
             on_workers(W, device, [&](int w) {
@@ -181,6 +227,7 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
         st->ms_total = ms_since(T0);
         st->ms_topology = ms_topology;
         st->ms_assembly = ms_assembly;
+        st->ms_factor = ms_factor;
         st->ms_solve = ms_solve;
         st->waves = (int)waves.size();
         st->solves = solves;

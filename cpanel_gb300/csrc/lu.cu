@@ -43,9 +43,8 @@ constexpr int DIAG_SMEM = (3 * NB * P + 6 * BS * TP) * 4;
 // d = 1..3 from the diagonal:
 // Linv[I][J] = -Linv[I][I] sum_{K=J}^{I-1} L[I][K] Linv[K][J] and
 // Uinv[I][J] = -Uinv[I][I] sum_{K=I+1}^{J} U[I][K] Uinv[K][J].
-__global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
-                                                float* __restrict__ Dinv, int* bad) {
-    extern __shared__ float sm[];
+__device__ __forceinline__ void lu_diag_body(float* sm, float* __restrict__ A, int64_t n, int64_t K, int b,
+                                             float* __restrict__ Dinv, int* bad) {
     float* S = sm;                 // S[r*P + c]
     float* ZL = sm + NB * P;       // L^{-1}, row-major
     float* ZU = sm + 2 * NB * P;   // U^{-1}, row-major
@@ -193,6 +192,302 @@ __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n
     }
 }
 
+__global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
+                                                float* __restrict__ Dinv, int* bad) {
+    extern __shared__ float sm[];
+    lu_diag_body(sm, A, n, K, b, Dinv, bad);
+}
+
+// ---- lockstep factorization of many matrices (the batch path) ----
+// Every kernel below takes work items of LB_ITEM ints: mesh, r0, r1, c0, c1, K, b, unused.
+// The matrices are column-major with their own order n (LU[c*n + r]).
+constexpr int LB_ITEM = 8;
+
+// diagonal block K of every listed mesh, one block of DT threads each
+__global__ void __launch_bounds__(DT) k_lu_diag_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                        const int* __restrict__ items) {
+    extern __shared__ float sm[];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    lu_diag_body(sm, d.LU, d.n, it[5], it[6], d.dinv, d.bad);
+}
+
+// L21 = A21 U_KK^{-1} in place for rows [r0, r1), columns K..K+b.  256 threads: thread t
+// owns row t % 64 and the 32 columns 32 (t / 64) ..; U^{-1} staged 16 rows at a time.
+constexpr int CS_R = 64;
+__global__ void __launch_bounds__(256) k_col_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                           const int* __restrict__ items) {
+    __shared__ float X[CS_R][NB + 1];
+    __shared__ __align__(16) float U[16][NB];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    const int64_t n = d.n, r0 = it[1], r1 = it[2], K = it[5];
+    const int b = it[6];
+    float* A = d.LU;
+    const float* Ui = d.dinv + (K / NB) * 2 * NB * NB + NB * NB;  // column-major, ld NB
+    const int t = threadIdx.x, r = t % CS_R, cg = t / CS_R;
+    for (int idx = t; idx < CS_R * NB; idx += 256) {
+        const int c = idx / CS_R, rr = idx % CS_R;
+        X[rr][c] = (r0 + rr < r1 && c < b) ? A[(K + c) * n + r0 + rr] : 0.f;
+    }
+    float acc[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) acc[j] = 0.f;
+    for (int k0 = 0; k0 < b; k0 += 16) {
+        __syncthreads();
+        for (int idx = t; idx < 16 * NB; idx += 256) {
+            const int kk = idx % 16, c = idx / 16;
+            U[kk][c] = (k0 + kk < b && c < b) ? Ui[(k0 + kk) + (int64_t)c * NB] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < 16; kk++) {
+            const float a = X[r][k0 + kk];
+            const float4* u4 = reinterpret_cast<const float4*>(&U[kk][32 * cg]);
+#pragma unroll
+            for (int j4 = 0; j4 < 8; j4++) {
+                const float4 u = u4[j4];
+                acc[4 * j4] = __fmaf_rn(a, u.x, acc[4 * j4]);
+                acc[4 * j4 + 1] = __fmaf_rn(a, u.y, acc[4 * j4 + 1]);
+                acc[4 * j4 + 2] = __fmaf_rn(a, u.z, acc[4 * j4 + 2]);
+                acc[4 * j4 + 3] = __fmaf_rn(a, u.w, acc[4 * j4 + 3]);
+            }
+        }
+    }
+    if (r0 + r < r1) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int c = 32 * cg + j;
+            if (c < b) A[(K + c) * n + r0 + r] = acc[j];
+        }
+    }
+}
+
+// U12 = L_KK^{-1} A12 in place for rows K..K+b, columns [c0, c1) (at most 64).  256
+// threads: thread t owns row t % 128 and the 32 columns 32 (t / 128) ..; L^{-1} staged 16
+// columns at a time.
+constexpr int RS_C = 64;
+__global__ void __launch_bounds__(256) k_row_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                           const int* __restrict__ items) {
+    __shared__ __align__(16) float X[NB][RS_C + 4];
+    __shared__ float L[16][NB + 1];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    const int64_t n = d.n, c0 = it[3], c1 = it[4], K = it[5];
+    const int b = it[6];
+    float* A = d.LU;
+    const float* Li = d.dinv + (K / NB) * 2 * NB * NB;  // column-major, ld NB
+    const int t = threadIdx.x, r = t % NB, cg = t / NB;
+    for (int idx = t; idx < NB * RS_C; idx += 256) {
+        const int c = idx / NB, k = idx % NB;
+        X[k][c] = (k < b && c0 + c < c1) ? A[(c0 + c) * n + K + k] : 0.f;
+    }
+    float acc[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) acc[j] = 0.f;
+    for (int k0 = 0; k0 < b; k0 += 16) {
+        __syncthreads();
+        for (int idx = t; idx < 16 * NB; idx += 256) {
+            const int kk = idx / NB, rr = idx % NB;
+            L[kk][rr] = (k0 + kk < b && rr < b) ? Li[rr + (int64_t)(k0 + kk) * NB] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < 16; kk++) {
+            const float a = L[kk][r];
+            const float4* x4 = reinterpret_cast<const float4*>(&X[k0 + kk][32 * cg]);
+#pragma unroll
+            for (int j4 = 0; j4 < 8; j4++) {
+                const float4 x = x4[j4];
+                acc[4 * j4] = __fmaf_rn(a, x.x, acc[4 * j4]);
+                acc[4 * j4 + 1] = __fmaf_rn(a, x.y, acc[4 * j4 + 1]);
+                acc[4 * j4 + 2] = __fmaf_rn(a, x.z, acc[4 * j4 + 2]);
+                acc[4 * j4 + 3] = __fmaf_rn(a, x.w, acc[4 * j4 + 3]);
+            }
+        }
+    }
+    if (r < b) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int64_t c = c0 + 32 * cg + j;
+            if (c < c1) A[c * n + K + r] = acc[j];
+        }
+    }
+}
+
+// C -= L(:, K..K+b) U(K..K+b, :) on the tile rows [r0, min(r0 + 128, r1)) x columns
+// [c0, min(c0 + 64, c1)).  256 threads: thread t owns row t % 128 and 32 columns.
+constexpr int GS_R = 128, GS_C = 64, GS_K = 32;
+__global__ void __launch_bounds__(256) k_gemm_sub_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                          const int* __restrict__ items) {
+    __shared__ float Ls[GS_K][GS_R];
+    __shared__ __align__(16) float Us[GS_K][GS_C + 4];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    const int64_t n = d.n, r0 = it[1], r1 = it[2], c0 = it[3], c1 = it[4], K = it[5];
+    const int b = it[6];
+    float* A = d.LU;
+    const int t = threadIdx.x, r = t % GS_R, cg = t / GS_R;
+    float acc[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) acc[j] = 0.f;
+    for (int k0 = 0; k0 < b; k0 += GS_K) {
+        __syncthreads();
+        for (int idx = t; idx < GS_K * GS_R; idx += 256) {
+            const int kk = idx / GS_R, rr = idx % GS_R;
+            Ls[kk][rr] = (k0 + kk < b && r0 + rr < r1) ? A[(K + k0 + kk) * n + r0 + rr] : 0.f;
+        }
+        for (int idx = t; idx < GS_K * GS_C; idx += 256) {
+            const int kk = idx % GS_K, c = idx / GS_K;
+            Us[kk][c] = (k0 + kk < b && c0 + c < c1) ? A[(c0 + c) * n + K + k0 + kk] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < GS_K; kk++) {
+            const float a = Ls[kk][r];
+            const float4* u4 = reinterpret_cast<const float4*>(&Us[kk][32 * cg]);
+#pragma unroll
+            for (int j4 = 0; j4 < 8; j4++) {
+                const float4 u = u4[j4];
+                acc[4 * j4] = __fmaf_rn(a, u.x, acc[4 * j4]);
+                acc[4 * j4 + 1] = __fmaf_rn(a, u.y, acc[4 * j4 + 1]);
+                acc[4 * j4 + 2] = __fmaf_rn(a, u.z, acc[4 * j4 + 2]);
+                acc[4 * j4 + 3] = __fmaf_rn(a, u.w, acc[4 * j4 + 3]);
+            }
+        }
+    }
+    if (r0 + r < r1) {
+#pragma unroll
+        for (int j = 0; j < 32; j++) {
+            const int64_t c = c0 + 32 * cg + j;
+            if (c < c1) {
+                float* p = A + c * n + r0 + r;
+                *p = *p - acc[j];
+            }
+        }
+    }
+}
+
+// ---- lockstep block substitutions (the batch path's refined solves) ----
+// X and Y are n x k (ld n); items of LB_ITEM ints: mesh, r0, r1, -, -, K, b, -.
+struct SubstMesh {
+    const float* LU;
+    const float* dinv;
+    float* X;
+    float* Y;
+    int64_t n;
+    int k;
+    int pad;
+};
+// KC right-hand sides per pass over the block (8, 16 or 32: the smallest that holds k,
+// or 32 in passes); the staged block Z is read as float4.
+
+// forward (dir 0): Y_K = L_KK^{-1} X_K; backward (dir 1): X_K = U_KK^{-1} Y_K.  One block of
+// NB threads per system, thread r computing row r.
+template <int KC>
+__global__ void __launch_bounds__(NB) k_subst_diag_batched(const SubstMesh* __restrict__ ms,
+                                                           const int* __restrict__ items,
+                                                           const int* __restrict__ active, int dir) {
+    __shared__ __align__(16) float Z[NB][KC];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    if (!active[it[0]]) return;
+    const SubstMesh d = ms[it[0]];
+    const int64_t n = d.n, K = it[5];
+    const int b = it[6], r = threadIdx.x;
+    const float* Mi = d.dinv + (K / NB) * 2 * NB * NB + (dir ? NB * NB : 0);  // column-major, ld NB
+    const float* src = dir ? d.Y : d.X;
+    float* dst = dir ? d.X : d.Y;
+    for (int c0 = 0; c0 < d.k; c0 += KC) {
+        const int kc = min(KC, d.k - c0);
+        __syncthreads();
+        for (int idx = r; idx < NB * KC; idx += NB) {
+            const int c = idx / NB, j = idx % NB;
+            Z[j][c] = (j < b && c < kc) ? src[(int64_t)(c0 + c) * n + K + j] : 0.f;
+        }
+        __syncthreads();
+        float acc[KC];
+#pragma unroll
+        for (int c = 0; c < KC; c++) acc[c] = 0.f;
+#pragma unroll 4
+        for (int j = 0; j < b; j++) {
+            const float a = Mi[r + j * NB];
+            const float4* z4 = reinterpret_cast<const float4*>(&Z[j][0]);
+#pragma unroll
+            for (int c4 = 0; c4 < KC / 4; c4++) {
+                const float4 z = z4[c4];
+                acc[4 * c4] = __fmaf_rn(a, z.x, acc[4 * c4]);
+                acc[4 * c4 + 1] = __fmaf_rn(a, z.y, acc[4 * c4 + 1]);
+                acc[4 * c4 + 2] = __fmaf_rn(a, z.z, acc[4 * c4 + 2]);
+                acc[4 * c4 + 3] = __fmaf_rn(a, z.w, acc[4 * c4 + 3]);
+            }
+        }
+        if (r < b) {
+#pragma unroll
+            for (int c = 0; c < KC; c++)
+                if (c < kc) dst[(int64_t)(c0 + c) * n + K + r] = acc[c];
+        }
+    }
+}
+
+// forward (dir 0): X_i -= L(i, K..K+b) Y_K for the rows i in [r0, min(r0 + NB, r1)) below the
+// block; backward (dir 1): Y_i -= U(i, K..K+b) X_K for rows above it.  Thread r owns row r0 + r.
+template <int KC>
+__global__ void __launch_bounds__(NB) k_subst_update_batched(const SubstMesh* __restrict__ ms,
+                                                             const int* __restrict__ items,
+                                                             const int* __restrict__ active, int dir) {
+    __shared__ __align__(16) float Z[NB][KC];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    if (!active[it[0]]) return;
+    const SubstMesh d = ms[it[0]];
+    const int64_t n = d.n, r0 = it[1], r1 = it[2], K = it[5];
+    const int b = it[6], r = threadIdx.x;
+    const int64_t i = r0 + r;
+    const float* src = dir ? d.X : d.Y;
+    float* dst = dir ? d.Y : d.X;
+    for (int c0 = 0; c0 < d.k; c0 += KC) {
+        const int kc = min(KC, d.k - c0);
+        __syncthreads();
+        for (int idx = r; idx < NB * KC; idx += NB) {
+            const int c = idx / NB, j = idx % NB;
+            Z[j][c] = (j < b && c < kc) ? src[(int64_t)(c0 + c) * n + K + j] : 0.f;
+        }
+        __syncthreads();
+        if (i < r1) {
+            float acc[KC];
+#pragma unroll
+            for (int c = 0; c < KC; c++) acc[c] = 0.f;
+            const float* Lp = d.LU + K * n + i;
+#pragma unroll 4
+            for (int j = 0; j < b; j++) {
+                const float a = Lp[(int64_t)j * n];
+                const float4* z4 = reinterpret_cast<const float4*>(&Z[j][0]);
+#pragma unroll
+                for (int c4 = 0; c4 < KC / 4; c4++) {
+                    const float4 z = z4[c4];
+                    acc[4 * c4] = __fmaf_rn(a, z.x, acc[4 * c4]);
+                    acc[4 * c4 + 1] = __fmaf_rn(a, z.y, acc[4 * c4 + 1]);
+                    acc[4 * c4 + 2] = __fmaf_rn(a, z.z, acc[4 * c4 + 2]);
+                    acc[4 * c4 + 3] = __fmaf_rn(a, z.w, acc[4 * c4 + 3]);
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < KC; c++)
+                if (c < kc) {
+                    float* p = dst + (int64_t)(c0 + c) * n + i;
+                    *p = *p - acc[c];
+                }
+        }
+    }
+}
+
+template <int KC>
+void subst_launch(int kind, unsigned g, const SubstMesh* d, const int* it, const int* act, int dir, cudaStream_t s) {
+    if (kind == 0)
+        k_subst_diag_batched<KC><<<g, NB, 0, s>>>(d, it, act, dir);
+    else
+        k_subst_update_batched<KC><<<g, NB, 0, s>>>(d, it, act, dir);
+}
+
 __global__ void k_d2f(const double* __restrict__ a, float* __restrict__ b, int64_t m) {
     int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < m) b[t] = (float)a[t];
@@ -210,7 +505,11 @@ void set_attrs() {
     int dev = 0;
     cudaGetDevice(&dev);
     std::call_once(once[dev & 63],
-                   [] { cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM); });
+                   [] {
+                       cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
+                       cudaFuncSetAttribute(k_lu_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            DIAG_SMEM);
+                   });
 }
 
 // GEMM arithmetic of the factorization: BF16x9 emulation of FP32 on the tensor cores by
@@ -487,6 +786,362 @@ cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* b
     const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
     ProfScope ps(Prof::LU_FACTOR, s);
     return factor_body(st, G, LU, G->dinv, G->panel, n, bad);
+}
+
+// Lockstep factorization of m matrices: the same two-level blocked LU as factor_body
+// (inner blocks of NB columns inside outer panels of outer_width() columns), with each
+// step taken for every matrix at once.  Block step K is one launch of the diagonal
+// kernel with one thread block per matrix that still has a block at K, then one launch
+// each of the column solve, the in-panel row solve and the in-panel update over all
+// matrices; after an outer panel, the U rows right of it by blocked forward substitution
+// (two launches per inner block), then the rank-OB update of each matrix through cuBLAS
+// (BF16x9).  The work items of every launch are planned on the host and uploaded once.
+// No look-ahead stream: the diagonal blocks of all matrices run side by side instead.
+cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs, const int64_t* ns,
+                              int* const* bads, int m, cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    set_attrs();
+    cublasHandle_t h = (cublasHandle_t)blas;
+    cudaError_t e = prepare_blas(h, Gs[0], s);
+    if (e != cudaSuccess) return e;
+    std::vector<LuBatchMesh> desc(m);
+    int64_t nmax = 0;
+    for (int q = 0; q < m; q++) {
+        LuGraphs* G = Gs[q];
+        const int64_t n = ns[q];
+        if (G->factor_n != n || !G->dinv) {
+            if (G->solve) cudaGraphExecDestroy(G->solve);  // it holds the old Dinv
+            G->solve = nullptr;
+            if (G->dinv) cudaFree(G->dinv);
+            G->dinv = nullptr;
+            const size_t nb = (size_t)((n + NB - 1) / NB);
+            if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
+            G->factor_n = n;
+        }
+        desc[q] = LuBatchMesh{LUs[q], G->dinv, n, bads[q]};
+        nmax = std::max(nmax, n);
+    }
+    // ---- plan
+    enum { DIAG = 0, COLS = 1, ROWS = 2, GEMM = 3, RANK = 4 };
+    struct Step {
+        int kind;
+        int64_t off, cnt;
+        int q;
+        int64_t KO, KE;
+    };
+    std::vector<Step> plan;
+    std::vector<int> items;
+    auto add = [&](int q, int64_t r0, int64_t r1, int64_t c0, int64_t c1, int64_t K, int b) {
+        const int v[LB_ITEM] = {q, (int)r0, (int)r1, (int)c0, (int)c1, (int)K, b, 0};
+        items.insert(items.end(), v, v + LB_ITEM);
+    };
+    int64_t mark = 0;
+    auto open = [&]() { mark = (int64_t)items.size() / LB_ITEM; };
+    auto close = [&](int kind) {
+        const int64_t now = (int64_t)items.size() / LB_ITEM;
+        if (now > mark) plan.push_back(Step{kind, mark, now - mark, -1, 0, 0});
+    };
+    const int64_t OB = outer_width();
+    for (int64_t KO = 0; KO < nmax; KO += OB) {
+        for (int64_t K = KO; K < KO + OB && K < nmax; K += NB) {
+            open();
+            for (int q = 0; q < m; q++)
+                if (K < ns[q]) add(q, 0, 0, 0, 0, K, (int)std::min<int64_t>(NB, ns[q] - K));
+            close(DIAG);
+            open();
+            for (int q = 0; q < m; q++) {
+                const int64_t n = ns[q];
+                if (K >= n) continue;
+                const int b = (int)std::min<int64_t>(NB, n - K);
+                for (int64_t r0 = K + b; r0 < n; r0 += CS_R) add(q, r0, n, 0, 0, K, b);
+            }
+            close(COLS);
+            open();
+            for (int q = 0; q < m; q++) {
+                const int64_t n = ns[q], KE = std::min(KO + OB, n);
+                if (K >= n) continue;
+                const int b = (int)std::min<int64_t>(NB, n - K);
+                for (int64_t c0 = K + b; c0 < KE; c0 += RS_C) add(q, 0, 0, c0, KE, K, b);
+            }
+            close(ROWS);
+            open();
+            for (int q = 0; q < m; q++) {
+                const int64_t n = ns[q], KE = std::min(KO + OB, n);
+                if (K >= n) continue;
+                const int b = (int)std::min<int64_t>(NB, n - K);
+                for (int64_t r0 = K + b; r0 < n; r0 += GS_R)
+                    for (int64_t c0 = K + b; c0 < KE; c0 += GS_C) add(q, r0, n, c0, KE, K, b);
+            }
+            close(GEMM);
+        }
+        // U rows right of the panel: forward substitution by inner blocks
+        for (int64_t K = KO; K < KO + OB; K += NB) {
+            open();
+            for (int q = 0; q < m; q++) {
+                const int64_t n = ns[q], KE = KO + OB;
+                if (KE >= n) continue;  // no columns right of the panel
+                for (int64_t c0 = KE; c0 < n; c0 += RS_C) add(q, 0, 0, c0, n, K, NB);
+            }
+            close(ROWS);
+            open();
+            for (int q = 0; q < m; q++) {
+                const int64_t n = ns[q], KE = KO + OB;
+                if (KE >= n) continue;
+                for (int64_t r0 = K + NB; r0 < KE; r0 += GS_R)
+                    for (int64_t c0 = KE; c0 < n; c0 += GS_C) add(q, r0, KE, c0, n, K, NB);
+            }
+            close(GEMM);
+        }
+        for (int q = 0; q < m; q++)
+            if (KO + OB < ns[q]) plan.push_back(Step{RANK, 0, 0, q, KO, KO + OB});
+    }
+    // ---- upload and issue
+    LuBatchMesh* ddesc = nullptr;
+    int* ditems = nullptr;
+    if ((e = cudaMallocAsync((void**)&ddesc, sizeof(LuBatchMesh) * m, s)) != cudaSuccess) return e;
+    if ((e = cudaMallocAsync((void**)&ditems, sizeof(int) * std::max<size_t>(1, items.size()), s)) != cudaSuccess) {
+        cudaFreeAsync(ddesc, s);
+        return e;
+    }
+    e = cudaMemcpyAsync(ddesc, desc.data(), sizeof(LuBatchMesh) * m, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !items.empty())
+        e = cudaMemcpyAsync(ditems, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, s);
+    {
+        ProfScope ps(Prof::LU_FACTOR, s);
+        for (size_t t = 0; t < plan.size() && e == cudaSuccess; t++) {
+            const Step& st = plan[t];
+            const int* it = ditems + st.off * LB_ITEM;
+            const unsigned g = (unsigned)st.cnt;
+            switch (st.kind) {
+                case DIAG: k_lu_diag_batched<<<g, DT, DIAG_SMEM, s>>>(ddesc, it); break;
+                case COLS: k_col_solve_batched<<<g, 256, 0, s>>>(ddesc, it); break;
+                case ROWS: k_row_solve_batched<<<g, 256, 0, s>>>(ddesc, it); break;
+                case GEMM: k_gemm_sub_batched<<<g, 256, 0, s>>>(ddesc, it); break;
+                default: {
+                    const int64_t n = ns[st.q];
+                    e = trailing(h, LUs[st.q], n, st.KO, (int)(st.KE - st.KO), st.KE, n - st.KE, st.KE, n - st.KE);
+                }
+            }
+            if (e == cudaSuccess) e = cudaGetLastError();
+        }
+    }
+    cudaFreeAsync(ditems, s);
+    cudaFreeAsync(ddesc, s);
+    return e;
+}
+
+cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, int max_steps, SolveStats* st,
+                                     cudaStream_t s) {
+    if (m <= 0) return cudaSuccess;
+    struct Bufs {
+        double *r64, *P64, *part, *dd;
+        float *d32, *y32;
+    };
+    std::vector<Bufs> B(m);
+    std::vector<SubstMesh> desc(m);
+    int64_t maxnb = 0;
+    int kmax = 1;
+    // each system's own work (conversions, residuals, norms) on its own stream; the
+    // substitutions of all of them on s between a join and a fork
+    std::vector<cudaStream_t> own;
+    for (int q = 0; q < m; q++) {
+        cudaStream_t t = ms[q].stream ? ms[q].stream : s;
+        if (t != s && std::find(own.begin(), own.end(), t) == own.end()) own.push_back(t);
+    }
+    auto sq = [&](int q) { return ms[q].stream ? ms[q].stream : s; };
+    std::vector<cudaEvent_t> evs(own.size() + 1);
+    for (auto& ev : evs)
+        if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) return cudaErrorUnknown;
+    struct EvFree {
+        std::vector<cudaEvent_t>& v;
+        ~EvFree() {
+            for (auto ev : v) cudaEventDestroy(ev);
+        }
+    } evf{evs};
+    auto join = [&]() -> cudaError_t {  // s waits for every system stream
+        for (size_t j = 0; j < own.size(); j++) {
+            cudaError_t ee = cudaEventRecord(evs[j], own[j]);
+            if (ee == cudaSuccess) ee = cudaStreamWaitEvent(s, evs[j], 0);
+            if (ee != cudaSuccess) return ee;
+        }
+        return cudaSuccess;
+    };
+    auto fork = [&]() -> cudaError_t {  // every system stream waits for s
+        cudaError_t ee = cudaEventRecord(evs.back(), s);
+        for (size_t j = 0; j < own.size() && ee == cudaSuccess; j++) ee = cudaStreamWaitEvent(own[j], evs.back(), 0);
+        return ee;
+    };
+    auto sync_all = [&]() -> cudaError_t {
+        cudaError_t ee = cudaStreamSynchronize(s);
+        for (size_t j = 0; j < own.size() && ee == cudaSuccess; j++) ee = cudaStreamSynchronize(own[j]);
+        return ee;
+    };
+    for (int q = 0; q < m; q++) {
+        const RefineMesh& R = ms[q];
+        if (R.k < 1 || R.k > 4096) return cudaErrorInvalidValue;
+        char* p = (char*)R.work;
+        auto take = [&](size_t bytes) {
+            char* r = p;
+            p += (bytes + 255) & ~size_t(255);
+            return r;
+        };
+        const size_t kn = (size_t)R.k * R.n;  // the carving of solve_lu_refined
+        B[q].r64 = (double*)take(sizeof(double) * kn);
+        B[q].d32 = (float*)take(sizeof(float) * kn);
+        B[q].y32 = (float*)take(sizeof(float) * kn);
+        B[q].P64 = (double*)take(sizeof(double) * (size_t)residual_chunks(R.n) * 17 * R.n);
+        B[q].part = (double*)take(sizeof(double) * 2 * R.k * 64);
+        B[q].dd = (double*)take(sizeof(double) * 2 * R.k);
+        desc[q] = SubstMesh{R.LU, R.dinv, B[q].d32, B[q].y32, R.n, R.k, 0};
+        maxnb = std::max(maxnb, (R.n + NB - 1) / NB);
+        kmax = std::max(kmax, R.k);
+    }
+    // the substitution plan (the same for every pass)
+    struct Step {
+        int kind, dir;
+        int64_t off, cnt;
+    };
+    std::vector<Step> plan;
+    std::vector<int> items;
+    auto add = [&](int q, int64_t r0, int64_t r1, int64_t K, int b) {
+        const int v[LB_ITEM] = {q, (int)r0, (int)r1, 0, 0, (int)K, b, 0};
+        items.insert(items.end(), v, v + LB_ITEM);
+    };
+    auto step = [&](int kind, int dir, int64_t t) {
+        const int64_t off = (int64_t)items.size() / LB_ITEM;
+        for (int q = 0; q < m; q++) {
+            const int64_t n = ms[q].n, K = t * NB;
+            if (K >= n) continue;
+            const int b = (int)std::min<int64_t>(NB, n - K);
+            if (kind == 0) {
+                add(q, 0, 0, K, b);
+            } else if (dir == 0) {
+                for (int64_t r0 = K + b; r0 < n; r0 += NB) add(q, r0, n, K, b);
+            } else {
+                for (int64_t r0 = 0; r0 < K; r0 += NB) add(q, r0, K, K, b);
+            }
+        }
+        const int64_t cnt = (int64_t)items.size() / LB_ITEM - off;
+        if (cnt > 0) plan.push_back(Step{kind, dir, off, cnt});
+    };
+    for (int64_t t = 0; t < maxnb; t++) {
+        step(0, 0, t);
+        step(1, 0, t);
+    }
+    for (int64_t t = maxnb - 1; t >= 0; t--) {
+        step(0, 1, t);
+        step(1, 1, t);
+    }
+    cudaError_t e;
+    SubstMesh* ddesc = nullptr;
+    int *ditems = nullptr, *dact = nullptr;
+    if ((e = cudaMallocAsync((void**)&ddesc, sizeof(SubstMesh) * m, s)) != cudaSuccess) return e;
+    if ((e = cudaMallocAsync((void**)&ditems, sizeof(int) * std::max<size_t>(1, items.size()), s)) != cudaSuccess) {
+        cudaFreeAsync(ddesc, s);
+        return e;
+    }
+    if ((e = cudaMallocAsync((void**)&dact, sizeof(int) * m, s)) != cudaSuccess) {
+        cudaFreeAsync(ditems, s);
+        cudaFreeAsync(ddesc, s);
+        return e;
+    }
+    struct Free {
+        void *a, *b, *c;
+        cudaStream_t s;
+        ~Free() {
+            cudaFreeAsync(a, s);
+            cudaFreeAsync(b, s);
+            cudaFreeAsync(c, s);
+        }
+    } fr{ddesc, ditems, dact, s};
+    if ((e = cudaMemcpyAsync(ddesc, desc.data(), sizeof(SubstMesh) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return e;
+    if (!items.empty() &&
+        (e = cudaMemcpyAsync(ditems, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess)
+        return e;
+    // start: x = 0, r = b, and the right-hand sides' norms
+    std::vector<std::vector<double>> hd(m);
+    if ((e = fork()) != cudaSuccess) return e;  // the plan's uploads before any system's work
+    for (int q = 0; q < m; q++) {
+        const RefineMesh& R = ms[q];
+        const size_t kn = (size_t)R.k * R.n;
+        hd[q].assign(2 * R.k, 0.0);
+        cudaMemsetAsync(R.x, 0, sizeof(double) * kn, sq(q));
+        cudaMemcpyAsync(B[q].r64, R.rhs, sizeof(double) * kn, cudaMemcpyDeviceToDevice, sq(q));
+        if ((e = column_norms2_device(R.rhs, R.n, R.k, B[q].part, B[q].dd, sq(q))) != cudaSuccess) return e;
+    }
+    // hd is pageable host memory: each copy returns when it is done, so the systems' copies
+    // are issued after all their kernels, stream by stream
+    auto read_norms = [&](const std::vector<int>& act) -> cudaError_t {
+        for (int q = 0; q < m; q++)
+            if (act[q]) {
+                cudaError_t ee = cudaMemcpyAsync(hd[q].data(), B[q].dd, sizeof(double) * ms[q].k,
+                                                 cudaMemcpyDeviceToHost, sq(q));
+                if (ee != cudaSuccess) return ee;
+            }
+        return sync_all();
+    };
+    std::vector<int> act(m, 1);
+    if ((e = read_norms(act)) != cudaSuccess) return e;
+    std::vector<std::vector<double>> bn(m);
+    for (int q = 0; q < m; q++) {
+        bn[q].resize(ms[q].k);
+        for (int c = 0; c < ms[q].k; c++) bn[q][c] = std::sqrt(hd[q][c]);
+        st[q].refinements = 0;
+        st[q].residual_max = 1;
+    }
+    for (int pass = 0; pass < max_steps; pass++) {
+        int nact = 0;
+        for (int q = 0; q < m; q++) nact += act[q];
+        if (nact == 0) break;
+        // every stream is idle here (after read_norms), so this small pageable copy costs
+        // no overlap
+        if ((e = cudaMemcpyAsync(dact, act.data(), sizeof(int) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+            return e;
+        if ((e = fork()) != cudaSuccess) return e;
+        for (int q = 0; q < m; q++)
+            if (act[q]) {
+                const size_t kn = (size_t)ms[q].k * ms[q].n;
+                k_d2f<<<nb256(kn), 256, 0, sq(q)>>>(B[q].r64, B[q].d32, kn);
+            }
+        if ((e = join()) != cudaSuccess) return e;
+        {
+            ProfScope ps(Prof::LU_SOLVE, s);
+            for (const Step& stp : plan) {
+                const int* it = ditems + stp.off * LB_ITEM;
+                if (kmax <= 8)
+                    subst_launch<8>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+                else if (kmax <= 16)
+                    subst_launch<16>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+                else
+                    subst_launch<32>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+            }
+        }
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        if ((e = fork()) != cudaSuccess) return e;
+        for (int q = 0; q < m; q++)
+            if (act[q]) {
+                const RefineMesh& R = ms[q];
+                const size_t kn = (size_t)R.k * R.n;
+                k_addf<<<nb256(kn), 256, 0, sq(q)>>>(R.x, B[q].d32, kn);
+                if ((e = residual_df(R.A32, R.Alo, R.n, R.k, R.x, R.rhs, B[q].r64, B[q].P64, sq(q))) != cudaSuccess)
+                    return e;
+                if ((e = column_norms2_device(B[q].r64, R.n, R.k, B[q].part, B[q].dd, sq(q))) != cudaSuccess)
+                    return e;
+            }
+        if ((e = read_norms(act)) != cudaSuccess) return e;
+        for (int q = 0; q < m; q++)
+            if (act[q]) {
+                double worst = 0;
+                for (int c = 0; c < ms[q].k; c++)
+                    worst = std::max(worst, bn[q][c] > 0 ? std::sqrt(hd[q][c]) / bn[q][c] : 0.0);
+                st[q].refinements++;
+                st[q].residual_max = worst;
+                if (worst <= tol) act[q] = 0;
+            }
+    }
+    return cudaGetLastError();
 }
 
 // X (n x k, ld n) <- U^{-1} L^{-1} X

@@ -581,4 +581,11 @@ cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, doubl
     return dots<double>(v, v, nullptr, nullptr, n, k, part, dd, host, s);
 }
 
+cudaError_t column_norms2_device(const double* v, int64_t n, int k, double* part, double* dd, cudaStream_t s) {
+    const int nb = 64;
+    k_dot2<double><<<dim3(nb, k), 256, 0, s>>>(v, v, nullptr, nullptr, n, k, part);
+    k_dot_finish<<<nblk(2 * k, 64), 64, 0, s>>>(part, nb, 2 * k, dd);
+    return cudaGetLastError();
+}
+
 }  // namespace cpg

@@ -11,6 +11,8 @@
  *   cpg_batch_solve            cpCase::run minus file output, CPanel/cpCase.cpp:31-139,
  *                              once per flow condition as CPanelMgr::run drives it
  *                              (CPanel/CPanelMgr.cpp:90-167), for m meshes at once
+ *   cpg_lu_factor_grouped      the LU of the mixed path's cpCase::solveMatrixEq replacement
+ *                              (CPanel/cpCase.cpp:185-214) for m geometries in lockstep
  *   cpg_group_schedule         no counterpart (host-only view of the grouped launch's
  *                              work queue, for checking and tuning)
  *
@@ -74,6 +76,17 @@ int  cpg_group_default_shape(cpg_group_shape* shape);
 int  cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cpg_group_shape* shape,
                                cpg_group_report* report);
 
+/* FP32 LU factorizations (the CPG_MIXED solve's) of m geometries at once, each holding its
+ * CPG_MIXED matrix.  The blocked LU of cpg_solve_cases taken in lockstep: every 128-column
+ * block step is one launch of the diagonal-block kernel for all geometries, then one launch
+ * each of the batched panel solves and updates; the rank-1024 trailing updates stay per
+ * geometry.  Runs on gs[0]'s context stream like cpg_set_inf_coeff_grouped, and the
+ * following cpg_solve_cases calls reuse the factors.  ms: device time (may be null).
+ * The factors agree with the per-geometry factorization to FP32 rounding (different
+ * summation orders), so the refined solutions agree within the refinement tolerance, not
+ * bit for bit. */
+int  cpg_lu_factor_grouped(cpg_geometry* const* gs, int m, double* ms);
+
 /* Host only (no device needed): the grouped launch's work queue for meshes of n_body
  * panels.  items: cap x 4 ints (mesh, row block of 128 rows, first source chunk, chunk
  * count), costliest first; *count = number of items (items may be null to count only).
@@ -106,12 +119,17 @@ typedef struct {
     int tune;             /* cpg_tune_mode of the grouped assembly                         */
     double budget_bytes;  /* device memory the meshes of one wave may hold together;
                              0 = three quarters of the free memory                         */
+    int lockstep;         /* 0: each mesh's LU, refined solves and post on its worker;
+                             1: the wave's LU factorizations in lockstep
+                             (cpg_lu_factor_grouped), then its refined solves in lockstep
+                             (one launch per substitution block step for every mesh)       */
 } cpg_batch_params;
 
 typedef struct {
     double ms_total;          /* host clock, whole call                                  */
     double ms_topology;       /* host clock: readTri topology and uploads (in parallel)  */
     double ms_assembly;       /* device time of the grouped launches                     */
+    double ms_factor;         /* device time of the lockstep factorizations             */
     double ms_solve;          /* host clock: factorizations, refined solves and post     */
     int waves;                /* grouped launches (meshes split by the memory budget)    */
     int64_t solves;           /* (mesh, flow condition) pairs solved                     */
@@ -119,11 +137,14 @@ typedef struct {
     cpg_group_report group;   /* the last wave's grouped launch                          */
 } cpg_batch_stats;
 
-/* Steady mixed-precision solves of m meshes: topology and uploads in parallel on the
- * workers, one grouped assembly per wave, then each mesh's FP32 LU, refined solves to
- * relative residual 1e-12 and post-processing on its worker's stream, the workers side by
- * side.  Per mesh the results equal cpg_solve_cases(g, ..., CPG_MIXED, ...) on the same
- * mesh bit for bit.  Returns CPG_OK when every mesh succeeded, else the first failing
+/* Steady mixed-precision solves of m meshes: topology, uploads and post-processing tables
+ * in parallel on the workers, one grouped assembly per wave, then either (lockstep = 0)
+ * each mesh's FP32 LU, refined solves to relative residual 1e-12 and post-processing on
+ * its worker's stream, the workers side by side, or (lockstep = 1) the wave's
+ * factorizations and refined solves in lockstep and each mesh's post-processing on one
+ * stream.  With lockstep = 0 the results equal cpg_solve_cases(g, ..., CPG_MIXED, ...) on
+ * the same mesh bit for bit; with lockstep = 1 they agree within the refinement tolerance
+ * (relative residual 1e-12).  Returns CPG_OK when every mesh succeeded, else the first failing
  * mesh's status (each mesh's own status is in meshes[i].status). */
 int  cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* meshes, int m, const cpg_batch_params* params,
                      cpg_batch_stats* stats);

@@ -446,6 +446,26 @@ def vp_loop_only(precision, steps):
     print(json.dumps({"vp_loop": precision, "ms_per_step": [round(t, 2) for t in ms], "info": S.info()}))
 
 
+def batch_loop_only(n_wings=64, lockstep=True):
+    """The uneven batch alone (profiling aid): n_wings seeded wings x 8 alphas through
+    cpg_batch_solve, a warm-up call (kernels, work-shape tuning) and one timed call."""
+    from cpanel_gb300 import batch, wing
+    meshes = []
+    for i in range(n_wings):
+        spec = wing.config_random(20261203 + i)
+        nodes, tris, ids, info = wing.make_wing(spec)
+        rng = np.random.default_rng(20261203 + i)
+        meshes.append(dict(nodes=nodes, tris=tris, ids=ids, flows=[(1.0, float(a), 0.0, MACH) for a in
+                                                                   rng.uniform(-2, 10, 8)],
+                           Sref=info["area"], bref=spec.span, cref=1.0, cg=(0.25, 0, 0)))
+    batch.batch_solve(meshes, workers=8, lockstep=lockstep)
+    t0 = time.perf_counter()
+    _, st = batch.batch_solve(meshes, workers=8, lockstep=lockstep)
+    wall = time.perf_counter() - t0
+    print(json.dumps({"batch_loop": n_wings, "lockstep": lockstep, "solves_per_s": st["solves"] / wall,
+                      "stats": st}))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -479,6 +499,8 @@ def main():
     ap.add_argument("--workload", default="multi_rhs", choices=["multi_rhs", "mid"])
     ap.add_argument("--no-serving", action="store_true", help="skip the uneven-batch and served-stream runs")
     ap.add_argument("--no-vp", action="store_true", help="skip the vortex-particle sample")
+    ap.add_argument("--batch-loop", type=int, default=0, metavar="N",
+                    help="only the uneven batch of N seeded wings (lockstep), warm-up and one timed call")
     ap.add_argument("--vp-loop", choices=["plain", "mixed"],
                     help="only the vortex-particle loop in this precision: 3 steps, then --steps timed "
                          "steps (one JSON line; for profiling)")
@@ -487,6 +509,8 @@ def main():
         return run_reference(args)
     if args.vp_loop:
         return vp_loop_only(args.vp_loop, args.steps)
+    if args.batch_loop:
+        return batch_loop_only(args.batch_loop)
 
     import torch
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -316,53 +316,60 @@ __global__ void __launch_bounds__(256) k_row_solve_batched(const cpg::LuBatchMes
 }
 
 // C -= L(:, K..K+b) U(K..K+b, :) on the tile rows [r0, min(r0 + 128, r1)) x columns
-// [c0, min(c0 + 64, c1)).  256 threads: thread t owns row t % 128 and 32 columns.
+// [c0, min(c0 + 64, c1)).  128 threads, each an 8 x 8 block of C in registers (rows
+// 8 (t % 16) .., columns 8 (t / 16) ..); L and U staged GS_K columns / rows at a time and
+// read as float4 (two loads each per k for 64 FMAs).
 constexpr int GS_R = 128, GS_C = 64, GS_K = 32;
-__global__ void __launch_bounds__(256) k_gemm_sub_batched(const cpg::LuBatchMesh* __restrict__ ms,
+__global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh* __restrict__ ms,
                                                           const int* __restrict__ items) {
-    __shared__ float Ls[GS_K][GS_R];
-    __shared__ __align__(16) float Us[GS_K][GS_C + 4];
+    __shared__ __align__(16) float Ls[GS_K][GS_R];
+    __shared__ __align__(16) float Us[GS_K][GS_C];
     const int* it = items + LB_ITEM * blockIdx.x;
     const cpg::LuBatchMesh d = ms[it[0]];
     const int64_t n = d.n, r0 = it[1], r1 = it[2], c0 = it[3], c1 = it[4], K = it[5];
     const int b = it[6];
     float* A = d.LU;
-    const int t = threadIdx.x, r = t % GS_R, cg = t / GS_R;
-    float acc[32];
+    const int t = threadIdx.x, tr = t % 16, tc = t / 16;
+    float acc[8][8];
 #pragma unroll
-    for (int j = 0; j < 32; j++) acc[j] = 0.f;
+    for (int i = 0; i < 8; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
     for (int k0 = 0; k0 < b; k0 += GS_K) {
         __syncthreads();
-        for (int idx = t; idx < GS_K * GS_R; idx += 256) {
+        for (int idx = t; idx < GS_K * GS_R; idx += 128) {
             const int kk = idx / GS_R, rr = idx % GS_R;
             Ls[kk][rr] = (k0 + kk < b && r0 + rr < r1) ? A[(K + k0 + kk) * n + r0 + rr] : 0.f;
         }
-        for (int idx = t; idx < GS_K * GS_C; idx += 256) {
+        for (int idx = t; idx < GS_K * GS_C; idx += 128) {
             const int kk = idx % GS_K, c = idx / GS_K;
             Us[kk][c] = (k0 + kk < b && c0 + c < c1) ? A[(c0 + c) * n + K + k0 + kk] : 0.f;
         }
         __syncthreads();
 #pragma unroll 4
         for (int kk = 0; kk < GS_K; kk++) {
-            const float a = Ls[kk][r];
-            const float4* u4 = reinterpret_cast<const float4*>(&Us[kk][32 * cg]);
+            const float4 a0 = *reinterpret_cast<const float4*>(&Ls[kk][8 * tr]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&Ls[kk][8 * tr + 4]);
+            const float4 u0 = *reinterpret_cast<const float4*>(&Us[kk][8 * tc]);
+            const float4 u1 = *reinterpret_cast<const float4*>(&Us[kk][8 * tc + 4]);
+            const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+            const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
 #pragma unroll
-            for (int j4 = 0; j4 < 8; j4++) {
-                const float4 u = u4[j4];
-                acc[4 * j4] = __fmaf_rn(a, u.x, acc[4 * j4]);
-                acc[4 * j4 + 1] = __fmaf_rn(a, u.y, acc[4 * j4 + 1]);
-                acc[4 * j4 + 2] = __fmaf_rn(a, u.z, acc[4 * j4 + 2]);
-                acc[4 * j4 + 3] = __fmaf_rn(a, u.w, acc[4 * j4 + 3]);
-            }
+            for (int i = 0; i < 8; i++)
+#pragma unroll
+                for (int j = 0; j < 8; j++) acc[i][j] = __fmaf_rn(a[i], u[j], acc[i][j]);
         }
     }
-    if (r0 + r < r1) {
 #pragma unroll
-        for (int j = 0; j < 32; j++) {
-            const int64_t c = c0 + 32 * cg + j;
-            if (c < c1) {
-                float* p = A + c * n + r0 + r;
-                *p = *p - acc[j];
+    for (int j = 0; j < 8; j++) {
+        const int64_t c = c0 + 8 * tc + j;
+        if (c >= c1) continue;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+            const int64_t r = r0 + 8 * tr + i;
+            if (r < r1) {
+                float* p = A + c * n + r;
+                *p = *p - acc[i][j];
             }
         }
     }
@@ -606,12 +613,16 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
 // runs.  (Measured: about 1 ms of 56 on the 19k wing.  cuBLAS's large GEMM holds every
 // SM until it ends, and keeping 8-32 SMs out of it for the panel measured 0.6-5 ms
 // slower.)
-// outer panel width: OB_BLOCKS inner blocks (CPG_LU_OUTER overrides, 1..16)
+// outer panel width: OB_BLOCKS inner blocks (CPG_LU_OUTER overrides, 1..16).  The lockstep
+// factorization of many matrices uses OB_BLOCKS_BATCHED: its rank-128 panel updates run in
+// FP32 on the CUDA cores and its rank-OB updates on the tensor cores, and on the 64-wing
+// batch 512 columns measured 220 ms against 269 ms for 1,024 (256: 224 ms; 2,048: 379 ms).
 constexpr int OB_BLOCKS = 8;
-int64_t outer_width() {
+constexpr int OB_BLOCKS_BATCHED = 4;
+int64_t outer_width(int def_blocks = OB_BLOCKS) {
     const char* e = std::getenv("CPG_LU_OUTER");
-    int k = e ? std::atoi(e) : OB_BLOCKS;
-    return (int64_t)NB * (k >= 1 && k <= 16 ? k : OB_BLOCKS);
+    int k = e ? std::atoi(e) : def_blocks;
+    return (int64_t)NB * (k >= 1 && k <= 16 ? k : def_blocks);
 }
 
 struct Streams {  // where the next cuBLAS calls go
@@ -841,7 +852,7 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
         const int64_t now = (int64_t)items.size() / LB_ITEM;
         if (now > mark) plan.push_back(Step{kind, mark, now - mark, -1, 0, 0});
     };
-    const int64_t OB = outer_width();
+    const int64_t OB = outer_width(OB_BLOCKS_BATCHED);
     for (int64_t KO = 0; KO < nmax; KO += OB) {
         for (int64_t K = KO; K < KO + OB && K < nmax; K += NB) {
             open();
@@ -916,7 +927,7 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
                 case DIAG: k_lu_diag_batched<<<g, DT, DIAG_SMEM, s>>>(ddesc, it); break;
                 case COLS: k_col_solve_batched<<<g, 256, 0, s>>>(ddesc, it); break;
                 case ROWS: k_row_solve_batched<<<g, 256, 0, s>>>(ddesc, it); break;
-                case GEMM: k_gemm_sub_batched<<<g, 256, 0, s>>>(ddesc, it); break;
+                case GEMM: k_gemm_sub_batched<<<g, 128, 0, s>>>(ddesc, it); break;
                 default: {
                     const int64_t n = ns[st.q];
                     e = trailing(h, LUs[st.q], n, st.KO, (int)(st.KE - st.KO), st.KE, n - st.KE, st.KE, n - st.KE);

@@ -498,7 +498,7 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
     } else if (precision == CPG_MIXED) {
         CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
         CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
-        CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n))), "alloc rhs basis");
+        CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n, g->H.n_wake))), "alloc rhs basis");
         if (g->order_n != n) {  // block schedule, once per geometry
             std::vector<int> ord;
             cpg::mixed_block_order(n, ord);
@@ -1047,14 +1047,14 @@ int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cp
     std::vector<int64_t> ns(m);
     int64_t rows = 0;
     double pairs = 0;
-    bool any_wake = false;
+    int64_t max_nw = 0;
     for (int q = 0; q < m; q++) {
         cpg_geometry* g = gs[q];
         const int64_t n = g->H.n_body;
         const size_t nn = (size_t)n * n;
         CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
         CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
-        CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n))), "alloc rhs basis");
+        CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n, g->H.n_wake))), "alloc rhs basis");
         desc[q] = cpg::MixedMeshDesc{g->rec.as<double>(), g->frec.as<float>(), g->erec.as<double>(), n,
                                      cpg::mixed_chunk(n), g->A32.as<float>(), g->Alo.as<float>(),
                                      g->rb.as<double>() + 3 * n, g->rb.as<double>(),
@@ -1063,7 +1063,7 @@ int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cp
         ns[q] = n;
         rows += n;
         pairs += (double)n * (double)n;
-        any_wake = any_wake || g->H.n_wake > 0;
+        max_nw = std::max<int64_t>(max_nw, g->H.n_wake);
     }
     int nsm = 0;
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
@@ -1172,7 +1172,8 @@ int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cp
     for (int q = 0; q < m; q++) CK(cudaMemsetAsync(gs[q]->count.p, 0, sizeof(unsigned long long), s), "clear counter");
     CK(cudaEventRecord(e0, s), "event");
     CK(launch_core(use), "grouped assembly (mixed)");
-    CK(cpg::launch_assemble_mixed_grouped_finish(ddesc, m, rows, any_wake, s), "grouped sums and wake columns");
+    if (max_nw > 65535) return fail(ctx, CPG_E_INVALID, "more than 65,535 wake panels");
+    CK(cpg::launch_assemble_mixed_grouped_finish(ddesc, m, rows, max_nw, s), "grouped sums and wake columns");
     CK(cudaEventRecord(e1, s), "event");
     // every geometry's stream continues after the grouped launch
     for (cpg_ctx* c : others) CK(cudaStreamWaitEvent(c->stream, e1, 0), "join");

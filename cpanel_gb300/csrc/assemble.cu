@@ -346,14 +346,14 @@ __global__ void k_wake_columns(const double* __restrict__ rec, const double* __r
     }
 }
 
-// Wake columns for the split (hi + lo) FP32 storage of the mixed path: row i.
-__device__ __forceinline__ void wake_row_split(const double* __restrict__ rec, const double* __restrict__ wrec,
-                                               const int32_t* __restrict__ widx, const double* __restrict__ wcoef,
-                                               int64_t n, int64_t nw, float* __restrict__ Ahi,
-                                               float* __restrict__ Alo, int64_t i) {
-    dv3 poi = ld3(rec + i * R_STRIDE + R_C);
+// Wake columns for the split (hi + lo) FP32 storage of the mixed path: the scatter of
+// k_wake_columns for row i, one rounding to hi + lo per update, with the influences read
+// from G[j * n + i] (k_wake_infl, all pairs in parallel) and added in wPanels order.
+__device__ __forceinline__ void wake_row_split_table(const double* __restrict__ G, const int32_t* __restrict__ widx,
+                                                     const double* __restrict__ wcoef, int64_t n, int64_t nw,
+                                                     float* __restrict__ Ahi, float* __restrict__ Alo, int64_t i) {
     for (int64_t j = 0; j < nw; j++) {
-        double infl = dub_phi_inf(wrec + j * R_STRIDE, poi);
+        double infl = G[j * n + i];
         double c = wcoef[j];
         const int32_t* ix = widx + 4 * j;
         const double add[4] = {infl * (1 - c), infl * (c - 1), infl * c, -(infl * c)};
@@ -367,12 +367,20 @@ __device__ __forceinline__ void wake_row_split(const double* __restrict__ rec, c
     }
 }
 
-__global__ void k_wake_columns_split(const double* __restrict__ rec, const double* __restrict__ wrec,
-                                     const int32_t* __restrict__ widx, const double* __restrict__ wcoef, int64_t n,
-                                     int64_t nw, float* __restrict__ Ahi, float* __restrict__ Alo) {
+// G[j * n + i] = dubPhiInf of wake panel j at body centroid i, all pairs in parallel
+__global__ void k_wake_infl(const double* __restrict__ rec, const double* __restrict__ wrec, int64_t n,
+                            double* __restrict__ G) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n) return;
+    G[j * n + i] = dub_phi_inf(wrec + j * R_STRIDE, ld3(rec + i * R_STRIDE + R_C));
+}
+
+__global__ void k_wake_columns_split(const double* __restrict__ G, const int32_t* __restrict__ widx,
+                                     const double* __restrict__ wcoef, int64_t n, int64_t nw,
+                                     float* __restrict__ Ahi, float* __restrict__ Alo) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    wake_row_split(rec, wrec, widx, wcoef, n, nw, Ahi, Alo, i);
+    wake_row_split_table(G, widx, wcoef, n, nw, Ahi, Alo, i);
 }
 
 __global__ void k_rb_reduce(const double* __restrict__ rbp, int64_t n, int64_t chunks, double* __restrict__ rb) {
@@ -430,11 +438,21 @@ __global__ void k_rb_reduce_grouped(const cpg::MixedMeshDesc* __restrict__ meshe
     }
 }
 
+// k_wake_infl for every mesh of a group into its partial-sum buffer (free after the reduction)
+__global__ void k_wake_infl_grouped(const cpg::MixedMeshDesc* __restrict__ meshes, int m, int64_t rows) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (r >= rows) return;
+    const cpg::MixedMeshDesc& d = meshes[mesh_of_row(meshes, m, r)];
+    if (j >= d.nw) return;
+    const int64_t i = r - d.row0;
+    d.rbp[j * d.n + i] = dub_phi_inf(d.wrec + j * R_STRIDE, ld3(d.rec + i * R_STRIDE + R_C));
+}
+
 __global__ void k_wake_columns_grouped(const cpg::MixedMeshDesc* __restrict__ meshes, int m, int64_t rows) {
     int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= rows) return;
     const cpg::MixedMeshDesc& d = meshes[mesh_of_row(meshes, m, r)];
-    if (d.nw > 0) wake_row_split(d.rec, d.wrec, d.widx, d.wcoef, d.n, d.nw, d.A32, d.Alo, r - d.row0);
+    if (d.nw > 0) wake_row_split_table(d.rbp, d.widx, d.wcoef, d.n, d.nw, d.A32, d.Alo, r - d.row0);
 }
 
 // panel::setGeom + getLocalSys on the device for free triangles (batched API).
@@ -636,16 +654,18 @@ cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const do
                                                               near_count);
         k_rb_reduce<<<(unsigned)((3 * n + 255) / 256), 256, 0, s>>>(rb_part, n, nby, rb);
     }
-    if (nw > 0) {
+    if (nw > 65535) return cudaErrorInvalidValue;  // one grid row per wake panel below
+    if (nw > 0) {  // the chunk partial sums are reduced: their buffer holds the wake table
         ProfScope ps(Prof::WAKE_COLUMNS, s);
-        k_wake_columns_split<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rec, wrec, widx, wcoef, n, nw, A32, Alo);
+        k_wake_infl<<<dim3((unsigned)((n + 127) / 128), (unsigned)nw), 128, 0, s>>>(rec, wrec, n, rb_part);
+        k_wake_columns_split<<<(unsigned)((n + 127) / 128), 128, 0, s>>>(rb_part, widx, wcoef, n, nw, A32, Alo);
     }
     return cudaGetLastError();
 }
 
-int64_t mixed_rb_part_doubles(int64_t n) {
+int64_t mixed_rb_part_doubles(int64_t n, int64_t nw) {
     int64_t ch = chunk_for(n);
-    return ((n + ch - 1) / ch) * 3 * n;
+    return std::max(((n + ch - 1) / ch) * 3 * n, nw * n);
 }
 
 int64_t mixed_chunk(int64_t n) { return chunk_for(n); }
@@ -710,7 +730,7 @@ cudaError_t launch_assemble_mixed_grouped_core(const MixedMeshDesc* meshes, cons
     return cudaGetLastError();
 }
 
-cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, int m, int64_t rows, bool any_wake,
+cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, int m, int64_t rows, int64_t max_nw,
                                                  cudaStream_t s) {
     if (rows <= 0) return cudaSuccess;
     const unsigned g = (unsigned)((rows + 127) / 128);
@@ -718,8 +738,9 @@ cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, in
         ProfScope ps(Prof::ASSEMBLE, s);
         k_rb_reduce_grouped<<<g, 128, 0, s>>>(meshes, m, rows);
     }
-    if (any_wake) {
+    if (max_nw > 0) {
         ProfScope ps(Prof::WAKE_COLUMNS, s);
+        k_wake_infl_grouped<<<dim3(g, (unsigned)max_nw), 128, 0, s>>>(meshes, m, rows);
         k_wake_columns_grouped<<<g, 128, 0, s>>>(meshes, m, rows);
     }
     return cudaGetLastError();

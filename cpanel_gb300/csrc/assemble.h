@@ -66,7 +66,7 @@ struct MixedMeshDesc {
     int64_t n, jchunk;
     float* A32;
     float* Alo;
-    double* rbp;  // mixed_rb_part_doubles(n)
+    double* rbp;  // mixed_rb_part_doubles(n, nw): chunk partial sums, then the wake table
     double* rb;   // 3n
     unsigned long long* near_count;  // may be null
     const double* wrec;
@@ -85,11 +85,12 @@ int64_t group_schedule(const int64_t* n, int m, int chunks_per_item, int near_ba
 // columns of every mesh (rows = the group's flattened row count).
 cudaError_t launch_assemble_mixed_grouped_core(const MixedMeshDesc* meshes, const int* items, int nitems,
                                                int blocks, int* next, cudaStream_t s);
-cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, int m, int64_t rows, bool any_wake,
+cudaError_t launch_assemble_mixed_grouped_finish(const MixedMeshDesc* meshes, int m, int64_t rows, int64_t max_nw,
                                                  cudaStream_t s);
 int assemble_mixed_grouped_max_blocks_per_sm();
-// doubles of the per-chunk partial sums that launch_assemble_mixed needs in rb_part
-int64_t mixed_rb_part_doubles(int64_t n);
+// doubles of rb_part that launch_assemble_mixed needs: the per-chunk partial sums, and
+// afterwards the wake influence table (nw x n)
+int64_t mixed_rb_part_doubles(int64_t n, int64_t nw);
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,
                              cudaStream_t s);
 cudaError_t launch_v_batch(const double* verts, const double* poi, int64_t m, double* vs, double* vd, cudaStream_t s);

@@ -101,9 +101,14 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
     int64_t i = (int64_t)blockIdx.x * MV_THREADS + threadIdx.x;
     int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
     double acc[KB];
+    float hi[KB], lo[KB];  // double-float partial sums over two tiles (64 columns)
 #pragma unroll
-    for (int c = 0; c < KB; c++) acc[c] = 0;
-    for (int64_t j0 = jb; j0 < je; j0 += MV_JT) {
+    for (int c = 0; c < KB; c++) {
+        acc[c] = 0;
+        hi[c] = lo[c] = 0.f;
+    }
+    int tile = 0;
+    for (int64_t j0 = jb; j0 < je; j0 += MV_JT, tile++) {
         __syncthreads();
         for (int t = threadIdx.x; t < MV_JT * KB; t += MV_THREADS) {
             int jj = t / KB, c = t % KB;
@@ -117,9 +122,6 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
             int cnt = (int)min((int64_t)MV_JT, je - j0);
             const float* Ap = A + j0 * n + i;
             const float* Lp = Alo + j0 * n + i;
-            float hi[KB], lo[KB];
-#pragma unroll
-            for (int c = 0; c < KB; c++) hi[c] = lo[c] = 0.f;
             int t = 0;
             for (; t + 3 < cnt; t += 4) {
                 float a[4], al[4];
@@ -138,8 +140,15 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
 #pragma unroll
                 for (int c = 0; c < KB; c++) df_acc(a, al, sx[t][c], hi[c], lo[c]);
             }
+            // into FP64 every second tile and after the last one (FP64 runs at 1/64 of the
+            // FP32 rate here, so flushing every tile cost as much as the products)
+            if ((tile & 1) || j0 + MV_JT >= je) {
 #pragma unroll
-            for (int c = 0; c < KB; c++) acc[c] += (double)hi[c] + (double)lo[c];
+                for (int c = 0; c < KB; c++) {
+                    acc[c] += (double)hi[c] + (double)lo[c];
+                    hi[c] = lo[c] = 0.f;
+                }
+            }
         }
     }
     if (i < n) {

@@ -183,3 +183,20 @@ def test_lockstep_factorization_then_solve_cases(per_mesh):
                              precision="mixed", want=("cp",))
         assert out["stats"]["residual_max"] <= 1e-12
         assert np.abs(out["cp"] - r["cp"]).max() < 1e-7
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("lockstep", [False, True])
+def test_batch_solve_isolates_a_bad_mesh(per_mesh, lockstep):
+    """A mesh the path rejects fails alone; the others are solved as before."""
+    from cpanel_gb300 import batch
+    ws = _wings()
+    bad = dict(ws[1])
+    bad["tris"] = bad["tris"][:1]  # one body triangle: fewer than two body panels
+    bad["ids"] = bad["ids"][:1]
+    res, st = batch.batch_solve([ws[0], bad, ws[2]], workers=2, lockstep=lockstep, want=("cp", "CL"))
+    assert st["failed"] == 1 and res[1]["status"] == 4  # CPG_E_BAD_MESH
+    for o, r in zip([res[0], res[2]], [per_mesh[0], per_mesh[2]]):
+        assert o["status"] == 0
+        assert np.abs(o["cp"] - r["cp"]).max() < 1e-7
+        assert np.allclose(o["CL"], r["CL"], rtol=1e-8, atol=0)

@@ -21,6 +21,7 @@
 namespace {
 
 constexpr int NB = 128;   // panel width
+constexpr int SB = 4 * NB; // blocks of the substitutions' combined inverses
 constexpr int P = NB + 1; // padded smem pitch (no bank conflicts on row access)
 
 constexpr int DT = 512;    // threads of the diagonal-block kernel
@@ -688,11 +689,25 @@ cudaError_t factor_body(const Streams& st, LuGraphs* G, float* LU, float* Dinv, 
 // Blocked forward and backward substitution with the diagonal-block inverses, two
 // GEMMs per block and direction and no copies: forward, Y_K = inv(L_KK) X_K and
 // X_below -= L_below,K Y_K; backward, X_K = inv(U_KK) Y_K and Y_above -= U_above,K X_K.
-// X (n x k, ld n) ends with the solution; Y is an n x k scratch array.
-cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int64_t n, float* X, float* Y, int k) {
+// X (n x k, ld n) ends with the solution; Y is an n x k scratch array.  The first nsup
+// 512-column blocks use their combined inverses (Dinv4), so a pass takes a quarter of the
+// dependent steps there; the rest of the matrix goes by 128-column blocks.
+cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, const float* Dinv4, int64_t nsup,
+                       int64_t n, float* X, float* Y, int k) {
     const float one = 1.f, mone = -1.f, zero = 0.f;
-    const int64_t nblk = (n + NB - 1) / NB;
-    for (int64_t blk = 0; blk < nblk; blk++) {
+    const int64_t nblk = (n + NB - 1) / NB, blk0 = nsup * (SB / NB);
+    for (int64_t sb = 0; sb < nsup; sb++) {
+        const int64_t K = sb * SB;
+        const float* Li = Dinv4 + sb * 2 * SB * SB;
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, SB, k, SB, &one, Li, SB, X + K, (int)n, &zero, Y + K, (int)n) !=
+            CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        const int64_t rest = n - K - SB;
+        if (rest > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, SB, &mone, LU + K * n + K + SB, (int)n,
+                                    Y + K, (int)n, &one, X + K + SB, (int)n) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+    }
+    for (int64_t blk = blk0; blk < nblk; blk++) {
         int64_t K = blk * NB;
         int b = (int)std::min<int64_t>(NB, n - K);
         const float* Li = Dinv + blk * 2 * NB * NB;
@@ -704,7 +719,7 @@ cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int
                                     Y + K, (int)n, &one, X + K + b, (int)n) != CUBLAS_STATUS_SUCCESS)
             return cudaErrorUnknown;
     }
-    for (int64_t blk = nblk - 1; blk >= 0; blk--) {
+    for (int64_t blk = nblk - 1; blk >= blk0; blk--) {
         int64_t K = blk * NB;
         int b = (int)std::min<int64_t>(NB, n - K);
         const float* Ui = Dinv + blk * 2 * NB * NB + NB * NB;
@@ -715,7 +730,96 @@ cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, int
                                  &one, Y, (int)n) != CUBLAS_STATUS_SUCCESS)
             return cudaErrorUnknown;
     }
+    for (int64_t sb = nsup - 1; sb >= 0; sb--) {
+        const int64_t K = sb * SB;
+        const float* Ui = Dinv4 + sb * 2 * SB * SB + SB * SB;
+        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, SB, k, SB, &one, Ui, SB, Y + K, (int)n, &zero, X + K, (int)n) !=
+            CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+        if (K > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, SB, &mone, LU + K * n, (int)n, X + K, (int)n,
+                                 &one, Y, (int)n) != CUBLAS_STATUS_SUCCESS)
+            return cudaErrorUnknown;
+    }
     return cudaGetLastError();
+}
+
+// Inverses of the full 512-column diagonal blocks from the four 128-column ones inside
+// each, by two block-triangular doublings (128 -> 256 -> 512):
+//   [[A, 0], [C, B]]^{-1} = [[A^{-1}, 0], [-B^{-1} C A^{-1}, B^{-1}]]   (L, unit lower)
+//   [[A, C], [0, B]]^{-1} = [[A^{-1}, -A^{-1} C B^{-1}], [0, B^{-1}]]   (U)
+// Every step is one strided-batched FP32 GEMM over all the 512-column blocks (their
+// diagonal blocks of LU, their inverses and their scratch all lie at fixed strides).
+// Layout: Dinv4 + s * 2 * SB^2 holds L^{-1} then U^{-1} of block s, column-major, ld SB.
+__global__ void k_super_init(const float* __restrict__ Dinv, float* __restrict__ Dinv4, int64_t nsup) {
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nsup * 2 * SB * SB) return;
+    const int64_t s = t / (2 * SB * SB);
+    const int64_t w = t % (2 * SB * SB);
+    const int u = (int)(w / (SB * SB));  // 0: L, 1: U
+    const int64_t e = w % (SB * SB);
+    const int r = (int)(e % SB), c = (int)(e / SB);
+    float v = 0.f;
+    if (r / NB == c / NB) {
+        const int64_t blk = s * (SB / NB) + r / NB;
+        v = Dinv[blk * 2 * NB * NB + u * NB * NB + (r % NB) + (int64_t)(c % NB) * NB];
+    }
+    Dinv4[t] = v;
+}
+
+cudaError_t build_super_inverses(cublasHandle_t h, LuGraphs* G, const float* LU, int64_t n, cudaStream_t s) {
+    const int64_t nsup = n / SB;
+    G->super_n = 0;
+    if (nsup == 0) return cudaSuccess;
+    cudaError_t e;
+    if (!G->dinv4 || G->super_cap != nsup) {  // same buffers for every factorization of this size,
+        if (G->solve) cudaGraphExecDestroy(G->solve);  // so a captured substitution stays valid
+        G->solve = nullptr;
+        if (G->dinv4) cudaFree(G->dinv4);
+        if (G->super_tmp) cudaFree(G->super_tmp);
+        G->dinv4 = G->super_tmp = nullptr;
+        G->super_cap = 0;
+        if ((e = cudaMalloc(&G->dinv4, sizeof(float) * nsup * 2 * SB * SB)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * nsup * 256 * 256)) != cudaSuccess) return e;
+        G->super_cap = nsup;
+    }
+    const int64_t tot = nsup * 2 * SB * SB;
+    k_super_init<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(G->dinv, G->dinv4, nsup);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const float one = 1.f, mone = -1.f, zero = 0.f;
+    const int ni = (int)n, bc = (int)nsup;
+    const long long sLU = (long long)SB * (n + 1), sD = 2LL * SB * SB, sT = 256LL * 256;
+    float* T = G->super_tmp;
+    auto gemm = [&](int m, int nn, int kk, float alpha, const float* A, int lda, long long sA, const float* B, int ldb,
+                    long long sB, float* C, int ldc) -> cudaError_t {
+        return cublasSgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_N, m, nn, kk, &alpha, A, lda, sA, B, ldb, sB, &zero,
+                                         C, ldc, C == T ? sT : sD, bc) == CUBLAS_STATUS_SUCCESS
+                   ? cudaSuccess
+                   : cudaErrorUnknown;
+    };
+    for (int half = 1; half <= 2; half++) {
+        const int w = NB * half;  // size of the two blocks combined at this level (128, then 256)
+        for (int p = 0; p < SB / (2 * w); p++) {
+            const int o = 2 * w * p;  // offset of the pair inside the 512-column block
+            float* Linv = G->dinv4;
+            float* Uinv = G->dinv4 + SB * SB;
+            // L: T = C A^{-1}, then -B^{-1} T into the lower-left block
+            if ((e = gemm(w, w, w, one, LU + (o + w) + (int64_t)o * n, ni, sLU, Linv + o + (int64_t)o * SB, SB, sD, T,
+                          w)) != cudaSuccess)
+                return e;
+            if ((e = gemm(w, w, w, mone, Linv + (o + w) + (int64_t)(o + w) * SB, SB, sD, T, w, sT,
+                          Linv + (o + w) + (int64_t)o * SB, SB)) != cudaSuccess)
+                return e;
+            // U: T = C B^{-1}, then -A^{-1} T into the upper-right block
+            if ((e = gemm(w, w, w, one, LU + o + (int64_t)(o + w) * n, ni, sLU, Uinv + (o + w) + (int64_t)(o + w) * SB,
+                          SB, sD, T, w)) != cudaSuccess)
+                return e;
+            if ((e = gemm(w, w, w, mone, Uinv + o + (int64_t)o * SB, SB, sD, T, w, sT, Uinv + o + (int64_t)(o + w) * SB,
+                          SB)) != cudaSuccess)
+                return e;
+        }
+    }
+    G->super_n = n;
+    return cudaSuccess;
 }
 
 // Capture body() on s into a graph (no profiler events inside the capture).
@@ -757,6 +861,10 @@ void LuGraphs::release() {
     if (dinv) cudaFree(dinv);
     if (panel) cudaFree(panel);
     if (tmp) cudaFree(tmp);
+    if (dinv4) cudaFree(dinv4);
+    if (super_tmp) cudaFree(super_tmp);
+    dinv4 = super_tmp = nullptr;
+    super_n = super_cap = 0;
     solve = nullptr;
     workspace = nullptr;
     dinv = panel = tmp = nullptr;
@@ -796,7 +904,8 @@ cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* b
     }
     const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
     ProfScope ps(Prof::LU_FACTOR, s);
-    return factor_body(st, G, LU, G->dinv, G->panel, n, bad);
+    if ((e = factor_body(st, G, LU, G->dinv, G->panel, n, bad)) != cudaSuccess) return e;
+    return build_super_inverses(h, G, LU, n, s);
 }
 
 // Lockstep factorization of m matrices: the same two-level blocked LU as factor_body
@@ -820,6 +929,9 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
     for (int q = 0; q < m; q++) {
         LuGraphs* G = Gs[q];
         const int64_t n = ns[q];
+        G->super_n = 0;  // no combined inverses for these factors: substitute by 128 columns
+        if (G->solve) cudaGraphExecDestroy(G->solve);
+        G->solve = nullptr;
         if (G->factor_n != n || !G->dinv) {
             if (G->solve) cudaGraphExecDestroy(G->solve);  // it holds the old Dinv
             G->solve = nullptr;
@@ -1171,7 +1283,8 @@ cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, f
             if ((e = cudaMalloc(&G->tmp, sizeof(float) * n * k)) != cudaSuccess) return e;
             G->tmp_floats = (size_t)n * k;
         }
-        e = capture(s, &G->solve, [&] { return solve_body(h, LU, G->dinv, n, X, G->tmp, k); });
+        const int64_t nsup = (G->super_n == n && G->dinv4) ? n / SB : 0;
+        e = capture(s, &G->solve, [&] { return solve_body(h, LU, G->dinv, G->dinv4, nsup, n, X, G->tmp, k); });
         if (e != cudaSuccess) return e;
         G->solve_X = X;
         G->solve_k = k;

@@ -138,10 +138,10 @@ struct LuGraphs {
     float* panel = nullptr;     // n x 128 staging for the panel GEMMs
     float* tmp = nullptr;       // n x k intermediate of the substitutions
     size_t tmp_floats = 0;
-    float* dinv4 = nullptr;     // inverses of the full 512-column diagonal blocks (L then U)
-    float* super_tmp = nullptr; // 256 x 256 scratch per 512-column block while they are built
+    float* dinv4 = nullptr;     // inverses of the full 1,024-column diagonal blocks (L then U)
+    float* super_tmp = nullptr; // 512 x 512 scratch per 1,024-column block while they are built
     int64_t super_n = 0;        // order they were built for (0: none, the substitutions use dinv)
-    int64_t super_cap = 0;      // 512-column blocks dinv4 and super_tmp hold
+    int64_t super_cap = 0;      // 1,024-column blocks dinv4 and super_tmp hold
     void release();
 };
 cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);

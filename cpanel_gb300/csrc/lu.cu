@@ -21,7 +21,7 @@
 namespace {
 
 constexpr int NB = 128;   // panel width
-constexpr int SB = 4 * NB; // blocks of the substitutions' combined inverses
+constexpr int SB = 8 * NB; // blocks of the substitutions' combined inverses
 constexpr int P = NB + 1; // padded smem pitch (no bank conflicts on row access)
 
 constexpr int DT = 512;    // threads of the diagonal-block kernel
@@ -690,7 +690,7 @@ cudaError_t factor_body(const Streams& st, LuGraphs* G, float* LU, float* Dinv, 
 // GEMMs per block and direction and no copies: forward, Y_K = inv(L_KK) X_K and
 // X_below -= L_below,K Y_K; backward, X_K = inv(U_KK) Y_K and Y_above -= U_above,K X_K.
 // X (n x k, ld n) ends with the solution; Y is an n x k scratch array.  The first nsup
-// 512-column blocks use their combined inverses (Dinv4), so a pass takes a quarter of the
+// SB-column blocks use their combined inverses (Dinv4), so a pass takes an eighth of the
 // dependent steps there; the rest of the matrix goes by 128-column blocks.
 cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, const float* Dinv4, int64_t nsup,
                        int64_t n, float* X, float* Y, int k) {
@@ -743,8 +743,8 @@ cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, con
     return cudaGetLastError();
 }
 
-// Inverses of the full 512-column diagonal blocks from the four 128-column ones inside
-// each, by two block-triangular doublings (128 -> 256 -> 512):
+// Inverses of the full SB-column diagonal blocks from the 128-column ones inside each, by
+// block-triangular doublings (128 -> 256 -> 512 -> 1024):
 //   [[A, 0], [C, B]]^{-1} = [[A^{-1}, 0], [-B^{-1} C A^{-1}, B^{-1}]]   (L, unit lower)
 //   [[A, C], [0, B]]^{-1} = [[A^{-1}, -A^{-1} C B^{-1}], [0, B^{-1}]]   (U)
 // Every step is one strided-batched FP32 GEMM over all the 512-column blocks (their
@@ -779,7 +779,7 @@ cudaError_t build_super_inverses(cublasHandle_t h, LuGraphs* G, const float* LU,
         G->dinv4 = G->super_tmp = nullptr;
         G->super_cap = 0;
         if ((e = cudaMalloc(&G->dinv4, sizeof(float) * nsup * 2 * SB * SB)) != cudaSuccess) return e;
-        if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * nsup * 256 * 256)) != cudaSuccess) return e;
+        if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * nsup * (SB / 2) * (SB / 2))) != cudaSuccess) return e;
         G->super_cap = nsup;
     }
     const int64_t tot = nsup * 2 * SB * SB;
@@ -787,7 +787,7 @@ cudaError_t build_super_inverses(cublasHandle_t h, LuGraphs* G, const float* LU,
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const float one = 1.f, mone = -1.f, zero = 0.f;
     const int ni = (int)n, bc = (int)nsup;
-    const long long sLU = (long long)SB * (n + 1), sD = 2LL * SB * SB, sT = 256LL * 256;
+    const long long sLU = (long long)SB * (n + 1), sD = 2LL * SB * SB, sT = (long long)(SB / 2) * (SB / 2);
     float* T = G->super_tmp;
     auto gemm = [&](int m, int nn, int kk, float alpha, const float* A, int lda, long long sA, const float* B, int ldb,
                     long long sB, float* C, int ldc) -> cudaError_t {
@@ -796,8 +796,7 @@ cudaError_t build_super_inverses(cublasHandle_t h, LuGraphs* G, const float* LU,
                    ? cudaSuccess
                    : cudaErrorUnknown;
     };
-    for (int half = 1; half <= 2; half++) {
-        const int w = NB * half;  // size of the two blocks combined at this level (128, then 256)
+    for (int w = NB; w < SB; w *= 2) {  // size of the two blocks combined at this level
         for (int p = 0; p < SB / (2 * w); p++) {
             const int o = 2 * w * p;  // offset of the pair inside the 512-column block
             float* Linv = G->dinv4;

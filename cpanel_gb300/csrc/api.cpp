@@ -36,6 +36,16 @@ struct cpg_ctx {
     cublasHandle_t blas = nullptr;
     int particle_precision = CPG_PLAIN_FP64;  // cpg_panels_velocity / cpg_panels_stretching
     std::vector<cpg_ctx*> workers;  // contexts of cpg_batch_solve, created on first use
+    // matrix buffers of destroyed geometries, kept for the next geometry of a similar size
+    // (no cudaMalloc for it, no device-wide synchronization in cudaFree); ev: recorded on
+    // the context's stream when the buffer was parked
+    struct Spare {
+        void* p;
+        size_t bytes;
+        cudaEvent_t ev;
+    };
+    std::vector<Spare> spare;
+    void* blas_ws[2] = {nullptr, nullptr};  // cuBLAS workspaces shared by the context's factorizations
 };
 
 namespace {
@@ -72,6 +82,72 @@ struct DevBuf {
     }
 };
 
+// Spare matrix buffers of a context: at most kSpareMax buffers and kSpareBytes bytes.
+constexpr size_t kSpareMax = 6;
+constexpr size_t kSpareBytes = size_t(16) << 30;
+
+void spare_free_oldest(cpg_ctx* c) {
+    auto sp = c->spare.front();
+    c->spare.erase(c->spare.begin());
+    cudaEventSynchronize(sp.ev);
+    cudaEventDestroy(sp.ev);
+    cudaFree(sp.p);
+}
+
+// hand b's memory to the context's spares (or free it)
+void park(cpg_ctx* c, DevBuf& b) {
+    if (!b.p) return;
+    cudaEvent_t ev = nullptr;
+    if (c && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess &&
+        cudaEventRecord(ev, c->stream) == cudaSuccess) {
+        c->spare.push_back(cpg_ctx::Spare{b.p, b.bytes, ev});
+        b.p = nullptr;
+        b.bytes = 0;
+        size_t tot = 0;
+        for (const auto& sp : c->spare) tot += sp.bytes;
+        while (!c->spare.empty() && (c->spare.size() > kSpareMax || tot > kSpareBytes)) {
+            tot -= c->spare.front().bytes;
+            spare_free_oldest(c);
+        }
+        return;
+    }
+    if (ev) cudaEventDestroy(ev);
+    b.release();
+}
+
+// DevBuf::ensure for the matrices: a spare of at least `bytes` (and at most twice that) is
+// taken once its last use has finished; otherwise cudaMalloc, after freeing the spares if
+// the device is out of memory
+cudaError_t ensure_big(cpg_ctx* c, DevBuf& b, size_t bytes) {
+    if (bytes <= b.bytes) return cudaSuccess;
+    park(c, b);
+    int best = -1;
+    for (size_t i = 0; i < c->spare.size(); i++) {
+        const auto& sp = c->spare[i];
+        if (sp.bytes >= bytes && sp.bytes <= 2 * bytes && (best < 0 || sp.bytes < c->spare[best].bytes)) best = (int)i;
+    }
+    if (best >= 0) {
+        auto sp = c->spare[best];
+        c->spare.erase(c->spare.begin() + best);
+        cudaError_t e = cudaEventSynchronize(sp.ev);
+        cudaEventDestroy(sp.ev);
+        b.p = sp.p;
+        b.bytes = sp.bytes;
+        return e;
+    }
+    cudaError_t e = b.ensure(bytes);
+    if (e == cudaErrorMemoryAllocation && !c->spare.empty()) {
+        cudaGetLastError();
+        while (!c->spare.empty()) spare_free_oldest(c);
+        e = b.ensure(bytes);
+    }
+    return e;
+}
+
+// the context's two cuBLAS workspaces for g's factorization and substitutions (one pair per
+// context: its work is ordered on its streams)
+cudaError_t attach_blas_ws(cpg_geometry* g);
+
 constexpr double kPi = 3.14159265358979323846;
 // Relative residual at which the mixed path's refinement stops (per right-hand side).
 // 1e-10 (two passes) measured Cp errors of 4.9e-6 against the plain path on the 19k
@@ -105,6 +181,22 @@ struct cpg_geometry {
     cpg::PostTables T;
     float ms_asm = 0;
 };
+
+namespace {
+cudaError_t attach_blas_ws(cpg_geometry* g) {
+    if (g->graphs.workspace) return cudaSuccess;
+    cpg_ctx* c = g->ctx;
+    for (void*& w : c->blas_ws)
+        if (!w) {
+            cudaError_t e = cudaMalloc(&w, cpg::lu_blas_workspace_bytes());
+            if (e != cudaSuccess) return e;
+        }
+    g->graphs.workspace = c->blas_ws[0];
+    g->graphs.workspace2 = c->blas_ws[1];
+    g->graphs.shared_ws = true;
+    return cudaSuccess;
+}
+}  // namespace
 
 struct cpg_ptree {
     cpg_ctx* ctx = nullptr;
@@ -282,6 +374,14 @@ int cpg_create(cpg_ctx** out, int device) {
 void cpg_destroy(cpg_ctx* c) {
     if (!c) return;
     for (cpg_ctx* w : c->workers) cpg_destroy(w);
+    for (auto& sp : c->spare) {
+        cudaEventSynchronize(sp.ev);
+        cudaEventDestroy(sp.ev);
+        cudaFree(sp.p);
+    }
+    c->spare.clear();
+    for (void*& w : c->blas_ws)
+        if (w) cudaFree(w);
     delete c->prof;
     if (c->blas) cublasDestroy(c->blas);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -395,6 +495,7 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
 
 void cpg_geometry_destroy(cpg_geometry* g) {
     if (!g) return;
+    for (DevBuf* b : {&g->A32, &g->Alo, &g->LU, &g->A64, &g->B64}) park(g->ctx, *b);
     DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
                       &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
                       &g->B64, &g->A32, &g->Alo, &g->rb, &g->LU, &g->bad, &g->count, &g->work, &g->post_work, &g->cases, &g->outs,
@@ -488,16 +589,16 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
     CK(cudaMemsetAsync(g->count.p, 0, sizeof(unsigned long long), s), "clear counter");
     CK(cudaEventRecord(e0, s), "event");
     if (precision == CPG_PLAIN_FP64) {
-        CK(g->A64.ensure(sizeof(double) * nn), "alloc A (FP64)");
-        CK(g->B64.ensure(sizeof(double) * nn), "alloc B (FP64)");
+        CK(ensure_big(ctx, g->A64, sizeof(double) * nn), "alloc A (FP64)");
+        CK(ensure_big(ctx, g->B64, sizeof(double) * nn), "alloc B (FP64)");
         CK(cpg::launch_assemble_fp64(g->rec.as<double>(), n, g->wrec.as<double>(), g->widx.as<int32_t>(),
                                      g->wcoef.as<double>(), g->H.n_wake, g->A64.as<double>(), g->B64.as<double>(),
                                      g->count.as<unsigned long long>(), s),
            "assembly (FP64)");
         g->have64 = true;
     } else if (precision == CPG_MIXED) {
-        CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
-        CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
+        CK(ensure_big(g->ctx, g->A32, sizeof(float) * nn), "alloc A (FP32)");
+        CK(ensure_big(g->ctx, g->Alo, sizeof(float) * nn), "alloc A low part (FP32)");
         CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n, g->H.n_wake))), "alloc rhs basis");
         if (g->order_n != n) {  // block schedule, once per geometry
             std::vector<int> ord;
@@ -612,7 +713,8 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
             return fail(ctx, CPG_E_CUDA, "cublasCreate failed");
         }
         if (!g->lu_ready) {  // per-geometry factorization, reused by every case
-            CK(g->LU.ensure(sizeof(float) * (size_t)n * n), "alloc LU");
+            CK(ensure_big(g->ctx, g->LU, sizeof(float) * (size_t)n * n), "alloc LU");
+            CK(attach_blas_ws(g), "alloc cuBLAS workspaces");
             CK(g->bad.ensure(sizeof(int)), "alloc flag");
             CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
             CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");
@@ -1052,8 +1154,8 @@ int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cp
         cpg_geometry* g = gs[q];
         const int64_t n = g->H.n_body;
         const size_t nn = (size_t)n * n;
-        CK(g->A32.ensure(sizeof(float) * nn), "alloc A (FP32)");
-        CK(g->Alo.ensure(sizeof(float) * nn), "alloc A low part (FP32)");
+        CK(ensure_big(g->ctx, g->A32, sizeof(float) * nn), "alloc A (FP32)");
+        CK(ensure_big(g->ctx, g->Alo, sizeof(float) * nn), "alloc A low part (FP32)");
         CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n, g->H.n_wake))), "alloc rhs basis");
         desc[q] = cpg::MixedMeshDesc{g->rec.as<double>(), g->frec.as<float>(), g->erec.as<double>(), n,
                                      cpg::mixed_chunk(n), g->A32.as<float>(), g->Alo.as<float>(),
@@ -1245,7 +1347,8 @@ int cpg_lu_factor_grouped(cpg_geometry* const* gs, int m, double* ms_out) {
     for (int q = 0; q < m; q++) {
         cpg_geometry* g = gs[q];
         const int64_t n = g->H.n_body;
-        CK(g->LU.ensure(sizeof(float) * (size_t)n * n), "alloc LU");
+        CK(ensure_big(g->ctx, g->LU, sizeof(float) * (size_t)n * n), "alloc LU");
+        CK(attach_blas_ws(g), "alloc cuBLAS workspaces");
         CK(g->bad.ensure(sizeof(int)), "alloc flag");
         CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
         CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");

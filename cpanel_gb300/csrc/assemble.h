@@ -132,6 +132,7 @@ struct LuGraphs {
     int solve_k = 0;
     void* workspace = nullptr;  // cuBLAS workspace (no allocation inside a capture)
     void* workspace2 = nullptr; // cuBLAS workspace of the panel stream
+    bool shared_ws = false;     // both workspaces belong to the caller (not freed by release)
     cudaStream_t panel_stream = nullptr;  // high-priority stream of the panel factorizations
     cudaEvent_t ev_update = nullptr, ev_panel = nullptr;  // fork / join inside the capture
     float* dinv = nullptr;      // inverses of the diagonal blocks (L then U per block)
@@ -145,6 +146,8 @@ struct LuGraphs {
     void release();
 };
 cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);
+// bytes of each of the two cuBLAS workspaces a LuGraphs uses
+size_t lu_blas_workspace_bytes();
 // One matrix of a lockstep factorization (device copy).
 struct LuBatchMesh {
     float* LU;

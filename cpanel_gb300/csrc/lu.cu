@@ -849,8 +849,10 @@ cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body, unsigned long 
 
 void LuGraphs::release() {
     if (solve) cudaGraphExecDestroy(solve);
-    if (workspace) cudaFree(workspace);
-    if (workspace2) cudaFree(workspace2);
+    if (workspace && !shared_ws) cudaFree(workspace);
+    if (workspace2 && !shared_ws) cudaFree(workspace2);
+    workspace = nullptr;
+    shared_ws = false;
     if (panel_stream) cudaStreamDestroy(panel_stream);
     if (ev_update) cudaEventDestroy(ev_update);
     if (ev_panel) cudaEventDestroy(ev_panel);
@@ -899,7 +901,7 @@ cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* b
             return e;
         if ((e = cudaEventCreateWithFlags(&G->ev_update, cudaEventDisableTiming)) != cudaSuccess) return e;
         if ((e = cudaEventCreateWithFlags(&G->ev_panel, cudaEventDisableTiming)) != cudaSuccess) return e;
-        if ((e = cudaMalloc(&G->workspace2, kBlasWorkspace)) != cudaSuccess) return e;
+        if (!G->workspace2 && (e = cudaMalloc(&G->workspace2, kBlasWorkspace)) != cudaSuccess) return e;
     }
     const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
     ProfScope ps(Prof::LU_FACTOR, s);
@@ -1265,6 +1267,8 @@ cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, in
     }
     return cudaGetLastError();
 }
+
+size_t lu_blas_workspace_bytes() { return kBlasWorkspace; }
 
 // X (n x k, ld n) <- U^{-1} L^{-1} X
 cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s) {

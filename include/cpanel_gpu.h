@@ -102,6 +102,8 @@ int         cpg_synchronize(cpg_ctx* ctx);
  * nodes n_nodes x 3, tris n_tris x 3 (1-based, Cart3D order), ids per tri (>1000: wake). */
 int  cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const int64_t* tris,
                          const int32_t* ids, int64_t n_tris, cpg_geometry** out);
+/* Destroy a geometry before its context: its matrix buffers go to the context's spares
+ * (at most 6 buffers and 16 GB), taken by the next geometry of a similar size. */
 void cpg_geometry_destroy(cpg_geometry* g);
 int  cpg_geometry_info_get(const cpg_geometry* g, cpg_geometry_info* out);
 /* Host copies of the topology for checking (same layouts as the CPU oracle):

@@ -1389,6 +1389,10 @@ int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* f
     cudaStream_t s = ctx->stream;
     cudaEvent_t join;
     CK(cudaEventCreateWithFlags(&join, cudaEventDisableTiming), "event");
+    struct EvGuard {
+        cudaEvent_t e;
+        ~EvGuard() { cudaEventDestroy(e); }
+    } jg{join};
     for (int q = 0; q < m; q++)
         if (gs[q]->ctx != ctx) {
             CK(cudaEventRecord(join, gs[q]->ctx->stream), "event");
@@ -1403,15 +1407,10 @@ int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* f
         cpg_geometry* g = gs[q];
         const int k = ks[q];
         const int64_t n = g->H.n_body, nw = g->H.n_wake;
-        if (!g->have32 || !g->lu_ready || k < 1 || k > 4096) {
-            cudaEventDestroy(join);
+        if (!g->have32 || !g->lu_ready || k < 1 || k > 4096)
             return fail(ctx, CPG_E_INVALID, "grouped solve: geometry without mixed matrix or factors, or bad k");
-        }
         int rc = prepare_post(g);
-        if (rc != CPG_OK) {
-            cudaEventDestroy(join);
-            return rc;
-        }
+        if (rc != CPG_OK) return rc;
         cudaStream_t t = g->ctx->stream;  // this geometry's own work
         std::vector<cpg::CaseScalars> cs(k);
         for (int c = 0; c < k; c++) case_scalars(flows[q][c], refs[q], cs[c]);
@@ -1436,7 +1435,6 @@ int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* f
         rm[q] = cpg::RefineMesh{g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(), g->graphs.dinv, n, k,
                                 o.rhs, o.mu, g->work.p, t};
     }
-    cudaEventDestroy(join);
     std::vector<cpg::SolveStats> st(m);
     CK(cpg::solve_lu_refined_batched(rm.data(), m, kMixedRefineTol, 16, st.data(), s), "refined solves (grouped)");
     for (int q = 0; q < m; q++) {

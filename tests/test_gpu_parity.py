@@ -125,6 +125,19 @@ def test_4412_reference_case_on_gpu(cg, case4412):
     assert abs(case.getBodyForces()[2] - CN) <= 5.01e-6
 
 
+def test_4412_reference_case_mixed_on_gpu(cg, case4412):
+    """The reference's own 4412 case (4,824 body panels) through the mixed path: the printed
+    CL and CDi (5 decimals) as the plain path reproduces them."""
+    gg = case4412
+    g = cg.Geometry(gg["nodes"], gg["tris"].astype(np.int64), gg["ids"])
+    case = cg.CpCase(g, float(gg["V"]), float(gg["alpha"]), float(gg["beta"]), float(gg["mach"]),
+                     Sref=float(gg["Sref"]), bref=float(gg["bref"]), cref=float(gg["cref"]), cg=tuple(gg["cg"]),
+                     precision="mixed")
+    assert case.run()
+    assert abs(case.getCL() - float(gg["CL"])) <= 5.01e-6
+    assert abs(case.getCD() - float(gg["CDi"])) <= 5.01e-6
+
+
 def test_mixed_matches_plain_within_tolerance(cg, small):
     g, m, Ao, Bo, refs = small
     flows = [(1.0, a, 0.0, 0.1) for a in (-4.0, 0.0, 5.0, 12.0)]

@@ -72,6 +72,10 @@ class Context:
     def synchronize(self):
         self.check(self.L.cpg_synchronize(self.h), "synchronize")
 
+    def release_spares(self):
+        """Free the matrix buffers kept from destroyed geometries (cpg_release_spares)."""
+        self.check(self.L.cpg_release_spares(self.h), "release_spares")
+
     def prof_enable(self, on=True):
         self.check(self.L.cpg_prof_enable(self.h, 1 if on else 0), "prof_enable")
 

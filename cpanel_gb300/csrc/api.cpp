@@ -391,6 +391,12 @@ void cpg_destroy(cpg_ctx* c) {
 
 const char* cpg_last_error(const cpg_ctx* c) { return c ? c->err.c_str() : "null context"; }
 
+int cpg_release_spares(cpg_ctx* c) {
+    if (!c) return CPG_E_INVALID;
+    while (!c->spare.empty()) spare_free_oldest(c);
+    return CPG_OK;
+}
+
 int cpg_set_stream(cpg_ctx* ctx, void* stream) {
     if (!ctx) return CPG_E_INVALID;
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);

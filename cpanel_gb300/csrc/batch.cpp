@@ -148,6 +148,8 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
     double ms_assembly = 0, ms_factor = 0, ms_solve = 0;
     cpg_group_report last{};
     for (const std::vector<int>& wave : waves) {
+        if (&wave != &waves.front())  // the previous wave's matrices: this wave was sized by the budget
+            for (cpg_ctx* w : wk) cpg_release_spares(w);
         std::vector<cpg_geometry*> gs;
         for (int i : wave) gs.push_back(g[i]);
         cpg_group_report rep{};

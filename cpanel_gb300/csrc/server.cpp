@@ -95,6 +95,7 @@ void run_request(cpg_ctx* ctx, int precision, Request& r) {
     if (rc != CPG_OK) r.message = cpg_last_error(ctx);
     r.status = rc;
     if (g) cpg_geometry_destroy(g);
+    cpg_release_spares(ctx);  // admission counts only the running requests' memory
 }
 
 void run_request_vp(cpg_ctx* ctx, Request& r) {

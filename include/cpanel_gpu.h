@@ -105,6 +105,9 @@ int  cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, con
 /* Destroy a geometry before its context: its matrix buffers go to the context's spares
  * (at most 6 buffers and 16 GB), taken by the next geometry of a similar size. */
 void cpg_geometry_destroy(cpg_geometry* g);
+/* Free the context's spare matrix buffers now (for callers that account for device memory
+ * themselves; the request loop and the batch solve call it after each request and wave). */
+int  cpg_release_spares(cpg_ctx* ctx);
 int  cpg_geometry_info_get(const cpg_geometry* g, cpg_geometry_info* out);
 /* Host copies of the topology for checking (same layouts as the CPU oracle):
  * body: n_body x 18 [c(3) n(3) l(3) area longSide tip upper lower TSorder surfID

@@ -148,6 +148,26 @@ def test_mixed_matches_plain_within_tolerance(cg, small):
     assert np.all(np.abs(rm["CL"] - rp["CL"]) <= 1e-6 * np.abs(rp["CL"]) + 1e-9)
 
 
+def test_repeated_geometries_reuse_matrix_buffers(cg, small):
+    """A destroyed geometry's matrices go to its context's spares and the next geometry of the
+    same size takes them: every solve overwrites them completely, so the results repeat bit
+    for bit; the spares can be freed at any time."""
+    g, m, Ao, Bo, refs = small
+    ctx = cg.Context(0)
+    flows = [(1.0, a, 0.0, 0.1) for a in (-2.0, 4.0)]
+    outs = []
+    for _ in range(3):
+        ge = cg.Geometry(m.nodes, m.tris, m.ids, ctx=ctx)
+        outs.append(cg.solve_cases(ge, flows, precision="mixed", want=("mu", "cp"), **refs))
+        del ge
+    for o in outs[1:]:
+        assert np.array_equal(o["cp"], outs[0]["cp"]) and np.array_equal(o["mu"], outs[0]["mu"])
+    ctx.release_spares()
+    ge = cg.Geometry(m.nodes, m.tris, m.ids, ctx=ctx)
+    o = cg.solve_cases(ge, flows, precision="mixed", want=("cp",), **refs)
+    assert np.array_equal(o["cp"], outs[0]["cp"])
+
+
 def test_mixed_many_right_hand_sides(cg, small):
     """More cases than one column group of the blocked triangular solves (32)."""
     g, m, Ao, Bo, refs = small

@@ -41,6 +41,17 @@ METRIC = "steady solves/s + p50/p99 latency at Cp err<=1e-5 vs FP64 plain GPU pa
 PLAIN_ITERS = 372
 
 
+def max_over_ranks(t, dist=None, device="cuda"):
+    """The slowest rank's time (every rank runs the whole workload on its own GPU: replicas,
+    weak scaling); t itself on one rank."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return t
+    import torch
+    tt = torch.tensor([t], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def workload(name="multi_rhs"):
     """multi_rhs: the benchmark wing.  mid: the same wing with 25 span stations
     (7,876 panels; matrices still larger than L2), used for profiler captures."""
@@ -583,11 +594,7 @@ def main():
     prof = ctx.prof_read()
     ctx.prof_enable(False)
     t_dev = sum(lat) / 1e3
-    t_max = t_dev
-    if dist:
-        tt = torch.tensor([t_dev], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = max_over_ranks(t_dev, dist)
     value = world * k * args.steps / t_max
     stats = r["stats"]
 

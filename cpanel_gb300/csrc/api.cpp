@@ -12,6 +12,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <stdexcept>
 #include <tuple>
 #include <string>
 #include <vector>
@@ -1091,8 +1092,8 @@ static bool group_shape_valid(const cpg_group_shape& s) {
            s.blocks_per_sm >= 0 && s.blocks_per_sm <= 64;
 }
 
-int cpg_group_schedule(const int64_t* n_body, int m, const cpg_group_shape* shape, int32_t* items, int64_t cap,
-                       int64_t* count, int64_t* chunk_len) {
+static int group_schedule_impl(const int64_t* n_body, int m, const cpg_group_shape* shape, int32_t* items,
+                               int64_t cap, int64_t* count, int64_t* chunk_len) {
     if (!n_body || m <= 0 || !count) return CPG_E_INVALID;
     cpg_group_shape sh;
     cpg_group_default_shape(&sh);
@@ -1112,12 +1113,21 @@ int cpg_group_schedule(const int64_t* n_body, int m, const cpg_group_shape* shap
     return CPG_OK;
 }
 
+int cpg_group_schedule(const int64_t* n_body, int m, const cpg_group_shape* shape, int32_t* items, int64_t cap,
+                       int64_t* count, int64_t* chunk_len) {
+    try {
+        return group_schedule_impl(n_body, m, shape, items, cap, count, chunk_len);
+    } catch (const std::bad_alloc&) {
+        return CPG_E_OOM;
+    }
+}
+
 namespace {
 std::mutex g_tune_mu;
 std::map<std::tuple<int, int, int>, cpg_group_shape> g_tune_cache;  // (device, log2 m, 2 log2 pairs)
 }  // namespace
 
-int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cpg_group_shape* shape,
+static int set_inf_coeff_grouped_impl(cpg_geometry* const* gs, int m, int tune, const cpg_group_shape* shape,
                               cpg_group_report* rep) {
     if (!gs || m <= 0) return CPG_E_INVALID;
     for (int q = 0; q < m; q++)
@@ -1312,7 +1322,19 @@ int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cp
     return CPG_OK;
 }
 
-int cpg_lu_factor_grouped(cpg_geometry* const* gs, int m, double* ms_out) {
+int cpg_set_inf_coeff_grouped(cpg_geometry* const* gs, int m, int tune, const cpg_group_shape* shape,
+                              cpg_group_report* rep) {
+    try {
+        return set_inf_coeff_grouped_impl(gs, m, tune, shape, rep);
+    } catch (const std::bad_alloc&) {
+        return fail((gs && m > 0 && gs[0]) ? gs[0]->ctx : nullptr, CPG_E_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail((gs && m > 0 && gs[0]) ? gs[0]->ctx : nullptr, CPG_E_INVALID, e.what());
+    }
+}
+
+
+static int lu_factor_grouped_impl(cpg_geometry* const* gs, int m, double* ms_out) {
     if (!gs || m <= 0) return CPG_E_INVALID;
     for (int q = 0; q < m; q++)
         if (!gs[q]) return CPG_E_INVALID;
@@ -1374,6 +1396,17 @@ int cpg_lu_factor_grouped(cpg_geometry* const* gs, int m, double* ms_out) {
     for (int q = 0; q < m; q++) gs[q]->lu_ready = true;
     return CPG_OK;
 }
+
+int cpg_lu_factor_grouped(cpg_geometry* const* gs, int m, double* ms_out) {
+    try {
+        return lu_factor_grouped_impl(gs, m, ms_out);
+    } catch (const std::bad_alloc&) {
+        return fail((gs && m > 0 && gs[0]) ? gs[0]->ctx : nullptr, CPG_E_OOM, "host allocation failed");
+    } catch (const std::exception& e) {
+        return fail((gs && m > 0 && gs[0]) ? gs[0]->ctx : nullptr, CPG_E_INVALID, e.what());
+    }
+}
+
 
 }  // extern "C"
 

@@ -20,6 +20,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <new>
+#include <stdexcept>
 #include <numeric>
 #include <string>
 #include <thread>
@@ -43,23 +45,29 @@ double ms_since(std::chrono::steady_clock::time_point t0) {
     return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
 }
 
-// runs fn(w) on one host thread per worker, each with the device current
+// runs fn(w) on one host thread per worker, each with the device current; if a thread
+// cannot be started, the started ones are joined and the error is passed on
 template <typename F>
 void on_workers(int W, int device, F fn) {
     std::vector<std::thread> th;
     th.reserve(W);
-    for (int w = 0; w < W; w++)
-        th.emplace_back([&, w] {
-            cudaSetDevice(device);
-            fn(w);
-        });
+    try {
+        for (int w = 0; w < W; w++)
+            th.emplace_back([&, w] {
+                cudaSetDevice(device);
+                fn(w);
+            });
+    } catch (...) {
+        for (auto& t : th) t.join();
+        throw;
+    }
     for (auto& t : th) t.join();
 }
 
 }  // namespace
 
-extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg_batch_params* p,
-                               cpg_batch_stats* st) {
+static int batch_solve_impl(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg_batch_params* p,
+                            cpg_batch_stats* st) {
     if (!ctx || !M || m <= 0) return CPG_E_INVALID;
     const auto T0 = std::chrono::steady_clock::now();
     int W = (p && p->workers > 0) ? p->workers : 8;
@@ -237,4 +245,17 @@ extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg
         st->group = last;
     }
     return first_bad;
+}
+
+extern "C" int cpg_batch_solve(cpg_ctx* ctx, cpg_batch_mesh* M, int m, const cpg_batch_params* p,
+                               cpg_batch_stats* st) {
+    try {
+        return batch_solve_impl(ctx, M, m, p, st);
+    } catch (const std::bad_alloc&) {
+        cpg::ctx_set_error(ctx, "host allocation failed");
+        return CPG_E_OOM;
+    } catch (const std::exception& e) {
+        cpg::ctx_set_error(ctx, e.what());
+        return CPG_E_INVALID;
+    }
 }

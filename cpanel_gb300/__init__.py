@@ -14,6 +14,7 @@ All compute runs in libcpanel_gb300.so (sm_103a); this module only marshals
 arguments.  There is no CPU fallback.
 """
 import atexit
+import os
 import ctypes as C
 import sys
 
@@ -253,6 +254,28 @@ class CpCase:
 
     def getVelocity(self):
         return self.res["vel"][0]
+
+    def writeFiles(self, directory=".", geom_file=""):
+        """cpCase::writeFiles (CPanel/cpCase.cpp:667-709) for the body: the case directory
+        V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, and
+        caseMgr::writeSummary's .CPout (CPanel/CPanelMgr.cpp:89-116) beside it.  Returns the
+        paths written."""
+        from . import io
+        V, alpha, beta, mach = self.flow
+        sub = os.path.join(directory, io.case_label(V, mach, alpha, beta))
+        os.makedirs(sub, exist_ok=True)
+        t = self.geom.tables()
+        body = t["body"]
+        tris = self.geom._tris[body[:, 17].astype(np.int64)] - 1  # file triangle of each panel, zero-based
+        vtu = os.path.join(sub, "surfaceData.vtu")
+        io.write_surface_vtu(vtu, self.geom._nodes, tris, self.res["mu"][0], self.res["sigma"][0],
+                             self.res["phi"][0], self.res["vel"][0], self.res["cp"][0], body[:, 3:6], body[:, 0:3])
+        stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
+        cpout = os.path.join(directory, stem + ".CPout")
+        io.write_cpout(cpout, [dict(V=V, alpha=alpha, beta=beta, mach=mach, CL=self.getCL(), CDi=self.getCD(),
+                                    Fbody=self.getBodyForces(), Fwind=self.getWindForces(), CM=self.getMoment())],
+                       geom_file=geom_file, **self.refs)
+        return vtu, cpout
 
 
 def _dev_ptr(t):

@@ -74,7 +74,9 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_server_submit_vp", "cpg_server_wait_vp", "cpg_server_footprint_vp",
            # cpanel_batch.h
            "cpg_group_default_shape", "cpg_set_inf_coeff_grouped", "cpg_group_schedule", "cpg_batch_solve",
-           "cpg_lu_factor_grouped"]
+           "cpg_lu_factor_grouped",
+           # cpanel_io.h
+           "cpg_write_cpout", "cpg_write_surface_vtu"]
 
 TUNE_OFF, TUNE_AUTO, TUNE_FORCE = 0, 1, 2
 
@@ -136,6 +138,20 @@ class BatchStats(C.Structure):
     _fields_ = [("ms_total", C.c_double), ("ms_topology", C.c_double), ("ms_assembly", C.c_double),
                 ("ms_factor", C.c_double), ("ms_solve", C.c_double), ("waves", C.c_int), ("solves", C.c_int64), ("failed", C.c_int),
                 ("group", GroupReport)]
+
+
+class CpoutInputs(C.Structure):
+    _fields_ = [("geom_file", C.c_char_p), ("Sref", C.c_double), ("bref", C.c_double), ("cref", C.c_double),
+                ("cg", C.c_double * 3), ("velocities", D), ("n_velocities", C.c_int), ("alphas", D),
+                ("n_alphas", C.c_int), ("betas", D), ("n_betas", C.c_int), ("machs", D), ("n_machs", C.c_int),
+                ("subsonic_hom", C.c_int), ("surface_streamlines", C.c_int), ("stability_derivatives", C.c_int),
+                ("write_inf_coeff", C.c_int), ("vortex_particles", C.c_int), ("accelerate_code", C.c_int),
+                ("unsteady", C.c_int)]
+
+
+class CpoutCase(C.Structure):
+    _fields_ = [("flow", Flow), ("CL", C.c_double), ("CDi", C.c_double), ("Fbody", C.c_double * 3),
+                ("Fwind", C.c_double * 3), ("CM", C.c_double * 3)]
 
 
 def load():
@@ -219,5 +235,7 @@ def load():
     L.cpg_group_schedule.argtypes = [I64, C.c_int, C.POINTER(GroupShape), I32, C.c_int64, I64, I64]
     L.cpg_batch_solve.argtypes = [vp, C.POINTER(BatchMesh), C.c_int, C.POINTER(BatchParams), C.POINTER(BatchStats)]
     L.cpg_lu_factor_grouped.argtypes = [C.POINTER(vp), C.c_int, D]
+    L.cpg_write_cpout.argtypes = [C.c_char_p, C.POINTER(CpoutInputs), C.POINTER(CpoutCase), C.c_int]
+    L.cpg_write_surface_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D, D, D, D, D, D]
     _lib = L
     return L

@@ -1,0 +1,89 @@
+"""CPanel's result files from this library's results (include/cpanel_io.h): the .CPout
+summary (caseMgr::writeSummary, CPanel/CPanelMgr.cpp:89-180) and surfaceData.vtu
+(cpCase::writeBodyData, CPanel/cpCase.cpp:711-763).  Host only: no device is needed.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+from . import _lib
+from ._lib import CpgError
+
+
+def _d(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(_lib.D)
+
+
+def _unique(vals):
+    out = []
+    for v in vals:
+        if v not in out:
+            out.append(v)
+    return np.array(out, dtype=np.float64)
+
+
+def write_cpout(path, cases, geom_file="", Sref=1.0, bref=1.0, cref=1.0, cg=(0.0, 0.0, 0.0), flags=None):
+    """cases: dicts with V, alpha, beta, mach, CL, CDi, Fbody (x, y, z), Fwind (x, y, z) and CM
+    (roll, pitch, yaw), as solve_cases / CpCase return them.  flags: the input flags to echo
+    (subsonic_hom, surface_streamlines, stability_derivatives, write_inf_coeff,
+    vortex_particles, accelerate_code, unsteady); all OFF by default."""
+    L = _lib.load()
+    keep = []
+    lists = {}
+    for key in ("V", "alpha", "beta", "mach"):
+        arr, ptr = _d(_unique([float(c[key]) for c in cases]))
+        keep.append(arr)
+        lists[key] = (ptr, len(arr))
+    f = dict(flags or {})
+    inp = _lib.CpoutInputs(geom_file.encode(), Sref, bref, cref, (C.c_double * 3)(*cg),
+                           lists["V"][0], lists["V"][1], lists["alpha"][0], lists["alpha"][1],
+                           lists["beta"][0], lists["beta"][1], lists["mach"][0], lists["mach"][1],
+                           *[int(bool(f.get(k, False))) for k in ("subsonic_hom", "surface_streamlines",
+                                                                  "stability_derivatives", "write_inf_coeff",
+                                                                  "vortex_particles", "accelerate_code",
+                                                                  "unsteady")])
+    arr = (_lib.CpoutCase * max(1, len(cases)))()
+    for i, c in enumerate(cases):
+        arr[i] = _lib.CpoutCase(_lib.Flow(c["V"], c["alpha"], c["beta"], c["mach"]), c["CL"], c["CDi"],
+                                (C.c_double * 3)(*c["Fbody"]), (C.c_double * 3)(*c["Fwind"]),
+                                (C.c_double * 3)(*c["CM"]))
+    rc = L.cpg_write_cpout(os.fsencode(path), C.byref(inp), arr, len(cases))
+    if rc != 0:
+        raise CpgError(rc, "cpg_write_cpout(%s)" % path)
+
+
+def write_surface_vtu(path, nodes, tris, mu, sigma, phi, vel, cp, bez, centers):
+    """nodes (n_nodes x 3); tris (n x 3) zero-based node indices of the body panels in matrix
+    order; per panel mu, sigma, phi, cp (n) and vel, bez, centers (n x 3)."""
+    L = _lib.load()
+    t = np.ascontiguousarray(tris, dtype=np.int64)
+    arrays = [_d(a) for a in (nodes, mu, sigma, phi, vel, cp, bez, centers)]
+    (nd, ndp), (m, mp), (s, sp), (p, pp), (v, vp), (c, cpp), (b, bp), (ce, cep) = arrays
+    rc = L.cpg_write_surface_vtu(os.fsencode(path), ndp, len(nd), t.ctypes.data_as(_lib.I64), len(t), mp, sp, pp, vp,
+                                 cpp, bp, cep)
+    if rc != 0:
+        raise CpgError(rc, "cpg_write_surface_vtu(%s)" % path)
+
+
+def read_vtu_cells(path):
+    """The cell data arrays, points and connectivity of an ASCII .vtu file (as written by CPanel
+    or by write_surface_vtu): {name: array}."""
+    txt = open(path).read()
+    out = {}
+    for m in re.finditer(r'<DataArray type="(\w+)" Name="([^"]+)"(?: NumberOfComponents="(\d+)")? Format="ascii">'
+                         r'(.*?)</DataArray>', txt, flags=re.S):
+        kind, name, comps, body = m.group(1), m.group(2), m.group(3), m.group(4)
+        vals = np.array(body.split(), dtype=np.float64 if kind == "Float64" else np.int64)
+        ncomp = int(comps) if comps else 1
+        out[name] = vals.reshape(-1, ncomp) if ncomp > 1 else vals
+    return out
+
+
+def case_label(V, mach, alpha, beta):
+    """The case directory name cpCase::writeFiles uses (CPanel/cpCase.cpp:669-670)."""
+    def g(x):
+        return ("%.6g" % x)
+    return "V%s_Mach%s_alpha%s_beta%s" % (g(V), g(mach), g(alpha), g(beta))

@@ -1,0 +1,66 @@
+/*
+ * cpanel_io.h -- CPanel's result files from this library's results (host only, no device).
+ *
+ * Reference interfaces replaced (paths relative to the CPanel project root):
+ *   cpg_write_cpout         caseMgr::writeSummary / writeCase, CPanel/CPanelMgr.cpp:89-180, with the
+ *                           input echo of inputParams::print, CPanel/inputParams.cpp:227-318
+ *   cpg_write_surface_vtu   cpCase::writeBodyData, CPanel/cpCase.cpp:711-763, through
+ *                           VTUfile::write, CPanel/VTUfile.cpp:20-147
+ *
+ * The text follows the reference's layout and stream formatting (the same column widths,
+ * precisions and array names), so the files diff against CPanel's own.  One difference is
+ * unavoidable: the reference numbers nodes after sorting node pointers (geometry.cpp:405-406),
+ * which varies from run to run; here nodes keep their .tri file order.
+ */
+#ifndef CPANEL_IO_H
+#define CPANEL_IO_H
+
+#include <stdint.h>
+
+#include "cpanel_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* The input echo of a .CPout file (what the reference reads from its .CPin). */
+typedef struct {
+    const char* geom_file;
+    double Sref, bref, cref, cg[3];
+    const double* velocities;
+    int n_velocities;
+    const double* alphas;
+    int n_alphas;
+    const double* betas;
+    int n_betas;
+    const double* machs;
+    int n_machs;
+    int subsonic_hom, surface_streamlines, stability_derivatives, write_inf_coeff, vortex_particles,
+        accelerate_code, unsteady; /* printed ON (non-zero) or OFF */
+} cpg_cpout_inputs;
+
+/* One case of a .CPout file: the coefficient vectors as cpCase returns them. */
+typedef struct {
+    cpg_flow flow;    /* V, alpha, beta, mach                                           */
+    double CL, CDi;   /* Trefftz plane                                                  */
+    double Fbody[3];  /* body-axis force coefficients (x, y, z): printed CN, CA, CY     */
+    double Fwind[3];  /* wind-axis force coefficients (x, y, z): printed CL, CD, CY     */
+    double CM[3];     /* moment coefficients (roll, pitch, yaw): printed Cm, Cl, Cn     */
+} cpg_cpout_case;
+
+/* Write the .CPout summary of n_cases cases. */
+int cpg_write_cpout(const char* path, const cpg_cpout_inputs* inputs, const cpg_cpout_case* cases, int n_cases);
+
+/* Write surfaceData.vtu for one case: nodes n_nodes x 3; tris n x 3 zero-based node indices of
+ * the body panels in matrix order; per body panel mu, sigma, phi, cp (n), vel, bez, centers
+ * (n x 3).  Cell arrays as the reference names them ("Doublet Strengths", "Source Strengths",
+ * "Velocity Potential", "Velocity", "Cp", "bezNormals", "xPosition", "yPosition",
+ * "zPostition"). */
+int cpg_write_surface_vtu(const char* path, const double* nodes, int64_t n_nodes, const int64_t* tris, int64_t n,
+                          const double* mu, const double* sigma, const double* phi, const double* vel,
+                          const double* cp, const double* bez, const double* centers);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CPANEL_IO_H */

@@ -26,6 +26,18 @@ def case4412():
     return dict(np.load(os.path.join(GOLDEN, "case4412.npz")))
 
 
+@pytest.fixture(scope="session")
+def solved4412(case4412):
+    """The reference's 4412 case through the CPU oracle: (mesh, A, B, results)."""
+    from oracle import pyoracle as po
+    g = case4412
+    m = po.Mesh(g["nodes"], g["tris"], g["ids"])
+    A, B = m.set_inf_coeff()
+    r = m.case(A, B, V=float(g["V"]), alpha=float(g["alpha"]), beta=float(g["beta"]), mach=float(g["mach"]),
+               Sref=float(g["Sref"]), bref=float(g["bref"]), cref=float(g["cref"]), cg=tuple(g["cg"]))
+    return m, A, B, r
+
+
 def small_wing(n_chord=12, n_span=6, alpha=5.0, wake_len=30.0, **kw):
     from cpanel_gb300 import wing
     spec = wing.WingSpec(m=kw.pop("m", 0.0), t=kw.pop("t", 0.12), root_chord=1.0, span=kw.pop("span", 4.0),

@@ -1,0 +1,90 @@
+"""CPanel's result files (include/cpanel_io.h), on the CPU: the reference's 4412 case solved by
+the oracle, written as surfaceData.vtu and .CPout by the library's writers, read back and
+compared with the reference's own output for that case (surfaceData-0.vtu and 4412.CPout, kept
+in tests/golden/case4412.npz) at the precision the reference prints."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+
+def _panel_tables(g):
+    import cpanel_gb300 as cg
+    t = cg.topology(g["nodes"], g["tris"].astype(np.int64), g["ids"])
+    return t["body"]
+
+
+def test_surface_vtu_round_trip_matches_reference_output(built, case4412, solved4412, tmp_path):
+    from scipy.spatial import cKDTree
+
+    from cpanel_gb300 import io
+    g = case4412
+    m, A, B, r = solved4412
+    body = _panel_tables(g)
+    tris = g["tris"].astype(np.int64)[body[:, 17].astype(np.int64)] - 1
+    path = str(tmp_path / "surfaceData.vtu")
+    io.write_surface_vtu(path, g["nodes"], tris, r["mu"], r["sigma"], r["phi"], r["vel"], r["cp"], body[:, 3:6],
+                         body[:, 0:3])
+    d = io.read_vtu_cells(path)
+    n = len(body)
+    assert set(d) == {"Doublet Strengths", "Source Strengths", "Velocity Potential", "Velocity", "Cp", "bezNormals",
+                      "xPosition", "yPosition", "zPostition", "Position", "connectivity", "offsets", "types"}
+    assert d["connectivity"].size == 3 * n and np.all(d["types"] == 5) and np.all(d["offsets"] == 3 * np.arange(1, n + 1))
+    assert np.array_equal(d["connectivity"].reshape(n, 3), tris)
+    # the reference's surfaceData-0.vtu, matched by panel centroid, at its 6 significant digits
+    c = np.stack([d["xPosition"], d["yPosition"], d["zPostition"]], axis=1)
+    dist, idx = cKDTree(c).query(g["centroid"].astype(np.float64))
+    assert dist.max() < 1e-5 and len(np.unique(idx)) == len(idx)
+    for name, key in (("Doublet Strengths", "mu"), ("Source Strengths", "sigma"), ("Velocity Potential", "phi"),
+                      ("Cp", "cp"), ("Velocity", "vel")):
+        ref = g[key].astype(np.float64)
+        assert np.all(np.abs(d[name][idx] - ref) <= 1.2e-5 * np.abs(ref) + 4e-7), name
+
+
+def test_cpout_matches_reference_summary(built, case4412, solved4412, tmp_path):
+    from cpanel_gb300 import io
+    g = case4412
+    m, A, B, r = solved4412
+    path = str(tmp_path / "4412.CPout")
+    io.write_cpout(path, [dict(V=float(g["V"]), alpha=float(g["alpha"]), beta=float(g["beta"]), mach=float(g["mach"]),
+                               CL=r["CL"], CDi=r["CDi"], Fbody=r["Fbody"], Fwind=r["Fwind"], CM=r["CM"])],
+                   geom_file="4412.tri", Sref=float(g["Sref"]), bref=float(g["bref"]), cref=float(g["cref"]),
+                   cg=tuple(float(x) for x in g["cg"]))
+    txt = open(path).read()
+    lines = txt.split("\n")
+    assert lines[0] == "-----------INPUTS-----------"
+    assert "              Geometry File -> 4412.tri" in lines
+    assert "             Reference Area -> 6 ft^2" in lines
+    assert "          Center of Gravity -> [0.25 0 0] ft" in lines
+    assert "                      Alpha -> 5 degrees" in lines
+    assert "                     Mach # -> 0.1 " in lines
+    assert "      Stability Derivatives -> OFF" in lines
+    assert "---Case #1---" in lines and "-----------RESULTS-----------" in lines
+    assert "\t\t1.000      0.100  5.000   0.000   " in lines
+    # the printed coefficients (5 decimals), as in the reference's 4412.CPout
+    cl, cdi = re.search(r"\t\t\tCL = (\S+)\tCDi = (\S+)", txt).groups()
+    assert abs(float(cl) - float(g["CL"])) < 1.01e-5 and abs(float(cdi) - float(g["CDi"])) < 1.01e-5
+    rows = [ln for ln in lines if ln.startswith("\t\t\t               ")]
+    body_row = [float(x) for x in rows[0].split()]
+    wind_row = [float(x) for x in rows[1].split()]
+    assert np.allclose(body_row, g["body_CN_CA_CY"], atol=1.01e-5)
+    assert np.allclose(wind_row, g["wind_CL_CD_CY"], atol=1.01e-5)
+    i = lines.index("\t\tCm (pitch)  Cl (roll)   Cn (yaw)    ")
+    assert np.allclose([float(x) for x in lines[i + 1].split()], g["Cm_Cl_Cn"], atol=1.01e-5)
+
+
+def test_case_label_follows_the_reference():
+    from cpanel_gb300 import io
+    assert io.case_label(1.0, 0.1, 5.0, 0.0) == "V1_Mach0.1_alpha5_beta0"
+    assert io.case_label(1.0, 0.1, -2.5, 0.5) == "V1_Mach0.1_alpha-2.5_beta0.5"
+
+
+def test_writers_reject_bad_input(built, tmp_path):
+    from cpanel_gb300 import CpgError, io
+    nodes = np.zeros((3, 3))
+    with pytest.raises(CpgError):  # node index outside the node list
+        io.write_surface_vtu(str(tmp_path / "x.vtu"), nodes, np.array([[0, 1, 3]]), *([np.zeros(1)] * 4)[:3],
+                             np.zeros((1, 3)), np.zeros(1), np.zeros((1, 3)), np.zeros((1, 3)))
+    with pytest.raises(CpgError):  # a directory that does not exist
+        io.write_cpout(str(tmp_path / "missing" / "x.CPout"), [])

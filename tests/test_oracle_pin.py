@@ -39,16 +39,6 @@ def test_wake_doublet_matches_body_doublet_off_panel():
         assert po.tri_dub_phi_inf(TRI, poi) == pytest.approx(dub, abs=1e-15)
 
 
-@pytest.fixture(scope="module")
-def solved4412(case4412):
-    g = case4412
-    m = po.Mesh(g["nodes"], g["tris"], g["ids"])
-    A, B = m.set_inf_coeff()
-    r = m.case(A, B, V=float(g["V"]), alpha=float(g["alpha"]), beta=float(g["beta"]), mach=float(g["mach"]),
-               Sref=float(g["Sref"]), bref=float(g["bref"]), cref=float(g["cref"]), cg=tuple(g["cg"]))
-    return m, A, B, r
-
-
 def test_4412_topology_counts(solved4412):
     m, A, B, r = solved4412
     assert m.n == 4824 and m.nw == 172

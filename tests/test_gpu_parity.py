@@ -7,6 +7,8 @@ Tolerances (from the path's specification):
   * mixed path: Cp max-abs error <= 1e-5 and CL relative error <= 1e-6 against the
     plain FP64 GPU path.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -136,6 +138,25 @@ def test_4412_reference_case_mixed_on_gpu(cg, case4412):
     assert case.run()
     assert abs(case.getCL() - float(gg["CL"])) <= 5.01e-6
     assert abs(case.getCD() - float(gg["CDi"])) <= 5.01e-6
+
+
+def test_case_write_files(cg, small, tmp_path):
+    """cpCase::writeFiles: the case directory with surfaceData.vtu and the .CPout beside it, read
+    back equal to the case's results at the printed precision."""
+    import re
+
+    from cpanel_gb300 import io
+    g, m, Ao, Bo, refs = small
+    case = cg.CpCase(g, 1.0, 5.0, 0.0, 0.1, precision="mixed", **refs)
+    assert case.run()
+    vtu, cpout = case.writeFiles(str(tmp_path), geom_file="wing.tri")
+    assert vtu.endswith(os.path.join("V1_Mach0.1_alpha5_beta0", "surfaceData.vtu"))
+    d = io.read_vtu_cells(vtu)
+    assert np.allclose(d["Cp"], case.getCp(), rtol=1e-5, atol=1e-6)
+    assert np.allclose(d["Doublet Strengths"], case.getMu(), rtol=1e-5, atol=1e-7)
+    assert d["connectivity"].reshape(-1, 3).max() < len(d["Position"])
+    cl = float(re.search(r"CL = (\S+)", open(cpout).read()).group(1))
+    assert abs(cl - case.getCL()) <= 5.01e-6
 
 
 def test_mixed_matches_plain_within_tolerance(cg, small):

@@ -226,6 +226,7 @@ class CpCase:
         self.refs = dict(Sref=Sref, bref=bref, cref=cref, cg=cg)
         self.precision = precision
         self.res = None
+        self.stab = None
 
     def run(self):
         self.res = solve_cases(self.geom, [self.flow], precision=self.precision, **self.refs)
@@ -255,6 +256,32 @@ class CpCase:
     def getVelocity(self):
         return self.res["vel"][0]
 
+    def stabilityDerivatives(self):
+        """cpCase::stabilityDerivatives (CPanel/cpCase.cpp:635-665): the base case and the two
+        0.5 deg sub-cases as three right-hand sides of one solve, forward differences per
+        radian.  Also runs the base case (its results as run() gives them).  Returns dict(
+        dF_dAlpha, dF_dBeta: (CD, CY, CL); dM_dAlpha, dM_dBeta: (roll, pitch, yaw))."""
+        g = self.geom
+        n = g.n
+        res = {name: np.zeros((1, n)) for name in ("mu", "sigma", "phi", "cp")}
+        res["vel"] = np.zeros((1, n, 3))
+        for name in ("CL", "CDi"):
+            res[name] = np.zeros(1)
+        for name in ("Fbody", "Fwind", "CM"):
+            res[name] = np.zeros((1, 3))
+        co = _lib.CaseOut(*[_p(res[f]) for f, _ in _lib.CaseOut._fields_])
+        st = _lib.Stability()
+        fl = _lib.Flow(*self.flow)
+        refs = _lib.Refs(self.refs["Sref"], self.refs["bref"], self.refs["cref"], (C.c_double * 3)(*self.refs["cg"]))
+        rc = g.ctx.L.cpg_stability_derivatives(g.h, C.byref(fl), C.byref(refs), _PREC[self.precision], C.byref(co),
+                                               C.byref(st))
+        if rc not in (0, 5):
+            g.ctx.check(rc, "stabilityDerivatives")
+        res["status"] = rc
+        self.res = res
+        self.stab = {k: np.array(getattr(st, k)[:]) for k in ("dF_dAlpha", "dF_dBeta", "dM_dAlpha", "dM_dBeta")}
+        return self.stab
+
     def writeFiles(self, directory=".", geom_file=""):
         """cpCase::writeFiles (CPanel/cpCase.cpp:667-709) for the body: the case directory
         V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, and
@@ -273,8 +300,10 @@ class CpCase:
         stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
         cpout = os.path.join(directory, stem + ".CPout")
         io.write_cpout(cpout, [dict(V=V, alpha=alpha, beta=beta, mach=mach, CL=self.getCL(), CDi=self.getCD(),
-                                    Fbody=self.getBodyForces(), Fwind=self.getWindForces(), CM=self.getMoment())],
-                       geom_file=geom_file, **self.refs)
+                                    Fbody=self.getBodyForces(), Fwind=self.getWindForces(), CM=self.getMoment(),
+                                    stability=self.stab)],
+                       geom_file=geom_file, flags=dict(stability_derivatives=self.stab is not None),
+                       **self.refs)
         return vtu, cpout
 
 

@@ -62,7 +62,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_geometry_create", "cpg_geometry_destroy", "cpg_geometry_info_get", "cpg_geometry_tables", "cpg_topology",
            "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
            "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read",
-           "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_release_spares",
+           "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_release_spares", "cpg_stability_derivatives",
            # cpanel_vp.h
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_ptree_set_precision", "cpg_set_particle_precision", "cpg_particles_velocity", "cpg_particles_stretch_diff",
@@ -149,9 +149,15 @@ class CpoutInputs(C.Structure):
                 ("unsteady", C.c_int)]
 
 
+class Stability(C.Structure):
+    _fields_ = [("dF_dAlpha", C.c_double * 3), ("dF_dBeta", C.c_double * 3), ("dM_dAlpha", C.c_double * 3),
+                ("dM_dBeta", C.c_double * 3)]
+
+
 class CpoutCase(C.Structure):
     _fields_ = [("flow", Flow), ("CL", C.c_double), ("CDi", C.c_double), ("Fbody", C.c_double * 3),
-                ("Fwind", C.c_double * 3), ("CM", C.c_double * 3)]
+                ("Fwind", C.c_double * 3), ("CM", C.c_double * 3), ("has_stability", C.c_int),
+                ("stability", Stability)]
 
 
 def load():
@@ -189,6 +195,8 @@ def load():
     L.cpg_prof_read.argtypes = [vp, C.POINTER(Prof)]
     L.cpg_measure_fp64_peak.argtypes = [vp, D]
     L.cpg_release_spares.argtypes = [vp]
+    L.cpg_stability_derivatives.argtypes = [vp, C.POINTER(Flow), C.POINTER(Refs), C.c_int, C.POINTER(CaseOut),
+                                            C.POINTER(Stability)]
     L.cpg_set_inf_coeff_noalloc.argtypes = [vp, C.c_int64, vp, vp, vp, C.c_int64, vp, vp, vp]
     L.cpg_ptree_build.argtypes = [vp, vp, vp, vp, C.c_int64, C.c_int64, C.c_double, C.POINTER(vp)]
     L.cpg_ptree_destroy.argtypes = [vp]

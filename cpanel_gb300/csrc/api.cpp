@@ -791,6 +791,64 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     return CPG_OK;
 }
 
+int cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_refs* refs, int precision,
+                              const cpg_case_out* base, cpg_stability* out) {
+    if (!g || !flow || !refs || !out) return CPG_E_INVALID;
+    const double delta = 0.5, dRad = delta * kPi / 180;  // CPanel/cpCase.cpp:637-638
+    cpg_flow fl[3] = {*flow, *flow, *flow};
+    fl[1].alpha += delta;
+    fl[2].beta += delta;
+    const int64_t n = g->H.n_body;
+    // per-panel outputs of all three cases where the caller wants the base case's
+    std::vector<double> mu, sigma, phi, vel, cp;
+    cpg_case_out o{};
+    if (base) {
+        auto want = [&](double* dst, std::vector<double>& v, size_t per) -> double* {
+            if (!dst) return nullptr;
+            v.assign(3 * per, 0.0);
+            return v.data();
+        };
+        o.mu = want(base->mu, mu, n);
+        o.sigma = want(base->sigma, sigma, n);
+        o.phi = want(base->phi, phi, n);
+        o.vel = want(base->vel, vel, 3 * n);
+        o.cp = want(base->cp, cp, n);
+    }
+    double CL[3], CDi[3], Fb[9], Fw[9], CM[9];
+    o.CL = CL;
+    o.CDi = CDi;
+    o.Fbody = Fb;
+    o.Fwind = Fw;
+    o.CM = CM;
+    const int rc = cpg_solve_cases(g, fl, 3, refs, precision, &o, nullptr);
+    if (rc != CPG_OK && rc != CPG_E_NOT_CONVERGED) return rc;
+    auto F = [&](int c, int q) { return q == 0 ? CDi[c] : (q == 2 ? CL[c] : Fw[3 * c + 1]); };
+    for (int q = 0; q < 3; q++) {
+        out->dF_dAlpha[q] = (F(1, q) - F(0, q)) / dRad;
+        out->dF_dBeta[q] = (F(2, q) - F(0, q)) / dRad;
+        out->dM_dAlpha[q] = (CM[3 + q] - CM[q]) / dRad;
+        out->dM_dBeta[q] = (CM[6 + q] - CM[q]) / dRad;
+    }
+    if (base) {
+        auto put = [&](double* dst, const std::vector<double>& v, size_t per) {
+            if (dst) std::copy(v.begin(), v.begin() + per, dst);
+        };
+        put(base->mu, mu, n);
+        put(base->sigma, sigma, n);
+        put(base->phi, phi, n);
+        put(base->vel, vel, 3 * n);
+        put(base->cp, cp, n);
+        if (base->CL) base->CL[0] = CL[0];
+        if (base->CDi) base->CDi[0] = CDi[0];
+        for (int q = 0; q < 3; q++) {
+            if (base->Fbody) base->Fbody[q] = Fb[q];
+            if (base->Fwind) base->Fwind[q] = Fw[q];
+            if (base->CM) base->CM[q] = CM[q];
+        }
+    }
+    return rc;
+}
+
 int cpg_panel_phi_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64_t m, double* src, double* dub) {
     if (!ctx || m < 0 || (m > 0 && (!verts || !poi || !src || !dub))) return fail(ctx, CPG_E_INVALID, "bad argument");
     CK(cpg::launch_phi_batch(verts, poi, m, src, dub, 0, ctx->stream), "panelPhiInf");

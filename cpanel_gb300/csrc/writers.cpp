@@ -91,6 +91,19 @@ void print_case(std::ostream& s, int number, const cpg_cpout_case& c) {
     s << "\t\t" << std::setw(12) << "Cm (pitch)" << std::setw(12) << "Cl (roll)" << std::setw(12) << "Cn (yaw)"
       << std::endl;
     s << "\t\t" << std::setw(12) << c.CM[1] << std::setw(12) << c.CM[0] << std::setw(12) << c.CM[2] << std::endl;
+    if (c.has_stability) {
+        const cpg_stability& d = c.stability;
+        s << "\n\t--Stability Derivatives--\n" << std::endl;
+        s << "\t\t" << std::setw(12) << "CL_alpha" << std::setw(12) << "CY_alpha" << std::setw(12) << "Cm_alpha"
+          << std::setw(12) << "Cl_alpha" << std::setw(12) << "Cn_alpha" << std::endl;
+        s << "\t\t" << std::setw(12) << d.dF_dAlpha[2] << std::setw(12) << d.dF_dAlpha[1] << std::setw(12)
+          << d.dM_dAlpha[1] << std::setw(12) << d.dM_dAlpha[0] << std::setw(12) << d.dM_dAlpha[2] << std::endl;
+        s << "\t\t" << std::setw(12) << "CL_beta" << std::setw(12) << "CY_beta" << std::setw(12) << "Cm_beta"
+          << std::setw(12) << "Cl_beta" << std::setw(12) << "Cn_beta" << std::endl;
+        s << "\t\t" << std::setw(12) << d.dF_dBeta[2] << std::setw(12) << d.dF_dBeta[1] << std::setw(12)
+          << d.dM_dBeta[1] << std::setw(12) << d.dM_dBeta[0] << std::setw(12) << d.dM_dBeta[2] << std::endl;
+        s << "\n\n" << std::endl;
+    }
 }
 
 // one DataArray of doubles: rows x cols, tab after every value, newline per row

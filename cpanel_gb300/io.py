@@ -27,7 +27,9 @@ def _unique(vals):
 
 def write_cpout(path, cases, geom_file="", Sref=1.0, bref=1.0, cref=1.0, cg=(0.0, 0.0, 0.0), flags=None):
     """cases: dicts with V, alpha, beta, mach, CL, CDi, Fbody (x, y, z), Fwind (x, y, z) and CM
-    (roll, pitch, yaw), as solve_cases / CpCase return them.  flags: the input flags to echo
+    (roll, pitch, yaw), as solve_cases / CpCase return them, and optionally "stability" (a dict
+    of dF_dAlpha, dF_dBeta, dM_dAlpha, dM_dBeta as CpCase.stabilityDerivatives returns it, printed
+    as the reference's stability block).  flags: the input flags to echo
     (subsonic_hom, surface_streamlines, stability_derivatives, write_inf_coeff,
     vortex_particles, accelerate_code, unsteady); all OFF by default."""
     L = _lib.load()
@@ -47,9 +49,12 @@ def write_cpout(path, cases, geom_file="", Sref=1.0, bref=1.0, cref=1.0, cg=(0.0
                                                                   "unsteady")])
     arr = (_lib.CpoutCase * max(1, len(cases)))()
     for i, c in enumerate(cases):
+        st = c.get("stability")
+        stab = _lib.Stability(*[(C.c_double * 3)(*st[k]) for k in ("dF_dAlpha", "dF_dBeta", "dM_dAlpha",
+                                                                     "dM_dBeta")]) if st else _lib.Stability()
         arr[i] = _lib.CpoutCase(_lib.Flow(c["V"], c["alpha"], c["beta"], c["mach"]), c["CL"], c["CDi"],
                                 (C.c_double * 3)(*c["Fbody"]), (C.c_double * 3)(*c["Fwind"]),
-                                (C.c_double * 3)(*c["CM"]))
+                                (C.c_double * 3)(*c["CM"]), 1 if st else 0, stab)
     rc = L.cpg_write_cpout(os.fsencode(path), C.byref(inp), arr, len(cases))
     if rc != 0:
         raise CpgError(rc, "cpg_write_cpout(%s)" % path)

@@ -12,6 +12,7 @@
  *   cpg_solve_cases       cpCase::run minus file output, CPanel/cpCase.cpp:31-139
  *                         (setSourceStrengths :174-183, solveMatrixEq :185-214,
  *                          compVelocity :342-365, trefftzPlaneAnalysis :541-552)
+ *   cpg_stability_derivatives  cpCase::stabilityDerivatives, CPanel/cpCase.cpp:635-665
  *   cpg_panel_phi_inf     bodyPanel::panelPhiInf, CPanel/bodyPanel.cpp:132-190
  *   cpg_dub_phi_inf       panel::dubPhiInf, CPanel/panel.cpp:208-252
  *   cpg_panel_v_inf       bodyPanel::panelVInf, CPanel/bodyPanel.cpp:305-348
@@ -154,6 +155,20 @@ int  cpg_set_inf_coeff_noalloc(const double* body_verts, int64_t n, const double
  * Assembles first if the geometry holds no matrix of that precision. */
 int  cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_refs* refs, int precision,
                      const cpg_case_out* out, cpg_solve_stats* stats);
+
+/* ---- stability derivatives (cpCase::stabilityDerivatives, CPanel/cpCase.cpp:635-665) ----
+ * The base case and the reference's two sub-cases (alpha + 0.5 deg, beta + 0.5 deg) solved as
+ * three right-hand sides of one cpg_solve_cases call, then the reference's forward differences
+ * over 0.5 deg: F = (CDi, CY wind, CL) with the Trefftz-plane CL and CDi, M = (roll, pitch, yaw).
+ * base (may be null): the base case's outputs as cpg_solve_cases would give them for k = 1.
+ * Unlike the reference, the base case's panel state is what base receives (the reference's
+ * sub-cases overwrite the panel state before its files are written). */
+typedef struct {
+    double dF_dAlpha[3], dF_dBeta[3];  /* per radian: (CD, CY, CL)    */
+    double dM_dAlpha[3], dM_dBeta[3];  /* per radian: (roll, pitch, yaw) */
+} cpg_stability;
+int  cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_refs* refs, int precision,
+                               const cpg_case_out* base, cpg_stability* out);
 
 /* ---- single-evaluation influence operators on DEVICE arrays (batched) ----
  * verts m x 9 (three vertices), poi m x 3; outputs m (phi) or m x 3 (velocity). */

@@ -46,6 +46,8 @@ typedef struct {
     double Fbody[3];  /* body-axis force coefficients (x, y, z): printed CN, CA, CY     */
     double Fwind[3];  /* wind-axis force coefficients (x, y, z): printed CL, CD, CY     */
     double CM[3];     /* moment coefficients (roll, pitch, yaw): printed Cm, Cl, Cn     */
+    int has_stability;          /* non-zero: print the stability derivatives block       */
+    cpg_stability stability;    /* as cpg_stability_derivatives gives them               */
 } cpg_cpout_case;
 
 /* Write the .CPout summary of n_cases cases. */

@@ -8,7 +8,11 @@ Run in a container where the CPanel reference tree is mounted (default path
                    (doublet, source, potential, velocity, Cp, centroid; 6 significant
                    digits as printed by the reference) and the .CPout summary numbers.
 
+  case4412AR6.npz -- Connor Cases/4412AR6 (Stability_Derivatives 1 in its .CPin): the mesh and the
+                   .CPout numbers, the ten stability derivatives included (5 decimals).
+
 The generated files are small and committed; tests never read the reference tree.
+Usage: python make_golden.py [4412 | 4412AR6]  (default: both).
 """
 import os
 import re
@@ -56,7 +60,39 @@ def read_cpout(path):
     return dict(CL=float(cl), CDi=float(cdi), body_CN_CA_CY=body, wind_CL_CD_CY=wind, Cm_Cl_Cn=mom)
 
 
+def read_stability(path):
+    """The two rows under CL_alpha ... and CL_beta ...: (CL, CY, Cm, Cl, Cn) per row."""
+    txt = open(path).read()
+    rows = []
+    for head in ("CL_alpha", "CL_beta"):
+        m = re.search(head + r"[^\n]*\n\s*([-\d.]+)\s+([-\d.]+)\s+([-\d.]+)\s+([-\d.]+)\s+([-\d.]+)", txt)
+        rows.append([float(v) for v in m.groups()])
+    return rows
+
+
+def main_4412ar6():
+    case = os.path.join(REF, "Connor Cases", "4412AR6")
+    if not os.path.isdir(case):
+        sys.exit("reference case folder not found: %s" % case)
+    nodes, tris, ids = read_tri(os.path.join(case, "4412AR6.tri"))
+    cp = read_cpout(os.path.join(case, "4412AR6.CPout"))
+    da, db = read_stability(os.path.join(case, "4412AR6.CPout"))
+    np.savez_compressed(
+        os.path.join(HERE, "case4412AR6.npz"),
+        nodes=nodes, tris=tris.astype(np.int32), ids=ids,
+        CL=cp["CL"], CDi=cp["CDi"], body_CN_CA_CY=np.array(cp["body_CN_CA_CY"]),
+        wind_CL_CD_CY=np.array(cp["wind_CL_CD_CY"]), Cm_Cl_Cn=np.array(cp["Cm_Cl_Cn"]),
+        d_alpha_CL_CY_Cm_Cl_Cn=np.array(da), d_beta_CL_CY_Cm_Cl_Cn=np.array(db),
+        V=1.0, alpha=5.0, beta=0.0, mach=0.1, Sref=6.0, bref=6.0, cref=1.0, cg=np.array([0.25, 0.0, 0.0]))
+    print("wrote case4412AR6.npz", nodes.shape, tris.shape, cp, da, db)
+
+
 def main():
+    which = sys.argv[1:] or ["4412", "4412AR6"]
+    if "4412AR6" in which:
+        main_4412ar6()
+    if "4412" not in which:
+        return
     case = os.path.join(REF, "Connor Cases", "4412")
     if not os.path.isdir(case):
         sys.exit("reference case folder not found: %s" % case)

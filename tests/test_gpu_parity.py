@@ -140,6 +140,21 @@ def test_4412_reference_case_mixed_on_gpu(cg, case4412):
     assert abs(case.getCD() - float(gg["CDi"])) <= 5.01e-6
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_4412AR6_stability_derivatives_on_gpu(cg, case4412ar6, precision):
+    """cpCase::stabilityDerivatives on the GPU for the reference's 4412AR6 case: the ten printed
+    derivatives of its .CPout (5 decimals), the base and both sub-cases solved together."""
+    from conftest import printed_stability
+    g = case4412ar6
+    geo = cg.Geometry(g["nodes"], g["tris"].astype(np.int64), g["ids"])
+    case = cg.CpCase(geo, 1.0, 5.0, 0.0, 0.1, Sref=6.0, bref=6.0, cref=1.0, cg=(0.25, 0.0, 0.0), precision=precision)
+    st = case.stabilityDerivatives()
+    assert abs(case.getCL() - float(g["CL"])) <= 5.01e-6
+    da, db = printed_stability(st)
+    assert np.all(np.abs(da - g["d_alpha_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), da
+    assert np.all(np.abs(db - g["d_beta_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), db
+
+
 def test_case_write_files(cg, small, tmp_path):
     """cpCase::writeFiles: the case directory with surfaceData.vtu and the .CPout beside it, read
     back equal to the case's results at the printed precision."""

@@ -88,3 +88,23 @@ def test_writers_reject_bad_input(built, tmp_path):
                              np.zeros((1, 3)), np.zeros(1), np.zeros((1, 3)), np.zeros((1, 3)))
     with pytest.raises(CpgError):  # a directory that does not exist
         io.write_cpout(str(tmp_path / "missing" / "x.CPout"), [])
+
+
+def test_cpout_stability_block_matches_reference(built, case4412ar6, solved4412ar6, tmp_path):
+    """The stability-derivative block of the reference's 4412AR6.CPout, from the oracle's
+    derivatives through the writer."""
+    from cpanel_gb300 import io
+    g = case4412ar6
+    r0, st = solved4412ar6
+    path = str(tmp_path / "4412AR6.CPout")
+    io.write_cpout(path, [dict(V=1.0, alpha=5.0, beta=0.0, mach=0.1, CL=r0["CL"], CDi=r0["CDi"], Fbody=r0["Fbody"],
+                               Fwind=r0["Fwind"], CM=r0["CM"], stability=st)],
+                   geom_file="4412AR6.tri", Sref=6.0, bref=6.0, cref=1.0, cg=(0.25, 0.0, 0.0),
+                   flags=dict(stability_derivatives=True))
+    lines = open(path).read().split("\n")
+    assert "      Stability Derivatives -> ON" in lines and "\t--Stability Derivatives--" in lines
+    i = lines.index("\t\tCL_alpha    CY_alpha    Cm_alpha    Cl_alpha    Cn_alpha    ")
+    assert lines[i + 2] == "\t\tCL_beta     CY_beta     Cm_beta     Cl_beta     Cn_beta     "
+    assert np.allclose([float(x) for x in lines[i + 1].split()], g["d_alpha_CL_CY_Cm_Cl_Cn"], atol=1.01e-5)
+    assert np.allclose([float(x) for x in lines[i + 3].split()], g["d_beta_CL_CY_Cm_Cl_Cn"], atol=1.01e-5)
+

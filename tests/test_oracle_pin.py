@@ -90,3 +90,20 @@ def test_doublet_rows_of_closed_body_sum_to_minus_one(case4412):
     m = po.Mesh(g["nodes"], g["tris"][body], g["ids"][body])
     A, _ = m.set_inf_coeff()
     assert np.abs(A.sum(axis=1) + 1).max() < 1e-3
+
+
+def test_4412AR6_stability_derivatives_match_reference(case4412ar6, solved4412ar6):
+    """The reference's 4412AR6 case (Stability_Derivatives 1): CL, CDi, forces, moments and the
+    ten stability derivatives of its .CPout, 5 printed decimals each."""
+    from conftest import printed_stability
+    g = case4412ar6
+    r0, st = solved4412ar6
+    assert abs(r0["CL"] - float(g["CL"])) <= 5.01e-6 and abs(r0["CDi"] - float(g["CDi"])) <= 5.01e-6
+    CN, CA, CY = g["body_CN_CA_CY"]
+    assert abs(r0["Fbody"][2] - CN) <= 5.01e-6 and abs(r0["Fbody"][0] - CA) <= 5.01e-6
+    Cm, Cl, Cn = g["Cm_Cl_Cn"]
+    assert abs(r0["CM"][1] - Cm) <= 5.01e-6 and abs(r0["CM"][0] - Cl) <= 5.01e-6 and abs(r0["CM"][2] - Cn) <= 5.01e-6
+    da, db = printed_stability(st)
+    assert np.all(np.abs(da - g["d_alpha_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), da
+    assert np.all(np.abs(db - g["d_beta_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), db
+

@@ -227,6 +227,7 @@ class CpCase:
         self.precision = precision
         self.res = None
         self.stab = None
+        self.survey = None
 
     def run(self):
         self.res = solve_cases(self.geom, [self.flow], precision=self.precision, **self.refs)
@@ -282,6 +283,34 @@ class CpCase:
         self.stab = {k: np.array(getattr(st, k)[:]) for k in ("dF_dAlpha", "dF_dBeta", "dM_dAlpha", "dM_dBeta")}
         return self.stab
 
+    def velocityAtPoints(self, pts):
+        """cpCase::velocityAtPoint (CPanel/cpCase.cpp:1007-1021) for many points: the velocity all
+        body and wake panels induce (V_inf not included), for this case's strengths."""
+        g = self.geom
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        vel = np.zeros_like(pts)
+        sig = np.ascontiguousarray(self.res["sigma"][0])
+        mu = np.ascontiguousarray(self.res["mu"][0])
+        g.ctx.check(g.ctx.L.cpg_volume_velocity(g.h, _p(sig), _p(mu), _p(pts), len(pts), _p(vel)), "velocityAtPoints")
+        return vel
+
+    def vinf(self):
+        """V_inf in body axes (cpCase::windToBody, CPanel/cpCase.cpp:142-165)."""
+        V, alpha, beta, _ = self.flow
+        a, b = np.radians(alpha), np.radians(beta)
+        return V * np.array([np.cos(a) * np.cos(b), -np.sin(b), np.sin(a) * np.cos(b)])
+
+    def volumeSurvey(self, bounds, res):
+        """cpCase::createVolMesh + populateVolMesh (CPanel/cpCase.cpp:1024-1122): velocity and Cp at
+        the cell centres of a structured grid.  Cp is the reference's (|V| / V_inf)^2, as written
+        there (not 1 - (|V| / V_inf)^2).  Returns dict(points, cells, centers, velocity, cp)."""
+        from . import io
+        pts, cells, centers = io.volume_grid(bounds, res)
+        vel = self.velocityAtPoints(centers) + self.vinf()
+        cp = (np.linalg.norm(vel, axis=1) / self.flow[0]) ** 2
+        self.survey = dict(points=pts, cells=cells, centers=centers, velocity=vel, cp=cp)
+        return self.survey
+
     def writeFiles(self, directory=".", geom_file=""):
         """cpCase::writeFiles (CPanel/cpCase.cpp:667-709) for the body: the case directory
         V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, and
@@ -297,6 +326,10 @@ class CpCase:
         vtu = os.path.join(sub, "surfaceData.vtu")
         io.write_surface_vtu(vtu, self.geom._nodes, tris, self.res["mu"][0], self.res["sigma"][0],
                              self.res["phi"][0], self.res["vel"][0], self.res["cp"][0], body[:, 3:6], body[:, 0:3])
+        if self.survey is not None:
+            sv = self.survey
+            io.write_volume_vtu(os.path.join(sub, "volumeMesh.vtu"), sv["points"], sv["cells"], sv["velocity"],
+                                sv["cp"])
         stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
         cpout = os.path.join(directory, stem + ".CPout")
         io.write_cpout(cpout, [dict(V=V, alpha=alpha, beta=beta, mach=mach, CL=self.getCL(), CDi=self.getCD(),

@@ -791,6 +791,50 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     return CPG_OK;
 }
 
+int cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu, const double* pts, int64_t m,
+                        double* vel) {
+    if (!g || !sigma || !mu || (m > 0 && (!pts || !vel)) || m < 0) return CPG_E_INVALID;
+    if (m == 0) return CPG_OK;
+    cpg_ctx* ctx = g->ctx;
+    ProfInstall pi(ctx);
+    cudaStream_t s = ctx->stream;
+    const cpg::HostMesh& H = g->H;
+    const int64_t n = H.n_body, nw = H.n_wake;
+    // wake doublets implied by the assembly's wake columns (CPanel/wakePanel.cpp:48-100):
+    // mu_w = (1 - t)(mu_up1 - mu_lo1) + t (mu_up2 - mu_lo2)
+    std::vector<double> wmu(std::max<int64_t>(1, nw), 0.0);
+    for (int64_t j = 0; j < nw; j++) {
+        const int32_t* ix = &H.widx[4 * j];
+        const double t = H.wcoef[j];
+        wmu[j] = (1 - t) * (mu[ix[0]] - mu[ix[1]]) + t * (mu[ix[2]] - mu[ix[3]]);
+    }
+    const size_t R = 24;  // doubles per packed panel record
+    DevBuf rec, sm, pv, vv;
+    CK(rec.ensure(sizeof(double) * R * (size_t)(n + nw)), "alloc records");
+    CK(cudaMemcpyAsync(rec.p, g->rec.p, sizeof(double) * R * n, cudaMemcpyDeviceToDevice, s), "records");
+    if (nw > 0)
+        CK(cudaMemcpyAsync(rec.as<double>() + R * n, g->wrec.p, sizeof(double) * R * nw, cudaMemcpyDeviceToDevice, s),
+           "wake records");
+    CK(sm.ensure(sizeof(double) * (2 * n + nw)), "alloc strengths");
+    CK(cudaMemcpyAsync(sm.as<double>(), sigma, sizeof(double) * n, cudaMemcpyHostToDevice, s), "sigma");
+    CK(cudaMemcpyAsync(sm.as<double>() + n, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s), "mu");
+    if (nw > 0)
+        CK(cudaMemcpyAsync(sm.as<double>() + 2 * n, wmu.data(), sizeof(double) * nw, cudaMemcpyHostToDevice, s),
+           "wake mu");
+    CK(pv.ensure(sizeof(double) * 3 * m), "alloc points");
+    CK(vv.ensure(sizeof(double) * 3 * m), "alloc velocities");
+    CK(cudaMemcpyAsync(pv.p, pts, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, s), "points");
+    {
+        cpg::ProfScope ps(cpg::Prof::POST, s);
+        CK(cpg::launch_panels_velocity_rec(rec.as<double>(), sm.as<double>(), sm.as<double>() + n, n,
+                                           sm.as<double>() + 2 * n, nw, pv.as<double>(), m, vv.as<double>(), s),
+           "panel velocities");
+    }
+    CK(cudaMemcpyAsync(vel, vv.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, s), "velocities");
+    CK(cudaStreamSynchronize(s), "volume velocity");
+    return CPG_OK;
+}
+
 int cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_refs* refs, int precision,
                               const cpg_case_out* base, cpg_stability* out) {
     if (!g || !flow || !refs || !out) return CPG_E_INVALID;

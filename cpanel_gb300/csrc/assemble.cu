@@ -609,6 +609,13 @@ cudaError_t launch_panels_velocity(const double* body_verts, const double* sigma
     return cudaGetLastError();
 }
 
+cudaError_t launch_panels_velocity_rec(const double* rec, const double* sigma, const double* mu, int64_t nb,
+                                       const double* wmu, int64_t nw, const double* pts, int64_t m, double* vel,
+                                       cudaStream_t s) {
+    if (m > 0) k_panels_velocity<<<(unsigned)((m + PV_T - 1) / PV_T), PV_T, 0, s>>>(rec, sigma, mu, nb, wmu, nw, pts, m, vel);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wrec, const int32_t* widx,
                                  const double* wcoef, int64_t nw, double* A, double* B,
                                  unsigned long long* near_count, cudaStream_t s) {

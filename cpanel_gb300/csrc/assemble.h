@@ -91,6 +91,11 @@ int assemble_mixed_grouped_max_blocks_per_sm();
 // doubles of rb_part that launch_assemble_mixed needs: the per-chunk partial sums, and
 // afterwards the wake influence table (nw x n)
 int64_t mixed_rb_part_doubles(int64_t n, int64_t nw);
+// Panel-induced velocity (bodyPanel::panelV + wakePanel::panelV) at m points from packed
+// records: nb body records followed by nw wake records at rec (R_STRIDE doubles each).
+cudaError_t launch_panels_velocity_rec(const double* rec, const double* sigma, const double* mu, int64_t nb,
+                                       const double* wmu, int64_t nw, const double* pts, int64_t m, double* vel,
+                                       cudaStream_t s);
 cudaError_t launch_phi_batch(const double* verts, const double* poi, int64_t m, double* src, double* dub, int mode,
                              cudaStream_t s);
 cudaError_t launch_v_batch(const double* verts, const double* poi, int64_t m, double* vs, double* vd, cudaStream_t s);

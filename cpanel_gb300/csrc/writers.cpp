@@ -189,4 +189,46 @@ int cpg_write_surface_vtu(const char* path, const double* nodes, int64_t nn, con
     }
 }
 
+int cpg_write_volume_vtu(const char* path, const double* pts, int64_t np, const int64_t* cells, int64_t nc,
+                         const double* vel, const double* cp) {
+    if (!path || !pts || !cells || np <= 0 || nc <= 0 || !vel || !cp) return CPG_E_INVALID;
+    for (int64_t i = 0; i < 8 * nc; i++)
+        if (cells[i] < 0 || cells[i] >= np) return CPG_E_INVALID;
+    try {
+        std::ofstream f(path);
+        if (!f) return CPG_E_INVALID;
+        f << "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+        f << "\t<UnstructuredGrid>\n";
+        f << "\t\t<Piece NumberOfPoints=\"" << np << "\" NumberOfCells=\"" << nc << "\">\n";
+        f << "\t\t\t<CellData Scalars=\"scalars\">\n";
+        print_doubles(f, "Velocity", vel, nc, 3);
+        print_doubles(f, "Cp", cp, nc, 1);
+        f << "\t\t\t</CellData>\n";
+        f << "\t\t\t<Points>\n";
+        print_doubles(f, "Position", pts, np, 3);
+        f << "\t\t\t</Points>\n";
+        f << "\t\t\t<Cells>\n";
+        f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n";
+        for (int64_t i = 0; i < nc; i++) {
+            for (int q = 0; q < 8; q++) f << cells[8 * i + q] << "\t";
+            f << "\n";
+        }
+        f << "\t\t\t\t</DataArray>\n";
+        f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n";
+        for (int64_t i = 0; i < nc; i++) f << (i + 1) * 8 << "\t\n";
+        f << "\t\t\t\t</DataArray>\n";
+        f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"types\" Format=\"ascii\">\n";
+        for (int64_t i = 0; i < nc; i++) f << 11 << "\t\n";  // VTK_VOXEL
+        f << "\t\t\t\t</DataArray>\n";
+        f << "\t\t\t</Cells>\n";
+        f << "\t\t</Piece>\n";
+        f << "\t</UnstructuredGrid>\n";
+        f << "</VTKFile>\n";
+        f.close();
+        return f ? CPG_OK : CPG_E_INVALID;
+    } catch (const std::bad_alloc&) {
+        return CPG_E_OOM;
+    }
+}
+
 }  // extern "C"

@@ -73,6 +73,36 @@ def write_surface_vtu(path, nodes, tris, mu, sigma, phi, vel, cp, bez, centers):
         raise CpgError(rc, "cpg_write_surface_vtu(%s)" % path)
 
 
+def volume_grid(bounds, res):
+    """cpCase::createVolMesh (CPanel/cpCase.cpp:1024-1097): the points of an (nX, nY, nZ)-cell grid
+    over bounds (x0, xf, y0, yf, z0, zf), x fastest; the cells as 8 point indices (VTK voxel
+    order), looping x, then y, then z innermost as the reference does; the cell centres.
+    Returns (points, cells, centers)."""
+    x0, xf, y0, yf, z0, zf = [float(b) for b in bounds]
+    nX, nY, nZ = [int(r) for r in res]
+    hx, hy, hz = (xf - x0) / nX, (yf - y0) / nY, (zf - z0) / nZ
+    nXp, nYp, nZp = nX + 1, nY + 1, nZ + 1
+    k, j, i = np.meshgrid(np.arange(nZp), np.arange(nYp), np.arange(nXp), indexing="ij")
+    pts = np.stack([x0 + hx * i.ravel(), y0 + hy * j.ravel(), z0 + hz * k.ravel()], axis=1)
+    I, J, K = np.meshgrid(np.arange(nX), np.arange(nY), np.arange(nZ), indexing="ij")
+    I, J, K = I.ravel(), J.ravel(), K.ravel()
+    base = K * (nXp * nYp) + J * nXp + I
+    cells = np.stack([base, base + 1, base + nXp, base + nXp + 1, base + nXp * nYp, base + nXp * nYp + 1,
+                      base + nXp * nYp + nXp, base + nXp * nYp + nXp + 1], axis=1).astype(np.int64)
+    centers = pts[cells].mean(axis=1)
+    return pts, cells, centers
+
+
+def write_volume_vtu(path, points, cells, vel, cp):
+    """volumeMesh.vtu (cpCase::writeVolMeshData): cell data Velocity and Cp on VTK voxels."""
+    L = _lib.load()
+    c = np.ascontiguousarray(cells, dtype=np.int64)
+    (p, pp), (v, vp), (q, qp) = _d(points), _d(vel), _d(cp)
+    rc = L.cpg_write_volume_vtu(os.fsencode(path), pp, len(p), c.ctypes.data_as(_lib.I64), len(c), vp, qp)
+    if rc != 0:
+        raise CpgError(rc, "cpg_write_volume_vtu(%s)" % path)
+
+
 def read_vtu_cells(path):
     """The cell data arrays, points and connectivity of an ASCII .vtu file (as written by CPanel
     or by write_surface_vtu): {name: array}."""

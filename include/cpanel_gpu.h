@@ -13,6 +13,7 @@
  *                         (setSourceStrengths :174-183, solveMatrixEq :185-214,
  *                          compVelocity :342-365, trefftzPlaneAnalysis :541-552)
  *   cpg_stability_derivatives  cpCase::stabilityDerivatives, CPanel/cpCase.cpp:635-665
+ *   cpg_volume_velocity   cpCase::velocityAtPoint, CPanel/cpCase.cpp:1007-1021
  *   cpg_panel_phi_inf     bodyPanel::panelPhiInf, CPanel/bodyPanel.cpp:132-190
  *   cpg_dub_phi_inf       panel::dubPhiInf, CPanel/panel.cpp:208-252
  *   cpg_panel_v_inf       bodyPanel::panelVInf, CPanel/bodyPanel.cpp:305-348
@@ -169,6 +170,14 @@ typedef struct {
 } cpg_stability;
 int  cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_refs* refs, int precision,
                                const cpg_case_out* base, cpg_stability* out);
+
+/* ---- velocity anywhere in the flow (cpCase::velocityAtPoint, CPanel/cpCase.cpp:1007-1021) ----
+ * The velocity that all body and wake panels of g induce at m points (host arrays pts m x 3 ->
+ * vel m x 3), for one case's source and doublet strengths (host arrays sigma, mu: n_body).  The
+ * wake doublets follow from mu through the trailing-edge interpolation of the assembly.  V_inf
+ * is not included (the reference adds it in populateVolMesh, CPanel/cpCase.cpp:1105-1122). */
+int  cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu, const double* pts, int64_t m,
+                         double* vel);
 
 /* ---- single-evaluation influence operators on DEVICE arrays (batched) ----
  * verts m x 9 (three vertices), poi m x 3; outputs m (phi) or m x 3 (velocity). */

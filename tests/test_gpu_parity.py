@@ -155,6 +155,27 @@ def test_4412AR6_stability_derivatives_on_gpu(cg, case4412ar6, precision):
     assert np.all(np.abs(db - g["d_beta_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), db
 
 
+def test_volume_survey_matches_oracle(cg, small, tmp_path):
+    """cpCase::velocityAtPoint over a volume grid around the wing (plain path): the GPU's panel
+    velocities with the wake doublets the library derives, against the oracle's own chain (its
+    solve, its wakePanel::setMu, its panelV sums) plus V_inf."""
+    from cpanel_gb300 import io
+    from oracle import pyoracle as po
+    g, m, Ao, Bo, refs = small
+    case = cg.CpCase(g, 1.0, 5.0, 0.0, 0.1, precision="fp64", **refs)
+    assert case.run()
+    sv = case.volumeSurvey((-0.5, 1.5, -1.0, 1.0, -0.5, 0.5), (8, 6, 5))
+    o = m.case(Ao, Bo, alpha=5.0, mach=0.1, **refs)
+    vo = po.panels_velocity(m.body_verts(), o["sigma"], o["mu"], m.wake_verts(), o["wake_mu"], sv["centers"])
+    vo = vo + case.vinf()
+    scale = np.abs(vo).max()
+    assert np.abs(sv["velocity"] - vo).max() <= 1e-9 * scale
+    assert np.allclose(sv["cp"], (np.linalg.norm(vo, axis=1) / 1.0) ** 2, rtol=1e-8)
+    vtu, cpout = case.writeFiles(str(tmp_path))
+    d = io.read_vtu_cells(os.path.join(os.path.dirname(vtu), "volumeMesh.vtu"))
+    assert np.allclose(d["Cp"], sv["cp"], rtol=1e-5)
+
+
 def test_case_write_files(cg, small, tmp_path):
     """cpCase::writeFiles: the case directory with surfaceData.vtu and the .CPout beside it, read
     back equal to the case's results at the printed precision."""

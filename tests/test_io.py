@@ -108,3 +108,38 @@ def test_cpout_stability_block_matches_reference(built, case4412ar6, solved4412a
     assert np.allclose([float(x) for x in lines[i + 1].split()], g["d_alpha_CL_CY_Cm_Cl_Cn"], atol=1.01e-5)
     assert np.allclose([float(x) for x in lines[i + 3].split()], g["d_beta_CL_CY_Cm_Cl_Cn"], atol=1.01e-5)
 
+
+def test_volume_grid_follows_create_vol_mesh():
+    """The grid of cpCase::createVolMesh (CPanel/cpCase.cpp:1024-1097), restated here as its
+    loops, against the vectorised io.volume_grid."""
+    from cpanel_gb300 import io
+    bounds, (nX, nY, nZ) = (-1.0, 2.0, 0.5, 1.5, -0.25, 0.75), (3, 2, 4)
+    pts, cells, centers = io.volume_grid(bounds, (nX, nY, nZ))
+    x0, xf, y0, yf, z0, zf = bounds
+    hx, hy, hz = (xf - x0) / nX, (yf - y0) / nY, (zf - z0) / nZ
+    nXp, nYp, nZp = nX + 1, nY + 1, nZ + 1
+    ref_pts = [(x0 + hx * i, y0 + hy * j, z0 + hz * k) for k in range(nZp) for j in range(nYp) for i in range(nXp)]
+    ref_cells = []
+    for i in range(nX):
+        for j in range(nY):
+            for k in range(nZ):
+                b = k * nXp * nYp + j * nXp + i
+                t = (k + 1) * nXp * nYp + j * nXp + i
+                ref_cells.append([b, b + 1, b + nXp, b + nXp + 1, t, t + 1, t + nXp, t + nXp + 1])
+    assert np.allclose(pts, ref_pts, rtol=0, atol=1e-15)
+    assert np.array_equal(cells, ref_cells)
+    assert np.allclose(centers, np.array(ref_pts)[np.array(ref_cells)].mean(axis=1), rtol=0, atol=1e-15)
+
+
+def test_volume_vtu_round_trip(built, tmp_path):
+    from cpanel_gb300 import io
+    pts, cells, centers = io.volume_grid((0, 1, 0, 1, 0, 1), (2, 2, 2))
+    vel = np.arange(3 * len(cells), dtype=float).reshape(-1, 3) / 7
+    cp = np.linspace(0.5, 1.5, len(cells))
+    path = str(tmp_path / "volumeMesh.vtu")
+    io.write_volume_vtu(path, pts, cells, vel, cp)
+    d = io.read_vtu_cells(path)
+    assert np.allclose(d["Velocity"], vel, rtol=1e-5) and np.allclose(d["Cp"], cp, rtol=1e-5)
+    assert np.array_equal(d["connectivity"].reshape(-1, 8), cells) and np.all(d["types"] == 11)
+    assert np.allclose(d["Position"], pts)
+

@@ -810,6 +810,12 @@ int cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu, 
     }
     const size_t R = 24;  // doubles per packed panel record
     DevBuf rec, sm, pv, vv;
+    struct Release {  // on every return: these buffers live for this call only
+        DevBuf* b[4];
+        ~Release() {
+            for (DevBuf* x : b) x->release();
+        }
+    } rel{{&rec, &sm, &pv, &vv}};
     CK(rec.ensure(sizeof(double) * R * (size_t)(n + nw)), "alloc records");
     CK(cudaMemcpyAsync(rec.p, g->rec.p, sizeof(double) * R * n, cudaMemcpyDeviceToDevice, s), "records");
     if (nw > 0)

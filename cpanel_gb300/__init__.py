@@ -312,10 +312,11 @@ class CpCase:
         return self.survey
 
     def writeFiles(self, directory=".", geom_file=""):
-        """cpCase::writeFiles (CPanel/cpCase.cpp:667-709) for the body: the case directory
-        V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, and
-        caseMgr::writeSummary's .CPout (CPanel/CPanelMgr.cpp:89-116) beside it.  Returns the
-        paths written."""
+        """cpCase::writeFiles (CPanel/cpCase.cpp:667-709): the case directory
+        V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, wakeData.vtu (when
+        the mesh has wake panels) and volumeMesh.vtu (after volumeSurvey), and
+        caseMgr::writeSummary's .CPout (CPanel/CPanelMgr.cpp:89-116) beside it.  Returns the paths
+        of surfaceData.vtu and the .CPout."""
         from . import io
         V, alpha, beta, mach = self.flow
         sub = os.path.join(directory, io.case_label(V, mach, alpha, beta))
@@ -326,6 +327,10 @@ class CpCase:
         vtu = os.path.join(sub, "surfaceData.vtu")
         io.write_surface_vtu(vtu, self.geom._nodes, tris, self.res["mu"][0], self.res["sigma"][0],
                              self.res["phi"][0], self.res["vel"][0], self.res["cp"][0], body[:, 3:6], body[:, 0:3])
+        if self.geom.nw > 0:
+            wt = io.wake_tris(self.geom._nodes, self.geom._tris, self.geom._ids)
+            wmu, wphi = io.wake_fields(self.res["mu"][0], t["idx4"], t["coef"], t["wake"][:, 0:3], self.vinf())
+            io.write_wake_vtu(os.path.join(sub, "wakeData.vtu"), self.geom._nodes, self.geom._tris[wt] - 1, wmu, wphi)
         if self.survey is not None:
             sv = self.survey
             io.write_volume_vtu(os.path.join(sub, "volumeMesh.vtu"), sv["points"], sv["cells"], sv["velocity"],

@@ -63,7 +63,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
            "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read",
            "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_release_spares", "cpg_stability_derivatives",
-           "cpg_volume_velocity",
+           "cpg_volume_velocity", "cpg_topology_wake_tris",
            # cpanel_vp.h
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_ptree_set_precision", "cpg_set_particle_precision", "cpg_particles_velocity", "cpg_particles_stretch_diff",
@@ -77,7 +77,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_group_default_shape", "cpg_set_inf_coeff_grouped", "cpg_group_schedule", "cpg_batch_solve",
            "cpg_lu_factor_grouped",
            # cpanel_io.h
-           "cpg_write_cpout", "cpg_write_surface_vtu", "cpg_write_volume_vtu"]
+           "cpg_write_cpout", "cpg_write_surface_vtu", "cpg_write_volume_vtu", "cpg_write_wake_vtu"]
 
 TUNE_OFF, TUNE_AUTO, TUNE_FORCE = 0, 1, 2
 
@@ -248,5 +248,7 @@ def load():
     L.cpg_write_surface_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D, D, D, D, D, D]
     L.cpg_write_volume_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D]
     L.cpg_volume_velocity.argtypes = [vp, D, D, D, C.c_int64, D]
+    L.cpg_topology_wake_tris.argtypes = [D, C.c_int64, I64, I32, C.c_int64, I64]
+    L.cpg_write_wake_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D]
     _lib = L
     return L

@@ -583,6 +583,16 @@ int cpg_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, cons
     return cpg_geometry_tables(&tmp, body, wake, idx4, coef, clusters);
 }
 
+int cpg_topology_wake_tris(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
+                           int64_t n_tris, int64_t* wake_tris) {
+    if (!nodes || !tris || !ids || !wake_tris) return CPG_E_INVALID;
+    cpg_geometry tmp;
+    std::string msg = cpg::build_mesh(nodes, n_nodes, tris, ids, n_tris, tmp.H);
+    if (!msg.empty()) return CPG_E_BAD_MESH;
+    for (size_t j = 0; j < tmp.H.wake_file_tri.size(); j++) wake_tris[j] = tmp.H.wake_file_tri[j];
+    return CPG_OK;
+}
+
 int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
     if (!g) return CPG_E_INVALID;
     cpg_ctx* ctx = g->ctx;

@@ -524,9 +524,11 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
                 }
         }
     };
+    H.wake_file_tri.resize(H.n_wake);
     for (int64_t j = 0; j < H.n_wake; j++) {
         const Panel& w = B.pan[wp[j]];
         pack(w, &H.wake[j * PF_STRIDE]);
+        H.wake_file_tri[j] = w.tri;
         const Line *a, *b;
         bracket(B.wakes[w.group].lines, w.c.y, a, b);
         if (!a) return "wake panel outside its wake lines";

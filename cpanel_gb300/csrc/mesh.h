@@ -46,6 +46,7 @@ struct HostMesh {
     std::vector<int32_t> cl_ptr, cl_idx;  // CHTLS cluster (matrix indices, self first)
     // wake panels in wPanels order
     std::vector<double> wake;          // n_wake x PF_STRIDE
+    std::vector<int32_t> wake_file_tri;  // n_wake: the .tri triangle of each wake panel
     std::vector<int32_t> widx;         // n_wake x 4 interpolation columns
     std::vector<double> wcoef;         // n_wake
     // Trefftz plane, per live wake

@@ -189,6 +189,45 @@ int cpg_write_surface_vtu(const char* path, const double* nodes, int64_t nn, con
     }
 }
 
+int cpg_write_wake_vtu(const char* path, const double* nodes, int64_t nn, const int64_t* tris, int64_t n,
+                       const double* mu, const double* phi) {
+    if (!path || !nodes || !tris || nn <= 0 || n <= 0 || !mu || !phi) return CPG_E_INVALID;
+    for (int64_t i = 0; i < 3 * n; i++)
+        if (tris[i] < 0 || tris[i] >= nn) return CPG_E_INVALID;
+    try {
+        std::ofstream f(path);
+        if (!f) return CPG_E_INVALID;
+        f << "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+        f << "\t<UnstructuredGrid>\n";
+        f << "\t\t<Piece NumberOfPoints=\"" << nn << "\" NumberOfCells=\"" << n << "\">\n";
+        f << "\t\t\t<CellData Scalars=\"scalars\">\n";
+        print_doubles(f, "Doublet Strengths", mu, n, 1);
+        print_doubles(f, "Velocity Potential", phi, n, 1);
+        f << "\t\t\t</CellData>\n";
+        f << "\t\t\t<Points>\n";
+        print_doubles(f, "Position", nodes, nn, 3);
+        f << "\t\t\t</Points>\n";
+        f << "\t\t\t<Cells>\n";
+        f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n";
+        for (int64_t i = 0; i < n; i++) f << tris[3 * i] << "\t" << tris[3 * i + 1] << "\t" << tris[3 * i + 2] << "\t\n";
+        f << "\t\t\t\t</DataArray>\n";
+        f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n";
+        for (int64_t i = 0; i < n; i++) f << (i + 1) * 3 << "\t\n";
+        f << "\t\t\t\t</DataArray>\n";
+        f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"types\" Format=\"ascii\">\n";
+        for (int64_t i = 0; i < n; i++) f << 5 << "\t\n";  // VTK_TRIANGLE
+        f << "\t\t\t\t</DataArray>\n";
+        f << "\t\t\t</Cells>\n";
+        f << "\t\t</Piece>\n";
+        f << "\t</UnstructuredGrid>\n";
+        f << "</VTKFile>\n";
+        f.close();
+        return f ? CPG_OK : CPG_E_INVALID;
+    } catch (const std::bad_alloc&) {
+        return CPG_E_OOM;
+    }
+}
+
 int cpg_write_volume_vtu(const char* path, const double* pts, int64_t np, const int64_t* cells, int64_t nc,
                          const double* vel, const double* cp) {
     if (!path || !pts || !cells || np <= 0 || nc <= 0 || !vel || !cp) return CPG_E_INVALID;

@@ -1,6 +1,7 @@
 """CPanel's result files from this library's results (include/cpanel_io.h): the .CPout
-summary (caseMgr::writeSummary, CPanel/CPanelMgr.cpp:89-180) and surfaceData.vtu
-(cpCase::writeBodyData, CPanel/cpCase.cpp:711-763).  Host only: no device is needed.
+summary (caseMgr::writeSummary, CPanel/CPanelMgr.cpp:89-180), surfaceData.vtu
+(cpCase::writeBodyData, CPanel/cpCase.cpp:711-763), wakeData.vtu (cpCase::writeWakeData) and
+volumeMesh.vtu (cpCase::writeVolMeshData).  Host only: no device is needed.
 """
 import ctypes as C
 import os
@@ -71,6 +72,42 @@ def write_surface_vtu(path, nodes, tris, mu, sigma, phi, vel, cp, bez, centers):
                                  cpp, bp, cep)
     if rc != 0:
         raise CpgError(rc, "cpg_write_surface_vtu(%s)" % path)
+
+
+def wake_tris(nodes, tris, ids):
+    """Zero-based .tri triangle of each wake panel in wPanels order (host topology)."""
+    L = _lib.load()
+    n_ = np.ascontiguousarray(nodes, dtype=np.float64)
+    t_ = np.ascontiguousarray(tris, dtype=np.int64)
+    i_ = np.ascontiguousarray(ids, dtype=np.int32)
+    out = np.zeros(int(np.count_nonzero(i_ > 1000)), dtype=np.int64)
+    rc = L.cpg_topology_wake_tris(n_.ctypes.data_as(_lib.D), len(n_), t_.ctypes.data_as(_lib.I64),
+                                  i_.ctypes.data_as(_lib.I32), len(i_), out.ctypes.data_as(_lib.I64))
+    if rc != 0:
+        raise CpgError(rc, "cpg_topology_wake_tris")
+    return out
+
+
+def wake_fields(mu, idx4, coef, wake_centers, vinf):
+    """wakePanel::setMu (CPanel/wakePanel.cpp:94-100) and panel::setPotential (CPanel/panel.cpp:106-111)
+    for every wake panel: mu_w = (1 - t) mu_0 + (t - 1) mu_1 + t mu_2 - t mu_3 over the four
+    interpolation panels (idx4, t = coef), phi_w = V_inf . c_w - mu_w."""
+    mu = np.asarray(mu, dtype=np.float64)
+    ix = np.asarray(idx4)
+    t = np.asarray(coef, dtype=np.float64)
+    mw = (1 - t) * mu[ix[:, 0]] + (t - 1) * mu[ix[:, 1]] + t * mu[ix[:, 2]] - t * mu[ix[:, 3]]
+    phi = np.asarray(wake_centers, dtype=np.float64) @ np.asarray(vinf, dtype=np.float64) - mw
+    return mw, phi
+
+
+def write_wake_vtu(path, nodes, tris, mu, phi):
+    """wakeData.vtu (cpCase::writeWakeData): tris n_wake x 3 zero-based node indices in wPanels order."""
+    L = _lib.load()
+    t = np.ascontiguousarray(tris, dtype=np.int64)
+    (nd, ndp), (m, mp), (p, pp) = _d(nodes), _d(mu), _d(phi)
+    rc = L.cpg_write_wake_vtu(os.fsencode(path), ndp, len(nd), t.ctypes.data_as(_lib.I64), len(t), mp, pp)
+    if rc != 0:
+        raise CpgError(rc, "cpg_write_wake_vtu(%s)" % path)
 
 
 def volume_grid(bounds, res):

@@ -124,6 +124,11 @@ int  cpg_topology(const double* nodes, int64_t n_nodes, const int64_t* tris, con
                   cpg_geometry_info* info, double* body, double* wake, int32_t* idx4, double* coef,
                   int32_t* clusters);
 
+/* Host-only (no device needed): the .tri triangle (zero-based) of each wake panel in wPanels
+ * order (n_wake values), for writing wake results against the input mesh. */
+int  cpg_topology_wake_tris(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
+                            int64_t n_tris, int64_t* wake_tris);
+
 /* ---- assembly (geometry::setInfCoeff) ----
  * CPG_PLAIN_FP64 builds A and B (n x n FP64, column-major, A(i,j) = A[j*n+i]).
  * CPG_MIXED builds A in FP32 plus the FP64 near-field correction and the three

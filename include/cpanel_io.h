@@ -6,6 +6,7 @@
  *                           input echo of inputParams::print, CPanel/inputParams.cpp:227-318
  *   cpg_write_surface_vtu   cpCase::writeBodyData, CPanel/cpCase.cpp:711-763, through
  *                           VTUfile::write, CPanel/VTUfile.cpp:20-147
+ *   cpg_write_wake_vtu      cpCase::writeWakeData, CPanel/cpCase.cpp:883-907
  *   cpg_write_volume_vtu    cpCase::writeVolMeshData, CPanel/cpCase.cpp:979-1004
  *
  * The text follows the reference's layout and stream formatting (the same column widths,
@@ -62,6 +63,12 @@ int cpg_write_cpout(const char* path, const cpg_cpout_inputs* inputs, const cpg_
 int cpg_write_surface_vtu(const char* path, const double* nodes, int64_t n_nodes, const int64_t* tris, int64_t n,
                           const double* mu, const double* sigma, const double* phi, const double* vel,
                           const double* cp, const double* bez, const double* centers);
+
+/* Write wakeData.vtu (cpCase::writeWakeData, CPanel/cpCase.cpp:883-907): tris n_wake x 3 zero-based
+ * node indices of the wake panels in wPanels order; per wake panel mu and phi (the reference's
+ * "Doublet Strengths" and "Velocity Potential"). */
+int cpg_write_wake_vtu(const char* path, const double* nodes, int64_t n_nodes, const int64_t* tris, int64_t n_wake,
+                       const double* mu, const double* phi);
 
 /* Write volumeMesh.vtu (cpCase::writeVolMeshData, CPanel/cpCase.cpp:979-1004): points n_points x 3,
  * cells n_cells x 8 zero-based point indices (VTK voxels, the order cpCase::createVolMesh uses),

@@ -8,11 +8,14 @@ Run in a container where the CPanel reference tree is mounted (default path
                    (doublet, source, potential, velocity, Cp, centroid; 6 significant
                    digits as printed by the reference) and the .CPout summary numbers.
 
+  case4412_wake.npz -- the same case's V1_Mach0.1_alpha5_beta0/wakeData-0.vtu: wake doublet strength and
+                   velocity potential per wake panel (6 significant digits) and the panel centroids from
+                   the file's points and connectivity.
   case4412AR6.npz -- Connor Cases/4412AR6 (Stability_Derivatives 1 in its .CPin): the mesh and the
                    .CPout numbers, the ten stability derivatives included (5 decimals).
 
 The generated files are small and committed; tests never read the reference tree.
-Usage: python make_golden.py [4412 | 4412AR6]  (default: both).
+Usage: python make_golden.py [4412 | 4412wake | 4412AR6]  (default: all).
 """
 import os
 import re
@@ -87,10 +90,25 @@ def main_4412ar6():
     print("wrote case4412AR6.npz", nodes.shape, tris.shape, cp, da, db)
 
 
+def main_4412wake():
+    case = os.path.join(REF, "Connor Cases", "4412")
+    if not os.path.isdir(case):
+        sys.exit("reference case folder not found: %s" % case)
+    vtu = read_vtu_arrays(os.path.join(case, "V1_Mach0.1_alpha5_beta0", "wakeData-0.vtu"))
+    con = vtu["connectivity"].reshape(-1, 3)
+    centroid = vtu["Position"][con].mean(axis=1)
+    np.savez_compressed(os.path.join(HERE, "case4412_wake.npz"),
+                        mu=vtu["Doublet Strengths"].astype(np.float32),
+                        phi=vtu["Velocity Potential"].astype(np.float32), centroid=centroid.astype(np.float32))
+    print("wrote case4412_wake.npz", con.shape)
+
+
 def main():
-    which = sys.argv[1:] or ["4412", "4412AR6"]
+    which = sys.argv[1:] or ["4412", "4412wake", "4412AR6"]
     if "4412AR6" in which:
         main_4412ar6()
+    if "4412wake" in which:
+        main_4412wake()
     if "4412" not in which:
         return
     case = os.path.join(REF, "Connor Cases", "4412")

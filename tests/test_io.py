@@ -143,3 +143,72 @@ def test_volume_vtu_round_trip(built, tmp_path):
     assert np.array_equal(d["connectivity"].reshape(-1, 8), cells) and np.all(d["types"] == 11)
     assert np.allclose(d["Position"], pts)
 
+
+def test_wake_vtu_matches_reference_output(built, case4412, solved4412, tmp_path):
+    """wakeData.vtu for the reference's 4412 case from the oracle's body doublets: the wake
+    doublets (wakePanel::setMu) and potentials (panel::setPotential) against the reference's
+    own wakeData-0.vtu, matched by panel centroid, at its 6 significant digits."""
+    from scipy.spatial import cKDTree
+
+    import cpanel_gb300 as cg
+    from cpanel_gb300 import io
+    from conftest import GOLDEN
+    g = case4412
+    ref = dict(np.load(os.path.join(GOLDEN, "case4412_wake.npz")))
+    m, A, B, r = solved4412
+    tri = g["tris"].astype(np.int64)
+    t = cg.topology(g["nodes"], tri, g["ids"])
+    a = np.radians(float(g["alpha"]))
+    vinf = float(g["V"]) * np.array([np.cos(a), 0.0, np.sin(a)])
+    wmu, wphi = io.wake_fields(r["mu"], t["idx4"], t["coef"], t["wake"][:, 0:3], vinf)
+    assert np.allclose(wmu, r["wake_mu"], rtol=0, atol=1e-14)  # the oracle's own wakePanel::setMu
+    wt = io.wake_tris(g["nodes"], tri, g["ids"])
+    path = str(tmp_path / "wakeData.vtu")
+    io.write_wake_vtu(path, g["nodes"], tri[wt] - 1, wmu, wphi)
+    d = io.read_vtu_cells(path)
+    con = d["connectivity"].reshape(-1, 3)
+    c = d["Position"][con].mean(axis=1)
+    assert np.allclose(c, t["wake"][:, 0:3], atol=1e-12)  # the written triangles are the wake panels
+    dist, idx = cKDTree(c).query(ref["centroid"].astype(np.float64))
+    assert dist.max() < 1e-4 and len(np.unique(idx)) == len(idx) == len(wmu)
+    for name, key in (("Doublet Strengths", "mu"), ("Velocity Potential", "phi")):
+        want = ref[key].astype(np.float64)
+        assert np.all(np.abs(d[name][idx] - want) <= 1.2e-5 * np.abs(want) + 4e-7), name
+
+
+def test_case_write_files_on_host(built, case4412, solved4412, tmp_path):
+    """CpCase.writeFiles itself, on the CPU: a stand-in geometry with the host topology tables
+    and the oracle's solution in place of the device results."""
+    import cpanel_gb300 as cg
+    from cpanel_gb300 import io
+    g = case4412
+    m, A, B, r = solved4412
+    tri = g["tris"].astype(np.int64)
+    t = cg.topology(g["nodes"], tri, g["ids"])
+
+    class HostGeometry:
+        _nodes, _tris, _ids = g["nodes"], tri, g["ids"]
+        n, nw = m.n, m.nw
+
+        def tables(self):
+            return t
+
+    case = cg.CpCase.__new__(cg.CpCase)
+    case.geom = HostGeometry()
+    case.flow = (float(g["V"]), float(g["alpha"]), float(g["beta"]), float(g["mach"]))
+    case.refs = dict(Sref=float(g["Sref"]), bref=float(g["bref"]), cref=float(g["cref"]),
+                     cg=tuple(float(x) for x in g["cg"]))
+    case.precision = "fp64"
+    case.stab = None
+    case.survey = None
+    case.res = {k: np.asarray(r[k])[None] for k in ("mu", "sigma", "phi", "cp", "vel", "Fbody", "Fwind", "CM")}
+    case.res.update(CL=np.array([r["CL"]]), CDi=np.array([r["CDi"]]))
+    vtu, cpout = case.writeFiles(str(tmp_path), geom_file="4412.tri")
+    sub = os.path.dirname(vtu)
+    assert os.path.basename(sub) == "V1_Mach0.1_alpha5_beta0" and os.path.basename(cpout) == "4412.CPout"
+    d = io.read_vtu_cells(vtu)
+    assert np.allclose(d["Cp"], r["cp"], rtol=1e-5, atol=1e-6)
+    w = io.read_vtu_cells(os.path.join(sub, "wakeData.vtu"))
+    assert np.allclose(w["Doublet Strengths"], r["wake_mu"], rtol=1e-5, atol=1e-7)
+    assert "CL = %.5f" % r["CL"] in open(cpout).read()
+

@@ -37,7 +37,8 @@ struct Panel {
     // body
     bool upper = false, lower = false, tip = false;
     int ts = 3, index = -1;
-    std::vector<int> nbr, cluster;
+    int nbr[3], nnb = 0;  // body neighbours across shared edges: at most one per edge
+    std::vector<int> cluster;
     // wake
     int upPan = -1, loPan = -1;
     bool teWake = false;
@@ -62,6 +63,11 @@ struct Wake {
     bool live = true;
 };
 
+struct Geo {
+    d3 c, n;
+    double area, longSide;
+};
+
 struct Builder {
     std::vector<d3> P;
     std::vector<Edge> E;
@@ -82,18 +88,20 @@ struct Builder {
         return (int)E.size() - 1;
     }
 
-    void geom(Panel& p) {  // panel::setGeom, CPanel/panel.cpp:33-72
-        p.longSide = 0;
+    // panel::setGeom, CPanel/panel.cpp:33-72.  The edges' lengths are taken from the panel's own
+    // node pairs: a stored edge may run the other way round, which gives the same length.
+    void geom(const int nd[3], Geo& g) const {
+        g.longSide = 0;
         for (int i = 0; i < 3; i++) {
-            double l = nrm(sub(P[E[p.ed[i]].n2], P[E[p.ed[i]].n1]));
-            if (l > p.longSide) p.longSide = l;
+            double l = nrm(sub(P[nd[i < 2 ? i + 1 : 0]], P[nd[i]]));
+            if (l > g.longSide) g.longSide = l;
         }
-        d3 p0 = P[p.nd[0]], p1 = P[p.nd[1]], p2 = P[p.nd[2]];
+        d3 p0 = P[nd[0]], p1 = P[nd[1]], p2 = P[nd[2]];
         d3 a = sub(p1, p0), b = sub(p2, p0);
-        p.c = divs(add(add(p0, p1), p2), 3.0);
+        g.c = divs(add(add(p0, p1), p2), 3.0);
         double th = std::acos(dot(a, b) / (nrm(a) * nrm(b)));
-        p.area = 0.5 * nrm(a) * nrm(b) * std::sin(th);
-        p.n = unit(cross(a, b));
+        g.area = 0.5 * nrm(a) * nrm(b) * std::sin(th);
+        g.n = unit(cross(a, b));
     }
 
     void addLine(int w, Line l) {  // wake::addWakeLine, CPanel/wake.cpp:140-144
@@ -134,8 +142,10 @@ struct Builder {
         } else {
             const Panel& b0 = pan[e.b[0]];
             const Panel& b1 = pan[e.b[1]];
-            double ang = std::acos(dot(b0.n, b1.n));
-            if (ang > 4.7 * kPi / 6 && b0.id == b1.id) {
+            // acos(d) > 4.7 pi / 6 needs d < cos(4.7 pi / 6) = -0.778: acos is evaluated only
+            // below -0.7, so the outcome is the reference's test for every d
+            double d = dot(b0.n, b1.n);
+            if (b0.id == b1.id && d < -0.7 && std::acos(d) > 4.7 * kPi / 6) {
                 e.te = true;
                 surfLS[b0.group] = true;
                 surfLS[b1.group] = true;
@@ -148,6 +158,25 @@ int fact(int i) {
     int o = 1;
     for (int k = 2; k <= i; k++) o *= k;
     return o;
+}
+
+// Runs f(worker, lo, hi) over [0, n) in contiguous slices, one host thread each (at most 16);
+// a small range, or a slice whose thread cannot be started, runs on the calling thread.
+template <class F>
+void par_slices(size_t n, F f) {
+    unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (n < 2048) nth = 1;
+    std::vector<std::thread> pool;
+    for (unsigned w = 1; w < nth; w++) {
+        size_t lo = n * w / nth, hi = n * (w + 1) / nth;
+        try {
+            pool.emplace_back([&f, w, lo, hi] { f(w, lo, hi); });
+        } catch (...) {
+            f(w, lo, hi);
+        }
+    }
+    f(0u, (size_t)0, n / nth);
+    for (auto& t : pool) t.join();
 }
 
 }  // namespace
@@ -251,8 +280,20 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
                 double l = nrm(sub(B.P[conn[3 * i + (j < 2 ? j + 1 : 0)]], B.P[conn[3 * i + j]]));
                 if (l < tol) tol = l;
             }
+        // a wake node farther than tol from the body nodes' bounding box in some axis matches
+        // none of them (rounded subtraction is monotone), so its scan is skipped
+        d3 lo = B.P[0], hi = B.P[0];
+        for (int64_t i = 0; i < wns; i++) {
+            const d3& q = B.P[i];
+            lo = {std::min(lo.x, q.x), std::min(lo.y, q.y), std::min(lo.z, q.z)};
+            hi = {std::max(hi.x, q.x), std::max(hi.y, q.y), std::max(hi.z, q.z)};
+        }
         std::vector<int64_t> rep(nn, -1);
-        for (int64_t j = wns; j < nn; j++)
+        for (int64_t j = wns; j < nn; j++) {
+            const d3& q = B.P[j];
+            if (q.x - hi.x >= tol || lo.x - q.x >= tol || q.y - hi.y >= tol || lo.y - q.y >= tol ||
+                q.z - hi.z >= tol || lo.z - q.z >= tol)
+                continue;
             for (int64_t i = 0; i < wns; i++) {
                 d3 v = sub(B.P[i], B.P[j]);
                 if (std::max(std::fabs(v.x), std::max(std::fabs(v.y), std::fabs(v.z))) < tol) {
@@ -260,10 +301,19 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
                     break;
                 }
             }
+        }
         for (int64_t i = wts; i < nt; i++)
             for (int j = 0; j < 3; j++)
                 if (rep[conn[3 * i + j]] >= 0) conn[3 * i + j] = rep[conn[3 * i + j]];
     }
+    // panel geometry of every triangle, in parallel: it needs only the node positions
+    std::vector<Geo> geo(nt);
+    par_slices((size_t)nt, [&](unsigned, size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; i++) {
+            int nd[3] = {(int)conn[3 * i], (int)conn[3 * i + 1], (int)conn[3 * i + 2]};
+            B.geom(nd, geo[i]);
+        }
+    });
     // createSurfaces, CPanel/geometry.cpp:712-747
     std::vector<std::vector<int>> surfPans;
     B.pan.reserve(nt);
@@ -288,7 +338,10 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
             if (fresh) B.wakes.emplace_back();
             p.group = (int)B.wakes.size() - 1;
         }
-        B.geom(p);
+        p.c = geo[i].c;
+        p.n = geo[i].n;
+        p.area = geo[i].area;
+        p.longSide = geo[i].longSide;
         B.pan.push_back(p);
         int pi = (int)B.pan.size() - 1;
         for (int k = 0; k < 3; k++) {
@@ -326,8 +379,9 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
     }
     for (const Edge& e : B.E)  // edge::setNeighbors
         if (e.nb == 2) {
-            B.pan[e.b[0]].nbr.push_back(e.b[1]);
-            B.pan[e.b[1]].nbr.push_back(e.b[0]);
+            Panel &a = B.pan[e.b[0]], &b = B.pan[e.b[1]];
+            if (a.nnb < 3) a.nbr[a.nnb++] = e.b[1];
+            if (b.nnb < 3) b.nbr[b.nnb++] = e.b[0];
         }
     // wake merge, CPanel/geometry.cpp:426-447
     std::vector<int> order;
@@ -374,44 +428,63 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
         Panel& p = B.pan[b];
         if (!B.surfLS[p.group]) continue;
         int count = 0;
-        for (int q : p.nbr) {
-            d3 nn2 = B.pan[q].n;
+        for (int t = 0; t < p.nnb; t++) {
+            d3 nn2 = B.pan[p.nbr[t]].n;
             double d = dot(p.n, nn2) / (nrm(p.n) * nrm(nn2));
             d = d > 1 ? 1 : (d < -1 ? -1 : d);
-            if (std::acos(d) < tipTol && std::asin(nn2.x) > -kPi / 12) count++;
+            // acos(d) < 1e-8 needs d > 1 - 1e-12 (below it acos(d) > 1.4e-6), so acos is
+            // evaluated only there
+            if (d > 1 - 1e-12 && std::acos(d) < tipTol && std::asin(nn2.x) > -kPi / 12) count++;
         }
         p.tip = count >= 2;
     }
     // bodyPanel::setCluster / clusterTest, CPanel/bodyPanel.cpp:402-487,617-640.  Each panel's
     // cluster depends only on the (fixed) panel data, so the panels are split over host
     // threads; the first failing panel in matrix order is reported, as a sequential loop would.
-    auto cluster_of = [&](int self) -> int {  // 0 ok, 1 no neighbourhood, 2 too large
+    // Membership of the growing cluster and of the candidate list is kept in two per-thread
+    // stamp arrays over all panels (inC stamped with self + 1, inA with a per-pass counter) in
+    // place of linear searches; the order in which panels join is unchanged.
+    struct Marks {
+        std::vector<uint32_t> inC, inA;
+        uint32_t pass = 0;
+    };
+    auto cluster_of = [&](int self, Marks& mk) -> int {  // 0 ok, 1 no neighbourhood, 2 too large
         Panel& p = B.pan[self];
         int dim = p.tip ? 2 : 3;
         size_t buffer = 10;
         size_t nObs = (size_t)(fact(p.ts + dim) / (fact(dim) * fact(p.ts)) - 1) + buffer;
         size_t nP = (nObs + 1) / 2;
         size_t old = 0;
+        const uint32_t me = (uint32_t)self + 1;
+        p.cluster.reserve(nP + 1);
         p.cluster.push_back(self);
+        mk.inC[self] = me;
         bool upF = p.upper, loF = p.lower;
-        auto inCluster = [&](int q) { return std::find(p.cluster.begin(), p.cluster.end(), q) != p.cluster.end(); };
         std::vector<int> add;
         while (p.cluster.size() < nP) {
             add.clear();
+            const uint32_t pass = ++mk.pass;
             for (size_t i = old; i < p.cluster.size(); i++) {
-                const std::vector<int>& nb = B.pan[p.cluster[i]].nbr;
-                for (int q : nb) {
+                const Panel& c = B.pan[p.cluster[i]];
+                for (int t = 0; t < c.nnb; t++) {
+                    int q = c.nbr[t];
                     const Panel& o = B.pan[q];
                     bool ok = !((upF && o.lower) || (loF && o.upper)) && p.tip == o.tip;
                     if (ok) {
                         double d = dot(o.n, p.n);
                         d = d > 1 ? 1 : (d < -1 ? -1 : d);
-                        ok = std::acos(d) < 5 * kPi / 6 && !inCluster(q) && q != self;
+                        // acos(d) < 5 pi / 6 holds for d > -0.8 and fails for d < -0.9; acos is
+                        // evaluated only between, so the outcome is the reference's test
+                        bool turn = d > -0.8 ? true : (d < -0.9 ? false : std::acos(d) < 5 * kPi / 6);
+                        ok = turn && mk.inC[q] != me && q != self;
                     }
                     if (ok) {
                         if (o.upper) upF = true;
                         else if (o.lower) loF = true;
-                        if (std::find(add.begin(), add.end(), q) == add.end()) add.push_back(q);
+                        if (mk.inA[q] != pass) {
+                            mk.inA[q] = pass;
+                            add.push_back(q);
+                        }
                     }
                 }
             }
@@ -428,6 +501,7 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
             old = p.cluster.size();
             for (int q : add) {
                 p.cluster.push_back(q);
+                mk.inC[q] = me;
                 if (p.cluster.size() == nP + 1) break;
             }
         }
@@ -438,14 +512,12 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
     {
         const size_t np = bp.size();
         std::vector<int> status(np, 0);
-        unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-        if (np < 2048) nth = 1;
-        std::vector<std::thread> pool;
-        for (unsigned w = 0; w < nth; w++)
-            pool.emplace_back([&, w] {
-                for (size_t i = w; i < np; i += nth) status[i] = cluster_of(bp[i]);
-            });
-        for (auto& th : pool) th.join();
+        par_slices(np, [&](unsigned, size_t lo, size_t hi) {
+            Marks mk;
+            mk.inC.assign(B.pan.size(), 0);
+            mk.inA.assign(B.pan.size(), 0);
+            for (size_t i = lo; i < hi; i++) status[i] = cluster_of(bp[i], mk);
+        });
         for (size_t i = 0; i < np; i++) {
             if (status[i] == 1) return "a body panel has no usable CHTLS neighbourhood";
             if (status[i] == 2) return "CHTLS cluster larger than 32 panels";
@@ -465,10 +537,10 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
     H.tsorder.resize(H.n_body);
     H.surf_id.resize(H.n_body);
     H.file_tri.resize(H.n_body);
-    H.cl_ptr.assign(1, 0);
-    H.cl_ptr.reserve(H.n_body + 1);
-    H.cl_idx.clear();
-    H.cl_idx.reserve(H.n_body * 16);
+    H.cl_ptr.assign(H.n_body + 1, 0);
+    for (int64_t i = 0; i < H.n_body; i++)
+        H.cl_ptr[i + 1] = H.cl_ptr[i] + (int32_t)B.pan[bp[i]].cluster.size();
+    H.cl_idx.assign(H.cl_ptr[H.n_body], 0);
     H.n_tip = 0;
     auto pack = [&](const Panel& p, double* o) {
         for (int k = 0; k < 3; k++) {
@@ -488,22 +560,24 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
         o[PF_AREA] = p.area;
         o[PF_LONG] = p.longSide;
     };
-    for (int64_t i = 0; i < H.n_body; i++) {
-        const Panel& p = B.pan[bp[i]];
-        pack(p, &H.body[i * PF_STRIDE]);
-        H.bez[3 * i] = p.n.x;
-        H.bez[3 * i + 1] = p.n.y;
-        H.bez[3 * i + 2] = p.n.z;
-        H.tip[i] = p.tip;
-        H.n_tip += p.tip;
-        H.upper[i] = p.upper;
-        H.lower[i] = p.lower;
-        H.tsorder[i] = p.ts;
-        H.surf_id[i] = p.id;
-        H.file_tri[i] = p.tri;
-        for (int q : p.cluster) H.cl_idx.push_back(B.pan[q].index);
-        H.cl_ptr.push_back((int32_t)H.cl_idx.size());
-    }
+    par_slices((size_t)H.n_body, [&](unsigned, size_t lo, size_t hi) {
+        for (size_t i = lo; i < hi; i++) {
+            const Panel& p = B.pan[bp[i]];
+            pack(p, &H.body[i * PF_STRIDE]);
+            H.bez[3 * i] = p.n.x;
+            H.bez[3 * i + 1] = p.n.y;
+            H.bez[3 * i + 2] = p.n.z;
+            H.tip[i] = p.tip;
+            H.upper[i] = p.upper;
+            H.lower[i] = p.lower;
+            H.tsorder[i] = p.ts;
+            H.surf_id[i] = p.id;
+            H.file_tri[i] = p.tri;
+            int32_t o = H.cl_ptr[i];
+            for (int q : p.cluster) H.cl_idx[o++] = B.pan[q].index;
+        }
+    });
+    for (int64_t i = 0; i < H.n_body; i++) H.n_tip += H.tip[i];
     H.wake.assign(H.n_wake * PF_STRIDE, 0.0);
     H.widx.resize(H.n_wake * 4);
     H.wcoef.resize(H.n_wake);

@@ -23,7 +23,7 @@ import numpy as np
 from . import _lib
 from ._lib import MIXED, PLAIN_FP64, CpgError
 
-__all__ = ["Context", "Geometry", "CpCase", "solve_cases", "topology", "read_tri", "panel_phi_inf", "dub_phi_inf",
+__all__ = ["Context", "Geometry", "CpCase", "solve_cases", "topology", "read_tri", "streamlines_field", "panel_phi_inf", "dub_phi_inf",
            "panel_v_inf", "CpgError", "PLAIN_FP64", "MIXED"]
 
 _shutting_down = False
@@ -294,6 +294,26 @@ class CpCase:
         g.ctx.check(g.ctx.L.cpg_volume_velocity(g.h, _p(sig), _p(mu), _p(pts), len(pts), _p(vel)), "velocityAtPoints")
         return vel
 
+    def streamlines(self, starts, x_max, tol=1e-4, max_points=1000):
+        """Off-body streamlines (streamline::streamline / rkf, CPanel/streamline.cpp:20-78) from the
+        start points (k x 3) to x_max, through geometry::pntVelocity (panels + V_inf, x divided by
+        the Prandtl-Glauert factor).  All lines advance together, one batched panel-velocity launch
+        per Runge-Kutta stage.  Returns (lines, ended) as streamlines_field does."""
+        g = self.geom
+        st = np.ascontiguousarray(starts, dtype=np.float64).reshape(-1, 3)
+        n = len(st)
+        pts = np.zeros((n, max_points, 3))
+        vel = np.zeros((n, max_points, 3))
+        counts = np.zeros(n, dtype=np.int32)
+        ended = np.zeros(n, dtype=np.int32)
+        sig = np.ascontiguousarray(self.res["sigma"][0])
+        mu = np.ascontiguousarray(self.res["mu"][0])
+        fl = _lib.Flow(*[float(x) for x in self.flow])
+        g.ctx.check(g.ctx.L.cpg_streamlines(g.h, _p(sig), _p(mu), C.byref(fl), _p(st), n, float(x_max), float(tol),
+                                            int(max_points), _p(pts), _p(vel), _p(counts, _lib.I32),
+                                            _p(ended, _lib.I32)), "streamlines")
+        return _streamline_lines(pts, vel, counts, ended)
+
     def vinf(self):
         """V_inf in body axes (cpCase::windToBody, CPanel/cpCase.cpp:142-165)."""
         V, alpha, beta, _ = self.flow
@@ -343,6 +363,45 @@ class CpCase:
                        geom_file=geom_file, flags=dict(stability_derivatives=self.stab is not None),
                        **self.refs)
         return vtu, cpout
+
+
+def _streamline_lines(pts, vel, counts, ended):
+    lines = [(pts[i, :counts[i]].copy(), vel[i, :counts[i]].copy()) for i in range(len(counts))]
+    return lines, ended.astype(bool)
+
+
+def streamlines_field(fn, speed, starts, x_max, tol=1e-4, max_points=1000):
+    """The library's streamline integrator (streamline::streamline / rkf, CPanel/streamline.cpp:20-78)
+    through a Python velocity field: fn(points m x 3) -> velocities m x 3, free stream and
+    compressibility included.  The first step is 0.1 / speed.  Returns (lines, ended): lines[i] is
+    (points, velocities) of every step start of line i; ended[i] is True where the line reached
+    x_max (False: max_points cut it short)."""
+    L = _lib.load()
+    st = np.ascontiguousarray(starts, dtype=np.float64).reshape(-1, 3)
+    n = len(st)
+    pts = np.zeros((n, max_points, 3))
+    vel = np.zeros((n, max_points, 3))
+    counts = np.zeros(n, dtype=np.int32)
+    ended = np.zeros(n, dtype=np.int32)
+    failure = []
+
+    def cb(user, p, m, v):
+        try:
+            P = np.ctypeslib.as_array(p, shape=(m, 3))
+            V = np.ctypeslib.as_array(v, shape=(m, 3))
+            V[:] = np.asarray(fn(P.copy()), dtype=np.float64).reshape(m, 3)
+            return 0
+        except Exception as e:  # reported after the call: an exception cannot cross the C frames
+            failure.append(e)
+            return 99
+
+    rc = L.cpg_streamlines_field(_lib.VELOCITY_FN(cb), None, float(speed), _p(st), n, float(x_max), float(tol),
+                                 int(max_points), _p(pts), _p(vel), _p(counts, _lib.I32), _p(ended, _lib.I32))
+    if failure:
+        raise failure[0]
+    if rc != 0:
+        raise CpgError(rc, "cpg_streamlines_field")
+    return _streamline_lines(pts, vel, counts, ended)
 
 
 def _dev_ptr(t):

@@ -12,6 +12,8 @@ LIB_PATH = os.path.join(HERE, "_build", "libcpanel_gb300.so")
 D = C.POINTER(C.c_double)
 I32 = C.POINTER(C.c_int32)
 I64 = C.POINTER(C.c_int64)
+# cpg_velocity_fn: (user, points m x 3, m, velocities m x 3) -> status
+VELOCITY_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, D, C.c_int64, D)
 
 STATUS = {0: "CPG_OK", 1: "CPG_E_INVALID", 2: "CPG_E_OOM", 3: "CPG_E_CUDA", 4: "CPG_E_BAD_MESH",
           5: "CPG_E_NOT_CONVERGED", 6: "CPG_E_TIMEOUT", 7: "CPG_E_NO_DEVICE"}
@@ -63,7 +65,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
            "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read",
            "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_release_spares", "cpg_stability_derivatives",
-           "cpg_volume_velocity", "cpg_topology_wake_tris",
+           "cpg_volume_velocity", "cpg_topology_wake_tris", "cpg_streamlines", "cpg_streamlines_field",
            # cpanel_vp.h
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_ptree_set_precision", "cpg_set_particle_precision", "cpg_particles_velocity", "cpg_particles_stretch_diff",
@@ -249,6 +251,10 @@ def load():
     L.cpg_write_volume_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D]
     L.cpg_volume_velocity.argtypes = [vp, D, D, D, C.c_int64, D]
     L.cpg_topology_wake_tris.argtypes = [D, C.c_int64, I64, I32, C.c_int64, I64]
+    L.cpg_streamlines.argtypes = [vp, D, D, C.POINTER(Flow), D, C.c_int, C.c_double, C.c_double, C.c_int, D, D, I32,
+                                  I32]
+    L.cpg_streamlines_field.argtypes = [VELOCITY_FN, vp, C.c_double, D, C.c_int, C.c_double, C.c_double, C.c_int, D,
+                                        D, I32, I32]
     L.cpg_write_wake_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D]
     _lib = L
     return L

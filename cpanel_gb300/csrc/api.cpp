@@ -22,6 +22,7 @@
 #include "../../include/cpanel_vp.h"
 #include "assemble.h"
 #include "mesh.h"
+#include "streamline.h"
 #include "octree.h"
 #include "particles.h"
 #include "vpkern.h"
@@ -801,54 +802,109 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     return CPG_OK;
 }
 
+// cpCase::velocityAtPoint's device state for one case (CPanel/cpCase.cpp:1007-1021): the packed body
+// and wake panel records and the case's strengths, uploaded once by prepare(); eval() then serves
+// any number of point batches through the batched panel-velocity kernel.
+struct PointField {
+    cpg_ctx* ctx = nullptr;
+    cudaStream_t s = nullptr;
+    int64_t n = 0, nw = 0;
+    DevBuf rec, sm, pv, vv;
+    ~PointField() {
+        rec.release();
+        sm.release();
+        pv.release();
+        vv.release();
+    }
+    int prepare(cpg_geometry* g, const double* sigma, const double* mu) {
+        ctx = g->ctx;
+        s = ctx->stream;
+        const cpg::HostMesh& H = g->H;
+        n = H.n_body;
+        nw = H.n_wake;
+        // wake doublets implied by the assembly's wake columns (CPanel/wakePanel.cpp:48-100):
+        // mu_w = (1 - t)(mu_up1 - mu_lo1) + t (mu_up2 - mu_lo2)
+        std::vector<double> wmu(std::max<int64_t>(1, nw), 0.0);
+        for (int64_t j = 0; j < nw; j++) {
+            const int32_t* ix = &H.widx[4 * j];
+            const double t = H.wcoef[j];
+            wmu[j] = (1 - t) * (mu[ix[0]] - mu[ix[1]]) + t * (mu[ix[2]] - mu[ix[3]]);
+        }
+        const size_t R = 24;  // doubles per packed panel record
+        CK(rec.ensure(sizeof(double) * R * (size_t)(n + nw)), "alloc records");
+        CK(cudaMemcpyAsync(rec.p, g->rec.p, sizeof(double) * R * n, cudaMemcpyDeviceToDevice, s), "records");
+        if (nw > 0)
+            CK(cudaMemcpyAsync(rec.as<double>() + R * n, g->wrec.p, sizeof(double) * R * nw, cudaMemcpyDeviceToDevice,
+                               s),
+               "wake records");
+        CK(sm.ensure(sizeof(double) * (2 * n + nw)), "alloc strengths");
+        CK(cudaMemcpyAsync(sm.as<double>(), sigma, sizeof(double) * n, cudaMemcpyHostToDevice, s), "sigma");
+        CK(cudaMemcpyAsync(sm.as<double>() + n, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s), "mu");
+        if (nw > 0)
+            CK(cudaMemcpyAsync(sm.as<double>() + 2 * n, wmu.data(), sizeof(double) * nw, cudaMemcpyHostToDevice, s),
+               "wake mu");
+        CK(cudaStreamSynchronize(s), "point field");  // wmu is a local: its copy has to finish here
+        return CPG_OK;
+    }
+    int eval(const double* pts, int64_t m, double* vel) {
+        if (m <= 0) return CPG_OK;
+        CK(pv.ensure(sizeof(double) * 3 * m), "alloc points");
+        CK(vv.ensure(sizeof(double) * 3 * m), "alloc velocities");
+        CK(cudaMemcpyAsync(pv.p, pts, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, s), "points");
+        {
+            cpg::ProfScope ps(cpg::Prof::POST, s);
+            CK(cpg::launch_panels_velocity_rec(rec.as<double>(), sm.as<double>(), sm.as<double>() + n, n,
+                                               sm.as<double>() + 2 * n, nw, pv.as<double>(), m, vv.as<double>(), s),
+               "panel velocities");
+        }
+        CK(cudaMemcpyAsync(vel, vv.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, s), "velocities");
+        CK(cudaStreamSynchronize(s), "volume velocity");
+        return CPG_OK;
+    }
+};
+
 int cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu, const double* pts, int64_t m,
                         double* vel) {
     if (!g || !sigma || !mu || (m > 0 && (!pts || !vel)) || m < 0) return CPG_E_INVALID;
     if (m == 0) return CPG_OK;
-    cpg_ctx* ctx = g->ctx;
-    ProfInstall pi(ctx);
-    cudaStream_t s = ctx->stream;
-    const cpg::HostMesh& H = g->H;
-    const int64_t n = H.n_body, nw = H.n_wake;
-    // wake doublets implied by the assembly's wake columns (CPanel/wakePanel.cpp:48-100):
-    // mu_w = (1 - t)(mu_up1 - mu_lo1) + t (mu_up2 - mu_lo2)
-    std::vector<double> wmu(std::max<int64_t>(1, nw), 0.0);
-    for (int64_t j = 0; j < nw; j++) {
-        const int32_t* ix = &H.widx[4 * j];
-        const double t = H.wcoef[j];
-        wmu[j] = (1 - t) * (mu[ix[0]] - mu[ix[1]]) + t * (mu[ix[2]] - mu[ix[3]]);
-    }
-    const size_t R = 24;  // doubles per packed panel record
-    DevBuf rec, sm, pv, vv;
-    struct Release {  // on every return: these buffers live for this call only
-        DevBuf* b[4];
-        ~Release() {
-            for (DevBuf* x : b) x->release();
+    ProfInstall pi(g->ctx);
+    PointField f;
+    int rc = f.prepare(g, sigma, mu);
+    return rc != CPG_OK ? rc : f.eval(pts, m, vel);
+}
+
+int cpg_streamlines(cpg_geometry* g, const double* sigma, const double* mu, const cpg_flow* flow,
+                    const double* starts, int n_lines, double x_max, double tol, int max_points, double* pts,
+                    double* vel, int32_t* counts, int32_t* ended) {
+    if (!g || !sigma || !mu || !flow || n_lines < 0 || max_points < 0 || !(tol > 0) || !(flow->V > 0))
+        return CPG_E_INVALID;
+    if (n_lines > 0 && (!starts || !counts || !ended || (max_points > 0 && (!pts || !vel)))) return CPG_E_INVALID;
+    if (!(flow->mach >= 0 && flow->mach < 1)) return CPG_E_INVALID;
+    ProfInstall pi(g->ctx);
+    PointField f;
+    int rc = f.prepare(g, sigma, mu);
+    if (rc != CPG_OK) return rc;
+    cpg_refs refs{1, 1, 1, {0, 0, 0}};
+    cpg::CaseScalars cs;
+    case_scalars(*flow, refs, cs);
+    struct Field {
+        PointField* f;
+        double vinf[3], pg;
+    } u{&f, {cs.Vinf[0], cs.Vinf[1], cs.Vinf[2]}, cs.PG};
+    // geometry::pntVelocity (CPanel/geometry.cpp:1239-1253): the panels' velocity plus V_inf, the x
+    // component then divided by the Prandtl-Glauert factor
+    cpg_velocity_fn fn = [](void* user, const double* p, int64_t m, double* v) -> int {
+        Field* u = (Field*)user;
+        int e = u->f->eval(p, m, v);
+        if (e != CPG_OK) return e;
+        for (int64_t i = 0; i < m; i++) {
+            for (int c = 0; c < 3; c++) v[3 * i + c] += u->vinf[c];
+            v[3 * i] /= u->pg;
         }
-    } rel{{&rec, &sm, &pv, &vv}};
-    CK(rec.ensure(sizeof(double) * R * (size_t)(n + nw)), "alloc records");
-    CK(cudaMemcpyAsync(rec.p, g->rec.p, sizeof(double) * R * n, cudaMemcpyDeviceToDevice, s), "records");
-    if (nw > 0)
-        CK(cudaMemcpyAsync(rec.as<double>() + R * n, g->wrec.p, sizeof(double) * R * nw, cudaMemcpyDeviceToDevice, s),
-           "wake records");
-    CK(sm.ensure(sizeof(double) * (2 * n + nw)), "alloc strengths");
-    CK(cudaMemcpyAsync(sm.as<double>(), sigma, sizeof(double) * n, cudaMemcpyHostToDevice, s), "sigma");
-    CK(cudaMemcpyAsync(sm.as<double>() + n, mu, sizeof(double) * n, cudaMemcpyHostToDevice, s), "mu");
-    if (nw > 0)
-        CK(cudaMemcpyAsync(sm.as<double>() + 2 * n, wmu.data(), sizeof(double) * nw, cudaMemcpyHostToDevice, s),
-           "wake mu");
-    CK(pv.ensure(sizeof(double) * 3 * m), "alloc points");
-    CK(vv.ensure(sizeof(double) * 3 * m), "alloc velocities");
-    CK(cudaMemcpyAsync(pv.p, pts, sizeof(double) * 3 * m, cudaMemcpyHostToDevice, s), "points");
-    {
-        cpg::ProfScope ps(cpg::Prof::POST, s);
-        CK(cpg::launch_panels_velocity_rec(rec.as<double>(), sm.as<double>(), sm.as<double>() + n, n,
-                                           sm.as<double>() + 2 * n, nw, pv.as<double>(), m, vv.as<double>(), s),
-           "panel velocities");
-    }
-    CK(cudaMemcpyAsync(vel, vv.p, sizeof(double) * 3 * m, cudaMemcpyDeviceToHost, s), "velocities");
-    CK(cudaStreamSynchronize(s), "volume velocity");
-    return CPG_OK;
+        return CPG_OK;
+    };
+    const double speed = std::sqrt(cs.Vinf[0] * cs.Vinf[0] + cs.Vinf[1] * cs.Vinf[1] + cs.Vinf[2] * cs.Vinf[2]);
+    return cpg::streamlines_rkf45(fn, &u, speed, starts, n_lines, x_max, tol, max_points, pts, vel, counts, ended);
 }
 
 int cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_refs* refs, int precision,

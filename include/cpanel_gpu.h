@@ -14,6 +14,8 @@
  *                          compVelocity :342-365, trefftzPlaneAnalysis :541-552)
  *   cpg_stability_derivatives  cpCase::stabilityDerivatives, CPanel/cpCase.cpp:635-665
  *   cpg_volume_velocity   cpCase::velocityAtPoint, CPanel/cpCase.cpp:1007-1021
+ *   cpg_streamlines       streamline::streamline / rkf, CPanel/streamline.cpp:20-78, through
+ *                         geometry::pntVelocity, CPanel/geometry.cpp:1239-1253
  *   cpg_panel_phi_inf     bodyPanel::panelPhiInf, CPanel/bodyPanel.cpp:132-190
  *   cpg_dub_phi_inf       panel::dubPhiInf, CPanel/panel.cpp:208-252
  *   cpg_panel_v_inf       bodyPanel::panelVInf, CPanel/bodyPanel.cpp:305-348
@@ -183,6 +185,30 @@ int  cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_
  * is not included (the reference adds it in populateVolMesh, CPanel/cpCase.cpp:1105-1122). */
 int  cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu, const double* pts, int64_t m,
                          double* vel);
+
+/* ---- off-body streamlines (streamline::streamline / rkf, CPanel/streamline.cpp:20-78) ----
+ * Integrates n_lines streamlines from starts (n_lines x 3) with the reference's adaptive
+ * Runge-Kutta-Fehlberg 4(5) step: the first step is 0.1 / |V_inf|; after each step whose error
+ * estimate err (the distance between the fifth- and fourth-order steps) is positive,
+ * dt <- dt (tol dt / (2 err))^(1/4); a line stops once a step ends at x >= x_max.  The velocity is
+ * geometry::pntVelocity's (CPanel/geometry.cpp:1239-1253): the panels' velocity for the case's
+ * strengths (as cpg_volume_velocity) plus V_inf, its x component divided by sqrt(1 - M^2).
+ * Every step start is recorded with its velocity: pts and vel are n_lines x max_points x 3, line i's
+ * points first; counts[i] is the number recorded; ended[i] is 1 where the line stopped as the
+ * reference's loop stops (x >= x_max, or x no longer a number) and 0 where max_points cut it short.
+ * All lines advance together: each of the six stages evaluates every live line's stage point in
+ * one batched panel-velocity launch. */
+int  cpg_streamlines(cpg_geometry* g, const double* sigma, const double* mu, const cpg_flow* flow,
+                     const double* starts, int n_lines, double x_max, double tol, int max_points, double* pts,
+                     double* vel, int32_t* counts, int32_t* ended);
+
+/* The same integrator through a caller's velocity field (host only): fn(user, p, m, v) writes into v
+ * (m x 3) the velocity at the points p (m x 3), free stream and compressibility included, and returns
+ * 0; a non-zero return stops the integration and is returned.  The first step is 0.1 / speed. */
+typedef int (*cpg_velocity_fn)(void* user, const double* p, int64_t m, double* v);
+int  cpg_streamlines_field(cpg_velocity_fn fn, void* user, double speed, const double* starts, int n_lines,
+                           double x_max, double tol, int max_points, double* pts, double* vel, int32_t* counts,
+                           int32_t* ended);
 
 /* ---- single-evaluation influence operators on DEVICE arrays (batched) ----
  * verts m x 9 (three vertices), poi m x 3; outputs m (phi) or m x 3 (velocity). */

@@ -1,5 +1,6 @@
 """ctypes front end of the CPU oracle (test infrastructure only)."""
 import ctypes as C
+import math
 import os
 
 import numpy as np
@@ -240,6 +241,86 @@ def panels_velocity(bverts, sigma, mu, wverts, wmu, pts, nthreads=None):
     L.cpo_panels_velocity(_p(bv), _p(sg), _p(m_), len(bv), _p(wv), _p(wm), len(wv), _p(p), len(p), _p(out),
                           nthreads or nthreads_default())
     return out
+
+
+def point_velocity(bverts, sigma, mu, wverts, wmu, vinf, mach):
+    """geometry::pntVelocity (CPanel/geometry.cpp:1239-1253) as a function of one point: the panels'
+    velocity plus V_inf, the x component divided by the Prandtl-Glauert factor sqrt(1 - M^2)."""
+    pg = math.sqrt(1 - mach ** 2)
+    vinf = np.asarray(vinf, dtype=np.float64)
+
+    def f(p):
+        v = panels_velocity(bverts, sigma, mu, wverts, wmu, np.asarray(p, dtype=np.float64).reshape(1, 3))[0] + vinf
+        v[0] /= pg
+        return v
+    return f
+
+
+def streamline(vel, start, speed, x_max, tol, max_points=100000):
+    """One off-body streamline as streamline::streamline and streamline::rkf integrate it
+    (CPanel/streamline.cpp:20-78): Runge-Kutta-Fehlberg 4(5) from start with a first step of
+    0.1 / speed; after each step with a positive error estimate err = |step5 - step4|,
+    dt <- dt (tol dt / (2 err))^(1/4); stop once a step ends at x >= x_max.  vel(point) -> velocity.
+    Every step start is kept with its velocity.  Returns (points, velocities, ended), ended False
+    where max_points stopped the line first."""
+    c5 = [16.0 / 135, 0, 6656.0 / 12825, 28561.0 / 56430, -9.0 / 50, 2.0 / 55]
+    c4 = [25.0 / 216, 0, 1408.0 / 2565, 2197.0 / 4104, -0.2, 0]
+    pts, vels = [], []
+
+    def rkf(x0, dt):
+        x = [float(v) for v in x0]
+        k = []
+        for s in range(6):
+            if s == 0:
+                y = list(x)
+            else:
+                k0 = k[0]
+                k1 = k[1] if s > 1 else None
+                k2 = k[2] if s > 2 else None
+                k3 = k[3] if s > 3 else None
+                k4 = k[4] if s > 4 else None
+                y = []
+                for c in range(3):
+                    if s == 1:
+                        y.append(x[c] + 1.0 / 4 * k0[c])
+                    elif s == 2:
+                        y.append(x[c] + 1.0 / 32 * (3 * k0[c] + 9.0 * k1[c]))
+                    elif s == 3:
+                        y.append(x[c] + 1.0 / 2197 * (1932 * k0[c] - 7200 * k1[c] + 7296 * k2[c]))
+                    elif s == 4:
+                        y.append(x[c] + 439.0 / 216 * k0[c] - 8 * k1[c] + 3680.0 / 513 * k2[c] - 845.0 / 4104 * k3[c])
+                    else:
+                        y.append(x[c] - 8.0 / 27 * k0[c] + 2 * k1[c] - 3544.0 / 2565 * k2[c] + 1859.0 / 4104 * k3[c]
+                                 - 11.0 / 40 * k4[c])
+            v = [float(q) for q in vel(np.array(y))]
+            if s == 0:
+                pts.append(list(x))
+                vels.append(v)
+            k.append([dt * v[c] for c in range(3)])
+        s5, s4 = [], []
+        for c in range(3):
+            a5 = a4 = 0.0
+            for j in range(6):
+                a5 += c5[j] * k[j][c]
+                a4 += c4[j] * k[j][c]
+            s5.append(a5)
+            s4.append(a4)
+        err = math.sqrt(sum((s5[c] - s4[c]) * (s5[c] - s4[c]) for c in range(3)))
+        return [x[c] + s5[c] for c in range(3)], err
+
+    dt = 0.1 / speed
+    if max_points < 1:
+        return np.zeros((0, 3)), np.zeros((0, 3)), False
+    nxt, err = rkf(start, dt)
+    ended = True
+    while nxt[0] < x_max:
+        if len(pts) >= max_points:
+            ended = False
+            break
+        if err > 0:
+            dt = dt * math.pow(tol * dt / (2 * err), 0.25)
+        nxt, err = rkf(nxt, dt)
+    return np.array(pts).reshape(-1, 3), np.array(vels).reshape(-1, 3), ended
 
 
 def _parts(pos, strength, radius):

@@ -176,6 +176,27 @@ def test_volume_survey_matches_oracle(cg, small, tmp_path):
     assert np.allclose(d["Cp"], sv["cp"], rtol=1e-5)
 
 
+def test_streamlines_match_oracle(cg, small):
+    """streamline::streamline through geometry::pntVelocity around the wing (plain path): the
+    library's lockstep integration, one batched panel-velocity launch per Runge-Kutta stage, against
+    the oracle integrating each line alone through its own solve and panel sums.  Points agree to
+    1e-7: the two velocity sums round differently and the step-size control carries that along."""
+    from oracle import pyoracle as po
+    g, m, Ao, Bo, refs = small
+    case = cg.CpCase(g, 1.0, 5.0, 0.0, 0.1, precision="fp64", **refs)
+    assert case.run()
+    starts = np.array([[-0.5, 0.3, 0.15], [-0.5, 1.0, -0.3], [-0.5, -0.8, 0.3]])
+    lines, ended = case.streamlines(starts, x_max=2.0, tol=1e-4, max_points=400)
+    assert ended.all()
+    o = m.case(Ao, Bo, alpha=5.0, mach=0.1, **refs)
+    vel = po.point_velocity(m.body_verts(), o["sigma"], o["mu"], m.wake_verts(), o["wake_mu"], case.vinf(), 0.1)
+    for (p, v), s in zip(lines, starts):
+        op, ov, oe = po.streamline(vel, s, 1.0, 2.0, 1e-4, 400)
+        assert oe and p.shape == op.shape and len(p) >= 3
+        assert np.abs(p - op).max() <= 1e-7
+        assert np.abs(v - ov).max() <= 1e-7 * np.abs(ov).max()
+
+
 def test_case_write_files(cg, small, tmp_path):
     """cpCase::writeFiles: the case directory with surfaceData.vtu and the .CPout beside it, read
     back equal to the case's results at the printed precision."""

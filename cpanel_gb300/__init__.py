@@ -228,6 +228,7 @@ class CpCase:
         self.res = None
         self.stab = None
         self.survey = None
+        self.lines = None
 
     def run(self):
         self.res = solve_cases(self.geom, [self.flow], precision=self.precision, **self.refs)
@@ -312,7 +313,9 @@ class CpCase:
         g.ctx.check(g.ctx.L.cpg_streamlines(g.h, _p(sig), _p(mu), C.byref(fl), _p(st), n, float(x_max), float(tol),
                                             int(max_points), _p(pts), _p(vel), _p(counts, _lib.I32),
                                             _p(ended, _lib.I32)), "streamlines")
-        return _streamline_lines(pts, vel, counts, ended)
+        lines, ended = _streamline_lines(pts, vel, counts, ended)
+        self.lines = lines
+        return lines, ended
 
     def vinf(self):
         """V_inf in body axes (cpCase::windToBody, CPanel/cpCase.cpp:142-165)."""
@@ -334,7 +337,8 @@ class CpCase:
     def writeFiles(self, directory=".", geom_file=""):
         """cpCase::writeFiles (CPanel/cpCase.cpp:667-709): the case directory
         V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, wakeData.vtu (when
-        the mesh has wake panels) and volumeMesh.vtu (after volumeSurvey), and
+        the mesh has wake panels), volumeMesh.vtu (after volumeSurvey), streamlines.vtu (after
+        streamlines), and
         caseMgr::writeSummary's .CPout (CPanel/CPanelMgr.cpp:89-116) beside it.  Returns the paths
         of surfaceData.vtu and the .CPout."""
         from . import io
@@ -355,6 +359,8 @@ class CpCase:
             sv = self.survey
             io.write_volume_vtu(os.path.join(sub, "volumeMesh.vtu"), sv["points"], sv["cells"], sv["velocity"],
                                 sv["cp"])
+        if self.lines is not None:
+            io.write_streamlines_vtu(os.path.join(sub, "streamlines.vtu"), self.lines)
         stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
         cpout = os.path.join(directory, stem + ".CPout")
         io.write_cpout(cpout, [dict(V=V, alpha=alpha, beta=beta, mach=mach, CL=self.getCL(), CDi=self.getCD(),

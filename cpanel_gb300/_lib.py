@@ -79,7 +79,8 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_group_default_shape", "cpg_set_inf_coeff_grouped", "cpg_group_schedule", "cpg_batch_solve",
            "cpg_lu_factor_grouped",
            # cpanel_io.h
-           "cpg_write_cpout", "cpg_write_surface_vtu", "cpg_write_volume_vtu", "cpg_write_wake_vtu"]
+           "cpg_write_cpout", "cpg_write_surface_vtu", "cpg_write_volume_vtu", "cpg_write_wake_vtu",
+           "cpg_write_streamlines_vtu"]
 
 TUNE_OFF, TUNE_AUTO, TUNE_FORCE = 0, 1, 2
 
@@ -249,6 +250,7 @@ def load():
     L.cpg_write_cpout.argtypes = [C.c_char_p, C.POINTER(CpoutInputs), C.POINTER(CpoutCase), C.c_int]
     L.cpg_write_surface_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D, D, D, D, D, D]
     L.cpg_write_volume_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D]
+    L.cpg_write_streamlines_vtu.argtypes = [C.c_char_p, D, D, I32, C.c_int, C.c_int]
     L.cpg_volume_velocity.argtypes = [vp, D, D, D, C.c_int64, D]
     L.cpg_topology_wake_tris.argtypes = [D, C.c_int64, I64, I32, C.c_int64, I64]
     L.cpg_streamlines.argtypes = [vp, D, D, C.POINTER(Flow), D, C.c_int, C.c_double, C.c_double, C.c_int, D, D, I32,

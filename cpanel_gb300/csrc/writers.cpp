@@ -270,4 +270,47 @@ int cpg_write_volume_vtu(const char* path, const double* pts, int64_t np, const 
     }
 }
 
+int cpg_write_streamlines_vtu(const char* path, const double* pts, const double* vel, const int32_t* counts,
+                              int n_lines, int max_points) {
+    if (!path || n_lines < 0 || max_points < 0 || (n_lines > 0 && !counts)) return CPG_E_INVALID;
+    for (int i = 0; i < n_lines; i++)
+        if (counts[i] < 0 || counts[i] > max_points) return CPG_E_INVALID;
+    if (n_lines > 0 && max_points > 0 && (!pts || !vel)) return CPG_E_INVALID;
+    try {
+        std::ofstream f(path);
+        if (!f) return CPG_E_INVALID;
+        f << "<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+        f << "\t<UnstructuredGrid>\n";
+        for (int i = 0; i < n_lines; i++) {  // one piece per line, cells (j, j + 1)
+            const int64_t np = counts[i], nc = np > 0 ? np - 1 : 0;
+            const int64_t o = (int64_t)i * max_points * 3;
+            f << "\t\t<Piece NumberOfPoints=\"" << np << "\" NumberOfCells=\"" << nc << "\">\n";
+            f << "\t\t\t<PointData Scalars=\"scalars\">\n";
+            print_doubles(f, "Velocity", vel + o, np, 3);
+            f << "\t\t\t</PointData>\n";
+            f << "\t\t\t<Points>\n";
+            print_doubles(f, "Position", pts + o, np, 3);
+            f << "\t\t\t</Points>\n";
+            f << "\t\t\t<Cells>\n";
+            f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"connectivity\" Format=\"ascii\">\n";
+            for (int64_t j = 0; j < nc; j++) f << j << "\t" << j + 1 << "\t\n";
+            f << "\t\t\t\t</DataArray>\n";
+            f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"offsets\" Format=\"ascii\">\n";
+            for (int64_t j = 0; j < nc; j++) f << (j + 1) * 2 << "\t\n";
+            f << "\t\t\t\t</DataArray>\n";
+            f << "\t\t\t\t<DataArray type=\"Int32\" Name=\"types\" Format=\"ascii\">\n";
+            for (int64_t j = 0; j < nc; j++) f << 3 << "\t\n";  // VTK_LINE
+            f << "\t\t\t\t</DataArray>\n";
+            f << "\t\t\t</Cells>\n";
+            f << "\t\t</Piece>\n";
+        }
+        f << "\t</UnstructuredGrid>\n";
+        f << "</VTKFile>\n";
+        f.close();
+        return f ? CPG_OK : CPG_E_INVALID;
+    } catch (const std::bad_alloc&) {
+        return CPG_E_OOM;
+    }
+}
+
 }  // extern "C"

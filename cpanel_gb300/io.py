@@ -140,6 +140,42 @@ def write_volume_vtu(path, points, cells, vel, cp):
         raise CpgError(rc, "cpg_write_volume_vtu(%s)" % path)
 
 
+def write_streamlines_vtu(path, lines):
+    """streamlines.vtu (cpCase::writeBodyStreamlines, CPanel/cpCase.cpp:937-977): lines as
+    CpCase.streamlines or streamlines_field return them, [(points k x 3, velocities k x 3), ...]; one
+    piece per line with point data Velocity and line cells."""
+    L = _lib.load()
+    n = len(lines)
+    width = max([len(p) for p, _ in lines] + [1])
+    pts = np.zeros((max(n, 1), width, 3))
+    vel = np.zeros((max(n, 1), width, 3))
+    counts = np.zeros(max(n, 1), dtype=np.int32)
+    for i, (p, v) in enumerate(lines):
+        counts[i] = len(p)
+        pts[i, :len(p)] = p
+        vel[i, :len(p)] = v
+    rc = L.cpg_write_streamlines_vtu(os.fsencode(path), pts.ctypes.data_as(_lib.D), vel.ctypes.data_as(_lib.D),
+                                     counts.ctypes.data_as(_lib.I32), n, width)
+    if rc != 0:
+        raise CpgError(rc, "cpg_write_streamlines_vtu(%s)" % path)
+
+
+def read_vtu_pieces(path):
+    """Every piece of an ASCII .vtu file as {array name: array} (points under "Position")."""
+    txt = open(path).read()
+    out = []
+    for piece in re.findall(r"<Piece .*?</Piece>", txt, flags=re.S):
+        d = {}
+        for m in re.finditer(r'<DataArray type="(\w+)" Name="([^"]+)"(?: NumberOfComponents="(\d+)")? Format="ascii">'
+                             r'(.*?)</DataArray>', piece, flags=re.S):
+            kind, name, comps, body = m.group(1), m.group(2), m.group(3), m.group(4)
+            vals = np.array(body.split(), dtype=np.float64 if kind == "Float64" else np.int64)
+            ncomp = int(comps) if comps else 1
+            d[name] = vals.reshape(-1, ncomp) if ncomp > 1 else vals
+        out.append(d)
+    return out
+
+
 def read_vtu_cells(path):
     """The cell data arrays, points and connectivity of an ASCII .vtu file (as written by CPanel
     or by write_surface_vtu): {name: array}."""

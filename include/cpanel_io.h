@@ -8,6 +8,7 @@
  *                           VTUfile::write, CPanel/VTUfile.cpp:20-147
  *   cpg_write_wake_vtu      cpCase::writeWakeData, CPanel/cpCase.cpp:883-907
  *   cpg_write_volume_vtu    cpCase::writeVolMeshData, CPanel/cpCase.cpp:979-1004
+ *   cpg_write_streamlines_vtu  cpCase::writeBodyStreamlines, CPanel/cpCase.cpp:937-977
  *
  * The text follows the reference's layout and stream formatting (the same column widths,
  * precisions and array names), so the files diff against CPanel's own.  One difference is
@@ -75,6 +76,13 @@ int cpg_write_wake_vtu(const char* path, const double* nodes, int64_t n_nodes, c
  * per cell vel (n_cells x 3) and cp (n_cells). */
 int cpg_write_volume_vtu(const char* path, const double* points, int64_t n_points, const int64_t* cells,
                          int64_t n_cells, const double* vel, const double* cp);
+
+/* Write streamlines.vtu (cpCase::writeBodyStreamlines, CPanel/cpCase.cpp:937-977; the same layout as the
+ * reference's commented-out off-body writer): one piece per line, its points with point data "Velocity"
+ * and line cells (j, j + 1).  pts, vel, counts are cpg_streamlines' outputs (n_lines x max_points x 3;
+ * the first counts[i] rows of line i are written). */
+int cpg_write_streamlines_vtu(const char* path, const double* pts, const double* vel, const int32_t* counts,
+                              int n_lines, int max_points);
 
 #ifdef __cplusplus
 }

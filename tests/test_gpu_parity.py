@@ -176,7 +176,7 @@ def test_volume_survey_matches_oracle(cg, small, tmp_path):
     assert np.allclose(d["Cp"], sv["cp"], rtol=1e-5)
 
 
-def test_streamlines_match_oracle(cg, small):
+def test_streamlines_match_oracle(cg, small, tmp_path):
     """streamline::streamline through geometry::pntVelocity around the wing (plain path): the
     library's lockstep integration, one batched panel-velocity launch per Runge-Kutta stage, against
     the oracle integrating each line alone through its own solve and panel sums.  Points agree to
@@ -195,6 +195,10 @@ def test_streamlines_match_oracle(cg, small):
         assert oe and p.shape == op.shape and len(p) >= 3
         assert np.abs(p - op).max() <= 1e-7
         assert np.abs(v - ov).max() <= 1e-7 * np.abs(ov).max()
+    from cpanel_gb300 import io
+    vtu, _ = case.writeFiles(str(tmp_path))
+    pieces = io.read_vtu_pieces(os.path.join(os.path.dirname(vtu), "streamlines.vtu"))
+    assert [len(d["Position"]) for d in pieces] == [len(p) for p, _ in lines]
 
 
 def test_case_write_files(cg, small, tmp_path):

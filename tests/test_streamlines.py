@@ -94,3 +94,24 @@ def test_errors_reach_the_caller(cg):
         cg.streamlines_field(rankine(), 1.0, STARTS, x_max=2.0, tol=0.0)
     lines, ended = cg.streamlines_field(rankine(), 1.0, np.zeros((0, 3)), x_max=2.0)
     assert lines == [] and len(ended) == 0
+
+
+def test_streamlines_vtu_round_trip(cg, tmp_path):
+    """streamlines.vtu as cpCase::writeBodyStreamlines lays it out: one piece per line, its points
+    with point data Velocity and line cells (j, j + 1), read back at the printed precision."""
+    from cpanel_gb300 import io
+    lines, _ = cg.streamlines_field(rankine(), 1.0, STARTS, x_max=2.0, tol=1e-5, max_points=2000)
+    path = str(tmp_path / "streamlines.vtu")
+    io.write_streamlines_vtu(path, lines)
+    pieces = io.read_vtu_pieces(path)
+    assert len(pieces) == len(lines)
+    for d, (p, v) in zip(pieces, lines):
+        k = len(p)
+        assert np.allclose(d["Position"], p, rtol=1e-5, atol=1e-6)
+        assert np.allclose(d["Velocity"], v, rtol=1e-5, atol=1e-6)
+        assert d["connectivity"].tolist() == [q for j in range(k - 1) for q in (j, j + 1)]
+        assert d["offsets"].tolist() == [2 * (j + 1) for j in range(k - 1)]
+        assert d["types"].tolist() == [3] * (k - 1)
+    from cpanel_gb300._lib import I32
+    bad = np.array([5], dtype=np.int32)  # more points than max_points: refused before the file is opened
+    assert cg._lib.load().cpg_write_streamlines_vtu(path.encode(), None, None, bad.ctypes.data_as(I32), 1, 2) == 1

@@ -359,7 +359,7 @@ class CpCase:
             sv = self.survey
             io.write_volume_vtu(os.path.join(sub, "volumeMesh.vtu"), sv["points"], sv["cells"], sv["velocity"],
                                 sv["cp"])
-        if self.lines is not None:
+        if getattr(self, "lines", None) is not None:
             io.write_streamlines_vtu(os.path.join(sub, "streamlines.vtu"), self.lines)
         stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
         cpout = os.path.join(directory, stem + ".CPout")

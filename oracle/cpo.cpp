@@ -1302,25 +1302,17 @@ int cpo_bicgstab(const double* A, int64_t n, const double* b, double* x, double 
     return 1;
 }
 
-int cpo_case_post(void* mp, const cpo_case_params* p, const double* mu_in, double* phi_out, double* vel_out,
-                  double* cp_out, cpo_case_result* res) {
-    Mesh& M = *(Mesh*)mp;
-    int64_t n = (int64_t)M.bPanels.size();
-    V3 Vinf;
-    double T[3][3];
-    windToBody(p->V, p->alpha, p->beta, Vinf, T);
-    double PG = std::sqrt(1 - std::pow(p->mach, 2));
-    std::vector<double> mu(mu_in, mu_in + n), phi(n);
-    // setMu / setPotential, cpCase.cpp:203-212; panel.cpp:106-111
-    for (int64_t i = 0; i < n; i++) phi[i] = dot(Vinf, M.body[M.bPanels[i]].center) - mu[i];
-    std::vector<double> wmu(M.wPanels.size());
-    for (size_t j = 0; j < M.wPanels.size(); j++) {  // wakePanel::setMu, wakePanel.cpp:94-100
-        int idx[4];
-        double c;
-        interpPanels(M, M.wPanels[j], idx, c);
-        wmu[j] = (1 - c) * mu[idx[0]] + (c - 1) * mu[idx[1]] + c * mu[idx[2]] - c * mu[idx[3]];
-    }
-    // compVelocity, cpCase.cpp:342-365
+}  // extern "C"
+
+namespace {
+
+/* The surface pass of cpCase::compVelocity (CPanel/cpCase.cpp:342-365) and of the steady
+ * branch of cpCaseVP::compVelocity (CPanel/cpCaseVP.cpp:370-393): CHTLS velocity from the
+ * panel potentials (bodyPanel::pntVelocity, bodyPanel.cpp:490-522), Cp against V, forces
+ * and moments.  Fills Fbody, Fwind and CM of res. */
+void surfacePost(Mesh& M, const std::vector<double>& phi, V3 Vinf, const double T[3][3], const cpo_case_params* p,
+                 double PG, double* vel_out, double* cp_out, cpo_case_result* res) {
+    const int64_t n = (int64_t)M.bPanels.size();
     V3 F{0, 0, 0}, CM{0, 0, 0};
     V3 cg{p->cg[0], p->cg[1], p->cg[2]};
     for (int64_t i = 0; i < n; i++) {
@@ -1348,11 +1340,37 @@ int cpo_case_post(void* mp, const cpo_case_params* p, const double* mu_in, doubl
         CM.y += mom.y / (p->Sref * p->cref);
         CM.z += mom.z / (p->Sref * p->bref);
     }
-    if (phi_out)
-        for (int64_t i = 0; i < n; i++) phi_out[i] = phi[i];
     res->Fbody[0] = F.x; res->Fbody[1] = F.y; res->Fbody[2] = F.z;
     for (int r = 0; r < 3; r++) res->Fwind[r] = T[0][r] * F.x + T[1][r] * F.y + T[2][r] * F.z;
     res->CM[0] = CM.x; res->CM[1] = CM.y; res->CM[2] = CM.z;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cpo_case_post(void* mp, const cpo_case_params* p, const double* mu_in, double* phi_out, double* vel_out,
+                  double* cp_out, cpo_case_result* res) {
+    Mesh& M = *(Mesh*)mp;
+    int64_t n = (int64_t)M.bPanels.size();
+    V3 Vinf;
+    double T[3][3];
+    windToBody(p->V, p->alpha, p->beta, Vinf, T);
+    double PG = std::sqrt(1 - std::pow(p->mach, 2));
+    std::vector<double> mu(mu_in, mu_in + n), phi(n);
+    // setMu / setPotential, cpCase.cpp:203-212; panel.cpp:106-111
+    for (int64_t i = 0; i < n; i++) phi[i] = dot(Vinf, M.body[M.bPanels[i]].center) - mu[i];
+    std::vector<double> wmu(M.wPanels.size());
+    for (size_t j = 0; j < M.wPanels.size(); j++) {  // wakePanel::setMu, wakePanel.cpp:94-100
+        int idx[4];
+        double c;
+        interpPanels(M, M.wPanels[j], idx, c);
+        wmu[j] = (1 - c) * mu[idx[0]] + (c - 1) * mu[idx[1]] + c * mu[idx[2]] - c * mu[idx[3]];
+    }
+    // compVelocity, cpCase.cpp:342-365
+    surfacePost(M, phi, Vinf, T, p, PG, vel_out, cp_out, res);
+    if (phi_out)
+        for (int64_t i = 0; i < n; i++) phi_out[i] = phi[i];
     // trefftzPlaneAnalysis, cpCase.cpp:541-552
     WakeEval pot{M, wmu};
     double CL = 0, CD = 0;

@@ -67,10 +67,12 @@ def lib():
         L.cpo_vpcase_matrices.argtypes = [C.c_void_p, D, D, D]
         L.cpo_vpcase_set_refs.argtypes = [C.c_void_p, C.c_double, C.c_double]
         L.cpo_vpcase_trefftz.argtypes = [C.c_void_p, D]
+        L.cpo_vpcase_trefftz_row.argtypes = [C.c_void_p, C.c_int, D]
         L.cpo_vpcase_step.restype = C.c_int
         L.cpo_vpcase_step.argtypes = [C.c_void_p]
         L.cpo_vpcase_particles.argtypes = [C.c_void_p, D, D, D, I32, I32]
         L.cpo_vpcase_strengths.argtypes = [C.c_void_p, D, D, D, D]
+        L.cpo_vpcase_surface.argtypes = [C.c_void_p, D, C.c_double, C.c_double, D, D, D, D]
         L.cpo_panels_stretching.argtypes = [D, D, D, C.c_int64, D, D, C.c_int64, D, D, C.c_int64, D]
         L.cpo_vp_direct_velocity.argtypes = [D, D, D, C.c_int64, D, C.c_int64, C.c_int, D]
         L.cpo_vp_direct_stretch.argtypes = [D, D, D, C.c_int64, D]
@@ -447,9 +449,11 @@ class VPCase:
             raise ValueError("mesh has wake panels; the vortex-particle case builds its own")
         L.cpo_vpcase_set_refs(self.h, Sref, mach)
 
-    def trefftz(self):
+    def trefftz(self, row=0):
+        """Trefftz-plane CL, CD of the current state; row > 0 integrates over the particles
+        shed at that step in place of the reference's row."""
         out = np.zeros(3)
-        lib().cpo_vpcase_trefftz(self.h, _p(out))
+        lib().cpo_vpcase_trefftz_row(self.h, int(row), _p(out))
         return dict(CL=out[0], CD=out[1], converged=bool(out[2]))
 
     def __del__(self):
@@ -502,3 +506,12 @@ class VPCase:
         m1, m2 = np.zeros(i["n_w1"]), np.zeros(i["n_w2"])
         lib().cpo_vpcase_strengths(self.h, _p(sg), _p(mu), _p(m1), _p(m2))
         return dict(sigma=sg, mu=mu, mu_w1=m1, mu_w2=m2)
+
+    def surface(self, cg=(0.0, 0.0, 0.0), bref=1.0, cref=1.0):
+        """cpCaseVP::compVelocity on the current state: phi, V, Cp per panel and the body,
+        wind and moment coefficients."""
+        n = self.info()["n_body"]
+        phi, vel, cp, f = np.zeros(n), np.zeros((n, 3)), np.zeros(n), np.zeros(9)
+        cgv = np.ascontiguousarray(cg, dtype=np.float64)
+        lib().cpo_vpcase_surface(self.h, _p(cgv), bref, cref, _p(phi), _p(vel), _p(cp), _p(f))
+        return dict(phi=phi, vel=vel, cp=cp, Fbody=f[0:3], Fwind=f[3:6], CM=f[6:9])

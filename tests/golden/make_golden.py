@@ -103,8 +103,75 @@ def main_4412wake():
     print("wrote case4412_wake.npz", con.shape)
 
 
+def read_cpin(path):
+    """The numeric settings of a .CPin file: single values by key, and the first value of
+    the list-valued case blocks (Velocity, Angle_of_Attack, Angle_of_Sideslip, Mach_Number)."""
+    lines = [ln.strip() for ln in open(path).read().splitlines()]
+    out = {}
+    for ln in lines:
+        m = re.match(r"(\w+) =\s*(\S+)$", ln)
+        if m:
+            try:
+                out[m.group(1)] = float(m.group(2))
+            except ValueError:
+                pass
+    for i, ln in enumerate(lines):
+        key = ln.split(" ")[0]
+        if key in ("Velocity", "Angle_of_Attack", "Angle_of_Sideslip", "Mach_Number") and i + 2 < len(lines):
+            out[key] = float(lines[i + 2])
+        if key in ("Vortex_Particle_Wake", "Accelerate_Code", "Time_Step", "Number_of_Timesteps", "Unsteady_Mode",
+                   "Stability_Derivatives") and i + 1 < len(lines):
+            out[key] = float(lines[i + 1])
+    return out
+
+
+STEADY_PART_STEPS = (3, 4, 5, 10, 20, 40)  # particle states kept (positions, strengths)
+STEADY_BODY_STEPS = (1, 2, 3, 10, 40)      # body doublet and source strengths kept
+
+
+def main_steadytest():
+    case = os.path.join(REF, "Connor Cases", "steadyTest")
+    if not os.path.isdir(case):
+        sys.exit("reference case folder not found: %s" % case)
+    nodes, tris, ids = read_tri(os.path.join(case, "steadyTest.tri"))
+    cpin = read_cpin(os.path.join(case, "steadyTest.CPin"))
+    cp = read_cpout(os.path.join(case, "steadyTest.CPout"))
+    res = os.path.join(case, "V1_Mach0.1_alpha10_beta0")
+    nsteps = int(cpin["Number_of_Timesteps"])
+    counts, arrays = [], {}
+    for s in range(1, nsteps + 1):
+        v = read_vtu_arrays(os.path.join(res, "particleData-%d.vtu" % s))
+        shed = v.get("Time Step Shed", np.zeros(0))
+        counts.append(len(shed))
+        if s in STEADY_PART_STEPS:
+            arrays["part_pos_%d" % s] = v["Position"].astype(np.float32)
+            arrays["part_str_%d" % s] = v["Strength"].astype(np.float32)
+        if s == nsteps:
+            arrays["shed_step"] = shed.astype(np.int16)
+    for s in STEADY_BODY_STEPS:
+        v = read_vtu_arrays(os.path.join(res, "surfaceData-%d.vtu" % s))
+        arrays["mu_%d" % s] = v["Doublet Strengths"].astype(np.float32)
+        arrays["sigma_%d" % s] = v["Source Strengths"].astype(np.float32)
+    v = read_vtu_arrays(os.path.join(res, "surfaceData-%d.vtu" % nsteps))
+    arrays.update(cp_final=v["Cp"].astype(np.float32), vel_final=v["Velocity"].astype(np.float32),
+                  phi_final=v["Velocity Potential"].astype(np.float32))
+    np.savez_compressed(
+        os.path.join(HERE, "steadyTest.npz"),
+        nodes=nodes, tris=tris.astype(np.int32), ids=ids, n_particles=np.array(counts, dtype=np.int32),
+        part_steps=np.array(STEADY_PART_STEPS), body_steps=np.array(STEADY_BODY_STEPS),
+        CL=cp["CL"], CDi=cp["CDi"], body_CN_CA_CY=np.array(cp["body_CN_CA_CY"]),
+        wind_CL_CD_CY=np.array(cp["wind_CL_CD_CY"]), Cm_Cl_Cn=np.array(cp["Cm_Cl_Cn"]),
+        V=cpin["Velocity"], alpha=cpin["Angle_of_Attack"], beta=cpin["Angle_of_Sideslip"], mach=cpin["Mach_Number"],
+        Sref=cpin["S_ref"], bref=cpin["b_ref"], cref=cpin["c_ref"],
+        cg=np.array([cpin["X_cg"], cpin["Y_cg"], cpin["Z_cg"]]), accelerate=int(cpin["Accelerate_Code"]),
+        dt=cpin["Time_Step"], steps=nsteps, **arrays)
+    print("wrote steadyTest.npz", nodes.shape, tris.shape, cp, cpin, counts[-1])
+
+
 def main():
-    which = sys.argv[1:] or ["4412", "4412wake", "4412AR6"]
+    which = sys.argv[1:] or ["4412", "4412wake", "4412AR6", "steadyTest"]
+    if "steadyTest" in which:
+        main_steadytest()
     if "4412AR6" in which:
         main_4412ar6()
     if "4412wake" in which:

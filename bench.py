@@ -625,7 +625,7 @@ def main():
     a_l, a_ms = prof["assembly"]
     if a_l:
         # near pairs in FP64: per pair 3 edges x (~101 flop + 5 sqrt + 2 div + atan2 + log) + 20
-        # flop + sqrt + div; transcendentals counted as one op each (op model in the design doc)
+        # flop + sqrt + div; transcendentals counted as one op each
         fl = stats["n_near"] * (3 * (101 + 5 + 2 + 2) + 22)
         ach = fl / (a_ms / a_l * 1e-3) / 1e12
         roofs["assembly"] = {"bound": "fp64", "kernel": "k_assemble_mixed (FP64 near field, df32 far field)",

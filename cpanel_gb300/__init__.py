@@ -199,7 +199,8 @@ def solve_cases(geom, flows, Sref=1.0, bref=1.0, cref=1.0, cg=(0.0, 0.0, 0.0), p
     fl = (_lib.Flow * k)(*[_lib.Flow(*f) for f in flows])
     refs = _lib.Refs(Sref, bref, cref, (C.c_double * 3)(*cg))
     n = geom.n
-    want = want or ("mu", "sigma", "phi", "vel", "cp")
+    # want=None: every per-panel output; an empty tuple: none (coefficients only)
+    want = ("mu", "sigma", "phi", "vel", "cp") if want is None else tuple(want)
     out = {name: np.zeros((k, n)) for name in ("mu", "sigma", "phi", "cp") if name in want}
     if "vel" in want:
         out["vel"] = np.zeros((k, n, 3))
@@ -337,8 +338,9 @@ class CpCase:
     def writeFiles(self, directory=".", geom_file=""):
         """cpCase::writeFiles (CPanel/cpCase.cpp:667-709): the case directory
         V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, wakeData.vtu (when
-        the mesh has wake panels), volumeMesh.vtu (after volumeSurvey), streamlines.vtu (after
-        streamlines), and
+        the mesh has wake panels), volumeMesh.vtu (after volumeSurvey), OffBodyStreamlines.vtu
+        (after streamlines; the reference's name for off-body lines, CPanel/cpCase.cpp:626, where
+        streamlines.vtu holds its surface streamlines), and
         caseMgr::writeSummary's .CPout (CPanel/CPanelMgr.cpp:89-116) beside it.  Returns the paths
         of surfaceData.vtu and the .CPout."""
         from . import io
@@ -360,7 +362,7 @@ class CpCase:
             io.write_volume_vtu(os.path.join(sub, "volumeMesh.vtu"), sv["points"], sv["cells"], sv["velocity"],
                                 sv["cp"])
         if getattr(self, "lines", None) is not None:
-            io.write_streamlines_vtu(os.path.join(sub, "streamlines.vtu"), self.lines)
+            io.write_streamlines_vtu(os.path.join(sub, "OffBodyStreamlines.vtu"), self.lines)
         stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
         cpout = os.path.join(directory, stem + ".CPout")
         io.write_cpout(cpout, [dict(V=V, alpha=alpha, beta=beta, mach=mach, CL=self.getCL(), CDi=self.getCD(),

@@ -71,7 +71,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_ptree_set_precision", "cpg_set_particle_precision", "cpg_particles_velocity", "cpg_particles_stretch_diff",
            "cpg_panels_velocity", "cpg_panels_stretching", "cpg_vp_topology", "cpg_vpcase_create",
            "cpg_vpcase_destroy", "cpg_vpcase_info_get", "cpg_vpcase_step", "cpg_vpcase_trefftz", "cpg_vpcase_velocities", "cpg_vpcase_particles",
-           "cpg_vpcase_strengths", "cpg_vpcase_wake", "cpg_vpcase_matrices",
+           "cpg_vpcase_strengths", "cpg_vpcase_surface", "cpg_vpcase_wake", "cpg_vpcase_matrices",
            # cpanel_serve.h
            "cpg_server_create", "cpg_server_destroy", "cpg_server_submit", "cpg_server_wait", "cpg_server_footprint",
            "cpg_server_submit_vp", "cpg_server_wait_vp", "cpg_server_footprint_vp",
@@ -238,6 +238,7 @@ def load():
     L.cpg_vpcase_velocities.argtypes = [vp, C.c_int, C.c_int, D]
     L.cpg_vpcase_particles.argtypes = [vp, D, D, D, I32, I32]
     L.cpg_vpcase_strengths.argtypes = [vp, D, D, D, D]
+    L.cpg_vpcase_surface.argtypes = [vp, D, C.c_double, C.c_double, D, D, D, D]
     L.cpg_vpcase_wake.argtypes = [vp, D, D]
     L.cpg_vpcase_matrices.argtypes = [vp, D, D, D]
     L.cpg_panels_velocity.argtypes = [vp, vp, vp, vp, C.c_int64, vp, vp, C.c_int64, vp, C.c_int64, vp]

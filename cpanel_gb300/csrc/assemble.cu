@@ -829,6 +829,8 @@ extern "C" int cpg_set_inf_coeff_noalloc(const double* body_verts, int64_t n, co
                                          double* A, double* B, void* stream) {
     if (n < 1 || nw < 0 || n + nw > kNoAllocMaxPanels) return CPG_E_INVALID;
     if (!body_verts || !A || !B || (nw > 0 && (!wake_verts || !wake_idx4 || !wake_coef))) return CPG_E_INVALID;
+    // an error left by earlier work is not this call's: report it without clearing it
+    if (cudaPeekAtLastError() != cudaSuccess) return CPG_E_CUDA;
     cudaStream_t s = (cudaStream_t)stream;
     double* rec = nullptr;
     if (noalloc_scratch(&rec) != cudaSuccess) return CPG_E_CUDA;

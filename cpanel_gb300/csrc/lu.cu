@@ -520,23 +520,11 @@ void set_attrs() {
                    });
 }
 
-// GEMM arithmetic of the factorization: BF16x9 emulation of FP32 on the tensor cores by
-// default; CPG_LU_GEMM=sgemm (FP32 SIMT), tf32 or bf16 (one tensor-core pass, fewer
-// correct bits: the refinement then takes more passes) for comparison.
-cublasComputeType_t lu_compute() {
-    const char* e = std::getenv("CPG_LU_GEMM");
-    if (e && std::string(e) == "sgemm") return CUBLAS_COMPUTE_32F;
-    if (e && std::string(e) == "tf32") return CUBLAS_COMPUTE_32F_FAST_TF32;
-    if (e && std::string(e) == "bf16") return CUBLAS_COMPUTE_32F_FAST_16BF;
-    return CUBLAS_COMPUTE_32F_EMULATED_16BFX9;
-}
-// the panel-sized GEMMs (inner dimension 128): FP32 SIMT by default (one kernel each,
-// where the BF16x9 emulation launches three); CPG_LU_SMALL=bf16x9 for the emulation
-cublasComputeType_t lu_compute_small() {
-    const char* e = std::getenv("CPG_LU_SMALL");
-    if (e && std::string(e) == "bf16x9") return lu_compute();
-    return CUBLAS_COMPUTE_32F;
-}
+// GEMM arithmetic of the factorization: the rank-OB updates in the BF16x9 emulation of FP32
+// on the tensor cores; the panel-sized GEMMs (inner dimension 128) in FP32 on the CUDA cores
+// (one kernel each, where the emulation launches three)
+cublasComputeType_t lu_compute() { return CUBLAS_COMPUTE_32F_EMULATED_16BFX9; }
+cublasComputeType_t lu_compute_small() { return CUBLAS_COMPUTE_32F; }
 
 }  // namespace
 
@@ -614,17 +602,13 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
 // runs.  (Measured: about 1 ms of 56 on the 19k wing.  cuBLAS's large GEMM holds every
 // SM until it ends, and keeping 8-32 SMs out of it for the panel measured 0.6-5 ms
 // slower.)
-// outer panel width: OB_BLOCKS inner blocks (CPG_LU_OUTER overrides, 1..16).  The lockstep
-// factorization of many matrices uses OB_BLOCKS_BATCHED: its rank-128 panel updates run in
-// FP32 on the CUDA cores and its rank-OB updates on the tensor cores, and on the 64-wing
-// batch 512 columns measured 220 ms against 269 ms for 1,024 (256: 224 ms; 2,048: 379 ms).
+// outer panel width: OB_BLOCKS inner blocks.  The lockstep factorization of many matrices
+// uses OB_BLOCKS_BATCHED: its rank-128 panel updates run in FP32 on the CUDA cores and its
+// rank-OB updates on the tensor cores, and on the 64-wing batch 512 columns measured 220 ms
+// against 269 ms for 1,024 (256: 224 ms; 2,048: 379 ms).
 constexpr int OB_BLOCKS = 8;
 constexpr int OB_BLOCKS_BATCHED = 4;
-int64_t outer_width(int def_blocks = OB_BLOCKS) {
-    const char* e = std::getenv("CPG_LU_OUTER");
-    int k = e ? std::atoi(e) : def_blocks;
-    return (int64_t)NB * (k >= 1 && k <= 16 ? k : def_blocks);
-}
+int64_t outer_width(int blocks = OB_BLOCKS) { return (int64_t)NB * blocks; }
 
 struct Streams {  // where the next cuBLAS calls go
     cublasHandle_t h;

@@ -253,7 +253,7 @@ void chtls_1d(const double* dx, int nf, int order, double* F) {
 }
 
 std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, const int32_t* ids, int64_t nt,
-                       HostMesh& out) {
+                       HostMesh& out, const int32_t* te_upper, const int32_t* te_lower, int64_t n_te) {
     if (nn <= 0 || nt <= 0) return "empty mesh";
     Builder B;
     B.P.resize(nn);
@@ -419,6 +419,16 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
     for (int w : order)
         for (int p : B.wakes[w].pans) wp.push_back(p);
     for (size_t i = 0; i < bp.size(); i++) B.pan[bp[i]].index = (int)i;
+    // trailing-edge parents given by the caller (matrix indices): a wake built outside the
+    // .tri file, such as the vortex-particle buffer wake, flags them as
+    // wakePanel::setParentPanels does (CPanel/wakePanel.cpp:120-152) before the clusters
+    for (int64_t q = 0; q < n_te; q++) {
+        if (te_upper[q] < 0 || te_upper[q] >= (int64_t)bp.size() || te_lower[q] < 0 ||
+            te_lower[q] >= (int64_t)bp.size())
+            return "trailing-edge parent outside the body panels";
+        B.pan[bp[te_upper[q]]].upper = true;
+        B.pan[bp[te_lower[q]]].lower = true;
+    }
     for (int w : order)
         if (B.wakes[w].lines.size() < 2) return "a wake has fewer than two trailing-edge wake lines";
 

@@ -54,9 +54,12 @@ struct HostMesh {
     std::vector<double> tz_pts;        // all sample points, 3 per point
 };
 
-// Returns "" on success, else an error message.  tris are 1-based.
+// Returns "" on success, else an error message.  tris are 1-based.  te_upper/te_lower
+// (n_te matrix indices, optional) flag the upper and lower parents of trailing edges whose
+// wake is not in the file (the vortex-particle buffer wake) before the CHTLS clusters grow.
 std::string build_mesh(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
-                       int64_t n_tris, HostMesh& out);
+                       int64_t n_tris, HostMesh& out, const int32_t* te_upper = nullptr,
+                       const int32_t* te_lower = nullptr, int64_t n_te = 0);
 
 // chtlsnd first-derivative weights (unconstrained branch, CPanel/chtlsnd.cpp:20-140,
 // 189-196) for a 1-D set of offsets, used for the Trefftz-plane downwash.

@@ -271,12 +271,14 @@ __global__ void __launch_bounds__(32 * WPB) k_chtls(cpg::PostTables T) {
     if (lane == 0) T.mode[p] = mode;
 }
 
-// Per (panel, case): phi, velocity, Cp and per-block force partials.
+// Per (panel, case): phi, velocity, Cp and per-block force partials.  The potential of panel
+// j is V.c_j - mu_j with V the case's free stream, or, when onset is given (n x 3, one case),
+// the onset velocity at that panel (the vortex-particle case's VinfPlusVecPot).
 constexpr int PT = 128;
 __global__ void __launch_bounds__(PT) k_velocity(cpg::PostTables T, int k, const cpg::CaseScalars* __restrict__ CS,
-                                                 const double* __restrict__ mu, double* __restrict__ phi_out,
-                                                 double* __restrict__ vel_out, double* __restrict__ cp_out,
-                                                 double* __restrict__ fpart) {
+                                                 const double* __restrict__ mu, const double* __restrict__ onset,
+                                                 double* __restrict__ phi_out, double* __restrict__ vel_out,
+                                                 double* __restrict__ cp_out, double* __restrict__ fpart) {
     __shared__ double red[9][PT / 32];
     int c = blockIdx.y;
     int64_t i = (int64_t)blockIdx.x * PT + threadIdx.x;
@@ -287,7 +289,8 @@ __global__ void __launch_bounds__(PT) k_velocity(cpg::PostTables T, int k, const
         const double* mc = mu + (int64_t)c * T.n;
         const double* rp = T.rec + i * R_STRIDE;
         dv3 ci = ld3(rp + R_C);
-        double phii = dot3(Vinf, ci) - mc[i];  // panel::setPotential, CPanel/panel.cpp:106-111
+        // panel::setPotential, CPanel/panel.cpp:106-111
+        double phii = dot3(onset ? ld3(onset + 3 * i) : Vinf, ci) - mc[i];
         int c0 = T.cl_ptr[i], nf = T.cl_ptr[i + 1] - c0 - 1;
         int mode = T.mode[i];
         bool tip = (mode & 4) != 0;
@@ -298,7 +301,8 @@ __global__ void __launch_bounds__(PT) k_velocity(cpg::PostTables T, int k, const
             double v[3] = {0, 0, 0};
             for (int q = 0; q < nf; q++) {
                 int j = T.cl_idx[c0 + 1 + q];
-                double df = (dot3(Vinf, ld3(T.rec + (int64_t)j * R_STRIDE + R_C)) - mc[j]) - phii;
+                double df = (dot3(onset ? ld3(onset + 3 * j) : Vinf, ld3(T.rec + (int64_t)j * R_STRIDE + R_C)) -
+                             mc[j]) - phii;
                 v[0] += F[q] * df;
                 v[1] += F[NF + q] * df;
                 v[2] += F[2 * NF + q] * df;
@@ -311,7 +315,8 @@ __global__ void __launch_bounds__(PT) k_velocity(cpg::PostTables T, int k, const
             double v[2] = {0, 0};
             for (int q = 0; q < nf; q++) {
                 int j = T.cl_idx[c0 + 1 + q];
-                double df = (dot3(Vinf, ld3(T.rec + (int64_t)j * R_STRIDE + R_C)) - mc[j]) - phii;
+                double df = (dot3(onset ? ld3(onset + 3 * j) : Vinf, ld3(T.rec + (int64_t)j * R_STRIDE + R_C)) -
+                             mc[j]) - phii;
                 v[0] += F[q] * df;
                 v[1] += F[NF + q] * df;
             }
@@ -511,9 +516,19 @@ cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs, const
     double* tz = fpart + (size_t)k * nb * 6;
     dim3 grid((unsigned)nb, (unsigned)k);
     ProfScope ps(Prof::POST, s);
-    k_velocity<<<grid, PT, 0, s>>>(t, k, cs, mu, phi, vel, cp, fpart);
+    k_velocity<<<grid, PT, 0, s>>>(t, k, cs, mu, nullptr, phi, vel, cp, fpart);
     k_forces_finish<<<(k + 31) / 32, 32, 0, s>>>(fpart, (int)nb, k, cs, forces);
     if (t.n_wakes > 0) k_trefftz<<<k, 256, 0, s>>>(t, k, cs, mu, wake_mu, tz, trefftz);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_surface(const PostTables& t, const CaseScalars* cs, const double* mu, const double* onset,
+                           double* phi, double* vel, double* cp, double* forces, void* work, cudaStream_t s) {
+    int64_t nb = (t.n + PT - 1) / PT;
+    double* fpart = (double*)work;
+    ProfScope ps(Prof::POST, s);
+    k_velocity<<<dim3((unsigned)nb, 1), PT, 0, s>>>(t, 1, cs, mu, onset, phi, vel, cp, fpart);
+    k_forces_finish<<<1, 32, 0, s>>>(fpart, (int)nb, 1, cs, forces);
     return cudaGetLastError();
 }
 

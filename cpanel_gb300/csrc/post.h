@@ -45,6 +45,12 @@ cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs_dev, c
                         double* vel, double* cp, double* forces, double* trefftz, double* wake_mu, void* work,
                         cudaStream_t s);
 
+// The surface pass alone for one case whose panel potentials come from an onset velocity
+// field (n x 3, device) instead of the free stream: phi, vel, cp as launch_post (any may be
+// null), forces 9 [Fbody Fwind CM]; work: post_work_bytes(t, 1).
+cudaError_t launch_surface(const PostTables& t, const CaseScalars* cs, const double* mu, const double* onset,
+                           double* phi, double* vel, double* cp, double* forces, void* work, cudaStream_t s);
+
 cudaError_t launch_sigma(const double* rec, int64_t n, int k, const CaseScalars* cs, double* sigma, cudaStream_t s);
 cudaError_t launch_rhs_basis(const double* rb, int64_t n, int k, const CaseScalars* cs, double* rhs, cudaStream_t s);
 // b = a (+ lo when lo is not null), FP32 -> FP64

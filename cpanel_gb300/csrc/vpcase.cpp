@@ -41,6 +41,7 @@
 #include "mesh.h"
 #include "octree.h"
 #include "particles.h"
+#include "post.h"
 #include "vpgeom.h"
 #include "vpkern.h"
 
@@ -132,6 +133,13 @@ struct cpg_vpcase {
     Buf rec, q1, q2, widx, wcoef, par, A, B, C, work;
     // device: strengths
     Buf sigma, mu, mu1, prev1, mu2, prev2, rhs, fil, vcent;
+    Buf vtot;  // onset velocity at the body centres (VinfPlusVecPot) of the last source strengths
+    // surface pass (cpCaseVP::compVelocity): CHTLS clusters of the body with the buffer wake's
+    // trailing-edge parents, weights built on the first call
+    cpg::HostMesh H;
+    cpg::PostTables PT;
+    bool post_ready = false;
+    Buf p_bez, p_clp, p_cli, p_tip, p_ts, p_F3, p_F2, p_mode, p_cs, p_work, p_out;
     // device: particles
     Buf pos, str, rad, pvel, pstr, packed, tP, tQ, tS, tD, tPan;
     // device: tree
@@ -612,8 +620,8 @@ cudaError_t step_once(cpg_vpcase& S) {
     cudaError_t e;
     const double vinf[3] = {S.vinf[0], S.vinf[1], S.vinf[2]};
     if (S.timestep == 0) {  // setSourceStrengths + solveMatrixEq
-        if ((e = cpg::vp_launch_sigma(S.rec.as<double>(), S.n, nullptr, nullptr, 0, vinf, S.sigma.as<double>(), S.s)) !=
-            cudaSuccess)
+        if ((e = cpg::vp_launch_sigma(S.rec.as<double>(), S.n, nullptr, nullptr, 0, vinf, S.sigma.as<double>(),
+                                      S.vtot.as<double>(), S.s)) != cudaSuccess)
             return e;
         if ((e = solve(S, false)) != cudaSuccess) return e;
         S.timestep = 1;
@@ -710,7 +718,8 @@ cudaError_t step_once(cpg_vpcase& S) {
             cudaSuccess)
             return e;
         if ((e = cpg::vp_launch_sigma(S.rec.as<double>(), S.n, S.vcent.as<double>(), S.fil.as<double>(),
-                                      S.have_fil ? S.n2 : 0, vinf, S.sigma.as<double>(), S.s)) != cudaSuccess)
+                                      S.have_fil ? S.n2 : 0, vinf, S.sigma.as<double>(), S.vtot.as<double>(), S.s)) !=
+            cudaSuccess)
             return e;
     }
     if ((e = solve(S, true)) != cudaSuccess) return e;
@@ -756,6 +765,17 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
     S.n1 = S.G.n_w1;
     S.n2 = S.G.n_w2;
     const int64_t n = S.n;
+    // readTri grows the CHTLS clusters after the buffer wake exists (CPanel/geometry.cpp:473-484),
+    // so its first row's trailing-edge parents bound them
+    err = cpg::build_mesh(nodes, n_nodes, tris, ids, n_tris, S.H, S.G.line_up.data(), S.G.line_lo.data(),
+                          (int64_t)S.G.line_up.size());
+    bool same = err.empty() && S.H.n_body == n;
+    for (int64_t i = 0; same && i < n * cpg::PF_STRIDE; i++) same = S.H.body[i] == S.G.body[i];
+    if (!same) {
+        cpg::ctx_set_error(ctx, err.empty() ? "surface topology disagrees with the vortex-particle geometry" : err);
+        delete Sp;
+        return CPG_E_BAD_MESH;
+    }
     auto fail_cuda = [&](cudaError_t e, const char* where) {
         cpg::ctx_set_error(ctx, std::string(where) + ": " + cudaGetErrorString(e));
         cpg_vpcase_destroy(Sp);
@@ -779,6 +799,7 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
     Buf* vec[] = {&S.sigma, &S.mu, &S.rhs};
     for (Buf* b : vec)
         if ((e = b->ensure(sizeof(double) * n, S.s)) != cudaSuccess) return fail_cuda(e, "alloc");
+    if ((e = S.vtot.ensure(sizeof(double) * 3 * n, S.s)) != cudaSuccess) return fail_cuda(e, "alloc");
     Buf* w[] = {&S.mu1, &S.prev1, &S.mu2, &S.prev2};
     for (Buf* b : w) {
         if ((e = b->ensure(sizeof(double) * std::max<int64_t>(1, std::max(S.n1, S.n2)), S.s)) != cudaSuccess)
@@ -835,7 +856,8 @@ void cpg_vpcase_destroy(cpg_vpcase* S) {
                   &S->sigma, &S->mu, &S->mu1, &S->prev1, &S->mu2, &S->prev2, &S->rhs, &S->fil, &S->vcent,
                   &S->pos, &S->str, &S->rad, &S->pvel, &S->pstr, &S->packed, &S->tP, &S->tQ, &S->tS, &S->tD,
                   &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr,
-                  &S->fnodes, &S->A32, &S->Alo, &S->LU, &S->bad, &S->Ainv};
+                  &S->fnodes, &S->A32, &S->Alo, &S->LU, &S->bad, &S->Ainv, &S->vtot, &S->p_bez, &S->p_clp,
+                  &S->p_cli, &S->p_tip, &S->p_ts, &S->p_F3, &S->p_F2, &S->p_mode, &S->p_cs, &S->p_work, &S->p_out};
     for (Buf* b : all) b->release();
     S->lug.release();
     delete S;
@@ -978,6 +1000,84 @@ int cpg_vpcase_strengths(cpg_vpcase* Sp, double* sigma, double* mu, double* mu_w
         cpg::ctx_set_error(S.ctx, std::string("strengths: ") + cudaGetErrorString(e));
         return CPG_E_CUDA;
     }
+    return CPG_OK;
+}
+
+int cpg_vpcase_surface(cpg_vpcase* Sp, const double* cg, double bref, double cref, double* phi, double* vel,
+                       double* cp, double* forces) {
+    if (!Sp || !cg || !(bref > 0) || !(cref > 0)) return CPG_E_INVALID;
+    cpg_vpcase& S = *Sp;
+    if (S.timestep < 1) {
+        cpg::ctx_set_error(S.ctx, "surface: no step taken yet");
+        return CPG_E_INVALID;
+    }
+    const int64_t n = S.n;
+    cudaError_t e = cudaSuccess;
+    auto fail = [&](const char* where) {
+        cpg::ctx_set_error(S.ctx, std::string("surface: ") + where + ": " + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? CPG_E_OOM : CPG_E_CUDA;
+    };
+    if (!S.post_ready) {  // CHTLS weights of the clusters, once
+        if ((e = up(S.p_bez, S.H.bez, S.s)) != cudaSuccess || (e = up(S.p_clp, S.H.cl_ptr, S.s)) != cudaSuccess ||
+            (e = up(S.p_cli, S.H.cl_idx, S.s)) != cudaSuccess || (e = up(S.p_tip, S.H.tip, S.s)) != cudaSuccess ||
+            (e = up(S.p_ts, S.H.tsorder, S.s)) != cudaSuccess)
+            return fail("upload");
+        if ((e = S.p_F3.ensure(sizeof(double) * n * 3 * (cpg::kClMax - 1), S.s)) != cudaSuccess ||
+            (e = S.p_F2.ensure(sizeof(double) * n * 2 * (cpg::kClMax - 1), S.s)) != cudaSuccess ||
+            (e = S.p_mode.ensure(sizeof(int32_t) * n, S.s)) != cudaSuccess)
+            return fail("alloc");
+        if ((e = cudaMemsetAsync(S.p_F2.p, 0, S.p_F2.bytes, S.s)) != cudaSuccess) return fail("clear");
+        cpg::PostTables& T = S.PT;
+        T = cpg::PostTables();
+        T.n = n;
+        T.rec = S.rec.as<double>();
+        T.bez = S.p_bez.as<double>();
+        T.cl_ptr = S.p_clp.as<int32_t>();
+        T.cl_idx = S.p_cli.as<int32_t>();
+        T.tip = S.p_tip.as<int32_t>();
+        T.tsorder = S.p_ts.as<int32_t>();
+        T.F3 = S.p_F3.as<double>();
+        T.F2 = S.p_F2.as<double>();
+        T.mode = S.p_mode.as<int32_t>();
+        if ((e = cpg::launch_chtls_weights(T, S.s)) != cudaSuccess) return fail("CHTLS weights");
+        S.post_ready = true;
+    }
+    // case scalars: cpCaseVP's free stream (steady), Vmag for Cp, the moment references
+    cpg::CaseScalars cs;
+    {
+        double a = S.alpha * (kPi / 180), b = S.beta * (kPi / 180);
+        double T[9] = {std::cos(a) * std::cos(b), std::cos(a) * std::sin(b), -std::sin(a),
+                       -std::sin(b), std::cos(b), 0,
+                       std::sin(a) * std::cos(b), std::sin(a) * std::sin(b), std::cos(a)};
+        for (int q = 0; q < 9; q++) cs.T[q] = T[q];
+        for (int q = 0; q < 3; q++) cs.Vinf[q] = S.vinf[q];
+        cs.V = S.V;
+        cs.PG = S.PG;
+        cs.Sref = S.Sref;
+        cs.bref = bref;
+        cs.cref = cref;
+        for (int q = 0; q < 3; q++) cs.cg[q] = cg[q];
+    }
+    if ((e = S.p_cs.ensure(sizeof(cs), S.s)) != cudaSuccess ||
+        (e = S.p_work.ensure(cpg::post_work_bytes(S.PT, 1), S.s)) != cudaSuccess ||
+        (e = S.p_out.ensure(sizeof(double) * (5 * n + 9), S.s)) != cudaSuccess)
+        return fail("alloc");
+    if ((e = cudaMemcpyAsync(S.p_cs.p, &cs, sizeof(cs), cudaMemcpyHostToDevice, S.s)) != cudaSuccess)
+        return fail("upload");
+    double* o = S.p_out.as<double>();
+    if ((e = cpg::launch_surface(S.PT, S.p_cs.as<cpg::CaseScalars>(), S.mu.as<double>(), S.vtot.as<double>(), o,
+                                 o + n, o + 4 * n, o + 5 * n, S.p_work.p, S.s)) != cudaSuccess)
+        return fail("surface pass");
+    if (phi && (e = cudaMemcpyAsync(phi, o, sizeof(double) * n, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
+        return fail("copy");
+    if (vel && (e = cudaMemcpyAsync(vel, o + n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
+        return fail("copy");
+    if (cp && (e = cudaMemcpyAsync(cp, o + 4 * n, sizeof(double) * n, cudaMemcpyDeviceToHost, S.s)) != cudaSuccess)
+        return fail("copy");
+    if (forces && (e = cudaMemcpyAsync(forces, o + 5 * n, sizeof(double) * 9, cudaMemcpyDeviceToHost, S.s)) !=
+                      cudaSuccess)
+        return fail("copy");
+    if ((e = cudaStreamSynchronize(S.s)) != cudaSuccess) return fail("sync");
     return CPG_OK;
 }
 

@@ -570,18 +570,30 @@ __global__ void k_vp_strength(const double* __restrict__ pos, double* __restrict
 
 // setSourceStrengthsVP, CPanel/cpCaseVP.cpp:173-202: sigma = -(Vinf + particles +
 // filaments) . n (vpart: the particle term at the centres, or null for none)
+// vtot (optional, n x 3): the same onset velocity summed as cpCaseVP::VinfPlusVecPot does
+// (CPanel/cpCaseVP.cpp:601-623: free stream, then particles, then each filament), whose dot
+// product with the centre gives the panel potential of solveVPmatrixEq
 __global__ void k_vp_sigma(const double* __restrict__ rec, int64_t n, const double* __restrict__ vpart,
-                           const double* __restrict__ fil, int64_t nf, dv3 vinf, double* __restrict__ sigma) {
+                           const double* __restrict__ fil, int64_t nf, dv3 vinf, double* __restrict__ sigma,
+                           double* __restrict__ vtot) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     dv3 c = ld3(rec + i * R_STRIDE + R_C), nn = ld3(rec + i * R_STRIDE + R_N);
     dv3 s = vpart ? ld3(vpart + 3 * i) : mk3(0, 0, 0);
+    dv3 t = vinf + s;
     for (int64_t j = 0; j < nf; j++) {
         const double* f = fil + 8 * j;
         dv3 p1 = ld3(f), p2 = ld3(f + 3);
-        s = s + (f[6] * vortex_v(c - p1, c - p2, p2 - p1)) / CPG_FOUR_PI;
+        dv3 term = (f[6] * vortex_v(c - p1, c - p2, p2 - p1)) / CPG_FOUR_PI;
+        s = s + term;
+        t = t + term;
     }
     sigma[i] = -dot3(vinf + s, nn) + 0;
+    if (vtot) {
+        vtot[3 * i] = t.x;
+        vtot[3 * i + 1] = t.y;
+        vtot[3 * i + 2] = t.z;
+    }
 }
 
 // rhs -= C mu2
@@ -699,8 +711,9 @@ cudaError_t vp_launch_strength(const double* pos, double* str, double* prevStr, 
     return cudaGetLastError();
 }
 cudaError_t vp_launch_sigma(const double* rec, int64_t n, const double* vpart, const double* fil, int64_t nf,
-                            const double vinf[3], double* sigma, cudaStream_t s) {
-    if (n > 0) k_vp_sigma<<<nblk(n, 256), 256, 0, s>>>(rec, n, vpart, fil, nf, dv3{vinf[0], vinf[1], vinf[2]}, sigma);
+                            const double vinf[3], double* sigma, double* vtot, cudaStream_t s) {
+    if (n > 0)
+        k_vp_sigma<<<nblk(n, 256), 256, 0, s>>>(rec, n, vpart, fil, nf, dv3{vinf[0], vinf[1], vinf[2]}, sigma, vtot);
     return cudaGetLastError();
 }
 cudaError_t vp_launch_rhs_c(const double* C, int64_t n, int64_t n2, const double* mu2, double* rhs, cudaStream_t s) {

@@ -32,7 +32,7 @@ cudaError_t vp_launch_strength(const double* pos, double* str, double* prevStr, 
                                const double* ddif, const double* dpan, int64_t m, double cref, double dt,
                                cudaStream_t s);
 cudaError_t vp_launch_sigma(const double* rec, int64_t n, const double* vpart, const double* fil, int64_t nf,
-                            const double vinf[3], double* sigma, cudaStream_t s);
+                            const double vinf[3], double* sigma, double* vtot, cudaStream_t s);
 cudaError_t vp_launch_rhs_c(const double* C, int64_t n, int64_t n2, const double* mu2, double* rhs, cudaStream_t s);
 cudaError_t vp_launch_wake_mu(const double* mu, const int32_t* widx, const double* wcoef, int64_t n1, double* mu1,
                               double* prev1, int keep_prev, cudaStream_t s);

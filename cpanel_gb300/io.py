@@ -141,7 +141,8 @@ def write_volume_vtu(path, points, cells, vel, cp):
 
 
 def write_streamlines_vtu(path, lines):
-    """streamlines.vtu (cpCase::writeBodyStreamlines, CPanel/cpCase.cpp:937-977): lines as
+    """A streamline file in cpCase::writeBodyStreamlines's layout (CPanel/cpCase.cpp:937-977; CpCase.writeFiles
+    writes the off-body lines as OffBodyStreamlines.vtu, the reference's name for them): lines as
     CpCase.streamlines or streamlines_field return them, [(points k x 3, velocities k x 3), ...]; one
     piece per line with point data Velocity and line cells."""
     L = _lib.load()

@@ -308,6 +308,17 @@ class VPCase:
                        "strengths")
         return dict(sigma=sg, mu=mu, mu_w1=m1, mu_w2=m2)
 
+    def surface(self, cg=(0.0, 0.0, 0.0), bref=1.0, cref=1.0):
+        """cpCaseVP::compVelocity on the current state (steady case): potential, surface
+        velocity and Cp per panel, and the body, wind and moment coefficients."""
+        n = self.info()["n_body"]
+        phi, vel, cp, f = np.zeros(n), np.zeros((n, 3)), np.zeros(n), np.zeros(9)
+        cgv = np.ascontiguousarray(cg, dtype=np.float64)
+        self.ctx.check(self.ctx.L.cpg_vpcase_surface(self.h, cgv.ctypes.data_as(_lib.D), bref, cref,
+                                                     phi.ctypes.data_as(_lib.D), vel.ctypes.data_as(_lib.D),
+                                                     cp.ctypes.data_as(_lib.D), f.ctypes.data_as(_lib.D)), "surface")
+        return dict(phi=phi, vel=vel, cp=cp, Fbody=f[0:3], Fwind=f[3:6], CM=f[6:9])
+
     def matrices(self):
         i = self.info()
         n, n2 = i["n_body"], i["n_w2"]

@@ -12,20 +12,22 @@ conventions readTri relies on:
   (panel::setGeom, CPanel/panel.cpp:53-61);
 * the trailing edge is closed (thickness coefficient -0.1036) so upper and lower
   trailing-edge nodes coincide and share one node;
-* closed tips are fan-triangulated from an added centroid node.
+* closed tips pair the upper and lower nodes of each chord station: a strip of
+  quads between consecutive stations, each split on its shorter diagonal, with one
+  triangle at the leading and one at the trailing edge (no added node).  A fan from
+  a centroid node would put long slivers (area/longSide^2 ~ 1e-3) beside the
+  cosine-clustered trailing edge, whose CHTLS fits turn 1e-10 changes of the
+  doublet strengths into Cp changes of order 0.1.
 
 Each quad between two span stations is split on one fixed diagonal.  Every wake
 trailing-edge quad sheds one flat quad of `wake_len` chords along `wake_dir`.
 
 Every node carries a seeded jitter of 1e-4 of its local spacing.  Without it the strips of an
-untwisted wing and the fan caps are exactly planar, and two reference heuristics
+untwisted wing and the caps are exactly planar, and two reference heuristics
 that real OpenVSP meshes never trip on a wing surface would fire: the on-edge
 branch of panel::vortexPhi (CPanel/panel.cpp:722-733) for exactly coplanar
 target/source pairs (doublet row sums then miss -1 by up to 0.5), and the
-tip-patch test of bodyPanel::setTipFlag (CPanel/bodyPanel.cpp:58-95).  On a fan
-cap of a thin section the tip-patch 2-D CHTLS fit sees nearly collinear sliver
-centroids and returns velocities of order 1e4; with the jitter the caps take the
-3-D fit and stay bounded.
+tip-patch test of bodyPanel::setTipFlag (CPanel/bodyPanel.cpp:58-95).
 """
 import math
 from dataclasses import dataclass
@@ -108,21 +110,13 @@ def make_wing(spec: WingSpec):
             tris.append((a, d, c))
             tris.append((a, c, b))
     n_surf = len(tris)
-    extra = []
     if spec.tips:
         for j, right in ((0, False), (S - 1, True)):
-            ring = nodes[j * R:(j + 1) * R]
-            cidx = len(nodes) + len(extra)
-            cen = ring.mean(axis=0)
-            if spec.jitter > 0:
-                h = np.linalg.norm(ring - cen, axis=1).min()
-                cen = cen + spec.jitter * h * rng.uniform(-1, 1, 3)
-            extra.append(cen)
-            for k in range(R):
-                a, b = node(j, k), node(j, k + 1)
-                tris.append((cidx, b, a) if right else (cidx, a, b))
-    if extra:
-        nodes = np.vstack([nodes, np.array(extra)])
+            for t in _cap_triangles(nodes, [node(j, k) for k in range(R)], N):
+                # outward: +y on the right tip, -y on the left
+                p0, p1, p2 = nodes[t[0]], nodes[t[1]], nodes[t[2]]
+                ny = np.cross(p1 - p0, p2 - p0)[1]
+                tris.append(t if (ny > 0) == right else (t[0], t[2], t[1]))
     n_body = len(tris)
     ids = [1] * n_body
     # wake: duplicated TE nodes then the downstream nodes (appended after body nodes)
@@ -143,6 +137,25 @@ def make_wing(spec: WingSpec):
     info = dict(n_body=n_body, n_surface=n_surf, n_wake=len(tris) - n_body, n_te=S - 1,
                 span=spec.span, area=_planform_area(spec))
     return nodes, tris, np.array(ids, dtype=np.int32), info
+
+
+def _cap_triangles(nodes, ring, N):
+    """Triangles closing one tip section: upper and lower nodes of the same chord station are
+    paired, so the cap is a strip of quads between consecutive stations (each split on its
+    shorter diagonal) with one triangle at the leading and one at the trailing edge.  ring
+    lists the section's node indices from the trailing edge over the upper side to the
+    leading edge (position N - 1) and back over the lower side."""
+    up = [ring[N - 1 - i] for i in range(N)]               # chord station i, 0 = leading edge
+    lo = [ring[N - 1]] + [ring[N - 1 + i] for i in range(1, N - 1)] + [ring[0]]
+    out = [(up[0], up[1], lo[1])]
+    for i in range(1, N - 2):
+        a, b, c, d = up[i], up[i + 1], lo[i + 1], lo[i]
+        if np.linalg.norm(nodes[a] - nodes[c]) <= np.linalg.norm(nodes[b] - nodes[d]):
+            out += [(a, b, c), (a, c, d)]
+        else:
+            out += [(a, b, d), (b, c, d)]
+    out.append((up[N - 2], up[N - 1], lo[N - 2]))
+    return out
 
 
 def _planform_area(spec):
@@ -184,7 +197,7 @@ def config_random(seed):
     for _ in range(100):
         nc = int(rng.integers(20, 101))
         ns = int(rng.integers(15, 61))
-        ntri = 4 * (nc - 1) * (ns - 1) + 4 * (nc - 1)
+        ntri = 4 * (nc - 1) * (ns - 1) + 2 * (2 * nc - 4)
         if 1000 <= ntri <= 12000:
             break
     span = ar * 1.0 * (1 + taper) / 2

@@ -149,6 +149,10 @@ int  cpg_get_B(cpg_geometry* g, double* host);
  * Inputs and outputs are caller-owned DEVICE arrays in matrix order: body_verts
  * n x 9, wake_verts nw x 9 (wPanels order), wake_idx4 nw x 4 and wake_coef nw (the
  * tables cpg_geometry_tables / cpg_topology return), A and B n x n column-major.
+ * Every wake_idx4 entry must lie in [0, n): the kernels index columns of A with them
+ * unchecked, as the geometry's own tables always satisfy.
+ * A CUDA error already pending on the calling thread when the call starts is returned as
+ * CPG_E_CUDA before anything is queued, and left pending for the caller to read.
  * The packed panel records live in a fixed per-device array of 16,384 panels
  * (n + nw <= 16384; larger sizes return CPG_E_INVALID, about 3 MB held by every GPU
  * that loads the library).  The first call on a device looks the array's address
@@ -196,7 +200,9 @@ int  cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu,
  * Every step start is recorded with its velocity: pts and vel are n_lines x max_points x 3, line i's
  * points first; counts[i] is the number recorded; ended[i] is 1 where the line stopped as the
  * reference's loop stops (x >= x_max, or x no longer a number) and 0 where max_points cut it short.
- * All lines advance together: each of the six stages evaluates every live line's stage point in
+ * Treat a line with ended 0 as truncated: its last point starts a step that was not taken.  The
+ * reference has no such cap (a line that never reaches x_max, at a stagnation point for one, keeps
+ * stepping there).  All lines advance together: each of the six stages evaluates every live line's stage point in
  * one batched panel-velocity launch. */
 int  cpg_streamlines(cpg_geometry* g, const double* sigma, const double* mu, const cpg_flow* flow,
                      const double* starts, int n_lines, double x_max, double tol, int max_points, double* pts,

@@ -31,6 +31,7 @@
  *                              at a time, with the Trefftz-plane early stop
  *                              (cpCaseVP::solutionConvergence, CPanel/cpCaseVP.cpp:204-229;
  *                              wake::trefftzPlaneVP, CPanel/wake.cpp:191-361)
+ *   cpg_vpcase_surface         cpCaseVP::compVelocity, CPanel/cpCaseVP.cpp:370-393
  */
 #ifndef CPANEL_VP_H
 #define CPANEL_VP_H
@@ -178,6 +179,16 @@ int  cpg_vpcase_velocities(cpg_vpcase* c, int precision, int direct, double* vel
 int  cpg_vpcase_particles(cpg_vpcase* c, double* pos, double* strength, double* radius, int32_t* shed_time,
                           int32_t* parent);
 int  cpg_vpcase_strengths(cpg_vpcase* c, double* sigma, double* mu, double* mu_w1, double* mu_w2);
+/* cpCaseVP::compVelocity of a steady case (CPanel/cpCaseVP.cpp:370-393) on the current state:
+ * the panel potentials solveVPmatrixEq sets, (Vinf + particle + filament velocity at the
+ * centre) . centre - mu (cpCaseVP::VinfPlusVecPot, :601-623), give the CHTLS surface velocity
+ * (x divided by the Prandtl-Glauert factor), Cp = 1 - (|V| / V)^2 and the surface-integrated
+ * coefficients.  The clusters are those readTri grows after the buffer wake exists
+ * (CPanel/geometry.cpp:473-484).  Host outputs, any may be null: phi (n), vel (n x 3), cp (n),
+ * forces (9: Fbody, Fwind, CM about cg with bref, cref; Sref of the case).  At least one step
+ * must have been taken. */
+int  cpg_vpcase_surface(cpg_vpcase* c, const double* cg, double bref, double cref, double* phi, double* vel,
+                        double* cp, double* forces);
 /* buffer-wake quadrilaterals (n_w1 x 12, n_w2 x 12 doubles) */
 int  cpg_vpcase_wake(const cpg_vpcase* c, double* w1_verts, double* w2_verts);
 /* A, B (n x n) and C (n x n_w2), column-major, host */

@@ -197,7 +197,7 @@ def test_streamlines_match_oracle(cg, small, tmp_path):
         assert np.abs(v - ov).max() <= 1e-7 * np.abs(ov).max()
     from cpanel_gb300 import io
     vtu, _ = case.writeFiles(str(tmp_path))
-    pieces = io.read_vtu_pieces(os.path.join(os.path.dirname(vtu), "streamlines.vtu"))
+    pieces = io.read_vtu_pieces(os.path.join(os.path.dirname(vtu), "OffBodyStreamlines.vtu"))
     assert [len(d["Position"]) for d in pieces] == [len(p) for p, _ in lines]
 
 

@@ -89,7 +89,8 @@ def test_bad_mesh_is_reported(built):
 def test_generator_counts_match_the_workloads():
     from cpanel_gb300 import wing
     n1 = wing.make_wing(wing.config_small_steady())[3]
-    assert n1["n_surface"] == 4 * 39 * 24 and n1["n_body"] == 3900 and n1["n_wake"] == 48
+    # 3,744 surface triangles and two paired tip caps of 2 x (2 x 40 - 4) / 2 triangles each
+    assert n1["n_surface"] == 4 * 39 * 24 and n1["n_body"] == 3744 + 2 * (2 * 40 - 4) and n1["n_wake"] == 48
     n2 = wing.make_wing(wing.config_multi_rhs())[3]
     assert 19000 <= n2["n_body"] <= 19400
     for s in range(8):

@@ -24,11 +24,12 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 FIX = os.path.join(HERE, "golden", "steadyTest.npz")
 
 
-def printed_match(ours, ref, rel=5e-6):
+def printed_match(ours, ref, rel=5e-6, slack=0.0):
     """|ours - ref| within half a unit in the 6th significant digit of ref (float32 storage of
-    the fixture adds 6e-8 relative; 1e-12 absolute covers printed zeros)."""
+    the fixture adds 6e-8 relative; 1e-12 absolute covers printed zeros), plus slack x max|ref|
+    (a reduced-precision form's own error, relative to the array's largest value)."""
     ours, ref = np.asarray(ours, dtype=np.float64), np.asarray(ref, dtype=np.float64)
-    tol = rel * 1.02 * np.abs(ref) + 1e-12
+    tol = rel * 1.02 * np.abs(ref) + 1e-12 + slack * np.abs(ref).max()
     return np.abs(ours - ref) <= tol
 
 
@@ -57,7 +58,7 @@ def oracle_case(fix):
                      mach=float(fix["mach"]))
 
 
-def check_against_fixture(run, fix):
+def check_against_fixture(run, fix, slack=0.0):
     # shedding: particle count after every step and the shedding step of every particle, exact
     assert run["counts"] == [int(c) for c in fix["n_particles"]]
     last = run["part_%d" % int(fix["steps"])]
@@ -65,25 +66,25 @@ def check_against_fixture(run, fix):
     # particle positions and strengths after the kept steps
     for s in fix["part_steps"]:
         p = run["part_%d" % s]
-        assert printed_match(p["pos"], fix["part_pos_%d" % s]).all(), "positions at step %d" % s
-        assert printed_match(p["strength"], fix["part_str_%d" % s]).all(), "strengths at step %d" % s
+        assert printed_match(p["pos"], fix["part_pos_%d" % s], slack=slack).all(), "positions at step %d" % s
+        assert printed_match(p["strength"], fix["part_str_%d" % s], slack=slack).all(), "strengths at step %d" % s
     # body doublet and source strengths after the kept steps
     for s in fix["body_steps"]:
         b = run["body_%d" % s]
-        assert printed_match(b["mu"], fix["mu_%d" % s]).all(), "doublets at step %d" % s
-        assert printed_match(b["sigma"], fix["sigma_%d" % s]).all(), "sources at step %d" % s
+        assert printed_match(b["mu"], fix["mu_%d" % s], slack=slack).all(), "doublets at step %d" % s
+        assert printed_match(b["sigma"], fix["sigma_%d" % s], slack=slack).all(), "sources at step %d" % s
 
 
-def check_surface(sf, fix):
-    assert printed_match(sf["cp"], fix["cp_final"]).all()
-    assert printed_match(sf["vel"], fix["vel_final"]).all()
-    assert printed_match(sf["phi"], fix["phi_final"]).all()
+def check_surface(sf, fix, slack=0.0):
+    assert printed_match(sf["cp"], fix["cp_final"], slack=slack).all()
+    assert printed_match(sf["vel"], fix["vel_final"], slack=slack).all()
+    assert printed_match(sf["phi"], fix["phi_final"], slack=slack).all()
     # the .CPout's surface-integrated coefficients, 5 decimals
     body = [sf["Fbody"][2], sf["Fbody"][0], sf["Fbody"][1]]   # CN CA CY
     wind = [sf["Fwind"][2], sf["Fwind"][0], sf["Fwind"][1]]   # CL CD CY
     mom = [sf["CM"][1], sf["CM"][0], sf["CM"][2]]             # Cm Cl Cn
     for ours, ref in ((body, fix["body_CN_CA_CY"]), (wind, fix["wind_CL_CD_CY"]), (mom, fix["Cm_Cl_Cn"])):
-        assert np.all(np.abs(np.array(ours) - ref) <= 0.5e-5 + 1e-12), (ours, ref)
+        assert np.all(np.abs(np.array(ours) - ref) <= 0.5e-5 + 1e-12 + slack), (ours, ref)
 
 
 @pytest.fixture(scope="module")

@@ -27,6 +27,7 @@
 #include "particles.h"
 #include "vpkern.h"
 #include "post.h"
+#include "tc_gemm.h"
 
 struct cpg_ctx {
     int device = 0;
@@ -1707,3 +1708,48 @@ int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* f
 }
 
 }  // namespace cpg
+
+// ---- C ABI: the tensor-core GEMM on caller-owned FP32 device matrices ----
+extern "C" int cpg_gemm_f32_tc(cpg_ctx* ctx, int64_t m, int64_t n, int64_t k, float alpha, const float* A,
+                               int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,
+                               int sm_budget) {
+    if (!ctx || m < 0 || n < 0 || k < 0 || (m > 0 && (!C || ldc < m)) || (k > 0 && (!A || !B || lda < m || ldb < k)))
+        return CPG_E_INVALID;
+    if (m == 0 || n == 0) return CPG_OK;
+    ProfInstall pi(ctx);
+    cudaStream_t s = ctx->stream;
+    const int64_t kp = std::max<int64_t>(cpg::kTcK, (k + cpg::kTcK - 1) / cpg::kTcK * cpg::kTcK);
+    const size_t ba = cpg::tc_operand_bytes(m, kp), bb = cpg::tc_operand_bytes(n, kp);
+    void* mem = nullptr;
+    cudaError_t e = cudaMalloc(&mem, ba + bb + 256);
+    if (e != cudaSuccess) {
+        cpg::ctx_set_error(ctx, std::string("gemm: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? CPG_E_OOM : CPG_E_CUDA;
+    }
+    cpg::TcOperand opA, opB;
+    cpg::tc_operand_bind(opA, mem, m, kp);
+    cpg::tc_operand_bind(opB, (char*)mem + ba, n, kp);
+    int* err = (int*)((char*)mem + ba + bb);
+    int herr = 0;
+    const int budget = sm_budget > 0 ? sm_budget : cpg::tc_num_sms();
+    if ((e = cudaMemsetAsync(mem, 0, ba + bb + 256, s)) == cudaSuccess &&
+        (k == 0 || (e = cpg::tc_split(A, 1, lda, m, k, opA, err, s)) == cudaSuccess) &&
+        (k == 0 || (e = cpg::tc_split(B, ldb, 1, n, k, opB, err, s)) == cudaSuccess))
+        e = cpg::tc_gemm(opA, m, opB, n, alpha, beta, C, ldc, budget, err, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(mem);
+    if (e != cudaSuccess) {
+        cpg::ctx_set_error(ctx, std::string("gemm: ") + cudaGetErrorString(e));
+        return CPG_E_CUDA;
+    }
+    if (herr == 2) {
+        cpg::ctx_set_error(ctx, "gemm: non-finite operand");
+        return CPG_E_INVALID;
+    }
+    if (herr != 0) {
+        cpg::ctx_set_error(ctx, "gemm: a wait of the kernel timed out");
+        return CPG_E_TIMEOUT;
+    }
+    return CPG_OK;
+}

@@ -12,7 +12,7 @@ namespace cpg {
 // thread for the duration of a call.
 struct Prof {
     enum { ASSEMBLE = 0, WAKE_COLUMNS, MATVEC_FP32, MATVEC_FP64, RESIDUAL, LU_FACTOR, PARTICLES, CHTLS, POST,
-           LU_SOLVE, NCLS };
+           LU_SOLVE, TC_GEMM, NCLS };
     struct Pair {
         cudaEvent_t a, b;
         int cls;
@@ -148,6 +148,8 @@ struct LuGraphs {
     float* super_tmp = nullptr; // 512 x 512 scratch per 1,024-column block while they are built
     int64_t super_n = 0;        // order they were built for (0: none, the substitutions use dinv)
     int64_t super_cap = 0;      // 1,024-column blocks dinv4 and super_tmp hold
+    void* tc_mem = nullptr;     // split FP16 operands of the tensor-core rank-OB updates
+    size_t tc_bytes = 0;
     void release();
 };
 cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);

@@ -9,6 +9,8 @@
 // FP32 (or its BF16x9 tensor-core emulation, which keeps FP32 accuracy).
 #include <cublas_v2.h>
 
+#include "tc_gemm.h"
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -608,6 +610,9 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
 // against 269 ms for 1,024 (256: 224 ms; 2,048: 379 ms).
 constexpr int OB_BLOCKS = 8;
 constexpr int OB_BLOCKS_BATCHED = 4;
+// SMs the rank-OB update of the columns past the next panel leaves to that panel's
+// factorization on its own stream
+constexpr int kPanelSms = 0;
 int64_t outer_width(int blocks = OB_BLOCKS) { return (int64_t)NB * blocks; }
 
 struct Streams {  // where the next cuBLAS calls go
@@ -658,11 +663,22 @@ cudaError_t factor_body(const Streams& st, LuGraphs* G, float* LU, float* Dinv, 
             if ((e = trailing(st.h, LU, n, K, b, K + b, KE - K - b, KE, n - KE)) != cudaSuccess) return e;
         }
         const int64_t KE2 = std::min<int64_t>(KE + OB, n);
-        // rank-OB update of the next panel's columns, then the next panel on its stream
-        // beside the update of the remaining columns
-        if ((e = trailing(st.h, LU, n, KO, (int)(KE - KO), KE, n - KE, KE, KE2 - KE)) != cudaSuccess) return e;
+        // rank-OB update A22 -= L21 U12 on the tensor cores: both operands split once, then the
+        // next panel's columns, then the next panel on its stream beside the update of the
+        // remaining columns
+        TcOperand tA, tB;
+        const int64_t rows = n - KE;
+        tc_operand_bind(tA, G->tc_mem, rows, OB);
+        tc_operand_bind(tB, (char*)G->tc_mem + tc_operand_bytes(rows, OB), rows, OB);
+        if ((e = tc_split(LU + KO * n + KE, 1, n, rows, KE - KO, tA, bad, st.main)) != cudaSuccess) return e;
+        if ((e = tc_split(LU + KE * n + KO, n, 1, rows, KE - KO, tB, bad, st.main)) != cudaSuccess) return e;
+        const int sms = tc_num_sms();
+        if ((e = tc_gemm(tA, rows, tB, KE2 - KE, -1.f, 1.f, LU + KE * n + KE, n, sms, bad, st.main)) != cudaSuccess)
+            return e;
         if ((e = cudaEventRecord(G->ev_update, st.main)) != cudaSuccess) return e;
-        if ((e = trailing(st.h, LU, n, KO, (int)(KE - KO), KE, n - KE, KE2, n - KE2)) != cudaSuccess) return e;
+        if ((e = tc_gemm(tA, rows, tc_rows(tB, KE2 - KE), n - KE2, -1.f, 1.f, LU + KE2 * n + KE, n,
+                         sms - kPanelSms, bad, st.main)) != cudaSuccess)
+            return e;
         if ((e = cudaStreamWaitEvent(st.panel, G->ev_update, 0)) != cudaSuccess) return e;
         if ((e = factor_panel(st, LU, Dinv, W, n, bad, KE, KE2)) != cudaSuccess) return e;
     }
@@ -848,6 +864,9 @@ void LuGraphs::release() {
     if (tmp) cudaFree(tmp);
     if (dinv4) cudaFree(dinv4);
     if (super_tmp) cudaFree(super_tmp);
+    if (tc_mem) cudaFree(tc_mem);
+    tc_mem = nullptr;
+    tc_bytes = 0;
     dinv4 = super_tmp = nullptr;
     super_n = super_cap = 0;
     solve = nullptr;
@@ -877,6 +896,14 @@ cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* b
         if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
         if ((e = cudaMalloc(&G->panel, sizeof(float) * (size_t)n * NB)) != cudaSuccess) return e;
         G->factor_n = n;
+    }
+    const size_t tcb = 2 * tc_operand_bytes(n, outer_width());
+    if (G->tc_bytes < tcb) {
+        if (G->tc_mem) cudaFree(G->tc_mem);
+        G->tc_mem = nullptr;
+        G->tc_bytes = 0;
+        if ((e = cudaMalloc(&G->tc_mem, tcb)) != cudaSuccess) return e;
+        G->tc_bytes = tcb;
     }
     if (!G->panel_stream) {
         int least = 0, greatest = 0;

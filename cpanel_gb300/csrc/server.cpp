@@ -199,9 +199,10 @@ extern "C" {
 
 int64_t cpg_server_footprint(int64_t n, int k, int precision) {
     // matrices and factors, per-case vectors, the CHTLS/Trefftz tables, the LU's
-    // cuBLAS workspace and panel staging (lu.cu), with a fixed margin
+    // cuBLAS workspace, panel staging and split tensor-core operands (two of n rows x 1,024
+    // halves x 2 and their scales: 8,208 bytes a row; lu.cu), with a fixed margin
     const int64_t nn = n * n;
-    int64_t mats = precision == CPG_PLAIN_FP64 ? 16 * nn : 12 * nn + (int64_t)n * 128 * 4 + ((int64_t)256 << 20);
+    int64_t mats = precision == CPG_PLAIN_FP64 ? 16 * nn : 12 * nn + (int64_t)n * (128 * 4 + 8208) + ((int64_t)256 << 20);
     return mats + (int64_t)n * (int64_t)(2000 + 64 * k) + ((int64_t)64 << 20);
 }
 
@@ -210,7 +211,8 @@ int64_t cpg_server_footprint_vp(int64_t n, int64_t n2, int nsteps, int precision
     // per particle its state, tree slot, step scratch and the panel kernels' partial sums
     const int64_t nn = n * n;
     int64_t mats = 16 * nn + 8 * n * n2;
-    if (precision == CPG_MIXED) mats += 20 * nn + n * 128 * 4 + ((int64_t)256 << 20);  // + inverse and its scratch
+    if (precision == CPG_MIXED)  // + inverse and its scratch, split tensor-core operands
+        mats += 20 * nn + n * (128 * 4 + 8208) + ((int64_t)256 << 20);
     const int64_t np = n2 * (int64_t)(nsteps > 0 ? nsteps : 0);
     return mats + n * 4000 + np * 4096 + ((int64_t)64 << 20);
 }

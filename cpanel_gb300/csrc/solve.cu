@@ -489,10 +489,13 @@ void Prof::begin(int cls, cudaStream_t s) {
     cudaEventRecord(p.a, s);
     pending.push_back(p);
 }
-void Prof::end(cudaStream_t s) {
-    Pair& p = pending.back();
-    p.b = get();
-    cudaEventRecord(p.b, s);
+void Prof::end(cudaStream_t s) {  // closes the innermost open scope: scopes nest
+    for (auto it = pending.rbegin(); it != pending.rend(); ++it)
+        if (!it->b) {
+            it->b = get();
+            cudaEventRecord(it->b, s);
+            return;
+        }
 }
 void Prof::collect() {
     for (Pair& p : pending) {

@@ -228,8 +228,9 @@ int  cpg_panel_v_inf(cpg_ctx* ctx, const double* verts, const double* poi, int64
  * Classes: 0 assembly, 1 wake columns, 2 FP32 matvec, 3 FP64 matvec, 4 refinement
  * residual, 5 LU factorization (one graph launch), 6 particle and panel-velocity
  * operators (cpanel_vp.h), 7 CHTLS weights,
- * 8 velocity/Cp/forces, 9 LU triangular solves (one graph launch per solve). */
-#define CPG_PROF_NCLS 10
+ * 8 velocity/Cp/forces, 9 LU triangular solves (one graph launch per solve), 10 tensor-core
+ * GEMM launches (cpg_gemm_f32_tc and the factorizations' GEMMs; nested in class 5 there). */
+#define CPG_PROF_NCLS 11
 typedef struct {
     long long launches[CPG_PROF_NCLS];
     double ms[CPG_PROF_NCLS];
@@ -240,6 +241,17 @@ int  cpg_prof_read(cpg_ctx* ctx, cpg_prof* out);      /* totals since enable    
 /* FP64 FMA throughput of the context's GPU in TFLOP/s (a short probe kernel), the
  * denominator for FP64-issue-bound kernels. */
 int  cpg_measure_fp64_peak(cpg_ctx* ctx, double* tflops);
+
+/* The tensor-core GEMM of the mixed path's factorizations, on caller-owned FP32 DEVICE matrices
+ * (column-major): C = alpha A B + beta C with A m x k (lda), B k x n (ldb), C m x n (ldc); beta = 0
+ * does not read C.  No counterpart in the reference (its solves are Eigen's BiCGSTAB): it is the
+ * sm_103a kernel the mixed LU runs (tcgen05 MMAs in tensor memory, operands by TMA), exposed so
+ * hosts and tests can call it.  Each operand row is scaled by a power of two and split into two
+ * FP16 halves; the three leading products are accumulated in FP32, which gives about 22
+ * significant bits per product.  sm_budget: SMs the persistent grid may take (0: all).
+ * Allocates its split operands for the call.  CPG_E_TIMEOUT when a wait of the kernel ran out. */
+int  cpg_gemm_f32_tc(cpg_ctx* ctx, int64_t m, int64_t n, int64_t k, float alpha, const float* A, int64_t lda,
+                     const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int sm_budget);
 
 /* Build identification: the sm architecture the kernels were compiled for. */
 int  cpg_compiled_arch(void);

@@ -37,15 +37,53 @@ constexpr int DIAG_SMEM = (3 * NB * P + 6 * BS * TP) * 4;
 // itself without touching the real entries.  Every phase below is a set of
 // independent items spread over the 512 threads; barriers separate the phases.
 //
-// LU: 128 right-looking steps, thread t owning row t % 128 and every fourth column;
-// step j reads column j and row j and writes only past them, and the multiplier of
-// column j is stored one step later, when nothing reads column j.
-// Inverses: the eight 32 x 32 diagonal blocks first, one warp each with a column per
-// lane in registers (right-looking; U as the unit upper factor of U scaled by its
-// diagonal, then the columns divided by it), then the off-diagonal blocks by distance
-// d = 1..3 from the diagonal:
+// LU: four 32-column steps (below); the inverses of the four 32 x 32 diagonal blocks come out
+// of them, and the off-diagonal blocks of the inverses follow by distance d = 1..3 from the
+// diagonal:
 // Linv[I][J] = -Linv[I][I] sum_{K=J}^{I-1} L[I][K] Linv[K][J] and
 // Uinv[I][J] = -Uinv[I][I] sum_{K=I+1}^{J} U[I][K] Uinv[K][J].
+// The 32 x 32 diagonal block of one blocked-LU step in one warp's registers, lane i holding
+// row i (template recursion keeps every register index static).
+// fact_step: step k of the elimination; the multipliers replace the entries below the pivot.
+template <int k>
+__device__ __forceinline__ void fact_step(float (&r)[32], int lane, int* bad) {
+    float u[32];
+#pragma unroll
+    for (int c = k; c < 32; c++) u[c] = __shfl_sync(0xffffffffu, r[c], k);
+    float piv = u[k];
+    if (piv == 0.f) {
+        if (lane == 0) atomicExch(bad, 1);
+        piv = 1.f;
+    }
+    const float rp = __frcp_rn(piv);  // the correctly rounded 1 / piv
+    // rows at or above the pivot take a zero multiplier (no branch: r + (-0) u is r)
+    const float l = lane > k ? r[k] * rp : 0.f;
+    r[k] = lane > k ? l : r[k];
+#pragma unroll
+    for (int c = k + 1; c < 32; c++) r[c] = __fmaf_rn(-l, u[c], r[c]);
+    if constexpr (k + 1 < 32) fact_step<k + 1>(r, lane, bad);
+}
+// X = L^{-1} (L unit lower, multipliers in r): row i of X is e_i - sum_{k<i} L[i][k] X[k],
+// and row k is final once steps 0..k-1 have run
+template <int k>
+__device__ __forceinline__ void linv_step(const float (&r)[32], float (&x)[32], int lane) {
+    const float m = lane > k ? r[k] : 0.f;
+#pragma unroll
+    for (int c = 0; c <= k; c++) x[c] = __fmaf_rn(-m, __shfl_sync(0xffffffffu, x[c], k), x[c]);
+    if constexpr (k + 1 < 31) linv_step<k + 1>(r, x, lane);
+}
+// Y = U^{-1}: from the last row up, row k = (e_k - sum_{j>k} U[k][j] Y[j]) / U[k][k]
+template <int k>
+__device__ __forceinline__ void uinv_step(const float (&r)[32], float (&y)[32], int lane) {
+    const float rd = __frcp_rn(__shfl_sync(0xffffffffu, r[k], k));  // 1 / U[k][k], once a step
+    const float sc = lane == k ? rd : 1.f, m = lane < k ? r[k] : 0.f;
+#pragma unroll
+    for (int c = k; c < 32; c++) y[c] *= sc;
+#pragma unroll
+    for (int c = k; c < 32; c++) y[c] = __fmaf_rn(-m, __shfl_sync(0xffffffffu, y[c], k), y[c]);
+    if constexpr (k > 0) uinv_step<k - 1>(r, y, lane);
+}
+
 __device__ __forceinline__ void lu_diag_body(float* sm, float* __restrict__ A, int64_t n, int64_t K, int b,
                                              float* __restrict__ Dinv, int* bad) {
     float* S = sm;                 // S[r*P + c]
@@ -53,83 +91,125 @@ __device__ __forceinline__ void lu_diag_body(float* sm, float* __restrict__ A, i
     float* ZU = sm + 2 * NB * P;   // U^{-1}, row-major
     float* Tb = sm + 3 * NB * P;   // 6 scratch blocks, Tb[slot*BS*TP + r*TP + c]
     const int t = threadIdx.x;
-    for (int idx = t; idx < NB * NB; idx += DT) {
-        int c = idx / NB, r = idx % NB;
-        S[r * P + c] = (r < b && c < b) ? A[(K + c) * n + K + r] : (r == c ? 1.f : 0.f);
-        ZL[r * P + c] = r == c ? 1.f : 0.f;
-        ZU[r * P + c] = r == c ? 1.f : 0.f;
+    {  // all 32 loads of a thread in flight together
+        float v[NB * NB / DT];
+#pragma unroll
+        for (int q = 0; q < NB * NB / DT; q++) {
+            const int idx = t + q * DT, c = idx / NB, r = idx % NB;
+            v[q] = (r < b && c < b) ? A[(K + c) * n + K + r] : (r == c ? 1.f : 0.f);
+        }
+#pragma unroll
+        for (int q = 0; q < NB * NB / DT; q++) {
+            const int idx = t + q * DT, c = idx / NB, r = idx % NB;
+            S[r * P + c] = v[q];
+            ZL[r * P + c] = r == c ? 1.f : 0.f;
+            ZU[r * P + c] = r == c ? 1.f : 0.f;
+        }
     }
     __syncthreads();
-    // ---- LU: thread t owns row t % 128 and the columns c = t / 128 (mod 4); one barrier
-    // per step; the multiplier of column j is stored during step j + 1
-    const int r = t % NB, q = t / NB;
-    float lprev = 0.f;
-    for (int j = 0; j < NB; j++) {
-        if (q == 0 && j > 0 && r > j - 1) S[r * P + j - 1] = lprev;
-        float piv = S[j * P + j];
-        if (piv == 0.f) {
-            if (t == 0) atomicExch(bad, 1);
-            piv = 1.f;
-        }
-        if (r > j) {
-            float l = S[r * P + j] / piv;
-            int c = j + 1 + ((q - (j + 1)) & 3);
-            // eight columns per batch: all loads first, so that the shared-memory
-            // latencies overlap instead of chaining through the stores
-            for (; c + 28 < NB; c += 32) {
-                float u[8], v[8];
+    // ---- blocked LU by 32-column steps o = 0, 32, 64, 96:
+    //  1. warp 0 factors the 32 x 32 diagonal block D, then warps 0 and 1 invert its unit lower
+    //     and upper triangles into the diagonal blocks of ZL and ZU, in registers (lane i: row i);
+    //  2. the block column below becomes L = A U_D^{-1} and the block row to the right
+    //     U = L_D^{-1} A (4 x 4 register tiles, written after a barrier: the products read
+    //     the rows they replace);
+    //  3. the trailing block loses L U.
+    const int w = t >> 5, lane = t & 31;
+    for (int o = 0; o < NB; o += BS) {
+        if (w < 2) {  // warp 0 factors; then warp 0 inverts L_D and warp 1 U_D, side by side
+            float r[32], x[32];
+            if (w == 0) {
 #pragma unroll
-                for (int m = 0; m < 8; m++) {
-                    u[m] = S[j * P + c + 4 * m];
-                    v[m] = S[r * P + c + 4 * m];
-                }
+                for (int c = 0; c < 32; c++) r[c] = S[(o + lane) * P + o + c];
+                fact_step<0>(r, lane, bad);
 #pragma unroll
-                for (int m = 0; m < 8; m++) S[r * P + c + 4 * m] = __fmaf_rn(-l, u[m], v[m]);
+                for (int c = 0; c < 32; c++) S[(o + lane) * P + o + c] = r[c];
             }
-            for (; c < NB; c += 4) S[r * P + c] = __fmaf_rn(-l, S[j * P + c], S[r * P + c]);
-            lprev = l;
+            asm volatile("bar.sync 1, 64;" ::: "memory");
+            if (w == 1) {
+#pragma unroll
+                for (int c = 0; c < 32; c++) r[c] = S[(o + lane) * P + o + c];
+            }
+#pragma unroll
+            for (int c = 0; c < 32; c++) x[c] = c == lane ? 1.f : 0.f;
+            if (w == 0) {
+                linv_step<0>(r, x, lane);
+#pragma unroll
+                for (int c = 0; c < 32; c++) ZL[(o + lane) * P + o + c] = x[c];
+            } else {
+                uinv_step<31>(r, x, lane);
+#pragma unroll
+                for (int c = 0; c < 32; c++) ZU[(o + lane) * P + o + c] = x[c];
+            }
+        }
+        __syncthreads();
+        const int nr = NB - o - BS;  // rows below and columns to the right
+        if (nr == 0) break;
+        // 2. block column (2 nr tiles) and block row (2 nr tiles)
+        float acc[4][4];
+        int tr = 0, tc = 0;
+        const bool col = t < 2 * nr, row = !col && t < 4 * nr;
+        if (col) {
+            tr = o + BS + 4 * (t >> 3);
+            tc = o + 4 * (t & 7);
+        } else if (row) {
+            tr = o + 4 * ((t - 2 * nr) & 7);
+            tc = o + BS + 4 * ((t - 2 * nr) >> 3);
+        }
+        if (col || row) {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 4; x++) acc[i][x] = 0.f;
+            const float* Pa = col ? S : ZL;
+            const float* Pb = col ? ZU : S;
+            for (int k = 0; k < BS; k++) {
+                float a[4], bb[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) a[i] = Pa[(tr + i) * P + o + k];
+#pragma unroll
+                for (int x = 0; x < 4; x++) bb[x] = Pb[(o + k) * P + tc + x];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int x = 0; x < 4; x++) acc[i][x] = __fmaf_rn(a[i], bb[x], acc[i][x]);
+            }
+        }
+        __syncthreads();
+        if (col || row) {
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 4; x++) S[(tr + i) * P + tc + x] = acc[i][x];
+        }
+        __syncthreads();
+        // 3. trailing update, (nr / 4)^2 tiles
+        const int q4 = nr >> 2;
+        for (int q = t; q < q4 * q4; q += DT) {
+            const int rr = o + BS + 4 * (q % q4), cc = o + BS + 4 * (q / q4);
+            float u[4][4];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 4; x++) u[i][x] = 0.f;
+            for (int k = 0; k < BS; k++) {
+                float a[4], bb[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) a[i] = S[(rr + i) * P + o + k];
+#pragma unroll
+                for (int x = 0; x < 4; x++) bb[x] = S[(o + k) * P + cc + x];
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int x = 0; x < 4; x++) u[i][x] = __fmaf_rn(a[i], bb[x], u[i][x]);
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 4; x++) S[(rr + i) * P + cc + x] -= u[i][x];
         }
         __syncthreads();
     }
-    // ---- inverses of the 32 x 32 diagonal blocks, one warp each (warps 0-3: L, 4-7: U);
-    // lane c holds column c.  L: right-looking over k.  U: the unit upper factor of U
-    // (rows scaled by the diagonal, staged in Tb) inverted from the last column back,
-    // then the columns divided by the diagonal.
-    {
-        const int w = t >> 5, c = t & 31;
-        if (w < 4) {
-            const int o = BS * w;
-            float x[32];
-#pragma unroll
-            for (int i = 0; i < 32; i++) x[i] = i == c ? 1.f : 0.f;
-#pragma unroll
-            for (int k = 0; k < 32; k++) {
-                const float xk = x[k];
-#pragma unroll
-                for (int i = k + 1; i < 32; i++) x[i] = __fmaf_rn(-S[(o + i) * P + o + k], xk, x[i]);
-            }
-#pragma unroll
-            for (int i = 0; i < 32; i++) ZL[(o + i) * P + o + c] = x[i];
-        } else if (w < 8) {
-            const int o = BS * (w - 4);
-            float* Us = Tb + 2 * NB + (w - 4) * BS * TP;  // Us[i * TP + k] = S[i][k] / S[i][i]
-            for (int i = 0; i < 32; i++) Us[i * TP + c] = S[(o + i) * P + o + c] / S[(o + i) * P + o + i];
-            __syncwarp();
-            float y[32];
-#pragma unroll
-            for (int i = 0; i < 32; i++) y[i] = i == c ? 1.f : 0.f;
-#pragma unroll
-            for (int k = 31; k >= 0; k--) {
-                const float yk = y[k];
-#pragma unroll
-                for (int i = 0; i < k; i++) y[i] = __fmaf_rn(-Us[i * TP + k], yk, y[i]);
-            }
-            const float dc = S[(o + c) * P + o + c];
-#pragma unroll
-            for (int i = 0; i < 32; i++) ZU[(o + i) * P + o + c] = i <= c ? y[i] / dc : y[i];
-        }
-    }
-    __syncthreads();
     // ---- off-diagonal blocks, by distance from the diagonal
     for (int d = 1; d < NB / BS; d++) {
         const int nL = NB / BS - d;
@@ -611,8 +691,9 @@ cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, i
 constexpr int OB_BLOCKS = 8;
 constexpr int OB_BLOCKS_BATCHED = 4;
 // SMs the rank-OB update of the columns past the next panel leaves to that panel's
-// factorization on its own stream
-constexpr int kPanelSms = 0;
+// factorization on its own stream (19k wing: LU 38.6 ms with 0, 37.5 with 8, 37.4 with 16,
+// 36.8 with 32)
+constexpr int kPanelSms = 32;
 int64_t outer_width(int blocks = OB_BLOCKS) { return (int64_t)NB * blocks; }
 
 struct Streams {  // where the next cuBLAS calls go

@@ -200,3 +200,29 @@ def test_batch_solve_isolates_a_bad_mesh(per_mesh, lockstep):
         assert o["status"] == 0
         assert np.abs(o["cp"] - r["cp"]).max() < 1e-7
         assert np.allclose(o["CL"], r["CL"], rtol=1e-8, atol=0)
+
+
+@pytest.mark.gpu
+def test_batch_meets_the_metric_bound_on_config_wings(built):
+    """Four of the uneven-batch wings (the benchmark's seeds: 20261203 + 0, 16, 32, 48, 8 alphas
+    each) through the lockstep batch path against the plain FP64 path: Cp max-abs <= 1e-5 over
+    every panel, tip caps included, and CL within 1e-6 relative, the metric's bounds."""
+    import cpanel_gb300 as cg
+    from cpanel_gb300 import batch, wing
+    meshes = []
+    for i in (0, 16, 32, 48):
+        spec = wing.config_random(20261203 + i)
+        nodes, tris, ids, info = wing.make_wing(spec)
+        rng = np.random.default_rng(20261203 + i)
+        flows = [(1.0, float(a), 0.0, 0.1) for a in rng.uniform(-2, 10, 8)]
+        meshes.append(dict(nodes=nodes, tris=tris, ids=ids, flows=flows, Sref=info["area"], bref=spec.span,
+                           cref=1.0, cg=(0.25, 0.0, 0.0)))
+    res, st = batch.batch_solve(meshes, workers=4, tune="auto", lockstep=True, want=("cp", "CL", "CDi"))
+    assert st["failed"] == 0
+    for mesh, o in zip(meshes, res):
+        g = cg.Geometry(mesh["nodes"], mesh["tris"], mesh["ids"])
+        ref = cg.solve_cases(g, mesh["flows"], Sref=mesh["Sref"], bref=mesh["bref"], cref=mesh["cref"],
+                             cg=mesh["cg"], precision="fp64", want=("cp",))
+        del g
+        assert np.abs(o["cp"] - ref["cp"]).max() <= 1e-5
+        assert (np.abs(o["CL"] - ref["CL"]) / np.abs(ref["CL"])).max() <= 1e-6

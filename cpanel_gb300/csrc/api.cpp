@@ -1735,7 +1735,7 @@ extern "C" int cpg_gemm_f32_tc(cpg_ctx* ctx, int64_t m, int64_t n, int64_t k, fl
     if ((e = cudaMemsetAsync(mem, 0, ba + bb + 256, s)) == cudaSuccess &&
         (k == 0 || (e = cpg::tc_split(A, 1, lda, m, k, opA, err, s)) == cudaSuccess) &&
         (k == 0 || (e = cpg::tc_split(B, ldb, 1, n, k, opB, err, s)) == cudaSuccess))
-        e = cpg::tc_gemm(opA, m, opB, n, alpha, beta, C, ldc, budget, err, s);
+        e = cpg::tc_gemm(opA, m, opB, n, alpha, beta, C, ldc, budget, err, s, err + 16);
     if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(mem);

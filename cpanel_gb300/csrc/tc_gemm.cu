@@ -2,8 +2,11 @@
 // memory, one persistent CTA per SM.
 //
 // CTA roles (320 threads):
-//   warp 0       TMA producer: per 64-wide K block one 3-D tensor load of the A tile (hi and
-//                lo, 128 rows) and one of the B tile (hi and lo, 256 rows) into a stage;
+//   warp 0       TMA producer: draws the CTA's next tile (from a device counter shared by the
+//                grid, so that CTAs that start late while other kernels hold SMs take fewer
+//                tiles; or round-robin) and hands it to the other warps through a 4-slot ring,
+//                then per 64-wide K block one 3-D tensor load of the A tile (hi and lo, 128 rows)
+//                and one of the B tile (hi and lo, 256 rows) into a stage;
 //   warp 1       allocates 512 tensor-memory columns (two 128 x 256 FP32 accumulators); one
 //                thread issues per K block 4 x 3 MMAs (K = 16 each: Ah Bh, Ah Bl, Al Bh) and
 //                commits the stage back to the producer, then the accumulator to the epilogue;
@@ -146,12 +149,17 @@ struct GemmArgs {
     const float* isa;
     const float* isb;
     int* err;
+    int* counter;  // next tile to hand out (zero at launch), or null: CTA b takes tiles b, b + grid, ...
 };
+
+constexpr int RING = 4;  // tiles handed from the producer to the MMA and epilogue warps
 
 __global__ void __launch_bounds__(THREADS, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, GemmArgs g) {
     extern __shared__ uint8_t smem_raw[];
     __shared__ __align__(8) uint64_t full_bar[STAGES], empty_bar[STAGES], accf_bar[2], acce_bar[2], fin_bar;
+    __shared__ __align__(8) uint64_t tfull_bar[RING], tempty_bar[RING];
+    __shared__ int tile_ring[RING];
     __shared__ uint32_t tmem_base_s;
     __shared__ int abort_s;
     uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
@@ -168,6 +176,10 @@ __global__ void __launch_bounds__(THREADS, 1)
             mbar_init(su32(&acce_bar[b]), EPI_WARPS);
         }
         mbar_init(su32(&fin_bar), 1);
+        for (int q = 0; q < RING; q++) {
+            mbar_init(su32(&tfull_bar[q]), 1);
+            mbar_init(su32(&tempty_bar[q]), 1 + EPI_WARPS);
+        }
         abort_s = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -181,9 +193,17 @@ __global__ void __launch_bounds__(THREADS, 1)
     const uint32_t tmem = tmem_base_s;
 
     if (warp == 0) {
-        if (lane == 0) {  // TMA producer
+        if (lane == 0) {  // TMA producer; it also draws the tiles and hands them on through the ring
             int issued = 0;
-            for (int t = blockIdx.x; t < g.tiles && !*abort_flag; t += gridDim.x) {
+            for (int j = 0; !*abort_flag; j++) {
+                const int slot = j % RING;
+                if (!mbar_wait(su32(&tempty_bar[slot]), ((uint32_t)(j / RING) & 1u) ^ 1u, abort_flag, g.err, true))
+                    break;
+                int t = g.counter ? atomicAdd(g.counter, 1) : blockIdx.x + j * (int)gridDim.x;
+                if (t >= g.tiles) t = -1;
+                *(volatile int*)&tile_ring[slot] = t;
+                mbar_arrive(su32(&tfull_bar[slot]));
+                if (t < 0) break;
                 const int tm = t % g.tiles_m, tn = t / g.tiles_m;
                 for (int kb = 0; kb < g.kblocks; kb++) {
                     const int s = issued % STAGES;
@@ -202,8 +222,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else if (warp == 1) {
         if (lane == 0) {  // MMA issuer
-            int used = 0, tl = 0;
-            for (int t = blockIdx.x; t < g.tiles && !*abort_flag; t += gridDim.x, tl++) {
+            int used = 0;
+            for (int tl = 0; !*abort_flag; tl++) {
+                const int slot = tl % RING;
+                if (!mbar_wait(su32(&tfull_bar[slot]), (uint32_t)(tl / RING) & 1u, abort_flag, g.err, true)) break;
+                const int t = *(volatile int*)&tile_ring[slot];
+                mbar_arrive(su32(&tempty_bar[slot]));
+                if (t < 0) break;
                 const int b = tl & 1;
                 if (!mbar_wait(su32(&acce_bar[b]), ((uint32_t)(tl >> 1) & 1u) ^ 1u, abort_flag, g.err, true)) break;
                 fence_after();
@@ -233,8 +258,13 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
     } else {  // epilogue
         const int e = warp - 2, q = warp & 3, hc = e >> 2;  // lane quarter, column half
-        int tl = 0;
-        for (int t = blockIdx.x; t < g.tiles; t += gridDim.x, tl++) {
+        for (int tl = 0;; tl++) {
+            const int slot = tl % RING;
+            if (!mbar_wait(su32(&tfull_bar[slot]), (uint32_t)(tl / RING) & 1u, abort_flag, g.err, true)) break;
+            const int t = *(volatile int*)&tile_ring[slot];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(su32(&tempty_bar[slot]));
+            if (t < 0) break;
             const int b = tl & 1;
             if (!mbar_wait(su32(&accf_bar[b]), (uint32_t)(tl >> 1) & 1u, abort_flag, g.err, true)) break;
             fence_after();
@@ -456,7 +486,7 @@ int tc_num_sms() {
 }
 
 cudaError_t tc_gemm(const TcOperand& A, int64_t m, const TcOperand& B, int64_t n, float alpha, float beta, float* C,
-                    int64_t ldc, int sm_budget, int* err, cudaStream_t s) {
+                    int64_t ldc, int sm_budget, int* err, cudaStream_t s, int* counter) {
     if (m <= 0 || n <= 0) return cudaSuccess;
     if (A.kp != B.kp || A.kp % BK != 0 || m > A.rows_cap || n > B.rows_cap || ldc < m) return cudaErrorInvalidValue;
     static std::once_flag attr[64];
@@ -480,7 +510,12 @@ cudaError_t tc_gemm(const TcOperand& A, int64_t m, const TcOperand& B, int64_t n
     g.isa = A.inv_scale;
     g.isb = B.inv_scale;
     g.err = err;
+    g.counter = counter;
     const int grid = std::max(1, std::min(g.tiles, sm_budget));
+    if (counter) {
+        cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(int), s);
+        if (e != cudaSuccess) return e;
+    }
     ProfScope ps(Prof::TC_GEMM, s);
     k_tc_gemm<<<grid, THREADS, SMEM_BYTES, s>>>(ta, tb, g);
     return cudaGetLastError();

@@ -47,9 +47,13 @@ cudaError_t tc_split(const float* src, int64_t rs, int64_t ks, int64_t rows, int
 // (n rows) split over the same kp.  beta = 0 does not read C.  The grid is persistent, one CTA per
 // SM, at most sm_budget CTAs (the rest of the SMs stay free for work on other streams).  err
 // (device) is set to 1 when one of the kernel's waits ran past its limit (about two seconds);
-// the kernel then stops early and C is incomplete.
+// the kernel then stops early and C is incomplete.  counter (device int, may be null): the
+// CTAs draw tiles from it (it is zeroed on the stream first), so a grid whose CTAs cannot all
+// start at once still finishes with the ones that did; it must not be shared by launches
+// that may run at the same time.  Each tile is computed by one CTA in a fixed order, so the
+// result does not depend on the schedule.
 cudaError_t tc_gemm(const TcOperand& A, int64_t m, const TcOperand& B, int64_t n, float alpha, float beta, float* C,
-                    int64_t ldc, int sm_budget, int* err, cudaStream_t s);
+                    int64_t ldc, int sm_budget, int* err, cudaStream_t s, int* counter = nullptr);
 
 // number of SMs of the current device
 int tc_num_sms();

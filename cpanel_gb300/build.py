@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_STRICT = ["assemble.cu", "post.cu", "vpkern.cu"]   # FP64 panel math: no contraction
 CU_FAST = ["solve.cu", "lu.cu", "particles.cu", "tc_gemm.cu"]  # particles.cu rounds its branch tests explicitly
 CPP = ["mesh.cpp", "api.cpp", "octree.cpp", "vpgeom.cpp", "vpcase.cpp", "server.cpp", "batch.cpp", "writers.cpp",
-       "streamline.cpp"]
+       "streamline.cpp", "shim.cpp"]
 HEADERS = ["common.cuh", "panel64.cuh", "df.cuh", "assemble.h", "post.h", "mesh.h", "octree.h", "particles.h", "vp.cuh",
            "vpgeom.h", "vpkern.h", "streamline.h", "tc_gemm.h"]
 
@@ -31,7 +31,7 @@ def _sources():
     return [os.path.join(SRC, f) for f in CU_STRICT + CU_FAST + CPP + HEADERS] + [
         os.path.join(ROOT, "include", "cpanel_gpu.h"), os.path.join(ROOT, "include", "cpanel_vp.h"),
         os.path.join(ROOT, "include", "cpanel_serve.h"), os.path.join(ROOT, "include", "cpanel_batch.h"),
-        os.path.join(ROOT, "include", "cpanel_io.h"),
+        os.path.join(ROOT, "include", "cpanel_io.h"), os.path.join(ROOT, "include", "cpanel_shim.hpp"),
         os.path.abspath(__file__)]
 
 

@@ -432,6 +432,8 @@ def vortex_particles(steps=20):
     names = ("bh_velocity", "bh_stretching", "bh_diffusion", "panel_velocity", "panel_stretching")
     ops["mixed_vs_plain_rel"] = {k: rel(outs["mixed"][i], outs["plain"][i]) for i, k in enumerate(names)}
     ops["tree_build_ms"] = timed(lambda: vp.ParticleFMM(Pt, A, R))
+    del tree, Pt, A, R, BV, SG, MU
+    at_scale = vp_config4_at_scale()
     return {"vp_unsteady": {
         "workload": "NACA 4412 AR 6 taper 0.6, %d body triangles, no wake panels, alpha 8 deg, dt 0.05, "
                     "Barnes-Hut theta 0.5" % len(verts),
@@ -439,7 +441,64 @@ def vortex_particles(steps=20):
         "what": "cpg_vpcase_step: convection, shedding, strength update, octree, source strengths, solve "
                 "(plain: FP64 BiCGSTAB; mixed: FP32 LU refined in FP64), Trefftz-plane convergence check",
         "velocity_check": check, "mixed_vs_plain_state": drift,
-        "operators_40k_particles": ops}}
+        "operators_40k_particles": ops, "config4_300_steps": at_scale}}
+
+
+def config4_wing():
+    """The unsteady workload's wing: NACA 4412, AR 6, taper 0.6, 21 points per side x 101 stations
+    (8,076 body triangles, 100 trailing-edge edges: 100 particles shed per step), no wake panels."""
+    from cpanel_gb300 import wing
+    spec = wing.WingSpec(m=0.04, p=0.4, t=0.12, root_chord=1.0, span=6 * (1 + 0.6) / 2, taper=0.6, sweep_deg=0.0,
+                         n_chord=21, n_span=101, wake_len=30.0, wake_dir=(1.0, 0.0, 0.0))
+    nodes, tris, ids, info = wing.make_wing(spec)
+    keep = ids < 1000
+    return nodes, tris[keep], ids[keep], info
+
+
+def vp_config4_at_scale(steps=300, chunk=50):
+    """The unsteady workload at its stated scale, mixed form: impulsive start at alpha 8 deg, dt
+    0.05, 300 steps with the Trefftz-plane early stop off, one particle per trailing-edge edge
+    per step (~29.8k particles at the end); ms per step and particle count per `chunk` steps,
+    then the convective velocities of the final state: the mixed octree against the FP64
+    octree (the arithmetic error of the mixed form) and both against the FP64 direct sum."""
+    import torch
+
+    from cpanel_gb300 import vp
+    nodes, tris, ids, info = config4_wing()
+    t0 = time.perf_counter()
+    S = vp.VPCase(nodes, tris, ids, V=1.0, alpha=8.0, dt=0.05, accelerate=True, Sref=info["area"],
+                  precision="mixed", run_all_steps=True)
+    torch.cuda.synchronize()
+    setup = time.perf_counter() - t0
+    rows, done = [], 0
+    t_all = time.perf_counter()
+    while done < steps:
+        k = min(chunk, steps - done)
+        t0 = time.perf_counter()
+        S.step(k)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        done += k
+        rows.append({"to_step": done, "particles": S.info()["n_particles"], "ms_per_step": dt / k * 1e3})
+    wall = time.perf_counter() - t_all
+    inf = S.info()
+    tz = S.trefftz()
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+    t0 = time.perf_counter()
+    v32, v64, vdir = S.velocities("mixed"), S.velocities("plain"), S.velocities("plain", direct=True)
+    t_check = time.perf_counter() - t0
+    return {"workload": "NACA 4412 AR 6 taper 0.6, %d body triangles (21 points per side x 101 stations), "
+                        "alpha 8 deg, dt 0.05, Barnes-Hut theta 0.5, mixed form" % inf["n_body"],
+            "steps": inf["timestep"], "particles_at_end": inf["n_particles"], "wall_s": wall,
+            "setup_s": setup, "ms_per_step_by_chunk": rows, "trefftz_CL": tz["CL"], "trefftz_CD": tz["CD"],
+            "trefftz_check_fired": tz["converged"], "solve_fallbacks": inf["solve_fallbacks"],
+            "velocity_check": {"particles": int(len(v32)), "mixed_vs_fp64_octree": rel(v32, v64),
+                               "fp64_octree_vs_fp64_direct": rel(v64, vdir), "mixed_vs_fp64_direct": rel(v32, vdir),
+                               "check_s": t_check,
+                               "what": "max |dv| / max |v| over the convective particle velocities"}}
 
 
 def vp_loop_only(precision, steps):
@@ -591,7 +650,14 @@ def main():
     ap.add_argument("--vp-loop", choices=["plain", "mixed"],
                     help="only the vortex-particle loop in this precision: 3 steps, then --steps timed "
                          "steps (one JSON line; for profiling)")
+    ap.add_argument("--vp-scale", action="store_true",
+                    help="only the unsteady workload at its stated scale (300 mixed steps; one JSON line)")
     args = ap.parse_args()
+    if args.vp_scale:
+        import __graft_entry__
+        __graft_entry__.build()
+        print(json.dumps({"config4_300_steps": vp_config4_at_scale()}), flush=True)
+        return
     if args.impl == "reference":
         return run_reference(args)
     if args.vp_loop:

@@ -105,7 +105,7 @@ class VPResult(C.Structure):
 class VPParams(C.Structure):
     _fields_ = [("V", C.c_double), ("alpha", C.c_double), ("beta", C.c_double), ("dt", C.c_double),
                 ("cref", C.c_double), ("accelerate", C.c_int), ("Sref", C.c_double), ("mach", C.c_double),
-                ("precision", C.c_int)]
+                ("precision", C.c_int), ("run_all_steps", C.c_int)]
 
 
 class VPInfo(C.Structure):

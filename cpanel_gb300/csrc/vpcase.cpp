@@ -154,6 +154,7 @@ struct cpg_vpcase {
     double Sref = 1, PG = 1;
     double CLt = 0, CDt = 0;
     bool converged = false;
+    bool run_all = false;  // keep stepping after the check has fired
     // mixed precision: FP32 far fields, LU-refined solve
     int precision = CPG_PLAIN_FP64;
     Buf fnodes, A32, Alo, LU, bad, Ainv;
@@ -612,7 +613,7 @@ cudaError_t convergence_check(cpg_vpcase& S) {
     cudaError_t e = trefftz(S, S.CLt, S.CDt);
     if (e != cudaSuccess) return e;
     double dCD = std::abs((S.CDt - prevCD) / prevCD), dCL = std::abs((S.CLt - prevCL) / prevCL);
-    S.converged = dCL < 0.0001 && dCD < 0.0001;
+    if (dCL < 0.0001 && dCD < 0.0001) S.converged = true;  // stays set (a run_all_steps case goes on)
     return cudaSuccess;
 }
 
@@ -758,6 +759,7 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
     S.accelerate = prm->accelerate != 0;
     S.Sref = prm->Sref;
     S.precision = prm->precision;
+    S.run_all = prm->run_all_steps != 0;
     S.PG = std::sqrt(1 - std::pow(prm->mach, 2));
     S.dt = S.G.dt;
     wind_to_body(S.V, S.alpha, S.beta, S.vinf);
@@ -880,7 +882,7 @@ int cpg_vpcase_info_get(const cpg_vpcase* S, cpg_vp_info* o) {
 int cpg_vpcase_step(cpg_vpcase* Sp, int nsteps) {
     if (!Sp || nsteps < 0) return CPG_E_INVALID;
     cpg_vpcase& S = *Sp;
-    for (int k = 0; k < nsteps && !S.converged; k++) {
+    for (int k = 0; k < nsteps && (S.run_all || !S.converged); k++) {
         cudaError_t e = step_once(S);
         if (e != cudaSuccess) {
             cpg::ctx_set_error(S.ctx, std::string("vortex-particle step: ") + cudaGetErrorString(e));

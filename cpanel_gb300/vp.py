@@ -248,12 +248,13 @@ class VPCase:
     """cpCaseVP on a body-only mesh, advanced step by step on the GPU."""
 
     def __init__(self, nodes, tris, ids, V=1.0, alpha=5.0, beta=0.0, dt=0.0, cref=1.0, accelerate=True, Sref=1.0,
-                 mach=0.0, precision="plain", ctx=None):
+                 mach=0.0, precision="plain", run_all_steps=False, ctx=None):
         self.ctx = _ctx(ctx)
         nodes = np.ascontiguousarray(nodes, dtype=np.float64)
         tris = np.ascontiguousarray(tris, dtype=np.int64)
         ids = np.ascontiguousarray(ids, dtype=np.int32)
-        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0, Sref, mach, _precision(precision))
+        prm = _lib.VPParams(V, alpha, beta, dt, cref, 1 if accelerate else 0, Sref, mach, _precision(precision),
+                            1 if run_all_steps else 0)
         h = C.c_void_p()
         self.ctx.check(self.ctx.L.cpg_vpcase_create(self.ctx.h, nodes.ctypes.data_as(_lib.D), len(nodes),
                                                     tris.ctypes.data_as(_lib.I64), ids.ctypes.data_as(_lib.I32),

@@ -136,6 +136,10 @@ typedef struct {
                               FP64 A to 1e-12 each step with an FP32 inverse of A formed
                               once from its LU (BiCGSTAB for a step whose refinement
                               stalls)                                                  */
+    int run_all_steps;     /* 0: the reference's loop, which stops once the Trefftz-plane
+                              check fires (CPanel/cpCaseVP.cpp:94-100); nonzero: keep
+                              stepping (a benchmark of the full step count; the check
+                              still runs and cpg_vpcase_trefftz reports that it fired)   */
 } cpg_vp_params;
 typedef struct {
     int64_t n_body, n_w1, n_w2;   /* body panels, first and second buffer rows           */
@@ -162,7 +166,7 @@ int  cpg_vpcase_info_get(const cpg_vpcase* c, cpg_vp_info* info);
  * loop).  From step 5 on every step ends with the Trefftz-plane convergence check of
  * cpCaseVP::solutionConvergence (CPanel/cpCaseVP.cpp:204-229): once CL and CD both change
  * by less than 0.01 % the case is converged and further steps do nothing, as the
- * reference leaves its time loop (CPanel/cpCaseVP.cpp:94-100). */
+ * reference leaves its time loop (CPanel/cpCaseVP.cpp:94-100), unless run_all_steps. */
 int  cpg_vpcase_step(cpg_vpcase* c, int nsteps);
 /* Trefftz-plane CL and CD of the current state (cpCaseVP::trefftzPlaneAnalysisVP,
  * CPanel/cpCaseVP.cpp:418-429; wake::trefftzPlaneVP, CPanel/wake.cpp:191-320) and whether

@@ -1174,18 +1174,21 @@ int cpg_particles_velocity(cpg_ctx* ctx, const double* pos, const double* streng
     if (m == 0) return CPG_OK;
     ProfInstall pi(ctx);
     cudaStream_t s = ctx->stream;
-    DevBuf parts;
+    DevBuf parts, split;
     CK(parts.ensure(sizeof(cpg::BHPart) * std::max<int64_t>(1, n)), "alloc particles");
     CK(cpg::launch_pack_parts(pos, strength, radius, n, parts.as<cpg::BHPart>(), s), "pack particles");
     {
         cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
         const cpg::BHPart* tg = pts ? nullptr : parts.as<cpg::BHPart>();
+        const int64_t need = cpg::direct_scratch_doubles(n, m);
+        if (need > 0) CK(split.ensure(sizeof(double) * need), "alloc direct-sum ranges");
         CK(cpg::launch_direct(kernel, false, false, parts.as<cpg::BHPart>(), n, tg, pts, m, cpg::vp_constants(), vel,
-                              nullptr, nullptr, s),
+                              nullptr, nullptr, s, split.as<double>(), need),
            "particle velocity");
     }
     cudaError_t e = cudaStreamSynchronize(s);
     parts.release();
+    split.release();
     CK(e, "particle velocity");
     return CPG_OK;
 }
@@ -1196,17 +1199,21 @@ int cpg_particles_stretch_diff(cpg_ctx* ctx, const double* pos, const double* st
     if (n == 0 || (!stretch && !diff)) return CPG_OK;
     ProfInstall pi(ctx);
     cudaStream_t s = ctx->stream;
-    DevBuf parts;
+    DevBuf parts, split;
     CK(parts.ensure(sizeof(cpg::BHPart) * n), "alloc particles");
     CK(cpg::launch_pack_parts(pos, strength, radius, n, parts.as<cpg::BHPart>(), s), "pack particles");
     {
         cpg::ProfScope ps(cpg::Prof::PARTICLES, s);
+        const int64_t need = cpg::direct_scratch_doubles(n, n);
+        if (need > 0) CK(split.ensure(sizeof(double) * need), "alloc direct-sum ranges");
         CK(cpg::launch_direct(0, stretch != nullptr, diff != nullptr, parts.as<cpg::BHPart>(), n,
-                              parts.as<cpg::BHPart>(), nullptr, n, cpg::vp_constants(), nullptr, stretch, diff, s),
+                              parts.as<cpg::BHPart>(), nullptr, n, cpg::vp_constants(), nullptr, stretch, diff, s,
+                              split.as<double>(), need),
            "particle strength update");
     }
     cudaError_t e = cudaStreamSynchronize(s);
     parts.release();
+    split.release();
     CK(e, "particle strength update");
     return CPG_OK;
 }

@@ -18,8 +18,9 @@
 // intrinsics, so they match the host exactly although this file keeps FMA
 // contraction for the pair arithmetic.
 //
-// The *_f32 traversals are the mixed-precision form: far nodes in FP32, leaves (the
-// direct near field) in FP64, the same decisions as the FP64 traversal.
+// The *_f32 traversals are the mixed-precision form: far nodes and leaf pairs in FP32
+// (leaf pairs closer than a hundredth of their core width in FP64), the same decisions as
+// the FP64 traversal.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -135,14 +136,14 @@ __device__ __forceinline__ Tgt load_part_g(const BHPart* __restrict__ parts, int
     return Tgt{mk3(a0.x, a0.y, a1.x), a1.y, mk3(b0.x, b0.y, b1.x), b1.y};
 }
 
-// ---- FP32 far field ----
+// ---- FP32 far field and leaves ----
 // A far node's interaction is evaluated in FP32 from the node's float view (BHNodeF)
-// and a target split into high and low floats; the near field (leaf members) stays
-// FP64.  Far/near and stretching cut-off decisions compare float squared distances
-// with a relative margin of 1e-5 (far beyond any float rounding of the distance) and
-// take the exact FP64 test inside it, so the traversal visits the same nodes in the
-// same order as the FP64 one.  Far contributions are summed with compensation
-// (Kahan) in float and added to the FP64 accumulators once per target.
+// and a target split into high and low floats; a leaf member's from the FP64 separation
+// rounded once (leaf_pair_f below).  Far/near and stretching cut-off decisions compare
+// float squared distances with a relative margin of 1e-5 (far beyond any float rounding
+// of the distance) and take the exact FP64 test inside it, so the traversal visits the
+// same nodes and pairs in the same order as the FP64 one.  Float contributions are
+// summed with compensation (Kahan) and added to the FP64 accumulators once per target.
 
 constexpr float kBandLo = 1.0f - 1e-5f, kBandHi = 1.0f + 1e-5f;
 
@@ -239,6 +240,101 @@ __device__ __forceinline__ void far_pair_f(const BHNodeF& f, const TgtF& t, floa
     }
 }
 
+// ---- FP32 leaf pairs ----
+// K(rho) and F(rho) = (3 K - xi) / rho^2 of the Gaussian core as Taylor series in rho^2,
+// from the series of erf and exp:
+//   K / c15 = sum_j (-1)^j rho^2j / ((2j + 3) 2^j j!),  F / c15 = sum_j (-1)^j rho^2j / ((2j + 5) 2^j j!)
+// (c15 = (2 pi)^-1.5).  Eleven terms hold both to 1e-8 relative for rho^2 < 2, where the
+// closed forms lose digits to cancellation; beyond it the closed forms are used.
+constexpr int kSeriesTerms = 11;
+constexpr float kSeriesRho2 = 2.0f;
+// pairs closer than rho^2 = kTinyRho2 (and coincident ones) stay in FP64
+constexpr float kTinyRho2 = 1e-4f;
+
+__host__ __device__ constexpr double series_coef(int j, int off) {
+    double f = 1;
+    for (int i = 1; i <= j; i++) f *= -2.0 * i;  // (-1)^j 2^j j!
+    return 1.0 / ((2 * j + off) * f);
+}
+
+template <int OFF, int J = 0>
+__device__ __forceinline__ float series_rho2(float r2) {
+    constexpr float c = (float)series_coef(J, OFF);
+    if constexpr (J == kSeriesTerms - 1)
+        return c;
+    else
+        return fmaf(series_rho2<OFF, J + 1>(r2), r2, c);
+}
+
+// Leaf member mb acting on target t in FP32 (symmetrised Gaussian velocity, stretching and
+// diffusion with `this` = the member, as the FP64 leaf sums).  The separation is taken in
+// FP64 and rounded once; the stretching cut-off |x_m - x_t| > 5 r_m is decided on the float
+// distance outside a 1e-5 relative margin and by the exact FP64 test inside it.  Returns
+// false, adding nothing, for pairs closer than rho^2 = kTinyRho2: the caller takes those
+// in FP64.
+template <bool V, bool S, bool D>
+__device__ __forceinline__ bool leaf_pair_f(const Tgt& mb, const Tgt& t, const TgtF& tf, const VPConstF& c,
+                                            KSum& v, KSum& s, KSum& dd) {
+    const float dx = __double2float_rn(t.x.x - mb.x.x), dy = __double2float_rn(t.x.y - mb.x.y),
+                dz = __double2float_rn(t.x.z - mb.x.z);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float rm = __double2float_rn(mb.r);
+    const float a = 1.5f * rm, b = 1.5f * tf.r;
+    const float sig2 = 0.5f * (a * a + b * b);
+    const float rho2 = d2 / sig2;
+    if (!(rho2 >= kTinyRho2)) return false;
+    const float ax = __double2float_rn(mb.a.x), ay = __double2float_rn(mb.a.y), az = __double2float_rn(mb.a.z);
+    const float isig = 1.0f / sqrtf(sig2);
+    const float isig3 = isig * isig * isig;
+    const float xi = c.c15 * expf(-0.5f * rho2);
+    const bool series = rho2 < kSeriesRho2;
+    const float rho = sqrtf(rho2);
+    bool on = false;
+    if (S) {
+        const float cut = 5.0f * rm, cut2 = cut * cut;
+        if (d2 < cut2 * kBandLo)
+            on = true;
+        else if (d2 > cut2 * kBandHi)
+            on = false;
+        else
+            on = !(exact_norm(mb.x.x - t.x.x, mb.x.y - t.x.y, mb.x.z - t.x.z) > __dmul_rn(5.0, mb.r));
+    }
+    float K = 0;
+    if (V || (S && on)) {
+        K = series ? c.c15 * series_rho2<3>(rho2)
+                   : (erff(rho * c.inv_sqrt2) * c.inv_four_pi / rho - xi) / rho2;
+    }
+    if (V) {
+        const float k = -K * isig3;
+        v.add(k * (dy * az - dz * ay), k * (dz * ax - dx * az), k * (dx * ay - dy * ax));
+    }
+    if (S && on) {
+        const float F = series ? c.c15 * series_rho2<5>(rho2) : (3 * K - xi) / rho2;
+        const float da = dx * ax + dy * ay + dz * az;
+        const float g = F * isig * isig * da;
+        const float mx = K * ax - g * dx, my = K * ay - g * dy, mz = K * az - g * dz;
+        s.add(isig3 * (tf.ay * mz - tf.az * my), isig3 * (tf.az * mx - tf.ax * mz), isig3 * (tf.ax * my - tf.ay * mx));
+    }
+    if (D) {
+        const float vi = c.four_pi_3 * (rm * rm * rm), vj = c.four_pi_3 * (tf.r * tf.r * tf.r);
+        const float k = c.two_nu * isig * isig * (xi / (rho2 * rho));
+        dd.add(k * (vi * tf.ax - vj * ax), k * (vi * tf.ay - vj * ay), k * (vi * tf.az - vj * az));
+    }
+    return true;
+}
+
+// leaf member mb at point x, algebraic core in FP32 (finite everywhere, zero at distance 0)
+__device__ __forceinline__ void leaf_alg_f(const Tgt& mb, dv3 x, float i4p, KSum& v) {
+    const float dx = __double2float_rn(x.x - mb.x.x), dy = __double2float_rn(x.y - mb.x.y),
+                dz = __double2float_rn(x.z - mb.x.z);
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    const float sg = 1.5f * __double2float_rn(mb.r), sg2 = sg * sg;
+    const float qq = d2 + sg2;
+    const float k = -i4p * (d2 + 2.5f * sg2) / (qq * qq * sqrtf(qq));
+    const float ax = __double2float_rn(mb.a.x), ay = __double2float_rn(mb.a.y), az = __double2float_rn(mb.a.z);
+    v.add(k * (dy * az - dz * ay), k * (dz * ax - dx * az), k * (dx * ay - dy * ax));
+}
+
 // float difference target - node centre
 __device__ __forceinline__ float3 diff_f(const TgtF& t, const BHNodeF& f) {
     return make_float3((t.hx - f.hx) + (t.lx - f.lx), (t.hy - f.hy) + (t.ly - f.ly), (t.hz - f.hz) + (t.lz - f.lz));
@@ -269,7 +365,7 @@ __device__ __forceinline__ void traverse_f32(const BHNode* __restrict__ nodes, c
         if (L.w) {
             for (int32_t k = L.x; k < L.x + L.y; k++) {
                 const Tgt m = load_part_g(parts, k);
-                if (m.idx == t.idx) continue;
+                if (m.idx == t.idx || leaf_pair_f<V, S, D>(m, t, tf, cf, fv, fs, fd)) continue;
                 if (V) v = v + vel_gauss_sym(m, t, c);
                 if (S) s = s + stretch(m, t, c);
                 if (D) d = d + diffusion(m, t, c);
@@ -387,7 +483,7 @@ __global__ void __launch_bounds__(128) k_bh_targets(const BHNode* __restrict__ n
     if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
 }
 
-// k_bh_particles / k_bh_targets with far nodes in FP32 (near field FP64)
+// k_bh_particles / k_bh_targets with far nodes and leaf pairs in FP32
 template <bool V, bool S, bool D>
 __global__ void __launch_bounds__(128) k_bh_particles_f32(const BHNode* __restrict__ nodes,
                                                           const BHNodeF* __restrict__ fn, int nn,
@@ -476,6 +572,7 @@ __global__ void __launch_bounds__(128) k_bh_targets_w(const BHNode* __restrict__
             for (int32_t k = L.x + lane; k < L.x + L.y; k += 32) {
                 const Tgt mb = load_part_g(slots, k);
                 if (mb.idx == t.idx) continue;
+                if (F32 && leaf_pair_f<V, S, D>(mb, t, tf, cf, fv, fs, fd)) continue;
                 if (V) v = v + vel_gauss_sym(mb, t, c);
                 if (S) s = s + stretch(mb, t, c);
                 if (D) d = d + diffusion(mb, t, c);
@@ -547,7 +644,12 @@ __global__ void __launch_bounds__(128) k_bh_points_w(const BHNode* __restrict__ 
     while (i < nn) {
         const int4 L = load_links(nodes, i);
         if (L.w) {
-            for (int32_t k = L.x + lane; k < L.x + L.y; k += 32) v = v + vel_alg(load_part_g(parts, k), x, c);
+            for (int32_t k = L.x + lane; k < L.x + L.y; k += 32) {
+                if (F32)
+                    leaf_alg_f(load_part_g(parts, k), x, i4p, fv);
+                else
+                    v = v + vel_alg(load_part_g(parts, k), x, c);
+            }
             i++;
             continue;
         }
@@ -620,7 +722,7 @@ __global__ void __launch_bounds__(128) k_bh_points(const BHNode* __restrict__ no
     vel[3 * q + 2] = v.z;
 }
 
-// k_bh_points with far nodes in FP32 (algebraic core; leaves FP64)
+// k_bh_points with far nodes and leaf members in FP32 (algebraic core)
 __global__ void __launch_bounds__(128) k_bh_points_f32(const BHNode* __restrict__ nodes,
                                                        const BHNodeF* __restrict__ fn, int nn,
                                                        const BHPart* __restrict__ parts, double theta,
@@ -638,7 +740,7 @@ __global__ void __launch_bounds__(128) k_bh_points_f32(const BHNode* __restrict_
     while (i < nn) {
         const int4 L = load_links(nodes, i);
         if (L.w) {
-            for (int32_t k = L.x; k < L.x + L.y; k++) v = v + vel_alg(load_part_g(parts, k), x, c);
+            for (int32_t k = L.x; k < L.x + L.y; k++) leaf_alg_f(load_part_g(parts, k), x, i4p, fv);
             i++;
             continue;
         }
@@ -674,12 +776,21 @@ constexpr int kTile = 128;
 // VK: 0 none, 1 gauss_sym (self skipped), 2 gauss_poi, 3 alg.  S/D: the direct
 // stretching/diffusion of cpCaseVP::particleStrengthUpdate (`this` = target, j != i).
 // Targets are particles (tgt != null) or points (pts).
+// Block (x, y) sums the sources [y * chunk, min(n, (y + 1) * chunk)) and writes its part of
+// each output at offset y * ystride: with one source range (chunk >= n) straight into the
+// outputs, else into per-range slices that k_direct_reduce adds up in range order.
 template <int VK, bool S, bool D>
 __global__ void __launch_bounds__(kTile) k_direct(const BHPart* __restrict__ src, int64_t n,
                                                   const BHPart* __restrict__ tgt, const double* __restrict__ pts,
                                                   int64_t m, VPConst c, double* __restrict__ vel,
-                                                  double* __restrict__ str, double* __restrict__ dif) {
+                                                  double* __restrict__ str, double* __restrict__ dif, int64_t chunk,
+                                                  int64_t ystride) {
     __shared__ BHPart tile[kTile];
+    const int64_t b0 = blockIdx.y * chunk;
+    const int64_t b1 = b0 + chunk < n ? b0 + chunk : n;
+    vel += blockIdx.y * ystride;
+    str += blockIdx.y * ystride;
+    dif += blockIdx.y * ystride;
     int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     bool live = q < m;
     Tgt t{mk3(0, 0, 0), 0, mk3(0, 0, 0), -1.0};
@@ -690,11 +801,11 @@ __global__ void __launch_bounds__(kTile) k_direct(const BHPart* __restrict__ src
             t.x = ld3(pts + 3 * q);
     }
     dv3 v = mk3(0, 0, 0), s = mk3(0, 0, 0), d = mk3(0, 0, 0);
-    for (int64_t b = 0; b < n; b += kTile) {
+    for (int64_t b = b0; b < b1; b += kTile) {
         __syncthreads();
-        if (b + threadIdx.x < n) tile[threadIdx.x] = src[b + threadIdx.x];
+        if (b + threadIdx.x < b1) tile[threadIdx.x] = src[b + threadIdx.x];
         __syncthreads();
-        int lim = (int)((n - b) < kTile ? (n - b) : kTile);
+        int lim = (int)((b1 - b) < kTile ? (b1 - b) : kTile);
         if (!live) continue;
         for (int k = 0; k < lim; k++) {
             const Tgt p = load_part(tile[k]);
@@ -710,6 +821,21 @@ __global__ void __launch_bounds__(kTile) k_direct(const BHPart* __restrict__ src
     if (VK) { vel[3 * q] = v.x; vel[3 * q + 1] = v.y; vel[3 * q + 2] = v.z; }
     if (S) { str[3 * q] = s.x; str[3 * q + 1] = s.y; str[3 * q + 2] = s.z; }
     if (D) { dif[3 * q] = d.x; dif[3 * q + 1] = d.y; dif[3 * q + 2] = d.z; }
+}
+
+// out_o[i] = sum over ranges y of part[o * ns * len + y * len + i], ranges in order
+__global__ void k_direct_reduce(const double* __restrict__ part, int ns, int64_t len, double* __restrict__ o0,
+                                double* __restrict__ o1, double* __restrict__ o2) {
+    int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= len) return;
+    double* outs[3] = {o0, o1, o2};
+    for (int o = 0; o < 3; o++) {
+        if (!outs[o]) continue;
+        const double* p = part + (int64_t)o * ns * len + i;
+        double a = 0;
+        for (int y = 0; y < ns; y++) a += p[(int64_t)y * len];
+        outs[o][i] = a;
+    }
 }
 
 __global__ void k_pack_parts(const double* __restrict__ pos, const double* __restrict__ str,
@@ -840,11 +966,49 @@ cudaError_t launch_pack_parts(const double* pos, const double* str, const double
     return cudaGetLastError();
 }
 
+namespace {
+int device_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0, v = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        n = v > 0 ? v : 1;
+    }
+    return n;
+}
+
+// source ranges for m targets over n sources: enough blocks for about eight per SM,
+// ranges of whole tiles
+int64_t direct_ranges(int64_t n, int64_t m) {
+    const int64_t tb = blocks(m, kTile), tiles = blocks(n, kTile);
+    const int64_t want = (8 * (int64_t)device_sms() + tb - 1) / tb;
+    int64_t r = want < tiles ? want : tiles;
+    return r > 1 ? r : 1;
+}
+}  // namespace
+
+int64_t direct_scratch_doubles(int64_t n, int64_t m) {
+    const int64_t r = direct_ranges(n, m);
+    return r > 1 ? 9 * m * r : 0;
+}
+
 cudaError_t launch_direct(int vk, bool S, bool D, const BHPart* src, int64_t n, const BHPart* tgt, const double* pts,
-                          int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s) {
+                          int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s,
+                          double* scratch, int64_t scratch_doubles) {
     if (m <= 0) return cudaSuccess;
-    dim3 g(blocks(m, kTile)), b(kTile);
-#define CPG_DIRECT(VK_, S_, D_) k_direct<VK_, S_, D_><<<g, b, 0, s>>>(src, n, tgt, pts, m, c, vel, str, dif)
+    int64_t ranges = direct_ranges(n, m);
+    if (!scratch || scratch_doubles < 9 * m * ranges) ranges = 1;
+    const int64_t chunk = ranges > 1 ? kTile * ((blocks(n, kTile) + ranges - 1) / ranges) : (n > 0 ? n : 1);
+    if (ranges > 1) ranges = (n + chunk - 1) / chunk;
+    dim3 g(blocks(m, kTile), (unsigned)ranges), b(kTile);
+    const int64_t len = 3 * m;
+    double* kv = ranges > 1 ? scratch : vel;
+    double* ks = ranges > 1 ? scratch + ranges * len : str;
+    double* kd = ranges > 1 ? scratch + 2 * ranges * len : dif;
+    const int64_t ystride = ranges > 1 ? len : 0;
+#define CPG_DIRECT(VK_, S_, D_) \
+    k_direct<VK_, S_, D_><<<g, b, 0, s>>>(src, n, tgt, pts, m, c, kv, ks, kd, chunk, ystride)
     int key = vk * 4 + (S ? 2 : 0) + (D ? 1 : 0);
     switch (key) {
         case 4: CPG_DIRECT(1, false, false); break;
@@ -859,6 +1023,9 @@ cudaError_t launch_direct(int vk, bool S, bool D, const BHPart* src, int64_t n, 
         default: return cudaErrorInvalidValue;
     }
 #undef CPG_DIRECT
+    if (ranges > 1)
+        k_direct_reduce<<<blocks(len, 256), 256, 0, s>>>(scratch, (int)ranges, len, vk ? vel : nullptr,
+                                                          S ? str : nullptr, D ? dif : nullptr);
     return cudaGetLastError();
 }
 

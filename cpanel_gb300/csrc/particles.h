@@ -31,9 +31,14 @@ cudaError_t launch_refresh_slots(const int64_t* perm, int64_t ns, const double* 
                                  const double* rad, BHPart* slots, cudaStream_t s);
 cudaError_t launch_bh_points(const BHNode* nodes, const BHNodeF* fnodes, int nn, const BHPart* parts, double theta,
                              const double* pts, int64_t m, const VPConst& c, double* vel, cudaStream_t s);
-// vk: 0 none, 1 symmetrised Gaussian (particle targets), 2 Gaussian at points, 3 algebraic
+// vk: 0 none, 1 symmetrised Gaussian (particle targets), 2 Gaussian at points, 3 algebraic.
+// With scratch of at least direct_scratch_doubles(n, m) doubles, few targets over many
+// sources split the sources into ranges summed by separate blocks and added in range order
+// (the same sum in a different association); without it one block row takes all sources.
 cudaError_t launch_direct(int vk, bool S, bool D, const BHPart* src, int64_t n, const BHPart* tgt, const double* pts,
-                          int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s);
+                          int64_t m, const VPConst& c, double* vel, double* str, double* dif, cudaStream_t s,
+                          double* scratch = nullptr, int64_t scratch_doubles = 0);
+int64_t direct_scratch_doubles(int64_t n, int64_t m);
 // panel records (24 doubles) of m free triangles (vertices m x 9)
 cudaError_t launch_pack_records(const double* verts, int64_t m, double* rec, cudaStream_t s);
 // Panel-induced velocity at points: body records (sigma, mu) and wake records (mu_w)

@@ -146,8 +146,9 @@ struct cpg_vpcase {
     cpg::ParticleTree T;
     bool tree_built = false;
     Buf tnodes, tperm, tslots;
-    // device: shedding evaluation points; scratch of the chunked panel kernels
-    Buf spts, sout, scr;
+    // device: shedding evaluation points; scratch of the chunked panel kernels and of the
+    // source-split direct sums
+    Buf spts, sout, scr, dsplit;
     std::vector<double> filh;  // host copy of the filaments (8 per w2 panel)
     bool have_fil = false;
     // Trefftz plane (cpCase CL_trefftz / CD_trefftz) and the early stop
@@ -188,6 +189,17 @@ cudaError_t refresh_slots(cpg_vpcase& S) {
                                      S.str.as<double>(), S.rad.as<double>(), S.tslots.as<cpg::BHPart>(), S.s);
 }
 
+// direct sums over n sources at m targets, source ranges split across blocks when the
+// targets alone would leave the GPU idle
+cudaError_t direct_sums(cpg_vpcase& S, int vk, bool st, bool df, int64_t n, const cpg::BHPart* tgt, const double* pts,
+                   int64_t m, double* vel, double* str, double* dif) {
+    const int64_t need = cpg::direct_scratch_doubles(n, m);
+    cudaError_t e;
+    if (need > 0 && (e = S.dsplit.ensure(sizeof(double) * need, S.s)) != cudaSuccess) return e;
+    return cpg::launch_direct(vk, st, df, S.packed.as<cpg::BHPart>(), n, tgt, pts, m, cpg::vp_constants(), vel, str,
+                              dif, S.s, S.dsplit.as<double>(), need);
+}
+
 // particle velocity term at m points: Barnes-Hut (algebraic) or direct Gaussian sums over
 // the first nsrc particles
 cudaError_t particle_term_points(cpg_vpcase& S, bool bh, const double* pts, int64_t m, int64_t nsrc, double* out) {
@@ -201,8 +213,7 @@ cudaError_t particle_term_points(cpg_vpcase& S, bool bh, const double* pts, int6
                                      cpg::vp_constants(), out, S.s);
     }
     if (nsrc <= 0) return cudaMemsetAsync(out, 0, sizeof(double) * 3 * m, S.s);
-    return cpg::launch_direct(2, false, false, S.packed.as<cpg::BHPart>(), nsrc, nullptr, pts, m, cpg::vp_constants(),
-                              out, nullptr, nullptr, S.s);
+    return direct_sums(S, 2, false, false, nsrc, nullptr, pts, m, out, nullptr, nullptr);
 }
 
 cudaError_t ensure_particles(cpg_vpcase& S, int64_t cap) {
@@ -650,8 +661,8 @@ cudaError_t step_once(cpg_vpcase& S) {
         } else if (S.accelerate && S.timestep > 2) {
             if ((e = cudaMemsetAsync(S.tP.p, 0, sizeof(double) * 3 * m, S.s)) != cudaSuccess) return e;
         } else {
-            if ((e = cpg::launch_direct(2, false, false, S.packed.as<cpg::BHPart>(), m, S.packed.as<cpg::BHPart>(),
-                                        nullptr, m, c, S.tP.as<double>(), nullptr, nullptr, S.s)) != cudaSuccess)
+            if ((e = direct_sums(S, 2, false, false, m, S.packed.as<cpg::BHPart>(), nullptr, m, S.tP.as<double>(), nullptr,
+                            nullptr)) != cudaSuccess)
                 return e;
         }
         if ((e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s)) != cudaSuccess) return e;
@@ -687,8 +698,8 @@ cudaError_t step_once(cpg_vpcase& S) {
             if ((e = cudaMemsetAsync(S.tS.p, 0, sizeof(double) * 3 * m, S.s)) != cudaSuccess) return e;
             if ((e = cudaMemsetAsync(S.tD.p, 0, sizeof(double) * 3 * m, S.s)) != cudaSuccess) return e;
         } else {
-            if ((e = cpg::launch_direct(0, true, true, S.packed.as<cpg::BHPart>(), m, S.packed.as<cpg::BHPart>(), nullptr,
-                                        m, c, nullptr, S.tS.as<double>(), S.tD.as<double>(), S.s)) != cudaSuccess)
+            if ((e = direct_sums(S, 0, true, true, m, S.packed.as<cpg::BHPart>(), nullptr, m, nullptr, S.tS.as<double>(),
+                            S.tD.as<double>())) != cudaSuccess)
                 return e;
         }
         if ((e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s)) != cudaSuccess) return e;
@@ -857,7 +868,7 @@ void cpg_vpcase_destroy(cpg_vpcase* S) {
     Buf* all[] = {&S->rec, &S->q1, &S->q2, &S->widx, &S->wcoef, &S->par, &S->A, &S->B, &S->C, &S->work,
                   &S->sigma, &S->mu, &S->mu1, &S->prev1, &S->mu2, &S->prev2, &S->rhs, &S->fil, &S->vcent,
                   &S->pos, &S->str, &S->rad, &S->pvel, &S->pstr, &S->packed, &S->tP, &S->tQ, &S->tS, &S->tD,
-                  &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr,
+                  &S->tPan, &S->tnodes, &S->tperm, &S->tslots, &S->spts, &S->sout, &S->scr, &S->dsplit,
                   &S->fnodes, &S->A32, &S->Alo, &S->LU, &S->bad, &S->Ainv, &S->vtot, &S->p_bez, &S->p_clp,
                   &S->p_cli, &S->p_tip, &S->p_ts, &S->p_F3, &S->p_F2, &S->p_mode, &S->p_cs, &S->p_work, &S->p_out};
     for (Buf* b : all) b->release();
@@ -918,8 +929,7 @@ int cpg_vpcase_velocities(cpg_vpcase* Sp, int precision, int direct, double* vel
     // particle term as convectParticles takes it (or the FP64 direct sum)
     if (e == cudaSuccess) {
         if (direct)
-            e = cpg::launch_direct(1, false, false, S.packed.as<cpg::BHPart>(), m, S.packed.as<cpg::BHPart>(), nullptr,
-                                   m, c, S.tP.as<double>(), nullptr, nullptr, S.s);
+            e = direct_sums(S, 1, false, false, m, S.packed.as<cpg::BHPart>(), nullptr, m, S.tP.as<double>(), nullptr, nullptr);
         else if (S.accelerate && S.tree_built && S.T.nodes.size() > 1) {
             e = refresh_slots(S);
             if (e == cudaSuccess)
@@ -929,8 +939,7 @@ int cpg_vpcase_velocities(cpg_vpcase* Sp, int precision, int direct, double* vel
         } else if (S.accelerate)
             e = cudaMemsetAsync(S.tP.p, 0, sizeof(double) * 3 * m, S.s);
         else
-            e = cpg::launch_direct(2, false, false, S.packed.as<cpg::BHPart>(), m, S.packed.as<cpg::BHPart>(), nullptr,
-                                   m, c, S.tP.as<double>(), nullptr, nullptr, S.s);
+            e = direct_sums(S, 2, false, false, m, S.packed.as<cpg::BHPart>(), nullptr, m, S.tP.as<double>(), nullptr, nullptr);
     }
     if (e == cudaSuccess) e = S.scr.ensure(sizeof(double) * cpg::vp_scratch_doubles(m, S.n), S.s);
     if (e == cudaSuccess)

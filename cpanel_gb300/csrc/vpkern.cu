@@ -53,11 +53,12 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part(const double* __restri
                                                           const double* __restrict__ sigma,
                                                           const double* __restrict__ mu, int64_t nb,
                                                           int64_t chunk, const double* __restrict__ pts, int64_t m,
-                                                          double skip_r, double* __restrict__ part) {
+                                                          double skip_r, double* __restrict__ part, int64_t sinv) {
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = q < m;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = t < m;
+    const int64_t q = live ? (int64_t)(((uint64_t)t * (uint64_t)sinv) % (uint64_t)m) : 0;
     dv3 poi = live ? ld3(pts + 3 * q) : mk3(0, 0, 0);
     if (live && skip_r > 0 && norm3(poi) > skip_r) live = false;
     const int64_t jb = (int64_t)blockIdx.y * chunk, je = min(nb, jb + chunk);
@@ -78,7 +79,7 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part(const double* __restri
             acc = acc + (ts[k] * vs + tm[k] * vd);
         }
     }
-    if (q >= m) return;
+    if (t >= m) return;
     double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
     o[0] = acc.x;
     o[1] = acc.y;
@@ -143,11 +144,12 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part(const double* __restrict
                                                         const double* __restrict__ mu, int64_t nb, int64_t chunk,
                                                         const double* __restrict__ pos,
                                                         const double* __restrict__ str, int64_t m, double skip_x,
-                                                        double* __restrict__ part) {
+                                                        double* __restrict__ part, int64_t sinv) {
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = q < m;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = t < m;
+    const int64_t q = live ? (int64_t)(((uint64_t)t * (uint64_t)sinv) % (uint64_t)m) : 0;
     dv3 x = live ? ld3(pos + 3 * q) : mk3(0, 0, 0);
     dv3 a = live ? ld3(str + 3 * q) : mk3(0, 0, 0);
     if (live && skip_x > 0 && fabs(x.x) > skip_x) live = false;
@@ -185,7 +187,7 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part(const double* __restrict
             acc = acc + mul_m3(G, a);
         }
     }
-    if (q >= m) return;
+    if (t >= m) return;
     double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
     o[0] = acc.x;
     o[1] = acc.y;
@@ -310,14 +312,15 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part_f32(const double* __re
                                                               const double* __restrict__ sigma,
                                                               const double* __restrict__ mu, int64_t nb,
                                                               int64_t chunk, const double* __restrict__ pts,
-                                                              int64_t m, double skip_r, double* __restrict__ part) {
+                                                              int64_t m, double skip_r, double* __restrict__ part, int64_t sinv) {
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
     __shared__ float ft[TILE * FT_STRIDE];
     __shared__ NearQueue nq;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = q < m;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = t < m;
+    const int64_t q = live ? (int64_t)(((uint64_t)t * (uint64_t)sinv) % (uint64_t)m) : 0;
     dv3 poi = live ? ld3(pts + 3 * q) : mk3(0, 0, 0);
     if (live && skip_r > 0 && norm3(poi) > skip_r) live = false;
     nq.put_target(w, lane, poi, mk3(0, 0, 0));
@@ -366,7 +369,7 @@ __global__ void __launch_bounds__(VT) k_vp_panel_vel_part_f32(const double* __re
             acc = nq.gather(w, lane, base, qn, acc);
         }
     }
-    if (q >= m) return;
+    if (t >= m) return;
     acc = acc + fa.value();
     double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
     o[0] = acc.x;
@@ -379,14 +382,15 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part_f32(const double* __rest
                                                             const double* __restrict__ mu, int64_t nb, int64_t chunk,
                                                             const double* __restrict__ pos,
                                                             const double* __restrict__ str, int64_t m,
-                                                            double skip_x, double* __restrict__ part) {
+                                                            double skip_x, double* __restrict__ part, int64_t sinv) {
     __shared__ double tile[TILE * R_STRIDE];
     __shared__ double ts[TILE], tm[TILE];
     __shared__ float ft[TILE * FT_STRIDE];
     __shared__ NearQueue nq;
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool live = q < m;
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool live = t < m;
+    const int64_t q = live ? (int64_t)(((uint64_t)t * (uint64_t)sinv) % (uint64_t)m) : 0;
     dv3 x = live ? ld3(pos + 3 * q) : mk3(0, 0, 0);
     dv3 a = live ? ld3(str + 3 * q) : mk3(0, 0, 0);
     if (live && skip_x > 0 && fabs(x.x) > skip_x) live = false;
@@ -462,7 +466,7 @@ __global__ void __launch_bounds__(VT) k_vp_stretch_part_f32(const double* __rest
             acc = nq.gather(w, lane, base, qn, acc);
         }
     }
-    if (q >= m) return;
+    if (t >= m) return;
     acc = acc + fa.value();
     double* o = part + ((int64_t)blockIdx.y * m + q) * 3;
     o[0] = acc.x;
@@ -666,6 +670,34 @@ int64_t vp_chunk_size(int64_t m, int64_t nb) {
 
 int64_t vp_scratch_doubles(int64_t m, int64_t nb) { return vp_chunks(m, nb) * m * 3; }
 
+// Target t of a panel kernel handles point (t * sinv) mod m, a bijection when sinv is
+// prime to m: points with consecutive indices (a row of particles shed in one step, which
+// meet the body panels' FP64 near field together) land in distant blocks, so that work
+// spreads over all SMs.  Each point's sums are the same in any placement.
+int64_t spread_inverse(int64_t m) {
+    if (m <= 2) return 1;
+    int64_t s = (int64_t)(0.6180339887498949 * (double)m);
+    auto gcd = [](int64_t a, int64_t b) {
+        while (b) {
+            int64_t r = a % b;
+            a = b;
+            b = r;
+        }
+        return a;
+    };
+    while (gcd(s, m) != 1) s++;
+    // inverse of s modulo m (extended Euclid)
+    int64_t r0 = m, r1 = s, t0 = 0, t1 = 1;
+    while (r1) {
+        const int64_t qq = r0 / r1, r2 = r0 - qq * r1, t2 = t0 - qq * t1;
+        r0 = r1;
+        r1 = r2;
+        t0 = t1;
+        t1 = t2;
+    }
+    return t0 < 0 ? t0 + m : t0;
+}
+
 cudaError_t vp_launch_panel_vel(const double* rec, const double* sigma, const double* mu, int64_t nb, const double* q1,
                                 const double* mu1, int64_t n1, const double* q2, const double* mu2, int64_t n2,
                                 const double* fil, int64_t nf, const double* pts, int64_t m, double skip_r,
@@ -675,10 +707,10 @@ cudaError_t vp_launch_panel_vel(const double* rec, const double* sigma, const do
     const int64_t ncu = nb > 0 ? (nb + chunk - 1) / chunk : 0;
     if (ncu > 0 && far_f32)
         k_vp_panel_vel_part_f32<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pts, m,
-                                                                               skip_r, scratch);
+                                                                               skip_r, scratch, spread_inverse(m));
     else if (ncu > 0)
         k_vp_panel_vel_part<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pts, m, skip_r,
-                                                                           scratch);
+                                                                           scratch, spread_inverse(m));
     k_vp_panel_vel_fin<<<nblk(32 * m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, q2, mu2, n2, fil, nf, pts, m, skip_r,
                                                     out);
     return cudaGetLastError();
@@ -692,10 +724,10 @@ cudaError_t vp_launch_stretch_panels(const double* rec, const double* sigma, con
     const int64_t ncu = nb > 0 ? (nb + chunk - 1) / chunk : 0;
     if (ncu > 0 && far_f32)
         k_vp_stretch_part_f32<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pos, str, m,
-                                                                             skip_x, scratch);
+                                                                             skip_x, scratch, spread_inverse(m));
     else if (ncu > 0)
         k_vp_stretch_part<<<dim3(nblk(m, VT), (unsigned)ncu), VT, 0, s>>>(rec, sigma, mu, nb, chunk, pos, str, m,
-                                                                         skip_x, scratch);
+                                                                         skip_x, scratch, spread_inverse(m));
     k_vp_stretch_fin<<<nblk(32 * m, 128), 128, 0, s>>>(scratch, ncu, q1, mu1, n1, pos, str, m, skip_x, out);
     return cudaGetLastError();
 }

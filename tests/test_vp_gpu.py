@@ -49,6 +49,18 @@ def test_direct_velocity_at_points(built, kernel):
     assert _rel(got, ref) < TOL
 
 
+@pytest.mark.parametrize("n,m", [(9001, 7), (20000, 300), (130, 1)])
+def test_direct_velocity_few_points_many_particles(built, n, m):
+    """Few targets over many sources (the Trefftz-plane downwash): the source ranges are
+    summed by separate blocks and added in order; the sum is the oracle's to 1e-12."""
+    from cpanel_gb300 import vp
+    pos, st, rad = _cloud(n, 40 + m)
+    pts = np.random.default_rng(41).normal(size=(m, 3))
+    ref = po.particles_velocity(pos, st, rad, pts, kernel="gauss")
+    got = _np(vp.particles_velocity(_cuda(pos), _cuda(st), _cuda(rad), _cuda(pts), kernel="gauss"))
+    assert _rel(got, ref) < TOL
+
+
 def test_direct_velocity_on_particles(built):
     from cpanel_gb300 import vp
     pos, st, rad = _cloud(1200, 3)

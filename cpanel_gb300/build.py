@@ -78,7 +78,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    link = [NVCC, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-lcublas", "-Xcompiler", "-pthread"]
+    link = [NVCC, "-shared", "-o", tmp] + objs + ARCH + ["-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))

@@ -3,7 +3,6 @@
 // A cpg_geometry owns its device tables; matrices are assembled lazily per
 // precision and kept resident, so further cases on the same mesh reuse them
 // (the reference assembles once per geometry too, CPanel/geometry.cpp:607-621).
-#include <cublas_v2.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,7 +35,6 @@ struct cpg_ctx {
     cudaStream_t aux = nullptr;  // per-geometry tables built beside the solve
     std::string err;
     cpg::Prof* prof = nullptr;  // device-time accounting, when enabled
-    cublasHandle_t blas = nullptr;
     int particle_precision = CPG_PLAIN_FP64;  // cpg_panels_velocity / cpg_panels_stretching
     std::vector<cpg_ctx*> workers;  // contexts of cpg_batch_solve, created on first use
     // matrix buffers of destroyed geometries, kept for the next geometry of a similar size
@@ -48,7 +46,6 @@ struct cpg_ctx {
         cudaEvent_t ev;
     };
     std::vector<Spare> spare;
-    void* blas_ws[2] = {nullptr, nullptr};  // cuBLAS workspaces shared by the context's factorizations
 };
 
 namespace {
@@ -147,10 +144,6 @@ cudaError_t ensure_big(cpg_ctx* c, DevBuf& b, size_t bytes) {
     return e;
 }
 
-// the context's two cuBLAS workspaces for g's factorization and substitutions (one pair per
-// context: its work is ordered on its streams)
-cudaError_t attach_blas_ws(cpg_geometry* g);
-
 constexpr double kPi = 3.14159265358979323846;
 // Relative residual at which the mixed path's refinement stops (per right-hand side).
 // 1e-10 (two passes) measured Cp errors of 4.9e-6 against the plain path on the 19k
@@ -185,22 +178,6 @@ struct cpg_geometry {
     float ms_asm = 0;
 };
 
-namespace {
-cudaError_t attach_blas_ws(cpg_geometry* g) {
-    if (g->graphs.workspace) return cudaSuccess;
-    cpg_ctx* c = g->ctx;
-    for (void*& w : c->blas_ws)
-        if (!w) {
-            cudaError_t e = cudaMalloc(&w, cpg::lu_blas_workspace_bytes());
-            if (e != cudaSuccess) return e;
-        }
-    g->graphs.workspace = c->blas_ws[0];
-    g->graphs.workspace2 = c->blas_ws[1];
-    g->graphs.shared_ws = true;
-    return cudaSuccess;
-}
-}  // namespace
-
 struct cpg_ptree {
     cpg_ctx* ctx = nullptr;
     cpg::ParticleTree T;
@@ -214,17 +191,6 @@ void ctx_set_error(cpg_ctx* ctx, const std::string& msg) {
 }
 cudaStream_t ctx_stream(cpg_ctx* ctx) { return ctx ? ctx->stream : nullptr; }
 int ctx_particle_precision(cpg_ctx* ctx) { return ctx ? ctx->particle_precision : CPG_PLAIN_FP64; }
-void* ctx_blas(cpg_ctx* ctx) {
-    if (!ctx) return nullptr;
-    if (!ctx->blas) {
-        if (cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) {
-            ctx->blas = nullptr;
-            return nullptr;
-        }
-        cublasSetStream(ctx->blas, ctx->stream);
-    }
-    return ctx->blas;
-}
 int ctx_device(cpg_ctx* ctx) { return ctx ? ctx->device : 0; }
 // the first w worker contexts of ctx (created on first use, destroyed with ctx)
 int ctx_workers(cpg_ctx* ctx, int w, std::vector<cpg_ctx*>& out) {
@@ -383,10 +349,7 @@ void cpg_destroy(cpg_ctx* c) {
         cudaFree(sp.p);
     }
     c->spare.clear();
-    for (void*& w : c->blas_ws)
-        if (w) cudaFree(w);
     delete c->prof;
-    if (c->blas) cublasDestroy(c->blas);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     if (c->aux) cudaStreamDestroy(c->aux);
     delete c;
@@ -727,26 +690,20 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
         CK(cpg::solve_fp64(g->A64.as<double>(), n, k, rhs, mu, g->work.p, 2.220446049250313e-16, 2 * n, &st, s),
            "BiCGSTAB (FP64)");
     } else {
-        if (!ctx->blas && cublasCreate(&ctx->blas) != CUBLAS_STATUS_SUCCESS) {
-            ctx->blas = nullptr;
-            return fail(ctx, CPG_E_CUDA, "cublasCreate failed");
-        }
         if (!g->lu_ready) {  // per-geometry factorization, reused by every case
             CK(ensure_big(g->ctx, g->LU, sizeof(float) * (size_t)n * n), "alloc LU");
-            CK(attach_blas_ws(g), "alloc cuBLAS workspaces");
             CK(g->bad.ensure(sizeof(int)), "alloc flag");
             CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
             CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");
-            CK(cpg::lu_factor_fp32(ctx->blas, &g->graphs, g->LU.as<float>(), n, g->bad.as<int>(), s),
+            CK(cpg::lu_factor_fp32(&g->graphs, g->LU.as<float>(), n, g->bad.as<int>(), s),
                "LU factorization");
             g->lu_ready = true;
         }
         size_t wb = cpg::solve_lu_work_bytes(n, k);
         CK(g->work.ensure(wb), "alloc solver workspace");
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");
-        CK(cpg::solve_lu_refined(ctx->blas, &g->graphs, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(),
-                                 n, k, rhs, mu,
-                                 g->work.p, kMixedRefineTol, 16, &st, s),
+        CK(cpg::solve_lu_refined(&g->graphs, g->A32.as<float>(), g->Alo.as<float>(), g->LU.as<float>(), n, k, rhs,
+                                 mu, g->work.p, kMixedRefineTol, 16, &st, s),
            "refined solve (mixed)");
     }
     CK(cudaEventRecord(e1, s), "event");
@@ -1528,8 +1485,6 @@ static int lu_factor_grouped_impl(cpg_geometry* const* gs, int m, double* ms_out
     }
     CK(cudaSetDevice(ctx->device), "device");
     cudaStream_t s = ctx->stream;
-    void* blas = cpg::ctx_blas(ctx);
-    if (!blas) return fail(ctx, CPG_E_CUDA, "cublasCreate failed");
     std::vector<cpg_ctx*> others;
     for (int q = 0; q < m; q++)
         if (gs[q]->ctx != ctx && std::find(others.begin(), others.end(), gs[q]->ctx) == others.end())
@@ -1558,7 +1513,6 @@ static int lu_factor_grouped_impl(cpg_geometry* const* gs, int m, double* ms_out
         cpg_geometry* g = gs[q];
         const int64_t n = g->H.n_body;
         CK(ensure_big(g->ctx, g->LU, sizeof(float) * (size_t)n * n), "alloc LU");
-        CK(attach_blas_ws(g), "alloc cuBLAS workspaces");
         CK(g->bad.ensure(sizeof(int)), "alloc flag");
         CK(cudaMemsetAsync(g->bad.p, 0, sizeof(int), s), "clear flag");
         CK(cudaMemcpyAsync(g->LU.p, g->A32.p, sizeof(float) * (size_t)n * n, cudaMemcpyDeviceToDevice, s), "copy A");
@@ -1568,7 +1522,7 @@ static int lu_factor_grouped_impl(cpg_geometry* const* gs, int m, double* ms_out
         bad[q] = g->bad.as<int>();
     }
     CK(cudaEventRecord(e0, s), "event");
-    CK(cpg::lu_factor_batched(blas, G.data(), LU.data(), ns.data(), bad.data(), m, s), "grouped LU factorization");
+    CK(cpg::lu_factor_batched(G.data(), LU.data(), ns.data(), bad.data(), m, s), "grouped LU factorization");
     CK(cudaEventRecord(e1, s), "event");
     for (cpg_ctx* c : others) CK(cudaStreamWaitEvent(c->stream, e1, 0), "join");
     CK(cudaEventSynchronize(e1), "grouped LU factorization");

@@ -126,35 +126,34 @@ cudaError_t column_norms2(const double* v, int64_t n, int k, double* part, doubl
 // The same into dd[0..k) on the device (no copy, no synchronization).
 cudaError_t column_norms2_device(const double* v, int64_t n, int k, double* part, double* dd, cudaStream_t s);
 
-// lu.cu: FP32 LU without pivoting (blocked, cuBLAS trailing GEMM) and the refined
-// solve x = A^{-1} b against A = A32 + Alo.  blas: a cublasHandle_t.  The substitutions
-// are captured once into a CUDA graph held in LuGraphs and replayed.
+// lu.cu: FP32 LU without pivoting (blocked; diagonal blocks on the CUDA cores, panel products
+// and trailing updates on the tensor cores) and the refined solve x = A^{-1} b against
+// A = A32 + Alo.  The substitutions are captured once into a CUDA graph held in LuGraphs and
+// replayed.
 struct LuGraphs {
     cudaGraphExec_t solve = nullptr;
     int64_t factor_n = 0;
     const float* solve_LU = nullptr;
     const float* solve_X = nullptr;
     int solve_k = 0;
-    void* workspace = nullptr;  // cuBLAS workspace (no allocation inside a capture)
-    void* workspace2 = nullptr; // cuBLAS workspace of the panel stream
-    bool shared_ws = false;     // both workspaces belong to the caller (not freed by release)
-    cudaStream_t panel_stream = nullptr;  // high-priority stream of the panel factorizations
-    cudaEvent_t ev_update = nullptr, ev_panel = nullptr;  // fork / join inside the capture
-    float* dinv = nullptr;      // inverses of the diagonal blocks (L then U per block)
-    float* panel = nullptr;     // n x 128 staging for the panel GEMMs
+    cudaStream_t panel_stream = nullptr;  // high-priority stream of the diagonal-block factorizations
+    cudaStream_t inv_stream = nullptr;    // and of the diagonal blocks' inverses beside them
+    cudaEvent_t ev_update = nullptr, ev_panel = nullptr;  // fork / join between the streams
+    cudaEvent_t ev_diag = nullptr, ev_inv = nullptr;
+    float* dinv = nullptr;      // inverses of the 128-column diagonal blocks (L then U per block)
     float* tmp = nullptr;       // n x k intermediate of the substitutions
     size_t tmp_floats = 0;
     float* dinv4 = nullptr;     // inverses of the full 1,024-column diagonal blocks (L then U)
-    float* super_tmp = nullptr; // 512 x 512 scratch per 1,024-column block while they are built
+    float* super_tmp = nullptr; // tile scratch while one of them is built
     int64_t super_n = 0;        // order they were built for (0: none, the substitutions use dinv)
-    int64_t super_cap = 0;      // 1,024-column blocks dinv4 and super_tmp hold
-    void* tc_mem = nullptr;     // split FP16 operands of the tensor-core rank-OB updates
+    int64_t super_cap = 0;      // 1,024-column blocks dinv4 holds
+    void* tc_mem = nullptr;     // split FP16 operands of the tensor-core products
     size_t tc_bytes = 0;
     void release();
 };
-cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);
-// bytes of each of the two cuBLAS workspaces a LuGraphs uses
-size_t lu_blas_workspace_bytes();
+cudaError_t lu_factor_fp32(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);
+// device bytes lu_factor_fp32 allocates for an n x n factorization (inverses, operands, scratch)
+size_t lu_factor_bytes(int64_t n);
 // One matrix of a lockstep factorization (device copy).
 struct LuBatchMesh {
     float* LU;
@@ -164,9 +163,9 @@ struct LuBatchMesh {
 };
 // The factorization of lu_factor_fp32 for m matrices at once (LUs[q]: n_q x n_q, A32 copied
 // in; Gs[q] receives the diagonal-block inverses the substitutions use), every block step
-// taken for all matrices in one launch.  Issued on s with the cuBLAS handle blas.
-cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs, const int64_t* ns,
-                              int* const* bads, int m, cudaStream_t s);
+// taken for all matrices in one launch.  Issued on s.
+cudaError_t lu_factor_batched(LuGraphs* const* Gs, float* const* LUs, const int64_t* ns, int* const* bads, int m,
+                              cudaStream_t s);
 // One system of a lockstep refined solve: A = A32 + Alo (n x n), its FP32 factors LU with
 // the diagonal-block inverses dinv (from lu_factor_fp32 or lu_factor_batched), k right-hand
 // sides rhs (k x n) -> x; work: solve_lu_work_bytes(n, k) bytes.
@@ -190,16 +189,16 @@ struct RefineMesh {
 // system's conversions, residual and norms on its own stream (joined and forked by events).
 cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, int max_steps, SolveStats* st,
                                      cudaStream_t s);
-cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
+cudaError_t lu_solve_fp32(LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s);
 size_t solve_lu_work_bytes(int64_t n, int k);
 // Ainv (optional): an FP32 inverse of A; the correction of each pass is then Ainv r
 // instead of the two substitutions with LU (LU may be null).
-cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n,
-                             int k, const double* rhs, double* x, void* work, double tol, int max_steps,
-                             SolveStats* st, cudaStream_t s, const float* Ainv = nullptr);
+cudaError_t solve_lu_refined(LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n, int k,
+                             const double* rhs, double* x, void* work, double tol, int max_steps, SolveStats* st,
+                             cudaStream_t s, const float* Ainv = nullptr);
 // Ainv (n x n) = U^{-1} L^{-1} from the factors (n substitutions at once); frees the
 // n x n scratch afterwards.
-cudaError_t lu_invert_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* Ainv, cudaStream_t s);
+cudaError_t lu_invert_fp32(LuGraphs* G, const float* LU, int64_t n, float* Ainv, cudaStream_t s);
 
 // y(k x n) = alpha * M x(k x n) for column-major FP64 M (used for -B sigma).
 cudaError_t gemm_fp64_nk(const double* M, int64_t n, int k, const double* x, double* y, double alpha, void* work,

@@ -3,12 +3,10 @@
 //
 // The panel matrix has a -0.5 self term on the diagonal; measured pivot growth of
 // the unpivoted factorization is 1.00003 on the synthetic wings, and refinement
-// with an exact-product residual reaches 1e-14 relative in three to four steps.
-// Diagonal blocks and the two triangular block solves are hand-written kernels;
-// the trailing update A22 -= L21 U12 is a plain GEMM issued through cuBLAS in
-// FP32 (or its BF16x9 tensor-core emulation, which keeps FP32 accuracy).
-#include <cublas_v2.h>
-
+// with an exact-product residual reaches 1e-12 relative in three passes.
+// Every kernel is hand-written: the diagonal blocks and the block steps inside them on the
+// CUDA cores, the panel products and the trailing updates on the tensor cores (tc_gemm.cu),
+// the substitutions as skinny products on the CUDA cores.
 #include "tc_gemm.h"
 
 #include <algorithm>
@@ -281,37 +279,31 @@ __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n
     lu_diag_body(sm, A, n, K, b, Dinv, bad);
 }
 
-// ---- lockstep factorization of many matrices (the batch path) ----
-// Every kernel below takes work items of LB_ITEM ints: mesh, r0, r1, c0, c1, K, b, unused.
+// ---- block steps of the factorization, shared by the single-matrix and the lockstep kernels ----
 // The matrices are column-major with their own order n (LU[c*n + r]).
-constexpr int LB_ITEM = 8;
 
-// diagonal block K of every listed mesh, one block of DT threads each
-__global__ void __launch_bounds__(DT) k_lu_diag_batched(const cpg::LuBatchMesh* __restrict__ ms,
-                                                        const int* __restrict__ items) {
-    extern __shared__ float sm[];
-    const int* it = items + LB_ITEM * blockIdx.x;
-    const cpg::LuBatchMesh d = ms[it[0]];
-    lu_diag_body(sm, d.LU, d.n, it[5], it[6], d.dinv, d.bad);
-}
-
-// L21 = A21 U_KK^{-1} in place for rows [r0, r1), columns K..K+b.  256 threads: thread t
-// owns row t % 64 and the 32 columns 32 (t / 64) ..; U^{-1} staged 16 rows at a time.
+// L21 = A21 U_KK^{-1} in place for rows [r0, min(r0 + 64, r1)), columns K..K+b.  256 threads:
+// thread t owns row t % 64 and the 32 columns 32 (t / 64) ..; U^{-1} staged 16 rows at a time.
 constexpr int CS_R = 64;
-__global__ void __launch_bounds__(256) k_col_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
-                                                           const int* __restrict__ items) {
-    __shared__ float X[CS_R][NB + 1];
-    __shared__ __align__(16) float U[16][NB];
-    const int* it = items + LB_ITEM * blockIdx.x;
-    const cpg::LuBatchMesh d = ms[it[0]];
-    const int64_t n = d.n, r0 = it[1], r1 = it[2], K = it[5];
-    const int b = it[6];
-    float* A = d.LU;
-    const float* Ui = d.dinv + (K / NB) * 2 * NB * NB + NB * NB;  // column-major, ld NB
+constexpr int CS_SMEM = (CS_R * (NB + 1) + 16 * NB) * 4;
+__device__ __forceinline__ void col_solve_body(float* __restrict__ A, int64_t n, const float* __restrict__ dinv,
+                                               int64_t r0, int64_t r1, int64_t K, int b, float* smem) {
+    float (*X)[NB + 1] = reinterpret_cast<float (*)[NB + 1]>(smem);
+    float (*U)[NB] = reinterpret_cast<float (*)[NB]>(smem + CS_R * (NB + 1));  // 16-byte aligned
+    const float* Ui = dinv + (K / NB) * 2 * NB * NB + NB * NB;  // column-major, ld NB
     const int t = threadIdx.x, r = t % CS_R, cg = t / CS_R;
-    for (int idx = t; idx < CS_R * NB; idx += 256) {
-        const int c = idx / CS_R, rr = idx % CS_R;
-        X[rr][c] = (r0 + rr < r1 && c < b) ? A[(K + c) * n + r0 + rr] : 0.f;
+    {
+        float v[CS_R * NB / 256];
+#pragma unroll
+        for (int q = 0; q < CS_R * NB / 256; q++) {
+            const int idx = t + 256 * q, c = idx / CS_R, rr = idx % CS_R;
+            v[q] = (r0 + rr < r1 && c < b) ? A[(K + c) * n + r0 + rr] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < CS_R * NB / 256; q++) {
+            const int idx = t + 256 * q;
+            X[idx % CS_R][idx / CS_R] = v[q];
+        }
     }
     float acc[32];
 #pragma unroll
@@ -346,24 +338,30 @@ __global__ void __launch_bounds__(256) k_col_solve_batched(const cpg::LuBatchMes
     }
 }
 
-// U12 = L_KK^{-1} A12 in place for rows K..K+b, columns [c0, c1) (at most 64).  256
-// threads: thread t owns row t % 128 and the 32 columns 32 (t / 128) ..; L^{-1} staged 16
-// columns at a time.
+// U12 = L_KK^{-1} A12 in place for rows K..K+b, columns [c0, min(c0 + 64, c1)).  256 threads:
+// thread t owns row t % 128 and the 32 columns 32 (t / 128) ..; L^{-1} staged 16 columns at a
+// time.
 constexpr int RS_C = 64;
-__global__ void __launch_bounds__(256) k_row_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
-                                                           const int* __restrict__ items) {
-    __shared__ __align__(16) float X[NB][RS_C + 4];
-    __shared__ float L[16][NB + 1];
-    const int* it = items + LB_ITEM * blockIdx.x;
-    const cpg::LuBatchMesh d = ms[it[0]];
-    const int64_t n = d.n, c0 = it[3], c1 = it[4], K = it[5];
-    const int b = it[6];
-    float* A = d.LU;
-    const float* Li = d.dinv + (K / NB) * 2 * NB * NB;  // column-major, ld NB
+constexpr int RS_SMEM = (NB * (RS_C + 4) + 16 * (NB + 1)) * 4;
+constexpr int CR_SMEM = CS_SMEM > RS_SMEM ? CS_SMEM : RS_SMEM;
+__device__ __forceinline__ void row_solve_body(float* __restrict__ A, int64_t n, const float* __restrict__ dinv,
+                                               int64_t c0, int64_t c1, int64_t K, int b, float* smem) {
+    float (*X)[RS_C + 4] = reinterpret_cast<float (*)[RS_C + 4]>(smem);  // rows of 272 bytes
+    float (*L)[NB + 1] = reinterpret_cast<float (*)[NB + 1]>(smem + NB * (RS_C + 4));
+    const float* Li = dinv + (K / NB) * 2 * NB * NB;  // column-major, ld NB
     const int t = threadIdx.x, r = t % NB, cg = t / NB;
-    for (int idx = t; idx < NB * RS_C; idx += 256) {
-        const int c = idx / NB, k = idx % NB;
-        X[k][c] = (k < b && c0 + c < c1) ? A[(c0 + c) * n + K + k] : 0.f;
+    {
+        float v[NB * RS_C / 256];
+#pragma unroll
+        for (int q = 0; q < NB * RS_C / 256; q++) {
+            const int idx = t + 256 * q, c = idx / NB, k = idx % NB;
+            v[q] = (k < b && c0 + c < c1) ? A[(c0 + c) * n + K + k] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < NB * RS_C / 256; q++) {
+            const int idx = t + 256 * q;
+            X[idx % NB][idx / NB] = v[q];
+        }
     }
     float acc[32];
 #pragma unroll
@@ -398,43 +396,59 @@ __global__ void __launch_bounds__(256) k_row_solve_batched(const cpg::LuBatchMes
     }
 }
 
-// C -= L(:, K..K+b) U(K..K+b, :) on the tile rows [r0, min(r0 + 128, r1)) x columns
-// [c0, min(c0 + 64, c1)).  128 threads, each an 8 x 8 block of C in registers (rows
-// 8 (t % 16) .., columns 8 (t / 16) ..); L and U staged GS_K columns / rows at a time and
-// read as float4 (two loads each per k for 64 FMAs).
+// acc = sum_k A[i + k lda] B[k + j ldb] for the TR x (8192 / TR) tile i < m, j < nc (A and B
+// already offset to the tile's first row and column), k < kk_n; TR = 128 or 64.  128 threads, each
+// an 8 x 8 block of the tile in registers (rows 8 (t % (TR / 8)) .., columns 8 (t / (TR / 8)) ..);
+// A and B copied GS_K columns / rows at a time into one of two shared-memory stages by cp.async
+// (the next chunk is in flight while the current one is multiplied) and read as float4 (two
+// loads each per k for 64 FMAs).  Elements outside the tile or past kk_n are zero-filled.
 constexpr int GS_R = 128, GS_C = 64, GS_K = 32;
-__global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh* __restrict__ ms,
-                                                          const int* __restrict__ items) {
-    __shared__ __align__(16) float Ls[GS_K][GS_R];
-    __shared__ __align__(16) float Us[GS_K][GS_C];
-    const int* it = items + LB_ITEM * blockIdx.x;
-    const cpg::LuBatchMesh d = ms[it[0]];
-    const int64_t n = d.n, r0 = it[1], r1 = it[2], c0 = it[3], c1 = it[4], K = it[5];
-    const int b = it[6];
-    float* A = d.LU;
-    const int t = threadIdx.x, tr = t % 16, tc = t / 16;
-    float acc[8][8];
+constexpr int GS_STAGE = GS_K * (GS_R + GS_C);
+__shared__ __align__(16) float s_tile[2 * GS_STAGE];
+__device__ __forceinline__ void cp_async4(float* dst, const float* src, bool valid) {
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(d), "l"(src), "r"(valid ? 4 : 0) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+template <int TR>
+__device__ __forceinline__ void tile_mm(const float* A, int64_t lda, const float* B, int64_t ldb, int64_t m,
+                                        int64_t nc, int kk_n, float (&acc)[8][8]) {
+    constexpr int TC = 8192 / TR, GR = TR / 8;
+    const int t = threadIdx.x, tr = t % GR, tc = t / GR;
 #pragma unroll
     for (int i = 0; i < 8; i++)
 #pragma unroll
         for (int j = 0; j < 8; j++) acc[i][j] = 0.f;
-    for (int k0 = 0; k0 < b; k0 += GS_K) {
-        __syncthreads();
-        for (int idx = t; idx < GS_K * GS_R; idx += 128) {
-            const int kk = idx / GS_R, rr = idx % GS_R;
-            Ls[kk][rr] = (k0 + kk < b && r0 + rr < r1) ? A[(K + k0 + kk) * n + r0 + rr] : 0.f;
+    auto stage = [&](int st, int k0) {
+        float* Ls = s_tile + st * GS_STAGE;  // [GS_K][TR]
+        float* Us = Ls + GS_K * TR;          // [GS_K][TC]
+        for (int idx = t; idx < GS_K * TR; idx += 128) {
+            const int kk = idx / TR, rr = idx % TR;
+            const bool v = k0 + kk < kk_n && rr < m;
+            cp_async4(Ls + idx, v ? A + (int64_t)(k0 + kk) * lda + rr : A, v);
         }
-        for (int idx = t; idx < GS_K * GS_C; idx += 128) {
+        for (int idx = t; idx < GS_K * TC; idx += 128) {
             const int kk = idx % GS_K, c = idx / GS_K;
-            Us[kk][c] = (k0 + kk < b && c0 + c < c1) ? A[(c0 + c) * n + K + k0 + kk] : 0.f;
+            const bool v = k0 + kk < kk_n && c < nc;
+            cp_async4(Us + kk * TC + c, v ? B + (int64_t)c * ldb + k0 + kk : B, v);
         }
+    };
+    if (kk_n > 0) stage(0, 0);
+    cp_async_commit();
+    for (int k0 = 0, st = 0; k0 < kk_n; k0 += GS_K, st ^= 1) {
+        if (k0 + GS_K < kk_n) stage(st ^ 1, k0 + GS_K);
+        cp_async_commit();
+        cp_async_wait1();  // this chunk's copies (all but the group just committed) have landed
         __syncthreads();
+        const float* Ls = s_tile + st * GS_STAGE;
+        const float* Us = Ls + GS_K * TR;
 #pragma unroll 4
         for (int kk = 0; kk < GS_K; kk++) {
-            const float4 a0 = *reinterpret_cast<const float4*>(&Ls[kk][8 * tr]);
-            const float4 a1 = *reinterpret_cast<const float4*>(&Ls[kk][8 * tr + 4]);
-            const float4 u0 = *reinterpret_cast<const float4*>(&Us[kk][8 * tc]);
-            const float4 u1 = *reinterpret_cast<const float4*>(&Us[kk][8 * tc + 4]);
+            const float4 a0 = *reinterpret_cast<const float4*>(&Ls[kk * TR + 8 * tr]);
+            const float4 a1 = *reinterpret_cast<const float4*>(&Ls[kk * TR + 8 * tr + 4]);
+            const float4 u0 = *reinterpret_cast<const float4*>(&Us[kk * TC + 8 * tc]);
+            const float4 u1 = *reinterpret_cast<const float4*>(&Us[kk * TC + 8 * tc + 4]);
             const float a[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
             const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
 #pragma unroll
@@ -442,7 +456,18 @@ __global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh
 #pragma unroll
                 for (int j = 0; j < 8; j++) acc[i][j] = __fmaf_rn(a[i], u[j], acc[i][j]);
         }
+        __syncthreads();  // the stage is free for the chunk after next
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// C -= L(:, K..K+b) U(K..K+b, :) on the tile rows [r0, min(r0 + 128, r1)) x columns
+// [c0, min(c0 + 64, c1)).
+__device__ __forceinline__ void gemm_sub_body(float* __restrict__ A, int64_t n, int64_t r0, int64_t r1, int64_t c0,
+                                              int64_t c1, int64_t K, int b) {
+    float acc[8][8];
+    tile_mm<GS_R>(A + K * n + r0, n, A + c0 * n + K, n, r1 - r0, c1 - c0, b, acc);
+    const int t = threadIdx.x, tr = t % 16, tc = t / 16;
 #pragma unroll
     for (int j = 0; j < 8; j++) {
         const int64_t c = c0 + 8 * tc + j;
@@ -456,6 +481,208 @@ __global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh
             }
         }
     }
+}
+
+// single matrix: the column solve of block K for rows [rb, re) (the first ceil((re - rb) / 64)
+// thread blocks, 64 rows each) and its row solve for columns [cb, ce) (the others, 64 columns
+// each), in one launch
+__global__ void __launch_bounds__(256) k_colrow_solve(float* __restrict__ A, int64_t n, const float* __restrict__ dinv,
+                                                      int64_t rb, int64_t re, int64_t cb, int64_t ce, int64_t K,
+                                                      int b) {
+    extern __shared__ __align__(16) float dsm[];
+    const int64_t nrt = (re - rb + CS_R - 1) / CS_R;
+    if ((int64_t)blockIdx.x < nrt)
+        col_solve_body(A, n, dinv, rb + (int64_t)blockIdx.x * CS_R, re, K, b, dsm);
+    else
+        row_solve_body(A, n, dinv, cb + ((int64_t)blockIdx.x - nrt) * RS_C, ce, K, b, dsm);
+}
+// single matrix: the update of rows [rb, re) x columns [cb, ce) by block K, one 128 x 64 tile
+// per thread block
+__global__ void __launch_bounds__(128) k_gemm_sub(float* __restrict__ A, int64_t n, int64_t rb, int64_t re,
+                                                  int64_t cb, int64_t ce, int64_t K, int b) {
+    gemm_sub_body(A, n, rb + (int64_t)blockIdx.x * GS_R, re, cb + (int64_t)blockIdx.y * GS_C, ce, K, b);
+}
+
+// ---- lockstep factorization of many matrices (the batch path) ----
+// Every kernel below takes work items of LB_ITEM ints: mesh, r0, r1, c0, c1, K, b, unused.
+constexpr int LB_ITEM = 8;
+
+// diagonal block K of every listed mesh, one block of DT threads each
+__global__ void __launch_bounds__(DT) k_lu_diag_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                        const int* __restrict__ items) {
+    extern __shared__ float sm[];
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    lu_diag_body(sm, d.LU, d.n, it[5], it[6], d.dinv, d.bad);
+}
+__global__ void __launch_bounds__(256) k_col_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                           const int* __restrict__ items) {
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    extern __shared__ __align__(16) float dsm[];
+    col_solve_body(d.LU, d.n, d.dinv, it[1], it[2], it[5], it[6], dsm);
+}
+__global__ void __launch_bounds__(256) k_row_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                           const int* __restrict__ items) {
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    extern __shared__ __align__(16) float dsm[];
+    row_solve_body(d.LU, d.n, d.dinv, it[3], it[4], it[5], it[6], dsm);
+}
+__global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh* __restrict__ ms,
+                                                          const int* __restrict__ items) {
+    const int* it = items + LB_ITEM * blockIdx.x;
+    const cpg::LuBatchMesh d = ms[it[0]];
+    gemm_sub_body(d.LU, d.n, it[1], it[2], it[3], it[4], it[5], it[6]);
+}
+
+// ---- inverses of the SB-column diagonal blocks, one 128-column step at a time ----
+// Step j of the inverses of the SB-column diagonal block at KO (D4: L^{-1} then U^{-1},
+// column-major, ld SB), once its 128-column block j is factored (inverses in Dinv) and the
+// L^{-1} rows and U^{-1} columns of the blocks before it are final:
+//   L^{-1}[j, c] = -L_jj^{-1} sum_{c <= k < j} L[j, k] L^{-1}[k, c]    (64-column tiles, c < j)
+//   U^{-1}[r, j] = -(sum_{r <= k < j} U^{-1}[r, k] U[k, j]) U_jj^{-1}    (64-row tiles, r < j)
+// (block indices of 128; the sums run over the columns and rows that are not zero), then the
+// rest of L^{-1}'s block row j (L_jj^{-1}, zeros to its right) and of U^{-1}'s block column j
+// (U_jj^{-1}, zeros below).  Thread blocks of 128 threads: 2j L tiles, 2j U tiles, 2 fill
+// blocks.  Each tile passes its first product through its own 8,192 floats of T.
+__global__ void __launch_bounds__(128) k_inv_step(const float* __restrict__ LU, int64_t n, int64_t KO, int j,
+                                                  const float* __restrict__ Dinv, float* D4, float* T) {
+    const int nt = 2 * j, q = blockIdx.x, t = threadIdx.x;
+    float* Linv = D4;
+    float* Uinv = D4 + SB * SB;
+    const int64_t J = (int64_t)NB * j;  // first row and column of block j inside the SB block
+    const float* Ljj = Dinv + (KO / NB + j) * 2 * NB * NB;  // ld NB
+    const float* Ujj = Ljj + NB * NB;
+    float acc[8][8];
+    if (q < nt) {  // L^{-1}[J.., c0..c0+64)
+        const int64_t c0 = 64 * (int64_t)q;
+        float* Tq = T + (int64_t)q * 8192;  // 128 x 64, ld 128
+        const int tr = t % 16, tc = t / 16;
+        tile_mm<128>(LU + (KO + c0) * n + KO + J, n, Linv + c0 + c0 * SB, SB, 128, 64, (int)(J - c0), acc);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int jj = 0; jj < 8; jj++) Tq[(8 * tc + jj) * 128 + 8 * tr + i] = acc[i][jj];
+        __syncthreads();
+        tile_mm<128>(Ljj, NB, Tq, 128, 128, 64, NB, acc);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int jj = 0; jj < 8; jj++) Linv[(J + 8 * tr + i) + (c0 + 8 * tc + jj) * SB] = -acc[i][jj];
+    } else if (q < 2 * nt) {  // U^{-1}[r0..r0+64, J..)
+        const int64_t r0 = 64 * (int64_t)(q - nt);
+        float* Tq = T + (int64_t)q * 8192;  // 64 x 128, ld 64
+        const int tr = t % 8, tc = t / 8;
+        tile_mm<64>(Uinv + r0 + r0 * SB, SB, LU + (KO + J) * n + KO + r0, n, 64, 128, (int)(J - r0), acc);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int jj = 0; jj < 8; jj++) Tq[(8 * tc + jj) * 64 + 8 * tr + i] = acc[i][jj];
+        __syncthreads();
+        tile_mm<64>(Tq, 64, Ujj, NB, 64, 128, NB, acc);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int jj = 0; jj < 8; jj++) Uinv[(r0 + 8 * tr + i) + (J + 8 * tc + jj) * SB] = -acc[i][jj];
+    } else if (q == 2 * nt) {  // L^{-1}[J.., J..SB): L_jj^{-1}, then zeros
+        for (int idx = t; idx < NB * (SB - (int)J); idx += 128) {
+            const int64_t c = J + idx / NB;
+            const int r = idx % NB;
+            Linv[(J + r) + c * SB] = c < J + NB ? Ljj[r + (c - J) * NB] : 0.f;
+        }
+    } else {  // U^{-1}[J..SB, J..): U_jj^{-1}, then zeros
+        const int h = SB - (int)J;
+        for (int idx = t; idx < NB * h; idx += 128) {
+            const int c = idx / h;
+            const int64_t r = J + idx % h;
+            Uinv[r + (J + c) * SB] = r < J + NB ? Ujj[(r - J) + (int64_t)c * NB] : 0.f;
+        }
+    }
+}
+
+// ---- skinny products of the block substitutions: C (m x kc) = alpha A (m x K) B (K x kc)
+// (+ C when accum), all column-major, kc small.  256 threads per 32 RH rows x KC columns: lane =
+// row, warp w takes rows 32 (w % RH) .. and the SK_CH / KG K indices (KG = 8 / RH) of group w / RH
+// in every SK_CH-long chunk of B, which is staged in shared memory column by column (coalesced,
+// conflict-free) and read back as float4 broadcasts of four consecutive K indices.  32 loads of
+// A in flight per thread, each element of A read once (coalesced along the rows) and used KC
+// times; the K groups' partial sums are added in a fixed order.  RH = 2 halves the staging of B
+// per row for tall products.
+constexpr int SK_CH = 512;
+template <int KC, int RH>
+__global__ void __launch_bounds__(256) k_skinny(const float* __restrict__ A, int64_t lda, const float* __restrict__ B,
+                                                int64_t ldb, float* __restrict__ C, int64_t ldc, int64_t m,
+                                                int64_t K, int kc, float alpha, int accum) {
+    constexpr int KG = 8 / RH, KW = SK_CH / KG, ROWS = 32 * RH;
+    extern __shared__ __align__(16) float dsm[];
+    float* Bs = dsm;  // [KC][SK_CH]
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5, rh = w % RH, kg = w / RH;
+    const int64_t r = (int64_t)blockIdx.x * ROWS + 32 * rh + lane;
+    const int c0 = blockIdx.y * KC, kb = KW * kg;
+    float acc[KC];
+#pragma unroll
+    for (int c = 0; c < KC; c++) acc[c] = 0.f;
+    for (int64_t k0 = 0; k0 < K; k0 += SK_CH) {
+        const int kch = (int)(K - k0 < SK_CH ? K - k0 : SK_CH);
+        const int kst = (kch + 31) & ~31;  // staged length: the compute reads whole groups of 32
+        __syncthreads();
+        {  // every load of this thread in flight together, then the stores
+            constexpr int PER = SK_CH * KC / 256;
+            float v[PER];
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+                const int idx = t + 256 * q, kk = idx % SK_CH, c = idx / SK_CH;
+                v[q] = (kk < kch && c0 + c < kc) ? B[(int64_t)(c0 + c) * ldb + k0 + kk] : 0.f;
+            }
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+                const int idx = t + 256 * q;
+                if (idx % SK_CH < kst) Bs[idx] = v[q];
+            }
+        }
+        __syncthreads();
+        if (r < m) {
+            for (int h = 0; h < KW && kb + h < kch; h += 32) {
+                float a[32];
+#pragma unroll
+                for (int j = 0; j < 32; j++) {
+                    const int kk = kb + h + j;
+                    a[j] = kk < kch ? A[(k0 + kk) * lda + r] : 0.f;
+                }
+#pragma unroll
+                for (int j = 0; j < 32; j += 4) {
+#pragma unroll
+                    for (int c = 0; c < KC; c++) {
+                        const float4 b = *reinterpret_cast<const float4*>(Bs + c * SK_CH + kb + h + j);
+                        acc[c] = __fmaf_rn(a[j], b.x, acc[c]);
+                        acc[c] = __fmaf_rn(a[j + 1], b.y, acc[c]);
+                        acc[c] = __fmaf_rn(a[j + 2], b.z, acc[c]);
+                        acc[c] = __fmaf_rn(a[j + 3], b.w, acc[c]);
+                    }
+                }
+            }
+        }
+    }
+    __syncthreads();
+    float* red = dsm;  // [KG][ROWS][KC + 1]
+#pragma unroll
+    for (int c = 0; c < KC; c++) red[(kg * ROWS + 32 * rh + lane) * (KC + 1) + c] = acc[c];
+    __syncthreads();
+    for (int idx = t; idx < ROWS * KC; idx += 256) {
+        const int rl = idx % ROWS, c = idx / ROWS;
+        const int64_t rr = (int64_t)blockIdx.x * ROWS + rl;
+        if (rr >= m || c0 + c >= kc) continue;
+        float s = 0.f;
+#pragma unroll
+        for (int q = 0; q < KG; q++) s += red[(q * ROWS + rl) * (KC + 1) + c];
+        float* p = C + (int64_t)(c0 + c) * ldc + rr;
+        *p = accum ? *p + alpha * s : alpha * s;
+    }
+}
+template <int KC>
+constexpr int skinny_smem() {
+    return SK_CH * KC * 4;
 }
 
 // ---- lockstep block substitutions (the batch path's refined solves) ----
@@ -599,14 +826,41 @@ void set_attrs() {
                        cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
                        cudaFuncSetAttribute(k_lu_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             DIAG_SMEM);
+                       cudaFuncSetAttribute(k_skinny<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            skinny_smem<32>());
+                       cudaFuncSetAttribute(k_skinny<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            skinny_smem<32>());
                    });
 }
 
-// GEMM arithmetic of the factorization: the rank-OB updates in the BF16x9 emulation of FP32
-// on the tensor cores; the panel-sized GEMMs (inner dimension 128) in FP32 on the CUDA cores
-// (one kernel each, where the emulation launches three)
-cublasComputeType_t lu_compute() { return CUBLAS_COMPUTE_32F_EMULATED_16BFX9; }
-cublasComputeType_t lu_compute_small() { return CUBLAS_COMPUTE_32F; }
+// C (m x kc) = alpha A (m x K) B (K x kc) (+ C when accum), column-major
+template <int KC, int RH>
+void skinny_launch(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
+                   int64_t K, int kc, float alpha, bool accum, cudaStream_t s) {
+    const dim3 g((unsigned)((m + 32 * RH - 1) / (32 * RH)), (unsigned)((kc + KC - 1) / KC));
+    k_skinny<KC, RH><<<g, 256, skinny_smem<KC>(), s>>>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum);
+}
+template <int KC>
+void skinny_rows(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
+                 int64_t K, int kc, float alpha, bool accum, cudaStream_t s) {
+    if (m >= 4096)
+        skinny_launch<KC, 2>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+    else
+        skinny_launch<KC, 1>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+}
+cudaError_t skinny(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
+                   int64_t K, int kc, float alpha, bool accum, cudaStream_t s) {
+    if (m <= 0 || kc <= 0) return cudaSuccess;
+    if (kc <= 8)
+        skinny_rows<8>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+    else if (kc <= 16)
+        skinny_rows<16>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+    else if (kc <= 24)
+        skinny_rows<24>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+    else
+        skinny_rows<32>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+    return cudaGetLastError();
+}
 
 }  // namespace
 
@@ -614,292 +868,159 @@ namespace cpg {
 
 namespace {
 
-// The blocked loops below issue ~4 launches (plus cuBLAS calls) per 128 columns;
-// replayed from a CUDA graph they run back to back on the device instead of
-// waiting on the host.  cuBLAS gets a fixed workspace so that it never allocates
-// while a stream is being captured.
-constexpr size_t kBlasWorkspace = size_t(256) << 20;
-
-cudaError_t prepare_blas(cublasHandle_t h, LuGraphs* G, cudaStream_t s) {
-    if (!G->workspace) {
-        cudaError_t e = cudaMalloc(&G->workspace, kBlasWorkspace);
-        if (e != cudaSuccess) return e;
-    }
-    if (cublasSetStream(h, s) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-    if (cublasSetWorkspace(h, G->workspace, kBlasWorkspace) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-    return cudaSuccess;
-}
-
-// L21 = A21 U_KK^{-1} for all rows below block K, as a GEMM through W (copied back).
-cudaError_t column_solve(cublasHandle_t h, float* LU, const float* Dinv, float* W, int64_t n, int64_t K,
-                         cudaStream_t s) {
-    const float one = 1.f, zero = 0.f;
-    int b = (int)std::min<int64_t>(NB, n - K);
-    const float* Ui = Dinv + (K / NB) * 2 * NB * NB + NB * NB;
-    int64_t rest = n - K - b;
-    if (rest <= 0) return cudaSuccess;
-    if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, b, b, &one, LU + K * n + K + b, CUDA_R_32F, (int)n, Ui,
-                     CUDA_R_32F, NB, &zero, W, CUDA_R_32F, (int)rest, lu_compute_small(), CUBLAS_GEMM_DEFAULT) !=
-        CUBLAS_STATUS_SUCCESS)
-        return cudaErrorUnknown;
-    return cudaMemcpy2DAsync(LU + K * n + K + b, n * sizeof(float), W, rest * sizeof(float), rest * sizeof(float), b,
-                             cudaMemcpyDeviceToDevice, s);
-}
-
-// U(K..K+b, c0..c0+nc) = L_KK^{-1} A(K..K+b, c0..c0+nc), as a GEMM through W (copied back).
-cudaError_t row_solve(cublasHandle_t h, float* LU, const float* Dinv, float* W, int64_t n, int64_t K, int64_t c0,
-                      int64_t nc, cudaStream_t s) {
-    if (nc <= 0) return cudaSuccess;
-    const float one = 1.f, zero = 0.f;
-    int b = (int)std::min<int64_t>(NB, n - K);
-    const float* Li = Dinv + (K / NB) * 2 * NB * NB;
-    if (cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, b, (int)nc, b, &one, Li, CUDA_R_32F, NB, LU + c0 * n + K,
-                     CUDA_R_32F, (int)n, &zero, W, CUDA_R_32F, b, lu_compute_small(), CUBLAS_GEMM_DEFAULT) !=
-        CUBLAS_STATUS_SUCCESS)
-        return cudaErrorUnknown;
-    return cudaMemcpy2DAsync(LU + c0 * n + K, n * sizeof(float), W, b * sizeof(float), b * sizeof(float), nc,
-                             cudaMemcpyDeviceToDevice, s);
-}
-
-// A22 block [r0, r0+m) x [c0, c0+nc) -= L(r0.., K..K+b) U(K..K+b, c0..)
-cudaError_t trailing(cublasHandle_t h, float* LU, int64_t n, int64_t K, int b, int64_t r0, int64_t m, int64_t c0,
-                     int64_t nc) {
-    if (m <= 0 || nc <= 0) return cudaSuccess;
-    const float one = 1.f, mone = -1.f;
-    cublasStatus_t st = cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)m, (int)nc, b, &mone, LU + K * n + r0,
-                                     CUDA_R_32F, (int)n, LU + c0 * n + K, CUDA_R_32F, (int)n, &one, LU + c0 * n + r0,
-                                     CUDA_R_32F, (int)n, b <= NB ? lu_compute_small() : lu_compute(),
-                                     CUBLAS_GEMM_DEFAULT);
-    return st == CUBLAS_STATUS_SUCCESS ? cudaSuccess : cudaErrorUnknown;
-}
-
-// Two-level right-looking blocked LU.  Inner blocks of NB columns are factored within an
-// outer panel of OB columns: per inner block the diagonal kernel, L21 for all rows
-// below, U12 and the trailing update only inside the outer panel (an (n - K) x < OB
-// update that stays in L2).  After the panel, its U rows right of it come from a
-// blocked forward substitution and the rest of the matrix from one rank-OB update, so the
-// large trailing matrix is read and written once per OB columns instead of once per NB.
-// Look-ahead: the rank-OB update is split into the next panel's columns and the rest;
-// the next panel is factored on a high-priority stream while the rest of the update
-// runs.  (Measured: about 1 ms of 56 on the 19k wing.  cuBLAS's large GEMM holds every
-// SM until it ends, and keeping 8-32 SMs out of it for the panel measured 0.6-5 ms
-// slower.)
-// outer panel width: OB_BLOCKS inner blocks.  The lockstep factorization of many matrices
-// uses OB_BLOCKS_BATCHED: its rank-128 panel updates run in FP32 on the CUDA cores and its
-// rank-OB updates on the tensor cores, and on the 64-wing batch 512 columns measured 220 ms
-// against 269 ms for 1,024 (256: 224 ms; 2,048: 379 ms).
-constexpr int OB_BLOCKS = 8;
-constexpr int OB_BLOCKS_BATCHED = 4;
-// SMs the rank-OB update of the columns past the next panel leaves to that panel's
-// factorization on its own stream (19k wing: LU 38.6 ms with 0, 37.5 with 8, 37.4 with 16,
-// 36.8 with 32)
+// Right-looking blocked LU by outer panels of SB = 1,024 columns.  Per panel [KO, KE):
+//   1. its diagonal block is factored in place by 128-column steps restricted to the block
+//      (k_lu_diag, then one launch of the column and row solves and one of the update inside
+//      the block); after each step's k_lu_diag a third stream extends L11^{-1} and U11^{-1} of
+//      the whole block by that step (k_inv_step), so the inverses are ready one step after
+//      the factors;
+//   2. L21 = A21 U11^{-1} and U12 = L11^{-1} A12 on the tensor cores (no pivoting, so the
+//      panel's off-diagonal factors are these products);
+//   3. A22 -= L21 U12 on the tensor cores.
+// Look-ahead: the rows of L21 and the columns of U12 that meet the next diagonal block come
+// first (1,024-wide products), then that block's update; it is factored on a high-priority
+// stream while the rest of L21, U12 and the update run with kPanelSms SMs left to it.  The
+// serial chain is the diagonal blocks and these three small products.
 constexpr int kPanelSms = 32;
-int64_t outer_width(int blocks = OB_BLOCKS) { return (int64_t)NB * blocks; }
+constexpr int64_t kInvScratch = 4 * (SB / 64) * 8192;  // tile scratch of k_inv_step (28 tiles at most)
 
-struct Streams {  // where the next cuBLAS calls go
-    cublasHandle_t h;
-    cudaStream_t main, panel;
-    void *ws_main, *ws_panel;
-    cudaError_t use(bool on_panel) const {
-        if (cublasSetStream(h, on_panel ? panel : main) != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
-        if (cublasSetWorkspace(h, on_panel ? ws_panel : ws_main, kBlasWorkspace) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        return cudaSuccess;
-    }
-};
-
-// factorization of the outer panel [KO, KE) (on st.panel)
-cudaError_t factor_panel(const Streams& st, float* LU, float* Dinv, float* W, int64_t n, int* bad, int64_t KO,
-                         int64_t KE) {
+// factorization of the diagonal block [KO, KE) x [KO, KE) in place on s (the updates of the
+// earlier panels applied), the inverses of its 128-column blocks into G->dinv; for a full SB
+// block also its combined inverses into G->dinv4 on G->inv_stream, joined back into s at the end
+cudaError_t factor_diag_block(LuGraphs* G, float* LU, int64_t n, int* bad, int64_t KO, int64_t KE, cudaStream_t s) {
     cudaError_t e;
-    if ((e = st.use(true)) != cudaSuccess) return e;
+    const bool inv = KE - KO == SB;
+    float* D4 = inv ? G->dinv4 + (KO / SB) * 2 * SB * SB : nullptr;
     for (int64_t K = KO; K < KE; K += NB) {
-        const int b = (int)std::min<int64_t>(NB, n - K);
-        k_lu_diag<<<1, DT, DIAG_SMEM, st.panel>>>(LU, n, K, b, Dinv, bad);
-        if ((e = column_solve(st.h, LU, Dinv, W, n, K, st.panel)) != cudaSuccess) return e;
-        const int64_t K1 = K + b;
-        if ((e = row_solve(st.h, LU, Dinv, W, n, K, K1, KE - K1, st.panel)) != cudaSuccess) return e;
-        if ((e = trailing(st.h, LU, n, K, b, K1, n - K1, K1, KE - K1)) != cudaSuccess) return e;
-    }
-    return cudaGetLastError();
-}
-
-cudaError_t factor_body(const Streams& st, LuGraphs* G, float* LU, float* Dinv, float* W, int64_t n, int* bad) {
-    cudaError_t e;
-    const int64_t OB = outer_width();
-    // first panel
-    if ((e = cudaEventRecord(G->ev_update, st.main)) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(st.panel, G->ev_update, 0)) != cudaSuccess) return e;
-    if ((e = factor_panel(st, LU, Dinv, W, n, bad, 0, std::min<int64_t>(OB, n))) != cudaSuccess) return e;
-    for (int64_t KO = 0; KO < n; KO += OB) {
-        const int64_t KE = std::min<int64_t>(KO + OB, n);
-        // this panel done (the main stream has finished the rest of the previous update)
-        if ((e = cudaEventRecord(G->ev_panel, st.panel)) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(st.main, G->ev_panel, 0)) != cudaSuccess) return e;
-        if (KE >= n) break;
-        if ((e = st.use(false)) != cudaSuccess) return e;
-        for (int64_t K = KO; K < KE; K += NB) {  // U(KO..KE, KE..n): forward substitution by blocks
-            const int b = (int)std::min<int64_t>(NB, n - K);
-            if ((e = row_solve(st.h, LU, Dinv, W, n, K, KE, n - KE, st.main)) != cudaSuccess) return e;
-            if ((e = trailing(st.h, LU, n, K, b, K + b, KE - K - b, KE, n - KE)) != cudaSuccess) return e;
+        const int b = (int)std::min<int64_t>(NB, KE - K);
+        k_lu_diag<<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, G->dinv, bad);
+        if (inv) {
+            const int j = (int)((K - KO) / NB);
+            if ((e = cudaEventRecord(G->ev_diag, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(G->inv_stream, G->ev_diag, 0)) != cudaSuccess) return e;
+            k_inv_step<<<4 * j + 2, 128, 0, G->inv_stream>>>(LU, n, KO, j, G->dinv, D4, G->super_tmp);
         }
-        const int64_t KE2 = std::min<int64_t>(KE + OB, n);
-        // rank-OB update A22 -= L21 U12 on the tensor cores: both operands split once, then the
-        // next panel's columns, then the next panel on its stream beside the update of the
-        // remaining columns
-        TcOperand tA, tB;
-        const int64_t rows = n - KE;
-        tc_operand_bind(tA, G->tc_mem, rows, OB);
-        tc_operand_bind(tB, (char*)G->tc_mem + tc_operand_bytes(rows, OB), rows, OB);
-        if ((e = tc_split(LU + KO * n + KE, 1, n, rows, KE - KO, tA, bad, st.main)) != cudaSuccess) return e;
-        if ((e = tc_split(LU + KE * n + KO, n, 1, rows, KE - KO, tB, bad, st.main)) != cudaSuccess) return e;
-        const int sms = tc_num_sms();
-        if ((e = tc_gemm(tA, rows, tB, KE2 - KE, -1.f, 1.f, LU + KE * n + KE, n, sms, bad, st.main)) != cudaSuccess)
-            return e;
-        if ((e = cudaEventRecord(G->ev_update, st.main)) != cudaSuccess) return e;
-        if ((e = tc_gemm(tA, rows, tc_rows(tB, KE2 - KE), n - KE2, -1.f, 1.f, LU + KE2 * n + KE, n,
-                         sms - kPanelSms, bad, st.main)) != cudaSuccess)
-            return e;
-        if ((e = cudaStreamWaitEvent(st.panel, G->ev_update, 0)) != cudaSuccess) return e;
-        if ((e = factor_panel(st, LU, Dinv, W, n, bad, KE, KE2)) != cudaSuccess) return e;
+        const int64_t K1 = K + b, rest = KE - K1;
+        if (rest <= 0) break;
+        const unsigned g = (unsigned)((rest + CS_R - 1) / CS_R + (rest + RS_C - 1) / RS_C);
+        k_colrow_solve<<<g, 256, CR_SMEM, s>>>(LU, n, G->dinv, K1, KE, K1, KE, K, b);
+        dim3 gg((unsigned)((rest + GS_R - 1) / GS_R), (unsigned)((rest + GS_C - 1) / GS_C));
+        k_gemm_sub<<<gg, 128, 0, s>>>(LU, n, K1, KE, K1, KE, K, b);
     }
-    if ((e = st.use(false)) != cudaSuccess) return e;
+    if (inv) {
+        if ((e = cudaEventRecord(G->ev_inv, G->inv_stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(s, G->ev_inv, 0)) != cudaSuccess) return e;
+    }
     return cudaGetLastError();
 }
 
-// Blocked forward and backward substitution with the diagonal-block inverses, two
-// GEMMs per block and direction and no copies: forward, Y_K = inv(L_KK) X_K and
+// bytes of the split operands: two of n rows (panel columns and rows), two of SB rows for the
+// products that meet the next diagonal block and two for the diagonal block's inverses, each SB
+// halves long
+size_t tc_bytes_for(int64_t n) { return 2 * tc_operand_bytes(n, SB) + 4 * tc_operand_bytes(SB, SB); }
+
+cudaError_t factor_body(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t main, cudaStream_t panel) {
+    cudaError_t e;
+    // A21 / L21 rows, A12 / U12 columns (all of them, and the SB that meet the next diagonal
+    // block), L11^{-1} rows, U11^{-1} columns
+    TcOperand rowsA, colsB, nearA, nearB, invA, invB;
+    char* mem = (char*)G->tc_mem;
+    for (TcOperand* op : {&rowsA, &colsB}) {
+        tc_operand_bind(*op, mem, n, SB);
+        mem += tc_operand_bytes(n, SB);
+    }
+    for (TcOperand* op : {&nearA, &nearB, &invA, &invB}) {
+        tc_operand_bind(*op, mem, SB, SB);
+        mem += tc_operand_bytes(SB, SB);
+    }
+    const int sms = tc_num_sms();
+    // first diagonal block
+    if ((e = cudaEventRecord(G->ev_update, main)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(panel, G->ev_update, 0)) != cudaSuccess) return e;
+    if ((e = factor_diag_block(G, LU, n, bad, 0, std::min<int64_t>(SB, n), panel)) != cudaSuccess) return e;
+    for (int64_t KO = 0; KO < n; KO += SB) {
+        const int64_t KE = std::min<int64_t>(KO + SB, n);
+        // this diagonal block factored and inverted (the main stream has finished the rest of
+        // the previous update)
+        if ((e = cudaEventRecord(G->ev_panel, panel)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(main, G->ev_panel, 0)) != cudaSuccess) return e;
+        if (KE >= n) break;  // a panel that ends short of n is the last one, so KE - KO == SB below
+        const int64_t rows = n - KE, KE2 = std::min<int64_t>(KE + SB, n), w2 = KE2 - KE, far = rows - w2;
+        const float* Li = G->dinv4 + (KO / SB) * 2 * SB * SB;
+        const float* Ui = Li + SB * SB;
+        float* A21 = LU + KO * n + KE;  // rows KE.., columns KO..KE (ld n)
+        float* A12 = LU + KE * n + KO;  // rows KO..KE, columns KE.. (ld n)
+        float* A22 = LU + KE * n + KE;
+        // operand rows: A21's rows (K along its columns), U11^{-1}'s columns, L11^{-1}'s rows, A12's
+        // columns
+        if ((e = tc_split(Ui, SB, 1, SB, SB, invB, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(Li, 1, SB, SB, SB, invA, bad, main)) != cudaSuccess) return e;
+        // the next diagonal block: L21 rows KE..KE2, U12 columns KE..KE2, then its update
+        if ((e = tc_split(A21, 1, n, w2, SB, nearA, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_gemm(nearA, w2, invB, SB, 1.f, 0.f, A21, n, sms, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(A12, n, 1, w2, SB, nearB, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_gemm(invA, SB, nearB, w2, 1.f, 0.f, A12, n, sms, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(A21, 1, n, w2, SB, nearA, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(A12, n, 1, w2, SB, nearB, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_gemm(nearA, w2, nearB, w2, -1.f, 1.f, A22, n, sms, bad, main)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(G->ev_update, main)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(panel, G->ev_update, 0)) != cudaSuccess) return e;
+        if ((e = factor_diag_block(G, LU, n, bad, KE, KE2, panel)) != cudaSuccess) return e;
+        if (far <= 0) continue;
+        // beside it: the rest of L21 and U12, then every other part of the update
+        const int rest_sms = sms - kPanelSms;
+        if ((e = tc_split(A21 + w2, 1, n, far, SB, rowsA, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_gemm(rowsA, far, invB, SB, 1.f, 0.f, A21 + w2, n, rest_sms, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(A12 + w2 * n, n, 1, far, SB, colsB, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_gemm(invA, SB, colsB, far, 1.f, 0.f, A12 + w2 * n, n, rest_sms, bad, main)) != cudaSuccess)
+            return e;
+        if ((e = tc_split(A21, 1, n, rows, SB, rowsA, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(A12, n, 1, rows, SB, colsB, bad, main)) != cudaSuccess) return e;
+        // below the next diagonal block in its columns, then every column right of it
+        if ((e = tc_gemm(tc_rows(rowsA, w2), far, colsB, w2, -1.f, 1.f, A22 + w2, n, rest_sms, bad, main)) !=
+            cudaSuccess)
+            return e;
+        if ((e = tc_gemm(rowsA, rows, tc_rows(colsB, w2), far, -1.f, 1.f, A22 + w2 * n, n, rest_sms, bad, main)) !=
+            cudaSuccess)
+            return e;
+    }
+    return cudaGetLastError();
+}
+
+// Blocked forward and backward substitution with the diagonal-block inverses, two skinny
+// products per block and direction and no copies: forward, Y_K = inv(L_KK) X_K and
 // X_below -= L_below,K Y_K; backward, X_K = inv(U_KK) Y_K and Y_above -= U_above,K X_K.
 // X (n x k, ld n) ends with the solution; Y is an n x k scratch array.  The first nsup
 // SB-column blocks use their combined inverses (Dinv4), so a pass takes an eighth of the
 // dependent steps there; the rest of the matrix goes by 128-column blocks.
-cudaError_t solve_body(cublasHandle_t h, const float* LU, const float* Dinv, const float* Dinv4, int64_t nsup,
-                       int64_t n, float* X, float* Y, int k) {
-    const float one = 1.f, mone = -1.f, zero = 0.f;
+cudaError_t solve_body(const float* LU, const float* Dinv, const float* Dinv4, int64_t nsup, int64_t n, float* X,
+                       float* Y, int k, cudaStream_t s) {
+    cudaError_t e;
     const int64_t nblk = (n + NB - 1) / NB, blk0 = nsup * (SB / NB);
-    for (int64_t sb = 0; sb < nsup; sb++) {
-        const int64_t K = sb * SB;
-        const float* Li = Dinv4 + sb * 2 * SB * SB;
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, SB, k, SB, &one, Li, SB, X + K, (int)n, &zero, Y + K, (int)n) !=
-            CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        const int64_t rest = n - K - SB;
-        if (rest > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, SB, &mone, LU + K * n + K + SB, (int)n,
-                                    Y + K, (int)n, &one, X + K + SB, (int)n) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-    }
+    auto fwd = [&](int64_t K, int64_t b, const float* Li, int64_t ldi) -> cudaError_t {
+        cudaError_t ee = skinny(Li, ldi, X + K, n, Y + K, n, b, b, k, 1.f, false, s);
+        if (ee != cudaSuccess) return ee;
+        return skinny(LU + K * n + K + b, n, Y + K, n, X + K + b, n, n - K - b, b, k, -1.f, true, s);
+    };
+    auto bwd = [&](int64_t K, int64_t b, const float* Ui, int64_t ldi) -> cudaError_t {
+        cudaError_t ee = skinny(Ui, ldi, Y + K, n, X + K, n, b, b, k, 1.f, false, s);
+        if (ee != cudaSuccess) return ee;
+        return skinny(LU + K * n, n, X + K, n, Y, n, K, b, k, -1.f, true, s);
+    };
+    for (int64_t sb = 0; sb < nsup; sb++)
+        if ((e = fwd(sb * SB, SB, Dinv4 + sb * 2 * SB * SB, SB)) != cudaSuccess) return e;
     for (int64_t blk = blk0; blk < nblk; blk++) {
-        int64_t K = blk * NB;
-        int b = (int)std::min<int64_t>(NB, n - K);
-        const float* Li = Dinv + blk * 2 * NB * NB;
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, k, b, &one, Li, NB, X + K, (int)n, &zero, Y + K, (int)n) !=
-            CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        int64_t rest = n - K - b;
-        if (rest > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)rest, k, b, &mone, LU + K * n + K + b, (int)n,
-                                    Y + K, (int)n, &one, X + K + b, (int)n) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
+        const int64_t K = blk * NB;
+        if ((e = fwd(K, std::min<int64_t>(NB, n - K), Dinv + blk * 2 * NB * NB, NB)) != cudaSuccess) return e;
     }
     for (int64_t blk = nblk - 1; blk >= blk0; blk--) {
-        int64_t K = blk * NB;
-        int b = (int)std::min<int64_t>(NB, n - K);
-        const float* Ui = Dinv + blk * 2 * NB * NB + NB * NB;
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, b, k, b, &one, Ui, NB, Y + K, (int)n, &zero, X + K, (int)n) !=
-            CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        if (K > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, b, &mone, LU + K * n, (int)n, X + K, (int)n,
-                                 &one, Y, (int)n) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
+        const int64_t K = blk * NB;
+        if ((e = bwd(K, std::min<int64_t>(NB, n - K), Dinv + blk * 2 * NB * NB + NB * NB, NB)) != cudaSuccess)
+            return e;
     }
-    for (int64_t sb = nsup - 1; sb >= 0; sb--) {
-        const int64_t K = sb * SB;
-        const float* Ui = Dinv4 + sb * 2 * SB * SB + SB * SB;
-        if (cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, SB, k, SB, &one, Ui, SB, Y + K, (int)n, &zero, X + K, (int)n) !=
-            CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-        if (K > 0 && cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)K, k, SB, &mone, LU + K * n, (int)n, X + K, (int)n,
-                                 &one, Y, (int)n) != CUBLAS_STATUS_SUCCESS)
-            return cudaErrorUnknown;
-    }
+    for (int64_t sb = nsup - 1; sb >= 0; sb--)
+        if ((e = bwd(sb * SB, SB, Dinv4 + sb * 2 * SB * SB + SB * SB, SB)) != cudaSuccess) return e;
     return cudaGetLastError();
-}
-
-// Inverses of the full SB-column diagonal blocks from the 128-column ones inside each, by
-// block-triangular doublings (128 -> 256 -> 512 -> 1024):
-//   [[A, 0], [C, B]]^{-1} = [[A^{-1}, 0], [-B^{-1} C A^{-1}, B^{-1}]]   (L, unit lower)
-//   [[A, C], [0, B]]^{-1} = [[A^{-1}, -A^{-1} C B^{-1}], [0, B^{-1}]]   (U)
-// Every step is one strided-batched FP32 GEMM over all the 512-column blocks (their
-// diagonal blocks of LU, their inverses and their scratch all lie at fixed strides).
-// Layout: Dinv4 + s * 2 * SB^2 holds L^{-1} then U^{-1} of block s, column-major, ld SB.
-__global__ void k_super_init(const float* __restrict__ Dinv, float* __restrict__ Dinv4, int64_t nsup) {
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nsup * 2 * SB * SB) return;
-    const int64_t s = t / (2 * SB * SB);
-    const int64_t w = t % (2 * SB * SB);
-    const int u = (int)(w / (SB * SB));  // 0: L, 1: U
-    const int64_t e = w % (SB * SB);
-    const int r = (int)(e % SB), c = (int)(e / SB);
-    float v = 0.f;
-    if (r / NB == c / NB) {
-        const int64_t blk = s * (SB / NB) + r / NB;
-        v = Dinv[blk * 2 * NB * NB + u * NB * NB + (r % NB) + (int64_t)(c % NB) * NB];
-    }
-    Dinv4[t] = v;
-}
-
-cudaError_t build_super_inverses(cublasHandle_t h, LuGraphs* G, const float* LU, int64_t n, cudaStream_t s) {
-    const int64_t nsup = n / SB;
-    G->super_n = 0;
-    if (nsup == 0) return cudaSuccess;
-    cudaError_t e;
-    if (!G->dinv4 || G->super_cap != nsup) {  // same buffers for every factorization of this size,
-        if (G->solve) cudaGraphExecDestroy(G->solve);  // so a captured substitution stays valid
-        G->solve = nullptr;
-        if (G->dinv4) cudaFree(G->dinv4);
-        if (G->super_tmp) cudaFree(G->super_tmp);
-        G->dinv4 = G->super_tmp = nullptr;
-        G->super_cap = 0;
-        if ((e = cudaMalloc(&G->dinv4, sizeof(float) * nsup * 2 * SB * SB)) != cudaSuccess) return e;
-        if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * nsup * (SB / 2) * (SB / 2))) != cudaSuccess) return e;
-        G->super_cap = nsup;
-    }
-    const int64_t tot = nsup * 2 * SB * SB;
-    k_super_init<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(G->dinv, G->dinv4, nsup);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    const float one = 1.f, mone = -1.f, zero = 0.f;
-    const int ni = (int)n, bc = (int)nsup;
-    const long long sLU = (long long)SB * (n + 1), sD = 2LL * SB * SB, sT = (long long)(SB / 2) * (SB / 2);
-    float* T = G->super_tmp;
-    auto gemm = [&](int m, int nn, int kk, float alpha, const float* A, int lda, long long sA, const float* B, int ldb,
-                    long long sB, float* C, int ldc) -> cudaError_t {
-        return cublasSgemmStridedBatched(h, CUBLAS_OP_N, CUBLAS_OP_N, m, nn, kk, &alpha, A, lda, sA, B, ldb, sB, &zero,
-                                         C, ldc, C == T ? sT : sD, bc) == CUBLAS_STATUS_SUCCESS
-                   ? cudaSuccess
-                   : cudaErrorUnknown;
-    };
-    for (int w = NB; w < SB; w *= 2) {  // size of the two blocks combined at this level
-        for (int p = 0; p < SB / (2 * w); p++) {
-            const int o = 2 * w * p;  // offset of the pair inside the 512-column block
-            float* Linv = G->dinv4;
-            float* Uinv = G->dinv4 + SB * SB;
-            // L: T = C A^{-1}, then -B^{-1} T into the lower-left block
-            if ((e = gemm(w, w, w, one, LU + (o + w) + (int64_t)o * n, ni, sLU, Linv + o + (int64_t)o * SB, SB, sD, T,
-                          w)) != cudaSuccess)
-                return e;
-            if ((e = gemm(w, w, w, mone, Linv + (o + w) + (int64_t)(o + w) * SB, SB, sD, T, w, sT,
-                          Linv + (o + w) + (int64_t)o * SB, SB)) != cudaSuccess)
-                return e;
-            // U: T = C B^{-1}, then -A^{-1} T into the upper-right block
-            if ((e = gemm(w, w, w, one, LU + o + (int64_t)(o + w) * n, ni, sLU, Uinv + (o + w) + (int64_t)(o + w) * SB,
-                          SB, sD, T, w)) != cudaSuccess)
-                return e;
-            if ((e = gemm(w, w, w, mone, Uinv + o + (int64_t)o * SB, SB, sD, T, w, sT, Uinv + o + (int64_t)(o + w) * SB,
-                          SB)) != cudaSuccess)
-                return e;
-        }
-    }
-    G->super_n = n;
-    return cudaSuccess;
 }
 
 // Capture body() on s into a graph (no profiler events inside the capture).
@@ -930,18 +1051,13 @@ cudaError_t capture(cudaStream_t s, cudaGraphExec_t* out, F body, unsigned long 
 
 void LuGraphs::release() {
     if (solve) cudaGraphExecDestroy(solve);
-    if (workspace && !shared_ws) cudaFree(workspace);
-    if (workspace2 && !shared_ws) cudaFree(workspace2);
-    workspace = nullptr;
-    shared_ws = false;
     if (panel_stream) cudaStreamDestroy(panel_stream);
-    if (ev_update) cudaEventDestroy(ev_update);
-    if (ev_panel) cudaEventDestroy(ev_panel);
-    workspace2 = nullptr;
-    panel_stream = nullptr;
-    ev_update = ev_panel = nullptr;
+    if (inv_stream) cudaStreamDestroy(inv_stream);
+    for (cudaEvent_t ev : {ev_update, ev_panel, ev_diag, ev_inv})
+        if (ev) cudaEventDestroy(ev);
+    panel_stream = inv_stream = nullptr;
+    ev_update = ev_panel = ev_diag = ev_inv = nullptr;
     if (dinv) cudaFree(dinv);
-    if (panel) cudaFree(panel);
     if (tmp) cudaFree(tmp);
     if (dinv4) cudaFree(dinv4);
     if (super_tmp) cudaFree(super_tmp);
@@ -951,34 +1067,45 @@ void LuGraphs::release() {
     dinv4 = super_tmp = nullptr;
     super_n = super_cap = 0;
     solve = nullptr;
-    workspace = nullptr;
-    dinv = panel = tmp = nullptr;
+    dinv = tmp = nullptr;
     tmp_floats = 0;
     solve_X = nullptr;
     solve_k = 0;
     factor_n = 0;
 }
 
-// Launched directly (not from a graph): a geometry is factored once, and its ~3,000
-// launches are each longer than their host-side cost, so a captured graph would only
-// add the capture and instantiation to every new geometry.
-cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s) {
+size_t lu_factor_bytes(int64_t n) {
+    const size_t nb = (size_t)((n + NB - 1) / NB), nsup = (size_t)(n / SB);
+    return sizeof(float) * (nb * 2 * NB * NB + nsup * 2 * SB * SB + (size_t)kInvScratch) + tc_bytes_for(n) +
+           4 * 256;
+}
+
+// Launched directly (not from a graph): a geometry is factored once, and its launches are
+// each longer than their host-side cost, so a captured graph would only add the capture and
+// instantiation to every new geometry.
+cudaError_t lu_factor_fp32(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s) {
     set_attrs();
-    cublasHandle_t h = (cublasHandle_t)blas;
-    cudaError_t e = prepare_blas(h, G, s);
-    if (e != cudaSuccess) return e;
-    if (G->factor_n != n || !G->dinv) {
-        if (G->solve) cudaGraphExecDestroy(G->solve);  // it holds the old Dinv
+    cudaError_t e;
+    const int64_t nsup = n / SB;
+    if (G->factor_n != n || !G->dinv || G->super_cap != nsup) {
+        if (G->solve) cudaGraphExecDestroy(G->solve);  // it holds the old inverses
         G->solve = nullptr;
         if (G->dinv) cudaFree(G->dinv);
-        if (G->panel) cudaFree(G->panel);
-        G->dinv = G->panel = nullptr;
-        size_t nb = (size_t)((n + NB - 1) / NB);
+        if (G->dinv4) cudaFree(G->dinv4);
+        if (G->super_tmp) cudaFree(G->super_tmp);
+        G->dinv = G->dinv4 = G->super_tmp = nullptr;
+        G->super_cap = 0;
+        G->factor_n = 0;
+        const size_t nb = (size_t)((n + NB - 1) / NB);
         if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
-        if ((e = cudaMalloc(&G->panel, sizeof(float) * (size_t)n * NB)) != cudaSuccess) return e;
+        if (nsup > 0) {
+            if ((e = cudaMalloc(&G->dinv4, sizeof(float) * nsup * 2 * SB * SB)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * kInvScratch)) != cudaSuccess) return e;
+        }
+        G->super_cap = nsup;
         G->factor_n = n;
     }
-    const size_t tcb = 2 * tc_operand_bytes(n, outer_width());
+    const size_t tcb = tc_bytes_for(n);
     if (G->tc_bytes < tcb) {
         if (G->tc_mem) cudaFree(G->tc_mem);
         G->tc_mem = nullptr;
@@ -991,32 +1118,34 @@ cudaError_t lu_factor_fp32(void* blas, LuGraphs* G, float* LU, int64_t n, int* b
         cudaDeviceGetStreamPriorityRange(&least, &greatest);
         if ((e = cudaStreamCreateWithPriority(&G->panel_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
             return e;
-        if ((e = cudaEventCreateWithFlags(&G->ev_update, cudaEventDisableTiming)) != cudaSuccess) return e;
-        if ((e = cudaEventCreateWithFlags(&G->ev_panel, cudaEventDisableTiming)) != cudaSuccess) return e;
-        if (!G->workspace2 && (e = cudaMalloc(&G->workspace2, kBlasWorkspace)) != cudaSuccess) return e;
+        if ((e = cudaStreamCreateWithPriority(&G->inv_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
+            return e;
+        for (cudaEvent_t* ev : {&G->ev_update, &G->ev_panel, &G->ev_diag, &G->ev_inv})
+            if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return e;
     }
-    const Streams st{h, s, G->panel_stream, G->workspace, G->workspace2};
     ProfScope ps(Prof::LU_FACTOR, s);
-    if ((e = factor_body(st, G, LU, G->dinv, G->panel, n, bad)) != cudaSuccess) return e;
-    return build_super_inverses(h, G, LU, n, s);
+    if ((e = factor_body(G, LU, n, bad, s, G->panel_stream)) != cudaSuccess) return e;
+    G->super_n = nsup > 0 ? n : 0;
+    return cudaSuccess;
 }
 
-// Lockstep factorization of m matrices: the same two-level blocked LU as factor_body
-// (inner blocks of NB columns inside outer panels of outer_width() columns), with each
-// step taken for every matrix at once.  Block step K is one launch of the diagonal
-// kernel with one thread block per matrix that still has a block at K, then one launch
-// each of the column solve, the in-panel row solve and the in-panel update over all
-// matrices; after an outer panel, the U rows right of it by blocked forward substitution
-// (two launches per inner block), then the rank-OB update of each matrix through cuBLAS
-// (BF16x9).  The work items of every launch are planned on the host and uploaded once.
+// Lockstep factorization of m matrices: blocked right-looking LU by outer panels of
+// outer_width() columns, each step taken for every matrix at once.  Block step K is one
+// launch of the diagonal kernel with one thread block per matrix that still has a block at K,
+// then one launch each of the column solve, the in-panel row solve and the in-panel update
+// over all matrices; after an outer panel, the U rows right of it by blocked forward
+// substitution (two launches per inner block), then the rank-OB update of each matrix on the
+// tensor cores.  The work items of every launch are planned on the host and uploaded once.
 // No look-ahead stream: the diagonal blocks of all matrices run side by side instead.
-cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs, const int64_t* ns,
-                              int* const* bads, int m, cudaStream_t s) {
+// Outer panel width 512 columns: its rank-128 panel updates run in FP32 on the CUDA cores and
+// its rank-512 updates on the tensor cores; on the 64-wing batch 512 columns measured 220 ms
+// against 269 ms for 1,024 (256: 224 ms; 2,048: 379 ms).
+constexpr int64_t OB_BATCHED = 4 * NB;
+cudaError_t lu_factor_batched(LuGraphs* const* Gs, float* const* LUs, const int64_t* ns, int* const* bads, int m,
+                              cudaStream_t s) {
     if (m <= 0) return cudaSuccess;
     set_attrs();
-    cublasHandle_t h = (cublasHandle_t)blas;
-    cudaError_t e = prepare_blas(h, Gs[0], s);
-    if (e != cudaSuccess) return e;
+    cudaError_t e;
     std::vector<LuBatchMesh> desc(m);
     int64_t nmax = 0;
     for (int q = 0; q < m; q++) {
@@ -1026,8 +1155,6 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
         if (G->solve) cudaGraphExecDestroy(G->solve);
         G->solve = nullptr;
         if (G->factor_n != n || !G->dinv) {
-            if (G->solve) cudaGraphExecDestroy(G->solve);  // it holds the old Dinv
-            G->solve = nullptr;
             if (G->dinv) cudaFree(G->dinv);
             G->dinv = nullptr;
             const size_t nb = (size_t)((n + NB - 1) / NB);
@@ -1057,7 +1184,7 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
         const int64_t now = (int64_t)items.size() / LB_ITEM;
         if (now > mark) plan.push_back(Step{kind, mark, now - mark, -1, 0, 0});
     };
-    const int64_t OB = outer_width(OB_BLOCKS_BATCHED);
+    const int64_t OB = OB_BATCHED;
     for (int64_t KO = 0; KO < nmax; KO += OB) {
         for (int64_t K = KO; K < KO + OB && K < nmax; K += NB) {
             open();
@@ -1114,11 +1241,24 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
     // ---- upload and issue
     LuBatchMesh* ddesc = nullptr;
     int* ditems = nullptr;
+    void* tcm = nullptr;
+    const size_t opb = tc_operand_bytes(nmax, OB);
     if ((e = cudaMallocAsync((void**)&ddesc, sizeof(LuBatchMesh) * m, s)) != cudaSuccess) return e;
-    if ((e = cudaMallocAsync((void**)&ditems, sizeof(int) * std::max<size_t>(1, items.size()), s)) != cudaSuccess) {
-        cudaFreeAsync(ddesc, s);
+    struct Free {
+        void** p[3];
+        cudaStream_t s;
+        ~Free() {
+            for (void** q : p)
+                if (*q) cudaFreeAsync(*q, s);
+        }
+    } fr{{(void**)&ddesc, (void**)&ditems, &tcm}, s};
+    if ((e = cudaMallocAsync((void**)&ditems, sizeof(int) * std::max<size_t>(1, items.size()), s)) != cudaSuccess)
         return e;
-    }
+    if ((e = cudaMallocAsync(&tcm, 2 * opb, s)) != cudaSuccess) return e;
+    TcOperand tA, tB;  // one pair for every matrix: the rank updates follow each other on s
+    tc_operand_bind(tA, tcm, nmax, OB);
+    tc_operand_bind(tB, (char*)tcm + opb, nmax, OB);
+    const int sms = tc_num_sms();
     e = cudaMemcpyAsync(ddesc, desc.data(), sizeof(LuBatchMesh) * m, cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess && !items.empty())
         e = cudaMemcpyAsync(ditems, items.data(), sizeof(int) * items.size(), cudaMemcpyHostToDevice, s);
@@ -1130,19 +1270,21 @@ cudaError_t lu_factor_batched(void* blas, LuGraphs* const* Gs, float* const* LUs
             const unsigned g = (unsigned)st.cnt;
             switch (st.kind) {
                 case DIAG: k_lu_diag_batched<<<g, DT, DIAG_SMEM, s>>>(ddesc, it); break;
-                case COLS: k_col_solve_batched<<<g, 256, 0, s>>>(ddesc, it); break;
-                case ROWS: k_row_solve_batched<<<g, 256, 0, s>>>(ddesc, it); break;
+                case COLS: k_col_solve_batched<<<g, 256, CS_SMEM, s>>>(ddesc, it); break;
+                case ROWS: k_row_solve_batched<<<g, 256, RS_SMEM, s>>>(ddesc, it); break;
                 case GEMM: k_gemm_sub_batched<<<g, 128, 0, s>>>(ddesc, it); break;
                 default: {
-                    const int64_t n = ns[st.q];
-                    e = trailing(h, LUs[st.q], n, st.KO, (int)(st.KE - st.KO), st.KE, n - st.KE, st.KE, n - st.KE);
+                    const int64_t n = ns[st.q], rows = n - st.KE;
+                    float* LU = LUs[st.q];
+                    e = tc_split(LU + st.KO * n + st.KE, 1, n, rows, OB, tA, bads[st.q], s);
+                    if (e == cudaSuccess) e = tc_split(LU + st.KE * n + st.KO, n, 1, rows, OB, tB, bads[st.q], s);
+                    if (e == cudaSuccess)
+                        e = tc_gemm(tA, rows, tB, rows, -1.f, 1.f, LU + st.KE * n + st.KE, n, sms, bads[st.q], s);
                 }
             }
             if (e == cudaSuccess) e = cudaGetLastError();
         }
     }
-    cudaFreeAsync(ditems, s);
-    cudaFreeAsync(ddesc, s);
     return e;
 }
 
@@ -1360,14 +1502,9 @@ cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, in
     return cudaGetLastError();
 }
 
-size_t lu_blas_workspace_bytes() { return kBlasWorkspace; }
-
 // X (n x k, ld n) <- U^{-1} L^{-1} X
-cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s) {
-    set_attrs();
-    cublasHandle_t h = (cublasHandle_t)blas;
-    cudaError_t e = prepare_blas(h, G, s);
-    if (e != cudaSuccess) return e;
+cudaError_t lu_solve_fp32(LuGraphs* G, const float* LU, int64_t n, float* X, int k, cudaStream_t s) {
+    cudaError_t e;
     if (!G->dinv) return cudaErrorInvalidValue;  // factor first
     if (!G->solve || G->solve_X != X || G->solve_k != k || G->solve_LU != LU) {
         if (G->solve) cudaGraphExecDestroy(G->solve);
@@ -1379,7 +1516,7 @@ cudaError_t lu_solve_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, f
             G->tmp_floats = (size_t)n * k;
         }
         const int64_t nsup = (G->super_n == n && G->dinv4) ? n / SB : 0;
-        e = capture(s, &G->solve, [&] { return solve_body(h, LU, G->dinv, G->dinv4, nsup, n, X, G->tmp, k); });
+        e = capture(s, &G->solve, [&] { return solve_body(LU, G->dinv, G->dinv4, nsup, n, X, G->tmp, k, s); });
         if (e != cudaSuccess) return e;
         G->solve_X = X;
         G->solve_k = k;
@@ -1394,9 +1531,9 @@ __global__ void k_identity(float* __restrict__ X, int64_t n) {
     if (t < n * n) X[t] = (t / n == t % n) ? 1.f : 0.f;
 }
 
-cudaError_t lu_invert_fp32(void* blas, LuGraphs* G, const float* LU, int64_t n, float* Ainv, cudaStream_t s) {
+cudaError_t lu_invert_fp32(LuGraphs* G, const float* LU, int64_t n, float* Ainv, cudaStream_t s) {
     k_identity<<<nb256(n * n), 256, 0, s>>>(Ainv, n);
-    cudaError_t e = lu_solve_fp32(blas, G, LU, n, Ainv, (int)n, s);
+    cudaError_t e = lu_solve_fp32(G, LU, n, Ainv, (int)n, s);
     if (e != cudaSuccess) return e;
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return e;
     // the n-column substitution graph and its n x n scratch are not needed again
@@ -1416,9 +1553,9 @@ size_t solve_lu_work_bytes(int64_t n, int k) {
            sizeof(double) * (size_t)residual_chunks(n) * 17 * (size_t)n + 64 * 1024;
 }
 
-cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n,
-                             int k, const double* rhs, double* x, void* work, double tol, int max_steps,
-                             SolveStats* st, cudaStream_t s, const float* Ainv) {
+cudaError_t solve_lu_refined(LuGraphs* G, const float* A32, const float* Alo, const float* LU, int64_t n, int k,
+                             const double* rhs, double* x, void* work, double tol, int max_steps, SolveStats* st,
+                             cudaStream_t s, const float* Ainv) {
     char* p = (char*)work;
     auto take = [&](size_t bytes) {
         char* r = p;
@@ -1443,17 +1580,10 @@ cudaError_t solve_lu_refined(void* blas, LuGraphs* G, const float* A32, const fl
     for (; steps < max_steps; steps++) {
         k_d2f<<<nb256(kn), 256, 0, s>>>(r64, d32, kn);
         if (Ainv) {  // correction = Ainv r (one product instead of the two substitutions)
-            cublasHandle_t h = (cublasHandle_t)blas;
-            if ((e = prepare_blas(h, G, s)) != cudaSuccess) return e;
-            const float one = 1.f, zero = 0.f;
-            cublasStatus_t bs = k == 1 ? cublasSgemv(h, CUBLAS_OP_N, (int)n, (int)n, &one, Ainv, (int)n, d32, 1, &zero,
-                                                     e32, 1)
-                                       : cublasSgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, (int)n, k, (int)n, &one, Ainv,
-                                                     (int)n, d32, (int)n, &zero, e32, (int)n);
-            if (bs != CUBLAS_STATUS_SUCCESS) return cudaErrorUnknown;
+            if ((e = skinny(Ainv, n, d32, n, e32, n, n, n, k, 1.f, false, s)) != cudaSuccess) return e;
             k_addf<<<nb256(kn), 256, 0, s>>>(x, e32, kn);
         } else {
-            if ((e = lu_solve_fp32(blas, G, LU, n, d32, k, s)) != cudaSuccess) return e;
+            if ((e = lu_solve_fp32(G, LU, n, d32, k, s)) != cudaSuccess) return e;
             k_addf<<<nb256(kn), 256, 0, s>>>(x, d32, kn);
         }
         if ((e = residual_df(A32, Alo, n, k, x, rhs, r64, P64, s)) != cudaSuccess) return e;

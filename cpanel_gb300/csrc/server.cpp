@@ -19,6 +19,7 @@
 #include "../../include/cpanel_gpu.h"
 #include "../../include/cpanel_serve.h"
 #include "../../include/cpanel_vp.h"
+#include "assemble.h"
 #include "vpgeom.h"
 
 namespace {
@@ -198,21 +199,21 @@ void fill_info(const Request& r, cpg_request_info* info) {
 extern "C" {
 
 int64_t cpg_server_footprint(int64_t n, int k, int precision) {
-    // matrices and factors, per-case vectors, the CHTLS/Trefftz tables, the LU's
-    // cuBLAS workspace, panel staging and split tensor-core operands (two of n rows x 1,024
-    // halves x 2 and their scales: 8,208 bytes a row; lu.cu), with a fixed margin
+    // matrices and factors, per-case vectors, the CHTLS/Trefftz tables, the factorization's
+    // diagonal-block inverses, split tensor-core operands and scratch (lu_factor_bytes), with a
+    // fixed margin
     const int64_t nn = n * n;
-    int64_t mats = precision == CPG_PLAIN_FP64 ? 16 * nn : 12 * nn + (int64_t)n * (128 * 4 + 8208) + ((int64_t)256 << 20);
+    int64_t mats = precision == CPG_PLAIN_FP64 ? 16 * nn : 12 * nn + (int64_t)cpg::lu_factor_bytes(n);
     return mats + (int64_t)n * (int64_t)(2000 + 64 * k) + ((int64_t)64 << 20);
 }
 
 int64_t cpg_server_footprint_vp(int64_t n, int64_t n2, int nsteps, int precision) {
-    // A and B (FP64), C; for CPG_MIXED the float pair of A, its LU and the LU's staging;
-    // per particle its state, tree slot, step scratch and the panel kernels' partial sums
+    // A and B (FP64), C; for CPG_MIXED the float pair of A, its LU, inverse and the inversion's
+    // n x n scratch, and the factorization's own buffers (lu_factor_bytes); per particle its
+    // state, tree slot, step scratch and the panel kernels' partial sums
     const int64_t nn = n * n;
     int64_t mats = 16 * nn + 8 * n * n2;
-    if (precision == CPG_MIXED)  // + inverse and its scratch, split tensor-core operands
-        mats += 20 * nn + n * (128 * 4 + 8208) + ((int64_t)256 << 20);
+    if (precision == CPG_MIXED) mats += 20 * nn + (int64_t)cpg::lu_factor_bytes(n);
     const int64_t np = n2 * (int64_t)(nsteps > 0 ? nsteps : 0);
     return mats + n * 4000 + np * 4096 + ((int64_t)64 << 20);
 }

@@ -363,10 +363,12 @@ __global__ void k_split_kmajor(const float* __restrict__ src, int64_t rs, int64_
     }
 }
 
-// column-major source, pass 1: row maxima.  Block 32 rows x 8 K groups.
-__global__ void k_rowmax_mmajor(const float* __restrict__ src, int64_t ks, int64_t rows, int64_t K,
-                                float* __restrict__ scale, float* __restrict__ inv, int* err) {
-    __shared__ float part[8][32];
+// column-major source, pass 1: row maxima.  Block 32 rows x 16 K groups, eight loads in flight
+// per thread.
+__global__ void __launch_bounds__(512) k_rowmax_mmajor(const float* __restrict__ src, int64_t ks, int64_t rows,
+                                                       int64_t K, float* __restrict__ scale, float* __restrict__ inv,
+                                                       int* err) {
+    __shared__ float part[16][32];
     __shared__ int bad;
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
@@ -375,16 +377,24 @@ __global__ void k_rowmax_mmajor(const float* __restrict__ src, int64_t ks, int64
     float mx = 0.f;
     bool fin = true;
     if (r < rows)
-        for (int64_t k = gi; k < K; k += 8) {
-            const float a = fabsf(src[k * ks + r]);
-            fin = fin && isfinite(a);
-            mx = fmaxf(mx, a);
+        for (int64_t k = gi; k < K; k += 16 * 8) {
+            float a[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                const int64_t kk = k + 16 * u;
+                a[u] = kk < K ? fabsf(src[kk * ks + r]) : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                fin = fin && isfinite(a[u]);
+                mx = fmaxf(mx, a[u]);
+            }
         }
     part[gi][rl] = mx;
     if (!fin) bad = 1;
     __syncthreads();
     if (gi == 0 && r < rows) {
-        for (int q = 1; q < 8; q++) mx = fmaxf(mx, part[q][rl]);
+        for (int q = 1; q < 16; q++) mx = fmaxf(mx, part[q][rl]);
         const float sc = row_scale(mx);
         scale[r] = sc;
         inv[r] = 1.f / sc;
@@ -471,7 +481,7 @@ cudaError_t tc_split(const float* src, int64_t rs, int64_t ks, int64_t rows, int
                                                                      op.inv_scale, err);
     } else {
         float* scale = op.inv_scale + op.rows_cap;  // the second half of the scale area
-        k_rowmax_mmajor<<<(unsigned)((rows + 31) / 32), 256, 0, s>>>(src, ks, rows, K, scale, op.inv_scale, err);
+        k_rowmax_mmajor<<<(unsigned)((rows + 31) / 32), 512, 0, s>>>(src, ks, rows, K, scale, op.inv_scale, err);
         dim3 grid((unsigned)((rows + 31) / 32), (unsigned)(op.kp / BK));
         k_split_mmajor<<<grid, 256, 0, s>>>(src, ks, rows, K, op.kp, op.rows_cap, scale, op.data);
     }

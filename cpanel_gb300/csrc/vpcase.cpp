@@ -33,8 +33,6 @@
 #include <string>
 #include <vector>
 
-#include <cublas_v2.h>
-
 #include "../../include/cpanel_gpu.h"
 #include "../../include/cpanel_vp.h"
 #include "assemble.h"
@@ -46,11 +44,9 @@
 #include "vpkern.h"
 
 namespace cpg {
-// context accessors (api.cpp): last error message, stream, cuBLAS handle (created on
-// first use; null if that fails)
+// context accessors (api.cpp): last error message, stream
 void ctx_set_error(cpg_ctx* ctx, const std::string& msg);
 cudaStream_t ctx_stream(cpg_ctx* ctx);
-void* ctx_blas(cpg_ctx* ctx);
 int ctx_particle_precision(cpg_ctx* ctx);
 }  // namespace cpg
 
@@ -241,7 +237,7 @@ cudaError_t solve(cpg_vpcase& S, bool with_c) {
     cpg::SolveStats st;
     bool done = false;
     if (S.mixed()) {
-        e = cpg::solve_lu_refined(cpg::ctx_blas(S.ctx), &S.lug, S.A32.as<float>(), S.Alo.as<float>(), nullptr, S.n, 1,
+        e = cpg::solve_lu_refined(&S.lug, S.A32.as<float>(), S.Alo.as<float>(), nullptr, S.n, 1,
                                   S.rhs.as<double>(), S.mu.as<double>(), S.work.p, kVPRefineTol, 8, &st, S.s,
                                   S.Ainv.as<float>());
         if (e != cudaSuccess) return e;
@@ -832,12 +828,6 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
     if ((e = cpg::vp_launch_cmat(S.rec.as<double>(), n, S.q2.as<double>(), S.n2, S.C.as<double>(), S.s)) != cudaSuccess)
         return fail_cuda(e, "C matrix");
     if (S.mixed()) {  // A as a float pair and its FP32 LU, once (A is the same every step)
-        void* blas = cpg::ctx_blas(ctx);
-        if (!blas) {
-            cpg::ctx_set_error(ctx, "cublasCreate failed");
-            cpg_vpcase_destroy(Sp);
-            return CPG_E_CUDA;
-        }
         const size_t nn = (size_t)n * n;
         Buf* f32[] = {&S.A32, &S.Alo, &S.LU};
         for (Buf* b : f32)
@@ -849,12 +839,12 @@ int cpg_vpcase_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, const 
             return fail_cuda(e, "split A");
         if ((e = cudaMemcpyAsync(S.LU.p, S.A32.p, sizeof(float) * nn, cudaMemcpyDeviceToDevice, S.s)) != cudaSuccess)
             return fail_cuda(e, "LU");
-        if ((e = cpg::lu_factor_fp32(blas, &S.lug, S.LU.as<float>(), n, S.bad.as<int>(), S.s)) != cudaSuccess)
+        if ((e = cpg::lu_factor_fp32(&S.lug, S.LU.as<float>(), n, S.bad.as<int>(), S.s)) != cudaSuccess)
             return fail_cuda(e, "LU factorization");
         // every step solves with the same A: its FP32 inverse makes each refinement pass one
         // matrix-vector product (the factors are not needed after this)
         if ((e = S.Ainv.ensure(sizeof(float) * nn, S.s)) != cudaSuccess) return fail_cuda(e, "alloc inverse");
-        if ((e = cpg::lu_invert_fp32(blas, &S.lug, S.LU.as<float>(), n, S.Ainv.as<float>(), S.s)) != cudaSuccess)
+        if ((e = cpg::lu_invert_fp32(&S.lug, S.LU.as<float>(), n, S.Ainv.as<float>(), S.s)) != cudaSuccess)
             return fail_cuda(e, "inverse");
         S.LU.release();
     }

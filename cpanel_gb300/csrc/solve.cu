@@ -76,20 +76,63 @@ __global__ void k_mv_reduce(const TACC* __restrict__ P, int nchunk, int KB, int 
     Y[o] = (TY)s;
 }
 
-// Double-float residual chunks: exact FP32 products of A32 with x = xh + xl.
-// x is staged as (hi, lo) pairs (one 8-byte shared load per product); the matrix
-// columns are read four at a time before any arithmetic so that four loads per
-// thread are in flight.
-__device__ __forceinline__ void df_acc(float a, float al, float2 x, float& hi, float& lo) {
-    float p = __fmul_rn(a, x.x);
-    float e = __fmaf_rn(a, x.x, -p);  // exact product error
-    e = __fmaf_rn(a, x.y, e);
-    e = __fmaf_rn(al, x.x, e);
-    float s = __fadd_rn(hi, p);  // TwoSum(hi, p)
-    float bb = __fsub_rn(s, hi);
-    float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+// Double-float residual chunks: exact FP32 products of A32 with x = xh + xl, two right-hand
+// sides at a time in packed FP32x2 arithmetic (every operation rounds as its scalar form: the
+// product is formed negated, -p = (-a) x, which rounds to exactly -(a x)).  x is staged as
+// packed pairs of its high and of its low parts; the matrix columns are read four at a time
+// before any arithmetic so that four loads per thread are in flight.
+__device__ __forceinline__ unsigned long long f2pack(float a, float b) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2mul(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b, unsigned long long c) {
+    unsigned long long r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2add(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ unsigned long long f2sub(unsigned long long a, unsigned long long b) {
+    unsigned long long r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+// hi + lo += (a + al) (xh + xl) for two right-hand sides: p = a xh exactly as p + e (e also
+// takes a xl and al xh), TwoSum(hi, p) into hi and its error into lo
+__device__ __forceinline__ void df_acc2(unsigned long long a2, unsigned long long na2, unsigned long long al2,
+                                        unsigned long long xh, unsigned long long xl, unsigned long long& hi,
+                                        unsigned long long& lo) {
+    const unsigned long long pn = f2mul(na2, xh);  // -p
+    unsigned long long e = f2fma(a2, xh, pn);      // exact product error
+    e = f2fma(a2, xl, e);
+    e = f2fma(al2, xh, e);
+    const unsigned long long s = f2sub(hi, pn);  // hi + p
+    const unsigned long long bb = f2sub(s, hi);
+    const unsigned long long err = f2sub(f2sub(hi, f2sub(s, bb)), f2add(pn, bb));  // (hi - (s - bb)) + (p - bb)
     hi = s;
-    lo = __fadd_rn(lo, __fadd_rn(err, e));
+    lo = f2add(lo, f2add(err, e));
+}
+
+// (H, L) += (h, l): TwoSum of the high parts, low parts and the error into L
+__device__ __forceinline__ void df_merge2(unsigned long long& H, unsigned long long& L, unsigned long long h,
+                                         unsigned long long l) {
+    const unsigned long long s = f2add(H, h);
+    const unsigned long long bb = f2sub(s, H);
+    const unsigned long long err = f2add(f2sub(H, f2sub(s, bb)), f2sub(h, bb));
+    H = s;
+    L = f2add(L, f2add(err, l));
 }
 
 template <int KB>
@@ -97,64 +140,81 @@ __global__ void __launch_bounds__(MV_THREADS) k_resid_df(const float* __restrict
                                                          int64_t n, int64_t jchunk,
                                                          const double* __restrict__ X, int col0, int kb,
                                                          double* __restrict__ P) {
-    __shared__ float2 sx[MV_JT][KB];
+    constexpr int KP = (KB + 1) / 2;  // packed pairs of right-hand sides
+    __shared__ unsigned long long sxh[MV_JT][KP], sxl[MV_JT][KP];
     int64_t i = (int64_t)blockIdx.x * MV_THREADS + threadIdx.x;
     int64_t jb = (int64_t)blockIdx.y * jchunk, je = min(n, jb + jchunk);
-    double acc[KB];
-    float hi[KB], lo[KB];  // double-float partial sums over two tiles (64 columns)
+    // double-float sums: (hi, lo) over two tiles (64 columns), merged into (H, L) for the chunk
+    unsigned long long hi[KP], lo[KP], H[KP], L[KP];
 #pragma unroll
-    for (int c = 0; c < KB; c++) {
-        acc[c] = 0;
-        hi[c] = lo[c] = 0.f;
-    }
+    for (int q = 0; q < KP; q++) hi[q] = lo[q] = H[q] = L[q] = 0ull;
     int tile = 0;
     for (int64_t j0 = jb; j0 < je; j0 += MV_JT, tile++) {
         __syncthreads();
-        for (int t = threadIdx.x; t < MV_JT * KB; t += MV_THREADS) {
-            int jj = t / KB, c = t % KB;
-            int64_t j = j0 + jj;
-            double xv = (j < je && c < kb) ? X[(int64_t)(col0 + c) * n + j] : 0.0;
-            float h = (float)xv;
-            sx[jj][c] = make_float2(h, (float)(xv - (double)h));
+        for (int t = threadIdx.x; t < MV_JT * KP; t += MV_THREADS) {
+            const int jj = t / KP, q = t % KP;
+            const int64_t j = j0 + jj;
+            float h[2], l[2];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const int c = 2 * q + u;
+                const double xv = (j < je && c < kb) ? X[(int64_t)(col0 + c) * n + j] : 0.0;
+                h[u] = (float)xv;
+                l[u] = (float)(xv - (double)h[u]);
+            }
+            sxh[jj][q] = f2pack(h[0], h[1]);
+            sxl[jj][q] = f2pack(l[0], l[1]);
         }
         __syncthreads();
         if (i < n) {
-            int cnt = (int)min((int64_t)MV_JT, je - j0);
+            const int cnt = (int)min((int64_t)MV_JT, je - j0);
             const float* Ap = A + j0 * n + i;
             const float* Lp = Alo + j0 * n + i;
-            int t = 0;
-            for (; t + 3 < cnt; t += 4) {
-                float a[4], al[4];
+            float a[4], al[4];  // the next four columns are loaded while these four are used
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                a[u] = u < cnt ? __ldg(Ap + (int64_t)u * n) : 0.f;
+                al[u] = u < cnt ? __ldg(Lp + (int64_t)u * n) : 0.f;
+            }
+            for (int t = 0; t < cnt; t += 4) {
+                float na[4], nal[4];
 #pragma unroll
                 for (int u = 0; u < 4; u++) {
-                    a[u] = __ldg(Ap + (int64_t)(t + u) * n);
-                    al[u] = __ldg(Lp + (int64_t)(t + u) * n);
+                    const int tt = t + 4 + u;
+                    na[u] = tt < cnt ? __ldg(Ap + (int64_t)tt * n) : 0.f;
+                    nal[u] = tt < cnt ? __ldg(Lp + (int64_t)tt * n) : 0.f;
                 }
 #pragma unroll
-                for (int u = 0; u < 4; u++)
+                for (int u = 0; u < 4; u++) {
+                    if (t + u < cnt) {
+                        const unsigned long long a2 = f2pack(a[u], a[u]), na2 = f2pack(-a[u], -a[u]),
+                                                 al2 = f2pack(al[u], al[u]);
 #pragma unroll
-                    for (int c = 0; c < KB; c++) df_acc(a[u], al[u], sx[t + u][c], hi[c], lo[c]);
+                        for (int q = 0; q < KP; q++)
+                            df_acc2(a2, na2, al2, sxh[t + u][q], sxl[t + u][q], hi[q], lo[q]);
+                    }
+                    a[u] = na[u];
+                    al[u] = nal[u];
+                }
             }
-            for (; t < cnt; t++) {
-                float a = __ldg(Ap + (int64_t)t * n), al = __ldg(Lp + (int64_t)t * n);
-#pragma unroll
-                for (int c = 0; c < KB; c++) df_acc(a, al, sx[t][c], hi[c], lo[c]);
-            }
-            // into FP64 every second tile and after the last one (FP64 runs at 1/64 of the
-            // FP32 rate here, so flushing every tile cost as much as the products)
             if ((tile & 1) || j0 + MV_JT >= je) {
 #pragma unroll
-                for (int c = 0; c < KB; c++) {
-                    acc[c] += (double)hi[c] + (double)lo[c];
-                    hi[c] = lo[c] = 0.f;
+                for (int q = 0; q < KP; q++) {
+                    df_merge2(H[q], L[q], hi[q], lo[q]);
+                    hi[q] = lo[q] = 0ull;
                 }
             }
         }
     }
     if (i < n) {
 #pragma unroll
-        for (int c = 0; c < KB; c++)
-            if (c < kb) P[((int64_t)blockIdx.y * KB + c) * n + i] = acc[c];
+        for (int q = 0; q < KP; q++) {
+            float h0, h1, l0, l1;
+            f2unpack(H[q], h0, h1);
+            f2unpack(L[q], l0, l1);
+            if (2 * q < kb) P[((int64_t)blockIdx.y * KB + 2 * q) * n + i] = (double)h0 + (double)l0;
+            if (2 * q + 1 < kb) P[((int64_t)blockIdx.y * KB + 2 * q + 1) * n + i] = (double)h1 + (double)l1;
+        }
     }
 }
 

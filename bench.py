@@ -544,6 +544,12 @@ def batch_loop_only(n_wings=64, lockstep=True):
 
 REF_SOLVES = 2  # config-2 right-hand sides the reference arm solves to convergence
 
+# DRAM bytes (read + write) of one factorization of the benchmark wing: the sum of dram__bytes_read.sum and
+# dram__bytes_write.sum over the 945 kernels of each factorization in a one-pass ncu capture of
+# `bench.py --steps 1 --warmup 1 --no-cpu --no-plain --no-serving --no-vp` (four factorizations: 31.8-32.1 GB)
+LU_TRAFFIC = {"multi_rhs": 3.20e10}
+LU_TRAFFIC_SOURCE = "ncu capture (dram__bytes_read.sum + dram__bytes_write.sum over every kernel of one factorization)"
+
 
 def cpu_model():
     """(model name, nproc) of the host."""
@@ -796,7 +802,8 @@ def main():
                               "k_tc_gemm rank-1024 updates (tcgen05, FP16 hi/lo split), panel products",
                               "achieved": ach, "unit": "TFLOP/s (FP32-equivalent)", "peak": pk, "frac": ach / pk,
                               "peak_source": "%s bf16 sustained / 3 FP16 products (of %s)" % (tc_src, tc_src),
-                              "traffic": None, "avg_launch_ms": g_ms / g_l, "launches": g_l}
+                              "traffic": LU_TRAFFIC.get(args.workload), "traffic_source": LU_TRAFFIC_SOURCE,
+                              "avg_launch_ms": g_ms / g_l, "launches": g_l}
     t_l, t_ms = prof["tc_gemm"]
     if t_l and g_l:
         # the tensor-core GEMM launches inside the factorizations: 2 (n - KE)^2 1024 flop per

@@ -104,7 +104,11 @@ def make_wing(spec: WingSpec):
         nodes = nodes + spec.jitter * h * rng.uniform(-1, 1, nodes.shape)
     tris = []
     for j in range(S - 1):
-        for k in range(R):
+        # each span strip lists its ring from the trailing edge over the lower side first, so the
+        # first triangle that names a trailing-edge edge is the lower one, as in the OpenVSP meshes
+        # of the reference's cases: the vortex-particle buffer wake takes its upper/lower panels
+        # from that edge's node order (edge::checkTE against the buffer quads' normals)
+        for k in reversed(range(R)):
             a, b = node(j, k), node(j, k + 1)
             c, d = node(j + 1, k + 1), node(j + 1, k)
             tris.append((a, d, c))

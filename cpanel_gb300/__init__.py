@@ -218,6 +218,17 @@ def solve_cases(geom, flows, Sref=1.0, bref=1.0, cref=1.0, cg=(0.0, 0.0, 0.0), p
     return out
 
 
+def spanwise_loads(geom, case=0, wake=0):
+    """The spanwise Trefftz-plane loads of one case of the last solve_cases call on geom and one of its
+    wakes, as cpCase::writeSpanwiseData scales them (CPanel/cpCase.cpp:910-935): a dict of 2y/b ("y2b"),
+    Cl / PG ("cl") and Cdi / PG^2 ("cdi") at the reference's 165 stations."""
+    n = C.c_int(512)
+    out = {k: np.zeros(512) for k in ("y2b", "cl", "cdi")}
+    geom.ctx.check(geom.ctx.L.cpg_spanwise_loads(geom.h, case, wake, _p(out["y2b"]), _p(out["cl"]), _p(out["cdi"]),
+                                                 C.byref(n)), "spanwise_loads")
+    return {k: v[:n.value].copy() for k, v in out.items()}
+
+
 class CpCase:
     """cpCase: one flow condition on a geometry (CPanel/cpCase.h:127-136)."""
 
@@ -233,6 +244,8 @@ class CpCase:
 
     def run(self):
         self.res = solve_cases(self.geom, [self.flow], precision=self.precision, **self.refs)
+        # the spanwise loads of every wake, read before another solve replaces them
+        self.span = [spanwise_loads(self.geom, 0, w) for w in range(self.geom.ctx.L.cpg_trefftz_wakes(self.geom.h))]
         return self.res["status"] == 0
 
     def getCL(self):
@@ -338,7 +351,8 @@ class CpCase:
     def writeFiles(self, directory=".", geom_file=""):
         """cpCase::writeFiles (CPanel/cpCase.cpp:667-709): the case directory
         V<V>_Mach<M>_alpha<a>_beta<b> under `directory` with surfaceData.vtu, wakeData.vtu (when
-        the mesh has wake panels), volumeMesh.vtu (after volumeSurvey), OffBodyStreamlines.vtu
+        the mesh has wake panels), spanwiseData_Wake<i>.csv per wake, volumeMesh.vtu (after volumeSurvey),
+        OffBodyStreamlines.vtu
         (after streamlines; the reference's name for off-body lines, CPanel/cpCase.cpp:626, where
         streamlines.vtu holds its surface streamlines), and
         caseMgr::writeSummary's .CPout (CPanel/CPanelMgr.cpp:89-116) beside it.  Returns the paths
@@ -363,6 +377,8 @@ class CpCase:
                                 sv["cp"])
         if getattr(self, "lines", None) is not None:
             io.write_streamlines_vtu(os.path.join(sub, "OffBodyStreamlines.vtu"), self.lines)
+        for w, span in enumerate(getattr(self, "span", None) or []):  # cpCase.cpp:694
+            io.write_spanwise_csv(os.path.join(sub, "spanwiseData_Wake%d.csv" % (w + 1)), span)
         stem = os.path.splitext(os.path.basename(geom_file))[0] if geom_file else "case"
         cpout = os.path.join(directory, stem + ".CPout")
         io.write_cpout(cpout, [dict(V=V, alpha=alpha, beta=beta, mach=mach, CL=self.getCL(), CDi=self.getCD(),

@@ -66,6 +66,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read",
            "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_gemm_f32_tc", "cpg_release_spares", "cpg_stability_derivatives",
            "cpg_volume_velocity", "cpg_topology_wake_tris", "cpg_streamlines", "cpg_streamlines_field",
+           "cpg_trefftz_wakes", "cpg_spanwise_loads",
            # cpanel_vp.h
            "cpg_ptree_build", "cpg_ptree_destroy", "cpg_ptree_info_get", "cpg_ptree_table", "cpg_ptree_host_table",
            "cpg_bh_velocity_points", "cpg_bh_particles", "cpg_ptree_set_precision", "cpg_set_particle_precision", "cpg_particles_velocity", "cpg_particles_stretch_diff",
@@ -80,7 +81,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_lu_factor_grouped",
            # cpanel_io.h
            "cpg_write_cpout", "cpg_write_surface_vtu", "cpg_write_volume_vtu", "cpg_write_wake_vtu",
-           "cpg_write_streamlines_vtu"]
+           "cpg_write_streamlines_vtu", "cpg_write_spanwise_csv"]
 
 TUNE_OFF, TUNE_AUTO, TUNE_FORCE = 0, 1, 2
 
@@ -254,6 +255,9 @@ def load():
     L.cpg_write_surface_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D, D, D, D, D, D]
     L.cpg_write_volume_vtu.argtypes = [C.c_char_p, D, C.c_int64, I64, C.c_int64, D, D]
     L.cpg_write_streamlines_vtu.argtypes = [C.c_char_p, D, D, I32, C.c_int, C.c_int]
+    L.cpg_write_spanwise_csv.argtypes = [C.c_char_p, D, D, D, C.c_int]
+    L.cpg_trefftz_wakes.argtypes = [vp]
+    L.cpg_spanwise_loads.argtypes = [vp, C.c_int, C.c_int, D, D, D, C.POINTER(C.c_int)]
     L.cpg_volume_velocity.argtypes = [vp, D, D, D, C.c_int64, D]
     L.cpg_topology_wake_tris.argtypes = [D, C.c_int64, I64, I32, C.c_int64, I64]
     L.cpg_streamlines.argtypes = [vp, D, D, C.POINTER(Flow), D, C.c_int, C.c_double, C.c_double, C.c_int, D, D, I32,

@@ -176,6 +176,11 @@ struct cpg_geometry {
     int64_t n_near64 = 0, n_near32 = 0;
     cpg::PostTables T;
     float ms_asm = 0;
+    // the last cpg_solve_cases whose post-processing left its Trefftz station loads in post_work:
+    // its case count, each case's Prandtl-Glauert factor and bref (0 cases: none yet)
+    int post_k = 0;
+    std::vector<double> post_pg;
+    double post_bref = 0;
 };
 
 struct cpg_ptree {
@@ -709,7 +714,12 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     CK(cudaEventRecord(e1, s), "event");
     CK(g->post_work.ensure(cpg::post_work_bytes(g->T, k)), "alloc post workspace");
     CK(cudaStreamWaitEvent(s, g->post_ev, 0), "wait for the post tables");
+    g->post_k = 0;
     CK(cpg::launch_post(g->T, k, dcs, mu, phi, vel, cp, forces, tz, wmu, g->post_work.p, s), "post");
+    g->post_k = k;
+    g->post_pg.resize(k);
+    for (int c = 0; c < k; c++) g->post_pg[c] = cs[c].PG;
+    g->post_bref = refs->bref;
     CK(cudaEventRecord(e2, s), "event");
     // host outputs
     auto copy = [&](double* dst, const double* src, size_t cnt) -> cudaError_t {
@@ -757,6 +767,40 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     }
     if (st.residual_max > (precision == CPG_PLAIN_FP64 ? 1e-10 : 1e-9))
         return fail(ctx, CPG_E_NOT_CONVERGED, "solver stopped above tolerance");
+    return CPG_OK;
+}
+
+int cpg_trefftz_wakes(const cpg_geometry* g) { return g ? (int)g->H.trefftz.size() : 0; }
+
+int cpg_spanwise_loads(cpg_geometry* g, int c, int wake, double* y2b, double* cl, double* cdi, int* n) {
+    if (!g || !n) return CPG_E_INVALID;
+    cpg_ctx* ctx = g->ctx;
+    if (g->post_k <= 0) return fail(ctx, CPG_E_INVALID, "no steady case solved on this geometry yet");
+    if (c < 0 || c >= g->post_k) return fail(ctx, CPG_E_INVALID, "case index out of range");
+    if (wake < 0 || wake >= (int)g->H.trefftz.size()) return fail(ctx, CPG_E_INVALID, "wake index out of range");
+    const cpg::TrefftzWake& W = g->H.trefftz[wake];
+    const int nst = (int)W.st.size(), m = nst + 2;  // the reference's stations 0..164
+    if (*n < m || !y2b || !cl || !cdi) {
+        *n = m;
+        return fail(ctx, CPG_E_INVALID, "spanwise buffers shorter than the station count");
+    }
+    std::vector<double> raw(2 * (size_t)nst);
+    CK(cudaSetDevice(ctx->device), "device");
+    CK(cudaMemcpyAsync(raw.data(), cpg::post_station_loads(g->T, g->post_k, c, wake, g->post_work.p),
+                       sizeof(double) * raw.size(), cudaMemcpyDeviceToHost, ctx->stream),
+       "copy station loads");
+    CK(cudaStreamSynchronize(ctx->stream), "copy station loads");
+    // cpCase::writeSpanwiseData (CPanel/cpCase.cpp:915-917) on wake::trefftzPlane's yLoc, Cl and Cd
+    // (wake.cpp:153-176): the end stations are yMin and yMax with zero loads
+    const double PG = g->post_pg[c], b = g->post_bref;
+    for (int i = 0; i < m; i++) {
+        const double y = i == 0 ? W.y0 : i == m - 1 ? W.y1 : W.y0 + i * W.step;
+        const bool inner = i > 0 && i < m - 1;
+        y2b[i] = 2 * y / b;
+        cl[i] = (inner ? raw[2 * (i - 1)] : 0.0) / PG;
+        cdi[i] = (inner ? raw[2 * (i - 1) + 1] : 0.0) / std::pow(PG, 2);
+    }
+    *n = m;
     return CPG_OK;
 }
 

@@ -632,6 +632,8 @@ std::string build_mesh(const double* nodes, int64_t nn, const int64_t* tris, con
         TrefftzWake T;
         const int nP2 = 164;
         T.step = (W.yMax - W.yMin) / nP2;
+        T.y0 = W.yMin;
+        T.y1 = W.yMax;
         double xT = W.x0 + 2 * (W.xf - W.x0) / 3;
         for (int i = 1; i < nP2; i++) {
             TrefftzStation S;

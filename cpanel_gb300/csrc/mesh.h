@@ -33,6 +33,7 @@ struct TrefftzStation {
 
 struct TrefftzWake {
     double step;                       // Simpson step
+    double y0 = 0, y1 = 0;             // wake::yMin, yMax: the end stations 0 and 164
     std::vector<TrefftzStation> st;    // 163 stations (i = 1..163)
 };
 

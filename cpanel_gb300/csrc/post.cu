@@ -509,6 +509,12 @@ size_t post_work_bytes(const PostTables& t, int k) {
     return sizeof(double) * ((size_t)k * nb * 6 + (size_t)k * (t.n_pts + 2 * t.n_st * t.n_wakes)) + 1024;
 }
 
+const double* post_station_loads(const PostTables& t, int k, int c, int w, const void* work) {
+    const int64_t nb = (t.n + PT - 1) / PT;
+    const double* tz = (const double*)work + (size_t)k * nb * 6;  // k_trefftz's scratch, as launch_post lays it out
+    return tz + (int64_t)c * (t.n_pts + 2 * t.n_st * t.n_wakes) + t.n_pts + 2 * (int64_t)w * t.n_st;
+}
+
 cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs, const double* mu, double* phi, double* vel,
                         double* cp, double* forces, double* trefftz, double* wake_mu, void* work, cudaStream_t s) {
     int64_t nb = (t.n + PT - 1) / PT;

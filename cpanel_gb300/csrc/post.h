@@ -41,6 +41,9 @@ cudaError_t launch_chtls_weights(const PostTables& t, cudaStream_t s);
 // mu: k x n; outputs k x n (phi, cp), k x n x 3 (vel); forces k x 9 [Fbody Fwind CM];
 // trefftz k x 2 [CL CDi]; work: device scratch of post_work_bytes.
 size_t post_work_bytes(const PostTables& t, int k);
+// Device address, inside the work area of the last launch_post over k cases, of case c's Trefftz
+// station loads of wake w: (Cl, Cd) pairs of stations 1..n_st, before the Prandtl-Glauert factors.
+const double* post_station_loads(const PostTables& t, int k, int c, int w, const void* work);
 cudaError_t launch_post(const PostTables& t, int k, const CaseScalars* cs_dev, const double* mu, double* phi,
                         double* vel, double* cp, double* forces, double* trefftz, double* wake_mu, void* work,
                         cudaStream_t s);

@@ -313,4 +313,15 @@ int cpg_write_streamlines_vtu(const char* path, const double* pts, const double*
     }
 }
 
+int cpg_write_spanwise_csv(const char* path, const double* y2b, const double* cl, const double* cdi, int n) {
+    if (!path || n < 0 || (n > 0 && (!y2b || !cl || !cdi))) return CPG_E_INVALID;
+    std::ofstream f(path);
+    if (!f) return CPG_E_INVALID;
+    // a header line, then one row per station in the stream's default format (six significant digits)
+    f << "2y/b,Cl,Cdi" << std::endl;
+    for (int j = 0; j < n; j++) f << y2b[j] << "," << cl[j] << "," << cdi[j] << std::endl;
+    f.close();
+    return f ? CPG_OK : CPG_E_INVALID;
+}
+
 }  // extern "C"

@@ -161,6 +161,16 @@ def write_streamlines_vtu(path, lines):
         raise CpgError(rc, "cpg_write_streamlines_vtu(%s)" % path)
 
 
+def write_spanwise_csv(path, span):
+    """spanwiseData_Wake<i>.csv in cpCase::writeSpanwiseData's layout (CPanel/cpCase.cpp:910-935): span as
+    spanwise_loads returns it, {"y2b", "cl", "cdi"}."""
+    L = _lib.load()
+    cols = [np.ascontiguousarray(span[k], dtype=np.float64) for k in ("y2b", "cl", "cdi")]
+    rc = L.cpg_write_spanwise_csv(os.fsencode(path), *[c.ctypes.data_as(_lib.D) for c in cols], len(cols[0]))
+    if rc != 0:
+        raise CpgError(rc, "cpg_write_spanwise_csv(%s)" % path)
+
+
 def read_vtu_pieces(path):
     """Every piece of an ASCII .vtu file as {array name: array} (points under "Position")."""
     txt = open(path).read()

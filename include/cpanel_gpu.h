@@ -14,6 +14,8 @@
  *                          compVelocity :342-365, trefftzPlaneAnalysis :541-552)
  *   cpg_stability_derivatives  cpCase::stabilityDerivatives, CPanel/cpCase.cpp:635-665
  *   cpg_volume_velocity   cpCase::velocityAtPoint, CPanel/cpCase.cpp:1007-1021
+ *   cpg_spanwise_loads    wake::getSpanwisePnts/Cl/Cd as cpCase::writeSpanwiseData scales them,
+ *                         CPanel/cpCase.cpp:910-935, wake.cpp:146-188
  *   cpg_streamlines       streamline::streamline / rkf, CPanel/streamline.cpp:20-78, through
  *                         geometry::pntVelocity, CPanel/geometry.cpp:1239-1253
  *   cpg_panel_phi_inf     bodyPanel::panelPhiInf, CPanel/bodyPanel.cpp:132-190
@@ -187,6 +189,17 @@ int  cpg_stability_derivatives(cpg_geometry* g, const cpg_flow* flow, const cpg_
  * vel m x 3), for one case's source and doublet strengths (host arrays sigma, mu: n_body).  The
  * wake doublets follow from mu through the trailing-edge interpolation of the assembly.  V_inf
  * is not included (the reference adds it in populateVolMesh, CPanel/cpCase.cpp:1105-1122). */
+/* ---- spanwise Trefftz-plane loads (cpCase::writeSpanwiseData, CPanel/cpCase.cpp:910-935) ----
+ * cpg_trefftz_wakes: the number of wakes with a Trefftz plane, in the order CL sums them (the
+ * reference's spanwiseData_Wake<i + 1>.csv).  cpg_spanwise_loads: for case c of the last
+ * cpg_solve_cases call on g and wake `wake`, the reference's 165 stations (wake::trefftzPlane,
+ * wake.cpp:146-188): 2y/b, Cl / PG and Cdi / PG^2 (PG = sqrt(1 - M^2); the end stations carry zero
+ * loads).  *n: in, the length of each buffer; out, the stations (165).  CPG_E_INVALID if no steady
+ * case was solved on g, if c or wake is out of range or the buffers are too short (*n then holds
+ * the length needed). */
+int  cpg_trefftz_wakes(const cpg_geometry* g);
+int  cpg_spanwise_loads(cpg_geometry* g, int c, int wake, double* y2b, double* cl, double* cdi, int* n);
+
 int  cpg_volume_velocity(cpg_geometry* g, const double* sigma, const double* mu, const double* pts, int64_t m,
                          double* vel);
 

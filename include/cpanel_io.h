@@ -9,6 +9,7 @@
  *   cpg_write_wake_vtu      cpCase::writeWakeData, CPanel/cpCase.cpp:883-907
  *   cpg_write_volume_vtu    cpCase::writeVolMeshData, CPanel/cpCase.cpp:979-1004
  *   cpg_write_streamlines_vtu  cpCase::writeBodyStreamlines, CPanel/cpCase.cpp:937-977
+ *   cpg_write_spanwise_csv  cpCase::writeSpanwiseData, CPanel/cpCase.cpp:910-935
  *
  * The text follows the reference's layout and stream formatting (the same column widths,
  * precisions and array names), so the files diff against CPanel's own.  One difference is
@@ -83,6 +84,11 @@ int cpg_write_volume_vtu(const char* path, const double* points, int64_t n_point
  * the first counts[i] rows of line i are written). */
 int cpg_write_streamlines_vtu(const char* path, const double* pts, const double* vel, const int32_t* counts,
                               int n_lines, int max_points);
+
+/* Write spanwiseData_Wake<i>.csv (cpCase::writeSpanwiseData, CPanel/cpCase.cpp:910-935): the header
+ * "2y/b,Cl,Cdi", then n rows "y2b,cl,cdi" in the stream's default format; the columns are
+ * cpg_spanwise_loads' outputs. */
+int cpg_write_spanwise_csv(const char* path, const double* y2b, const double* cl, const double* cdi, int n);
 
 #ifdef __cplusplus
 }

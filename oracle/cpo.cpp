@@ -102,6 +102,9 @@ struct Mesh {
     std::vector<int> bPanels;  // matrix order -> body index
     std::vector<int> wPanels;  // wPanels order -> wakeP index
     std::vector<int> bodyIndex;  // body index -> matrix index
+    // spanwise loads of the last post-processing, per live wake: 2y/b, Cl / PG, Cd / PG^2 at the
+    // 165 Trefftz stations (cpCase::writeSpanwiseData, CPanel/cpCase.cpp:910-935)
+    std::vector<std::vector<double>> span;
 };
 
 /* ------------------------------------------------------------ panel geometry */
@@ -1009,9 +1012,12 @@ double Vradial(const Wake& W, const WakeEval& pot, V3 pWake) {
 
 /* wake::trefftzPlane, CPanel/wake.cpp:146-188 */
 void trefftzPlane(const Mesh& M, const Wake& W, const WakeEval& pot, const std::vector<double>& mu, double Vinf,
-                  double Sref, double& CL, double& CD) {
+                  double Sref, double& CL, double& CD, std::vector<double>& yLoc, std::vector<double>& Cl,
+                  std::vector<double>& Cd) {
     const int nPnts = 164;
-    std::vector<double> yLoc(nPnts + 1), Cl(nPnts + 1, 0.0), Cd(nPnts + 1, 0.0);
+    yLoc.assign(nPnts + 1, 0.0);
+    Cl.assign(nPnts + 1, 0.0);
+    Cd.assign(nPnts + 1, 0.0);
     yLoc[0] = W.yMin;
     yLoc[nPnts] = W.yMax;
     double step = (W.yMax - W.yMin) / nPnts;
@@ -1349,6 +1355,19 @@ void surfacePost(Mesh& M, const std::vector<double>& phi, V3 Vinf, const double 
 
 extern "C" {
 
+int cpo_spanwise(void* mp, int wake, double* y2b, double* cl, double* cdi) {
+    const Mesh& M = *(const Mesh*)mp;
+    if (wake < 0 || (size_t)wake >= M.span.size() || M.span[wake].empty()) return -1;
+    const std::vector<double>& sp = M.span[wake];
+    const size_t m = sp.size() / 3;
+    for (size_t i = 0; i < m; i++) {
+        y2b[i] = sp[i];
+        cl[i] = sp[m + i];
+        cdi[i] = sp[2 * m + i];
+    }
+    return (int)m;
+}
+
 int cpo_case_post(void* mp, const cpo_case_params* p, const double* mu_in, double* phi_out, double* vel_out,
                   double* cp_out, cpo_case_result* res) {
     Mesh& M = *(Mesh*)mp;
@@ -1374,11 +1393,18 @@ int cpo_case_post(void* mp, const cpo_case_params* p, const double* mu_in, doubl
     // trefftzPlaneAnalysis, cpCase.cpp:541-552
     WakeEval pot{M, wmu};
     double CL = 0, CD = 0;
-    for (const auto& W : M.wakes) {
+    M.span.assign(M.wakes.size(), {});
+    for (size_t w = 0; w < M.wakes.size(); w++) {
         double cl, cd;
-        trefftzPlane(M, W, pot, mu, p->V, p->Sref, cl, cd);
+        std::vector<double> y, Cl, Cd;
+        trefftzPlane(M, M.wakes[w], pot, mu, p->V, p->Sref, cl, cd, y, Cl, Cd);
         CL += cl / PG;
         CD += cd / std::pow(PG, 2);
+        // cpCase::writeSpanwiseData, CPanel/cpCase.cpp:915-917
+        std::vector<double>& sp = M.span[w];
+        for (double v : y) sp.push_back(2 * v / p->bref);
+        for (double v : Cl) sp.push_back(v / PG);
+        for (double v : Cd) sp.push_back(v / std::pow(PG, 2));
     }
     res->CL = CL;
     res->CDi = CD;

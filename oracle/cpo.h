@@ -80,6 +80,10 @@ typedef struct {
 int     cpo_case_run(void* m, const double* A, const double* B, const cpo_case_params* p,
                      double* sigma, double* mu, double* phi, double* vel, double* cp,
                      double* wake_mu, cpo_case_result* res, int nthreads);
+/* The spanwise Trefftz-plane loads of the last cpo_case_run / cpo_case_post on m, for live wake
+ * `wake`: 2y/b, Cl / PG and Cdi / PG^2 at the reference's 165 stations (cpCase::writeSpanwiseData,
+ * CPanel/cpCase.cpp:910-935; wake::trefftzPlane, wake.cpp:146-188).  Returns the station count or -1. */
+int     cpo_spanwise(void* m, int wake, double* y2b, double* cl, double* cdi);
 /* Post-processing only, from a given mu (used to isolate solver differences). */
 int     cpo_case_post(void* m, const cpo_case_params* p, const double* mu,
                       double* phi, double* vel, double* cp, cpo_case_result* res);

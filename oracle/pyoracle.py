@@ -52,6 +52,8 @@ def lib():
                                    C.POINTER(CaseResult), C.c_int]
         L.cpo_case_post.restype = C.c_int
         L.cpo_case_post.argtypes = [C.c_void_p, C.POINTER(CaseParams), D, D, D, D, C.POINTER(CaseResult)]
+        L.cpo_spanwise.restype = C.c_int
+        L.cpo_spanwise.argtypes = [C.c_void_p, C.c_int, D, D, D]
         L.cpo_bicgstab.restype = C.c_int
         L.cpo_bicgstab.argtypes = [D, C.c_int64, D, D, C.c_double, C.c_int64, I64, D, C.c_int]
         L.cpo_tri_dub_v_inf.argtypes = [D, D, D]
@@ -182,6 +184,15 @@ class Mesh:
         self.L.cpo_case_post(self.h, C.byref(p), _p(mu), _p(phi), _p(vel), _p(cp), C.byref(r))
         return dict(phi=phi, cp=cp, vel=vel, CL=r.CL, CDi=r.CDi, Fbody=np.array(r.Fbody[:]),
                     Fwind=np.array(r.Fwind[:]), CM=np.array(r.CM[:]))
+
+    def spanwise(self, wake=0):
+        """The last case's spanwise Trefftz loads of one wake (cpCase::writeSpanwiseData,
+        CPanel/cpCase.cpp:910-935): dict of y2b, cl, cdi at the 165 stations."""
+        out = {k: np.zeros(512) for k in ("y2b", "cl", "cdi")}
+        m = self.L.cpo_spanwise(self.h, wake, _p(out["y2b"]), _p(out["cl"]), _p(out["cdi"]))
+        if m < 0:
+            raise ValueError("no spanwise loads for wake %d" % wake)
+        return {k: v[:m].copy() for k, v in out.items()}
 
 
 def tri_phi_inf(verts9, poi):

@@ -13,9 +13,11 @@ Run in a container where the CPanel reference tree is mounted (default path
                    the file's points and connectivity.
   case4412AR6.npz -- Connor Cases/4412AR6 (Stability_Derivatives 1 in its .CPin): the mesh and the
                    .CPout numbers, the ten stability derivatives included (5 decimals).
+  case4412_spanwise.npz -- the 4412 case's V1_Mach0.1_alpha5_beta0/spanwiseData_Wake1.csv
+                   (cpCase::writeSpanwiseData): its lines as text and the 2y/b, Cl, Cdi columns.
 
 The generated files are small and committed; tests never read the reference tree.
-Usage: python make_golden.py [4412 | 4412wake | 4412AR6]  (default: all).
+Usage: python make_golden.py [4412 | 4412wake | 4412AR6 | 4412span | steadyTest]  (default: all).
 """
 import os
 import re
@@ -168,8 +170,20 @@ def main_steadytest():
     print("wrote steadyTest.npz", nodes.shape, tris.shape, cp, cpin, counts[-1])
 
 
+def main_4412span():
+    path = os.path.join(REF, "Connor Cases", "4412", "V1_Mach0.1_alpha5_beta0", "spanwiseData_Wake1.csv")
+    with open(path) as f:
+        lines = f.read().splitlines()
+    vals = np.array([[float(v) for v in ln.split(",")] for ln in lines[1:]])
+    np.savez_compressed(os.path.join(HERE, "case4412_spanwise.npz"), lines=np.array(lines),
+                        y2b=vals[:, 0], cl=vals[:, 1], cdi=vals[:, 2])
+    print("wrote case4412_spanwise.npz", vals.shape)
+
+
 def main():
-    which = sys.argv[1:] or ["4412", "4412wake", "4412AR6", "steadyTest"]
+    which = sys.argv[1:] or ["4412", "4412wake", "4412AR6", "4412span", "steadyTest"]
+    if "4412span" in which:
+        main_4412span()
     if "steadyTest" in which:
         main_steadytest()
     if "4412AR6" in which:

@@ -127,6 +127,34 @@ def test_4412_reference_case_on_gpu(cg, case4412):
     assert abs(case.getBodyForces()[2] - CN) <= 5.01e-6
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_4412_spanwise_loads_on_gpu(cg, case4412, precision, tmp_path):
+    """cpg_spanwise_loads on the reference's 4412 case: 2y/b, Cl and Cdi at the 165 Trefftz stations
+    within the 6 printed digits of the reference's spanwiseData_Wake1.csv (the mixed form with its
+    own error added, 1e-7 of each column's largest value), and CpCase.writeFiles' CSV from the plain
+    path equal to the reference's file line for line."""
+    from test_oracle_pin import spanwise_reference
+    gg = case4412
+    g = cg.Geometry(gg["nodes"], gg["tris"].astype(np.int64), gg["ids"])
+    case = cg.CpCase(g, float(gg["V"]), float(gg["alpha"]), float(gg["beta"]), float(gg["mach"]),
+                     Sref=float(gg["Sref"]), bref=float(gg["bref"]), cref=float(gg["cref"]), cg=tuple(gg["cg"]),
+                     precision=precision)
+    assert case.run()
+    ref = spanwise_reference()
+    assert len(case.span) == 1
+    slack = 1e-7 if precision == "mixed" else 0.0
+    for k in ("y2b", "cl", "cdi"):
+        ours = case.span[0][k]
+        assert len(ours) == 165
+        tol = 5e-6 * 1.02 * np.abs(ref[k]) + 1e-12 + slack * np.abs(ref[k]).max()
+        assert (np.abs(ours - ref[k]) <= tol).all(), k
+    if precision == "fp64":
+        case.writeFiles(str(tmp_path), geom_file="4412.tri")
+        sub = [d for d in os.listdir(tmp_path) if os.path.isdir(os.path.join(tmp_path, d))][0]
+        with open(os.path.join(tmp_path, sub, "spanwiseData_Wake1.csv")) as f:
+            assert f.read().splitlines() == list(ref["lines"])
+
+
 def test_4412_reference_case_mixed_on_gpu(cg, case4412):
     """The reference's own 4412 case (4,824 body panels) through the mixed path: the printed
     CL and CDi (5 decimals) as the plain path reproduces them."""

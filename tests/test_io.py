@@ -212,3 +212,22 @@ def test_case_write_files_on_host(built, case4412, solved4412, tmp_path):
     assert np.allclose(w["Doublet Strengths"], r["wake_mu"], rtol=1e-5, atol=1e-7)
     assert "CL = %.5f" % r["CL"] in open(cpout).read()
 
+
+
+def test_spanwise_csv_matches_reference_file(built, case4412, solved4412, tmp_path):
+    """cpg_write_spanwise_csv on the oracle's loads of the reference's 4412 case writes the reference's
+    own spanwiseData_Wake1.csv character for character (cpCase::writeSpanwiseData,
+    CPanel/cpCase.cpp:910-935); the fixture's parsed numbers print back to the same text."""
+    from cpanel_gb300 import io
+    from test_oracle_pin import spanwise_reference
+    g = case4412
+    m, A, B, r = solved4412
+    m.post(r["mu"], V=float(g["V"]), alpha=float(g["alpha"]), beta=float(g["beta"]), mach=float(g["mach"]),
+           Sref=float(g["Sref"]), bref=float(g["bref"]), cref=float(g["cref"]), cg=tuple(g["cg"]))
+    ref = spanwise_reference()
+    ours = tmp_path / "spanwiseData_Wake1.csv"
+    io.write_spanwise_csv(str(ours), m.spanwise(0))
+    assert ours.read_text().splitlines() == list(ref["lines"])
+    back = tmp_path / "fixture.csv"
+    io.write_spanwise_csv(str(back), {k: ref[k] for k in ("y2b", "cl", "cdi")})
+    assert back.read_text().splitlines() == list(ref["lines"])

@@ -6,6 +6,8 @@
   and moments from 4412.CPout (5 decimals), and per-panel doublet, source,
   potential, velocity and Cp from surfaceData-0.vtu (6 significant digits).
 """
+import os
+
 import numpy as np
 import pytest
 from scipy.linalg import lu_factor, lu_solve
@@ -107,3 +109,27 @@ def test_4412AR6_stability_derivatives_match_reference(case4412ar6, solved4412ar
     assert np.all(np.abs(da - g["d_alpha_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), da
     assert np.all(np.abs(db - g["d_beta_CL_CY_Cm_Cl_Cn"]) <= 5.01e-6), db
 
+
+
+def spanwise_reference():
+    """The reference's own spanwiseData_Wake1.csv of the 4412 case (tests/golden/make_golden.py)."""
+    return np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "case4412_spanwise.npz"))
+
+
+def within_printed(ours, ref):
+    """|ours - ref| within half a unit of ref's 6th significant digit (1e-12 covers printed zeros)."""
+    return np.abs(ours - ref) <= 5e-6 * 1.02 * np.abs(ref) + 1e-12
+
+
+def test_4412_spanwise_loads_match_reference_csv(solved4412, case4412):
+    """cpCase::writeSpanwiseData's columns (CPanel/cpCase.cpp:910-935: 2y/b, Cl / PG, Cdi / PG^2 at
+    wake::trefftzPlane's 165 stations) for the reference's 4412 case, within the 6 printed digits
+    of its spanwiseData_Wake1.csv."""
+    g = case4412
+    m, A, B, r = solved4412
+    m.post(r["mu"], V=float(g["V"]), alpha=float(g["alpha"]), beta=float(g["beta"]), mach=float(g["mach"]),
+           Sref=float(g["Sref"]), bref=float(g["bref"]), cref=float(g["cref"]), cg=tuple(g["cg"]))
+    sp, ref = m.spanwise(0), spanwise_reference()
+    for k in ("y2b", "cl", "cdi"):
+        assert len(sp[k]) == len(ref[k]) == 165
+        assert within_printed(sp[k], ref[k]).all(), k

@@ -343,6 +343,32 @@ def batched_and_served():
         "max_concurrent": max(r["info"]["running_at_start"] for r in res),
         "latency": "submit -> results on the host (steady: topology, uploads, assembly, LU, solves, post; "
                    "unsteady: buffer wake, matrices, LU, 100 steps)"}
+
+    # ---- the same stream's first steady requests served in each precision (config 5: against the plain
+    # FP64 GPU path): same arrival gaps, same slots
+    sub = [q for q in range(nreq) if reqs[q][0] == "steady"][:8]
+    comp = {}
+    for prec in ("mixed", "plain"):
+        srv = serve.Server(slots=4, budget_gb=160.0, precision=prec)
+        srv.wait(submit(srv, reqs[sub[0]]))  # warm-up
+        tickets = []
+        t0 = time.perf_counter()
+        for q in sub:
+            time.sleep(gaps[q])
+            tickets.append(submit(srv, reqs[q]))
+        res = [srv.wait(t) for t in tickets]
+        wall = time.perf_counter() - t0
+        srv.close()
+        lat = [r["info"]["total_ms"] for r in res]
+        comp[prec] = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                      "solves_per_s": sum(len(reqs[q][4]) for q in sub) / wall, "wall_s": wall}
+    nbs = [int(res_i["info"]["n_body"]) for res_i in res]
+    out["serving_vs_plain_fp64"] = {
+        "workload": "the served stream's first %d steady requests (%d-%d body panels, 4 alphas each) at the same "
+                    "arrival gaps, 4 slots, served once in each precision" % (len(sub), min(nbs), max(nbs)),
+        "mixed": comp["mixed"], "plain_fp64": comp["plain"],
+        "speedup_solves_per_s": comp["mixed"]["solves_per_s"] / comp["plain"]["solves_per_s"],
+        "p50_ratio_plain_over_mixed": comp["plain"]["p50_ms"] / comp["mixed"]["p50_ms"]}
     return out
 
 

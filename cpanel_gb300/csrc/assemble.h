@@ -138,8 +138,9 @@ struct LuGraphs {
     int solve_k = 0;
     cudaStream_t panel_stream = nullptr;  // high-priority stream of the diagonal-block factorizations
     cudaStream_t inv_stream = nullptr;    // and of the diagonal blocks' inverses beside them
+    cudaStream_t rest_stream = nullptr;   // and of the in-block updates beside the next diagonal step
     cudaEvent_t ev_update = nullptr, ev_panel = nullptr;  // fork / join between the streams
-    cudaEvent_t ev_diag = nullptr, ev_inv = nullptr;
+    cudaEvent_t ev_diag = nullptr, ev_inv = nullptr, ev_solve = nullptr, ev_rest = nullptr;
     float* dinv = nullptr;      // inverses of the 128-column diagonal blocks (L then U per block)
     float* tmp = nullptr;       // n x k intermediate of the substitutions
     size_t tmp_floats = 0;

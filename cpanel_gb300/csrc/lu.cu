@@ -82,6 +82,10 @@ __device__ __forceinline__ void uinv_step(const float (&r)[32], float (&y)[32], 
     if constexpr (k > 0) uinv_step<k - 1>(r, y, lane);
 }
 
+// PRE: before factoring, the block takes the update of the 128-column step before it,
+// A_KK -= L(K.., K-NB..K) U(K-NB..K, K..): the caller's update of the rest of the trailing matrix
+// then skips this block, and this kernel is the only launch between two diagonal steps.
+template <bool PRE>
 __device__ __forceinline__ void lu_diag_body(float* sm, float* __restrict__ A, int64_t n, int64_t K, int b,
                                              float* __restrict__ Dinv, int* bad) {
     float* S = sm;                 // S[r*P + c]
@@ -100,6 +104,54 @@ __device__ __forceinline__ void lu_diag_body(float* sm, float* __restrict__ A, i
         for (int q = 0; q < NB * NB / DT; q++) {
             const int idx = t + q * DT, c = idx / NB, r = idx % NB;
             S[r * P + c] = v[q];
+            if constexpr (!PRE) {
+                ZL[r * P + c] = r == c ? 1.f : 0.f;
+                ZU[r * P + c] = r == c ? 1.f : 0.f;
+            }
+        }
+    }
+    if constexpr (PRE) {
+        // the previous step's L rows of this block (into ZL) and U columns of it (into ZU), zero
+        // outside the block's b rows and columns
+        float vl[NB * NB / DT], vu[NB * NB / DT];
+#pragma unroll
+        for (int q = 0; q < NB * NB / DT; q++) {
+            const int idx = t + q * DT, c = idx / NB, r = idx % NB;
+            vl[q] = r < b ? A[(K - NB + c) * n + K + r] : 0.f;
+            vu[q] = c < b ? A[(K + c) * n + K - NB + r] : 0.f;
+        }
+#pragma unroll
+        for (int q = 0; q < NB * NB / DT; q++) {
+            const int idx = t + q * DT, c = idx / NB, r = idx % NB;
+            ZL[r * P + c] = vl[q];
+            ZU[r * P + c] = vu[q];
+        }
+        __syncthreads();
+        // S -= ZL ZU: thread t takes rows 4 (t / 16) .. + 3 and columns t % 16 + 16 x (x < 8)
+        const int tr = t / 16, tc = t % 16;
+        float acc[4][8];
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int x = 0; x < 8; x++) acc[i][x] = 0.f;
+        for (int k = 0; k < NB; k++) {
+            float a[4], u[8];
+#pragma unroll
+            for (int i = 0; i < 4; i++) a[i] = ZL[(4 * tr + i) * P + k];
+#pragma unroll
+            for (int x = 0; x < 8; x++) u[x] = ZU[k * P + tc + 16 * x];
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int x = 0; x < 8; x++) acc[i][x] = __fmaf_rn(a[i], u[x], acc[i][x]);
+        }
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int x = 0; x < 8; x++) S[(4 * tr + i) * P + tc + 16 * x] -= acc[i][x];
+        __syncthreads();
+        for (int idx = t; idx < NB * NB; idx += DT) {
+            const int c = idx / NB, r = idx % NB;
             ZL[r * P + c] = r == c ? 1.f : 0.f;
             ZU[r * P + c] = r == c ? 1.f : 0.f;
         }
@@ -273,10 +325,11 @@ __device__ __forceinline__ void lu_diag_body(float* sm, float* __restrict__ A, i
     }
 }
 
+template <bool PRE>
 __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n, int64_t K, int b,
                                                 float* __restrict__ Dinv, int* bad) {
     extern __shared__ float sm[];
-    lu_diag_body(sm, A, n, K, b, Dinv, bad);
+    lu_diag_body<PRE>(sm, A, n, K, b, Dinv, bad);
 }
 
 // ---- block steps of the factorization, shared by the single-matrix and the lockstep kernels ----
@@ -497,9 +550,10 @@ __global__ void __launch_bounds__(256) k_colrow_solve(float* __restrict__ A, int
         row_solve_body(A, n, dinv, cb + ((int64_t)blockIdx.x - nrt) * RS_C, ce, K, b, dsm);
 }
 // single matrix: the update of rows [rb, re) x columns [cb, ce) by block K, one 128 x 64 tile
-// per thread block
+// per thread block, except the 128 x 128 block at (rb, cb), which the next diagonal kernel updates
 __global__ void __launch_bounds__(128) k_gemm_sub(float* __restrict__ A, int64_t n, int64_t rb, int64_t re,
                                                   int64_t cb, int64_t ce, int64_t K, int b) {
+    if (blockIdx.x == 0 && blockIdx.y < NB / GS_C) return;
     gemm_sub_body(A, n, rb + (int64_t)blockIdx.x * GS_R, re, cb + (int64_t)blockIdx.y * GS_C, ce, K, b);
 }
 
@@ -513,7 +567,7 @@ __global__ void __launch_bounds__(DT) k_lu_diag_batched(const cpg::LuBatchMesh* 
     extern __shared__ float sm[];
     const int* it = items + LB_ITEM * blockIdx.x;
     const cpg::LuBatchMesh d = ms[it[0]];
-    lu_diag_body(sm, d.LU, d.n, it[5], it[6], d.dinv, d.bad);
+    lu_diag_body<false>(sm, d.LU, d.n, it[5], it[6], d.dinv, d.bad);
 }
 __global__ void __launch_bounds__(256) k_col_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
                                                            const int* __restrict__ items) {
@@ -823,7 +877,8 @@ void set_attrs() {
     cudaGetDevice(&dev);
     std::call_once(once[dev & 63],
                    [] {
-                       cudaFuncSetAttribute(k_lu_diag, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
+                       cudaFuncSetAttribute(k_lu_diag<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
+                       cudaFuncSetAttribute(k_lu_diag<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
                        cudaFuncSetAttribute(k_lu_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             DIAG_SMEM);
                        cudaFuncSetAttribute(k_skinny<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -886,14 +941,20 @@ constexpr int64_t kInvScratch = 4 * (SB / 64) * 8192;  // tile scratch of k_inv_
 
 // factorization of the diagonal block [KO, KE) x [KO, KE) in place on s (the updates of the
 // earlier panels applied), the inverses of its 128-column blocks into G->dinv; for a full SB
-// block also its combined inverses into G->dinv4 on G->inv_stream, joined back into s at the end
+// block also its combined inverses into G->dinv4 on G->inv_stream, joined back into s at the end.
+// Look-ahead inside the block: step j's column and row solves, then the next diagonal kernel on s,
+// which first applies step j's update to its own block; step j's update of the rest of the block
+// runs on G->rest_stream beside it, and step j + 1's solves wait for it.
 cudaError_t factor_diag_block(LuGraphs* G, float* LU, int64_t n, int* bad, int64_t KO, int64_t KE, cudaStream_t s) {
     cudaError_t e;
     const bool inv = KE - KO == SB;
     float* D4 = inv ? G->dinv4 + (KO / SB) * 2 * SB * SB : nullptr;
     for (int64_t K = KO; K < KE; K += NB) {
         const int b = (int)std::min<int64_t>(NB, KE - K);
-        k_lu_diag<<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, G->dinv, bad);
+        if (K == KO)
+            k_lu_diag<false><<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, G->dinv, bad);
+        else
+            k_lu_diag<true><<<1, DT, DIAG_SMEM, s>>>(LU, n, K, b, G->dinv, bad);
         if (inv) {
             const int j = (int)((K - KO) / NB);
             if ((e = cudaEventRecord(G->ev_diag, s)) != cudaSuccess) return e;
@@ -902,10 +963,18 @@ cudaError_t factor_diag_block(LuGraphs* G, float* LU, int64_t n, int* bad, int64
         }
         const int64_t K1 = K + b, rest = KE - K1;
         if (rest <= 0) break;
+        if (K > KO) {  // the previous step's update of the rest of the block
+            if ((e = cudaStreamWaitEvent(s, G->ev_rest, 0)) != cudaSuccess) return e;
+        }
         const unsigned g = (unsigned)((rest + CS_R - 1) / CS_R + (rest + RS_C - 1) / RS_C);
         k_colrow_solve<<<g, 256, CR_SMEM, s>>>(LU, n, G->dinv, K1, KE, K1, KE, K, b);
-        dim3 gg((unsigned)((rest + GS_R - 1) / GS_R), (unsigned)((rest + GS_C - 1) / GS_C));
-        k_gemm_sub<<<gg, 128, 0, s>>>(LU, n, K1, KE, K1, KE, K, b);
+        if (rest > NB) {  // beyond the next diagonal block
+            if ((e = cudaEventRecord(G->ev_solve, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(G->rest_stream, G->ev_solve, 0)) != cudaSuccess) return e;
+            dim3 gg((unsigned)((rest + GS_R - 1) / GS_R), (unsigned)((rest + GS_C - 1) / GS_C));
+            k_gemm_sub<<<gg, 128, 0, G->rest_stream>>>(LU, n, K1, KE, K1, KE, K, b);
+            if ((e = cudaEventRecord(G->ev_rest, G->rest_stream)) != cudaSuccess) return e;
+        }
     }
     if (inv) {
         if ((e = cudaEventRecord(G->ev_inv, G->inv_stream)) != cudaSuccess) return e;
@@ -1053,10 +1122,11 @@ void LuGraphs::release() {
     if (solve) cudaGraphExecDestroy(solve);
     if (panel_stream) cudaStreamDestroy(panel_stream);
     if (inv_stream) cudaStreamDestroy(inv_stream);
-    for (cudaEvent_t ev : {ev_update, ev_panel, ev_diag, ev_inv})
+    if (rest_stream) cudaStreamDestroy(rest_stream);
+    for (cudaEvent_t ev : {ev_update, ev_panel, ev_diag, ev_inv, ev_solve, ev_rest})
         if (ev) cudaEventDestroy(ev);
-    panel_stream = inv_stream = nullptr;
-    ev_update = ev_panel = ev_diag = ev_inv = nullptr;
+    panel_stream = inv_stream = rest_stream = nullptr;
+    ev_update = ev_panel = ev_diag = ev_inv = ev_solve = ev_rest = nullptr;
     if (dinv) cudaFree(dinv);
     if (tmp) cudaFree(tmp);
     if (dinv4) cudaFree(dinv4);
@@ -1120,7 +1190,9 @@ cudaError_t lu_factor_fp32(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStre
             return e;
         if ((e = cudaStreamCreateWithPriority(&G->inv_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
             return e;
-        for (cudaEvent_t* ev : {&G->ev_update, &G->ev_panel, &G->ev_diag, &G->ev_inv})
+        if ((e = cudaStreamCreateWithPriority(&G->rest_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
+            return e;
+        for (cudaEvent_t* ev : {&G->ev_update, &G->ev_panel, &G->ev_diag, &G->ev_inv, &G->ev_solve, &G->ev_rest})
             if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return e;
     }
     ProfScope ps(Prof::LU_FACTOR, s);

@@ -589,7 +589,8 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
         CK(g->rb.ensure(sizeof(double) * (3 * n + cpg::mixed_rb_part_doubles(n, g->H.n_wake))), "alloc rhs basis");
         if (g->order_n != n) {  // block schedule, once per geometry
             std::vector<int> ord;
-            cpg::mixed_block_order(n, ord);
+            cpg::mixed_block_order(n, g->H.body.data() + cpg::PF_C, cpg::PF_STRIDE, g->H.body.data() + cpg::PF_LONG,
+                                   cpg::PF_STRIDE, ord);
             CK(upload(g->order, ord, s), "upload block order");
             g->order_n = n;
         }

@@ -581,9 +581,11 @@ __global__ void __launch_bounds__(PV_T) k_panels_velocity(const double* __restri
 }
 
 int64_t chunk_for(int64_t n) {
-    // enough blocks in y to fill the 152 SMs several times over
+    // short source chunks (96 on the 19k wing): the FP64 near field concentrates in the few blocks
+    // whose targets and sources are neighbours, and one such block of 128 x 1,152 pairs had run for
+    // the whole kernel (27.8 of 28.5 ms, the SMs 52% occupied); 128 x 96 blocks spread it out
     int64_t bx = (n + TI - 1) / TI;
-    int64_t want = 152 * 16;
+    int64_t want = 152 * 256;
     int64_t by = (want + bx - 1) / bx;
     if (by < 1) by = 1;
     int64_t ch = (n + by - 1) / by;
@@ -632,14 +634,44 @@ cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wre
     return cudaGetLastError();
 }
 
-void mixed_block_order(int64_t n, std::vector<int>& out) {
+void mixed_block_order(int64_t n, const double* cent, int64_t cstride, const double* longside, int64_t lstride,
+                       std::vector<int>& out) {
     const int64_t ch = chunk_for(n);
-    const int64_t nbx = (n + TI - 1) / TI, nby = (n + ch - 1) / ch;
-    std::vector<std::pair<int64_t, int64_t>> key;  // (distance of the index ranges' centres, block)
+    const int64_t nbx = (n + TI - 1) / TI, nby = (n + ch - 1) / ch, ntj = (n + TJ - 1) / TJ;
+    // bounding boxes of the row blocks' and the source tiles' centroids, the tiles' longest side
+    std::vector<double> rb(6 * nbx), sb(6 * ntj), sl(ntj, 0.0);
+    auto box = [&](int64_t i0, int64_t i1, double* b) {
+        for (int d = 0; d < 3; d++) b[d] = 1e300, b[3 + d] = -1e300;
+        for (int64_t i = i0; i < i1; i++)
+            for (int d = 0; d < 3; d++) {
+                const double v = cent[i * cstride + d];
+                b[d] = std::min(b[d], v);
+                b[3 + d] = std::max(b[3 + d], v);
+            }
+    };
+    for (int64_t bx = 0; bx < nbx; bx++) box(bx * TI, std::min(n, (bx + 1) * TI), &rb[6 * bx]);
+    for (int64_t t = 0; t < ntj; t++) {
+        box(t * TJ, std::min(n, (t + 1) * TJ), &sb[6 * t]);
+        for (int64_t j = t * TJ; j < std::min(n, (t + 1) * TJ); j++) sl[t] = std::max(sl[t], longside[j * lstride]);
+    }
+    // a block's cost: per source tile of its chunk, 64 when the boxes come within 3 long sides (FP64
+    // near pairs, run at 1/64 of the FP32 rate), 8 within 5 (the double-float band), else 1
+    std::vector<std::pair<int64_t, int64_t>> key;  // (-cost, block): costliest first
+    key.reserve(nbx * nby);
     for (int64_t by = 0; by < nby; by++)
         for (int64_t bx = 0; bx < nbx; bx++) {
-            int64_t rc = bx * TI + TI / 2, cc = by * ch + ch / 2;
-            key.push_back({rc > cc ? rc - cc : cc - rc, by * nbx + bx});
+            int64_t cost = 0;
+            const double* r = &rb[6 * bx];
+            for (int64_t t = by * ch / TJ; t < std::min(ntj, (by + 1) * ch / TJ); t++) {
+                const double* q = &sb[6 * t];
+                double d2 = 0;
+                for (int d = 0; d < 3; d++) {
+                    const double gap = std::max(0.0, std::max(q[d] - r[3 + d], r[d] - q[3 + d]));
+                    d2 += gap * gap;
+                }
+                cost += d2 < 9 * sl[t] * sl[t] ? 64 : d2 < 25 * sl[t] * sl[t] ? 8 : 1;
+            }
+            key.push_back({-cost, by * nbx + bx});
         }
     std::sort(key.begin(), key.end());
     out.resize(2 * key.size());

@@ -43,7 +43,8 @@ struct ProfScope {
 cudaError_t launch_assemble_fp64(const double* rec, int64_t n, const double* wrec, const int32_t* widx,
                                  const double* wcoef, int64_t nw, double* A, double* B,
                                  unsigned long long* near_count, cudaStream_t s);
-// order: mixed_block_order(n) on the device (2 ints per block: row block, source chunk);
+// order: mixed_block_order's blocks on the device (2 ints per block: row block, source chunk;
+// the costliest first);
 // erec: per-panel FP64 edge constants of the near field (E_STRIDE doubles per body panel:
 // |s_k|, 1/|s_k|, s_k.m with s_k = v_{k+1} - v_k, rounded as the device rounds them)
 cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const double* erec, int64_t n,
@@ -52,7 +53,9 @@ cudaError_t launch_assemble_mixed(const double* rec, const float* frec, const do
                                   unsigned long long* near_count, cudaStream_t s);
 // block schedule of the mixed assembly: blocks sorted by the distance between their row
 // and source index ranges (near-field-heavy blocks first)
-void mixed_block_order(int64_t n, std::vector<int>& out);
+// cent: target/source centroids (3 doubles, stride cstride), longside (stride lstride), matrix order
+void mixed_block_order(int64_t n, const double* cent, int64_t cstride, const double* longside, int64_t lstride,
+                       std::vector<int>& out);
 
 // Grouped mixed assembly of many meshes in one persistent launch.  One descriptor per
 // mesh (device copy); row0 = first row of the mesh in the group's flattened rows, the

@@ -203,7 +203,10 @@ int64_t cpg_server_footprint(int64_t n, int k, int precision) {
     // diagonal-block inverses, split tensor-core operands and scratch (lu_factor_bytes), with a
     // fixed margin
     const int64_t nn = n * n;
-    int64_t mats = precision == CPG_PLAIN_FP64 ? 16 * nn : 12 * nn + (int64_t)cpg::lu_factor_bytes(n);
+    // (mixed: also the assembly's per-chunk partial sums of the right-hand-side basis)
+    int64_t mats = precision == CPG_PLAIN_FP64
+                       ? 16 * nn
+                       : 12 * nn + (int64_t)cpg::lu_factor_bytes(n) + 8 * (3 * n + cpg::mixed_rb_part_doubles(n, 0));
     return mats + (int64_t)n * (int64_t)(2000 + 64 * k) + ((int64_t)64 << 20);
 }
 

@@ -46,6 +46,9 @@ struct cpg_ctx {
         cudaEvent_t ev;
     };
     std::vector<Spare> spare;
+    // the FP32 factorization state (inverses, split operands, scratch, streams, events) of the last
+    // destroyed geometry, taken over by the next geometry's mixed solve instead of allocated again
+    cpg::LuGraphs* lu_pool = nullptr;
 };
 
 namespace {
@@ -357,6 +360,10 @@ void cpg_destroy(cpg_ctx* c) {
     delete c->prof;
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     if (c->aux) cudaStreamDestroy(c->aux);
+    if (c->lu_pool) {
+        c->lu_pool->release();
+        delete c->lu_pool;
+    }
     delete c;
 }
 
@@ -479,6 +486,11 @@ void cpg_geometry_destroy(cpg_geometry* g) {
                       &g->order, &g->erec};
     // cudaFree synchronizes with outstanding work; the context may already be gone
     for (DevBuf* b : bufs) b->release();
+    cpg_ctx* c = g->ctx;
+    if (c && g->graphs.dinv && !c->lu_pool) {  // kept for the context's next geometry
+        c->lu_pool = new (std::nothrow) cpg::LuGraphs(g->graphs);
+        if (c->lu_pool) g->graphs = cpg::LuGraphs();
+    }
     g->graphs.release();
     if (g->post_ev) cudaEventDestroy(g->post_ev);
     delete g;
@@ -663,7 +675,10 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
     if ((precision == CPG_PLAIN_FP64 && !g->have64) || (precision == CPG_MIXED && !g->have32))
         if ((rc = cpg_set_inf_coeff(g, precision)) != CPG_OK) return rc;
     float ms_asm = g->ms_asm;
-    if ((rc = prepare_post(g)) != CPG_OK) return rc;
+    // the post tables (CHTLS weights, Trefftz operator) of a new geometry go on the aux stream: in the
+    // plain path beside the solve; in the mixed path after the factorization, beside the refinement,
+    // where they do not take SMs from the factorization's serial diagonal-block chain
+    if (precision == CPG_PLAIN_FP64 && (rc = prepare_post(g)) != CPG_OK) return rc;
     std::vector<cpg::CaseScalars> cs(k);
     for (int c = 0; c < k; c++) case_scalars(flows[c], *refs, cs[c]);
     CK(upload(g->cases, cs, s), "upload cases");
@@ -696,6 +711,11 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
         CK(cpg::solve_fp64(g->A64.as<double>(), n, k, rhs, mu, g->work.p, 2.220446049250313e-16, 2 * n, &st, s),
            "BiCGSTAB (FP64)");
     } else {
+        if (!g->lu_ready && !g->graphs.dinv && ctx->lu_pool) {  // a destroyed geometry's factorization state
+            g->graphs = *ctx->lu_pool;
+            delete ctx->lu_pool;
+            ctx->lu_pool = nullptr;
+        }
         if (!g->lu_ready) {  // per-geometry factorization, reused by every case
             CK(ensure_big(g->ctx, g->LU, sizeof(float) * (size_t)n * n), "alloc LU");
             CK(g->bad.ensure(sizeof(int)), "alloc flag");
@@ -705,6 +725,7 @@ int cpg_solve_cases(cpg_geometry* g, const cpg_flow* flows, int k, const cpg_ref
                "LU factorization");
             g->lu_ready = true;
         }
+        if ((rc = prepare_post(g)) != CPG_OK) return rc;
         size_t wb = cpg::solve_lu_work_bytes(n, k);
         CK(g->work.ensure(wb), "alloc solver workspace");
         CK(cpg::launch_rhs_basis(g->rb.as<double>(), n, k, dcs, rhs, s), "rhs");

@@ -656,8 +656,8 @@ void mixed_block_order(int64_t n, const double* cent, int64_t cstride, const dou
     }
     // a block's cost: per source tile of its chunk, 64 when the boxes come within 3 long sides (FP64
     // near pairs, run at 1/64 of the FP32 rate), 8 within 5 (the double-float band), else 1
-    std::vector<std::pair<int64_t, int64_t>> key;  // (-cost, block): costliest first
-    key.reserve(nbx * nby);
+    std::vector<int32_t> cost_of(nbx * nby);
+    int32_t cmax = 0;
     for (int64_t by = 0; by < nby; by++)
         for (int64_t bx = 0; bx < nbx; bx++) {
             int64_t cost = 0;
@@ -671,9 +671,15 @@ void mixed_block_order(int64_t n, const double* cent, int64_t cstride, const dou
                 }
                 cost += d2 < 9 * sl[t] * sl[t] ? 64 : d2 < 25 * sl[t] * sl[t] ? 8 : 1;
             }
-            key.push_back({-cost, by * nbx + bx});
+            cost_of[by * nbx + bx] = (int32_t)cost;
+            cmax = std::max(cmax, (int32_t)cost);
         }
-    std::sort(key.begin(), key.end());
+    // costliest first, blocks of equal cost in index order (a counting sort over the small integer costs)
+    std::vector<int64_t> start(cmax + 2, 0);
+    for (int32_t c : cost_of) start[cmax - c + 1]++;
+    for (int32_t c = 1; c <= cmax + 1; c++) start[c] += start[c - 1];
+    std::vector<std::pair<int64_t, int64_t>> key(cost_of.size());
+    for (int64_t blk = 0; blk < (int64_t)cost_of.size(); blk++) key[start[cmax - cost_of[blk]]++] = {-cost_of[blk], blk};
     out.resize(2 * key.size());
     for (size_t b = 0; b < key.size(); b++) {
         out[2 * b] = (int)(key[b].second % nbx);

@@ -64,7 +64,7 @@ EXPORTS = ["cpg_create", "cpg_destroy", "cpg_last_error", "cpg_set_stream", "cpg
            "cpg_geometry_create", "cpg_geometry_destroy", "cpg_geometry_info_get", "cpg_geometry_tables", "cpg_topology",
            "cpg_set_inf_coeff", "cpg_get_A", "cpg_get_B", "cpg_solve_cases", "cpg_panel_phi_inf",
            "cpg_dub_phi_inf", "cpg_panel_v_inf", "cpg_compiled_arch", "cpg_prof_enable", "cpg_prof_read",
-           "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_gemm_f32_tc", "cpg_release_spares", "cpg_stability_derivatives",
+           "cpg_set_inf_coeff_noalloc", "cpg_measure_fp64_peak", "cpg_gemm_f32_tc", "cpg_lu_solve_f32", "cpg_release_spares", "cpg_stability_derivatives",
            "cpg_volume_velocity", "cpg_topology_wake_tris", "cpg_streamlines", "cpg_streamlines_field",
            "cpg_trefftz_wakes", "cpg_spanwise_loads",
            # cpanel_vp.h
@@ -201,6 +201,7 @@ def load():
     L.cpg_measure_fp64_peak.argtypes = [vp, D]
     L.cpg_gemm_f32_tc.argtypes = [vp, C.c_int64, C.c_int64, C.c_int64, C.c_float, vp, C.c_int64, vp, C.c_int64,
                                   C.c_float, vp, C.c_int64, C.c_int]
+    L.cpg_lu_solve_f32.argtypes = [vp, C.c_int64, vp, C.c_int64, vp]
     L.cpg_release_spares.argtypes = [vp]
     L.cpg_stability_derivatives.argtypes = [vp, C.POINTER(Flow), C.POINTER(Refs), C.c_int, C.POINTER(CaseOut),
                                             C.POINTER(Stability)]

@@ -1736,6 +1736,38 @@ int solve_cases_grouped(cpg_geometry* const* gs, int m, const cpg_flow* const* f
 
 }  // namespace cpg
 
+// ---- C ABI: the FP32 LU and its block substitutions on caller-owned device matrices ----
+extern "C" int cpg_lu_solve_f32(cpg_ctx* ctx, int64_t n, float* A, int64_t k, float* X) {
+    if (!ctx || n < 0 || k < 0 || k > INT32_MAX || (n > 0 && (!A || (k > 0 && !X)))) return CPG_E_INVALID;
+    if (n == 0) return CPG_OK;
+    ProfInstall pi(ctx);
+    cudaStream_t s = ctx->stream;
+    cpg::LuGraphs G;
+    int* bad = nullptr;
+    int hbad = 0;
+    cudaError_t e = cudaMalloc(&bad, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(int), s);
+    if (e == cudaSuccess) e = cpg::lu_factor_fp32(&G, A, n, bad, s);
+    if (e == cudaSuccess && k > 0) e = cpg::lu_solve_fp32(&G, A, n, X, (int)k, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    G.release();
+    if (bad) cudaFree(bad);
+    if (e != cudaSuccess) {
+        cpg::ctx_set_error(ctx, std::string("lu: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? CPG_E_OOM : CPG_E_CUDA;
+    }
+    if (hbad == 2) {
+        cpg::ctx_set_error(ctx, "lu: non-finite entry");
+        return CPG_E_INVALID;
+    }
+    if (hbad != 0) {
+        cpg::ctx_set_error(ctx, "lu: zero pivot, or a wait of a tensor-core product ran out");
+        return CPG_E_INVALID;
+    }
+    return CPG_OK;
+}
+
 // ---- C ABI: the tensor-core GEMM on caller-owned FP32 device matrices ----
 extern "C" int cpg_gemm_f32_tc(cpg_ctx* ctx, int64_t m, int64_t n, int64_t k, float alpha, const float* A,
                                int64_t lda, const float* B, int64_t ldb, float beta, float* C, int64_t ldc,

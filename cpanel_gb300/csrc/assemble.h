@@ -153,6 +153,8 @@ struct LuGraphs {
     int64_t super_cap = 0;      // 1,024-column blocks dinv4 holds
     void* tc_mem = nullptr;     // split FP16 operands of the tensor-core products
     size_t tc_bytes = 0;
+    float* split_ws = nullptr;      // partials of the split-K substitution products
+    unsigned* split_cnt = nullptr;  // and their per-tile arrival counters
     void release();
 };
 cudaError_t lu_factor_fp32(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_t s);

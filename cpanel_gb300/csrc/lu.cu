@@ -657,29 +657,45 @@ __global__ void __launch_bounds__(128) k_inv_step(const float* __restrict__ LU, 
 
 // ---- skinny products of the block substitutions: C (m x kc) = alpha A (m x K) B (K x kc)
 // (+ C when accum), all column-major, kc small.  256 threads per 32 RH rows x KC columns: lane =
-// row, warp w takes rows 32 (w % RH) .. and the SK_CH / KG K indices (KG = 8 / RH) of group w / RH
-// in every SK_CH-long chunk of B, which is staged in shared memory column by column (coalesced,
+// row, warp w takes rows 32 (w % RH) .. and a 32-aligned share of every SK_CH-long chunk of B
+// (group w / RH of KG = 8 / RH), which is staged in shared memory column by column (coalesced,
 // conflict-free) and read back as float4 broadcasts of four consecutive K indices.  32 loads of
 // A in flight per thread, each element of A read once (coalesced along the rows) and used KC
 // times; the K groups' partial sums are added in a fixed order.  RH = 2 halves the staging of B
 // per row for tall products.
+// Split K (gridDim.z > 1): thread block z takes K indices [z kseg, (z + 1) kseg) and writes its
+// ROWS x KC partial to ws; the last of a tile's blocks to arrive (counter cnt[tile], which it
+// returns to 0) adds the gridDim.z partials in z order and updates C, so the result does not
+// depend on the order the blocks ran in.
 constexpr int SK_CH = 512;
 template <int KC, int RH>
 __global__ void __launch_bounds__(256) k_skinny(const float* __restrict__ A, int64_t lda, const float* __restrict__ B,
                                                 int64_t ldb, float* __restrict__ C, int64_t ldc, int64_t m,
-                                                int64_t K, int kc, float alpha, int accum) {
-    constexpr int KG = 8 / RH, KW = SK_CH / KG, ROWS = 32 * RH;
+                                                int64_t K, int kc, float alpha, int accum, int64_t kseg,
+                                                float* __restrict__ ws, unsigned* __restrict__ cnt) {
+    constexpr int KG = 8 / RH, ROWS = 32 * RH;
     extern __shared__ __align__(16) float dsm[];
+    __shared__ int s_last;
     float* Bs = dsm;  // [KC][SK_CH]
     const int t = threadIdx.x, lane = t & 31, w = t >> 5, rh = w % RH, kg = w / RH;
     const int64_t r = (int64_t)blockIdx.x * ROWS + 32 * rh + lane;
-    const int c0 = blockIdx.y * KC, kb = KW * kg;
+    const int c0 = blockIdx.y * KC;
+    const int64_t kz0 = (int64_t)blockIdx.z * kseg, kz1 = kz0 + kseg < K ? kz0 + kseg : K;
     float acc[KC];
 #pragma unroll
     for (int c = 0; c < KC; c++) acc[c] = 0.f;
-    for (int64_t k0 = 0; k0 < K; k0 += SK_CH) {
-        const int kch = (int)(K - k0 < SK_CH ? K - k0 : SK_CH);
+    for (int64_t k0 = kz0; k0 < kz1; k0 += SK_CH) {
+        const int kch = (int)(kz1 - k0 < SK_CH ? kz1 - k0 : SK_CH);
         const int kst = (kch + 31) & ~31;  // staged length: the compute reads whole groups of 32
+        const int kw = ((kch + 32 * KG - 1) / (32 * KG)) * 32, kb = kw * kg;
+        float a[32];
+        auto load_a = [&](int h) {
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int kk = kb + h + j;
+                a[j] = (r < m && kk < kch) ? A[(k0 + kk) * lda + r] : 0.f;
+            }
+        };
         __syncthreads();
         {  // every load of this thread in flight together, then the stores
             constexpr int PER = SK_CH * KC / 256;
@@ -697,13 +713,8 @@ __global__ void __launch_bounds__(256) k_skinny(const float* __restrict__ A, int
         }
         __syncthreads();
         if (r < m) {
-            for (int h = 0; h < KW && kb + h < kch; h += 32) {
-                float a[32];
-#pragma unroll
-                for (int j = 0; j < 32; j++) {
-                    const int kk = kb + h + j;
-                    a[j] = kk < kch ? A[(k0 + kk) * lda + r] : 0.f;
-                }
+            for (int h = 0; h < kw && kb + h < kch; h += 32) {
+                load_a(h);
 #pragma unroll
                 for (int j = 0; j < 32; j += 4) {
 #pragma unroll
@@ -723,13 +734,37 @@ __global__ void __launch_bounds__(256) k_skinny(const float* __restrict__ A, int
 #pragma unroll
     for (int c = 0; c < KC; c++) red[(kg * ROWS + 32 * rh + lane) * (KC + 1) + c] = acc[c];
     __syncthreads();
+    const int nz = (int)gridDim.z;
+    const int64_t tile = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+    if (nz > 1) {
+        float* part = ws + (tile * nz + blockIdx.z) * (ROWS * KC);
+        for (int idx = t; idx < ROWS * KC; idx += 256) {
+            const int rl = idx % ROWS, c = idx / ROWS;
+            float s = 0.f;
+#pragma unroll
+            for (int q = 0; q < KG; q++) s += red[(q * ROWS + rl) * (KC + 1) + c];
+            part[idx] = s;
+        }
+        __threadfence();
+        __syncthreads();
+        if (t == 0) s_last = atomicAdd(cnt + tile, 1u) == (unsigned)(nz - 1);
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        if (t == 0) cnt[tile] = 0u;
+    }
     for (int idx = t; idx < ROWS * KC; idx += 256) {
         const int rl = idx % ROWS, c = idx / ROWS;
         const int64_t rr = (int64_t)blockIdx.x * ROWS + rl;
         if (rr >= m || c0 + c >= kc) continue;
         float s = 0.f;
+        if (nz > 1) {
+            const float* part = ws + tile * nz * (ROWS * KC) + idx;
+            for (int z = 0; z < nz; z++) s += __ldcg(part + z * (ROWS * KC));
+        } else {
 #pragma unroll
-        for (int q = 0; q < KG; q++) s += red[(q * ROWS + rl) * (KC + 1) + c];
+            for (int q = 0; q < KG; q++) s += red[(q * ROWS + rl) * (KC + 1) + c];
+        }
         float* p = C + (int64_t)(c0 + c) * ldc + rr;
         *p = accum ? *p + alpha * s : alpha * s;
     }
@@ -881,6 +916,11 @@ void set_attrs() {
                        cudaFuncSetAttribute(k_lu_diag<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
                        cudaFuncSetAttribute(k_lu_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             DIAG_SMEM);
+                       // 48 KB and more of dynamic shared memory, beside the kernel's static flag
+                       cudaFuncSetAttribute(k_skinny<24, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            skinny_smem<24>());
+                       cudaFuncSetAttribute(k_skinny<24, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            skinny_smem<24>());
                        cudaFuncSetAttribute(k_skinny<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             skinny_smem<32>());
                        cudaFuncSetAttribute(k_skinny<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -888,32 +928,55 @@ void set_attrs() {
                    });
 }
 
-// C (m x kc) = alpha A (m x K) B (K x kc) (+ C when accum), column-major
+// Scratch of the split-K skinny products: partials and per-tile arrival counters (zero between
+// launches).  A split launch has fewer than kSkinnyTarget tiles and at most that many thread
+// blocks, which bounds both.
+struct SkinnySplit {
+    float* ws = nullptr;
+    unsigned* cnt = nullptr;
+};
+constexpr int kSkinnyTarget = 2 * 152;  // thread blocks a split launch aims at (two resident per SM)
+constexpr size_t kSkinnyWsFloats = (size_t)2 * kSkinnyTarget * 64 * 32;
+
+// C (m x kc) = alpha A (m x K) B (K x kc) (+ C when accum), column-major.  With split scratch,
+// a grid of fewer than kSkinnyTarget tiles is split along K into segments of at least 32 KG.
 template <int KC, int RH>
 void skinny_launch(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
-                   int64_t K, int kc, float alpha, bool accum, cudaStream_t s) {
-    const dim3 g((unsigned)((m + 32 * RH - 1) / (32 * RH)), (unsigned)((kc + KC - 1) / KC));
-    k_skinny<KC, RH><<<g, 256, skinny_smem<KC>(), s>>>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum);
+                   int64_t K, int kc, float alpha, bool accum, const SkinnySplit* sp, cudaStream_t s) {
+    constexpr int KG = 8 / RH, ROWS = 32 * RH;
+    const int64_t gx = (m + ROWS - 1) / ROWS, gy = (kc + KC - 1) / KC, tiles = gx * gy;
+    int64_t kseg = K > 0 ? K : 1, z = 1;
+    if (sp && sp->ws && tiles < kSkinnyTarget) {
+        const int64_t want = std::min<int64_t>(kSkinnyTarget / tiles, (K + 32 * KG - 1) / (32 * KG));
+        if (want > 1) {
+            kseg = ((K + want - 1) / want + 32 * KG - 1) / (32 * KG) * (32 * KG);
+            z = (K + kseg - 1) / kseg;
+        }
+        if (z > 1 && (size_t)(tiles * z * ROWS * KC) > kSkinnyWsFloats) z = 1, kseg = K;
+    }
+    const dim3 g((unsigned)gx, (unsigned)gy, (unsigned)z);
+    k_skinny<KC, RH><<<g, 256, skinny_smem<KC>(), s>>>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, kseg,
+                                                       z > 1 ? sp->ws : nullptr, z > 1 ? sp->cnt : nullptr);
 }
 template <int KC>
 void skinny_rows(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
-                 int64_t K, int kc, float alpha, bool accum, cudaStream_t s) {
+                 int64_t K, int kc, float alpha, bool accum, const SkinnySplit* sp, cudaStream_t s) {
     if (m >= 4096)
-        skinny_launch<KC, 2>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+        skinny_launch<KC, 2>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
     else
-        skinny_launch<KC, 1>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+        skinny_launch<KC, 1>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
 }
 cudaError_t skinny(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
-                   int64_t K, int kc, float alpha, bool accum, cudaStream_t s) {
+                   int64_t K, int kc, float alpha, bool accum, cudaStream_t s, const SkinnySplit* sp = nullptr) {
     if (m <= 0 || kc <= 0) return cudaSuccess;
     if (kc <= 8)
-        skinny_rows<8>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+        skinny_rows<8>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
     else if (kc <= 16)
-        skinny_rows<16>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+        skinny_rows<16>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
     else if (kc <= 24)
-        skinny_rows<24>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+        skinny_rows<24>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
     else
-        skinny_rows<32>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, s);
+        skinny_rows<32>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
     return cudaGetLastError();
 }
 
@@ -1063,18 +1126,18 @@ cudaError_t factor_body(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_
 // SB-column blocks use their combined inverses (Dinv4), so a pass takes an eighth of the
 // dependent steps there; the rest of the matrix goes by 128-column blocks.
 cudaError_t solve_body(const float* LU, const float* Dinv, const float* Dinv4, int64_t nsup, int64_t n, float* X,
-                       float* Y, int k, cudaStream_t s) {
+                       float* Y, int k, const SkinnySplit* sp, cudaStream_t s) {
     cudaError_t e;
     const int64_t nblk = (n + NB - 1) / NB, blk0 = nsup * (SB / NB);
     auto fwd = [&](int64_t K, int64_t b, const float* Li, int64_t ldi) -> cudaError_t {
-        cudaError_t ee = skinny(Li, ldi, X + K, n, Y + K, n, b, b, k, 1.f, false, s);
+        cudaError_t ee = skinny(Li, ldi, X + K, n, Y + K, n, b, b, k, 1.f, false, s, sp);
         if (ee != cudaSuccess) return ee;
-        return skinny(LU + K * n + K + b, n, Y + K, n, X + K + b, n, n - K - b, b, k, -1.f, true, s);
+        return skinny(LU + K * n + K + b, n, Y + K, n, X + K + b, n, n - K - b, b, k, -1.f, true, s, sp);
     };
     auto bwd = [&](int64_t K, int64_t b, const float* Ui, int64_t ldi) -> cudaError_t {
-        cudaError_t ee = skinny(Ui, ldi, Y + K, n, X + K, n, b, b, k, 1.f, false, s);
+        cudaError_t ee = skinny(Ui, ldi, Y + K, n, X + K, n, b, b, k, 1.f, false, s, sp);
         if (ee != cudaSuccess) return ee;
-        return skinny(LU + K * n, n, X + K, n, Y, n, K, b, k, -1.f, true, s);
+        return skinny(LU + K * n, n, X + K, n, Y, n, K, b, k, -1.f, true, s, sp);
     };
     for (int64_t sb = 0; sb < nsup; sb++)
         if ((e = fwd(sb * SB, SB, Dinv4 + sb * 2 * SB * SB, SB)) != cudaSuccess) return e;
@@ -1131,6 +1194,10 @@ void LuGraphs::release() {
     if (tmp) cudaFree(tmp);
     if (dinv4) cudaFree(dinv4);
     if (super_tmp) cudaFree(super_tmp);
+    if (split_ws) cudaFree(split_ws);
+    if (split_cnt) cudaFree(split_cnt);
+    split_ws = nullptr;
+    split_cnt = nullptr;
     if (tc_mem) cudaFree(tc_mem);
     tc_mem = nullptr;
     tc_bytes = 0;
@@ -1146,8 +1213,8 @@ void LuGraphs::release() {
 
 size_t lu_factor_bytes(int64_t n) {
     const size_t nb = (size_t)((n + NB - 1) / NB), nsup = (size_t)(n / SB);
-    return sizeof(float) * (nb * 2 * NB * NB + nsup * 2 * SB * SB + (size_t)kInvScratch) + tc_bytes_for(n) +
-           4 * 256;
+    return sizeof(float) * (nb * 2 * NB * NB + nsup * 2 * SB * SB + (size_t)kInvScratch + kSkinnyWsFloats) +
+           tc_bytes_for(n) + sizeof(unsigned) * kSkinnyTarget + 4 * 256;
 }
 
 // Launched directly (not from a graph): a geometry is factored once, and its launches are
@@ -1587,8 +1654,17 @@ cudaError_t lu_solve_fp32(LuGraphs* G, const float* LU, int64_t n, float* X, int
             if ((e = cudaMalloc(&G->tmp, sizeof(float) * n * k)) != cudaSuccess) return e;
             G->tmp_floats = (size_t)n * k;
         }
+        if (!G->split_ws) {
+            if ((e = cudaMalloc(&G->split_ws, sizeof(float) * kSkinnyWsFloats)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&G->split_cnt, sizeof(unsigned) * kSkinnyTarget)) != cudaSuccess) return e;
+            if ((e = cudaMemset(G->split_cnt, 0, sizeof(unsigned) * kSkinnyTarget)) != cudaSuccess) return e;
+        }
         const int64_t nsup = (G->super_n == n && G->dinv4) ? n / SB : 0;
-        e = capture(s, &G->solve, [&] { return solve_body(LU, G->dinv, G->dinv4, nsup, n, X, G->tmp, k, s); });
+        SkinnySplit sp;
+        sp.ws = G->split_ws;
+        sp.cnt = G->split_cnt;
+        e = capture(s, &G->solve,
+                    [&] { return solve_body(LU, G->dinv, G->dinv4, nsup, n, X, G->tmp, k, &sp, s); });
         if (e != cudaSuccess) return e;
         G->solve_X = X;
         G->solve_k = k;

@@ -266,6 +266,14 @@ int  cpg_measure_fp64_peak(cpg_ctx* ctx, double* tflops);
 int  cpg_gemm_f32_tc(cpg_ctx* ctx, int64_t m, int64_t n, int64_t k, float alpha, const float* A, int64_t lda,
                      const float* B, int64_t ldb, float beta, float* C, int64_t ldc, int sm_budget);
 
+/* A (n x n, column-major FP32 device matrix) <- its unpivoted LU factors (unit lower L below the
+ * diagonal, U on and above it); X (n x k, ld n, device) <- A^{-1} X by the blocked forward and
+ * backward substitutions.  The factorization and substitutions of the mixed precision, without
+ * the refinement.  No counterpart in the reference (its solves are Eigen's BiCGSTAB,
+ * CPanel/cpCase.cpp:192); exposed so hosts and tests can call the kernels directly.  Allocates
+ * its inverses and scratch for the call.  CPG_E_INVALID on a zero pivot or non-finite entry. */
+int  cpg_lu_solve_f32(cpg_ctx* ctx, int64_t n, float* A, int64_t k, float* X);
+
 /* Build identification: the sm architecture the kernels were compiled for. */
 int  cpg_compiled_arch(void);
 

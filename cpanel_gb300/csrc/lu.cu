@@ -6,7 +6,7 @@
 // with an exact-product residual reaches 1e-12 relative in three passes.
 // Every kernel is hand-written: the diagonal blocks and the block steps inside them on the
 // CUDA cores, the panel products and the trailing updates on the tensor cores (tc_gemm.cu),
-// the substitutions as skinny products on the CUDA cores.
+// the substitutions as skinny products on the CUDA cores (skinny.cu).
 #include "tc_gemm.h"
 
 #include <algorithm>
@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "assemble.h"
+#include "skinny.h"
 
 namespace {
 
@@ -655,124 +656,6 @@ __global__ void __launch_bounds__(128) k_inv_step(const float* __restrict__ LU, 
     }
 }
 
-// ---- skinny products of the block substitutions: C (m x kc) = alpha A (m x K) B (K x kc)
-// (+ C when accum), all column-major, kc small.  256 threads per 32 RH rows x KC columns: lane =
-// row, warp w takes rows 32 (w % RH) .. and a 32-aligned share of every SK_CH-long chunk of B
-// (group w / RH of KG = 8 / RH), which is staged in shared memory column by column (coalesced,
-// conflict-free) and read back as float4 broadcasts of four consecutive K indices.  32 loads of
-// A in flight per thread, each element of A read once (coalesced along the rows) and used KC
-// times; the K groups' partial sums are added in a fixed order.  RH = 2 halves the staging of B
-// per row for tall products.
-// Split K (gridDim.z > 1): thread block z takes K indices [z kseg, (z + 1) kseg) and writes its
-// ROWS x KC partial to ws; the last of a tile's blocks to arrive (counter cnt[tile], which it
-// returns to 0) adds the gridDim.z partials in z order and updates C, so the result does not
-// depend on the order the blocks ran in.
-constexpr int SK_CH = 512;
-template <int KC, int RH>
-__global__ void __launch_bounds__(256) k_skinny(const float* __restrict__ A, int64_t lda, const float* __restrict__ B,
-                                                int64_t ldb, float* __restrict__ C, int64_t ldc, int64_t m,
-                                                int64_t K, int kc, float alpha, int accum, int64_t kseg,
-                                                float* __restrict__ ws, unsigned* __restrict__ cnt) {
-    constexpr int KG = 8 / RH, ROWS = 32 * RH;
-    extern __shared__ __align__(16) float dsm[];
-    __shared__ int s_last;
-    float* Bs = dsm;  // [KC][SK_CH]
-    const int t = threadIdx.x, lane = t & 31, w = t >> 5, rh = w % RH, kg = w / RH;
-    const int64_t r = (int64_t)blockIdx.x * ROWS + 32 * rh + lane;
-    const int c0 = blockIdx.y * KC;
-    const int64_t kz0 = (int64_t)blockIdx.z * kseg, kz1 = kz0 + kseg < K ? kz0 + kseg : K;
-    float acc[KC];
-#pragma unroll
-    for (int c = 0; c < KC; c++) acc[c] = 0.f;
-    for (int64_t k0 = kz0; k0 < kz1; k0 += SK_CH) {
-        const int kch = (int)(kz1 - k0 < SK_CH ? kz1 - k0 : SK_CH);
-        const int kst = (kch + 31) & ~31;  // staged length: the compute reads whole groups of 32
-        const int kw = ((kch + 32 * KG - 1) / (32 * KG)) * 32, kb = kw * kg;
-        float a[32];
-        auto load_a = [&](int h) {
-#pragma unroll
-            for (int j = 0; j < 32; j++) {
-                const int kk = kb + h + j;
-                a[j] = (r < m && kk < kch) ? A[(k0 + kk) * lda + r] : 0.f;
-            }
-        };
-        __syncthreads();
-        {  // every load of this thread in flight together, then the stores
-            constexpr int PER = SK_CH * KC / 256;
-            float v[PER];
-#pragma unroll
-            for (int q = 0; q < PER; q++) {
-                const int idx = t + 256 * q, kk = idx % SK_CH, c = idx / SK_CH;
-                v[q] = (kk < kch && c0 + c < kc) ? B[(int64_t)(c0 + c) * ldb + k0 + kk] : 0.f;
-            }
-#pragma unroll
-            for (int q = 0; q < PER; q++) {
-                const int idx = t + 256 * q;
-                if (idx % SK_CH < kst) Bs[idx] = v[q];
-            }
-        }
-        __syncthreads();
-        if (r < m) {
-            for (int h = 0; h < kw && kb + h < kch; h += 32) {
-                load_a(h);
-#pragma unroll
-                for (int j = 0; j < 32; j += 4) {
-#pragma unroll
-                    for (int c = 0; c < KC; c++) {
-                        const float4 b = *reinterpret_cast<const float4*>(Bs + c * SK_CH + kb + h + j);
-                        acc[c] = __fmaf_rn(a[j], b.x, acc[c]);
-                        acc[c] = __fmaf_rn(a[j + 1], b.y, acc[c]);
-                        acc[c] = __fmaf_rn(a[j + 2], b.z, acc[c]);
-                        acc[c] = __fmaf_rn(a[j + 3], b.w, acc[c]);
-                    }
-                }
-            }
-        }
-    }
-    __syncthreads();
-    float* red = dsm;  // [KG][ROWS][KC + 1]
-#pragma unroll
-    for (int c = 0; c < KC; c++) red[(kg * ROWS + 32 * rh + lane) * (KC + 1) + c] = acc[c];
-    __syncthreads();
-    const int nz = (int)gridDim.z;
-    const int64_t tile = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
-    if (nz > 1) {
-        float* part = ws + (tile * nz + blockIdx.z) * (ROWS * KC);
-        for (int idx = t; idx < ROWS * KC; idx += 256) {
-            const int rl = idx % ROWS, c = idx / ROWS;
-            float s = 0.f;
-#pragma unroll
-            for (int q = 0; q < KG; q++) s += red[(q * ROWS + rl) * (KC + 1) + c];
-            part[idx] = s;
-        }
-        __threadfence();
-        __syncthreads();
-        if (t == 0) s_last = atomicAdd(cnt + tile, 1u) == (unsigned)(nz - 1);
-        __syncthreads();
-        if (!s_last) return;
-        __threadfence();
-        if (t == 0) cnt[tile] = 0u;
-    }
-    for (int idx = t; idx < ROWS * KC; idx += 256) {
-        const int rl = idx % ROWS, c = idx / ROWS;
-        const int64_t rr = (int64_t)blockIdx.x * ROWS + rl;
-        if (rr >= m || c0 + c >= kc) continue;
-        float s = 0.f;
-        if (nz > 1) {
-            const float* part = ws + tile * nz * (ROWS * KC) + idx;
-            for (int z = 0; z < nz; z++) s += __ldcg(part + z * (ROWS * KC));
-        } else {
-#pragma unroll
-            for (int q = 0; q < KG; q++) s += red[(q * ROWS + rl) * (KC + 1) + c];
-        }
-        float* p = C + (int64_t)(c0 + c) * ldc + rr;
-        *p = accum ? *p + alpha * s : alpha * s;
-    }
-}
-template <int KC>
-constexpr int skinny_smem() {
-    return SK_CH * KC * 4;
-}
 
 // ---- lockstep block substitutions (the batch path's refined solves) ----
 // X and Y are n x k (ld n); items of LB_ITEM ints: mesh, r0, r1, -, -, K, b, -.
@@ -916,68 +799,7 @@ void set_attrs() {
                        cudaFuncSetAttribute(k_lu_diag<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
                        cudaFuncSetAttribute(k_lu_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             DIAG_SMEM);
-                       // 48 KB and more of dynamic shared memory, beside the kernel's static flag
-                       cudaFuncSetAttribute(k_skinny<24, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            skinny_smem<24>());
-                       cudaFuncSetAttribute(k_skinny<24, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            skinny_smem<24>());
-                       cudaFuncSetAttribute(k_skinny<32, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            skinny_smem<32>());
-                       cudaFuncSetAttribute(k_skinny<32, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                            skinny_smem<32>());
                    });
-}
-
-// Scratch of the split-K skinny products: partials and per-tile arrival counters (zero between
-// launches).  A split launch has fewer than kSkinnyTarget tiles and at most that many thread
-// blocks, which bounds both.
-struct SkinnySplit {
-    float* ws = nullptr;
-    unsigned* cnt = nullptr;
-};
-constexpr int kSkinnyTarget = 2 * 152;  // thread blocks a split launch aims at (two resident per SM)
-constexpr size_t kSkinnyWsFloats = (size_t)2 * kSkinnyTarget * 64 * 32;
-
-// C (m x kc) = alpha A (m x K) B (K x kc) (+ C when accum), column-major.  With split scratch,
-// a grid of fewer than kSkinnyTarget tiles is split along K into segments of at least 32 KG.
-template <int KC, int RH>
-void skinny_launch(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
-                   int64_t K, int kc, float alpha, bool accum, const SkinnySplit* sp, cudaStream_t s) {
-    constexpr int KG = 8 / RH, ROWS = 32 * RH;
-    const int64_t gx = (m + ROWS - 1) / ROWS, gy = (kc + KC - 1) / KC, tiles = gx * gy;
-    int64_t kseg = K > 0 ? K : 1, z = 1;
-    if (sp && sp->ws && tiles < kSkinnyTarget) {
-        const int64_t want = std::min<int64_t>(kSkinnyTarget / tiles, (K + 32 * KG - 1) / (32 * KG));
-        if (want > 1) {
-            kseg = ((K + want - 1) / want + 32 * KG - 1) / (32 * KG) * (32 * KG);
-            z = (K + kseg - 1) / kseg;
-        }
-        if (z > 1 && (size_t)(tiles * z * ROWS * KC) > kSkinnyWsFloats) z = 1, kseg = K;
-    }
-    const dim3 g((unsigned)gx, (unsigned)gy, (unsigned)z);
-    k_skinny<KC, RH><<<g, 256, skinny_smem<KC>(), s>>>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, kseg,
-                                                       z > 1 ? sp->ws : nullptr, z > 1 ? sp->cnt : nullptr);
-}
-template <int KC>
-void skinny_rows(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
-                 int64_t K, int kc, float alpha, bool accum, const SkinnySplit* sp, cudaStream_t s) {
-    if (m >= 4096)
-        skinny_launch<KC, 2>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
-    else
-        skinny_launch<KC, 1>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
-}
-cudaError_t skinny(const float* A, int64_t lda, const float* B, int64_t ldb, float* C, int64_t ldc, int64_t m,
-                   int64_t K, int kc, float alpha, bool accum, cudaStream_t s, const SkinnySplit* sp = nullptr) {
-    if (m <= 0 || kc <= 0) return cudaSuccess;
-    if (kc <= 8)
-        skinny_rows<8>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
-    else if (kc <= 16)
-        skinny_rows<16>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
-    else if (kc <= 24)
-        skinny_rows<24>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
-    else
-        skinny_rows<32>(A, lda, B, ldb, C, ldc, m, K, kc, alpha, accum, sp, s);
-    return cudaGetLastError();
 }
 
 }  // namespace
@@ -1214,7 +1036,7 @@ void LuGraphs::release() {
 size_t lu_factor_bytes(int64_t n) {
     const size_t nb = (size_t)((n + NB - 1) / NB), nsup = (size_t)(n / SB);
     return sizeof(float) * (nb * 2 * NB * NB + nsup * 2 * SB * SB + (size_t)kInvScratch + kSkinnyWsFloats) +
-           tc_bytes_for(n) + sizeof(unsigned) * kSkinnyTarget + 4 * 256;
+           tc_bytes_for(n) + sizeof(unsigned) * kSkinnyCounters + 4 * 256;
 }
 
 // Launched directly (not from a graph): a geometry is factored once, and its launches are
@@ -1656,8 +1478,8 @@ cudaError_t lu_solve_fp32(LuGraphs* G, const float* LU, int64_t n, float* X, int
         }
         if (!G->split_ws) {
             if ((e = cudaMalloc(&G->split_ws, sizeof(float) * kSkinnyWsFloats)) != cudaSuccess) return e;
-            if ((e = cudaMalloc(&G->split_cnt, sizeof(unsigned) * kSkinnyTarget)) != cudaSuccess) return e;
-            if ((e = cudaMemset(G->split_cnt, 0, sizeof(unsigned) * kSkinnyTarget)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&G->split_cnt, sizeof(unsigned) * kSkinnyCounters)) != cudaSuccess) return e;
+            if ((e = cudaMemset(G->split_cnt, 0, sizeof(unsigned) * kSkinnyCounters)) != cudaSuccess) return e;
         }
         const int64_t nsup = (G->super_n == n && G->dinv4) ? n / SB : 0;
         SkinnySplit sp;

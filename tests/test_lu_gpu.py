@@ -2,12 +2,13 @@
 
 The mixed precision factors A32 once without pivoting (1,024-column panels, tensor-core products
 for the off-diagonal factors and the trailing updates) and solves by forward and backward block
-substitutions with the diagonal blocks' inverses: skinny products, split along K into per-tile
-partials when a step has too few rows to fill the GPU.  The matrices here are R / sqrt(n) + 2 I,
+substitutions with the diagonal blocks' inverses: skinny products with one kernel per column
+count (groups of at most 32 columns), split along K into per-tile partials when a step has too
+few rows to fill the GPU.  The matrices here are R / sqrt(n) + 2 I,
 R standard normal, for which elimination without pivoting is stable.  Sizes cover a matrix below
 one 1,024-column panel, whole panels followed by a ragged 128-column tail, and tall steps whose
-products switch to 64-row tiles; the right-hand side counts cover the 8-, 24- and 32-column
-kernels and more than one column group.  Bounds, normwise:
+products switch to 64-row tiles; the right-hand side counts cover single columns, odd counts and
+more than one column group.  Bounds, normwise:
 
     ||A X - B|| <= 1e-5 ||A|| ||X||        (backward error of an FP32 factorization)
     ||X - X64|| <= 1e-4 ||X64||            (the condition number here is below 10)
@@ -49,7 +50,7 @@ def _system(n, k, seed):
     return A.float().cuda(), B.float().cuda()
 
 
-@pytest.mark.parametrize("n,k", [(300, 1), (1100, 17), (2100, 40), (2500, 8), (6000, 17)])
+@pytest.mark.parametrize("n,k", [(300, 1), (1100, 17), (2100, 40), (2500, 8), (2600, 33), (6000, 17), (5000, 3)])
 def test_lu_solve_matches_fp64(cg, n, k):
     import torch
     A, B = _system(n, k, 100 + n + k)

@@ -8,7 +8,6 @@
 #include <cmath>
 #include <limits>
 #include <thread>
-#include <unordered_map>
 
 namespace cpg {
 namespace {
@@ -71,21 +70,20 @@ struct Geo {
 struct Builder {
     std::vector<d3> P;
     std::vector<Edge> E;
-    std::unordered_map<uint64_t, int> emap;
+    EdgeMap emap;
     std::vector<Panel> pan;
     std::vector<bool> surfLS;
     std::vector<Wake> wakes;
 
     int edge(int a, int b) {  // geometry::findEdge, CPanel/geometry.cpp:771-787
-        uint64_t k = ((uint64_t)std::min(a, b) << 32) | (uint64_t)std::max(a, b);
-        auto it = emap.find(k);
-        if (it != emap.end()) return it->second;
+        int& slot = emap.slot(((uint64_t)std::min(a, b) << 32) | (uint64_t)std::max(a, b));
+        if (slot >= 0) return slot;
         Edge e;
         e.n1 = a;
         e.n2 = b;
         E.push_back(e);
-        emap.emplace(k, (int)E.size() - 1);
-        return (int)E.size() - 1;
+        slot = (int)E.size() - 1;
+        return slot;
     }
 
     // panel::setGeom, CPanel/panel.cpp:33-72.  The edges' lengths are taken from the panel's own

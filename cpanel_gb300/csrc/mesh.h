@@ -16,6 +16,42 @@ struct d3 {
     double x = 0, y = 0, z = 0;
 };
 
+// Edge index by node pair (the search of geometry::findEdge, CPanel/geometry.cpp:771-787):
+// open addressing with linear probing, at most half full.  slot(key) is the value of key, -1
+// until the caller sets it, so an edge takes its index when it is first seen, as in a search
+// of the edge list.
+struct EdgeMap {
+    std::vector<uint64_t> keys;  // key + 1; 0 marks an empty slot
+    std::vector<int> vals;
+    uint64_t mask = 0;
+    size_t used = 0;
+    void reserve(size_t n) {
+        size_t c = 64;
+        while (c < 2 * n) c <<= 1;
+        if (c <= keys.size()) return;
+        std::vector<uint64_t> ok = std::move(keys);
+        std::vector<int> ov = std::move(vals);
+        keys.assign(c, 0);
+        vals.assign(c, -1);
+        mask = c - 1;
+        used = 0;
+        for (size_t i = 0; i < ok.size(); i++)
+            if (ok[i]) slot(ok[i] - 1) = ov[i];
+    }
+    int& slot(uint64_t key) {
+        if (2 * (used + 1) > keys.size()) reserve(used + 1 > 32 ? 2 * (used + 1) : 64);
+        for (uint64_t h = (key * 0x9E3779B97F4A7C15ull) >> 20;; h++) {
+            const uint64_t i = h & mask;
+            if (keys[i] == key + 1) return vals[i];
+            if (keys[i] == 0) {
+                keys[i] = key + 1;
+                used++;
+                return vals[i];
+            }
+        }
+    }
+};
+
 // Packed per-panel record staged by the assembly kernels (24 doubles, 192 bytes).
 enum PanelField {
     PF_V0 = 0, PF_V1 = 3, PF_V2 = 6, PF_C = 9, PF_N = 12, PF_L = 15, PF_M = 18, PF_AREA = 21, PF_LONG = 22,

@@ -7,7 +7,6 @@
 #include <algorithm>
 #include <array>
 #include <cmath>
-#include <unordered_map>
 
 #include "mesh.h"
 
@@ -49,20 +48,19 @@ struct Line {
 struct Topo {
     std::vector<d3> P;
     std::vector<Edge> E;
-    std::unordered_map<uint64_t, int> emap;
+    EdgeMap emap;
     std::vector<Pan> body, wake;
     std::vector<Line> lines;
 
     int edge(int a, int b) {  // geometry::findEdge, CPanel/geometry.cpp:771-787
-        uint64_t k = ((uint64_t)std::min(a, b) << 32) | (uint64_t)std::max(a, b);
-        auto it = emap.find(k);
-        if (it != emap.end()) return it->second;
+        int& slot = emap.slot(((uint64_t)std::min(a, b) << 32) | (uint64_t)std::max(a, b));
+        if (slot >= 0) return slot;
         Edge e;
         e.n1 = a;
         e.n2 = b;
         E.push_back(e);
-        emap.emplace(k, (int)E.size() - 1);
-        return (int)E.size() - 1;
+        slot = (int)E.size() - 1;
+        return slot;
     }
     double len(int e) const { return nrm(sub(P[E[e].n2], P[E[e].n1])); }
     void geomTri(Pan& p) {  // panel::setGeom, CPanel/panel.cpp:33-72

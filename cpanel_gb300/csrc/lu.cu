@@ -1373,6 +1373,14 @@ cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, in
             cudaFreeAsync(c, s);
         }
     } fr{ddesc, ditems, dact, s};
+    // The substitution plan reads which systems are active from dact, so one graph of its launches
+    // serves every pass; it is destroyed before the plan's buffers are freed.
+    struct SubstGraph {
+        cudaGraphExec_t exec = nullptr;
+        ~SubstGraph() {
+            if (exec) cudaGraphExecDestroy(exec);
+        }
+    } sg;
     if ((e = cudaMemcpyAsync(ddesc, desc.data(), sizeof(SubstMesh) * m, cudaMemcpyHostToDevice, s)) != cudaSuccess)
         return e;
     if (!items.empty() &&
@@ -1427,15 +1435,22 @@ cudaError_t solve_lu_refined_batched(const RefineMesh* ms, int m, double tol, in
         if ((e = join()) != cudaSuccess) return e;
         {
             ProfScope ps(Prof::LU_SOLVE, s);
-            for (const Step& stp : plan) {
-                const int* it = ditems + stp.off * LB_ITEM;
-                if (kmax <= 8)
-                    subst_launch<8>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
-                else if (kmax <= 16)
-                    subst_launch<16>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
-                else
-                    subst_launch<32>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+            if (!sg.exec) {  // captured on the first pass, replayed on every later one
+                e = capture(s, &sg.exec, [&] {
+                    for (const Step& stp : plan) {
+                        const int* it = ditems + stp.off * LB_ITEM;
+                        if (kmax <= 8)
+                            subst_launch<8>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+                        else if (kmax <= 16)
+                            subst_launch<16>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+                        else
+                            subst_launch<32>(stp.kind, (unsigned)stp.cnt, ddesc, it, dact, stp.dir, s);
+                    }
+                    return cudaGetLastError();
+                });
+                if (e != cudaSuccess) return e;
             }
+            if ((e = cudaGraphLaunch(sg.exec, s)) != cudaSuccess) return e;
         }
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         if ((e = fork()) != cudaSuccess) return e;

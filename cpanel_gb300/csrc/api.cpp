@@ -52,6 +52,17 @@ struct cpg_ctx {
 };
 
 namespace {
+// Streams of a context: its own stream one priority level above the lowest, the aux stream (the
+// per-geometry post tables, queued beside a solve) at the lowest, so the solve's kernels take the
+// SMs first and the tables fill what they leave free.  The LU's own side streams are at the
+// highest level.
+cudaError_t make_stream(cudaStream_t* s, bool background) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = greatest = 0;
+    const int prio = (background || greatest >= least) ? least : least - 1;
+    return cudaStreamCreateWithPriority(s, cudaStreamNonBlocking, prio);
+}
+
 // installs the context's profiler for the calling thread during one API call
 struct ProfInstall {
     cpg::Prof* saved;
@@ -262,10 +273,8 @@ void case_scalars(const cpg_flow& f, const cpg_refs& r, cpg::CaseScalars& cs) {
 int prepare_post(cpg_geometry* g) {
     cpg_ctx* ctx = g->ctx;
     if (g->post_ready) return CPG_OK;
-    if (!ctx->aux) CK(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking), "aux stream");
+    if (!ctx->aux) CK(make_stream(&ctx->aux, true), "aux stream");
     if (!g->post_ev) CK(cudaEventCreateWithFlags(&g->post_ev, cudaEventDisableTiming), "event");
-    CK(cudaEventRecord(g->post_ev, ctx->stream), "event");  // the geometry's uploads
-    CK(cudaStreamWaitEvent(ctx->aux, g->post_ev, 0), "event");
     cudaStream_t s = ctx->aux;
     const cpg::HostMesh& H = g->H;
     int64_t n = H.n_body;
@@ -310,9 +319,14 @@ int prepare_post(cpg_geometry* g) {
     T.n_wakes = (int)H.trefftz.size();
     T.n_st = nst;
     T.n_pts = (int64_t)H.tz_pts.size() / 3;
+    // the host tables first, while the aux stream is idle (a pageable copy returns only when the
+    // work queued before it on its stream is done), then the wait for the geometry's uploads and
+    // whatever the caller queued before this call
     CK(upload(g->tzst, st, s), "upload Trefftz");
     CK(upload(g->tzln, ln, s), "upload Trefftz");
     CK(upload(g->tzpts, H.tz_pts, s), "upload Trefftz");
+    CK(cudaEventRecord(g->post_ev, ctx->stream), "event");
+    CK(cudaStreamWaitEvent(s, g->post_ev, 0), "event");
     CK(cpg::launch_chtls_weights(T, s), "CHTLS weights");
     CK(g->G.ensure(std::max<size_t>(8, sizeof(double) * T.n_pts * H.n_wake)), "alloc G");
     CK(cpg::launch_wake_potential_op(g->wrec.as<double>(), H.n_wake, g->tzpts.as<double>(), T.n_pts,
@@ -339,7 +353,7 @@ int cpg_create(cpg_ctx** out, int device) {
     cpg_ctx* c = new (std::nothrow) cpg_ctx();
     if (!c) return CPG_E_OOM;
     c->device = device;
-    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (cudaSetDevice(device) != cudaSuccess || make_stream(&c->stream, false) != cudaSuccess) {
         delete c;
         return CPG_E_CUDA;
     }
@@ -381,7 +395,7 @@ int cpg_set_stream(cpg_ctx* ctx, void* stream) {
     ctx->own_stream = false;
     ctx->stream = (cudaStream_t)stream;
     if (!stream) {
-        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking), "stream");
+        CK(make_stream(&ctx->stream, false), "stream");
         ctx->own_stream = true;
     }
     return CPG_OK;

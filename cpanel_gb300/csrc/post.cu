@@ -18,10 +18,15 @@ namespace {
 // zero row) for N = 3 and N = 2, orders 0..3.  c_ms[N-2][order][k][d].
 __constant__ int8_t c_ms[2][4][19][3];
 __constant__ int c_t[2][4];
+// 1 / (m_1! ... m_N!) of each row, divided out in the order the fit divides it (1 / m_1!, then
+// / m_2!, ...): the same correctly rounded quotients as dividing at each fit, without the FP64
+// divisions per panel, term and cluster member
+__constant__ double c_fact[2][4][19];
 
 void build_tables() {
     int8_t ms[2][4][19][3] = {};
     int tt[2][4] = {};
+    double fa[2][4][19] = {};
     for (int N = 2; N <= 3; N++)
         for (int q = 0; q <= 3; q++) {
             // recursive derivSequence
@@ -67,11 +72,20 @@ void build_tables() {
             }
             o.erase(o.begin());
             tt[N - 2][q] = (int)o.size();
-            for (size_t k = 0; k < o.size() && k < 19; k++)
-                for (int a = 0; a < N; a++) ms[N - 2][q][k][a] = (int8_t)o[k][a];
+            for (size_t k = 0; k < o.size() && k < 19; k++) {
+                double f = 1;
+                for (int a = 0; a < N; a++) {
+                    ms[N - 2][q][k][a] = (int8_t)o[k][a];
+                    int fi = 1;
+                    for (int j = 2; j <= o[k][a]; j++) fi *= j;
+                    f /= (double)fi;
+                }
+                fa[N - 2][q][k] = f;
+            }
         }
     cudaMemcpyToSymbol(c_ms, ms, sizeof(ms));
     cudaMemcpyToSymbol(c_t, tt, sizeof(tt));
+    cudaMemcpyToSymbol(c_fact, fa, sizeof(fa));
 }
 
 // once per device, also when several host threads start at the same time
@@ -93,12 +107,6 @@ __device__ __forceinline__ double powi(double x, int e) {
     double r = 1;
     for (int k = 0; k < e; k++) r = k == 0 ? x : r * x;
     return r;
-}
-
-__device__ __forceinline__ int ifact(int i) {
-    int o = 1;
-    for (int k = 2; k <= i; k++) o *= k;
-    return o;
 }
 
 struct WarpSmem {
@@ -137,8 +145,7 @@ __device__ bool chtls_warp(WarpSmem& S, int N, int order, int nf, bool withB, do
     const int t = c_t[N - 2][order];
     if (lane < nf) {
         for (int k = 0; k < t; k++) {
-            double fact = 1;
-            for (int d = 0; d < N; d++) fact /= ifact(c_ms[N - 2][order][k][d]);
+            const double fact = c_fact[N - 2][order][k];
             double prod = 1;
             for (int d = 0; d < N; d++) prod *= powi(S.dX[lane][d], c_ms[N - 2][order][k][d]);
             S.A[lane][k] = fact * prod;

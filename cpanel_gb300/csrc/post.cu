@@ -167,17 +167,34 @@ __device__ bool chtls_warp(WarpSmem& S, int N, int order, int nf, bool withB, do
         }
     }
     __syncwarp();
-    for (int q = lane; q < t * t; q += 32) {
-        int rr = q / t, cc = q % t;
-        double s1 = 0, s2 = 0;
-        for (int i = 0; i < nf; i++) s1 += S.A[i][rr] * S.W[i] * S.A[i][cc];
-        if (withB)
-            for (int i = 0; i < nf; i++) s2 += S.Bm[i][rr] * S.W[i] * S.Bm[i][cc];
-        S.M[rr][cc] = s1 + s2;
-    }
+    // Normal matrix M = A^T W A (+ Bm^T W Bm), each term (A_i,rr W_i) A_i,cc summed over i in order.
+    // The left factor A_i,rr W_i is the same rounded product for every cc: it is formed once, as
+    // the right-hand side R = (A W)^T, and for the second sum as Bm W in A's place (A is not read
+    // again); M = s1 + s2 as one addition, s2 = +0 without the B rows.
     for (int q = lane; q < t * nf; q += 32) {
         int rr = q / nf, i = q % nf;
         S.R[rr][i] = S.A[i][rr] * S.W[i];
+    }
+    __syncwarp();
+    for (int q = lane; q < t * t; q += 32) {
+        int rr = q / t, cc = q % t;
+        double s1 = 0;
+        for (int i = 0; i < nf; i++) s1 += S.R[rr][i] * S.A[i][cc];
+        S.M[rr][cc] = withB ? s1 : s1 + 0.0;
+    }
+    if (withB) {
+        __syncwarp();
+        for (int q = lane; q < t * nf; q += 32) {
+            int rr = q / nf, i = q % nf;
+            S.A[i][rr] = S.Bm[i][rr] * S.W[i];
+        }
+        __syncwarp();
+        for (int q = lane; q < t * t; q += 32) {
+            int rr = q / t, cc = q % t;
+            double s2 = 0;
+            for (int i = 0; i < nf; i++) s2 += S.A[i][rr] * S.Bm[i][cc];
+            S.M[rr][cc] = S.M[rr][cc] + s2;
+        }
     }
     __syncwarp();
     // Householder QR (Eigen::HouseholderQR, unblocked) and Q^T R
@@ -205,18 +222,17 @@ __device__ bool chtls_warp(WarpSmem& S, int N, int order, int nf, bool withB, do
         }
         __syncwarp();
         if (tau != 0) {
-            int j = k + 1 + lane;
-            if (j < t) {
-                double tmp = S.M[k][j];
-                for (int i = k + 1; i < t; i++) tmp += S.M[i][k] * S.M[i][j];
-                S.M[k][j] -= tau * tmp;
-                for (int i = k + 1; i < t; i++) S.M[i][j] -= tau * S.M[i][k] * tmp;
-            }
-            if (lane < nf) {
-                double tmp = S.R[k][lane];
-                for (int i = k + 1; i < t; i++) tmp += S.M[i][k] * S.R[i][lane];
-                S.R[k][lane] -= tau * tmp;
-                for (int i = k + 1; i < t; i++) S.R[i][lane] -= tau * S.M[i][k] * tmp;
+            // the reflector on the columns of M right of k and on every column of R, one column a
+            // lane in one pass (u < nm: column k + 1 + u of M, else column u - nm of R), each with
+            // the operations in the order of a column at a time
+            const int nm = t - k - 1;
+            for (int u = lane; u < nm + nf; u += 32) {
+                double* X = u < nm ? &S.M[0][k + 1 + u] : &S.R[0][u - nm];
+                const int ld = u < nm ? TM : NF;
+                double tmp = X[k * ld];
+                for (int i = k + 1; i < t; i++) tmp += S.M[i][k] * X[i * ld];
+                X[k * ld] -= tau * tmp;
+                for (int i = k + 1; i < t; i++) X[i * ld] -= tau * S.M[i][k] * tmp;
             }
         }
         __syncwarp();

@@ -433,48 +433,52 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
         *hi = (float)v;
         *lo = (float)(v - (double)*hi);
     };
-    for (int64_t i = 0; i < n; i++) {
-        const double* r = &H.body[i * cpg::PF_STRIDE];
-        float* o = &fr[i * F_STRIDE_HOST];
-        for (int q = 0; q < 3; q++) {
-            split(r[cpg::PF_C + q], o + q, o + 3 + q);
-            split(r[cpg::PF_N + q], o + 6 + q, o + 9 + q);
-        }
-        split(r[cpg::PF_AREA], o + 12, o + 13);
-        o[14] = (float)r[cpg::PF_LONG];
-        // exact-formula band: vertices about the centroid, n x s_k, |s_k|, 1/|s_k|
-        const double* c = r + cpg::PF_C;
-        const double* nv = r + cpg::PF_N;
-        for (int k = 0; k < 3; k++) {
-            const double* v = r + cpg::PF_V0 + 3 * k;
-            const double* w = r + cpg::PF_V0 + 3 * ((k + 1) % 3);
-            double sv[3] = {w[0] - v[0], w[1] - v[1], w[2] - v[2]};
-            double ns[3] = {nv[1] * sv[2] - nv[2] * sv[1], nv[2] * sv[0] - nv[0] * sv[2], nv[0] * sv[1] - nv[1] * sv[0]};
-            double S = std::sqrt(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]);
+    cpg::host_parallel((size_t)n, [&](unsigned, size_t lo, size_t hi) {
+        for (int64_t i = (int64_t)lo; i < (int64_t)hi; i++) {
+            const double* r = &H.body[i * cpg::PF_STRIDE];
+            float* o = &fr[i * F_STRIDE_HOST];
             for (int q = 0; q < 3; q++) {
-                split(v[q] - c[q], o + 16 + 2 * (3 * k + q), o + 17 + 2 * (3 * k + q));
-                split(ns[q], o + 34 + 2 * (3 * k + q), o + 35 + 2 * (3 * k + q));
+                split(r[cpg::PF_C + q], o + q, o + 3 + q);
+                split(r[cpg::PF_N + q], o + 6 + q, o + 9 + q);
             }
-            split(S, o + 52 + 2 * k, o + 53 + 2 * k);
-            split(1.0 / S, o + 58 + 2 * k, o + 59 + 2 * k);
+            split(r[cpg::PF_AREA], o + 12, o + 13);
+            o[14] = (float)r[cpg::PF_LONG];
+            // exact-formula band: vertices about the centroid, n x s_k, |s_k|, 1/|s_k|
+            const double* c = r + cpg::PF_C;
+            const double* nv = r + cpg::PF_N;
+            for (int k = 0; k < 3; k++) {
+                const double* v = r + cpg::PF_V0 + 3 * k;
+                const double* w = r + cpg::PF_V0 + 3 * ((k + 1) % 3);
+                double sv[3] = {w[0] - v[0], w[1] - v[1], w[2] - v[2]};
+                double ns[3] = {nv[1] * sv[2] - nv[2] * sv[1], nv[2] * sv[0] - nv[0] * sv[2], nv[0] * sv[1] - nv[1] * sv[0]};
+                double S = std::sqrt(sv[0] * sv[0] + sv[1] * sv[1] + sv[2] * sv[2]);
+                for (int q = 0; q < 3; q++) {
+                    split(v[q] - c[q], o + 16 + 2 * (3 * k + q), o + 17 + 2 * (3 * k + q));
+                    split(ns[q], o + 34 + 2 * (3 * k + q), o + 35 + 2 * (3 * k + q));
+                }
+                split(S, o + 52 + 2 * k, o + 53 + 2 * k);
+                split(1.0 / S, o + 58 + 2 * k, o + 59 + 2 * k);
+            }
         }
-    }
+    });
     // FP64 edge constants of the mixed near field: |s_k|, 1/|s_k|, s_k.m (E_STRIDE = 12 per panel),
     // rounded exactly as the device would form them (no contraction in this file)
     std::vector<double> er(n * 12, 0.0);
-    for (int64_t i = 0; i < n; i++) {
-        const double* r = &H.body[i * cpg::PF_STRIDE];
-        const double* m = r + cpg::PF_M;
-        for (int k = 0; k < 3; k++) {
-            const double* v = r + cpg::PF_V0 + 3 * k;
-            const double* w = r + cpg::PF_V0 + 3 * ((k + 1) % 3);
-            const double sx = w[0] - v[0], sy = w[1] - v[1], sz = w[2] - v[2];
-            const double S = std::sqrt(sx * sx + sy * sy + sz * sz);
-            er[i * 12 + k] = S;
-            er[i * 12 + 3 + k] = 1 / S;
-            er[i * 12 + 6 + k] = sx * m[0] + sy * m[1] + sz * m[2];
+    cpg::host_parallel((size_t)n, [&](unsigned, size_t lo, size_t hi) {
+        for (int64_t i = (int64_t)lo; i < (int64_t)hi; i++) {
+            const double* r = &H.body[i * cpg::PF_STRIDE];
+            const double* m = r + cpg::PF_M;
+            for (int k = 0; k < 3; k++) {
+                const double* v = r + cpg::PF_V0 + 3 * k;
+                const double* w = r + cpg::PF_V0 + 3 * ((k + 1) % 3);
+                const double sx = w[0] - v[0], sy = w[1] - v[1], sz = w[2] - v[2];
+                const double S = std::sqrt(sx * sx + sy * sy + sz * sz);
+                er[i * 12 + k] = S;
+                er[i * 12 + 3 + k] = 1 / S;
+                er[i * 12 + 6 + k] = sx * m[0] + sy * m[1] + sz * m[2];
+            }
         }
-    }
+    });
     cudaError_t e;
     if ((e = upload(g->rec, H.body, s)) != cudaSuccess || (e = upload(g->frec, fr, s)) != cudaSuccess ||
         (e = upload(g->erec, er, s)) != cudaSuccess ||

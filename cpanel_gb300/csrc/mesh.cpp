@@ -7,6 +7,12 @@
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <atomic>
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <thread>
 
 namespace cpg {
@@ -158,26 +164,102 @@ int fact(int i) {
     return o;
 }
 
-// Runs f(worker, lo, hi) over [0, n) in contiguous slices, one host thread each (at most 16);
-// a small range, or a slice whose thread cannot be started, runs on the calling thread.
-template <class F>
-void par_slices(size_t n, F f) {
-    unsigned nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-    if (n < 2048) nth = 1;
-    std::vector<std::thread> pool;
-    for (unsigned w = 1; w < nth; w++) {
-        size_t lo = n * w / nth, hi = n * (w + 1) / nth;
-        try {
-            pool.emplace_back([&f, w, lo, hi] { f(w, lo, hi); });
-        } catch (...) {
-            f(w, lo, hi);
+// Host threads for par_slices, started on first use and kept for the life of the process (they
+// wait on a condition variable between calls; starting and joining 15 threads per call had cost
+// up to a millisecond).  A call queues its slices and runs slices itself as well, so it finishes
+// when every pool thread is busy with other calls (meshes built on several threads at once) or
+// when the pool has no threads at all (a forked child).
+class SlicePool {
+  public:
+    struct Job {
+        std::function<void(unsigned, size_t, size_t)> f;
+        size_t n = 0;
+        unsigned nth = 1;
+        std::atomic<unsigned> next{0}, left{0};
+        std::mutex m;
+        std::condition_variable cv;
+        void work() {
+            for (unsigned w; (w = next.fetch_add(1)) < nth;) {
+                f(w, n * w / nth, n * (w + 1) / nth);
+                if (left.fetch_sub(1) == 1) {
+                    std::lock_guard<std::mutex> l(m);
+                    cv.notify_all();
+                }
+            }
+        }
+    };
+    static SlicePool& get() {
+        static SlicePool* pool = new SlicePool();  // never destroyed: its threads outlive main
+        return *pool;
+    }
+    void run(const std::shared_ptr<Job>& j) {
+        {
+            std::lock_guard<std::mutex> l(m_);
+            q_.push_back(j);
+        }
+        cv_.notify_all();
+        j->work();
+        {
+            std::unique_lock<std::mutex> l(j->m);
+            j->cv.wait(l, [&] { return j->left.load() == 0; });
+        }
+        std::lock_guard<std::mutex> l(m_);
+        auto it = std::find(q_.begin(), q_.end(), j);
+        if (it != q_.end()) q_.erase(it);
+    }
+
+  private:
+    SlicePool() {
+        const unsigned k = std::max(1u, std::min(16u, std::thread::hardware_concurrency())) - 1;
+        for (unsigned i = 0; i < k; i++) {
+            try {
+                std::thread([this] { loop(); }).detach();
+            } catch (...) {
+                break;
+            }
         }
     }
-    f(0u, (size_t)0, n / nth);
-    for (auto& t : pool) t.join();
+    void loop() {
+        for (;;) {
+            std::shared_ptr<Job> j;
+            {
+                std::unique_lock<std::mutex> l(m_);
+                cv_.wait(l, [&] { return !q_.empty(); });
+                j = q_.front();
+                if (j->next.load() >= j->nth) {  // every slice taken: the job leaves the queue
+                    q_.pop_front();
+                    continue;
+                }
+            }
+            j->work();
+        }
+    }
+    std::mutex m_;
+    std::condition_variable cv_;
+    std::deque<std::shared_ptr<Job>> q_;
+};
+
+// Runs f(slice, lo, hi) over [0, n) in contiguous slices (at most 16, each on one thread at a
+// time, so per-slice scratch indexed by the slice needs no lock); a small range runs on the
+// calling thread.
+template <class F>
+void par_slices(size_t n, F f) {
+    const unsigned nth = n < 2048 ? 1u : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    if (nth == 1) {
+        f(0u, (size_t)0, n);
+        return;
+    }
+    auto j = std::make_shared<SlicePool::Job>();
+    j->f = [&f](unsigned w, size_t lo, size_t hi) { f(w, lo, hi); };
+    j->n = n;
+    j->nth = nth;
+    j->left = nth;
+    SlicePool::get().run(j);
 }
 
 }  // namespace
+
+void host_parallel(size_t n, const std::function<void(unsigned, size_t, size_t)>& f) { par_slices(n, f); }
 
 // chtlsnd::chtlsnd for N = 1, no derivative observations (used by wake::Vradial,
 // CPanel/wake.cpp:587-594).  Monomials x, x^2/2, x^3/6 (orders 1..order).

@@ -6,7 +6,9 @@
 // Everything downstream (assembly, solve, post-processing) runs on the GPU from
 // the flat tables built here.
 #pragma once
+#include <cstddef>
 #include <cstdint>
+#include <functional>
 #include <string>
 #include <vector>
 
@@ -94,6 +96,10 @@ struct HostMesh {
 // Returns "" on success, else an error message.  tris are 1-based.  te_upper/te_lower
 // (n_te matrix indices, optional) flag the upper and lower parents of trailing edges whose
 // wake is not in the file (the vortex-particle buffer wake) before the CHTLS clusters grow.
+// Runs f(slice, lo, hi) over [0, n) in contiguous slices on the host threads of the mesh builder
+// (each slice on one thread; the calling thread takes part; small ranges run on the caller).
+void host_parallel(size_t n, const std::function<void(unsigned, size_t, size_t)>& f);
+
 std::string build_mesh(const double* nodes, int64_t n_nodes, const int64_t* tris, const int32_t* ids,
                        int64_t n_tris, HostMesh& out, const int32_t* te_upper = nullptr,
                        const int32_t* te_lower = nullptr, int64_t n_te = 0);

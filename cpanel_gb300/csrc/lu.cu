@@ -599,63 +599,109 @@ __global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh
 //   U^{-1}[r, j] = -(sum_{r <= k < j} U^{-1}[r, k] U[k, j]) U_jj^{-1}    (64-row tiles, r < j)
 // (block indices of 128; the sums run over the columns and rows that are not zero), then the
 // rest of L^{-1}'s block row j (L_jj^{-1}, zeros to its right) and of U^{-1}'s block column j
-// (U_jj^{-1}, zeros below).  Thread blocks of 128 threads: 2j L tiles, 2j U tiles, 2 fill
-// blocks.  Each tile passes its first product through its own 8,192 floats of T.
+// (U_jj^{-1}, zeros below).  Thread blocks of 128 threads.  The sum of a tile runs in K chunks of
+// at most INV_KCH, one thread block each, so that the step takes about as long as its shortest
+// tiles: each chunk's product goes to its own 8,192 floats of T, and the last chunk of a tile to
+// arrive (counter cnt[tile], returned to 0) adds them in chunk order and applies the diagonal
+// block's inverse.  Blocks: the chunks of the 2j L tiles, then of the 2j U tiles, then 2 fill.
+constexpr int INV_KCH = 256;
+__host__ __device__ constexpr int inv_chunks(int j, int q) { return (64 * (2 * j - q) + INV_KCH - 1) / INV_KCH; }
+int inv_step_blocks(int j) {
+    int c = 0;
+    for (int q = 0; q < 2 * j; q++) c += inv_chunks(j, q);
+    return 2 * c + 2;
+}
 __global__ void __launch_bounds__(128) k_inv_step(const float* __restrict__ LU, int64_t n, int64_t KO, int j,
-                                                  const float* __restrict__ Dinv, float* D4, float* T) {
-    const int nt = 2 * j, q = blockIdx.x, t = threadIdx.x;
+                                                  const float* __restrict__ Dinv, float* D4, float* T,
+                                                  unsigned* __restrict__ cnt) {
+    __shared__ int s_last;
+    const int nt = 2 * j, t = threadIdx.x;
     float* Linv = D4;
     float* Uinv = D4 + SB * SB;
     const int64_t J = (int64_t)NB * j;  // first row and column of block j inside the SB block
     const float* Ljj = Dinv + (KO / NB + j) * 2 * NB * NB;  // ld NB
     const float* Ujj = Ljj + NB * NB;
+    // this block's tile (side 0: L, 1: U; q), chunk ch of nch, and its first slot of T
+    int b = blockIdx.x, side = 0, q = 0, slot = 0;
+    for (; side < 2; side++) {
+        for (q = 0; q < nt; q++) {
+            const int c = inv_chunks(j, q);
+            if (b < c) break;
+            b -= c;
+            slot += c;
+        }
+        if (q < nt) break;
+    }
+    if (side == 2) {  // the fill blocks
+        if (b == 0) {  // L^{-1}[J.., J..SB): L_jj^{-1}, then zeros
+            for (int idx = t; idx < NB * (SB - (int)J); idx += 128) {
+                const int64_t c = J + idx / NB;
+                const int r = idx % NB;
+                Linv[(J + r) + c * SB] = c < J + NB ? Ljj[r + (c - J) * NB] : 0.f;
+            }
+        } else {  // U^{-1}[J..SB, J..): U_jj^{-1}, then zeros
+            const int h = SB - (int)J;
+            for (int idx = t; idx < NB * h; idx += 128) {
+                const int c = idx / h;
+                const int64_t r = J + idx % h;
+                Uinv[r + (J + c) * SB] = r < J + NB ? Ujj[(r - J) + (int64_t)c * NB] : 0.f;
+            }
+        }
+        return;
+    }
+    const int ch = b, nch = inv_chunks(j, q);
+    const int64_t o0 = 64 * (int64_t)q;  // c0 (L) or r0 (U)
+    const int kt = (int)(J - o0), k0 = ch * INV_KCH, kn = min(INV_KCH, kt - k0);
+    float* Tq = T + (int64_t)(slot + ch) * 8192;
     float acc[8][8];
-    if (q < nt) {  // L^{-1}[J.., c0..c0+64)
-        const int64_t c0 = 64 * (int64_t)q;
-        float* Tq = T + (int64_t)q * 8192;  // 128 x 64, ld 128
+    if (side == 0) {  // partial of L^{-1}[J.., c0..c0+64): 128 x 64, ld 128
         const int tr = t % 16, tc = t / 16;
-        tile_mm<128>(LU + (KO + c0) * n + KO + J, n, Linv + c0 + c0 * SB, SB, 128, 64, (int)(J - c0), acc);
+        tile_mm<128>(LU + (KO + o0 + k0) * n + KO + J, n, Linv + o0 + k0 + o0 * SB, SB, 128, 64, kn, acc);
 #pragma unroll
         for (int i = 0; i < 8; i++)
 #pragma unroll
             for (int jj = 0; jj < 8; jj++) Tq[(8 * tc + jj) * 128 + 8 * tr + i] = acc[i][jj];
-        __syncthreads();
-        tile_mm<128>(Ljj, NB, Tq, 128, 128, 64, NB, acc);
-#pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-            for (int jj = 0; jj < 8; jj++) Linv[(J + 8 * tr + i) + (c0 + 8 * tc + jj) * SB] = -acc[i][jj];
-    } else if (q < 2 * nt) {  // U^{-1}[r0..r0+64, J..)
-        const int64_t r0 = 64 * (int64_t)(q - nt);
-        float* Tq = T + (int64_t)q * 8192;  // 64 x 128, ld 64
+    } else {  // partial of U^{-1}[r0..r0+64, J..): 64 x 128, ld 64
         const int tr = t % 8, tc = t / 8;
-        tile_mm<64>(Uinv + r0 + r0 * SB, SB, LU + (KO + J) * n + KO + r0, n, 64, 128, (int)(J - r0), acc);
+        tile_mm<64>(Uinv + o0 + (o0 + k0) * SB, SB, LU + (KO + J) * n + KO + o0 + k0, n, 64, 128, kn, acc);
 #pragma unroll
         for (int i = 0; i < 8; i++)
 #pragma unroll
             for (int jj = 0; jj < 8; jj++) Tq[(8 * tc + jj) * 64 + 8 * tr + i] = acc[i][jj];
+    }
+    float* T0 = T + (int64_t)slot * 8192;  // the tile's sum (chunk 0's slot)
+    if (nch > 1) {
+        __threadfence();
         __syncthreads();
-        tile_mm<64>(Tq, 64, Ujj, NB, 64, 128, NB, acc);
+        const int tile = side * nt + q;
+        if (t == 0) s_last = atomicAdd(cnt + tile, 1u) == (unsigned)(nch - 1);
+        __syncthreads();
+        if (!s_last) return;
+        __threadfence();
+        if (t == 0) cnt[tile] = 0u;
+        for (int e = t; e < 8192; e += 128) {
+            float v = __ldcg(T0 + e);
+            for (int c = 1; c < nch; c++) v += __ldcg(T0 + (int64_t)c * 8192 + e);
+            T0[e] = v;
+        }
+    }
+    __syncthreads();
+    if (side == 0) {
+        const int tr = t % 16, tc = t / 16;
+        tile_mm<128>(Ljj, NB, T0, 128, 128, 64, NB, acc);
 #pragma unroll
         for (int i = 0; i < 8; i++)
 #pragma unroll
-            for (int jj = 0; jj < 8; jj++) Uinv[(r0 + 8 * tr + i) + (J + 8 * tc + jj) * SB] = -acc[i][jj];
-    } else if (q == 2 * nt) {  // L^{-1}[J.., J..SB): L_jj^{-1}, then zeros
-        for (int idx = t; idx < NB * (SB - (int)J); idx += 128) {
-            const int64_t c = J + idx / NB;
-            const int r = idx % NB;
-            Linv[(J + r) + c * SB] = c < J + NB ? Ljj[r + (c - J) * NB] : 0.f;
-        }
-    } else {  // U^{-1}[J..SB, J..): U_jj^{-1}, then zeros
-        const int h = SB - (int)J;
-        for (int idx = t; idx < NB * h; idx += 128) {
-            const int c = idx / h;
-            const int64_t r = J + idx % h;
-            Uinv[r + (J + c) * SB] = r < J + NB ? Ujj[(r - J) + (int64_t)c * NB] : 0.f;
-        }
+            for (int jj = 0; jj < 8; jj++) Linv[(J + 8 * tr + i) + (o0 + 8 * tc + jj) * SB] = -acc[i][jj];
+    } else {
+        const int tr = t % 8, tc = t / 8;
+        tile_mm<64>(T0, 64, Ujj, NB, 64, 128, NB, acc);
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+            for (int jj = 0; jj < 8; jj++) Uinv[(o0 + 8 * tr + i) + (J + 8 * tc + jj) * SB] = -acc[i][jj];
     }
 }
-
 
 // ---- lockstep block substitutions (the batch path's refined solves) ----
 // X and Y are n x k (ld n); items of LB_ITEM ints: mesh, r0, r1, -, -, K, b, -.
@@ -822,7 +868,9 @@ namespace {
 // stream while the rest of L21, U12 and the update run with kPanelSms SMs left to it.  The
 // serial chain is the diagonal blocks and these three small products.
 constexpr int kPanelSms = 32;
-constexpr int64_t kInvScratch = 4 * (SB / 64) * 8192;  // tile scratch of k_inv_step (28 tiles at most)
+// tile scratch of k_inv_step: the chunks of step 7 (32 L and 32 U), then its per-tile counters
+constexpr int64_t kInvScratch = 4 * (SB / 64) * 8192;
+constexpr int64_t kInvCounters = 32;
 
 // factorization of the diagonal block [KO, KE) x [KO, KE) in place on s (the updates of the
 // earlier panels applied), the inverses of its 128-column blocks into G->dinv; for a full SB
@@ -844,7 +892,8 @@ cudaError_t factor_diag_block(LuGraphs* G, float* LU, int64_t n, int* bad, int64
             const int j = (int)((K - KO) / NB);
             if ((e = cudaEventRecord(G->ev_diag, s)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(G->inv_stream, G->ev_diag, 0)) != cudaSuccess) return e;
-            k_inv_step<<<4 * j + 2, 128, 0, G->inv_stream>>>(LU, n, KO, j, G->dinv, D4, G->super_tmp);
+            k_inv_step<<<inv_step_blocks(j), 128, 0, G->inv_stream>>>(LU, n, KO, j, G->dinv, D4, G->super_tmp,
+                                                                      (unsigned*)(G->super_tmp + kInvScratch));
         }
         const int64_t K1 = K + b, rest = KE - K1;
         if (rest <= 0) break;
@@ -1035,7 +1084,7 @@ void LuGraphs::release() {
 
 size_t lu_factor_bytes(int64_t n) {
     const size_t nb = (size_t)((n + NB - 1) / NB), nsup = (size_t)(n / SB);
-    return sizeof(float) * (nb * 2 * NB * NB + nsup * 2 * SB * SB + (size_t)kInvScratch + kSkinnyWsFloats) +
+    return sizeof(float) * (nb * 2 * NB * NB + nsup * 2 * SB * SB + (size_t)(kInvScratch + kInvCounters) + kSkinnyWsFloats) +
            tc_bytes_for(n) + sizeof(unsigned) * kSkinnyCounters + 4 * 256;
 }
 
@@ -1059,7 +1108,8 @@ cudaError_t lu_factor_fp32(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStre
         if ((e = cudaMalloc(&G->dinv, sizeof(float) * nb * 2 * NB * NB)) != cudaSuccess) return e;
         if (nsup > 0) {
             if ((e = cudaMalloc(&G->dinv4, sizeof(float) * nsup * 2 * SB * SB)) != cudaSuccess) return e;
-            if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * kInvScratch)) != cudaSuccess) return e;
+            if ((e = cudaMalloc(&G->super_tmp, sizeof(float) * (kInvScratch + kInvCounters))) != cudaSuccess) return e;
+            if ((e = cudaMemset(G->super_tmp + kInvScratch, 0, sizeof(float) * kInvCounters)) != cudaSuccess) return e;
         }
         G->super_cap = nsup;
         G->factor_n = n;

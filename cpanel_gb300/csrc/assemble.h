@@ -144,6 +144,7 @@ struct LuGraphs {
     cudaStream_t rest_stream = nullptr;   // and of the in-block updates beside the next diagonal step
     cudaEvent_t ev_update = nullptr, ev_panel = nullptr;  // fork / join between the streams
     cudaEvent_t ev_diag = nullptr, ev_inv = nullptr, ev_solve = nullptr, ev_rest = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // the products between two diagonal blocks
     float* dinv = nullptr;      // inverses of the 128-column diagonal blocks (L then U per block)
     float* tmp = nullptr;       // n x k intermediate of the substitutions
     size_t tmp_floats = 0;

@@ -943,28 +943,38 @@ cudaError_t factor_body(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStream_
     if ((e = factor_diag_block(G, LU, n, bad, 0, std::min<int64_t>(SB, n), panel)) != cudaSuccess) return e;
     for (int64_t KO = 0; KO < n; KO += SB) {
         const int64_t KE = std::min<int64_t>(KO + SB, n);
+        const int64_t rows = n - KE, KE2 = std::min<int64_t>(KE + SB, n), w2 = KE2 - KE, far = rows - w2;
+        float* A21 = LU + KO * n + KE;  // rows KE.., columns KO..KE (ld n)
+        float* A12 = LU + KE * n + KO;  // rows KO..KE, columns KE.. (ld n)
+        float* A22 = LU + KE * n + KE;
+        // operand rows: A21's rows (K along its columns), U11^{-1}'s columns, L11^{-1}'s rows, A12's
+        // columns.  The strips that meet the next diagonal block (A21 rows KE..KE2, A12 columns
+        // KE..KE2) are final once the previous panel's update is queued: split them beside this
+        // diagonal block, which does not touch them.
+        if (KE < n) {
+            if ((e = tc_split(A21, 1, n, w2, SB, nearA, bad, main)) != cudaSuccess) return e;
+            if ((e = tc_split(A12, n, 1, w2, SB, nearB, bad, main)) != cudaSuccess) return e;
+        }
         // this diagonal block factored and inverted (the main stream has finished the rest of
         // the previous update)
         if ((e = cudaEventRecord(G->ev_panel, panel)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(main, G->ev_panel, 0)) != cudaSuccess) return e;
         if (KE >= n) break;  // a panel that ends short of n is the last one, so KE - KO == SB below
-        const int64_t rows = n - KE, KE2 = std::min<int64_t>(KE + SB, n), w2 = KE2 - KE, far = rows - w2;
         const float* Li = G->dinv4 + (KO / SB) * 2 * SB * SB;
         const float* Ui = Li + SB * SB;
-        float* A21 = LU + KO * n + KE;  // rows KE.., columns KO..KE (ld n)
-        float* A12 = LU + KE * n + KO;  // rows KO..KE, columns KE.. (ld n)
-        float* A22 = LU + KE * n + KE;
-        // operand rows: A21's rows (K along its columns), U11^{-1}'s columns, L11^{-1}'s rows, A12's
-        // columns
+        // the next diagonal block: L21 rows KE..KE2 on the main stream and U12 columns KE..KE2 on
+        // the in-block update stream (idle between two diagonal blocks) side by side, each with its
+        // inverse's split before and its own split after, then its update
+        if ((e = cudaEventRecord(G->ev_fork, main)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(G->rest_stream, G->ev_fork, 0)) != cudaSuccess) return e;
         if ((e = tc_split(Ui, SB, 1, SB, SB, invB, bad, main)) != cudaSuccess) return e;
-        if ((e = tc_split(Li, 1, SB, SB, SB, invA, bad, main)) != cudaSuccess) return e;
-        // the next diagonal block: L21 rows KE..KE2, U12 columns KE..KE2, then its update
-        if ((e = tc_split(A21, 1, n, w2, SB, nearA, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(Li, 1, SB, SB, SB, invA, bad, G->rest_stream)) != cudaSuccess) return e;
         if ((e = tc_gemm(nearA, w2, invB, SB, 1.f, 0.f, A21, n, sms, bad, main)) != cudaSuccess) return e;
-        if ((e = tc_split(A12, n, 1, w2, SB, nearB, bad, main)) != cudaSuccess) return e;
-        if ((e = tc_gemm(invA, SB, nearB, w2, 1.f, 0.f, A12, n, sms, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_gemm(invA, SB, nearB, w2, 1.f, 0.f, A12, n, sms, bad, G->rest_stream)) != cudaSuccess) return e;
         if ((e = tc_split(A21, 1, n, w2, SB, nearA, bad, main)) != cudaSuccess) return e;
-        if ((e = tc_split(A12, n, 1, w2, SB, nearB, bad, main)) != cudaSuccess) return e;
+        if ((e = tc_split(A12, n, 1, w2, SB, nearB, bad, G->rest_stream)) != cudaSuccess) return e;
+        if ((e = cudaEventRecord(G->ev_join, G->rest_stream)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(main, G->ev_join, 0)) != cudaSuccess) return e;
         if ((e = tc_gemm(nearA, w2, nearB, w2, -1.f, 1.f, A22, n, sms, bad, main)) != cudaSuccess) return e;
         if ((e = cudaEventRecord(G->ev_update, main)) != cudaSuccess) return e;
         if ((e = cudaStreamWaitEvent(panel, G->ev_update, 0)) != cudaSuccess) return e;
@@ -1057,10 +1067,10 @@ void LuGraphs::release() {
     if (panel_stream) cudaStreamDestroy(panel_stream);
     if (inv_stream) cudaStreamDestroy(inv_stream);
     if (rest_stream) cudaStreamDestroy(rest_stream);
-    for (cudaEvent_t ev : {ev_update, ev_panel, ev_diag, ev_inv, ev_solve, ev_rest})
+    for (cudaEvent_t ev : {ev_update, ev_panel, ev_diag, ev_inv, ev_solve, ev_rest, ev_fork, ev_join})
         if (ev) cudaEventDestroy(ev);
     panel_stream = inv_stream = rest_stream = nullptr;
-    ev_update = ev_panel = ev_diag = ev_inv = ev_solve = ev_rest = nullptr;
+    ev_update = ev_panel = ev_diag = ev_inv = ev_solve = ev_rest = ev_fork = ev_join = nullptr;
     if (dinv) cudaFree(dinv);
     if (tmp) cudaFree(tmp);
     if (dinv4) cudaFree(dinv4);
@@ -1131,7 +1141,8 @@ cudaError_t lu_factor_fp32(LuGraphs* G, float* LU, int64_t n, int* bad, cudaStre
             return e;
         if ((e = cudaStreamCreateWithPriority(&G->rest_stream, cudaStreamNonBlocking, greatest)) != cudaSuccess)
             return e;
-        for (cudaEvent_t* ev : {&G->ev_update, &G->ev_panel, &G->ev_diag, &G->ev_inv, &G->ev_solve, &G->ev_rest})
+        for (cudaEvent_t* ev : {&G->ev_update, &G->ev_panel, &G->ev_diag, &G->ev_inv, &G->ev_solve, &G->ev_rest,
+                                &G->ev_fork, &G->ev_join})
             if ((e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming)) != cudaSuccess) return e;
     }
     ProfScope ps(Prof::LU_FACTOR, s);

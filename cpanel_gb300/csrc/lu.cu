@@ -867,7 +867,9 @@ namespace {
 // first (1,024-wide products), then that block's update; it is factored on a high-priority
 // stream while the rest of L21, U12 and the update run with kPanelSms SMs left to it.  The
 // serial chain is the diagonal blocks and these three small products.
-constexpr int kPanelSms = 32;
+// (the 19,272-panel wing's factorization: 26.0 ms with 24 SMs, 26.2-26.3 ms with 16, 20 or 32,
+// 26.7 ms with 12 or 40)
+constexpr int kPanelSms = 24;
 // tile scratch of k_inv_step: the chunks of step 7 (32 L and 32 U), then its per-tile counters
 constexpr int64_t kInvScratch = 4 * (SB / 64) * 8192;
 constexpr int64_t kInvCounters = 32;

@@ -12,6 +12,7 @@
 
 #include "../../include/cpanel_gpu.h"
 #include "assemble.h"
+#include "mesh.h"
 #include "df.cuh"
 #include "panel64.cuh"
 #include "particles.h"
@@ -657,9 +658,9 @@ void mixed_block_order(int64_t n, const double* cent, int64_t cstride, const dou
     // a block's cost: per source tile of its chunk, 64 when the boxes come within 3 long sides (FP64
     // near pairs, run at 1/64 of the FP32 rate), 8 within 5 (the double-float band), else 1
     std::vector<int32_t> cost_of(nbx * nby);
-    int32_t cmax = 0;
-    for (int64_t by = 0; by < nby; by++)
-        for (int64_t bx = 0; bx < nbx; bx++) {
+    host_parallel((size_t)(nbx * nby), [&](unsigned, size_t lo, size_t hi) {
+        for (int64_t blk = (int64_t)lo; blk < (int64_t)hi; blk++) {
+            const int64_t by = blk / nbx, bx = blk % nbx;
             int64_t cost = 0;
             const double* r = &rb[6 * bx];
             for (int64_t t = by * ch / TJ; t < std::min(ntj, (by + 1) * ch / TJ); t++) {
@@ -671,9 +672,11 @@ void mixed_block_order(int64_t n, const double* cent, int64_t cstride, const dou
                 }
                 cost += d2 < 9 * sl[t] * sl[t] ? 64 : d2 < 25 * sl[t] * sl[t] ? 8 : 1;
             }
-            cost_of[by * nbx + bx] = (int32_t)cost;
-            cmax = std::max(cmax, (int32_t)cost);
+            cost_of[blk] = (int32_t)cost;
         }
+    });
+    int32_t cmax = 0;
+    for (int32_t c : cost_of) cmax = std::max(cmax, c);
     // costliest first, blocks of equal cost in index order (a counting sort over the small integer costs)
     std::vector<int64_t> start(cmax + 2, 0);
     for (int32_t c : cost_of) start[cmax - c + 1]++;

@@ -337,9 +337,13 @@ __global__ void __launch_bounds__(DT) k_lu_diag(float* __restrict__ A, int64_t n
 // The matrices are column-major with their own order n (LU[c*n + r]).
 
 // L21 = A21 U_KK^{-1} in place for rows [r0, min(r0 + 64, r1)), columns K..K+b.  256 threads:
-// thread t owns row t % 64 and the 32 columns 32 (t / 64) ..; U^{-1} staged 16 rows at a time.
+// thread t owns row t % 64 and the 32 columns 32 (t / 64) ..; U^{-1} staged 16 rows at a time, or
+// (FULL, the single-matrix chain kernel, one thread block per SM at most) all of it at once, with
+// one barrier instead of sixteen.  The products are summed in the same order either way.
 constexpr int CS_R = 64;
 constexpr int CS_SMEM = (CS_R * (NB + 1) + 16 * NB) * 4;
+constexpr int CS_FULL_SMEM = (CS_R * (NB + 1) + NB * (NB + 4)) * 4;
+template <bool FULL>
 __device__ __forceinline__ void col_solve_body(float* __restrict__ A, int64_t n, const float* __restrict__ dinv,
                                                int64_t r0, int64_t r1, int64_t K, int b, float* smem) {
     float (*X)[NB + 1] = reinterpret_cast<float (*)[NB + 1]>(smem);
@@ -362,7 +366,28 @@ __device__ __forceinline__ void col_solve_body(float* __restrict__ A, int64_t n,
     float acc[32];
 #pragma unroll
     for (int j = 0; j < 32; j++) acc[j] = 0.f;
-    for (int k0 = 0; k0 < b; k0 += 16) {
+    if constexpr (FULL) {
+        float (*Uf)[NB + 4] = reinterpret_cast<float (*)[NB + 4]>(smem + CS_R * (NB + 1));  // 16-byte aligned
+        for (int idx = t; idx < NB * NB; idx += 256) {
+            const int kk = idx % NB, c = idx / NB;
+            Uf[kk][c] = (kk < b && c < b) ? Ui[kk + (int64_t)c * NB] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < b; kk++) {
+            const float a = X[r][kk];
+            const float4* u4 = reinterpret_cast<const float4*>(&Uf[kk][32 * cg]);
+#pragma unroll
+            for (int j4 = 0; j4 < 8; j4++) {
+                const float4 u = u4[j4];
+                acc[4 * j4] = __fmaf_rn(a, u.x, acc[4 * j4]);
+                acc[4 * j4 + 1] = __fmaf_rn(a, u.y, acc[4 * j4 + 1]);
+                acc[4 * j4 + 2] = __fmaf_rn(a, u.z, acc[4 * j4 + 2]);
+                acc[4 * j4 + 3] = __fmaf_rn(a, u.w, acc[4 * j4 + 3]);
+            }
+        }
+    }
+    for (int k0 = 0; !FULL && k0 < b; k0 += 16) {
         __syncthreads();
         for (int idx = t; idx < 16 * NB; idx += 256) {
             const int kk = idx % 16, c = idx / 16;
@@ -394,10 +419,12 @@ __device__ __forceinline__ void col_solve_body(float* __restrict__ A, int64_t n,
 
 // U12 = L_KK^{-1} A12 in place for rows K..K+b, columns [c0, min(c0 + 64, c1)).  256 threads:
 // thread t owns row t % 128 and the 32 columns 32 (t / 128) ..; L^{-1} staged 16 columns at a
-// time.
+// time, or (FULL) all of it at once.
 constexpr int RS_C = 64;
 constexpr int RS_SMEM = (NB * (RS_C + 4) + 16 * (NB + 1)) * 4;
-constexpr int CR_SMEM = CS_SMEM > RS_SMEM ? CS_SMEM : RS_SMEM;
+constexpr int RS_FULL_SMEM = (NB * (RS_C + 4) + NB * (NB + 1)) * 4;
+constexpr int CR_FULL_SMEM = CS_FULL_SMEM > RS_FULL_SMEM ? CS_FULL_SMEM : RS_FULL_SMEM;
+template <bool FULL>
 __device__ __forceinline__ void row_solve_body(float* __restrict__ A, int64_t n, const float* __restrict__ dinv,
                                                int64_t c0, int64_t c1, int64_t K, int b, float* smem) {
     float (*X)[RS_C + 4] = reinterpret_cast<float (*)[RS_C + 4]>(smem);  // rows of 272 bytes
@@ -420,7 +447,27 @@ __device__ __forceinline__ void row_solve_body(float* __restrict__ A, int64_t n,
     float acc[32];
 #pragma unroll
     for (int j = 0; j < 32; j++) acc[j] = 0.f;
-    for (int k0 = 0; k0 < b; k0 += 16) {
+    if constexpr (FULL) {
+        for (int idx = t; idx < NB * NB; idx += 256) {
+            const int kk = idx / NB, rr = idx % NB;
+            L[kk][rr] = (kk < b && rr < b) ? Li[rr + (int64_t)kk * NB] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 4
+        for (int kk = 0; kk < b; kk++) {
+            const float a = L[kk][r];
+            const float4* x4 = reinterpret_cast<const float4*>(&X[kk][32 * cg]);
+#pragma unroll
+            for (int j4 = 0; j4 < 8; j4++) {
+                const float4 x = x4[j4];
+                acc[4 * j4] = __fmaf_rn(a, x.x, acc[4 * j4]);
+                acc[4 * j4 + 1] = __fmaf_rn(a, x.y, acc[4 * j4 + 1]);
+                acc[4 * j4 + 2] = __fmaf_rn(a, x.z, acc[4 * j4 + 2]);
+                acc[4 * j4 + 3] = __fmaf_rn(a, x.w, acc[4 * j4 + 3]);
+            }
+        }
+    }
+    for (int k0 = 0; !FULL && k0 < b; k0 += 16) {
         __syncthreads();
         for (int idx = t; idx < 16 * NB; idx += 256) {
             const int kk = idx / NB, rr = idx % NB;
@@ -546,9 +593,9 @@ __global__ void __launch_bounds__(256) k_colrow_solve(float* __restrict__ A, int
     extern __shared__ __align__(16) float dsm[];
     const int64_t nrt = (re - rb + CS_R - 1) / CS_R;
     if ((int64_t)blockIdx.x < nrt)
-        col_solve_body(A, n, dinv, rb + (int64_t)blockIdx.x * CS_R, re, K, b, dsm);
+        col_solve_body<true>(A, n, dinv, rb + (int64_t)blockIdx.x * CS_R, re, K, b, dsm);
     else
-        row_solve_body(A, n, dinv, cb + ((int64_t)blockIdx.x - nrt) * RS_C, ce, K, b, dsm);
+        row_solve_body<true>(A, n, dinv, cb + ((int64_t)blockIdx.x - nrt) * RS_C, ce, K, b, dsm);
 }
 // single matrix: the update of rows [rb, re) x columns [cb, ce) by block K, one 128 x 64 tile
 // per thread block, except the 128 x 128 block at (rb, cb), which the next diagonal kernel updates
@@ -575,14 +622,14 @@ __global__ void __launch_bounds__(256) k_col_solve_batched(const cpg::LuBatchMes
     const int* it = items + LB_ITEM * blockIdx.x;
     const cpg::LuBatchMesh d = ms[it[0]];
     extern __shared__ __align__(16) float dsm[];
-    col_solve_body(d.LU, d.n, d.dinv, it[1], it[2], it[5], it[6], dsm);
+    col_solve_body<false>(d.LU, d.n, d.dinv, it[1], it[2], it[5], it[6], dsm);
 }
 __global__ void __launch_bounds__(256) k_row_solve_batched(const cpg::LuBatchMesh* __restrict__ ms,
                                                            const int* __restrict__ items) {
     const int* it = items + LB_ITEM * blockIdx.x;
     const cpg::LuBatchMesh d = ms[it[0]];
     extern __shared__ __align__(16) float dsm[];
-    row_solve_body(d.LU, d.n, d.dinv, it[3], it[4], it[5], it[6], dsm);
+    row_solve_body<false>(d.LU, d.n, d.dinv, it[3], it[4], it[5], it[6], dsm);
 }
 __global__ void __launch_bounds__(128) k_gemm_sub_batched(const cpg::LuBatchMesh* __restrict__ ms,
                                                           const int* __restrict__ items) {
@@ -845,6 +892,8 @@ void set_attrs() {
                        cudaFuncSetAttribute(k_lu_diag<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, DIAG_SMEM);
                        cudaFuncSetAttribute(k_lu_diag_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                             DIAG_SMEM);
+                       cudaFuncSetAttribute(k_colrow_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            CR_FULL_SMEM);
                    });
 }
 
@@ -903,7 +952,7 @@ cudaError_t factor_diag_block(LuGraphs* G, float* LU, int64_t n, int* bad, int64
             if ((e = cudaStreamWaitEvent(s, G->ev_rest, 0)) != cudaSuccess) return e;
         }
         const unsigned g = (unsigned)((rest + CS_R - 1) / CS_R + (rest + RS_C - 1) / RS_C);
-        k_colrow_solve<<<g, 256, CR_SMEM, s>>>(LU, n, G->dinv, K1, KE, K1, KE, K, b);
+        k_colrow_solve<<<g, 256, CR_FULL_SMEM, s>>>(LU, n, G->dinv, K1, KE, K1, KE, K, b);
         if (rest > NB) {  // beyond the next diagonal block
             if ((e = cudaEventRecord(G->ev_solve, s)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(G->rest_stream, G->ev_solve, 0)) != cudaSuccess) return e;

@@ -75,6 +75,37 @@ def test_topology_synthetic_matches_oracle(built, which):
     assert t["info"]["n_wakelines"] == spec.n_span - 1
 
 
+def test_topology_from_many_threads_is_unchanged(built):
+    """Meshes built from several host threads at once share the builder's thread pool (each call
+    queues its slices and runs some itself): every table equals the one built alone."""
+    import threading
+
+    import cpanel_gb300 as cg
+    from cpanel_gb300 import wing
+    meshes = [wing.make_wing(wing.config_random(20261203 + s))[:3] for s in range(3)]
+    alone = [cg.topology(*m) for m in meshes]
+    got = [None] * 6
+    errs = []
+
+    def run(i):
+        try:
+            got[i] = cg.topology(*meshes[i % 3])
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(6)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errs
+    for i, t in enumerate(got):
+        ref = alone[i % 3]
+        assert t["info"] == ref["info"]
+        for key in ("body", "wake", "idx4", "coef", "clusters"):
+            assert np.array_equal(t[key], ref[key]), key
+
+
 def test_bad_mesh_is_reported(built):
     import cpanel_gb300 as cg
     nodes = np.zeros((3, 3))

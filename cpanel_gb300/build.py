@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_STRICT = ["assemble.cu", "post.cu", "vpkern.cu"]   # FP64 panel math: no contraction
 CU_FAST = ["solve.cu", "lu.cu", "skinny.cu", "particles.cu", "tc_gemm.cu"]  # particles.cu rounds its branch tests explicitly
 CPP = ["mesh.cpp", "api.cpp", "octree.cpp", "vpgeom.cpp", "vpcase.cpp", "server.cpp", "batch.cpp", "writers.cpp",
-       "streamline.cpp", "shim.cpp"]
+       "streamline.cpp", "shim.cpp", "chtls_host.cpp"]
 HEADERS = ["common.cuh", "panel64.cuh", "df.cuh", "assemble.h", "post.h", "mesh.h", "octree.h", "particles.h", "vp.cuh",
            "vpgeom.h", "vpkern.h", "streamline.h", "tc_gemm.h", "skinny.h"]
 

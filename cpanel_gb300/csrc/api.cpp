@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <future>
 #include <map>
 #include <mutex>
 #include <new>
@@ -186,6 +187,11 @@ struct cpg_geometry {
     DevBuf work, post_work, cases, outs;
     bool have64 = false, have32 = false, post_ready = false;
     cudaEvent_t post_ev = nullptr;  // recorded on the aux stream when the post tables are built
+    // the CHTLS weights computed on the host threads while the device assembles (cpg_set_inf_coeff
+    // starts it; prepare_post uploads its result, or launches the device kernel when there is none)
+    std::future<void> chtls;
+    std::vector<double> hF3, hF2;
+    std::vector<int32_t> hmode;
     int64_t h2d_bytes = 0;
     int64_t n_near64 = 0, n_near32 = 0;
     cpg::PostTables T;
@@ -281,7 +287,28 @@ int prepare_post(cpg_geometry* g) {
     CK(g->F3.ensure(sizeof(double) * n * 3 * (cpg::kClMax - 1)), "alloc F3");
     CK(g->F2.ensure(sizeof(double) * n * 2 * (cpg::kClMax - 1)), "alloc F2");
     CK(g->mode.ensure(sizeof(int32_t) * n), "alloc mode");
-    CK(cudaMemsetAsync(g->F2.p, 0, g->F2.bytes, s), "clear F2");
+    bool host_weights = false;
+    if (g->chtls.valid()) {  // computed on the host threads beside the assembly: the same bits
+        try {
+            g->chtls.get();
+            host_weights = true;
+        } catch (...) {  // a host allocation failed: the device kernel below instead
+        }
+    }
+    if (host_weights) {
+        CK(cudaMemcpyAsync(g->F3.p, g->hF3.data(), sizeof(double) * g->hF3.size(), cudaMemcpyHostToDevice, s),
+           "upload F3");
+        CK(cudaMemcpyAsync(g->F2.p, g->hF2.data(), sizeof(double) * g->hF2.size(), cudaMemcpyHostToDevice, s),
+           "upload F2");
+        CK(cudaMemcpyAsync(g->mode.p, g->hmode.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, s),
+           "upload mode");
+        CK(cudaStreamSynchronize(s), "upload CHTLS weights");  // the host arrays are freed next
+        std::vector<double>().swap(g->hF3);
+        std::vector<double>().swap(g->hF2);
+        std::vector<int32_t>().swap(g->hmode);
+    } else {
+        CK(cudaMemsetAsync(g->F2.p, 0, g->F2.bytes, s), "clear F2");
+    }
     cpg::PostTables& T = g->T;
     T.n = n;
     T.nw = H.n_wake;
@@ -327,7 +354,7 @@ int prepare_post(cpg_geometry* g) {
     CK(upload(g->tzpts, H.tz_pts, s), "upload Trefftz");
     CK(cudaEventRecord(g->post_ev, ctx->stream), "event");
     CK(cudaStreamWaitEvent(s, g->post_ev, 0), "event");
-    CK(cpg::launch_chtls_weights(T, s), "CHTLS weights");
+    if (!host_weights) CK(cpg::launch_chtls_weights(T, s), "CHTLS weights");
     CK(g->G.ensure(std::max<size_t>(8, sizeof(double) * T.n_pts * H.n_wake)), "alloc G");
     CK(cpg::launch_wake_potential_op(g->wrec.as<double>(), H.n_wake, g->tzpts.as<double>(), T.n_pts,
                                      g->G.as<double>(), s),
@@ -497,6 +524,7 @@ int cpg_geometry_create(cpg_ctx* ctx, const double* nodes, int64_t n_nodes, cons
 
 void cpg_geometry_destroy(cpg_geometry* g) {
     if (!g) return;
+    if (g->chtls.valid()) g->chtls.wait();  // it reads the host mesh
     for (DevBuf* b : {&g->A32, &g->Alo, &g->LU, &g->A64, &g->B64}) park(g->ctx, *b);
     DevBuf* bufs[] = {&g->rec, &g->frec, &g->bez, &g->clp, &g->cli, &g->tip, &g->ts, &g->wrec, &g->widx,
                       &g->wcoef, &g->tzst, &g->tzln, &g->tzpts, &g->G, &g->F3, &g->F2, &g->mode, &g->A64,
@@ -636,6 +664,18 @@ int cpg_set_inf_coeff(cpg_geometry* g, int precision) {
         return fail(ctx, CPG_E_INVALID, "unknown precision");
     }
     CK(cudaEventRecord(e1, s), "event");
+    if (!g->post_ready && !g->chtls.valid()) {  // the post tables' CHTLS weights, beside the assembly
+        try {
+            g->chtls = std::async(std::launch::async, [g] {
+                const size_t nb = (size_t)g->H.n_body;
+                g->hF3.assign(nb * 3 * (cpg::kClMax - 1), 0.0);
+                g->hF2.assign(nb * 2 * (cpg::kClMax - 1), 0.0);
+                g->hmode.assign(nb, 0);
+                cpg::chtls_weights_host(g->H, g->hF3.data(), g->hF2.data(), g->hmode.data());
+            });
+        } catch (...) {  // no thread: prepare_post launches the device kernel
+        }
+    }
     unsigned long long cnt = 0;
     CK(cudaMemcpyAsync(&cnt, g->count.p, sizeof(cnt), cudaMemcpyDeviceToHost, s), "counter");
     CK(cudaStreamSynchronize(s), "assembly");

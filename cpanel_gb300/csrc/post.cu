@@ -27,62 +27,7 @@ void build_tables() {
     int8_t ms[2][4][19][3] = {};
     int tt[2][4] = {};
     double fa[2][4][19] = {};
-    for (int N = 2; N <= 3; N++)
-        for (int q = 0; q <= 3; q++) {
-            // recursive derivSequence
-            std::vector<std::vector<int>> d;
-            struct R {
-                static std::vector<std::vector<int>> seq(int q, int N) {
-                    std::vector<std::vector<int>> out;
-                    if (q == 0) {
-                        out.push_back(std::vector<int>(N, 0));
-                        return out;
-                    }
-                    for (int i = 0; i <= q; i++) {
-                        if (N > 1) {
-                            auto sub = seq(q - i, N - 1);
-                            for (auto& r : sub) {
-                                r.push_back(i);
-                                out.push_back(r);
-                            }
-                        } else {
-                            out.push_back(std::vector<int>{i});
-                        }
-                    }
-                    return out;
-                }
-            };
-            d = R::seq(q, N);
-            // stable insertion by row sum (sortBySum)
-            auto sum = [](const std::vector<int>& r) {
-                int s = 0;
-                for (int v : r) s += v;
-                return s;
-            };
-            std::vector<std::vector<int>> o{d[0]};
-            for (size_t i = 1; i < d.size(); i++) {
-                bool ins = false;
-                for (size_t j = 0; j < o.size(); j++)
-                    if (sum(d[i]) < sum(o[j])) {
-                        o.insert(o.begin() + (long)j, d[i]);
-                        ins = true;
-                        break;
-                    }
-                if (!ins) o.push_back(d[i]);
-            }
-            o.erase(o.begin());
-            tt[N - 2][q] = (int)o.size();
-            for (size_t k = 0; k < o.size() && k < 19; k++) {
-                double f = 1;
-                for (int a = 0; a < N; a++) {
-                    ms[N - 2][q][k][a] = (int8_t)o[k][a];
-                    int fi = 1;
-                    for (int j = 2; j <= o[k][a]; j++) fi *= j;
-                    f /= (double)fi;
-                }
-                fa[N - 2][q][k] = f;
-            }
-        }
+    cpg::chtls_tables(ms, tt, fa);
     cudaMemcpyToSymbol(c_ms, ms, sizeof(ms));
     cudaMemcpyToSymbol(c_t, tt, sizeof(tt));
     cudaMemcpyToSymbol(c_fact, fa, sizeof(fa));

@@ -8,6 +8,16 @@ namespace cpg {
 
 constexpr int kClMax = 32;  // max cluster size (self included)
 
+struct HostMesh;
+// Sorted derivative sequences of chtlsnd (derivSequence + sortBySum, without the zero row) for N = 3
+// and N = 2, orders 0..3: ms[N-2][order][k][d], tt[N-2][order] rows, fa[N-2][order][k] =
+// 1 / (m_1! ... m_N!) divided out in that order (chtls_host.cpp).
+void chtls_tables(int8_t ms[2][4][19][3], int tt[2][4], double fa[2][4][19]);
+// The CHTLS weights and modes of every body panel on the host threads, the same bits as
+// launch_chtls_weights: F3 (n x 3 x 31), F2 (n x 2 x 31), mode (n); entries past a panel's cluster
+// are left as they are.
+void chtls_weights_host(const HostMesh& H, double* F3, double* F2, int32_t* mode);
+
 struct PostTables {
     int64_t n = 0, nw = 0;
     const double* rec = nullptr;     // body panel records (n x 24)
